@@ -1,0 +1,157 @@
+/*
+ * kel_lbm_cuda.h -- C ABI of the GB300 lattice-Boltzmann hot path.
+ *
+ * Drop-in boundary for the per-cell collide + boundary + stream sweep of
+ * keldu/lbm_mirror (kel::lbm).  The reference exposes that path only as
+ * header-only C++ templates executed inside SYCL parallel_for lambdas; a
+ * foreign caller would bind exactly these entry points.  Every function is
+ * extern "C", takes plain pointers/sizes and returns an int status
+ * (KEL_OK = 0, negative KEL_ERR_* on failure; kel_last_error_string() gives
+ * the message of the last failure on the calling thread).
+ *
+ * Layout conventions (same as the reference's host data):
+ *   - cell index c = x + nx*(y + ny*z)  (x fastest, flatten.hpp:11-39)
+ *   - AoS populations: f[c*Q + i], direction order of df_info<T,Desc>
+ *     (descriptor/d2q9.hpp:17-27, d3q19.hpp:15-37, d3q27.hpp:9-103)
+ *   - flags: one uint8 per cell, meaning given by kel_step_program.ops[flag]
+ *
+ * Inside, the populations live in HBM as structure-of-arrays in a single
+ * in-place (AA-pattern) lattice; uploads/downloads convert.
+ */
+#ifndef KEL_LBM_CUDA_H
+#define KEL_LBM_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define KEL_OK 0
+#define KEL_ERR_INVALID_ARGUMENT (-1)
+#define KEL_ERR_OUT_OF_MEMORY (-2)
+#define KEL_ERR_CUDA (-3)
+#define KEL_ERR_DEVICE_CHECK (-4)
+#define KEL_ERR_TIMEOUT (-5)
+#define KEL_ERR_UNSUPPORTED (-6)
+#define KEL_ERR_STATE (-7)
+
+/* ---- lattice descriptors (df_info<T,Desc>) ------------------------------ */
+#define KEL_D2Q9 9   /* descriptor/d2q9.hpp:11-57 */
+#define KEL_D3Q19 19 /* descriptor/d3q19.hpp:9-70 */
+#define KEL_D3Q27 27 /* descriptor/d3q27.hpp:9-103 */
+
+/* ---- population storage in HBM ----------------------------------------- */
+#define KEL_STORAGE_FP32 0  /* f_i as float */
+#define KEL_STORAGE_FP16S 1 /* f_i - w_i as half, arithmetic in float */
+
+/* ---- lattice creation flags -------------------------------------------- */
+#define KEL_LATTICE_PERIODIC_X 1u /* x wraps (ghost columns copied from the opposite side) */
+
+/* ---- per-flag boundary operation (the reference drivers' switch(info)) - */
+#define KEL_BC_NONE 0              /* no collide, no stream; reads as the zero ghost ring */
+#define KEL_BC_BOUNCE_BACK 1       /* cmpt::BounceBack, full-way (boundary.hpp:32-76) */
+#define KEL_BC_FLUID 2             /* no boundary step; collide if .collide */
+#define KEL_BC_ZOUHE_VELOCITY_X 3  /* cmpt::ZouHeVelocityX<east> D2Q9 (boundary.hpp:759-805) */
+#define KEL_BC_ZOUHE_PRESSURE_X 4  /* cmpt::ZouHePressureX<east> D2Q9/D3Q27 (boundary.hpp:175-756) */
+#define KEL_BC_MOVING_WALL 5       /* lid: f_i = f_opp + 2 w_i (c_i.u_w)/cs^2 (cavity_2d_gpu.cpp:204-235) */
+#define KEL_BC_ANTI_BOUNCE_BACK 6  /* cmpt::AntiBounceBack, D2Q9 y-mirror (boundary.hpp:81-133) */
+#define KEL_BC_EQUILIBRIUM 7       /* cmpt::Equilibrium(rho,u) (boundary.hpp:135-161) */
+
+/* ---- collision operator applied to cells whose op has .collide = 1 ------ */
+#define KEL_COLL_BGK 0     /* cmpt::BGK (collision.hpp:19-97) */
+#define KEL_COLL_BGK_GUO 1 /* cmpt::BGKGuo (collision.hpp:99-205) */
+#define KEL_COLL_PSM 2     /* cmpt::Psm (psm.hpp:37-90) */
+#define KEL_COLL_PSM_GUO 3 /* cmpt::Psm followed by the BGKGuo forcing term */
+
+/* ---- arithmetic mode of the sweep -------------------------------------- */
+#define KEL_ARITH_FAST 0      /* float throughout, contractions allowed */
+#define KEL_ARITH_REFERENCE 1 /* the reference's rounding sequence (double equilibrium bracket) */
+
+#define KEL_MAX_FLAGS 8
+
+typedef struct kel_flag_op {
+	int32_t bc;          /* KEL_BC_* */
+	int32_t collide;     /* 1: run the program's collision after the boundary step */
+	int32_t east;        /* template argument of ZouHe*X<East> */
+	int32_t use_profile; /* ZouHeVelocityX: u_x taken from the inlet profile at this y */
+	double rho;          /* ZouHePressureX rho setting / Equilibrium density */
+	double u[3];         /* ZouHeVelocityX / MovingWall / Equilibrium velocity */
+} kel_flag_op;
+
+typedef struct kel_step_program {
+	int32_t collision;  /* KEL_COLL_* */
+	int32_t arithmetic; /* KEL_ARITH_* */
+	double tau;         /* relaxation time */
+	double global_force[3];
+	kel_flag_op ops[KEL_MAX_FLAGS]; /* indexed by the cell's flag value */
+} kel_step_program;
+
+typedef struct kel_lattice_desc {
+	int32_t descriptor; /* KEL_D2Q9 / KEL_D3Q19 / KEL_D3Q27 */
+	int32_t storage;    /* KEL_STORAGE_* */
+	int64_t nx, ny, nz; /* nz = 1 for D2Q9 */
+	uint32_t flags;     /* KEL_LATTICE_* */
+	uint32_t reserved;
+} kel_lattice_desc;
+
+typedef struct kel_lattice kel_lattice;
+
+/* Dtype / layout selectors for uploads and downloads. */
+#define KEL_DTYPE_F32 0
+#define KEL_DTYPE_F64 1
+#define KEL_LAYOUT_AOS 0 /* f[c*Q + i] (reference FixedArray order) */
+#define KEL_LAYOUT_SOA 1 /* f[i*N + c] */
+
+/* Field selectors. */
+#define KEL_FIELD_POROSITY 1 /* macros "porosity" (psm.hpp:20-32), 1 fluid .. 0 solid */
+#define KEL_FIELD_FORCE 2    /* macros "force" per cell, D values (collision.hpp:148-151) */
+
+/* Replaces data<ChunkStruct, encode::Sycl<>> construction + malloc_device
+ * (modules/sycl/c++/data.hpp:23-61).  Initial state: every cell flag 0,
+ * populations rest equilibrium f = w_i, macros rho = 1, u = 0, porosity 1,
+ * force 0, time step 0. */
+int kel_lattice_create(const kel_lattice_desc *desc, kel_lattice **out);
+int kel_lattice_destroy(kel_lattice *lat);
+/* Launches of this lattice go to `stream` (a cudaStream_t; NULL = legacy default). */
+int kel_lattice_set_stream(kel_lattice *lat, void *stream);
+int kel_lattice_time_step(const kel_lattice *lat, uint64_t *t);
+
+/* Replaces device::copy_to_device of the "info" chunk (sycl/data.hpp:932-965). */
+int kel_upload_flags(kel_lattice *lat, const uint8_t *host_flags);
+/* Populations at the current time step (post-stream, pre-collision), as the
+ * reference's buffer selected by time-step parity holds them. */
+int kel_upload_populations(kel_lattice *lat, const void *host, int32_t dtype, int32_t layout);
+int kel_download_populations(kel_lattice *lat, void *host, int32_t dtype, int32_t layout);
+/* macros "density" / "velocity" as written by the most recent collide that
+ * had KEL_STEP_WRITE_MACROS set (collision.hpp:83-89).  rho: N values, u: N*D (AoS). */
+int kel_download_macros(kel_lattice *lat, float *host_rho, float *host_u);
+int kel_upload_field(kel_lattice *lat, int32_t field, const float *host);
+int kel_download_field(kel_lattice *lat, int32_t field, float *host);
+/* Inlet velocity profile u_x(y) for ops with use_profile = 1 (ny doubles). */
+int kel_upload_inlet_profile(kel_lattice *lat, const double *host_ux, int64_t n);
+
+/* Step flags. */
+#define KEL_STEP_WRITE_MACROS 1u /* store rho, u of the last of the n steps */
+#define KEL_STEP_ALL_MACROS 2u   /* store rho, u on every step */
+
+/* Replaces one iteration of the drivers' loop: the collide+BC
+ * parallel_for (e.g. examples/poiseulle_2d_gpu/poiseulle_2d_gpu.cpp:169-224)
+ * followed by the Stream parallel_for (:384-399), n_steps times. */
+int kel_step(kel_lattice *lat, const kel_step_program *prog, uint64_t n_steps, uint32_t step_flags);
+
+/* Synchronise the lattice's stream. */
+int kel_lattice_synchronize(kel_lattice *lat);
+
+/* Thread-local message of the last failure. */
+const char *kel_last_error_string(void);
+/* Library version string. */
+const char *kel_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,178 @@
+"""ctypes mirror of include/kel_lbm_cuda.h (the C ABI of the sweep).
+
+Only plain-old-data types, constants and the library loader live here.  The
+library is the in-tree build ``lbm_mirror_gb300/_build/libkel_lbm_cuda.so``;
+if it is missing the import of the loader raises instead of falling back to
+anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libkel_lbm_cuda.so")
+
+# ---- status codes --------------------------------------------------------
+KEL_OK = 0
+KEL_ERR_INVALID_ARGUMENT = -1
+KEL_ERR_OUT_OF_MEMORY = -2
+KEL_ERR_CUDA = -3
+KEL_ERR_DEVICE_CHECK = -4
+KEL_ERR_TIMEOUT = -5
+KEL_ERR_UNSUPPORTED = -6
+KEL_ERR_STATE = -7
+
+# ---- descriptors / storage -----------------------------------------------
+KEL_D2Q9, KEL_D3Q19, KEL_D3Q27 = 9, 19, 27
+KEL_STORAGE_FP32, KEL_STORAGE_FP16S = 0, 1
+KEL_LATTICE_PERIODIC_X = 1
+
+# ---- boundary ops (values of kel_flag_op.bc) -------------------------------
+KEL_BC_NONE = 0
+KEL_BC_BOUNCE_BACK = 1
+KEL_BC_FLUID = 2
+KEL_BC_ZOUHE_VELOCITY_X = 3
+KEL_BC_ZOUHE_PRESSURE_X = 4
+KEL_BC_MOVING_WALL = 5
+KEL_BC_ANTI_BOUNCE_BACK = 6
+KEL_BC_EQUILIBRIUM = 7
+
+KEL_COLL_BGK, KEL_COLL_BGK_GUO, KEL_COLL_PSM, KEL_COLL_PSM_GUO = 0, 1, 2, 3
+KEL_ARITH_FAST, KEL_ARITH_REFERENCE = 0, 1
+KEL_MAX_FLAGS = 8
+
+KEL_DTYPE_F32, KEL_DTYPE_F64 = 0, 1
+KEL_LAYOUT_AOS, KEL_LAYOUT_SOA = 0, 1
+KEL_FIELD_POROSITY, KEL_FIELD_FORCE = 1, 2
+KEL_STEP_WRITE_MACROS, KEL_STEP_ALL_MACROS = 1, 2
+
+
+class FlagOp(C.Structure):
+    _fields_ = [
+        ("bc", C.c_int32),
+        ("collide", C.c_int32),
+        ("east", C.c_int32),
+        ("use_profile", C.c_int32),
+        ("rho", C.c_double),
+        ("u", C.c_double * 3),
+    ]
+
+
+class StepProgram(C.Structure):
+    _fields_ = [
+        ("collision", C.c_int32),
+        ("arithmetic", C.c_int32),
+        ("tau", C.c_double),
+        ("global_force", C.c_double * 3),
+        ("ops", FlagOp * KEL_MAX_FLAGS),
+    ]
+
+
+class LatticeDesc(C.Structure):
+    _fields_ = [
+        ("descriptor", C.c_int32),
+        ("storage", C.c_int32),
+        ("nx", C.c_int64),
+        ("ny", C.c_int64),
+        ("nz", C.c_int64),
+        ("flags", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+def make_program(tau, collision=KEL_COLL_BGK, ops=None, global_force=(0.0, 0.0, 0.0),
+                 arithmetic=KEL_ARITH_FAST):
+    """Build a StepProgram.
+
+    ``ops`` maps a flag value (0..7) to a dict with keys bc, collide, east,
+    use_profile, rho, u -- the per-flag ``switch(info)`` of a reference driver.
+    """
+    p = StepProgram()
+    p.collision = collision
+    p.arithmetic = arithmetic
+    p.tau = float(tau)
+    for k in range(3):
+        p.global_force[k] = float(global_force[k]) if k < len(global_force) else 0.0
+    for flag, op in (ops or {}).items():
+        o = p.ops[flag]
+        o.bc = int(op.get("bc", KEL_BC_NONE))
+        o.collide = int(op.get("collide", 0))
+        o.east = int(op.get("east", 1))
+        o.use_profile = int(op.get("use_profile", 0))
+        o.rho = float(op.get("rho", 1.0))
+        u = list(op.get("u", (0.0, 0.0, 0.0))) + [0.0, 0.0, 0.0]
+        for k in range(3):
+            o.u[k] = float(u[k])
+    return p
+
+
+def program_to_dict(p):
+    """Plain-Python view of a StepProgram (for fixtures and logging)."""
+    return {
+        "collision": p.collision,
+        "arithmetic": p.arithmetic,
+        "tau": p.tau,
+        "global_force": list(p.global_force),
+        "ops": {
+            i: {"bc": o.bc, "collide": o.collide, "east": o.east, "use_profile": o.use_profile,
+                "rho": o.rho, "u": list(o.u)}
+            for i, o in enumerate(p.ops) if o.bc != KEL_BC_NONE or o.collide
+        },
+    }
+
+
+def program_from_dict(d):
+    return make_program(d["tau"], d["collision"], {int(k): v for k, v in d["ops"].items()},
+                        d["global_force"], d.get("arithmetic", KEL_ARITH_FAST))
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load the CUDA library and declare its signatures.  Raises if absent."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(
+            f"CUDA extension not built: {p} is missing (run __graft_entry__.build() "
+            "or python -m lbm_mirror_gb300.build)")
+    lib = C.CDLL(p)
+    vp, i32, i64, u32, u64 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint32, C.c_uint64
+    sigs = {
+        "kel_lattice_create": ([C.POINTER(LatticeDesc), C.POINTER(vp)], C.c_int),
+        "kel_lattice_destroy": ([vp], C.c_int),
+        "kel_lattice_set_stream": ([vp, vp], C.c_int),
+        "kel_lattice_time_step": ([vp, C.POINTER(u64)], C.c_int),
+        "kel_upload_flags": ([vp, vp], C.c_int),
+        "kel_upload_populations": ([vp, vp, i32, i32], C.c_int),
+        "kel_download_populations": ([vp, vp, i32, i32], C.c_int),
+        "kel_download_macros": ([vp, vp, vp], C.c_int),
+        "kel_upload_field": ([vp, i32, vp], C.c_int),
+        "kel_download_field": ([vp, i32, vp], C.c_int),
+        "kel_upload_inlet_profile": ([vp, vp, i64], C.c_int),
+        "kel_step": ([vp, C.POINTER(StepProgram), u64, u32], C.c_int),
+        "kel_lattice_synchronize": ([vp], C.c_int),
+        "kel_last_error_string": ([], C.c_char_p),
+        "kel_version": ([], C.c_char_p),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def header_symbols(header_path: str | None = None):
+    """Names of every function declared in include/kel_lbm_cuda.h."""
+    import re
+    hp = header_path or os.path.join(os.path.dirname(HERE), "include", "kel_lbm_cuda.h")
+    text = open(hp).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(kel_[a-z_0-9]+)\s*\(", text, flags=re.M)))

@@ -1,0 +1,138 @@
+"""ctypes binding of the CPU oracle (oracle/lbm_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py, never by the product package.  The oracle is a
+plain-C restatement of keldu/lbm_mirror's two-lattice sweep; see the header of
+lbm_oracle.c for the reference lines each part follows.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD_DIR, "libkel_oracle.so")
+REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the restatement with gcc (no FMA contraction, OpenMP)."""
+    src = [os.path.join(HERE, "lbm_oracle.c"), os.path.join(HERE, "lbm_oracle_impl.h"),
+           os.path.join(HERE, "particles_oracle.c")]
+    src = [s for s in src if os.path.exists(s)]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in src):
+        return LIB
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    cfiles = [s for s in src if s.endswith(".c")]
+    cmd = ["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
+           "-o", LIB + ".tmp"] + cfiles + ["-lm"]
+    subprocess.check_call(cmd)
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        vp, i64, u64 = C.c_void_p, C.c_int64, C.c_uint64
+        L.ko_create.argtypes = [C.c_int, C.c_int, i64, i64, i64, C.c_int]
+        L.ko_create.restype = vp
+        L.ko_destroy.argtypes = [vp]
+        L.ko_set_flags.argtypes = [vp, vp]
+        L.ko_set_profile.argtypes = [vp, vp]
+        L.ko_set_populations.argtypes = [vp, vp]
+        L.ko_get_populations.argtypes = [vp, vp]
+        L.ko_set_porosity.argtypes = [vp, vp]
+        L.ko_set_force.argtypes = [vp, vp]
+        L.ko_get_macros.argtypes = [vp, vp, vp]
+        L.ko_run.argtypes = [vp, vp, u64]
+        L.ko_run.restype = C.c_int
+        L.ko_time_step.argtypes = [vp]
+        L.ko_time_step.restype = u64
+        L.ko_equilibrium_f32.argtypes = [C.c_int, C.c_float, vp, vp]
+        L.ko_program_size.restype = C.c_size_t
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class OracleLattice:
+    """Two-lattice AoS+ghost restatement of the reference sweep (float or double)."""
+
+    def __init__(self, q, dims, f64=False, periodic_x=False):
+        nx, ny = dims[0], dims[1]
+        nz = dims[2] if len(dims) > 2 else 1
+        self.q, self.dims, self.f64 = q, (nx, ny, nz), f64
+        self.D = 2 if q == 9 else 3
+        self.n = nx * ny * nz
+        self._h = lib().ko_create(q, int(f64), nx, ny, nz, int(periodic_x))
+        if not self._h:
+            raise ValueError("oracle: bad lattice arguments")
+        self._keep = []
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().ko_destroy(self._h)
+            self._h = None
+
+    def set_flags(self, flags):
+        a = np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1)
+        assert a.size == self.n
+        lib().ko_set_flags(self._h, _ptr(a))
+
+    def set_profile(self, prof):
+        a = np.ascontiguousarray(prof, dtype=np.float64)
+        self._keep.append(a)
+        lib().ko_set_profile(self._h, _ptr(a))
+
+    def set_populations(self, aos):
+        a = np.ascontiguousarray(aos, dtype=np.float64).reshape(-1)
+        assert a.size == self.n * self.q
+        lib().ko_set_populations(self._h, _ptr(a))
+
+    def populations(self):
+        out = np.empty(self.n * self.q, dtype=np.float64)
+        lib().ko_get_populations(self._h, _ptr(out))
+        return out.reshape(self.n, self.q)
+
+    def set_porosity(self, v):
+        a = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        lib().ko_set_porosity(self._h, _ptr(a))
+
+    def set_force(self, v):
+        a = np.ascontiguousarray(v, dtype=np.float64).reshape(-1)
+        lib().ko_set_force(self._h, _ptr(a))
+
+    def macros(self):
+        rho = np.empty(self.n, dtype=np.float64)
+        vel = np.empty(self.n * self.D, dtype=np.float64)
+        lib().ko_get_macros(self._h, _ptr(rho), _ptr(vel))
+        return rho, vel.reshape(self.n, self.D)
+
+    def run(self, program, steps):
+        rc = lib().ko_run(self._h, C.byref(program), steps)
+        if rc != 0:
+            raise RuntimeError("oracle: program not supported for this descriptor")
+
+    @property
+    def t(self):
+        return lib().ko_time_step(self._h)
+
+
+def equilibrium_f32(q, rho, u):
+    u3 = np.zeros(3, dtype=np.float32)
+    u3[:len(u)] = u
+    out = np.zeros(q, dtype=np.float32)
+    lib().ko_equilibrium_f32(q, C.c_float(rho), _ptr(u3), _ptr(out))
+    return out

@@ -1,0 +1,139 @@
+"""Generate the golden sweep vectors from keldu/lbm_mirror's own components.
+
+Runs oracle/_ref/ref_harness (built by oracle/Makefile from the reference's
+headers, unchanged) on every case below and stores inputs + outputs as
+tests/golden/<name>.npz.  Needs the reference tree, so it runs only where the
+reference is mounted; the committed .npz files are what the tests read.
+
+    python tests/golden/make_golden.py [--check]
+
+Inputs are rounded to float32 before use so that the stored float32 copy is
+exactly what both the reference and the implementations under test consume.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from lbm_mirror_gb300 import capi as K  # noqa: E402
+from tests import cases  # noqa: E402
+
+GOLDEN = os.path.dirname(os.path.abspath(__file__))
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+
+def registry():
+    """name -> (harness case id, case dict)."""
+    r = {}
+    r["poiseuille_48x20"] = ("d2q9_f32_48x20", cases.poiseuille_2d(48, 20, steps=301, u_max=0.05))
+    r["poiseuille_48x20_f64"] = ("d2q9_f64_48x20", cases.poiseuille_2d(48, 20, steps=301, f64=True))
+    r["poiseuille_256x64"] = ("d2q9_f32_256x64", cases.poiseuille_2d(256, 64, steps=10000))
+    for nm, coll in (("bgk", K.KEL_COLL_BGK), ("guo", K.KEL_COLL_BGK_GUO), ("psm", K.KEL_COLL_PSM),
+                     ("psmguo", K.KEL_COLL_PSM_GUO)):
+        r[f"mixed2d_{nm}"] = ("d2q9_f32_48x20", cases.mixed_2d(coll))
+    r["mixed2d_guo_f64"] = ("d2q9_f64_48x20", cases.mixed_2d(K.KEL_COLL_BGK_GUO, f64=True))
+    for q in (19, 27):
+        r[f"cavity_d3q{q}"] = (f"d3q{q}_f32_16x12x10", cases.cavity_3d(q))
+        r[f"cavity_d3q{q}_f64"] = (f"d3q{q}_f64_16x12x10", cases.cavity_3d(q, f64=True))
+        r[f"mixed3d_d3q{q}_bgk"] = (f"d3q{q}_f32_16x12x10", cases.mixed_3d(q, K.KEL_COLL_BGK))
+        r[f"mixed3d_d3q{q}_guo"] = (f"d3q{q}_f32_16x12x10", cases.mixed_3d(q, K.KEL_COLL_BGK_GUO, seed=3))
+        r[f"mixed3d_d3q{q}_psmguo"] = (f"d3q{q}_f32_16x12x10", cases.mixed_3d(q, K.KEL_COLL_PSM_GUO, seed=4))
+    return r
+
+
+def _f32_round(a):
+    return None if a is None else np.asarray(a, dtype=np.float64).astype(np.float32).astype(np.float64)
+
+
+def normalise(case):
+    """Round every floating input to float32 (the stored precision)."""
+    c = dict(case)
+    for k in ("init", "profile", "porosity", "force"):
+        c[k] = _f32_round(c[k])
+    return c
+
+
+def run_harness(hcase, case, workdir):
+    ind = os.path.join(workdir, "in")
+    outd = os.path.join(workdir, "out")
+    os.makedirs(ind, exist_ok=True)
+    os.makedirs(outd, exist_ok=True)
+    p = case["program"]
+    lines = [f"steps {case['steps']}", f"tau {p.tau!r}", f"collision {p.collision}",
+             "gforce " + " ".join(repr(float(v)) for v in p.global_force)]
+    for i, o in enumerate(p.ops):
+        lines.append(f"op {i} {o.bc} {o.collide} {o.east} {o.rho!r} {o.u[0]!r} {o.u[1]!r} {o.u[2]!r} {o.use_profile}")
+    open(os.path.join(ind, "params.txt"), "w").write("\n".join(lines) + "\n")
+    case["flags"].astype(np.uint8).tofile(os.path.join(ind, "flags.u8"))
+    for k, fn in (("init", "init.f64"), ("profile", "profile.f64"), ("porosity", "porosity.f64"),
+                  ("force", "force.f64")):
+        if case[k] is not None:
+            np.asarray(case[k], dtype=np.float64).tofile(os.path.join(ind, fn))
+    subprocess.check_call([HARNESS, hcase, ind, outd])
+    q, n = case["q"], case["flags"].size
+    D = 2 if q == 9 else 3
+    dfs = np.fromfile(os.path.join(outd, "dfs.f64")).reshape(n, q)
+    rho = np.fromfile(os.path.join(outd, "rho.f64"))
+    vel = np.fromfile(os.path.join(outd, "vel.f64")).reshape(n, D)
+    return dfs, rho, vel
+
+
+def save(name, case, dfs, rho, vel):
+    odt = np.float64 if case["f64"] else np.float32
+    arrays = dict(
+        meta=np.array(json.dumps(dict(
+            q=case["q"], dims=list(case["dims"]), f64=bool(case["f64"]), periodic=bool(case["periodic"]),
+            steps=int(case["steps"]), program=K.program_to_dict(case["program"])))),
+        flags=case["flags"].astype(np.uint8),
+        dfs=dfs.astype(odt), rho=rho.astype(odt), vel=vel.astype(odt))
+    for k in ("init", "profile", "porosity", "force"):
+        if case[k] is not None:
+            arrays[k] = np.asarray(case[k]).astype(np.float32)
+    np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), **arrays)
+
+
+def load(name):
+    """Fixture -> (case dict, dfs, rho, vel) with float64 arrays."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(z["meta"]))
+    case = dict(q=meta["q"], dims=tuple(meta["dims"]), f64=meta["f64"], periodic=meta["periodic"],
+                steps=meta["steps"], program=K.program_from_dict(meta["program"]), flags=z["flags"])
+    for k in ("init", "profile", "porosity", "force"):
+        case[k] = z[k].astype(np.float64) if k in z.files else None
+    return case, z["dfs"].astype(np.float64), z["rho"].astype(np.float64), z["vel"].astype(np.float64)
+
+
+def names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--only", default=None)
+    args = ap.parse_args()
+    if not os.path.exists(HARNESS):
+        subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle")])
+    for name, (hcase, case) in registry().items():
+        if args.only and args.only not in name:
+            continue
+        case = normalise(case)
+        with tempfile.TemporaryDirectory() as td:
+            dfs, rho, vel = run_harness(hcase, case, td)
+        save(name, case, dfs, rho, vel)
+        odfs, orho, ovel = cases.run_oracle(case)
+        same = np.array_equal(odfs, dfs) and np.array_equal(orho, rho) and np.array_equal(ovel, vel)
+        print(f"{name:28s} steps={case['steps']:6d}  oracle bit-exact: {same}  "
+              f"max|dfs diff|={np.abs(odfs - dfs).max():.3e}")
+
+
+if __name__ == "__main__":
+    main()
