@@ -1,0 +1,324 @@
+"""Benchmark of the lattice-Boltzmann sweep on GB300.
+
+Default workload (the configuration the headline metric is quoted on): D3Q19
+BGK lid-driven cavity, 256^3 cells, FP32 populations, tau = 0.55, lid
+u = (0.1, 0, 0) by moving bounce-back, all other walls full-way bounce-back,
+rest-equilibrium start.  One bench step = one time step = one fused
+collide+boundary+stream sweep over all 16.8 M cells.  The populations
+(1.27 GB) are far larger than L2 (129 MB), so no flush is needed between
+steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload d3q19_cavity_256|d3q27_cavity_256|d2q9_poiseuille_256x64|...]
+                    [--storage fp32|fp16s]
+
+Prints one JSON line (rank 0).  For N > 1 (torchrun), every rank runs an
+independent replica of the workload on its own GPU (the sweep has no exchange
+step on one lattice); value = all ranks' cell updates / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    # name: (descriptor, dims, tau, kind)
+    "d3q19_cavity_256": (19, (256, 256, 256), 0.55, "cavity"),
+    "d3q27_cavity_256": (27, (256, 256, 256), 0.55, "cavity"),
+    "d2q9_poiseuille_256x64": (9, (256, 64), 0.8, "poiseuille"),
+    "d2q9_channel_4096x4096": (9, (4096, 4096), 0.8, "poiseuille"),
+}
+
+
+def bytes_per_update(q, storage):
+    s = 4 if storage == "fp32" else 2
+    return 2 * q * s + 1  # read + write every population, read the flag byte
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def make_case(name):
+    from tests import cases
+    q, dims, tau, kind = WORKLOADS[name]
+    if kind == "cavity":
+        return cases.cavity_3d(q, dims=dims, steps=0, tau=tau)
+    return cases.poiseuille_2d(dims[0], dims[1], steps=0, tau=tau)
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        for line in open(self.file.name):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline_sample(name, seconds=10.0):
+    """The CPU oracle (plain-C restatement of the reference sweep, all host
+    threads) on the same lattice, timed over a bounded sample of rows."""
+    from oracle.oracle import OracleLattice
+    case = make_case(name)
+    q, dims = case["q"], case["dims"]
+    lat = OracleLattice(q, dims)
+    lat.set_flags(case["flags"])
+    if case["profile"] is not None:
+        lat.set_profile(case["profile"])
+    nrows = int(np.prod(dims[1:]))
+    nx = dims[0]
+    chunk = max(1, min(nrows, 1_048_576 // nx))
+    lat.run_rows(case["program"], 0, chunk)  # warm-up
+    done = 0
+    t0 = time.perf_counter()
+    r = 0
+    while True:
+        r1 = min(nrows, r + chunk)
+        lat.run_rows(case["program"], r, r1)
+        done += (r1 - r) * nx
+        r = 0 if r1 >= nrows else r1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = time.perf_counter() - t0
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return {"value": done / dt / 1e6, "unit": "MLUPS", "cores": cores, "kind": "port",
+            "sample": f"{done} cell updates of {name} ({done / (nx * nrows):.2f} sweeps, "
+                      f"row blocks of {chunk * nx} cells) in {dt:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        print(json.dumps({"impl": "reference", "rank": rank, "skipped": "rank 0 runs the CPU reference"}),
+              file=sys.stderr)
+        return
+    from oracle.oracle import OracleLattice
+    case = make_case(args.workload)
+    q, dims = case["q"], case["dims"]
+    lat = OracleLattice(q, dims)
+    lat.set_flags(case["flags"])
+    if case["profile"] is not None:
+        lat.set_profile(case["profile"])
+    nrows = int(np.prod(dims[1:]))
+    nx = dims[0]
+    chunk = max(1, min(nrows, 1_048_576 // nx))  # ~1 M cell updates per bench step
+    r = 0
+    for _ in range(args.warmup):
+        r1 = min(nrows, r + chunk)
+        lat.run_rows(case["program"], r, r1)
+        r = 0 if r1 >= nrows else r1
+    done = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r1 = min(nrows, r + chunk)
+        lat.run_rows(case["program"], r, r1)
+        done += (r1 - r) * nx
+        r = 0 if r1 >= nrows else r1
+    dt = time.perf_counter() - t0
+    v = done / dt / 1e6
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    line = {
+        "impl": "reference", "metric": "MLUPS", "value": v, "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "cells": int(np.prod(dims)), "storage": "fp32 AoS two-lattice",
+                   "sample_cells_per_step": chunk * nx},
+        "cpu_baseline": {"value": v, "unit": "MLUPS", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} steps of {chunk * nx} cell updates (row blocks of the "
+                                   f"{'x'.join(map(str, dims))} lattice), oracle restatement of the reference's "
+                                   f"two-lattice sweep, OpenMP"},
+        "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="d3q19_cavity_256", choices=sorted(WORKLOADS))
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16s"])
+    ap.add_argument("--e2e-iters", type=int, default=3)
+    ap.add_argument("--e2e-lbm-steps", type=int, default=100)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if world > 1:
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    from lbm_mirror_gb300 import Lattice
+    from lbm_mirror_gb300 import capi as K
+    from tests.gpu_util import QNAME
+
+    case = make_case(args.workload)
+    q, dims = case["q"], case["dims"]
+    ncell = int(np.prod(dims))
+    stream = torch.cuda.Stream()
+    lat = Lattice(QNAME[q], dims, storage=args.storage, stream=stream.cuda_stream)
+    lat.upload_flags(case["flags"])
+    if case["profile"] is not None:
+        lat.upload_inlet_profile(case["profile"])
+    prog = case["program"]
+
+    # ---- device-resident throughput (value) and per-launch duration -------
+    lat.step(prog, args.warmup, write_macros=False)
+    lat.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0.record(stream)
+    lat.step(prog, args.steps, write_macros=False)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    per_launch_s = ms / 1e3 / args.steps
+    value = world * ncell * args.steps / (ms / 1e3) / 1e6
+
+    bpu = bytes_per_update(q, args.storage)
+    peak, peak_src = load_peaks()
+    achieved = bpu * ncell / per_launch_s / 1e9
+
+    # ---- end to end through the C ABI with pinned host buffers ------------
+    Q, D = q, (2 if q == 9 else 3)
+    h_flags = torch.from_numpy(np.ascontiguousarray(case["flags"], dtype=np.uint8)).pin_memory()
+    from tests.cases import _weights
+    init = np.broadcast_to(_weights(q).astype(np.float32), (ncell, Q))
+    h_pop = torch.empty((ncell, Q), dtype=torch.float32).pin_memory()
+    h_pop.numpy()[:] = init
+    h_rho = torch.empty(ncell, dtype=torch.float32).pin_memory()
+    h_u = torch.empty(ncell * D, dtype=torch.float32).pin_memory()
+    lib = lat.lib
+    import ctypes as C
+
+    def e2e_once():
+        rc = lib.kel_upload_flags(lat.handle, C.c_void_p(h_flags.data_ptr()))
+        rc |= lib.kel_upload_populations(lat.handle, C.c_void_p(h_pop.data_ptr()), K.KEL_DTYPE_F32, K.KEL_LAYOUT_AOS)
+        rc |= lib.kel_step(lat.handle, C.byref(prog), args.e2e_lbm_steps, K.KEL_STEP_WRITE_MACROS)
+        rc |= lib.kel_download_macros(lat.handle, C.c_void_p(h_rho.data_ptr()), C.c_void_p(h_u.data_ptr()))
+        if rc:
+            raise RuntimeError(lib.kel_last_error_string().decode())
+
+    e2e_once()  # warm-up (staging buffer allocation)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_iters):
+        e2e_once()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * ncell * args.e2e_lbm_steps * args.e2e_iters / e2e_s / 1e6
+    mass = float(h_rho.numpy()[case["flags"] == 2].astype(np.float64).mean())
+
+    line = {
+        "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32" if args.storage == "fp32" else "f16-shifted storage, f32 arithmetic",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "descriptor": f"D{D}Q{Q}", "dims": list(dims), "cells": ncell,
+                   "storage": args.storage, "tau": float(prog.tau), "collision": "BGK", "arithmetic": "fast",
+                   "scheme": "AA in-place, SoA", "l2": "populations 1.27 GB >> 129 MB L2, no flush needed"
+                   if ncell * Q * 4 > 4e8 else "working set smaller than L2",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_source": peak_src, "bytes_per_update": bpu,
+                     "per_launch_ms": per_launch_s * 1e3},
+        "e2e": {"value": e2e_value, "unit": "MLUPS", "h2d_bytes_per_step": int(ncell + ncell * Q * 4),
+                "d2h_bytes_per_step": int(ncell * 4 * (1 + D)), "lbm_steps_per_step": args.e2e_lbm_steps,
+                "iters": args.e2e_iters, "mean_rho_fluid": mass},
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample(args.workload, args.cpu_seconds)
+    lat.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,574 @@
+// C ABI of the sweep (include/kel_lbm_cuda.h): lattice ownership, host
+// uploads/downloads with the AA-parity conversion, program lowering and the
+// per-step launch.
+//
+// Replaces, for the hot path, the reference's SYCL device layer
+// (modules/sycl/c++/data.hpp:23-61 ownership, :557-819 copies, :932-965
+// device) and the per-driver step()/stream loops.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/kel_lbm_cuda.h"
+#include "descriptors.cuh"
+#include "sweep.cuh"
+
+using namespace kel::gb;
+
+namespace kel {
+namespace gb {
+template <class L>
+cudaError_t launch_sweep(const SweepParams &p, int storage, bool odd, int coll, bool exact, cudaStream_t st);
+} // namespace gb
+} // namespace kel
+
+// ---------------------------------------------------------------------------
+// errors
+
+static thread_local std::string g_err;
+
+static int fail(int code, const char *fmt, ...) {
+	char buf[512];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	g_err = buf;
+	return code;
+}
+
+#define KEL_CUDA(call)                                                                             \
+	do {                                                                                           \
+		cudaError_t e__ = (call);                                                                  \
+		if (e__ != cudaSuccess)                                                                    \
+			return fail(e__ == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA,   \
+						"%s: %s (%s:%d)", #call, cudaGetErrorString(e__), __FILE__, __LINE__);      \
+	} while (0)
+
+extern "C" const char *kel_last_error_string(void) { return g_err.c_str(); }
+extern "C" const char *kel_version(void) { return "kel-lbm-gb300 0.1 (sm_103a)"; }
+
+// ---------------------------------------------------------------------------
+// descriptor tables on the host
+
+struct HostDesc {
+	int D = 0, Q = 0;
+	int c[27][3];
+	int opp[27];
+	double w[27];
+};
+
+template <class L>
+static HostDesc host_desc() {
+	HostDesc h;
+	h.D = L::D;
+	h.Q = L::Q;
+	for (int i = 0; i < L::Q; ++i) {
+		h.c[i][0] = L::cx(i);
+		h.c[i][1] = L::cy(i);
+		h.c[i][2] = L::cz(i);
+		h.opp[i] = L::opp(i);
+		h.w[i] = L::w(i);
+	}
+	return h;
+}
+
+static bool desc_for(int q, HostDesc &h) {
+	if (q == KEL_D2Q9) h = host_desc<D2Q9>();
+	else if (q == KEL_D3Q19) h = host_desc<D3Q19>();
+	else if (q == KEL_D3Q27) h = host_desc<D3Q27>();
+	else return false;
+	return true;
+}
+
+// equilibrium.hpp:7-48 on the host with the reference's rounding (this file
+// is compiled without floating-point contraction).
+static void host_equilibrium(const HostDesc &d, float rho, const float *u, float *eq) {
+	float vv = 0.f;
+	for (int k = 0; k < d.D; ++k) vv = vv + u[k] * u[k];
+	for (int i = 0; i < d.Q; ++i) {
+		float vc = 0.f;
+		for (int k = 0; k < d.D; ++k) vc = vc + u[k] * (float)d.c[i][k];
+		float vcc = vc * 3.0f;
+		float wr = (float)d.w[i] * rho;
+		double br = 1.0 + (double)vcc - (double)3.0f * 0.5 * (double)vv + (double)(vcc * vcc) * 0.5;
+		eq[i] = (float)((double)wr * br);
+	}
+}
+
+// ---------------------------------------------------------------------------
+// lattice
+
+struct kel_lattice {
+	kel_lattice_desc desc;
+	HostDesc d;
+	int nxp = 0, nq = 0, wpr = 0;
+	int64_t plane = 0, ncell = 0;
+	size_t elem = 4;
+	void *f = nullptr;
+	uint8_t *flags = nullptr;
+	float *rho = nullptr, *u = nullptr, *por = nullptr, *force = nullptr, *profile = nullptr;
+	OpEntry *ops = nullptr;
+	void *staging = nullptr;
+	size_t staging_bytes = 0;
+	cudaStream_t stream = nullptr;
+	uint64_t t = 0;
+	float wshift[27];
+	bool have_ops = false;
+	kel_step_program last_prog;
+	int device = 0;
+};
+
+__global__ void k_fill_f32(float *p, int64_t n, float v) {
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+__global__ void k_fill_pop(void *f, int64_t plane, int storage, float v, float s) {
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < plane; i += (int64_t)gridDim.x * blockDim.x) {
+		if (storage == STORE_FP32) static_cast<float *>(f)[i] = v;
+		else static_cast<__half *>(f)[i] = __float2half_rn(v - s);
+	}
+}
+
+static int grid_for(int64_t n) {
+	int64_t b = (n + 255) / 256;
+	if (b > 152 * 64) b = 152 * 64;
+	if (b < 1) b = 1;
+	return (int)b;
+}
+
+static int ensure_staging(kel_lattice *L, size_t bytes) {
+	if (L->staging_bytes >= bytes) return KEL_OK;
+	if (L->staging) cudaFree(L->staging);
+	L->staging = nullptr;
+	L->staging_bytes = 0;
+	KEL_CUDA(cudaMalloc(&L->staging, bytes));
+	L->staging_bytes = bytes;
+	return KEL_OK;
+}
+
+static int ensure_field(kel_lattice *L, float **ptr, int64_t count, float init) {
+	if (*ptr) return KEL_OK;
+	KEL_CUDA(cudaMalloc(ptr, count * sizeof(float)));
+	k_fill_f32<<<grid_for(count), 256, 0, L->stream>>>(*ptr, count, init);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+extern "C" int kel_lattice_create(const kel_lattice_desc *desc, kel_lattice **out) {
+	if (!desc || !out) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_create: null argument");
+	*out = nullptr;
+	HostDesc d;
+	if (!desc_for(desc->descriptor, d))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_create: unknown descriptor %d", desc->descriptor);
+	if (desc->storage != KEL_STORAGE_FP32 && desc->storage != KEL_STORAGE_FP16S)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_create: unknown storage %d", desc->storage);
+	if (desc->nx < 1 || desc->ny < 1 || desc->nz < 1 || desc->nx > (1 << 30) || desc->ny > (1 << 30) ||
+		desc->nz > (1 << 30))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_create: bad extents %lld x %lld x %lld",
+					(long long)desc->nx, (long long)desc->ny, (long long)desc->nz);
+	if (d.D == 2 && desc->nz != 1) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_create: D2Q9 needs nz = 1");
+	if ((desc->flags & KEL_LATTICE_PERIODIC_X) && (desc->nx % 4) != 0)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_create: periodic x needs nx %% 4 == 0");
+	if (desc->flags & ~KEL_LATTICE_PERIODIC_X) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_create: unknown flags");
+
+	kel_lattice *L = new kel_lattice();
+	L->desc = *desc;
+	L->d = d;
+	L->nxp = (int)((desc->nx + 3) / 4 * 4);
+	L->nq = L->nxp / 4;
+	L->wpr = (L->nq + 31) / 32;
+	L->ncell = desc->nx * desc->ny * desc->nz;
+	L->plane = (int64_t)L->nxp * desc->ny * desc->nz;
+	L->elem = desc->storage == KEL_STORAGE_FP32 ? 4 : 2;
+	cudaGetDevice(&L->device);
+	for (int i = 0; i < 27; ++i) L->wshift[i] = 0.f;
+	if (desc->storage == KEL_STORAGE_FP16S)
+		for (int i = 0; i < d.Q; ++i) L->wshift[i] = __half2float(__float2half_rn((float)d.w[i]));
+
+	auto cleanup = [&](int rc) {
+		kel_lattice_destroy(L);
+		return rc;
+	};
+	cudaError_t e;
+	if ((e = cudaMalloc(&L->f, (size_t)d.Q * L->plane * L->elem)) != cudaSuccess ||
+		(e = cudaMalloc(&L->flags, (size_t)L->plane)) != cudaSuccess ||
+		(e = cudaMalloc(&L->rho, (size_t)L->plane * sizeof(float))) != cudaSuccess ||
+		(e = cudaMalloc(&L->u, (size_t)d.D * L->plane * sizeof(float))) != cudaSuccess ||
+		(e = cudaMalloc(&L->profile, (size_t)desc->ny * sizeof(float))) != cudaSuccess ||
+		(e = cudaMalloc(&L->ops, sizeof(OpEntry) * MAX_FLAGS)) != cudaSuccess) {
+		int rc = fail(e == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA,
+					  "kel_lattice_create: %s", cudaGetErrorString(e));
+		return cleanup(rc);
+	}
+	// rest equilibrium f = w_i everywhere, flags 0, rho = 1, u = 0
+	for (int i = 0; i < d.Q; ++i) {
+		void *pl = static_cast<char *>(L->f) + (size_t)i * L->plane * L->elem;
+		k_fill_pop<<<grid_for(L->plane), 256, 0, L->stream>>>(pl, L->plane, desc->storage, (float)d.w[i], L->wshift[i]);
+	}
+	k_fill_f32<<<grid_for(L->plane), 256, 0, L->stream>>>(L->rho, L->plane, 1.0f);
+	k_fill_f32<<<grid_for(d.D * L->plane), 256, 0, L->stream>>>(L->u, d.D * L->plane, 0.0f);
+	k_fill_f32<<<grid_for(desc->ny), 256, 0, L->stream>>>(L->profile, desc->ny, 0.0f);
+	if ((e = cudaMemsetAsync(L->flags, 0, (size_t)L->plane, L->stream)) != cudaSuccess ||
+		(e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamSynchronize(L->stream)) != cudaSuccess) {
+		int rc = fail(KEL_ERR_CUDA, "kel_lattice_create: %s", cudaGetErrorString(e));
+		return cleanup(rc);
+	}
+	*out = L;
+	return KEL_OK;
+}
+
+extern "C" int kel_lattice_destroy(kel_lattice *L) {
+	if (!L) return KEL_OK;
+	if (L->stream) cudaStreamSynchronize(L->stream);
+	else cudaDeviceSynchronize();
+	cudaFree(L->f);
+	cudaFree(L->flags);
+	cudaFree(L->rho);
+	cudaFree(L->u);
+	cudaFree(L->por);
+	cudaFree(L->force);
+	cudaFree(L->profile);
+	cudaFree(L->ops);
+	cudaFree(L->staging);
+	delete L;
+	return KEL_OK;
+}
+
+extern "C" int kel_lattice_set_stream(kel_lattice *L, void *stream) {
+	if (!L) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_set_stream: null lattice");
+	L->stream = static_cast<cudaStream_t>(stream);
+	return KEL_OK;
+}
+
+extern "C" int kel_lattice_time_step(const kel_lattice *L, uint64_t *t) {
+	if (!L || !t) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_time_step: null argument");
+	*t = L->t;
+	return KEL_OK;
+}
+
+extern "C" int kel_lattice_synchronize(kel_lattice *L) {
+	if (!L) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_synchronize: null lattice");
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	return KEL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// flags
+
+extern "C" int kel_upload_flags(kel_lattice *L, const uint8_t *host) {
+	if (!L || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_upload_flags: null argument");
+	const auto &D = L->desc;
+	KEL_CUDA(cudaMemcpy2DAsync(L->flags, (size_t)L->nxp, host, (size_t)D.nx, (size_t)D.nx, (size_t)(D.ny * D.nz),
+							   cudaMemcpyHostToDevice, L->stream));
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	return KEL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// populations: host AoS/SoA <-> AA lattice, parity aware
+
+struct ConvArgs {
+	void *f;
+	void *buf;
+	int64_t plane, ncell;
+	int nx, ny, nz, nxp;
+	int Q, D;
+	int storage, dtype, layout;
+	int odd, periodic;
+	int c[27][3];
+	int opp[27];
+	float wshift[27];
+};
+
+__device__ __forceinline__ float ldpop(const ConvArgs &a, int64_t idx, int i) {
+	if (a.storage == STORE_FP32) return static_cast<const float *>(a.f)[idx];
+	return __half2float(static_cast<const __half *>(a.f)[idx]) + a.wshift[i];
+}
+
+__device__ __forceinline__ void stpop(const ConvArgs &a, int64_t idx, int i, float v) {
+	if (a.storage == STORE_FP32) static_cast<float *>(a.f)[idx] = v;
+	else static_cast<__half *>(a.f)[idx] = __float2half_rn(v - a.wshift[i]);
+}
+
+// Location in the AA lattice of the post-stream population f_i(x):
+// even t: A[i][x]; odd t: A[opp i][x - c_i] (or nothing if that is outside).
+__device__ __forceinline__ bool pop_slot(const ConvArgs &a, int x, int y, int z, int i, int64_t &idx) {
+	if (!a.odd) {
+		idx = (int64_t)i * a.plane + ((int64_t)z * a.ny + y) * a.nxp + x;
+		return true;
+	}
+	int sx = x - a.c[i][0], sy = y - a.c[i][1], sz = z - a.c[i][2];
+	if (a.periodic) sx = (sx + a.nx) % a.nx;
+	if (sx < 0 || sx >= a.nxp || sy < 0 || sy >= a.ny || sz < 0 || sz >= a.nz) return false;
+	idx = (int64_t)a.opp[i] * a.plane + ((int64_t)sz * a.ny + sy) * a.nxp + sx;
+	return true;
+}
+
+__global__ void k_pop_convert(ConvArgs a, int upload) {
+	const int64_t total = a.ncell * a.Q;
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+		int64_t c, i;
+		if (a.layout == KEL_LAYOUT_AOS) {
+			c = k / a.Q;
+			i = k % a.Q;
+		} else {
+			i = k / a.ncell;
+			c = k % a.ncell;
+		}
+		const int x = (int)(c % a.nx);
+		const int y = (int)((c / a.nx) % a.ny);
+		const int z = (int)(c / ((int64_t)a.nx * a.ny));
+		int64_t idx;
+		const bool ok = pop_slot(a, x, y, z, (int)i, idx);
+		if (upload) {
+			if (!ok) continue;
+			float v = a.dtype == KEL_DTYPE_F32 ? static_cast<const float *>(a.buf)[k]
+											   : (float)static_cast<const double *>(a.buf)[k];
+			stpop(a, idx, (int)i, v);
+		} else {
+			float v = ok ? ldpop(a, idx, (int)i) : 0.f;
+			if (a.dtype == KEL_DTYPE_F32) static_cast<float *>(a.buf)[k] = v;
+			else static_cast<double *>(a.buf)[k] = (double)v;
+		}
+	}
+}
+
+static ConvArgs conv_args(const kel_lattice *L, int dtype, int layout) {
+	ConvArgs a;
+	memset(&a, 0, sizeof(a));
+	a.f = L->f;
+	a.buf = L->staging;
+	a.plane = L->plane;
+	a.ncell = L->ncell;
+	a.nx = (int)L->desc.nx;
+	a.ny = (int)L->desc.ny;
+	a.nz = (int)L->desc.nz;
+	a.nxp = L->nxp;
+	a.Q = L->d.Q;
+	a.D = L->d.D;
+	a.storage = L->desc.storage;
+	a.dtype = dtype;
+	a.layout = layout;
+	a.odd = (int)(L->t & 1u);
+	a.periodic = (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0;
+	for (int i = 0; i < L->d.Q; ++i) {
+		for (int k = 0; k < 3; ++k) a.c[i][k] = L->d.c[i][k];
+		a.opp[i] = L->d.opp[i];
+		a.wshift[i] = L->wshift[i];
+	}
+	return a;
+}
+
+static int check_io(kel_lattice *L, const void *host, int32_t dtype, int32_t layout, const char *who) {
+	if (!L || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: null argument", who);
+	if (dtype != KEL_DTYPE_F32 && dtype != KEL_DTYPE_F64) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: bad dtype", who);
+	if (layout != KEL_LAYOUT_AOS && layout != KEL_LAYOUT_SOA) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: bad layout", who);
+	return KEL_OK;
+}
+
+extern "C" int kel_upload_populations(kel_lattice *L, const void *host, int32_t dtype, int32_t layout) {
+	int rc = check_io(L, host, dtype, layout, "kel_upload_populations");
+	if (rc) return rc;
+	const size_t bytes = (size_t)L->ncell * L->d.Q * (dtype == KEL_DTYPE_F32 ? 4 : 8);
+	if ((rc = ensure_staging(L, bytes))) return rc;
+	KEL_CUDA(cudaMemcpyAsync(L->staging, host, bytes, cudaMemcpyHostToDevice, L->stream));
+	k_pop_convert<<<grid_for(L->ncell * L->d.Q), 256, 0, L->stream>>>(conv_args(L, dtype, layout), 1);
+	KEL_CUDA(cudaGetLastError());
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_download_populations(kel_lattice *L, void *host, int32_t dtype, int32_t layout) {
+	int rc = check_io(L, host, dtype, layout, "kel_download_populations");
+	if (rc) return rc;
+	const size_t bytes = (size_t)L->ncell * L->d.Q * (dtype == KEL_DTYPE_F32 ? 4 : 8);
+	if ((rc = ensure_staging(L, bytes))) return rc;
+	k_pop_convert<<<grid_for(L->ncell * L->d.Q), 256, 0, L->stream>>>(conv_args(L, dtype, layout), 0);
+	KEL_CUDA(cudaGetLastError());
+	KEL_CUDA(cudaMemcpyAsync(host, L->staging, bytes, cudaMemcpyDeviceToHost, L->stream));
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	return KEL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// macros and per-cell fields: padded plane layout <-> host AoS
+
+__global__ void k_field_io(float *dev, float *buf, int64_t plane, int64_t ncell, int nx, int ny, int nxp, int comps,
+						   int upload) {
+	const int64_t total = ncell * comps;
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+		const int64_t c = k / comps;
+		const int d = (int)(k % comps);
+		const int x = (int)(c % nx);
+		const int64_t row = c / nx;
+		const int64_t idx = (int64_t)d * plane + row * nxp + x;
+		(void)ny;
+		if (upload) dev[idx] = buf[k];
+		else buf[k] = dev[idx];
+	}
+}
+
+static int field_io(kel_lattice *L, float *dev, float *host_out, const float *host_in, int comps) {
+	const size_t bytes = (size_t)L->ncell * comps * sizeof(float);
+	int rc = ensure_staging(L, bytes);
+	if (rc) return rc;
+	float *buf = static_cast<float *>(L->staging);
+	if (host_in) KEL_CUDA(cudaMemcpyAsync(buf, host_in, bytes, cudaMemcpyHostToDevice, L->stream));
+	k_field_io<<<grid_for(L->ncell * comps), 256, 0, L->stream>>>(dev, buf, L->plane, L->ncell, (int)L->desc.nx,
+																   (int)L->desc.ny, L->nxp, comps, host_in ? 1 : 0);
+	KEL_CUDA(cudaGetLastError());
+	if (host_out) KEL_CUDA(cudaMemcpyAsync(host_out, buf, bytes, cudaMemcpyDeviceToHost, L->stream));
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_download_macros(kel_lattice *L, float *host_rho, float *host_u) {
+	if (!L || (!host_rho && !host_u)) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_download_macros: null argument");
+	int rc;
+	if (host_rho && (rc = field_io(L, L->rho, host_rho, nullptr, 1))) return rc;
+	if (host_u && (rc = field_io(L, L->u, host_u, nullptr, L->d.D))) return rc;
+	return KEL_OK;
+}
+
+extern "C" int kel_upload_field(kel_lattice *L, int32_t field, const float *host) {
+	if (!L || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_upload_field: null argument");
+	int rc;
+	if (field == KEL_FIELD_POROSITY) {
+		if ((rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
+		return field_io(L, L->por, nullptr, host, 1);
+	}
+	if (field == KEL_FIELD_FORCE) {
+		if ((rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
+		return field_io(L, L->force, nullptr, host, L->d.D);
+	}
+	return fail(KEL_ERR_INVALID_ARGUMENT, "kel_upload_field: unknown field %d", field);
+}
+
+extern "C" int kel_download_field(kel_lattice *L, int32_t field, float *host) {
+	if (!L || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_download_field: null argument");
+	int rc;
+	if (field == KEL_FIELD_POROSITY) {
+		if ((rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
+		return field_io(L, L->por, host, nullptr, 1);
+	}
+	if (field == KEL_FIELD_FORCE) {
+		if ((rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
+		return field_io(L, L->force, host, nullptr, L->d.D);
+	}
+	return fail(KEL_ERR_INVALID_ARGUMENT, "kel_download_field: unknown field %d", field);
+}
+
+extern "C" int kel_upload_inlet_profile(kel_lattice *L, const double *host_ux, int64_t n) {
+	if (!L || !host_ux) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_upload_inlet_profile: null argument");
+	if (n != L->desc.ny) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_upload_inlet_profile: need ny = %lld values",
+									 (long long)L->desc.ny);
+	std::vector<float> v(n);
+	for (int64_t i = 0; i < n; ++i) v[i] = (float)host_ux[i];
+	KEL_CUDA(cudaMemcpyAsync(L->profile, v.data(), n * sizeof(float), cudaMemcpyHostToDevice, L->stream));
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	return KEL_OK;
+}
+
+// ---------------------------------------------------------------------------
+// program lowering and stepping
+
+static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops) {
+	const HostDesc &d = L->d;
+	if (P->collision < KEL_COLL_BGK || P->collision > KEL_COLL_PSM_GUO)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown collision %d", P->collision);
+	if (P->arithmetic != KEL_ARITH_FAST && P->arithmetic != KEL_ARITH_REFERENCE)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown arithmetic mode %d", P->arithmetic);
+	if (P->arithmetic == KEL_ARITH_REFERENCE && L->desc.storage != KEL_STORAGE_FP32)
+		return fail(KEL_ERR_UNSUPPORTED, "kel_step: reference arithmetic needs FP32 storage");
+	if (!(P->tau > 0.0)) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: tau must be positive");
+	memset(ops, 0, sizeof(OpEntry) * MAX_FLAGS);
+	for (int fl = 0; fl < MAX_FLAGS; ++fl) {
+		const kel_flag_op &o = P->ops[fl];
+		OpEntry &e = ops[fl];
+		if (o.bc < KEL_BC_NONE || o.bc > KEL_BC_EQUILIBRIUM)
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: flag %d: unknown boundary op %d", fl, o.bc);
+		if (o.bc == KEL_BC_ZOUHE_VELOCITY_X && d.Q != 9)
+			return fail(KEL_ERR_UNSUPPORTED, "kel_step: ZouHeVelocityX exists only for D2Q9 (boundary.hpp:759)");
+		if (o.bc == KEL_BC_ZOUHE_PRESSURE_X && d.Q == 19)
+			return fail(KEL_ERR_UNSUPPORTED, "kel_step: ZouHePressureX has no D3Q19 specialisation");
+		if (o.bc == KEL_BC_ANTI_BOUNCE_BACK && d.Q != 9)
+			return fail(KEL_ERR_UNSUPPORTED, "kel_step: AntiBounceBack is D2Q9 only (boundary.hpp:117)");
+		e.bc = o.bc;
+		e.collide = o.collide ? 1 : 0;
+		e.east = o.east ? 1 : 0;
+		e.use_profile = o.use_profile ? 1 : 0;
+		e.rho = (float)o.rho;
+		for (int k = 0; k < 3; ++k) e.u[k] = (float)o.u[k];
+		// moving wall, cavity_2d_gpu.cpp:224-233, e.u summed over all axes in double
+		for (int i = 0; i < d.Q; ++i) {
+			double edu = 0.0;
+			for (int k = 0; k < d.D; ++k) edu = edu + (double)(float)d.c[i][k] * o.u[k];
+			e.lid[i] = (float)(2.0 * (double)(float)d.w[i] * (double)3.0f * edu);
+		}
+		float uf[3] = {(float)o.u[0], (float)o.u[1], (float)o.u[2]};
+		host_equilibrium(d, (float)o.rho, uf, e.eq);
+	}
+	return KEL_OK;
+}
+
+extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_steps, uint32_t step_flags) {
+	if (!L || !P) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: null argument");
+	if (step_flags & ~(KEL_STEP_WRITE_MACROS | KEL_STEP_ALL_MACROS))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown step flags");
+	int rc;
+	if (!L->have_ops || memcmp(&L->last_prog, P, sizeof(*P)) != 0) {
+		OpEntry ops[MAX_FLAGS];
+		if ((rc = lower_program(L, P, ops))) return rc;
+		KEL_CUDA(cudaMemcpyAsync(L->ops, ops, sizeof(ops), cudaMemcpyHostToDevice, L->stream));
+		KEL_CUDA(cudaStreamSynchronize(L->stream));
+		L->last_prog = *P;
+		L->have_ops = true;
+	}
+	const bool psm = P->collision == KEL_COLL_PSM || P->collision == KEL_COLL_PSM_GUO;
+	const bool guo = P->collision == KEL_COLL_BGK_GUO || P->collision == KEL_COLL_PSM_GUO;
+	if (psm && (rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
+	if (guo && (rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
+
+	SweepParams p;
+	memset(&p, 0, sizeof(p));
+	p.f = L->f;
+	p.plane = L->plane;
+	p.flags = L->flags;
+	p.rho = L->rho;
+	p.u = L->u;
+	p.por = L->por;
+	p.force = L->force;
+	p.profile = L->profile;
+	p.ops = L->ops;
+	p.nxp = L->nxp;
+	p.ny = (int)L->desc.ny;
+	p.nz = (int)L->desc.nz;
+	p.nq = L->nq;
+	p.wpr = L->wpr;
+	p.periodic = (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0;
+	const float tau = (float)P->tau;
+	p.omega = 1.0f / tau;
+	p.guo_scale = 1.0f - 0.5f * p.omega;
+	for (int k = 0; k < 3; ++k) p.g[k] = (float)P->global_force[k];
+	for (int i = 0; i < 27; ++i) p.wshift[i] = L->wshift[i];
+	const bool exact = P->arithmetic == KEL_ARITH_REFERENCE;
+	for (uint64_t s = 0; s < n_steps; ++s) {
+		p.write_macros = (step_flags & KEL_STEP_ALL_MACROS) || ((step_flags & KEL_STEP_WRITE_MACROS) && s + 1 == n_steps);
+		const bool odd = (L->t & 1u) != 0;
+		cudaError_t e;
+		switch (L->d.Q) {
+		case 9: e = launch_sweep<D2Q9>(p, L->desc.storage, odd, P->collision, exact, L->stream); break;
+		case 19: e = launch_sweep<D3Q19>(p, L->desc.storage, odd, P->collision, exact, L->stream); break;
+		default: e = launch_sweep<D3Q27>(p, L->desc.storage, odd, P->collision, exact, L->stream); break;
+		}
+		if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_step: launch failed: %s", cudaGetErrorString(e));
+		L->t += 1;
+	}
+	return KEL_OK;
+}

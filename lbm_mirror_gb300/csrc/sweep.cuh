@@ -1,0 +1,628 @@
+// Fused collide + boundary + stream sweep (AA pattern, in place) for sm_103a.
+//
+// One kernel launch is one time step of keldu/lbm_mirror's driver loop: the
+// collide+BC parallel_for and the pull-Stream parallel_for of
+// examples/poiseulle_2d_gpu/poiseulle_2d_gpu.cpp:169-224,384-399 fused into a
+// single pass over HBM.
+//
+// Memory: one lattice of populations, structure of arrays.  Direction plane i
+// holds f_i of every cell; a plane is nz*ny rows of nxp cells (nxp = nx padded
+// to a multiple of 4; padding cells carry flag 0).  The AA pattern keeps the
+// reference's two-lattice semantics with one array:
+//   even t: cell x reads f_i from A[i][x] and writes f*_i to A[opp i][x];
+//   odd  t: cell x reads f_i from A[opp i][x - c_i] and writes f*_i to
+//           A[i][x + c_i].
+// Every location touched in a step is read and written by the same cell, so
+// the step is race free.  The reference's zero ghost ring is reproduced by
+// substituting zero for reads whose source lies outside the lattice and by
+// dropping writes whose destination does; a flag-0 cell emits zero
+// populations, which is what the ghost ring supplies.
+//
+// Threads: each thread owns 4 consecutive cells of a row (128-bit accesses for
+// FP32, 64-bit for FP16S).  Warps never straddle rows, so the x-shifted
+// accesses of odd steps are realigned with warp shuffles; only the first and
+// last lane of a warp touch a neighbouring warp's cells with scalar accesses.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cstdint>
+
+#include "descriptors.cuh"
+
+namespace kel {
+namespace gb {
+
+enum : int { STORE_FP32 = 0, STORE_FP16S = 1 };
+enum : int { COLL_BGK = 0, COLL_BGK_GUO = 1, COLL_PSM = 2, COLL_PSM_GUO = 3 };
+enum : int {
+	BC_NONE = 0,
+	BC_BOUNCE_BACK = 1,
+	BC_FLUID = 2,
+	BC_ZOUHE_VELOCITY_X = 3,
+	BC_ZOUHE_PRESSURE_X = 4,
+	BC_MOVING_WALL = 5,
+	BC_ANTI_BOUNCE_BACK = 6,
+	BC_EQUILIBRIUM = 7
+};
+constexpr int MAX_FLAGS = 8;
+
+// Per-flag operation, resident in device memory (read through the read-only path).
+struct OpEntry {
+	int32_t bc, collide, east, use_profile;
+	float rho;
+	float u[3];
+	float lid[27]; // moving-wall additive term 2 w_i (c_i.u_w)/cs^2, rounded like the reference
+	float eq[27];  // equilibrium(rho, u) for the Equilibrium boundary
+};
+
+struct SweepParams {
+	void *f;          // populations (float or __half), plane-major
+	int64_t plane;    // cells per direction plane (nz*ny*nxp)
+	const uint8_t *flags;
+	float *rho;       // macros "density" (plane layout)
+	float *u;         // macros "velocity", D planes
+	const float *por; // macros "porosity"
+	const float *force; // macros "force", D planes
+	const float *profile; // inlet u_x per y
+	const OpEntry *ops;
+	int nxp, ny, nz;
+	int nq;  // quads per row (nxp / 4)
+	int wpr; // warps per row
+	int periodic;
+	int write_macros;
+	float omega;      // 1/tau in float, as the reference divides
+	float guo_scale;  // 1 - 0.5 * omega
+	float g[3];       // global force
+	float wshift[27]; // FP16S: stored value is f - wshift[i]
+};
+
+// ---------------------------------------------------------------------------
+// Arithmetic policy.  EXACT: the reference's rounding sequence (no fused
+// multiply-add, equilibrium bracket in double); otherwise plain float math.
+template <bool EXACT>
+struct Ar;
+
+template <>
+struct Ar<true> {
+	__device__ static __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+	__device__ static __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+	__device__ static __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+	__device__ static __forceinline__ float div(float a, float b) { return __fdiv_rn(a, b); }
+};
+
+template <>
+struct Ar<false> {
+	__device__ static __forceinline__ float add(float a, float b) { return a + b; }
+	__device__ static __forceinline__ float sub(float a, float b) { return a - b; }
+	__device__ static __forceinline__ float mul(float a, float b) { return a * b; }
+	__device__ static __forceinline__ float div(float a, float b) { return a / b; }
+};
+
+// ---------------------------------------------------------------------------
+// Storage policy.
+template <int STORE>
+struct Store;
+
+template <>
+struct Store<STORE_FP32> {
+	using T = float;
+	__device__ static __forceinline__ float4 ld4(const void *base, int64_t idx, float) {
+		return __ldcs(reinterpret_cast<const float4 *>(static_cast<const float *>(base) + idx));
+	}
+	__device__ static __forceinline__ float ld1(const void *base, int64_t idx, float) {
+		return __ldcs(static_cast<const float *>(base) + idx);
+	}
+	__device__ static __forceinline__ void st4(void *base, int64_t idx, float4 v, float) {
+		__stcs(reinterpret_cast<float4 *>(static_cast<float *>(base) + idx), v);
+	}
+	__device__ static __forceinline__ void st1(void *base, int64_t idx, float v, float) {
+		__stcs(static_cast<float *>(base) + idx, v);
+	}
+};
+
+template <>
+struct Store<STORE_FP16S> {
+	using T = __half;
+	__device__ static __forceinline__ float4 ld4(const void *base, int64_t idx, float s) {
+		uint2 r = __ldcs(reinterpret_cast<const uint2 *>(static_cast<const __half *>(base) + idx));
+		__half2 a = *reinterpret_cast<__half2 *>(&r.x);
+		__half2 b = *reinterpret_cast<__half2 *>(&r.y);
+		float2 fa = __half22float2(a), fb = __half22float2(b);
+		return make_float4(fa.x + s, fa.y + s, fb.x + s, fb.y + s);
+	}
+	__device__ static __forceinline__ float ld1(const void *base, int64_t idx, float s) {
+		return __half2float(static_cast<const __half *>(base)[idx]) + s;
+	}
+	__device__ static __forceinline__ void st4(void *base, int64_t idx, float4 v, float s) {
+		__half2 a = __floats2half2_rn(v.x - s, v.y - s);
+		__half2 b = __floats2half2_rn(v.z - s, v.w - s);
+		uint2 r;
+		r.x = *reinterpret_cast<uint32_t *>(&a);
+		r.y = *reinterpret_cast<uint32_t *>(&b);
+		__stcs(reinterpret_cast<uint2 *>(static_cast<__half *>(base) + idx), r);
+	}
+	__device__ static __forceinline__ void st1(void *base, int64_t idx, float v, float s) {
+		static_cast<__half *>(base)[idx] = __float2half_rn(v - s);
+	}
+};
+
+// ---------------------------------------------------------------------------
+// Cell physics (one cell, populations in registers).
+
+// compute_rho_u, modules/core/c++/macroscopic.hpp:10-35
+template <class L, bool EXACT>
+__device__ __forceinline__ void moments(const float (&f)[L::Q], float &rho, float (&u)[3]) {
+	using A = Ar<EXACT>;
+	float r = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f;
+#pragma unroll
+	for (int j = 0; j < L::Q; ++j) {
+		r = A::add(r, f[j]);
+		if (L::cx(j) > 0) v0 = A::add(v0, f[j]);
+		if (L::cx(j) < 0) v0 = A::sub(v0, f[j]);
+		if (L::cy(j) > 0) v1 = A::add(v1, f[j]);
+		if (L::cy(j) < 0) v1 = A::sub(v1, f[j]);
+		if (L::D == 3) {
+			if (L::cz(j) > 0) v2 = A::add(v2, f[j]);
+			if (L::cz(j) < 0) v2 = A::sub(v2, f[j]);
+		}
+	}
+	rho = r;
+	if (EXACT) {
+		u[0] = A::div(v0, r);
+		u[1] = A::div(v1, r);
+		u[2] = L::D == 3 ? A::div(v2, r) : 0.f;
+	} else {
+		const float ir = 1.0f / r;
+		u[0] = v0 * ir;
+		u[1] = v1 * ir;
+		u[2] = L::D == 3 ? v2 * ir : 0.f;
+	}
+}
+
+// c_i . u with the reference's summation order (0 + u_0 c_0 + u_1 c_1 ...)
+template <class L, bool EXACT>
+__device__ __forceinline__ float cdot(int i, const float (&u)[3]) {
+	using A = Ar<EXACT>;
+	float s = 0.f;
+	if (L::cx(i) > 0) s = A::add(s, u[0]);
+	if (L::cx(i) < 0) s = A::sub(s, u[0]);
+	if (L::cy(i) > 0) s = A::add(s, u[1]);
+	if (L::cy(i) < 0) s = A::sub(s, u[1]);
+	if (L::D == 3) {
+		if (L::cz(i) > 0) s = A::add(s, u[2]);
+		if (L::cz(i) < 0) s = A::sub(s, u[2]);
+	}
+	return s;
+}
+
+// equilibrium, modules/core/c++/equilibrium.hpp:7-48
+template <class L, bool EXACT>
+__device__ __forceinline__ void equilibrium(float rho, const float (&u)[3], float (&eq)[L::Q]) {
+	using A = Ar<EXACT>;
+	float vv = A::mul(u[0], u[0]);
+	vv = A::add(vv, A::mul(u[1], u[1]));
+	if (L::D == 3) vv = A::add(vv, A::mul(u[2], u[2]));
+	if (EXACT) {
+		const double h = __dmul_rn(1.5, (double)vv);
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) {
+			const float vcc = A::mul(cdot<L, EXACT>(i, u), 3.0f);
+			const float wr = A::mul((float)L::w(i), rho);
+			double br = __dsub_rn(__dadd_rn(1.0, (double)vcc), h);
+			br = __dadd_rn(br, __dmul_rn((double)A::mul(vcc, vcc), 0.5));
+			eq[i] = __double2float_rn(__dmul_rn((double)wr, br));
+		}
+	} else {
+		const float a0 = 1.0f - 1.5f * vv;
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) {
+			const float vcc = 3.0f * cdot<L, false>(i, u);
+			const float wr = (float)L::w(i) * rho;
+			eq[i] = wr * (a0 + vcc * (1.0f + 0.5f * vcc));
+		}
+	}
+}
+
+// Guo forcing term F_i, modules/core/c++/collision.hpp:170-196
+template <class L, bool EXACT>
+__device__ __forceinline__ float guo_term(int i, const float (&u)[3], const float (&F)[3]) {
+	using A = Ar<EXACT>;
+	const float s = A::mul(A::mul(cdot<L, EXACT>(i, u), 3.0f), 3.0f);
+	float proj = 0.f;
+#pragma unroll
+	for (int k = 0; k < L::D; ++k) {
+		const float ck = (float)cdir<L>(i, k);
+		const float t1 = A::mul(A::sub(ck, u[k]), 3.0f);
+		const float t2 = A::mul(ck, s);
+		proj = A::add(proj, A::mul(A::add(t1, t2), F[k]));
+	}
+	return A::mul((float)L::w(i), proj);
+}
+
+// D2Q9 ZouHePressureX<Dir>, modules/core/c++/boundary.hpp:186-226
+template <bool EXACT>
+__device__ __forceinline__ void zouhe_pressure_d2q9(float (&f)[9], bool east, float rs) {
+	using A = Ar<EXACT>;
+	const float c23 = (float)(2.0 / 3.0), c16 = (float)(1.0 / 6.0);
+	if (east) {
+		const float S = A::add(A::add(A::add(f[0], f[3]), f[4]), A::mul(A::add(A::add(f[1], f[5]), f[7]), 2.f));
+		const float r = A::sub(rs, S);
+		f[2] = A::add(f[1], A::mul(c23, r));
+		f[6] = A::add(A::add(f[5], A::mul(c16, r)), A::mul(0.5f, A::sub(f[3], f[4])));
+		f[8] = A::add(A::add(f[7], A::mul(c16, r)), A::mul(0.5f, A::sub(f[4], f[3])));
+	} else {
+		const float S = A::add(A::add(A::add(f[0], f[3]), f[4]), A::mul(A::add(A::add(f[2], f[6]), f[8]), 2.f));
+		const float r = A::sub(S, rs);
+		f[1] = A::sub(f[2], A::mul(c23, r));
+		f[5] = A::add(A::sub(f[6], A::mul(c16, r)), A::mul(0.5f, A::sub(f[4], f[3])));
+		f[7] = A::add(A::sub(f[8], A::mul(c16, r)), A::mul(0.5f, A::sub(f[3], f[4])));
+	}
+}
+
+// D2Q9 ZouHeVelocityX<East>, modules/core/c++/boundary.hpp:775-802
+template <bool EXACT>
+__device__ __forceinline__ void zouhe_velocity_d2q9(float (&f)[9], bool east, float ux, float uy) {
+	using A = Ar<EXACT>;
+	const float c23 = (float)(2.0 / 3.0), c16 = (float)(1.0 / 6.0);
+	const float ds = east ? A::add(A::add(f[1], f[5]), f[7]) : A::add(A::add(f[2], f[6]), f[8]);
+	const float rho = A::div(A::add(A::add(A::add(f[0], f[4]), f[3]), A::mul(ds, 2.f)), A::add(ux, 1.0f));
+	const float rux = A::mul(A::mul(c16, rho), ux);
+	const float ruy = A::mul(rho, uy);
+	if (east) {
+		f[2] = A::add(f[1], A::mul(A::mul(c23, rho), ux));
+		f[6] = A::add(A::add(f[5], rux), A::mul(A::add(A::sub(f[3], f[4]), ruy), 0.5f));
+		f[8] = A::add(A::add(f[7], rux), A::mul(A::add(A::sub(f[4], f[3]), ruy), 0.5f));
+	} else {
+		f[1] = A::add(f[2], A::mul(A::mul(c23, rho), ux));
+		f[5] = A::add(A::add(f[6], rux), A::mul(A::add(A::sub(f[4], f[3]), ruy), 0.5f));
+		f[7] = A::add(A::add(f[8], rux), A::mul(A::add(A::sub(f[3], f[4]), ruy), 0.5f));
+	}
+}
+
+// D3Q27 ZouHePressureX<East>, modules/core/c++/boundary.hpp:229-756
+template <bool EXACT>
+__device__ __forceinline__ void zouhe_pressure_d3q27(float (&f)[27], bool east, float rs) {
+	using A = Ar<EXACT>;
+	const float a = (float)(4.0 / 9.0), b = (float)(1.0 / 9.0), e = (float)(1.0 / 36.0);
+	float S = f[0];
+	S = A::add(S, f[3]);
+	S = A::add(S, f[6]);
+	S = A::add(S, f[9]);
+	S = A::add(S, f[12]);
+	S = A::add(S, f[15]);
+	S = A::add(S, f[18]);
+	S = A::add(S, f[21]);
+	S = A::add(S, f[24]);
+	// known side: cx = +1 at x = max (east = false), cx = -1 at x = 0 (east = true)
+	const int k0 = east ? 1 : 2;
+	float K = f[k0];
+#pragma unroll
+	for (int j = 1; j < 9; ++j) K = A::add(K, f[k0 + 3 * j]);
+	S = A::add(S, A::mul(2.f, K));
+	const float rux = east ? A::sub(rs, S) : A::sub(S, rs);
+	// tangential momenta
+	float ruy = A::add(-f[3], f[6]);
+	ruy = A::sub(ruy, f[12]);
+	ruy = A::add(ruy, f[15]);
+	ruy = A::sub(ruy, f[21]);
+	ruy = A::add(ruy, f[24]);
+	float ty = A::add(-f[k0 + 3], f[k0 + 6]);
+	ty = A::sub(ty, f[k0 + 12]);
+	ty = A::add(ty, f[k0 + 15]);
+	ty = A::sub(ty, f[k0 + 21]);
+	ty = A::add(ty, f[k0 + 24]);
+	ruy = A::add(ruy, A::mul(2.f, ty));
+	float ruz = A::sub(-f[9], f[12]);
+	ruz = A::sub(ruz, f[15]);
+	ruz = A::add(ruz, f[18]);
+	ruz = A::add(ruz, f[21]);
+	ruz = A::add(ruz, f[24]);
+	float tz = A::sub(-f[k0 + 9], f[k0 + 12]);
+	tz = A::sub(tz, f[k0 + 15]);
+	tz = A::add(tz, f[k0 + 18]);
+	tz = A::add(tz, f[k0 + 21]);
+	tz = A::add(tz, f[k0 + 24]);
+	ruz = A::add(ruz, A::mul(2.f, tz));
+	if (!east) {
+		f[1] = A::sub(f[2], A::mul(a, rux));
+		f[4] = A::sub(f[5], A::mul(b, A::add(rux, ruy)));
+		f[7] = A::add(f[8], A::mul(b, A::add(-rux, ruy)));
+		f[10] = A::sub(f[11], A::mul(b, A::add(rux, ruz)));
+		f[13] = A::sub(f[14], A::mul(e, A::add(A::add(rux, ruy), ruz)));
+		f[16] = A::add(f[17], A::mul(e, A::add(A::add(-rux, ruy), ruz)));
+		f[19] = A::add(f[20], A::mul(b, A::add(-rux, ruz)));
+		f[22] = A::add(f[23], A::mul(e, A::add(A::sub(-rux, ruy), ruz)));
+		f[25] = A::add(f[26], A::mul(e, A::add(A::add(-rux, ruy), ruz)));
+	} else {
+		f[2] = A::add(f[1], A::mul(a, rux));
+		f[5] = A::add(f[4], A::mul(b, A::sub(rux, ruy)));
+		f[8] = A::add(f[7], A::mul(b, A::add(rux, ruy)));
+		f[11] = A::add(f[10], A::mul(b, A::sub(rux, ruz)));
+		f[14] = A::add(f[13], A::mul(e, A::sub(A::sub(rux, ruy), ruz)));
+		f[17] = A::add(f[16], A::mul(e, A::sub(A::add(rux, ruy), ruz)));
+		f[20] = A::add(f[19], A::mul(b, A::add(rux, ruz)));
+		f[23] = A::add(f[22], A::mul(e, A::add(A::sub(rux, ruy), ruz)));
+		f[26] = A::add(f[25], A::mul(e, A::add(A::add(rux, ruy), ruz)));
+	}
+}
+
+// The collision chosen by the program (BGK / BGKGuo / Psm / Psm + Guo).
+template <class L, int COLL, bool EXACT>
+__device__ __forceinline__ void collide(float (&f)[L::Q], const SweepParams &p, float por, const float (&Fc)[3],
+										float &rho, float (&u)[3]) {
+	using A = Ar<EXACT>;
+	moments<L, EXACT>(f, rho, u);
+	float eq[L::Q];
+	equilibrium<L, EXACT>(rho, u, eq);
+	float F[3] = {0.f, 0.f, 0.f};
+	if (COLL == COLL_BGK_GUO || COLL == COLL_PSM_GUO) {
+#pragma unroll
+		for (int k = 0; k < L::D; ++k) F[k] = A::add(Fc[k], p.g[k]);
+	}
+	if (COLL == COLL_BGK) {
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) f[i] = A::add(f[i], A::mul(p.omega, A::sub(eq[i], f[i])));
+	} else if (COLL == COLL_BGK_GUO) {
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) {
+			const float Fi = guo_term<L, EXACT>(i, u, F);
+			f[i] = A::add(A::add(f[i], A::mul(p.omega, A::sub(eq[i], f[i]))), A::mul(Fi, p.guo_scale));
+		}
+	} else { // PSM, psm.hpp:79-88
+		const float flip = A::sub(1.0f, por);
+		float pre[L::Q];
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) pre[i] = f[i];
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) {
+			float v = A::add(pre[i], A::mul(A::mul(p.omega, A::sub(eq[i], pre[i])), por));
+			v = A::add(v, A::mul(A::sub(pre[L::opp(i)], pre[i]), flip));
+			if (COLL == COLL_PSM_GUO) v = A::add(v, A::mul(guo_term<L, EXACT>(i, u, F), p.guo_scale));
+			f[i] = v;
+		}
+	}
+}
+
+// Boundary step + collision of one cell (the body of a driver's switch(info)).
+// Returns true when the cell collided (its moments go to the macro fields).
+template <class L, int COLL, bool EXACT>
+__device__ __forceinline__ bool cell_update(float (&f)[L::Q], int flag, int y, const SweepParams &p, float por,
+											const float (&Fc)[3], float &rho, float (&u)[3]) {
+	using A = Ar<EXACT>;
+	if (flag == 0) { // outside the lattice: what the zero ghost ring supplies
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) f[i] = 0.f;
+		return false;
+	}
+	if (flag >= MAX_FLAGS) return false; // the drivers' `default: break;`
+	const OpEntry *op = p.ops + flag;
+	const int bc = __ldg(&op->bc);
+	float cpy[L::Q];
+	switch (bc) {
+	case BC_BOUNCE_BACK: // boundary.hpp:58-75 (full-way)
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) cpy[i] = f[i];
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) f[i] = cpy[L::opp(i)];
+		break;
+	case BC_MOVING_WALL: // examples/cavity_2d_gpu/cavity_2d_gpu.cpp:222-234
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) cpy[i] = f[i];
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) f[i] = A::add(cpy[L::opp(i)], __ldg(&op->lid[i]));
+		break;
+	case BC_EQUILIBRIUM: // boundary.hpp:147-160
+#pragma unroll
+		for (int i = 0; i < L::Q; ++i) f[i] = __ldg(&op->eq[i]);
+		break;
+	case BC_ANTI_BOUNCE_BACK: // boundary.hpp:119-132 (D2Q9 only)
+		if constexpr (L::Q == 9) {
+			float t;
+			t = f[3]; f[3] = f[4]; f[4] = t;
+			t = f[5]; f[5] = f[7]; f[7] = t;
+			t = f[6]; f[6] = f[8]; f[8] = t;
+		}
+		break;
+	case BC_ZOUHE_PRESSURE_X:
+		if constexpr (L::Q == 9) zouhe_pressure_d2q9<EXACT>(f, __ldg(&op->east) != 0, __ldg(&op->rho));
+		if constexpr (L::Q == 27) zouhe_pressure_d3q27<EXACT>(f, __ldg(&op->east) != 0, __ldg(&op->rho));
+		break;
+	case BC_ZOUHE_VELOCITY_X:
+		if constexpr (L::Q == 9) {
+			const float ux = __ldg(&op->use_profile) ? __ldg(p.profile + y) : __ldg(&op->u[0]);
+			zouhe_velocity_d2q9<EXACT>(f, __ldg(&op->east) != 0, ux, __ldg(&op->u[1]));
+		}
+		break;
+	default:
+		break;
+	}
+	if (__ldg(&op->collide)) {
+		collide<L, COLL, EXACT>(f, p, por, Fc, rho, u);
+		return true;
+	}
+	return false;
+}
+
+// ---------------------------------------------------------------------------
+// The sweep kernel.
+
+__device__ __forceinline__ float f4get(const float4 &v, int k) {
+	return k == 0 ? v.x : (k == 1 ? v.y : (k == 2 ? v.z : v.w));
+}
+
+template <class L, int STORE, bool ODD, int COLL, bool EXACT>
+__global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ SweepParams p) {
+	using S = Store<STORE>;
+	constexpr int Q = L::Q;
+	const int lane = threadIdx.x & 31;
+	const int64_t gwarp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+	const int64_t row = gwarp / p.wpr;
+	const int64_t nrows = static_cast<int64_t>(p.ny) * p.nz;
+	if (row >= nrows) return; // warp-uniform: a warp never spans rows
+	const int qd = static_cast<int>(gwarp % p.wpr) * 32 + lane;
+	const bool active = qd < p.nq;
+	const int x0 = qd * 4;
+	const int y = static_cast<int>(row % p.ny);
+	const int z = static_cast<int>(row / p.ny);
+	const int nxp = p.nxp;
+	const int64_t rbase = row * nxp; // first cell of this row
+	const unsigned FULL = 0xffffffffu;
+
+	float f[Q][4];
+
+	// ---- gather the post-stream populations f_i of the 4 cells -------------
+#pragma unroll
+	for (int i = 0; i < Q; ++i) {
+		const float s = p.wshift[i];
+		if (!ODD) {
+			float4 v = active ? S::ld4(p.f, i * p.plane + rbase + x0, s) : make_float4(0.f, 0.f, 0.f, 0.f);
+			f[i][0] = v.x; f[i][1] = v.y; f[i][2] = v.z; f[i][3] = v.w;
+		} else {
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int sy = y - cy, sz = z - cz;
+			const bool row_in = (sy >= 0) && (sy < p.ny) && (sz >= 0) && (sz < p.nz);
+			const int64_t sb = static_cast<int64_t>(L::opp(i)) * p.plane + (static_cast<int64_t>(sz) * p.ny + sy) * nxp;
+			float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+			if (row_in && active) v = S::ld4(p.f, sb + x0, s);
+			if (cx == 0) {
+				f[i][0] = v.x; f[i][1] = v.y; f[i][2] = v.z; f[i][3] = v.w;
+			} else if (cx > 0) { // source x - 1
+				float prev = __shfl_up_sync(FULL, v.w, 1);
+				if (lane == 0 || x0 == 0) {
+					prev = 0.f;
+					if (row_in && active) {
+						if (x0 > 0) prev = S::ld1(p.f, sb + x0 - 1, s);
+						else if (p.periodic) prev = S::ld1(p.f, sb + nxp - 1, s);
+					}
+				}
+				f[i][0] = prev; f[i][1] = v.x; f[i][2] = v.y; f[i][3] = v.z;
+			} else { // source x + 1
+				float next = __shfl_down_sync(FULL, v.x, 1);
+				if (lane == 31 || x0 + 4 >= nxp) {
+					next = 0.f;
+					if (row_in && active) {
+						if (x0 + 4 < nxp) next = S::ld1(p.f, sb + x0 + 4, s);
+						else if (p.periodic) next = S::ld1(p.f, sb, s);
+					}
+				}
+				f[i][0] = v.y; f[i][1] = v.z; f[i][2] = v.w; f[i][3] = next;
+			}
+		}
+	}
+
+	// ---- boundary step + collision per cell ---------------------------------
+	uchar4 fl = make_uchar4(0, 0, 0, 0);
+	if (active) fl = *reinterpret_cast<const uchar4 *>(p.flags + rbase + x0);
+	float4 porv = make_float4(1.f, 1.f, 1.f, 1.f);
+	if ((COLL == COLL_PSM || COLL == COLL_PSM_GUO) && active)
+		porv = *reinterpret_cast<const float4 *>(p.por + rbase + x0);
+	float4 fcv[3] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
+	if ((COLL == COLL_BGK_GUO || COLL == COLL_PSM_GUO) && active) {
+#pragma unroll
+		for (int k = 0; k < L::D; ++k) fcv[k] = *reinterpret_cast<const float4 *>(p.force + k * p.plane + rbase + x0);
+	}
+	float4 rho4 = make_float4(0.f, 0.f, 0.f, 0.f);
+	float4 u4[3] = {rho4, rho4, rho4};
+	int collided = 0;
+#pragma unroll
+	for (int k = 0; k < 4; ++k) {
+		const int flag = k == 0 ? fl.x : (k == 1 ? fl.y : (k == 2 ? fl.z : fl.w));
+		float c[Q];
+#pragma unroll
+		for (int i = 0; i < Q; ++i) c[i] = f[i][k];
+		float Fc[3] = {f4get(fcv[0], k), f4get(fcv[1], k), f4get(fcv[2], k)};
+		float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
+		const bool col = cell_update<L, COLL, EXACT>(c, flag, y, p, f4get(porv, k), Fc, rho, u);
+		collided |= (col ? 1 : 0) << k;
+		if (k == 0) { rho4.x = rho; u4[0].x = u[0]; u4[1].x = u[1]; u4[2].x = u[2]; }
+		if (k == 1) { rho4.y = rho; u4[0].y = u[0]; u4[1].y = u[1]; u4[2].y = u[2]; }
+		if (k == 2) { rho4.z = rho; u4[0].z = u[0]; u4[1].z = u[1]; u4[2].z = u[2]; }
+		if (k == 3) { rho4.w = rho; u4[0].w = u[0]; u4[1].w = u[1]; u4[2].w = u[2]; }
+#pragma unroll
+		for (int i = 0; i < Q; ++i) f[i][k] = c[i];
+	}
+
+	// ---- macros of collided cells (collision.hpp:83-89) ---------------------
+	if (p.write_macros && active && collided) {
+		if (collided == 0xF) {
+			*reinterpret_cast<float4 *>(p.rho + rbase + x0) = rho4;
+#pragma unroll
+			for (int k = 0; k < L::D; ++k) *reinterpret_cast<float4 *>(p.u + k * p.plane + rbase + x0) = u4[k];
+		} else {
+#pragma unroll
+			for (int k = 0; k < 4; ++k) {
+				if (collided & (1 << k)) {
+					p.rho[rbase + x0 + k] = f4get(rho4, k);
+#pragma unroll
+					for (int d = 0; d < L::D; ++d) p.u[d * p.plane + rbase + x0 + k] = f4get(u4[d], k);
+				}
+			}
+		}
+	}
+
+	// ---- scatter the post-collision populations -----------------------------
+#pragma unroll
+	for (int i = 0; i < Q; ++i) {
+		const float s = p.wshift[i];
+		if (!ODD) {
+			if (active)
+				S::st4(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + rbase + x0,
+					   make_float4(f[i][0], f[i][1], f[i][2], f[i][3]), s);
+		} else {
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int64_t pb = static_cast<int64_t>(i) * p.plane;
+			// slots of this row whose source lies outside: the ghost ring's zero
+			{
+				const int sy = y - cy, sz = z - cz;
+				const bool src_row_in = (sy >= 0) && (sy < p.ny) && (sz >= 0) && (sz < p.nz);
+				if (!src_row_in) {
+					if (active) S::st4(p.f, pb + rbase + x0, make_float4(0.f, 0.f, 0.f, 0.f), s);
+				} else if (!p.periodic && active) {
+					if (cx > 0 && x0 == 0) S::st1(p.f, pb + rbase, 0.f, s);
+					if (cx < 0 && x0 + 4 == nxp) S::st1(p.f, pb + rbase + nxp - 1, 0.f, s);
+				}
+			}
+			const int dy = y + cy, dz = z + cz;
+			const bool row_in = (dy >= 0) && (dy < p.ny) && (dz >= 0) && (dz < p.nz);
+			const int64_t db = pb + (static_cast<int64_t>(dz) * p.ny + dy) * nxp;
+			if (cx == 0) {
+				if (row_in && active) S::st4(p.f, db + x0, make_float4(f[i][0], f[i][1], f[i][2], f[i][3]), s);
+			} else if (cx > 0) { // destination x + 1
+				const float q = __shfl_up_sync(FULL, f[i][3], 1);
+				if (row_in && active) {
+					if (lane > 0) {
+						S::st4(p.f, db + x0, make_float4(q, f[i][0], f[i][1], f[i][2]), s);
+					} else { // element x0 belongs to the previous warp (or is a ghost slot zeroed above)
+						S::st1(p.f, db + x0 + 1, f[i][0], s);
+						S::st1(p.f, db + x0 + 2, f[i][1], s);
+						S::st1(p.f, db + x0 + 3, f[i][2], s);
+					}
+					if (x0 + 4 < nxp) {
+						if (lane == 31) S::st1(p.f, db + x0 + 4, f[i][3], s);
+					} else if (p.periodic) {
+						S::st1(p.f, db, f[i][3], s);
+					}
+				}
+			} else { // destination x - 1
+				const float r = __shfl_down_sync(FULL, f[i][0], 1);
+				if (row_in && active) {
+					if (lane < 31 && x0 + 4 < nxp) {
+						S::st4(p.f, db + x0, make_float4(f[i][1], f[i][2], f[i][3], r), s);
+					} else { // element x0+3 belongs to the next warp (or is a ghost slot zeroed above)
+						S::st1(p.f, db + x0, f[i][1], s);
+						S::st1(p.f, db + x0 + 1, f[i][2], s);
+						S::st1(p.f, db + x0 + 2, f[i][3], s);
+					}
+					if (x0 > 0) {
+						if (lane == 0) S::st1(p.f, db + x0 - 1, f[i][0], s);
+					} else if (p.periodic) {
+						S::st1(p.f, db + nxp - 1, f[i][0], s);
+					}
+				}
+			}
+		}
+	}
+}
+
+} // namespace gb
+} // namespace kel

@@ -1,0 +1,250 @@
+"""Python host mirror of the reference's lattice/component interface.
+
+A reference driver builds components (``component<T,Desc,cmpt::BGK>{tau}``,
+``cmpt::BounceBack``, ``cmpt::ZouHeVelocityX<true>{u}``, ...) and applies
+them per cell through ``switch(info)`` (e.g.
+examples/poiseulle_2d_gpu/poiseulle_2d_gpu.cpp:169-224).  Here the same
+components are plain descriptions; ``program_from_switch`` lowers a
+``{flag: [components]}`` switch into the C ABI's kel_step_program and a
+``Lattice`` runs it on the GPU through libkel_lbm_cuda.so.  There is no CPU
+path: constructing a Lattice without the built library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi as K
+
+DESCRIPTORS = {"D2Q9": K.KEL_D2Q9, "D3Q19": K.KEL_D3Q19, "D3Q27": K.KEL_D3Q27}
+
+
+class KelError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{msg} (status {code})")
+        self.code = code
+
+
+def _check(rc, lib):
+    if rc != K.KEL_OK:
+        raise KelError(rc, lib.kel_last_error_string().decode())
+
+
+# ---- components (parameter carriers, reference spellings) -------------------
+@dataclass
+class BGK:
+    """cmpt::BGK (collision.hpp:19-97)."""
+    tau: float
+    collision = K.KEL_COLL_BGK
+
+
+@dataclass
+class BGKGuo:
+    """cmpt::BGKGuo (collision.hpp:99-205); adds the cell "force" field."""
+    tau: float
+    global_force: tuple = (0.0, 0.0, 0.0)
+    collision = K.KEL_COLL_BGK_GUO
+
+
+@dataclass
+class Psm:
+    """cmpt::Psm (psm.hpp:37-90); reads the cell "porosity" field."""
+    tau: float
+    collision = K.KEL_COLL_PSM
+
+
+@dataclass
+class PsmGuo:
+    """cmpt::Psm followed by the BGKGuo forcing term (no reference component)."""
+    tau: float
+    global_force: tuple = (0.0, 0.0, 0.0)
+    collision = K.KEL_COLL_PSM_GUO
+
+
+@dataclass
+class BounceBack:
+    """cmpt::BounceBack, full-way (boundary.hpp:32-76)."""
+    bc = K.KEL_BC_BOUNCE_BACK
+
+
+@dataclass
+class AntiBounceBack:
+    """cmpt::AntiBounceBack<0>, D2Q9 (boundary.hpp:81-133)."""
+    bc = K.KEL_BC_ANTI_BOUNCE_BACK
+
+
+@dataclass
+class Equilibrium:
+    """cmpt::Equilibrium(rho, u) (boundary.hpp:135-161)."""
+    rho: float
+    u: tuple
+    bc = K.KEL_BC_EQUILIBRIUM
+
+
+@dataclass
+class ZouHePressureX:
+    """cmpt::ZouHePressureX<East>(rho) (boundary.hpp:175-756)."""
+    east: bool
+    rho: float
+    bc = K.KEL_BC_ZOUHE_PRESSURE_X
+
+
+@dataclass
+class ZouHeVelocityX:
+    """cmpt::ZouHeVelocityX<East>(u) (boundary.hpp:759-805); ``u`` may be
+    "profile" to take u_x(y) from the uploaded inlet profile."""
+    east: bool
+    u: object
+    bc = K.KEL_BC_ZOUHE_VELOCITY_X
+
+
+@dataclass
+class MovingWall:
+    """Lid: f_i = f_opp + 2 w_i (c_i.u_w)/cs^2 (cavity_2d_gpu.cpp:204-235)."""
+    u: tuple
+    bc = K.KEL_BC_MOVING_WALL
+
+
+def program_from_switch(switch, arithmetic=K.KEL_ARITH_FAST):
+    """Lower ``{flag: [boundary?, collision?]}`` into a StepProgram.
+
+    Every collision in the switch must be the same operator (one per step, as
+    in every reference driver)."""
+    coll = None
+    ops = {}
+    for flag, comps in switch.items():
+        if not 0 < flag < K.KEL_MAX_FLAGS:
+            raise ValueError(f"flag {flag} out of range 1..{K.KEL_MAX_FLAGS - 1}")
+        op = dict(bc=K.KEL_BC_FLUID, collide=0)
+        for c in comps:
+            if hasattr(c, "collision"):
+                if coll is not None and (type(c) is not type(coll) or c != coll):
+                    raise ValueError("one collision operator per program")
+                coll = c
+                op["collide"] = 1
+            else:
+                op["bc"] = c.bc
+                if isinstance(c, (ZouHePressureX, ZouHeVelocityX)):
+                    op["east"] = int(c.east)
+                if isinstance(c, (ZouHePressureX, Equilibrium)):
+                    op["rho"] = c.rho
+                if isinstance(c, ZouHeVelocityX):
+                    if isinstance(c.u, str):
+                        op["use_profile"] = 1
+                    else:
+                        op["u"] = tuple(c.u)
+                if isinstance(c, (MovingWall, Equilibrium)):
+                    op["u"] = tuple(c.u)
+        ops[flag] = op
+    if coll is None:
+        coll = BGK(1.0)
+    return K.make_program(coll.tau, coll.collision, ops, getattr(coll, "global_force", (0.0, 0.0, 0.0)),
+                          arithmetic)
+
+
+def _ptr(a):
+    return C.c_void_p(a.ctypes.data)
+
+
+class Lattice:
+    """One lattice in HBM (structure of arrays, AA in-place), driven through
+    the C ABI.  ``dims`` = (nx, ny) for D2Q9, (nx, ny, nz) for D3Q*."""
+
+    def __init__(self, descriptor, dims, storage="fp32", periodic_x=False, stream=None):
+        self.lib = K.load_library()
+        q = DESCRIPTORS[descriptor] if isinstance(descriptor, str) else int(descriptor)
+        self.q = q
+        self.D = 2 if q == K.KEL_D2Q9 else 3
+        nx, ny = int(dims[0]), int(dims[1])
+        nz = int(dims[2]) if len(dims) > 2 else 1
+        self.dims = (nx, ny, nz)
+        self.n = nx * ny * nz
+        d = K.LatticeDesc()
+        d.descriptor = q
+        d.storage = {"fp32": K.KEL_STORAGE_FP32, "fp16s": K.KEL_STORAGE_FP16S}[storage]
+        d.nx, d.ny, d.nz = nx, ny, nz
+        d.flags = K.KEL_LATTICE_PERIODIC_X if periodic_x else 0
+        h = C.c_void_p()
+        _check(self.lib.kel_lattice_create(C.byref(d), C.byref(h)), self.lib)
+        self._h = h
+        if stream is not None:
+            self.set_stream(stream)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.kel_lattice_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream_handle: int):
+        _check(self.lib.kel_lattice_set_stream(self._h, C.c_void_p(stream_handle)), self.lib)
+
+    @property
+    def t(self):
+        v = C.c_uint64()
+        _check(self.lib.kel_lattice_time_step(self._h, C.byref(v)), self.lib)
+        return v.value
+
+    def upload_flags(self, flags):
+        a = np.ascontiguousarray(flags, dtype=np.uint8).reshape(-1)
+        if a.size != self.n:
+            raise ValueError("flags: wrong size")
+        _check(self.lib.kel_upload_flags(self._h, _ptr(a)), self.lib)
+
+    def upload_populations(self, f, layout="aos"):
+        a = np.ascontiguousarray(f)
+        if a.dtype not in (np.float32, np.float64):
+            a = a.astype(np.float64)
+        if a.size != self.n * self.q:
+            raise ValueError("populations: wrong size")
+        dt = K.KEL_DTYPE_F32 if a.dtype == np.float32 else K.KEL_DTYPE_F64
+        lay = K.KEL_LAYOUT_AOS if layout == "aos" else K.KEL_LAYOUT_SOA
+        _check(self.lib.kel_upload_populations(self._h, _ptr(a), dt, lay), self.lib)
+
+    def populations(self, dtype=np.float32, layout="aos"):
+        out = np.empty(self.n * self.q, dtype=dtype)
+        dt = K.KEL_DTYPE_F32 if out.dtype == np.float32 else K.KEL_DTYPE_F64
+        lay = K.KEL_LAYOUT_AOS if layout == "aos" else K.KEL_LAYOUT_SOA
+        _check(self.lib.kel_download_populations(self._h, _ptr(out), dt, lay), self.lib)
+        return out.reshape(self.n, self.q) if layout == "aos" else out.reshape(self.q, self.n)
+
+    def macros(self):
+        rho = np.empty(self.n, dtype=np.float32)
+        u = np.empty(self.n * self.D, dtype=np.float32)
+        _check(self.lib.kel_download_macros(self._h, _ptr(rho), _ptr(u)), self.lib)
+        return rho, u.reshape(self.n, self.D)
+
+    def upload_porosity(self, por):
+        a = np.ascontiguousarray(por, dtype=np.float32).reshape(-1)
+        _check(self.lib.kel_upload_field(self._h, K.KEL_FIELD_POROSITY, _ptr(a)), self.lib)
+
+    def upload_force(self, force):
+        a = np.ascontiguousarray(force, dtype=np.float32).reshape(-1)
+        _check(self.lib.kel_upload_field(self._h, K.KEL_FIELD_FORCE, _ptr(a)), self.lib)
+
+    def download_field(self, field_id, comps):
+        out = np.empty(self.n * comps, dtype=np.float32)
+        _check(self.lib.kel_download_field(self._h, field_id, _ptr(out)), self.lib)
+        return out
+
+    def upload_inlet_profile(self, ux):
+        a = np.ascontiguousarray(ux, dtype=np.float64)
+        _check(self.lib.kel_upload_inlet_profile(self._h, _ptr(a), a.size), self.lib)
+
+    def step(self, program, n_steps=1, write_macros=True, all_macros=False):
+        fl = (K.KEL_STEP_WRITE_MACROS if write_macros else 0) | (K.KEL_STEP_ALL_MACROS if all_macros else 0)
+        _check(self.lib.kel_step(self._h, C.byref(program), n_steps, fl), self.lib)
+
+    def synchronize(self):
+        _check(self.lib.kel_lattice_synchronize(self._h), self.lib)

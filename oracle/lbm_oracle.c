@@ -220,6 +220,11 @@ int ko_run(ko_lattice *h, const kel_step_program *prog, uint64_t steps) {
 	return run_f32(&h->f32, prog, steps);
 }
 
+int ko_run_rows(ko_lattice *h, const kel_step_program *prog, int64_t r0, int64_t r1) {
+	if (h->is_f64) return run_rows_f64(&h->f64, prog, r0, r1);
+	return run_rows_f32(&h->f32, prog, r0, r1);
+}
+
 uint64_t ko_time_step(const ko_lattice *h) { return h->is_f64 ? h->f64.t : h->f32.t; }
 
 /* Helper for tests: the reference equilibrium of (rho, u) in float

@@ -189,7 +189,8 @@ static void KO(zouhe_velocity_d2q9)(REAL *f, int east, REAL ux, REAL uy) {
 static int KO(cell_step)(KO(ko_lat) * L, const kel_step_program *P, int64_t c, int64_t x, int64_t y, int64_t z, REAL *buf) {
 	const ko_desc *d = &L->d;
 	uint8_t info = L->info[c];
-	if (info >= KEL_MAX_FLAGS) return 0;
+	/* `case 0u: break;` and `default: break;` of the drivers' switch(info) */
+	if (info == 0u || info >= KEL_MAX_FLAGS) return 0;
 	const kel_flag_op *o = &P->ops[info];
 	REAL *f = buf + KO(gidx)(L, x, y, z) * d->Q;
 	REAL cpy[27];
@@ -277,6 +278,30 @@ static int KO(run)(KO(ko_lat) * L, const kel_step_program *P, uint64_t steps) {
 		}
 		(void)d;
 		L->t += 1;
+	}
+	return 0;
+}
+
+/* Throughput sample: the collide+boundary pass and the stream pass of one
+ * time step restricted to rows [r0, r1) (row = z*ny + y).  The time step
+ * counter does not advance; used only to time the reference algorithm on a
+ * bounded part of a large lattice. */
+static int KO(run_rows)(KO(ko_lat) * L, const kel_step_program *P, int64_t r0, int64_t r1) {
+	int even = (L->t % 2u) == 0u;
+	REAL *old = even ? L->dfs[0] : L->dfs[1];
+	REAL *nw = even ? L->dfs[1] : L->dfs[0];
+	int err = 0;
+#pragma omp parallel for schedule(static) reduction(| : err)
+	for (int64_t zy = r0; zy < r1; ++zy) {
+		int64_t z = zy / L->ny, y = zy % L->ny;
+		for (int64_t x = 0; x < L->nx; ++x) err |= KO(cell_step)(L, P, x + L->nx * zy, x, y, z, old) != 0;
+	}
+	if (err) return -1;
+#pragma omp parallel for schedule(static)
+	for (int64_t zy = r0; zy < r1; ++zy) {
+		int64_t z = zy / L->ny, y = zy % L->ny;
+		for (int64_t x = 0; x < L->nx; ++x)
+			if (L->info[x + L->nx * zy] > 0u) KO(stream_cell)(L, x, y, z, old, nw);
 	}
 	return 0;
 }

@@ -55,6 +55,8 @@ def lib():
         L.ko_get_macros.argtypes = [vp, vp, vp]
         L.ko_run.argtypes = [vp, vp, u64]
         L.ko_run.restype = C.c_int
+        L.ko_run_rows.argtypes = [vp, vp, i64, i64]
+        L.ko_run_rows.restype = C.c_int
         L.ko_time_step.argtypes = [vp]
         L.ko_time_step.restype = u64
         L.ko_equilibrium_f32.argtypes = [C.c_int, C.c_float, vp, vp]
@@ -122,6 +124,12 @@ class OracleLattice:
 
     def run(self, program, steps):
         rc = lib().ko_run(self._h, C.byref(program), steps)
+        if rc != 0:
+            raise RuntimeError("oracle: program not supported for this descriptor")
+
+    def run_rows(self, program, r0, r1):
+        """One collide+stream pass over rows [r0, r1) only (timing sample)."""
+        rc = lib().ko_run_rows(self._h, C.byref(program), r0, r1)
         if rc != 0:
             raise RuntimeError("oracle: program not supported for this descriptor")
 

@@ -1,0 +1,156 @@
+"""GPU sweep vs the reference (golden vectors) and vs the CPU oracle.
+
+Bar: KEL_ARITH_REFERENCE (the reference's rounding sequence) is bit-exact
+against the reference's own outputs; KEL_ARITH_FAST (float, fused multiply-add)
+stays within 1e-5 relative (max |diff| / max |ref|) on populations, density and
+velocity; FP16-shifted storage is within 1e-3 relative velocity error of FP64.
+"""
+import numpy as np
+import pytest
+
+from lbm_mirror_gb300 import capi as K
+from tests import cases
+from tests.golden import make_golden as G
+from tests.gpu_util import make_lattice, rel_err, run_gpu, with_arith
+
+pytestmark = pytest.mark.gpu
+
+FAST_TOL = 1e-5
+F32_NAMES = [n for n in G.names() if not n.endswith("_f64")]
+
+
+@pytest.mark.parametrize("name", F32_NAMES)
+def test_reference_arithmetic_bit_exact(name):
+    case, dfs, rho, vel = G.load(name)
+    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE)
+    np.testing.assert_array_equal(f, dfs)
+    np.testing.assert_array_equal(r, rho)
+    np.testing.assert_array_equal(v, vel)
+
+
+@pytest.mark.parametrize("name", F32_NAMES)
+def test_fast_arithmetic_within_1e5(name):
+    case, dfs, rho, vel = G.load(name)
+    f, r, v = run_gpu(case, K.KEL_ARITH_FAST)
+    assert rel_err(f, dfs) < FAST_TOL
+    assert rel_err(r, rho) < FAST_TOL
+    assert rel_err(v, vel) < FAST_TOL
+
+
+@pytest.mark.parametrize("chunks", [[1, 1, 1, 18], [2, 7, 12], [21]])
+def test_step_chunking_and_parity(chunks):
+    """Stepping 1, 2, 7 ... at a time (odd and even entry parities) gives the
+    same bits as one call."""
+    case, dfs, rho, vel = G.load("mixed3d_d3q19_guo")
+    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE, chunks=chunks)
+    np.testing.assert_array_equal(f, dfs)
+
+
+def test_upload_at_odd_time_step():
+    """Download at odd t, upload into a fresh lattice advanced to odd t, and
+    continue: identical to the uninterrupted run."""
+    case = G.normalise(cases.mixed_2d(K.KEL_COLL_BGK_GUO, steps=0))
+    prog = with_arith(case["program"], K.KEL_ARITH_REFERENCE)
+    a = make_lattice(case)
+    a.step(prog, 5)
+    mid = a.populations(np.float64)
+    a.step(prog, 6)
+    ref = a.populations(np.float64)
+    b = make_lattice(case)
+    b.step(prog, 5)
+    b.upload_populations(mid)
+    b.step(prog, 6)
+    np.testing.assert_array_equal(b.populations(np.float64), ref)
+
+
+@pytest.mark.parametrize("q", [9, 27])
+def test_periodic_x_matches_oracle(q):
+    if q == 9:
+        case = G.normalise(cases.mixed_2d(K.KEL_COLL_PSM_GUO, dims=(48, 20), periodic=True, steps=23))
+    else:
+        case = G.normalise(cases.mixed_3d(27, K.KEL_COLL_BGK_GUO, dims=(16, 12, 10), periodic=True, steps=15))
+    odfs, orho, ovel = cases.run_oracle(case)
+    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE)
+    np.testing.assert_array_equal(f, odfs)
+    np.testing.assert_array_equal(v, ovel)
+
+
+@pytest.mark.parametrize("nx", [5, 37, 130, 131])
+def test_ragged_widths_match_oracle(nx):
+    """Row widths that are not multiples of 4 or of a warp's 128 cells."""
+    case = G.normalise(cases.mixed_2d(K.KEL_COLL_BGK, dims=(nx, 9), steps=9, seed=7))
+    odfs, orho, ovel = cases.run_oracle(case)
+    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE)
+    np.testing.assert_array_equal(f, odfs)
+    np.testing.assert_array_equal(r, orho)
+
+
+def test_config1_full_size_bit_exact():
+    """C1 at full size: D2Q9 256x64 Poiseuille, 10,000 steps."""
+    case, dfs, rho, vel = G.load("poiseuille_256x64")
+    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE)
+    np.testing.assert_array_equal(v, vel)
+    np.testing.assert_array_equal(r, rho)
+    f2, r2, v2 = run_gpu(case, K.KEL_ARITH_FAST)
+    assert rel_err(v2, vel) < FAST_TOL
+    assert rel_err(r2, rho) < FAST_TOL
+
+
+@pytest.mark.parametrize("q", [19, 27])
+def test_fp16s_velocity_error_vs_fp64(q):
+    """FP16-shifted storage: relative L2 velocity error against the FP64 oracle
+    of the same cavity below 1e-3."""
+    case = cases.cavity_3d(q, dims=(32, 32, 32), steps=400)
+    c64 = dict(case, f64=True)
+    _, rho64, vel64 = cases.run_oracle(c64)
+    _, r16, v16 = run_gpu(case, K.KEL_ARITH_FAST, storage="fp16s")
+    err = np.linalg.norm(v16 - vel64) / np.linalg.norm(vel64)
+    assert err < 1e-3, err
+    _, r32, v32 = run_gpu(case, K.KEL_ARITH_FAST, storage="fp32")
+    assert np.linalg.norm(v32 - vel64) / np.linalg.norm(vel64) < 1e-4
+
+
+def test_closed_box_mass_conservation_and_determinism():
+    """Full-size property (C2 extents): 256^3 D3Q19 closed box, all walls
+    full-way bounce-back, walls start empty so no population ever leaves the
+    lattice.  Total mass is conserved to float accuracy and two runs give
+    identical bits."""
+    dims = (256, 256, 256)
+    case = cases.cavity_3d(19, dims=dims, steps=20)
+    d = K.program_to_dict(case["program"])
+    d["ops"][5] = dict(bc=K.KEL_BC_BOUNCE_BACK, collide=0, east=1, use_profile=0, rho=1.0, u=[0, 0, 0])
+    prog = K.program_from_dict(d)
+    rng = np.random.default_rng(5)
+    w = cases._weights(19).astype(np.float32)
+    init = w[None, :] * (1 + 0.01 * rng.standard_normal((dims[0] * dims[1] * dims[2], 19), dtype=np.float32))
+    init[case["flags"] != 2] = 0.0
+    m0 = init.sum(dtype=np.float64)
+    sums = []
+    digests = []
+    for _ in range(2):
+        lat = make_lattice(case)
+        lat.upload_populations(init)
+        lat.step(prog, 20)
+        f = lat.populations(np.float32)
+        sums.append(f.sum(dtype=np.float64))
+        digests.append(hash(f.tobytes()))
+        del f
+        lat.close()
+    assert abs(sums[0] - m0) / m0 < 1e-5
+    assert digests[0] == digests[1]
+
+
+def test_invalid_arguments_return_errors():
+    from lbm_mirror_gb300 import KelError, Lattice
+    with pytest.raises(KelError):
+        Lattice("D2Q9", (8, 8, 2))
+    with pytest.raises(KelError):
+        Lattice("D2Q9", (10, 8), periodic_x=True)
+    lat = Lattice("D3Q19", (8, 8, 8))
+    bad = K.make_program(0.8, K.KEL_COLL_BGK, {3: dict(bc=K.KEL_BC_ZOUHE_VELOCITY_X, collide=1)})
+    with pytest.raises(KelError) as e:
+        lat.step(bad, 1)
+    assert e.value.code == K.KEL_ERR_UNSUPPORTED
+    with pytest.raises(KelError):
+        lat.step(K.make_program(-1.0), 1)
+    lat.close()
