@@ -120,6 +120,7 @@ struct kel_lattice {
 	uint64_t t = 0;
 	float wshift[27];
 	bool have_ops = false;
+	uint8_t present[MAX_FLAGS] = {0}; // flag values present in the uploaded flag field
 	kel_step_program last_prog;
 	int device = 0;
 };
@@ -266,6 +267,10 @@ extern "C" int kel_upload_flags(kel_lattice *L, const uint8_t *host) {
 	const auto &D = L->desc;
 	KEL_CUDA(cudaMemcpy2DAsync(L->flags, (size_t)L->nxp, host, (size_t)D.nx, (size_t)D.nx, (size_t)(D.ny * D.nz),
 							   cudaMemcpyHostToDevice, L->stream));
+	bool seen[256] = {false};
+	for (int64_t c = 0; c < L->ncell; ++c) seen[host[c]] = true;
+	for (int fl = 0; fl < MAX_FLAGS; ++fl) L->present[fl] = seen[fl] ? 1 : 0;
+	L->have_ops = false; // re-validate the program against the new flag set
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
 	return KEL_OK;
 }
@@ -493,13 +498,16 @@ static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops
 		OpEntry &e = ops[fl];
 		if (o.bc < KEL_BC_NONE || o.bc > KEL_BC_EQUILIBRIUM)
 			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: flag %d: unknown boundary op %d", fl, o.bc);
-		if (o.bc == KEL_BC_ZOUHE_VELOCITY_X && d.Q != 9)
+		// A boundary the descriptor has no reference specialisation for is an
+		// error only where a cell carries that flag.
+		const bool used = L->present[fl] != 0;
+		if (used && o.bc == KEL_BC_ZOUHE_VELOCITY_X && d.Q != 9)
 			return fail(KEL_ERR_UNSUPPORTED, "kel_step: ZouHeVelocityX exists only for D2Q9 (boundary.hpp:759)");
-		if (o.bc == KEL_BC_ZOUHE_PRESSURE_X && d.Q == 19)
+		if (used && o.bc == KEL_BC_ZOUHE_PRESSURE_X && d.Q == 19)
 			return fail(KEL_ERR_UNSUPPORTED, "kel_step: ZouHePressureX has no D3Q19 specialisation");
-		if (o.bc == KEL_BC_ANTI_BOUNCE_BACK && d.Q != 9)
+		if (used && o.bc == KEL_BC_ANTI_BOUNCE_BACK && d.Q != 9)
 			return fail(KEL_ERR_UNSUPPORTED, "kel_step: AntiBounceBack is D2Q9 only (boundary.hpp:117)");
-		e.bc = o.bc;
+		e.bc = used ? o.bc : KEL_BC_NONE;
 		e.collide = o.collide ? 1 : 0;
 		e.east = o.east ? 1 : 0;
 		e.use_profile = o.use_profile ? 1 : 0;

@@ -150,9 +150,9 @@ struct Store<STORE_FP16S> {
 // Cell physics (one cell, populations in registers).
 
 // compute_rho_u, modules/core/c++/macroscopic.hpp:10-35
-template <class L, bool EXACT>
+template <class L, bool EXACT_UNUSED>
 __device__ __forceinline__ void moments(const float (&f)[L::Q], float &rho, float (&u)[3]) {
-	using A = Ar<EXACT>;
+	using A = Ar<true>;
 	float r = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f;
 #pragma unroll
 	for (int j = 0; j < L::Q; ++j) {
@@ -167,16 +167,9 @@ __device__ __forceinline__ void moments(const float (&f)[L::Q], float &rho, floa
 		}
 	}
 	rho = r;
-	if (EXACT) {
-		u[0] = A::div(v0, r);
-		u[1] = A::div(v1, r);
-		u[2] = L::D == 3 ? A::div(v2, r) : 0.f;
-	} else {
-		const float ir = 1.0f / r;
-		u[0] = v0 * ir;
-		u[1] = v1 * ir;
-		u[2] = L::D == 3 ? v2 * ir : 0.f;
-	}
+	u[0] = A::div(v0, r);
+	u[1] = A::div(v1, r);
+	u[2] = L::D == 3 ? A::div(v2, r) : 0.f;
 }
 
 // c_i . u with the reference's summation order (0 + u_0 c_0 + u_1 c_1 ...)
@@ -198,7 +191,7 @@ __device__ __forceinline__ float cdot(int i, const float (&u)[3]) {
 // equilibrium, modules/core/c++/equilibrium.hpp:7-48
 template <class L, bool EXACT>
 __device__ __forceinline__ void equilibrium(float rho, const float (&u)[3], float (&eq)[L::Q]) {
-	using A = Ar<EXACT>;
+	using A = Ar<true>;
 	float vv = A::mul(u[0], u[0]);
 	vv = A::add(vv, A::mul(u[1], u[1]));
 	if (L::D == 3) vv = A::add(vv, A::mul(u[2], u[2]));
@@ -206,19 +199,35 @@ __device__ __forceinline__ void equilibrium(float rho, const float (&u)[3], floa
 		const double h = __dmul_rn(1.5, (double)vv);
 #pragma unroll
 		for (int i = 0; i < L::Q; ++i) {
-			const float vcc = A::mul(cdot<L, EXACT>(i, u), 3.0f);
+			const float vcc = A::mul(cdot<L, true>(i, u), 3.0f);
 			const float wr = A::mul((float)L::w(i), rho);
 			double br = __dsub_rn(__dadd_rn(1.0, (double)vcc), h);
 			br = __dadd_rn(br, __dmul_rn((double)A::mul(vcc, vcc), 0.5));
 			eq[i] = __double2float_rn(__dmul_rn((double)wr, br));
 		}
 	} else {
-		const float a0 = 1.0f - 1.5f * vv;
+		// Float-float evaluation of w rho (1 + vcc - 1.5 vv + vcc^2/2) with the
+		// reference's float sub-terms (vcc, vcc^2, w rho) and a single final
+		// rounding: the correctly rounded value of the expression the reference
+		// evaluates in double, without the FP64 pipe.
+		const float h_hi = __fmul_rn(1.5f, vv);
+		const float h_lo = __fmaf_rn(1.5f, vv, -h_hi);
 #pragma unroll
 		for (int i = 0; i < L::Q; ++i) {
-			const float vcc = 3.0f * cdot<L, false>(i, u);
-			const float wr = (float)L::w(i) * rho;
-			eq[i] = wr * (a0 + vcc * (1.0f + 0.5f * vcc));
+			const float vcc = __fmul_rn(3.0f, cdot<L, true>(i, u));
+			const float ht = __fmul_rn(0.5f, __fmul_rn(vcc, vcc));
+			const float s1 = __fadd_rn(vcc, ht); // |vcc| >= |ht|: Fast2Sum
+			const float e1 = __fsub_rn(ht, __fsub_rn(s1, vcc));
+			const float s2 = __fsub_rn(s1, h_hi); // TwoSum(s1, -h_hi)
+			const float bb = __fsub_rn(s2, s1);
+			const float e2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, bb)), __fsub_rn(-h_hi, bb));
+			const float d_lo = __fsub_rn(__fadd_rn(e1, e2), h_lo);
+			const float wr = __fmul_rn((float)L::w(i), rho);
+			const float q_hi = __fmul_rn(wr, s2);
+			const float q_err = __fmaf_rn(wr, s2, -q_hi);
+			const float t_hi = __fadd_rn(wr, q_hi); // |wr| >= |q_hi|: Fast2Sum
+			const float t_lo = __fsub_rn(q_hi, __fsub_rn(t_hi, wr));
+			eq[i] = __fadd_rn(t_hi, __fadd_rn(__fmaf_rn(wr, d_lo, q_err), t_lo));
 		}
 	}
 }
@@ -226,8 +235,8 @@ __device__ __forceinline__ void equilibrium(float rho, const float (&u)[3], floa
 // Guo forcing term F_i, modules/core/c++/collision.hpp:170-196
 template <class L, bool EXACT>
 __device__ __forceinline__ float guo_term(int i, const float (&u)[3], const float (&F)[3]) {
-	using A = Ar<EXACT>;
-	const float s = A::mul(A::mul(cdot<L, EXACT>(i, u), 3.0f), 3.0f);
+	using A = Ar<true>;
+	const float s = A::mul(A::mul(cdot<L, true>(i, u), 3.0f), 3.0f);
 	float proj = 0.f;
 #pragma unroll
 	for (int k = 0; k < L::D; ++k) {
@@ -242,7 +251,7 @@ __device__ __forceinline__ float guo_term(int i, const float (&u)[3], const floa
 // D2Q9 ZouHePressureX<Dir>, modules/core/c++/boundary.hpp:186-226
 template <bool EXACT>
 __device__ __forceinline__ void zouhe_pressure_d2q9(float (&f)[9], bool east, float rs) {
-	using A = Ar<EXACT>;
+	using A = Ar<true>;
 	const float c23 = (float)(2.0 / 3.0), c16 = (float)(1.0 / 6.0);
 	if (east) {
 		const float S = A::add(A::add(A::add(f[0], f[3]), f[4]), A::mul(A::add(A::add(f[1], f[5]), f[7]), 2.f));
@@ -262,7 +271,7 @@ __device__ __forceinline__ void zouhe_pressure_d2q9(float (&f)[9], bool east, fl
 // D2Q9 ZouHeVelocityX<East>, modules/core/c++/boundary.hpp:775-802
 template <bool EXACT>
 __device__ __forceinline__ void zouhe_velocity_d2q9(float (&f)[9], bool east, float ux, float uy) {
-	using A = Ar<EXACT>;
+	using A = Ar<true>;
 	const float c23 = (float)(2.0 / 3.0), c16 = (float)(1.0 / 6.0);
 	const float ds = east ? A::add(A::add(f[1], f[5]), f[7]) : A::add(A::add(f[2], f[6]), f[8]);
 	const float rho = A::div(A::add(A::add(A::add(f[0], f[4]), f[3]), A::mul(ds, 2.f)), A::add(ux, 1.0f));
@@ -282,7 +291,7 @@ __device__ __forceinline__ void zouhe_velocity_d2q9(float (&f)[9], bool east, fl
 // D3Q27 ZouHePressureX<East>, modules/core/c++/boundary.hpp:229-756
 template <bool EXACT>
 __device__ __forceinline__ void zouhe_pressure_d3q27(float (&f)[27], bool east, float rs) {
-	using A = Ar<EXACT>;
+	using A = Ar<true>;
 	const float a = (float)(4.0 / 9.0), b = (float)(1.0 / 9.0), e = (float)(1.0 / 36.0);
 	float S = f[0];
 	S = A::add(S, f[3]);
@@ -350,7 +359,7 @@ __device__ __forceinline__ void zouhe_pressure_d3q27(float (&f)[27], bool east, 
 template <class L, int COLL, bool EXACT>
 __device__ __forceinline__ void collide(float (&f)[L::Q], const SweepParams &p, float por, const float (&Fc)[3],
 										float &rho, float (&u)[3]) {
-	using A = Ar<EXACT>;
+	using A = Ar<true>;
 	moments<L, EXACT>(f, rho, u);
 	float eq[L::Q];
 	equilibrium<L, EXACT>(rho, u, eq);
@@ -361,7 +370,8 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], const SweepParams &p, 
 	}
 	if (COLL == COLL_BGK) {
 #pragma unroll
-		for (int i = 0; i < L::Q; ++i) f[i] = A::add(f[i], A::mul(p.omega, A::sub(eq[i], f[i])));
+		for (int i = 0; i < L::Q; ++i)
+			f[i] = EXACT ? A::add(f[i], A::mul(p.omega, A::sub(eq[i], f[i]))) : __fmaf_rn(p.omega, A::sub(eq[i], f[i]), f[i]);
 	} else if (COLL == COLL_BGK_GUO) {
 #pragma unroll
 		for (int i = 0; i < L::Q; ++i) {
@@ -388,7 +398,7 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], const SweepParams &p, 
 template <class L, int COLL, bool EXACT>
 __device__ __forceinline__ bool cell_update(float (&f)[L::Q], int flag, int y, const SweepParams &p, float por,
 											const float (&Fc)[3], float &rho, float (&u)[3]) {
-	using A = Ar<EXACT>;
+	using A = Ar<true>;
 	if (flag == 0) { // outside the lattice: what the zero ghost ring supplies
 #pragma unroll
 		for (int i = 0; i < L::Q; ++i) f[i] = 0.f;

@@ -48,6 +48,16 @@ def run_gpu(case, arithmetic=K.KEL_ARITH_REFERENCE, storage="fp32", chunks=None)
     return f, rho.astype(np.float64), vel.astype(np.float64)
 
 
+def rel_l2(a, b):
+    """||a - b||_2 / ||b||_2: the field comparison of the reference's own
+    tooling (scripts/python/csv_l2_norm.py prints ||a - b||_2)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.linalg.norm(b)
+    num = np.linalg.norm(a - b)
+    return 0.0 if num == 0 else num / max(den, 1e-300)
+
+
 def rel_err(a, b):
     """max |a - b| / max |b| (0 when both vanish)."""
     a = np.asarray(a, dtype=np.float64)

