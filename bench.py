@@ -193,6 +193,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="d3q19_cavity_256", choices=sorted(WORKLOADS))
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16s"])
+    ap.add_argument("--cpt", type=int, default=0, help="cells per thread of the sweep (0: library default)")
+    ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--e2e-iters", type=int, default=3)
     ap.add_argument("--e2e-lbm-steps", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -226,6 +228,9 @@ def main():
     ncell = int(np.prod(dims))
     stream = torch.cuda.Stream()
     lat = Lattice(QNAME[q], dims, storage=args.storage, stream=stream.cuda_stream)
+    if args.cpt:
+        lat.set_launch(args.cpt, args.block)
+    cpt, block = lat.launch()
     lat.upload_flags(case["flags"])
     if case["profile"] is not None:
         lat.upload_inlet_profile(case["profile"])
@@ -300,7 +305,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": args.workload, "descriptor": f"D{D}Q{Q}", "dims": list(dims), "cells": ncell,
                    "storage": args.storage, "tau": float(prog.tau), "collision": "BGK", "arithmetic": "fast",
-                   "scheme": "AA in-place, SoA", "l2": "populations 1.27 GB >> 129 MB L2, no flush needed"
+                   "scheme": "AA in-place, SoA", "cells_per_thread": cpt, "block": block, "l2": "populations 1.27 GB >> 129 MB L2, no flush needed"
                    if ncell * Q * 4 > 4e8 else "working set smaller than L2",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -50,8 +50,12 @@ extern "C" {
 /* ---- lattice creation flags -------------------------------------------- */
 #define KEL_LATTICE_PERIODIC_X 1u /* x wraps (ghost columns copied from the opposite side) */
 
-/* ---- per-flag boundary operation (the reference drivers' switch(info)) - */
-#define KEL_BC_NONE 0              /* no collide, no stream; reads as the zero ghost ring */
+/* ---- per-flag boundary operation (the reference drivers' switch(info)) - *
+ * Flag value 0 is the drivers' `case 0u: break;`: the cell is neither
+ * collided nor streamed, and its neighbours read zero from it, as from the
+ * ghost ring.  Flag values >= KEL_MAX_FLAGS take the `default: break;` path
+ * (no boundary step, no collision, streamed). */
+#define KEL_BC_NONE 0              /* no boundary step (collide if .collide) */
 #define KEL_BC_BOUNCE_BACK 1       /* cmpt::BounceBack, full-way (boundary.hpp:32-76) */
 #define KEL_BC_FLUID 2             /* no boundary step; collide if .collide */
 #define KEL_BC_ZOUHE_VELOCITY_X 3  /* cmpt::ZouHeVelocityX<east> D2Q9 (boundary.hpp:759-805) */
@@ -67,8 +71,8 @@ extern "C" {
 #define KEL_COLL_PSM_GUO 3 /* cmpt::Psm followed by the BGKGuo forcing term */
 
 /* ---- arithmetic mode of the sweep -------------------------------------- */
-#define KEL_ARITH_FAST 0      /* float throughout, contractions allowed */
-#define KEL_ARITH_REFERENCE 1 /* the reference's rounding sequence (double equilibrium bracket) */
+#define KEL_ARITH_FAST 0      /* float-float equilibrium bracket, fused BGK relaxation */
+#define KEL_ARITH_REFERENCE 1 /* the reference's rounding sequence (double equilibrium bracket): bit-exact */
 
 #define KEL_MAX_FLAGS 8
 
@@ -141,6 +145,74 @@ int kel_upload_inlet_profile(kel_lattice *lat, const double *host_ux, int64_t n)
  * parallel_for (e.g. examples/poiseulle_2d_gpu/poiseulle_2d_gpu.cpp:169-224)
  * followed by the Stream parallel_for (:384-399), n_steps times. */
 int kel_step(kel_lattice *lat, const kel_step_program *prog, uint64_t n_steps, uint32_t step_flags);
+
+/* ---- particles: spheres (3D) / discs (2D) coupled by PSM -------------- */
+
+/* Solid fraction used by the couple pass. */
+#define KEL_POROSITY_RAMP 0    /* sin^2 ramp of width eps around R (particle/porosity.hpp:56-89) */
+#define KEL_POROSITY_SUBCELL 1 /* 4^D sub-cell point sampling over the cell [x-1/2, x+1/2]^D */
+
+/* One rigid body, the fields of sch::ParticleRigidBody + collision radius
+ * (particle/schema.hpp:51-115).  2D: rotation, torque and their derivatives
+ * use component [0]. */
+typedef struct kel_particle_state {
+	double position[3];
+	double position_old[3];
+	double rotation[3];
+	double rotation_old[3];
+	double acceleration[3];
+	double angular_acceleration[3];
+	double force[3];  /* accumulator, zeroed by kel_particles_reset */
+	double torque[3]; /* accumulator */
+	double mass;
+	double inertia;
+	double radius;
+	double density;
+} kel_particle_state;
+
+typedef struct kel_particle_params {
+	int32_t porosity_mode; /* KEL_POROSITY_* */
+	int32_t sub_steps;     /* Verlet sub-steps (0 acts as 1; the gather divides by the raw value) */
+	double eps;            /* ramp width (the reference's gathers use 1.5) */
+	double k_n, zeta_n, gamma_t, mu; /* dem_params (particle/contact.hpp:36-61) */
+	double body_acceleration[3];     /* ParticleIntegrate(g) (particle/integrate.hpp:263-296) */
+	uint32_t wall_axes;    /* DEM box walls at 0 and the extent on these axes (bit a = axis a) */
+	uint32_t reserved;
+} kel_particle_params;
+
+typedef struct kel_particles kel_particles;
+
+/* A set of `count` bodies living on `lat` (the lattice must outlive it). */
+int kel_particles_create(kel_lattice *lat, int32_t count, kel_particles **out);
+int kel_particles_destroy(kel_particles *ps);
+int kel_particles_upload(kel_particles *ps, const kel_particle_state *host);
+int kel_particles_download(kel_particles *ps, kel_particle_state *host);
+/* ParticleForceReset (particle/integrate.hpp:195-261): force = torque = 0. */
+int kel_particles_reset(kel_particles *ps);
+/* PsmReset + ParticleFluidCouple (psm.hpp:20-32, particle/couple.hpp:26-105):
+ * porosity of every cell = product over bodies of their solid-fraction
+ * complement. */
+int kel_particles_couple(kel_particles *ps, const kel_particle_params *prm);
+/* PsmOneParticleGather (psm.hpp:95-446) for every body at once: momentum
+ * exchange over the body's AABB, force -= sum of cell forces and
+ * torque -= sum (x - X) x cell force, both accumulated in FP64.  When
+ * `host_cell_force` is not NULL it receives the per-cell force field
+ * (N*D floats, zero outside the bodies). */
+int kel_particles_gather(kel_particles *ps, const kel_particle_params *prm, float *host_cell_force);
+/* ParticleContact (particle/contact.hpp:466-567): pair + box-wall DEM. */
+int kel_particles_contact(kel_particles *ps, const kel_particle_params *prm);
+/* ParticleIntegrate (particle/integrate.hpp:45-83,263-296): position Verlet. */
+int kel_particles_integrate(kel_particles *ps, const kel_particle_params *prm);
+/* One coupled time step, n times: reset, couple, gather, contact, integrate,
+ * then the sweep (examples/moving_poiseulle_particles_2d_psm_gpu/sim.cpp:176-260). */
+int kel_particles_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
+					   uint64_t n_steps, uint32_t step_flags);
+
+/* Launch shape of the sweep: cells per thread (1: 32-bit accesses, one cell;
+ * 4: 128-bit accesses, four consecutive cells) and threads per block (64, 128
+ * or 256).  Results do not depend on it. */
+int kel_lattice_set_launch(kel_lattice *lat, int32_t cells_per_thread, int32_t block_threads);
+int kel_lattice_get_launch(const kel_lattice *lat, int32_t *cells_per_thread, int32_t *block_threads);
 
 /* Synchronise the lattice's stream. */
 int kel_lattice_synchronize(kel_lattice *lat);

@@ -28,6 +28,11 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr
                      "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + os.path.join(ROOT, "include")]
 
 
+# Per-file extra flags: the particle kernels must not fuse multiply-adds, so
+# their FP64 rigid-body arithmetic rounds like the reference's C++.
+EXTRA_FLAGS = {"particles.cu": ["-fmad=false"]}
+
+
 def nvcc():
     p = shutil.which("nvcc")
     if p:
@@ -52,7 +57,7 @@ def _stale(target, sources):
 def _compile(src, force):
     obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
     if force or _stale(obj, [src] + _deps()):
-        cmd = [nvcc()] + NVCC_FLAGS + ["-c", src, "-o", obj + ".tmp"]
+        cmd = [nvcc()] + NVCC_FLAGS + EXTRA_FLAGS.get(os.path.basename(src), []) + ["-c", src, "-o", obj + ".tmp"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")

@@ -128,6 +128,67 @@ def program_from_dict(d):
                         d["global_force"], d.get("arithmetic", KEL_ARITH_FAST))
 
 
+KEL_POROSITY_RAMP, KEL_POROSITY_SUBCELL = 0, 1
+
+
+class ParticleState(C.Structure):
+    """kel_particle_state: 28 doubles (particle/schema.hpp:51-115 + radius)."""
+    _fields_ = [
+        ("position", C.c_double * 3),
+        ("position_old", C.c_double * 3),
+        ("rotation", C.c_double * 3),
+        ("rotation_old", C.c_double * 3),
+        ("acceleration", C.c_double * 3),
+        ("angular_acceleration", C.c_double * 3),
+        ("force", C.c_double * 3),
+        ("torque", C.c_double * 3),
+        ("mass", C.c_double),
+        ("inertia", C.c_double),
+        ("radius", C.c_double),
+        ("density", C.c_double),
+    ]
+
+
+class ParticleParams(C.Structure):
+    _fields_ = [
+        ("porosity_mode", C.c_int32),
+        ("sub_steps", C.c_int32),
+        ("eps", C.c_double),
+        ("k_n", C.c_double),
+        ("zeta_n", C.c_double),
+        ("gamma_t", C.c_double),
+        ("mu", C.c_double),
+        ("body_acceleration", C.c_double * 3),
+        ("wall_axes", C.c_uint32),
+        ("reserved", C.c_uint32),
+    ]
+
+
+def make_particle_params(porosity_mode=KEL_POROSITY_RAMP, sub_steps=1, eps=1.5, k_n=1.0, zeta_n=0.3, gamma_t=0.0,
+                         mu=0.0, body_acceleration=(0.0, 0.0, 0.0), wall_axes=0):
+    p = ParticleParams()
+    p.porosity_mode, p.sub_steps, p.eps = porosity_mode, sub_steps, eps
+    p.k_n, p.zeta_n, p.gamma_t, p.mu = k_n, zeta_n, gamma_t, mu
+    for k in range(3):
+        p.body_acceleration[k] = body_acceleration[k] if k < len(body_acceleration) else 0.0
+    p.wall_axes = wall_axes
+    return p
+
+
+def states_to_array(states):
+    """ctypes array of ParticleState -> (P, 28) float64 numpy array (copy)."""
+    import numpy as np
+    return np.frombuffer(bytes(states), dtype=np.float64).reshape(len(states), 28).copy()
+
+
+def states_from_array(a):
+    import numpy as np
+    a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1, 28)
+    arr = (ParticleState * a.shape[0])()
+    C.memmove(arr, a.ctypes.data, a.nbytes)
+    return arr
+
+
 _lib = None
 
 
@@ -157,6 +218,18 @@ def load_library(path: str | None = None):
         "kel_upload_inlet_profile": ([vp, vp, i64], C.c_int),
         "kel_step": ([vp, C.POINTER(StepProgram), u64, u32], C.c_int),
         "kel_lattice_synchronize": ([vp], C.c_int),
+        "kel_lattice_set_launch": ([vp, i32, i32], C.c_int),
+        "kel_lattice_get_launch": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
+        "kel_particles_create": ([vp, i32, C.POINTER(vp)], C.c_int),
+        "kel_particles_destroy": ([vp], C.c_int),
+        "kel_particles_upload": ([vp, vp], C.c_int),
+        "kel_particles_download": ([vp, vp], C.c_int),
+        "kel_particles_reset": ([vp], C.c_int),
+        "kel_particles_couple": ([vp, C.POINTER(ParticleParams)], C.c_int),
+        "kel_particles_gather": ([vp, C.POINTER(ParticleParams), vp], C.c_int),
+        "kel_particles_contact": ([vp, C.POINTER(ParticleParams)], C.c_int),
+        "kel_particles_integrate": ([vp, C.POINTER(ParticleParams)], C.c_int),
+        "kel_particles_step": ([vp, C.POINTER(ParticleParams), C.POINTER(StepProgram), u64, u32], C.c_int),
         "kel_last_error_string": ([], C.c_char_p),
         "kel_version": ([], C.c_char_p),
     }

@@ -14,9 +14,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/kel_lbm_cuda.h"
-#include "descriptors.cuh"
-#include "sweep.cuh"
+#include "lattice_internal.cuh"
 
 using namespace kel::gb;
 
@@ -32,7 +30,9 @@ cudaError_t launch_sweep(const SweepParams &p, int storage, bool odd, int coll, 
 
 static thread_local std::string g_err;
 
-static int fail(int code, const char *fmt, ...) {
+namespace kel {
+namespace gb {
+int fail(int code, const char *fmt, ...) {
 	char buf[512];
 	va_list ap;
 	va_start(ap, fmt);
@@ -41,27 +41,14 @@ static int fail(int code, const char *fmt, ...) {
 	g_err = buf;
 	return code;
 }
-
-#define KEL_CUDA(call)                                                                             \
-	do {                                                                                           \
-		cudaError_t e__ = (call);                                                                  \
-		if (e__ != cudaSuccess)                                                                    \
-			return fail(e__ == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA,   \
-						"%s: %s (%s:%d)", #call, cudaGetErrorString(e__), __FILE__, __LINE__);      \
-	} while (0)
+} // namespace gb
+} // namespace kel
 
 extern "C" const char *kel_last_error_string(void) { return g_err.c_str(); }
 extern "C" const char *kel_version(void) { return "kel-lbm-gb300 0.1 (sm_103a)"; }
 
 // ---------------------------------------------------------------------------
 // descriptor tables on the host
-
-struct HostDesc {
-	int D = 0, Q = 0;
-	int c[27][3];
-	int opp[27];
-	double w[27];
-};
 
 template <class L>
 static HostDesc host_desc() {
@@ -101,30 +88,6 @@ static void host_equilibrium(const HostDesc &d, float rho, const float *u, float
 	}
 }
 
-// ---------------------------------------------------------------------------
-// lattice
-
-struct kel_lattice {
-	kel_lattice_desc desc;
-	HostDesc d;
-	int nxp = 0, nq = 0, wpr = 0;
-	int64_t plane = 0, ncell = 0;
-	size_t elem = 4;
-	void *f = nullptr;
-	uint8_t *flags = nullptr;
-	float *rho = nullptr, *u = nullptr, *por = nullptr, *force = nullptr, *profile = nullptr;
-	OpEntry *ops = nullptr;
-	void *staging = nullptr;
-	size_t staging_bytes = 0;
-	cudaStream_t stream = nullptr;
-	uint64_t t = 0;
-	float wshift[27];
-	bool have_ops = false;
-	uint8_t present[MAX_FLAGS] = {0}; // flag values present in the uploaded flag field
-	kel_step_program last_prog;
-	int device = 0;
-};
-
 __global__ void k_fill_f32(float *p, int64_t n, float v) {
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -136,7 +99,7 @@ __global__ void k_fill_pop(void *f, int64_t plane, int storage, float v, float s
 	}
 }
 
-static int grid_for(int64_t n) {
+int kel::gb::grid_for(int64_t n) {
 	int64_t b = (n + 255) / 256;
 	if (b > 152 * 64) b = 152 * 64;
 	if (b < 1) b = 1;
@@ -153,7 +116,7 @@ static int ensure_staging(kel_lattice *L, size_t bytes) {
 	return KEL_OK;
 }
 
-static int ensure_field(kel_lattice *L, float **ptr, int64_t count, float init) {
+int kel::gb::ensure_field(kel_lattice *L, float **ptr, int64_t count, float init) {
 	if (*ptr) return KEL_OK;
 	KEL_CUDA(cudaMalloc(ptr, count * sizeof(float)));
 	k_fill_f32<<<grid_for(count), 256, 0, L->stream>>>(*ptr, count, init);
@@ -433,6 +396,10 @@ static int field_io(kel_lattice *L, float *dev, float *host_out, const float *ho
 	return KEL_OK;
 }
 
+int kel::gb::field_to_host(kel_lattice *L, const float *dev, float *host, int comps) {
+	return field_io(L, const_cast<float *>(dev), host, nullptr, comps);
+}
+
 extern "C" int kel_download_macros(kel_lattice *L, float *host_rho, float *host_u) {
 	if (!L || (!host_rho && !host_u)) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_download_macros: null argument");
 	int rc;
@@ -525,6 +492,39 @@ static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops
 	return KEL_OK;
 }
 
+static cudaError_t launch_one(const kel_lattice *L, const SweepParams &p, int coll, bool exact, bool odd) {
+	switch (L->d.Q) {
+	case 9: return launch_sweep<D2Q9>(p, L->desc.storage, odd, coll, exact, L->stream);
+	case 19: return launch_sweep<D3Q19>(p, L->desc.storage, odd, coll, exact, L->stream);
+	default: return launch_sweep<D3Q27>(p, L->desc.storage, odd, coll, exact, L->stream);
+	}
+}
+
+static bool launch_ok(const kel_lattice *L, int cpt, int block) {
+	if (cpt != 1 && cpt != 4) return false;
+	if (block != 64 && block != 128 && block != 256) return false;
+	if (cpt == 1 && (L->desc.ny > 65535 || L->desc.nz > 65535)) return false;
+	return true;
+}
+
+extern "C" int kel_lattice_set_launch(kel_lattice *L, int32_t cells_per_thread, int32_t block_threads) {
+	if (!L) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_set_launch: null lattice");
+	if (!launch_ok(L, cells_per_thread, block_threads))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_set_launch: unsupported launch %d cells x %d threads",
+					cells_per_thread, block_threads);
+	L->cpt = cells_per_thread;
+	L->block = block_threads;
+	L->tuned = true;
+	return KEL_OK;
+}
+
+extern "C" int kel_lattice_get_launch(const kel_lattice *L, int32_t *cells_per_thread, int32_t *block_threads) {
+	if (!L || !cells_per_thread || !block_threads) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_get_launch: null");
+	*cells_per_thread = L->cpt;
+	*block_threads = L->block;
+	return KEL_OK;
+}
+
 extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_steps, uint32_t step_flags) {
 	if (!L || !P) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: null argument");
 	if (step_flags & ~(KEL_STEP_WRITE_MACROS | KEL_STEP_ALL_MACROS))
@@ -565,16 +565,13 @@ extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_st
 	p.guo_scale = 1.0f - 0.5f * p.omega;
 	for (int k = 0; k < 3; ++k) p.g[k] = (float)P->global_force[k];
 	for (int i = 0; i < 27; ++i) p.wshift[i] = L->wshift[i];
+	p.cpt = L->cpt;
+	p.block = L->block;
 	const bool exact = P->arithmetic == KEL_ARITH_REFERENCE;
 	for (uint64_t s = 0; s < n_steps; ++s) {
 		p.write_macros = (step_flags & KEL_STEP_ALL_MACROS) || ((step_flags & KEL_STEP_WRITE_MACROS) && s + 1 == n_steps);
 		const bool odd = (L->t & 1u) != 0;
-		cudaError_t e;
-		switch (L->d.Q) {
-		case 9: e = launch_sweep<D2Q9>(p, L->desc.storage, odd, P->collision, exact, L->stream); break;
-		case 19: e = launch_sweep<D3Q19>(p, L->desc.storage, odd, P->collision, exact, L->stream); break;
-		default: e = launch_sweep<D3Q27>(p, L->desc.storage, odd, P->collision, exact, L->stream); break;
-		}
+		cudaError_t e = launch_one(L, p, P->collision, exact, odd);
 		if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_step: launch failed: %s", cudaGetErrorString(e));
 		L->t += 1;
 	}

@@ -1,0 +1,64 @@
+// Internal state of the C ABI objects, shared by the translation units that
+// implement include/kel_lbm_cuda.h (lattice.cu, particles.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "../../include/kel_lbm_cuda.h"
+#include "descriptors.cuh"
+#include "sweep.cuh"
+
+namespace kel {
+namespace gb {
+
+int fail(int code, const char *fmt, ...);
+
+#define KEL_CUDA(call)                                                                             \
+	do {                                                                                           \
+		cudaError_t e__ = (call);                                                                  \
+		if (e__ != cudaSuccess)                                                                    \
+			return ::kel::gb::fail(e__ == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA, \
+								   "%s: %s (%s:%d)", #call, cudaGetErrorString(e__), __FILE__, __LINE__); \
+	} while (0)
+
+struct HostDesc {
+	int D = 0, Q = 0;
+	int c[27][3];
+	int opp[27];
+	double w[27];
+};
+
+int grid_for(int64_t n);
+int ensure_field(kel_lattice *L, float **ptr, int64_t count, float init);
+// Copy `comps` device planes (padded plane layout) to host AoS (N*comps).
+int field_to_host(kel_lattice *L, const float *dev, float *host, int comps);
+
+} // namespace gb
+} // namespace kel
+
+struct kel_lattice {
+	kel_lattice_desc desc;
+	kel::gb::HostDesc d;
+	int nxp = 0, nq = 0, wpr = 0;
+	int64_t plane = 0, ncell = 0;
+	size_t elem = 4;
+	void *f = nullptr;
+	uint8_t *flags = nullptr;
+	float *rho = nullptr, *u = nullptr, *por = nullptr, *force = nullptr, *profile = nullptr;
+	kel::gb::OpEntry *ops = nullptr;
+	void *staging = nullptr;
+	size_t staging_bytes = 0;
+	cudaStream_t stream = nullptr;
+	uint64_t t = 0;
+	float wshift[27];
+	bool have_ops = false;
+	uint8_t present[kel::gb::MAX_FLAGS] = {0}; // flag values present in the uploaded flag field
+	kel_step_program last_prog;
+	int device = 0;
+	int cpt = 1;      // cells per thread of the sweep launch (1 or 4)
+	int block = 256;  // threads per block of the sweep launch
+	bool tuned = false;
+};

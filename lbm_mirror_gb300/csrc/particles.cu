@@ -1,0 +1,670 @@
+// Particle coupling and rigid-body kernels (C ABI kel_particles_*).
+//
+// Reference path (keldu/lbm_mirror), per time step of
+// examples/moving_poiseulle_particles_2d_psm_gpu/sim.cpp:176-224:
+//   PsmReset + porosity stamp   psm.hpp:20-32, particle/porosity.hpp:56-89
+//   PsmOneParticleGather        psm.hpp:95-446 (one work-item per particle,
+//                               a serial loop over its AABB)
+//   ParticleContact             particle/contact.hpp:466-567 (brute-force pairs)
+//   ParticleIntegrate           particle/integrate.hpp:45-83,263-296
+// GB300 shape:
+//   couple     one thread per cell; each 32x8 tile first culls the bodies
+//              whose AABB touches it (in index order), then every cell takes
+//              the product of their solid-fraction complements (race free,
+//              order fixed);
+//   gather     one block per body, cells of its AABB spread over the block,
+//              FP64 force/torque per thread, then a fixed-order warp-shuffle +
+//              shared-memory reduction (deterministic);
+//   contact    one thread per body over all other bodies, FP64;
+//   integrate  one thread per body, FP64 position Verlet.
+// This file is compiled with -fmad=false: the FP64 contact/integrate
+// arithmetic and the float momentum-exchange arithmetic round exactly like
+// the reference's (unfused) C++.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+
+#include "lattice_internal.cuh"
+
+using namespace kel::gb;
+
+struct kel_particles {
+	kel_lattice *lat = nullptr;
+	int n = 0;
+	kel_particle_state *d = nullptr; // device copy of the bodies
+	float *cell_force = nullptr;     // D planes, allocated on first request
+};
+
+namespace {
+
+constexpr double PI_D = 3.14159265358979323846;
+
+struct PView {
+	const void *f;
+	int storage;
+	int64_t plane;
+	int nx, nxp, ny, nz, D, Q;
+	int odd, periodic;
+	float *por;
+	float *cell_force;
+	float wshift[27];
+};
+
+// ---- geometry shared by couple and gather -----------------------------------
+
+// aabb.hpp:41-84: [a, b) per axis.  Sub-cell mode widens to every cell the
+// body can touch; periodic x leaves the x range unclamped (cells wrap).
+__host__ __device__ inline void body_aabb(int D, const kel_particle_state &p, int nx, int ny, int nz, int periodic,
+										  int subcell, int64_t *a, int64_t *b) {
+	const int64_t ext[3] = {nx, ny, nz};
+	for (int k = 0; k < 3; ++k) {
+		a[k] = 0;
+		b[k] = 1;
+	}
+	for (int k = 0; k < D; ++k) {
+		const double X = p.position[k], r = p.radius;
+		if (subcell) {
+			a[k] = (int64_t)floor(X - r - 0.5);
+			b[k] = (int64_t)ceil(X + r + 0.5) + 1;
+		} else {
+			a[k] = (X >= r) ? (int64_t)(X - r) : 0;
+			if (periodic && k == 0 && X < r) a[k] = (int64_t)floor(X - r);
+			b[k] = (int64_t)(X + r + 1.0);
+		}
+		if (!(periodic && k == 0)) {
+			if (a[k] < 0) a[k] = 0;
+			if (b[k] > ext[k]) b[k] = ext[k];
+		}
+	}
+}
+
+__device__ inline double rel_coord(double cell, double X, int periodic, int n) {
+	double r = cell - X;
+	if (periodic) {
+		const double L = (double)n;
+		if (r > 0.5 * L) r -= L;
+		else if (r < -0.5 * L) r += L;
+	}
+	return r;
+}
+
+// particle_porosity<T,D,1,ParticleSpheroid>::calculate (porosity.hpp:56-89)
+__device__ inline double ramp(double s, double rad, double eps) {
+	const double eps_h = eps / 2;
+	const double lo = rad - eps_h, hi = rad + eps_h;
+	if (s <= lo) return 0.0;
+	if (s >= hi) return 1.0;
+	const double inner = (PI_D / (2 * eps)) * (s - lo);
+	const double c = sin(inner);
+	return c * c;
+}
+
+// Solid fraction by 4^D point sampling of the cell [x-1/2, x+1/2]^D.
+__device__ inline double subcell_porosity(int D, const double *x, const double *X, double rad) {
+	const double r2 = rad * rad;
+	int inside = 0;
+	for (int a = 0; a < 4; ++a)
+		for (int b = 0; b < 4; ++b)
+			for (int g = 0; g < (D == 3 ? 4 : 1); ++g) {
+				const double px = x[0] + (2 * a - 3) / 8.0 - X[0];
+				const double py = x[1] + (2 * b - 3) / 8.0 - X[1];
+				const double pz = D == 3 ? x[2] + (2 * g - 3) / 8.0 - X[2] : 0.0;
+				const double d2 = px * px + py * py + pz * pz;
+				if (d2 <= r2) ++inside;
+			}
+	return 1.0 - (double)inside / (double)(D == 3 ? 64 : 16);
+}
+
+// ---- couple -------------------------------------------------------------------
+
+constexpr int TX = 32, TY = 8, TT = TX * TY;
+
+__global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state *P, int np, int mode, double eps) {
+	__shared__ int cand[TT];
+	__shared__ int warp_count[TT / 32];
+	__shared__ int ncand;
+	const int tid = threadIdx.y * TX + threadIdx.x;
+	const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z = blockIdx.z;
+	const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+	const int sub = mode == KEL_POROSITY_SUBCELL;
+	double por = 1.0;
+	for (int c0 = 0; c0 < np; c0 += TT) {
+		// cull: does body c0+tid's AABB touch this tile?  (ordered compaction)
+		bool hit = false;
+		const int pi = c0 + tid;
+		if (pi < np) {
+			int64_t a[3], b[3];
+			body_aabb(v.D, P[pi], v.nx, v.ny, v.nz, v.periodic, sub, a, b);
+			bool yz = a[1] < y0 + TY && b[1] > y0 && (v.D == 2 || (a[2] <= z && b[2] > z));
+			bool xs = a[0] < x0 + TX && b[0] > x0;
+			if (v.periodic) xs = xs || (a[0] < x0 + TX - v.nx && b[0] > x0 - v.nx) || (a[0] < x0 + TX + v.nx && b[0] > x0 + v.nx);
+			hit = yz && xs;
+		}
+		const unsigned m = __ballot_sync(0xffffffffu, hit);
+		if ((tid & 31) == 0) warp_count[tid >> 5] = __popc(m);
+		__syncthreads();
+		if (tid == 0) {
+			int s = 0;
+			for (int w = 0; w < TT / 32; ++w) {
+				const int c = warp_count[w];
+				warp_count[w] = s;
+				s += c;
+			}
+			ncand = s;
+		}
+		__syncthreads();
+		if (hit) cand[warp_count[tid >> 5] + __popc(m & ((1u << (tid & 31)) - 1u))] = pi;
+		__syncthreads();
+		if (x < v.nx && y < v.ny) {
+			for (int k = 0; k < ncand; ++k) {
+				const kel_particle_state &p = P[cand[k]];
+				int64_t a[3], b[3];
+				body_aabb(v.D, p, v.nx, v.ny, v.nz, v.periodic, sub, a, b);
+				double rel[3] = {rel_coord((double)x, p.position[0], v.periodic, v.nx), (double)y - p.position[1],
+								 v.D == 3 ? (double)z - p.position[2] : 0.0};
+				const double xi = p.position[0] + rel[0];
+				const int64_t xc = v.periodic ? (int64_t)llround(xi) : x;
+				if (xc < a[0] || xc >= b[0] || y < a[1] || y >= b[1] || (v.D == 3 && (z < a[2] || z >= b[2]))) continue;
+				double pp;
+				if (sub) {
+					const double xs[3] = {xi, (double)y, (double)z};
+					pp = subcell_porosity(v.D, xs, p.position, p.radius);
+				} else {
+					double s2 = 0.0;
+					for (int d = 0; d < v.D; ++d) s2 = s2 + rel[d] * rel[d];
+					pp = ramp(sqrt(s2), p.radius, eps);
+				}
+				por = por * pp;
+			}
+		}
+		__syncthreads();
+	}
+	if (x < v.nx && y < v.ny) v.por[((int64_t)z * v.ny + y) * v.nxp + x] = (float)por;
+}
+
+// ---- gather ---------------------------------------------------------------------
+
+// Post-stream population f_i at a lattice cell (the buffer the next collide
+// reads); outside the lattice the reference's zero ghost ring.
+template <class L, int STORE>
+__device__ inline float pop_post(const PView &v, int x, int y, int z, int i) {
+	if (v.periodic) x = x < 0 ? x + v.nx : (x >= v.nx ? x - v.nx : x);
+	if (x < 0 || x >= v.nx || y < 0 || y >= v.ny || z < 0 || z >= v.nz) return 0.f;
+	int64_t idx;
+	if (!v.odd) {
+		idx = (int64_t)i * v.plane + ((int64_t)z * v.ny + y) * v.nxp + x;
+	} else {
+		int sx = x - L::cx(i);
+		const int sy = y - L::cy(i), sz = z - L::cz(i);
+		if (v.periodic) sx = sx < 0 ? sx + v.nxp : (sx >= v.nxp ? sx - v.nxp : sx);
+		if (sx < 0 || sx >= v.nxp || sy < 0 || sy >= v.ny || sz < 0 || sz >= v.nz) return 0.f;
+		idx = (int64_t)L::opp(i) * v.plane + ((int64_t)sz * v.ny + sy) * v.nxp + sx;
+	}
+	if (STORE == STORE_FP32) return static_cast<const float *>(v.f)[idx];
+	return __half2float(static_cast<const __half *>(v.f)[idx]) + v.wshift[i];
+}
+
+constexpr int GT = 256;
+
+template <class L, int STORE>
+__global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, int steps, int mode) {
+	constexpr int D = L::D;
+	__shared__ double part[GT / 32][6];
+	kel_particle_state &p = P[blockIdx.x];
+	int64_t a[3], b[3];
+	body_aabb(D, p, v.nx, v.ny, v.nz, v.periodic, mode == KEL_POROSITY_SUBCELL, a, b);
+	const int64_t ex = b[0] - a[0], ey = b[1] - a[1], ez = D == 3 ? b[2] - a[2] : 1;
+	const int64_t ncell = (ex > 0 && ey > 0 && ez > 0) ? ex * ey * ez : 0;
+	// psm.hpp:178-184: u_p = (X - X_old) / (1 / sub_steps), raw sub_steps
+	const double ts = 1.0 / (double)steps;
+	double vp[3] = {0.0, 0.0, 0.0};
+	for (int k = 0; k < D; ++k) vp[k] = (p.position[k] - p.position_old[k]) / ts;
+	double acc[6] = {0, 0, 0, 0, 0, 0}; // force[3], torque[3] (sums of minus the cell forces)
+	for (int64_t k = threadIdx.x; k < ncell; k += GT) {
+		const int ix = (int)(a[0] + k % ex);
+		const int iy = (int)(a[1] + (k / ex) % ey);
+		const int iz = D == 3 ? (int)(a[2] + k / (ex * ey)) : 0;
+		const int x = v.periodic ? ((ix % v.nx) + v.nx) % v.nx : ix;
+		const int64_t pc = ((int64_t)iz * v.ny + iy) * v.nxp + x;
+		const float por = v.por[pc];
+		if (por >= 1.0f) continue;
+		float mom[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+		for (int i = 1; i < L::Q; ++i) {
+			double upe_d = 0.0;
+			upe_d = upe_d + (double)L::cx(i) * vp[0];
+			upe_d = upe_d + (double)L::cy(i) * vp[1];
+			if (D == 3) upe_d = upe_d + (double)L::cz(i) * vp[2];
+			const float upe = (float)upe_d;
+			const float fi = pop_post<L, STORE>(v, x, iy, iz, i);
+			const float fo = pop_post<L, STORE>(v, x + L::cx(i), iy + L::cy(i), iz + L::cz(i), L::opp(i));
+			const float da = __fadd_rn(__fmul_rn(fi, __fsub_rn(1.0f, upe)), __fmul_rn(fo, __fadd_rn(1.0f, upe)));
+			mom[0] = __fadd_rn(mom[0], __fmul_rn((float)L::cx(i), da));
+			mom[1] = __fadd_rn(mom[1], __fmul_rn((float)L::cy(i), da));
+			if (D == 3) mom[2] = __fadd_rn(mom[2], __fmul_rn((float)L::cz(i), da));
+		}
+		const float flip = __fsub_rn(1.0f, por);
+		double F[3] = {0.0, 0.0, 0.0};
+		for (int d = 0; d < D; ++d) F[d] = (double)__fmul_rn(mom[d], flip);
+		if (v.cell_force)
+			for (int d = 0; d < D; ++d) v.cell_force[(int64_t)d * v.plane + pc] = (float)F[d];
+		for (int d = 0; d < D; ++d) acc[d] -= F[d];
+		const double r[3] = {rel_coord((double)x, p.position[0], v.periodic, v.nx), (double)iy - p.position[1],
+							 D == 3 ? (double)iz - p.position[2] : 0.0};
+		if (D == 2) {
+			acc[3] -= r[0] * F[1] - r[1] * F[0];
+		} else {
+			acc[3] -= r[1] * F[2] - r[2] * F[1];
+			acc[4] -= r[2] * F[0] - r[0] * F[2];
+			acc[5] -= r[0] * F[1] - r[1] * F[0];
+		}
+	}
+	// fixed-order reduction: warp shuffle, then warps in index order
+#pragma unroll
+	for (int q = 0; q < 6; ++q) {
+		double s = acc[q];
+		for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+		if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5][q] = s;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double tot[6] = {0, 0, 0, 0, 0, 0};
+		for (int w = 0; w < GT / 32; ++w)
+			for (int q = 0; q < 6; ++q) tot[q] += part[w][q];
+		for (int d = 0; d < D; ++d) p.force[d] = p.force[d] + tot[d];
+		for (int d = 0; d < (D == 2 ? 1 : 3); ++d) p.torque[d] = p.torque[d] + tot[3 + d];
+	}
+}
+
+// ---- DEM contact (contact.hpp) ----------------------------------------------------
+
+__device__ inline bool safe_normalize(int D, const double *in, double *out) {
+	double l2 = 0.0;
+	for (int k = 0; k < D; ++k) l2 = l2 + in[k] * in[k];
+	if (!(l2 > 0)) return false;
+	const double inv = 1.0 / sqrt(l2);
+	for (int k = 0; k < D; ++k) out[k] = in[k] * inv;
+	return true;
+}
+
+__device__ inline void surface_velocity(int D, const kel_particle_state &p, const double *r, double steps, double *v) {
+	for (int k = 0; k < D; ++k) v[k] = (p.position[k] - p.position_old[k]) * steps;
+	if (D == 2) {
+		const double om = (p.rotation[0] - p.rotation_old[0]) * steps;
+		const double t0 = -(om * r[1]), t1 = om * r[0];
+		v[0] = v[0] + t0;
+		v[1] = v[1] + t1;
+	} else {
+		double om[3];
+		for (int k = 0; k < 3; ++k) om[k] = (p.rotation[k] - p.rotation_old[k]) * steps;
+		const double t[3] = {om[1] * r[2] - om[2] * r[1], om[2] * r[0] - om[0] * r[2], om[0] * r[1] - om[1] * r[0]};
+		for (int k = 0; k < 3; ++k) v[k] = v[k] + t[k];
+	}
+}
+
+// soft_shell_response, contact.hpp:204-264
+__device__ inline void soft_shell(int D, const double *n, double depth, const double *r_self, const double *v_rel,
+								  double m_eff, const kel_particle_params &dem, double *F, double *T) {
+	const double k_n = dem.k_n, zeta = dem.zeta_n;
+	const double g_n = 2.0 * zeta * sqrt(m_eff * k_n);
+	double v_n = 0.0;
+	for (int k = 0; k < D; ++k) v_n = v_n + v_rel[k] * n[k];
+	double f_n = k_n * depth - g_n * v_n;
+	if (f_n < 0) f_n = 0;
+	double v_t[3] = {0, 0, 0}, t_hat[3] = {0, 0, 0};
+	for (int k = 0; k < D; ++k) v_t[k] = v_rel[k] - v_n * n[k];
+	const bool have_t = safe_normalize(D, v_t, t_hat);
+	double vtt = 0.0;
+	for (int k = 0; k < D; ++k) vtt = vtt + v_t[k] * v_t[k];
+	const double v_t_len = sqrt(vtt);
+	double f_t = dem.gamma_t * v_t_len;
+	const double f_t_cap = dem.mu * f_n;
+	if (f_t > f_t_cap) f_t = f_t_cap;
+	for (int k = 0; k < D; ++k) {
+		double val = f_n * n[k];
+		if (have_t) val -= f_t * t_hat[k];
+		F[k] = val;
+	}
+	if (D == 2) {
+		T[0] = r_self[0] * F[1] - r_self[1] * F[0];
+	} else {
+		T[0] = r_self[1] * F[2] - r_self[2] * F[1];
+		T[1] = r_self[2] * F[0] - r_self[0] * F[2];
+		T[2] = r_self[0] * F[1] - r_self[1] * F[0];
+	}
+}
+
+__device__ inline void pdiff(int D, const double *a, const double *b, int per, double Lx, double *d) {
+	for (int k = 0; k < D; ++k) d[k] = a[k] - b[k];
+	if (per) {
+		if (d[0] > 0.5 * Lx) d[0] -= Lx;
+		else if (d[0] < -0.5 * Lx) d[0] += Lx;
+	}
+}
+
+__global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_params prm, int nx, int ny, int nz,
+						  int periodic) {
+	const int s = blockIdx.x * blockDim.x + threadIdx.x;
+	if (s >= np) return;
+	const double steps = (double)(prm.sub_steps == 0 ? 1 : prm.sub_steps);
+	const double Lx = (double)nx;
+	const double ext[3] = {(double)nx, (double)ny, (double)nz};
+	const kel_particle_state &self = P[s];
+	double force[3] = {self.force[0], self.force[1], self.force[2]};
+	double torque0 = self.torque[0];
+	for (int j = 0; j < np; ++j) {
+		if (j == s) continue;
+		const kel_particle_state &other = P[j];
+		double dd[3] = {0, 0, 0};
+		pdiff(D, self.position, other.position, periodic, Lx, dd);
+		double n2 = 0.0;
+		for (int k = 0; k < D; ++k) n2 = n2 + dd[k] * dd[k];
+		const double rl = self.radius, rr = other.radius;
+		if (!(n2 < rl * rl + rr * rr + rr * rl * 2.0)) continue;
+		const bool self_is_lo = s < j;
+		const kel_particle_state &lo = self_is_lo ? self : other;
+		const kel_particle_state &hi = self_is_lo ? other : self;
+		double d[3] = {0, 0, 0};
+		pdiff(D, lo.position, hi.position, periodic, Lx, d);
+		double len2 = 0.0;
+		for (int k = 0; k < D; ++k) len2 = len2 + d[k] * d[k];
+		const double sum_r = lo.radius + hi.radius;
+		if (!(len2 < sum_r * sum_r)) continue;
+		const double len = sqrt(len2);
+		double depth = sum_r - len;
+		const double cap = (lo.radius < hi.radius) ? lo.radius : hi.radius;
+		if (depth > cap) depth = cap;
+		double n[3] = {0, 0, 0};
+		if (!safe_normalize(D, d, n)) {
+			for (int k = 0; k < D; ++k) n[k] = 0;
+			n[0] = 1;
+		}
+		double off[3] = {0, 0, 0};
+		for (int k = 0; k < D; ++k) off[k] = n[k] * (hi.radius - depth * 0.5);
+		if (!self_is_lo)
+			for (int k = 0; k < D; ++k) n[k] = -n[k];
+		double r_s[3] = {0, 0, 0}, r_o[3] = {0, 0, 0};
+		for (int k = 0; k < D; ++k) {
+			const double pt = hi.position[k] + off[k];
+			r_s[k] = pt - self.position[k];
+			r_o[k] = pt - other.position[k];
+		}
+		if (periodic) {
+			if (r_s[0] > 0.5 * Lx) r_s[0] -= Lx; else if (r_s[0] < -0.5 * Lx) r_s[0] += Lx;
+			if (r_o[0] > 0.5 * Lx) r_o[0] -= Lx; else if (r_o[0] < -0.5 * Lx) r_o[0] += Lx;
+		}
+		double v_s[3] = {0, 0, 0}, v_o[3] = {0, 0, 0}, v_rel[3] = {0, 0, 0};
+		surface_velocity(D, self, r_s, steps, v_s);
+		surface_velocity(D, other, r_o, steps, v_o);
+		for (int k = 0; k < D; ++k) v_rel[k] = v_s[k] - v_o[k];
+		const double m_eff = (self.mass * other.mass) / (self.mass + other.mass);
+		double f[3] = {0, 0, 0}, t[3] = {0, 0, 0};
+		soft_shell(D, n, depth, r_s, v_rel, m_eff, prm, f, t);
+		for (int k = 0; k < D; ++k) force[k] = force[k] + f[k];
+		if (D == 2) torque0 = torque0 + t[0];
+	}
+	for (int ax = 0; ax < D; ++ax) {
+		if (!(prm.wall_axes & (1u << ax))) continue;
+		const double x = self.position[ax], r = self.radius, hb = ext[ax];
+		for (int side = 0; side < 2; ++side) {
+			double depth = side == 0 ? (r - x) : (x - (hb - r));
+			if (!(depth > 0)) continue;
+			if (depth > r) depth = r;
+			double n[3] = {0, 0, 0}, pt[3] = {0, 0, 0};
+			for (int k = 0; k < D; ++k) pt[k] = self.position[k];
+			n[ax] = side == 0 ? 1.0 : -1.0;
+			pt[ax] = side == 0 ? 0.0 : hb;
+			double r_s[3] = {0, 0, 0}, vv[3] = {0, 0, 0};
+			for (int k = 0; k < D; ++k) r_s[k] = pt[k] - self.position[k];
+			surface_velocity(D, self, r_s, steps, vv);
+			double f[3] = {0, 0, 0}, t[3] = {0, 0, 0};
+			soft_shell(D, n, depth, r_s, vv, self.mass, prm, f, t);
+			for (int k = 0; k < D; ++k) force[k] = force[k] + f[k];
+			if (D == 2) torque0 = torque0 + t[0];
+		}
+	}
+	// only this thread writes body s; the others read its position fields only
+	P[s].force[0] = force[0];
+	P[s].force[1] = force[1];
+	P[s].force[2] = force[2];
+	if (D == 2) P[s].torque[0] = torque0;
+}
+
+// integrate_particle + verlet_step_lambda (integrate.hpp:45-83, particle.hpp:171-211)
+__global__ void k_integrate(kel_particle_state *P, int np, int D, kel_particle_params prm, int nx, int periodic) {
+	const int pi = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pi >= np) return;
+	kel_particle_state q = P[pi];
+	const int steps = prm.sub_steps == 0 ? 1 : prm.sub_steps;
+	const double ts = 1.0 / (double)steps;
+	for (int k = 0; k < D; ++k) q.acceleration[k] = q.force[k] / q.mass + prm.body_acceleration[k];
+	if (D == 2) q.angular_acceleration[0] = q.torque[0] / q.inertia;
+	for (int s = 0; s < steps; ++s) {
+		const double t2 = ts * ts;
+		for (int k = 0; k < D; ++k) {
+			const double nw = q.position[k] * 2.0 - q.position_old[k] + q.acceleration[k] * t2;
+			q.position_old[k] = q.position[k];
+			q.position[k] = nw;
+		}
+		const int nr = D == 2 ? 1 : 3;
+		for (int k = 0; k < nr; ++k) {
+			const double nw = q.rotation[k] * 2.0 - q.rotation_old[k] + q.angular_acceleration[k] * t2;
+			q.rotation_old[k] = q.rotation[k];
+			q.rotation[k] = nw;
+		}
+	}
+	if (periodic) {
+		const double L = (double)nx;
+		if (q.position[0] >= L) {
+			q.position[0] -= L;
+			q.position_old[0] -= L;
+		} else if (q.position[0] < 0.0) {
+			q.position[0] += L;
+			q.position_old[0] += L;
+		}
+	}
+	P[pi] = q;
+}
+
+__global__ void k_reset(kel_particle_state *P, int np) {
+	const int pi = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pi >= np) return;
+	for (int k = 0; k < 3; ++k) {
+		P[pi].force[k] = 0.0;
+		P[pi].torque[k] = 0.0;
+	}
+}
+
+PView make_view(kel_lattice *L) {
+	PView v;
+	memset(&v, 0, sizeof(v));
+	v.f = L->f;
+	v.storage = L->desc.storage;
+	v.plane = L->plane;
+	v.nx = (int)L->desc.nx;
+	v.nxp = L->nxp;
+	v.ny = (int)L->desc.ny;
+	v.nz = (int)L->desc.nz;
+	v.D = L->d.D;
+	v.Q = L->d.Q;
+	v.odd = (int)(L->t & 1u);
+	v.periodic = (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0;
+	v.por = L->por;
+	for (int i = 0; i < 27; ++i) v.wshift[i] = L->wshift[i];
+	return v;
+}
+
+int check_params(const kel_particles *ps, const kel_particle_params *prm, const char *who) {
+	if (!ps || !prm) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: null argument", who);
+	if (prm->porosity_mode != KEL_POROSITY_RAMP && prm->porosity_mode != KEL_POROSITY_SUBCELL)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: unknown porosity mode %d", who, prm->porosity_mode);
+	if (prm->sub_steps < 0) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: negative sub_steps", who);
+	if (prm->porosity_mode == KEL_POROSITY_RAMP && !(prm->eps > 0))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: eps must be positive", who);
+	return KEL_OK;
+}
+
+} // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+extern "C" int kel_particles_create(kel_lattice *lat, int32_t count, kel_particles **out) {
+	if (!lat || !out || count < 1) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_create: bad arguments");
+	*out = nullptr;
+	kel_particles *ps = new kel_particles();
+	ps->lat = lat;
+	ps->n = count;
+	cudaError_t e = cudaMalloc(&ps->d, sizeof(kel_particle_state) * count);
+	if (e != cudaSuccess) {
+		delete ps;
+		return fail(e == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA, "kel_particles_create: %s",
+					cudaGetErrorString(e));
+	}
+	cudaMemsetAsync(ps->d, 0, sizeof(kel_particle_state) * count, lat->stream);
+	int rc = ensure_field(lat, &lat->por, lat->plane, 1.0f);
+	if (rc) {
+		cudaFree(ps->d);
+		delete ps;
+		return rc;
+	}
+	*out = ps;
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_destroy(kel_particles *ps) {
+	if (!ps) return KEL_OK;
+	cudaStreamSynchronize(ps->lat->stream);
+	cudaFree(ps->d);
+	cudaFree(ps->cell_force);
+	delete ps;
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_upload(kel_particles *ps, const kel_particle_state *host) {
+	if (!ps || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_upload: null argument");
+	KEL_CUDA(cudaMemcpyAsync(ps->d, host, sizeof(kel_particle_state) * ps->n, cudaMemcpyHostToDevice, ps->lat->stream));
+	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_download(kel_particles *ps, kel_particle_state *host) {
+	if (!ps || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_download: null argument");
+	KEL_CUDA(cudaMemcpyAsync(host, ps->d, sizeof(kel_particle_state) * ps->n, cudaMemcpyDeviceToHost, ps->lat->stream));
+	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	return KEL_OK;
+}
+
+static int particles_reset(kel_particles *ps) {
+	k_reset<<<(ps->n + 127) / 128, 128, 0, ps->lat->stream>>>(ps->d, ps->n);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+static int particles_couple(kel_particles *ps, const kel_particle_params *prm) {
+	kel_lattice *L = ps->lat;
+	PView v = make_view(L);
+	dim3 grid((unsigned)((L->desc.nx + TX - 1) / TX), (unsigned)((L->desc.ny + TY - 1) / TY), (unsigned)L->desc.nz);
+	k_couple<<<grid, dim3(TX, TY), 0, L->stream>>>(v, ps->d, ps->n, prm->porosity_mode, prm->eps);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+template <class Lc, int STORE>
+static void launch_gather(const PView &v, kel_particles *ps, int steps, int mode) {
+	k_gather<Lc, STORE><<<ps->n, GT, 0, ps->lat->stream>>>(v, ps->d, steps, mode);
+}
+
+static int particles_gather(kel_particles *ps, const kel_particle_params *prm, bool want_cell_force) {
+	kel_lattice *L = ps->lat;
+	PView v = make_view(L);
+	if (want_cell_force) {
+		if (!ps->cell_force) KEL_CUDA(cudaMalloc(&ps->cell_force, sizeof(float) * L->plane * L->d.D));
+		KEL_CUDA(cudaMemsetAsync(ps->cell_force, 0, sizeof(float) * L->plane * L->d.D, L->stream));
+		v.cell_force = ps->cell_force;
+	}
+	const bool f32 = L->desc.storage == KEL_STORAGE_FP32;
+	switch (L->d.Q) {
+	case 9: f32 ? launch_gather<D2Q9, STORE_FP32>(v, ps, prm->sub_steps, prm->porosity_mode)
+				: launch_gather<D2Q9, STORE_FP16S>(v, ps, prm->sub_steps, prm->porosity_mode); break;
+	case 19: f32 ? launch_gather<D3Q19, STORE_FP32>(v, ps, prm->sub_steps, prm->porosity_mode)
+				 : launch_gather<D3Q19, STORE_FP16S>(v, ps, prm->sub_steps, prm->porosity_mode); break;
+	default: f32 ? launch_gather<D3Q27, STORE_FP32>(v, ps, prm->sub_steps, prm->porosity_mode)
+				 : launch_gather<D3Q27, STORE_FP16S>(v, ps, prm->sub_steps, prm->porosity_mode); break;
+	}
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+static int particles_contact(kel_particles *ps, const kel_particle_params *prm) {
+	kel_lattice *L = ps->lat;
+	k_contact<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(ps->d, ps->n, L->d.D, *prm, (int)L->desc.nx, (int)L->desc.ny,
+														   (int)L->desc.nz, (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+static int particles_integrate(kel_particles *ps, const kel_particle_params *prm) {
+	kel_lattice *L = ps->lat;
+	k_integrate<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(ps->d, ps->n, L->d.D, *prm, (int)L->desc.nx,
+															 (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_reset(kel_particles *ps) {
+	if (!ps) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_reset: null argument");
+	int rc = particles_reset(ps);
+	if (rc) return rc;
+	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_couple(kel_particles *ps, const kel_particle_params *prm) {
+	int rc = check_params(ps, prm, "kel_particles_couple");
+	if (rc || (rc = particles_couple(ps, prm))) return rc;
+	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_gather(kel_particles *ps, const kel_particle_params *prm, float *host_cell_force) {
+	int rc = check_params(ps, prm, "kel_particles_gather");
+	if (rc || (rc = particles_gather(ps, prm, host_cell_force != nullptr))) return rc;
+	if (host_cell_force) {
+		kel_lattice *L = ps->lat;
+		if ((rc = field_to_host(L, ps->cell_force, host_cell_force, L->d.D))) return rc;
+	}
+	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_contact(kel_particles *ps, const kel_particle_params *prm) {
+	int rc = check_params(ps, prm, "kel_particles_contact");
+	if (rc || (rc = particles_contact(ps, prm))) return rc;
+	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_integrate(kel_particles *ps, const kel_particle_params *prm) {
+	int rc = check_params(ps, prm, "kel_particles_integrate");
+	if (rc || (rc = particles_integrate(ps, prm))) return rc;
+	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
+								  uint64_t n_steps, uint32_t step_flags) {
+	int rc = check_params(ps, prm, "kel_particles_step");
+	if (rc) return rc;
+	if (!prog) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_step: null program");
+	for (uint64_t s = 0; s < n_steps; ++s) {
+		if ((rc = particles_reset(ps)) || (rc = particles_couple(ps, prm)) || (rc = particles_gather(ps, prm, false)) ||
+			(rc = particles_contact(ps, prm)) || (rc = particles_integrate(ps, prm)))
+			return rc;
+		const uint32_t fl = (s + 1 == n_steps) ? step_flags : (step_flags & KEL_STEP_ALL_MACROS);
+		if ((rc = kel_step(ps->lat, prog, 1, fl))) return rc;
+	}
+	return KEL_OK;
+}

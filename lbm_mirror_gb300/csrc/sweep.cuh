@@ -74,6 +74,8 @@ struct SweepParams {
 	float guo_scale;  // 1 - 0.5 * omega
 	float g[3];       // global force
 	float wshift[27]; // FP16S: stored value is f - wshift[i]
+	int cpt;          // cells per thread: 4 (sweep_kernel) or 1 (sweep1_kernel)
+	int block;        // threads per block
 };
 
 // ---------------------------------------------------------------------------
@@ -630,6 +632,74 @@ __global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ Swee
 					}
 				}
 			}
+		}
+	}
+}
+
+
+// One cell per thread.  Same physics and the same AA addressing as
+// sweep_kernel, with 32-bit accesses: the x-shifted loads/stores of odd steps
+// are plain unit offsets, coalesced across the warp, and the register budget
+// (~70) leaves room for four times as many resident warps.
+// Grid: (ceil(nxp / blockDim.x), ny, nz).
+template <class L, int STORE, bool ODD, int COLL, bool EXACT>
+__global__ void __launch_bounds__(256) sweep1_kernel(const __grid_constant__ SweepParams p) {
+	using S = Store<STORE>;
+	constexpr int Q = L::Q;
+	const int x = blockIdx.x * blockDim.x + threadIdx.x;
+	if (x >= p.nxp) return;
+	const int y = blockIdx.y, z = blockIdx.z;
+	const int nxp = p.nxp;
+	const int64_t cell = (static_cast<int64_t>(z) * p.ny + y) * nxp + x;
+
+	float f[Q];
+#pragma unroll
+	for (int i = 0; i < Q; ++i) {
+		const float s = p.wshift[i];
+		if (!ODD) {
+			f[i] = S::ld1(p.f, i * p.plane + cell, s);
+		} else {
+			int sx = x - L::cx(i);
+			const int sy = y - L::cy(i), sz = z - L::cz(i);
+			if (p.periodic) sx = sx < 0 ? sx + nxp : (sx >= nxp ? sx - nxp : sx);
+			const bool in = sx >= 0 && sx < nxp && sy >= 0 && sy < p.ny && sz >= 0 && sz < p.nz;
+			f[i] = in ? S::ld1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane +
+									   (static_cast<int64_t>(sz) * p.ny + sy) * nxp + sx, s)
+					  : 0.f;
+		}
+	}
+	const int flag = p.flags[cell];
+	const float por = (COLL == COLL_PSM || COLL == COLL_PSM_GUO) ? p.por[cell] : 1.f;
+	float Fc[3] = {0.f, 0.f, 0.f};
+	if (COLL == COLL_BGK_GUO || COLL == COLL_PSM_GUO) {
+#pragma unroll
+		for (int k = 0; k < L::D; ++k) Fc[k] = p.force[k * p.plane + cell];
+	}
+	float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
+	const bool col = cell_update<L, COLL, EXACT>(f, flag, y, p, por, Fc, rho, u);
+	if (p.write_macros && col) {
+		p.rho[cell] = rho;
+#pragma unroll
+		for (int k = 0; k < L::D; ++k) p.u[k * p.plane + cell] = u[k];
+	}
+#pragma unroll
+	for (int i = 0; i < Q; ++i) {
+		const float s = p.wshift[i];
+		if (!ODD) {
+			S::st1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + cell, f[i], s);
+		} else {
+			const int64_t pb = static_cast<int64_t>(i) * p.plane;
+			// this cell's slot whose source lies outside: the ghost ring's zero
+			{
+				const int sx = x - L::cx(i), sy = y - L::cy(i), sz = z - L::cz(i);
+				const bool out_x = !p.periodic && (sx < 0 || sx >= nxp);
+				if (out_x || sy < 0 || sy >= p.ny || sz < 0 || sz >= p.nz) S::st1(p.f, pb + cell, 0.f, s);
+			}
+			int dx = x + L::cx(i);
+			const int dy = y + L::cy(i), dz = z + L::cz(i);
+			if (p.periodic) dx = dx < 0 ? dx + nxp : (dx >= nxp ? dx - nxp : dx);
+			if (dx >= 0 && dx < nxp && dy >= 0 && dy < p.ny && dz >= 0 && dz < p.nz)
+				S::st1(p.f, pb + (static_cast<int64_t>(dz) * p.ny + dy) * nxp + dx, f[i], s);
 		}
 	}
 }

@@ -12,10 +12,15 @@ namespace gb {
 
 template <class L, int STORE, bool ODD, int COLL, bool EXACT>
 static cudaError_t launch_variant(const SweepParams &p, cudaStream_t st) {
-	const int64_t threads = static_cast<int64_t>(p.ny) * p.nz * p.wpr * 32;
-	const int block = 256;
-	const int64_t blocks = (threads + block - 1) / block;
-	sweep_kernel<L, STORE, ODD, COLL, EXACT><<<static_cast<unsigned>(blocks), block, 0, st>>>(p);
+	const int block = p.block > 0 ? p.block : 256;
+	if (p.cpt == 1) {
+		dim3 grid((p.nxp + block - 1) / block, p.ny, p.nz);
+		sweep1_kernel<L, STORE, ODD, COLL, EXACT><<<grid, block, 0, st>>>(p);
+	} else {
+		const int64_t threads = static_cast<int64_t>(p.ny) * p.nz * p.wpr * 32;
+		const int64_t blocks = (threads + block - 1) / block;
+		sweep_kernel<L, STORE, ODD, COLL, EXACT><<<static_cast<unsigned>(blocks), block, 0, st>>>(p);
+	}
 	return cudaGetLastError();
 }
 

@@ -246,5 +246,71 @@ class Lattice:
         fl = (K.KEL_STEP_WRITE_MACROS if write_macros else 0) | (K.KEL_STEP_ALL_MACROS if all_macros else 0)
         _check(self.lib.kel_step(self._h, C.byref(program), n_steps, fl), self.lib)
 
+    def set_launch(self, cells_per_thread, block_threads=256):
+        _check(self.lib.kel_lattice_set_launch(self._h, cells_per_thread, block_threads), self.lib)
+
+    def launch(self):
+        a, b = C.c_int32(), C.c_int32()
+        _check(self.lib.kel_lattice_get_launch(self._h, C.byref(a), C.byref(b)), self.lib)
+        return a.value, b.value
+
     def synchronize(self):
         _check(self.lib.kel_lattice_synchronize(self._h), self.lib)
+
+
+class Particles:
+    """Rigid spheres/discs on a Lattice (C ABI kel_particles_*): PSM porosity
+    couple, FP64 momentum-exchange force/torque gather, DEM contact and
+    position-Verlet integration -- the per-particle components of the
+    reference (psm.hpp, particle/contact.hpp, particle/integrate.hpp)."""
+
+    def __init__(self, lattice: Lattice, states):
+        self.lat = lattice
+        self.lib = lattice.lib
+        self.n = len(states)
+        h = C.c_void_p()
+        _check(self.lib.kel_particles_create(lattice.handle, self.n, C.byref(h)), self.lib)
+        self._h = h
+        self.upload(states)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.kel_particles_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, states):
+        arr = states if isinstance(states, C.Array) else K.states_from_array(states)
+        _check(self.lib.kel_particles_upload(self._h, arr), self.lib)
+
+    def download(self):
+        arr = (K.ParticleState * self.n)()
+        _check(self.lib.kel_particles_download(self._h, arr), self.lib)
+        return K.states_to_array(arr)
+
+    def reset(self):
+        _check(self.lib.kel_particles_reset(self._h), self.lib)
+
+    def couple(self, params):
+        _check(self.lib.kel_particles_couple(self._h, C.byref(params)), self.lib)
+
+    def gather(self, params, cell_force=False):
+        out = np.empty(self.lat.n * self.lat.D, dtype=np.float32) if cell_force else None
+        _check(self.lib.kel_particles_gather(self._h, C.byref(params), _ptr(out) if out is not None else None),
+               self.lib)
+        return out
+
+    def contact(self, params):
+        _check(self.lib.kel_particles_contact(self._h, C.byref(params)), self.lib)
+
+    def integrate(self, params):
+        _check(self.lib.kel_particles_integrate(self._h, C.byref(params)), self.lib)
+
+    def step(self, params, program, n_steps=1, write_macros=True):
+        fl = K.KEL_STEP_WRITE_MACROS if write_macros else 0
+        _check(self.lib.kel_particles_step(self._h, C.byref(params), C.byref(program), n_steps, fl), self.lib)

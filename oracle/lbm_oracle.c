@@ -236,3 +236,54 @@ void ko_equilibrium_f32(int q, float rho, const float *u, float *eq) {
 }
 
 size_t ko_program_size(void) { return sizeof(kel_step_program); }
+
+/* ---- accessors for the particle restatement (particles_oracle.c) ------- */
+float ko_lattice_pop_f32(const ko_lattice *h, int64_t x, int64_t y, int64_t z, int i);
+int ko_lattice_info(const ko_lattice *h, int *D, int *Q, int64_t *nx, int64_t *ny, int64_t *nz, int *is_f64,
+					int *periodic) {
+	const ko_desc *d = h->is_f64 ? &h->f64.d : &h->f32.d;
+	*D = d->D;
+	*Q = d->Q;
+	*nx = h->is_f64 ? h->f64.nx : h->f32.nx;
+	*ny = h->is_f64 ? h->f64.ny : h->f32.ny;
+	*nz = h->is_f64 ? h->f64.nz : h->f32.nz;
+	*is_f64 = h->is_f64;
+	*periodic = h->is_f64 ? h->f64.periodic_x : h->f32.periodic_x;
+	return 0;
+}
+
+int ko_lattice_dir(const ko_lattice *h, int i, int k) { return (h->is_f64 ? &h->f64.d : &h->f32.d)->c[i][k]; }
+int ko_lattice_opp(const ko_lattice *h, int i) { return (h->is_f64 ? &h->f64.d : &h->f32.d)->opp[i]; }
+
+/* Post-stream population f_i at (x,y,z) of the buffer the next collide reads;
+ * outside the lattice: the zero ghost ring. */
+double ko_lattice_pop(const ko_lattice *h, int64_t x, int64_t y, int64_t z, int i) {
+	if (h->is_f64) {
+		const ko_lat_f64 *L = &h->f64;
+		if (x < 0 || y < 0 || z < 0 || x >= L->nx || y >= L->ny || z >= L->nz) return 0.0;
+		const double *cur = (L->t % 2u == 0u) ? L->dfs[0] : L->dfs[1];
+		return cur[gidx_f64(L, x, y, z) * L->d.Q + i];
+	}
+	return (double)ko_lattice_pop_f32(h, x, y, z, i);
+}
+
+float ko_lattice_pop_f32(const ko_lattice *h, int64_t x, int64_t y, int64_t z, int i) {
+	const ko_lat_f32 *L = &h->f32;
+	if (x < 0 || y < 0 || z < 0 || x >= L->nx || y >= L->ny || z >= L->nz) return 0.0f;
+	const float *cur = (L->t % 2u == 0u) ? L->dfs[0] : L->dfs[1];
+	return cur[gidx_f32(L, x, y, z) * L->d.Q + i];
+}
+
+void ko_lattice_set_porosity_at(ko_lattice *h, int64_t c, double v) {
+	if (h->is_f64) h->f64.por[c] = v;
+	else h->f32.por[c] = (float)v;
+}
+
+double ko_lattice_porosity_at(const ko_lattice *h, int64_t c) {
+	return h->is_f64 ? h->f64.por[c] : (double)h->f32.por[c];
+}
+
+void ko_get_porosity(ko_lattice *h, double *out) {
+	if (h->is_f64) get_vec_f64(h->f64.por, out, h->f64.n);
+	else get_vec_f32(h->f32.por, out, h->f32.n);
+}

@@ -61,6 +61,12 @@ def lib():
         L.ko_time_step.restype = u64
         L.ko_equilibrium_f32.argtypes = [C.c_int, C.c_float, vp, vp]
         L.ko_program_size.restype = C.c_size_t
+        L.ko_get_porosity.argtypes = [vp, vp]
+        L.ko_particles_couple.argtypes = [vp, vp, C.c_int, vp]
+        L.ko_particles_gather.argtypes = [vp, vp, C.c_int, vp, vp]
+        L.ko_particles_reset.argtypes = [vp, C.c_int]
+        L.ko_particles_contact.argtypes = [vp, C.c_int, C.c_int, vp, vp, C.c_int]
+        L.ko_particles_integrate.argtypes = [vp, C.c_int, C.c_int, vp, vp, C.c_int]
         _lib = L
     return _lib
 
@@ -136,6 +142,37 @@ class OracleLattice:
     @property
     def t(self):
         return lib().ko_time_step(self._h)
+
+    def porosity(self):
+        out = np.empty(self.n, dtype=np.float64)
+        lib().ko_get_porosity(self._h, _ptr(out))
+        return out
+
+    # ---- particle restatement (particles_oracle.c) -------------------------
+    def particles_couple(self, states, params):
+        lib().ko_particles_couple(self._h, C.byref(states), len(states), C.byref(params))
+
+    def particles_gather(self, states, params, want_cell_force=False):
+        cf = np.zeros(self.n * self.D, dtype=np.float64) if want_cell_force else None
+        lib().ko_particles_gather(self._h, C.byref(states), len(states), C.byref(params),
+                                  _ptr(cf) if cf is not None else None)
+        return cf
+
+
+def particles_reset(states):
+    lib().ko_particles_reset(C.byref(states), len(states))
+
+
+def particles_contact(states, D, params, extent, periodic_x=False):
+    ext = np.zeros(3, dtype=np.int64)
+    ext[:len(extent)] = extent
+    lib().ko_particles_contact(C.byref(states), len(states), D, C.byref(params), _ptr(ext), int(periodic_x))
+
+
+def particles_integrate(states, D, params, extent, periodic_x=False):
+    ext = np.zeros(3, dtype=np.int64)
+    ext[:len(extent)] = extent
+    lib().ko_particles_integrate(C.byref(states), len(states), D, C.byref(params), _ptr(ext), int(periodic_x))
 
 
 def equilibrium_f32(q, rho, u):

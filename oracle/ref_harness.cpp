@@ -379,6 +379,147 @@ struct Case {
 	}
 };
 
+
+/*
+ * Particle path of one coupled step, phase by phase (reset, gather, contact,
+ * integrate), driving the reference's own components:
+ *   ParticleForceReset, PsmOneParticleGather (psm.hpp:95-446),
+ *   ParticleContact (particle/contact.hpp:522-567), ParticleIntegrate
+ *   (particle/integrate.hpp:263-296),
+ * on a group built by create_spheroid_particle_group (particle/particle.hpp:19-116).
+ * The reference driver runs the four per particle in one work-item
+ * (examples/moving_poiseulle_particles_2d_psm_gpu/sim.cpp:198-224), so later
+ * particles' contacts can read positions already integrated; here every
+ * phase completes for all particles before the next starts.
+ *
+ * in_dir/pparams.txt: sub_steps k_n zeta_n gamma_t mu gx gy walls
+ * in_dir/particles.f64: per particle x y xo yo rot roto radius density
+ * in_dir/init.f64: AoS populations at t = 0
+ * out_dir/porosity.f64, force_field.f64, after_gather.f64, after_contact.f64,
+ *   after_integrate.f64 (28 doubles per particle, kel_particle_state order)
+ */
+template <typename T, typename Desc, uint64_t NX, uint64_t NY, uint64_t NP>
+struct ParticleCase {
+	using Base = Case<T, Desc, NX, NY>;
+	using NT = typename native_data_type<T>::type;
+	static constexpr uint64_t D = 2, Q = Desc::Q, N = NX * NY;
+	using GroupSch = sch::ParticleGroup<T, D, NP, coll::Spheroid<T>>;
+
+	template <typename G>
+	static void dump(const std::string &path, G &g) {
+		std::vector<double> out;
+		auto &parts = g.template get<"particles">();
+		for (uint64_t p = 0; p < NP; ++p) {
+			auto &rb = parts.at({p}).template get<"rigid_body">();
+			double st[28] = {0};
+			for (uint64_t k = 0; k < D; ++k) {
+				st[0 + k] = rb.template get<"position">().at({{k}}).get();
+				st[3 + k] = rb.template get<"position_old">().at({{k}}).get();
+				st[12 + k] = rb.template get<"acceleration">().at({{k}}).get();
+				st[18 + k] = rb.template get<"force">().at({{k}}).get();
+			}
+			st[6] = rb.template get<"rotation">().at({}).get();
+			st[9] = rb.template get<"rotation_old">().at({}).get();
+			st[15] = rb.template get<"angular_acceleration">().at({}).get();
+			st[21] = rb.template get<"torque">().at({}).get();
+			st[24] = rb.template get<"mass">().at({}).get();
+			st[25] = rb.template get<"inertia">().at({}).get();
+			st[26] = parts.at({p}).template get<"collision">().template get<"radius">().at({}).get();
+			st[27] = rb.template get<"density">().at({}).get();
+			out.insert(out.end(), st, st + 28);
+		}
+		write_f64(path, out);
+	}
+
+	static int run(const std::string &in, const std::string &out) {
+		std::ifstream pf(in + "/pparams.txt");
+		uint64_t sub_steps;
+		double k_n, zeta, gamma_t, mu, gx, gy;
+		int walls;
+		pf >> sub_steps >> k_n >> zeta >> gamma_t >> mu >> gx >> gy >> walls;
+		auto pv = read_file(in + "/particles.f64", true);
+		auto init = read_file(in + "/init.f64", true);
+		if (pv.size() != NP * 8 * 8 || init.size() != N * Q * 8) return 5;
+		const double *P = reinterpret_cast<const double *>(pv.data());
+		const double *I = reinterpret_cast<const double *>(init.data());
+
+		auto fields_own = heap<data<typename Base::ChunkStruct>>();
+		auto macros_own = heap<data<typename Base::MacroStruct>>();
+		data<sch::Ptr<typename Base::ChunkStruct>> fields{*fields_own};
+		data<sch::Ptr<typename Base::MacroStruct>> macros{*macros_own};
+		auto &dfs_old_f = fields.template get<"dfs_old">();
+		auto &por_f = macros.template get<"porosity">();
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			for (uint64_t i = 0; i < Q; ++i) dfs_old_f.at(idx).at({i}).set(static_cast<NT>(I[c * Q + i]));
+			por_f.at(idx).at({}).set(NT(1));
+			macros.template get<"density">().at(idx).at({}).set(NT(1));
+		}
+
+		data<sch::LbmMeter<sch::Scalar<T>>> r0;
+		r0.at({}).set(static_cast<NT>(P[6]));
+		data<sch::Scalar<T>> d0;
+		d0.at({}).set(static_cast<NT>(P[7]));
+		auto g = create_spheroid_particle_group<T, D, NP>(r0, d0, {4u});
+		auto &parts = g.template get<"particles">();
+		for (uint64_t p = 0; p < NP; ++p) {
+			const double *q = P + p * 8;
+			auto &pi = parts.at({p});
+			auto &rb = pi.template get<"rigid_body">();
+			rb.template get<"position">().at({{0u}}).set(static_cast<NT>(q[0]));
+			rb.template get<"position">().at({{1u}}).set(static_cast<NT>(q[1]));
+			rb.template get<"position_old">().at({{0u}}).set(static_cast<NT>(q[2]));
+			rb.template get<"position_old">().at({{1u}}).set(static_cast<NT>(q[3]));
+			rb.template get<"rotation">().at({}).set(static_cast<NT>(q[4]));
+			rb.template get<"rotation_old">().at({}).set(static_cast<NT>(q[5]));
+			/* per-particle size: mass pi r^2 rho, inertia m r^2 / 2 (particle.hpp:79-101) */
+			constexpr NT pi_c = 3.14159265358979323846;
+			NT r = static_cast<NT>(q[6]), rho = static_cast<NT>(q[7]);
+			NT m = pi_c * r * r * rho;
+			pi.template get<"collision">().template get<"radius">().at({}).set(r);
+			rb.template get<"mass">().at({}).set(m);
+			rb.template get<"inertia">().at({}).set(NT(0.5) * m * r * r);
+			rb.template get<"density">().at({}).set(rho);
+		}
+		data<sch::Ptr<GroupSch>, enc::Native> view{g};
+
+		component<T, Desc, cmpt::ParticleForceReset> reset;
+		component<T, Desc, cmpt::PsmOneParticleGather> gather;
+		dem_params<T> dem{static_cast<NT>(k_n), static_cast<NT>(zeta), static_cast<NT>(gamma_t), static_cast<NT>(mu)};
+		data<sch::FixedArray<sch::UInt64, D>> extent{{NX, NY}};
+		data<sch::LbmAcceleration<sch::Vector<T, D>>> grav;
+		grav.at({{0u}}).set(static_cast<NT>(gx));
+		grav.at({{1u}}).set(static_cast<NT>(gy));
+		component<T, Desc, cmpt::ParticleIntegrate> integrate{grav};
+		data<sch::UInt64> t0{0u}, ss{sub_steps};
+
+		for (uint64_t p = 0; p < NP; ++p) reset.apply(view, {{p}}, t0);
+		for (uint64_t p = 0; p < NP; ++p) gather.apply(fields, macros, view, {{p}}, t0, ss);
+		dump(out + "/after_gather.f64", g);
+		{
+			std::vector<double> por(N), ff(N * D);
+			for (uint64_t c = 0; c < N; ++c) {
+				auto idx = Base::unflat(c);
+				por[c] = por_f.at(idx).at({}).get();
+				for (uint64_t k = 0; k < D; ++k) ff[c * D + k] = macros.template get<"force">().at(idx).at({{k}}).get();
+			}
+			write_f64(out + "/porosity.f64", por);
+			write_f64(out + "/force_field.f64", ff);
+		}
+		if (walls) {
+			component<T, Desc, cmpt::ParticleContact> contact{dem, extent};
+			for (uint64_t p = 0; p < NP; ++p) contact.apply(view, {{p}}, t0, ss);
+		} else {
+			component<T, Desc, cmpt::ParticleContact> contact{dem};
+			for (uint64_t p = 0; p < NP; ++p) contact.apply(view, {{p}}, t0, ss);
+		}
+		dump(out + "/after_contact.f64", g);
+		for (uint64_t p = 0; p < NP; ++p) integrate.apply(view, {{p}}, t0, ss);
+		dump(out + "/after_integrate.f64", g);
+		return 0;
+	}
+};
+
 int main(int argc, char **argv) {
 	if (argc != 4) {
 		std::fprintf(stderr, "usage: %s <case> <in_dir> <out_dir>\n", argv[0]);
@@ -393,6 +534,8 @@ int main(int argc, char **argv) {
 	if (c == "d3q19_f32_16x12x10") return Case<F32, sch::D3Q19, 16, 12, 10>::run(argv[2], argv[3]);
 	if (c == "d3q19_f64_16x12x10") return Case<F64, sch::D3Q19, 16, 12, 10>::run(argv[2], argv[3]);
 	if (c == "d3q27_f32_16x12x10") return Case<F32, sch::D3Q27, 16, 12, 10>::run(argv[2], argv[3]);
+	if (c == "particles_d2q9_f64_64x48x5") return ParticleCase<F64, sch::D2Q9, 64, 48, 5>::run(argv[2], argv[3]);
+	if (c == "particles_d2q9_f32_64x48x5") return ParticleCase<F32, sch::D2Q9, 64, 48, 5>::run(argv[2], argv[3]);
 	if (c == "d3q27_f64_16x12x10") return Case<F64, sch::D3Q27, 16, 12, 10>::run(argv[2], argv[3]);
 	std::fprintf(stderr, "unknown case %s\n", c.c_str());
 	return 1;

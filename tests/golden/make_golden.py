@@ -112,8 +112,67 @@ def load(name):
     return case, z["dfs"].astype(np.float64), z["rho"].astype(np.float64), z["vel"].astype(np.float64)
 
 
+# ---- particle path ------------------------------------------------------------
+
+PART_DIMS = (64, 48)
+PART_PARAMS = dict(sub_steps=2, k_n=100.0, zeta_n=0.1, gamma_t=0.5, mu=0.3, gravity=(0.0, -1e-4), walls=1)
+
+
+def particle_inputs(kind, seed=11):
+    """Bodies (x, y, x_old, y_old, rot, rot_old, radius, density) and AoS
+    populations.  'gather': well separated bodies (no ramp overlaps);
+    'contact': two overlapping pairs and bodies pressed into two walls."""
+    rng = np.random.default_rng(cases.SEED + seed)
+    if kind == "gather":
+        xy = [(12.3, 11.7, 5.0), (33.6, 14.2, 4.5), (51.1, 30.4, 6.0), (14.8, 35.5, 5.5), (38.2, 35.9, 4.0)]
+    else:
+        xy = [(20.2, 20.4, 6.0), (30.1, 21.3, 5.5), (44.6, 4.1, 5.0), (58.2, 30.3, 6.5), (23.9, 31.0, 5.0)]
+    bodies = []
+    for (x, y, r) in xy:
+        vx, vy = 0.01 * rng.standard_normal(2)
+        rot = 0.05 * rng.standard_normal()
+        bodies.append([x, y, x - vx, y - vy, rot, rot - 0.002 * rng.standard_normal(), r, 1.5])
+    bodies = np.array(bodies, dtype=np.float64)
+    n = PART_DIMS[0] * PART_DIMS[1]
+    init = cases.random_populations(9, n, rng, amp=0.05)
+    init = init.astype(np.float32).astype(np.float64)
+    return bodies, init
+
+
+def run_particle_harness(hcase, bodies, init, workdir):
+    ind = os.path.join(workdir, "in")
+    outd = os.path.join(workdir, "out")
+    os.makedirs(ind, exist_ok=True)
+    os.makedirs(outd, exist_ok=True)
+    P = PART_PARAMS
+    open(os.path.join(ind, "pparams.txt"), "w").write(
+        f"{P['sub_steps']} {P['k_n']!r} {P['zeta_n']!r} {P['gamma_t']!r} {P['mu']!r} "
+        f"{P['gravity'][0]!r} {P['gravity'][1]!r} {P['walls']}\n")
+    bodies.astype(np.float64).tofile(os.path.join(ind, "particles.f64"))
+    init.astype(np.float64).tofile(os.path.join(ind, "init.f64"))
+    subprocess.check_call([HARNESS, hcase, ind, outd])
+    out = {}
+    for k in ("porosity", "force_field", "after_gather", "after_contact", "after_integrate"):
+        a = np.fromfile(os.path.join(outd, k + ".f64"))
+        out[k] = a.reshape(-1, 28) if k.startswith("after") else a
+    return out
+
+
+def particle_registry():
+    return {
+        "particles_gather_f64": ("particles_d2q9_f64_64x48x5", "gather"),
+        "particles_gather_f32": ("particles_d2q9_f32_64x48x5", "gather"),
+        "particles_contact_f64": ("particles_d2q9_f64_64x48x5", "contact"),
+    }
+
+
+def load_particles(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return {k: z[k] for k in z.files}
+
+
 def names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("particles_"))
 
 
 def main():
@@ -122,6 +181,15 @@ def main():
     args = ap.parse_args()
     if not os.path.exists(HARNESS):
         subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle")])
+    for name, (hcase, kind) in particle_registry().items():
+        if args.only and args.only not in name:
+            continue
+        bodies, init = particle_inputs(kind)
+        with tempfile.TemporaryDirectory() as td:
+            out = run_particle_harness(hcase, bodies, init, td)
+        np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), bodies=bodies, init=init.astype(np.float32),
+                            params=np.array(json.dumps(PART_PARAMS)), **out)
+        print(f"{name:28s} particles: force after gather {out['after_gather'][:, 18:20].ravel()[:4]}")
     for name, (hcase, case) in registry().items():
         if args.only and args.only not in name:
             continue

@@ -9,8 +9,10 @@ from lbm_mirror_gb300 import capi as K
 QNAME = {9: "D2Q9", 19: "D3Q19", 27: "D3Q27"}
 
 
-def make_lattice(case, storage="fp32"):
+def make_lattice(case, storage="fp32", launch=None):
     lat = Lattice(QNAME[case["q"]], case["dims"], storage=storage, periodic_x=case["periodic"])
+    if launch is not None:
+        lat.set_launch(*launch)
     lat.upload_flags(case["flags"])
     if case["init"] is not None:
         lat.upload_populations(case["init"].astype(np.float32))
@@ -29,9 +31,9 @@ def with_arith(program, arithmetic):
     return K.program_from_dict(d)
 
 
-def run_gpu(case, arithmetic=K.KEL_ARITH_REFERENCE, storage="fp32", chunks=None):
+def run_gpu(case, arithmetic=K.KEL_ARITH_REFERENCE, storage="fp32", chunks=None, launch=None):
     """Run ``case`` on the GPU; returns (populations AoS f64, rho, vel)."""
-    lat = make_lattice(case, storage)
+    lat = make_lattice(case, storage, launch)
     prog = with_arith(case["program"], arithmetic)
     steps = case["steps"]
     if chunks:

@@ -21,10 +21,15 @@ FAST_TOL = 1e-5
 F32_NAMES = [n for n in G.names() if not n.endswith("_f64")]
 
 
+LAUNCHES = [(1, 256), (4, 256), (1, 64), (4, 128)]
+
+
+@pytest.mark.parametrize("launch", LAUNCHES, ids=lambda l: f"{l[0]}cell_{l[1]}thr")
 @pytest.mark.parametrize("name", F32_NAMES)
-def test_reference_arithmetic_bit_exact(name):
+def test_reference_arithmetic_bit_exact(name, launch):
+    """Bit-exact for every launch shape (one or four cells per thread)."""
     case, dfs, rho, vel = G.load(name)
-    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE)
+    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE, launch=launch)
     np.testing.assert_array_equal(f, dfs)
     np.testing.assert_array_equal(r, rho)
     np.testing.assert_array_equal(v, vel)
@@ -66,24 +71,26 @@ def test_upload_at_odd_time_step():
     np.testing.assert_array_equal(b.populations(np.float64), ref)
 
 
+@pytest.mark.parametrize("launch", [(1, 256), (4, 256)], ids=lambda l: f"{l[0]}cell")
 @pytest.mark.parametrize("q", [9, 27])
-def test_periodic_x_matches_oracle(q):
+def test_periodic_x_matches_oracle(q, launch):
     if q == 9:
         case = G.normalise(cases.mixed_2d(K.KEL_COLL_PSM_GUO, dims=(48, 20), periodic=True, steps=23))
     else:
         case = G.normalise(cases.mixed_3d(27, K.KEL_COLL_BGK_GUO, dims=(16, 12, 10), periodic=True, steps=15))
     odfs, orho, ovel = cases.run_oracle(case)
-    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE)
+    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE, launch=launch)
     np.testing.assert_array_equal(f, odfs)
     np.testing.assert_array_equal(v, ovel)
 
 
+@pytest.mark.parametrize("launch", [(1, 64), (4, 256)], ids=lambda l: f"{l[0]}cell")
 @pytest.mark.parametrize("nx", [5, 37, 130, 131])
-def test_ragged_widths_match_oracle(nx):
+def test_ragged_widths_match_oracle(nx, launch):
     """Row widths that are not multiples of 4 or of a warp's 128 cells."""
     case = G.normalise(cases.mixed_2d(K.KEL_COLL_BGK, dims=(nx, 9), steps=9, seed=7))
     odfs, orho, ovel = cases.run_oracle(case)
-    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE)
+    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE, launch=launch)
     np.testing.assert_array_equal(f, odfs)
     np.testing.assert_array_equal(r, orho)
 
@@ -160,4 +167,8 @@ def test_invalid_arguments_return_errors():
     assert e.value.code == K.KEL_ERR_UNSUPPORTED
     with pytest.raises(KelError):
         lat.step(K.make_program(-1.0), 1)
+    with pytest.raises(KelError):
+        lat.set_launch(2, 256)
+    with pytest.raises(KelError):
+        lat.set_launch(1, 100)
     lat.close()
