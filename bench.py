@@ -39,6 +39,7 @@ WORKLOADS = {
     "d3q19_cavity_128": (19, (128, 128, 128), 0.55, "cavity"),
     "d2q9_poiseuille_256x64": (9, (256, 64), 0.8, "poiseuille"),
     "d2q9_channel_4096x4096": (9, (4096, 4096), 0.8, "poiseuille"),
+    "d2q9_batch_1024": (9, None, None, "batch"),
 }
 
 
@@ -185,6 +186,36 @@ def run_reference(args, rank, world):
     print(json.dumps(line))
 
 
+def run_batch(args, rank, world):
+    """Config C4: 1024 seeded uneven D2Q9 channels in one batched launch."""
+    import torch
+    from lbm_mirror_gb300 import Batch
+    from tests import cases
+    chans = cases.batch_channels()
+    b = Batch(chans, cases.channel_program(0.8))
+    tile, tune_ms = b.autotune(steps=6)
+    cells, padded, _ = b.info()
+    b.step(args.warmup)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    b.step(args.steps)
+    dt = time.perf_counter() - t0
+    value = world * cells * args.steps / dt / 1e6
+    bpu = bytes_per_update(9, "fp32")
+    peak, src = load_peaks()
+    line = {"metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "d2q9_batch_1024", "channels": len(chans), "cells": cells, "padded_cells": padded,
+                       "tile": tile, "autotune_ms_per_step": tune_ms},
+            "roofline": {"bound": "hbm", "achieved": bpu * cells / (dt / args.steps) / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": bpu * cells / (dt / args.steps) / 1e9 / peak, "traffic": None,
+                         "peak_source": src, "bytes_per_update": bpu},
+            "gpu_launches": args.steps}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -214,6 +245,9 @@ def main():
 
     import torch
     torch.cuda.set_device(local)
+    if WORKLOADS[args.workload][3] == "batch":
+        run_batch(args, rank, world)
+        return
     dist = None
     if world > 1:
         import torch.distributed as dist

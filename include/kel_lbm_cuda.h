@@ -208,6 +208,46 @@ int kel_particles_integrate(kel_particles *ps, const kel_particle_params *prm);
 int kel_particles_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
 					   uint64_t n_steps, uint32_t step_flags);
 
+/* ---- batches: many independent D2Q9 channels in one launch ------------ */
+
+typedef struct kel_channel_desc {
+	int64_t nx, ny; /* extents of this channel */
+	double tau;     /* relaxation time of this channel (BGK) */
+	double u_max;   /* amplitude of its parabolic inlet: u_x(y) = 4 u_max eta (1 - eta),
+					   eta = (y - 1/2) / (ny - 2), zero on the rim rows */
+} kel_channel_desc;
+
+typedef struct kel_batch kel_batch;
+
+/* All channels packed into one allocation, laid out in tiles of `tile` cells
+ * (128, 256 or 512; 0 = 256), one thread block per tile.  No counterpart in
+ * the reference, which runs one compile-time-sized chunk per process
+ * (modules/core/c++/chunk.hpp:25-39). */
+int kel_batch_create(int32_t n_channels, const kel_channel_desc *channels, int32_t tile, kel_batch **out);
+int kel_batch_destroy(kel_batch *b);
+/* Flags of every channel, concatenated (nx*ny bytes each, x fastest). */
+int kel_batch_upload_flags(kel_batch *b, const uint8_t *packed_flags);
+/* Shared flag -> operation table; BGK only (tau comes from each channel);
+ * ZouHeVelocityX ops with use_profile take the channel's parabolic inlet. */
+int kel_batch_set_program(kel_batch *b, const kel_step_program *prog);
+/* Time `steps` sweeps per candidate tile and keep the fastest (before the first step). */
+int kel_batch_autotune(kel_batch *b, int32_t steps, int32_t *chosen_tile, float *ms_per_step);
+int kel_batch_step(kel_batch *b, uint64_t n_steps);
+/* Run every active channel until its relative L2 velocity change over
+ * `check_every` steps, sqrt(sum |u_t - u_{t-k}|^2 / sum |u_t|^2) in FP64, is
+ * below `tol`, or until `max_steps`.  With use_graph the `check_every` sweeps
+ * and the residual are one captured CUDA graph, replayed.  steps_out and
+ * residual_out (n values each, may be NULL) receive each channel's final time
+ * step and last residual. */
+int kel_batch_run_until(kel_batch *b, double tol, uint64_t check_every, uint64_t max_steps, int32_t use_graph,
+						uint64_t *steps_out, double *residual_out);
+int kel_batch_active_count(kel_batch *b, int32_t *count);
+int kel_batch_channel_time_step(const kel_batch *b, int32_t channel, uint64_t *t);
+int kel_batch_info(const kel_batch *b, int64_t *cells, int64_t *padded_cells, int32_t *tile);
+/* One channel's populations (AoS, nx*ny*9) or macros (rho, u_x, u_y per cell). */
+int kel_batch_download_populations(kel_batch *b, int32_t channel, float *host_aos);
+int kel_batch_download_macros(kel_batch *b, int32_t channel, float *host_rho_u);
+
 /* Launch shape of the sweep: cells per thread (1: 32-bit accesses, one cell;
  * 4: 128-bit accesses, four consecutive cells) and threads per block (64, 128
  * or 256).  Results do not depend on it. */

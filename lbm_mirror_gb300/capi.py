@@ -189,6 +189,10 @@ def states_from_array(a):
     return arr
 
 
+class ChannelDesc(C.Structure):
+    _fields_ = [("nx", C.c_int64), ("ny", C.c_int64), ("tau", C.c_double), ("u_max", C.c_double)]
+
+
 _lib = None
 
 
@@ -219,6 +223,18 @@ def load_library(path: str | None = None):
         "kel_step": ([vp, C.POINTER(StepProgram), u64, u32], C.c_int),
         "kel_lattice_synchronize": ([vp], C.c_int),
         "kel_lattice_set_launch": ([vp, i32, i32], C.c_int),
+        "kel_batch_create": ([i32, C.POINTER(ChannelDesc), i32, C.POINTER(vp)], C.c_int),
+        "kel_batch_destroy": ([vp], C.c_int),
+        "kel_batch_upload_flags": ([vp, vp], C.c_int),
+        "kel_batch_set_program": ([vp, C.POINTER(StepProgram)], C.c_int),
+        "kel_batch_autotune": ([vp, i32, C.POINTER(i32), C.POINTER(C.c_float)], C.c_int),
+        "kel_batch_step": ([vp, u64], C.c_int),
+        "kel_batch_run_until": ([vp, C.c_double, u64, u64, i32, vp, vp], C.c_int),
+        "kel_batch_active_count": ([vp, C.POINTER(i32)], C.c_int),
+        "kel_batch_channel_time_step": ([vp, i32, C.POINTER(u64)], C.c_int),
+        "kel_batch_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i32)], C.c_int),
+        "kel_batch_download_populations": ([vp, i32, vp], C.c_int),
+        "kel_batch_download_macros": ([vp, i32, vp], C.c_int),
         "kel_lattice_get_launch": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "kel_particles_create": ([vp, i32, C.POINTER(vp)], C.c_int),
         "kel_particles_destroy": ([vp], C.c_int),

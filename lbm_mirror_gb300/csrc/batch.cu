@@ -1,0 +1,653 @@
+// Many independent D2Q9 channels of uneven size in one launch (C ABI
+// kel_batch_*).
+//
+// The reference runs one compile-time-sized Chunk per process
+// (modules/core/c++/chunk.hpp:25-39; SuperChunk "Not needed for now"), so a
+// parameter sweep over many channels is many separate runs.  Here all channels
+// share one allocation:
+//   - populations: 9 planes over the packed cells of every channel; channel c
+//     owns [off_c, off_c + nxp_c * ny_c), padded up to whole tiles;
+//   - one tile (= one thread block, `tile` cells, one cell per thread) never
+//     spans two channels: block b reads its channel from block_ch[b];
+//   - per-channel relaxation rate and parabolic inlet profile come from the
+//     channel table; the flag -> operation table is shared.
+// Steps run as a captured CUDA graph of `check_every` sweeps followed by the
+// FP64 convergence residual per channel; converged channels drop out (their
+// blocks return at once) and the graph is replayed until none is left.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "lattice_internal.cuh"
+
+using namespace kel::gb;
+
+namespace {
+
+struct ChannelRec {
+	int64_t off;     // first packed cell
+	int nx, nxp, ny; // extents (nxp = nx padded to 4)
+	int first_block; // first tile
+	int nblocks;     // tiles
+	int prof_off;    // offset into the packed inlet profiles
+	float omega;     // 1 / tau in float
+	float guo_scale; // 1 - omega / 2
+};
+
+struct BatchParams {
+	float *f;
+	int64_t plane;
+	const uint8_t *flags;
+	float *rho, *u, *u_prev;
+	const OpEntry *ops;
+	const float *profiles;
+	const ChannelRec *ch;
+	const int *block_ch;
+	int *active;
+	double2 *partial; // per-tile residual partial sums (scratch)
+	int tile;
+	int write_macros;
+};
+
+template <bool ODD, bool EXACT>
+__global__ void __launch_bounds__(512) k_batch_sweep(const __grid_constant__ BatchParams p) {
+	using L = D2Q9;
+	const int c = p.block_ch[blockIdx.x];
+	if (!p.active[c]) return;
+	const ChannelRec ch = p.ch[c];
+	const int l = (blockIdx.x - ch.first_block) * blockDim.x + threadIdx.x;
+	if (l >= ch.nxp * ch.ny) return;
+	const int y = l / ch.nxp, x = l - y * ch.nxp;
+	const int64_t cell = ch.off + l;
+	float f[9];
+#pragma unroll
+	for (int i = 0; i < 9; ++i) {
+		if (!ODD) {
+			f[i] = __ldcs(p.f + i * p.plane + cell);
+		} else {
+			const int sx = x - L::cx(i), sy = y - L::cy(i);
+			const bool in = sx >= 0 && sx < ch.nxp && sy >= 0 && sy < ch.ny;
+			f[i] = in ? __ldcs(p.f + L::opp(i) * p.plane + ch.off + sy * ch.nxp + sx) : 0.f;
+		}
+	}
+	CellCtx ctx;
+	ctx.ops = p.ops;
+	ctx.profile = p.profiles + ch.prof_off;
+	ctx.omega = ch.omega;
+	ctx.guo_scale = ch.guo_scale;
+	ctx.g[0] = ctx.g[1] = ctx.g[2] = 0.f;
+	const float Fc[3] = {0.f, 0.f, 0.f};
+	float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
+	const bool col = cell_update<L, COLL_BGK, EXACT>(f, p.flags[cell], y, ctx, 1.f, Fc, rho, u);
+	if (p.write_macros && col) {
+		p.rho[cell] = rho;
+		p.u[cell] = u[0];
+		p.u[p.plane + cell] = u[1];
+	}
+#pragma unroll
+	for (int i = 0; i < 9; ++i) {
+		if (!ODD) {
+			__stcs(p.f + L::opp(i) * p.plane + cell, f[i]);
+		} else {
+			const int64_t pb = static_cast<int64_t>(i) * p.plane;
+			const int sx = x - L::cx(i), sy = y - L::cy(i);
+			if (sx < 0 || sx >= ch.nxp || sy < 0 || sy >= ch.ny) __stcs(p.f + pb + cell, 0.f);
+			const int dx = x + L::cx(i), dy = y + L::cy(i);
+			if (dx >= 0 && dx < ch.nxp && dy >= 0 && dy < ch.ny) __stcs(p.f + pb + ch.off + dy * ch.nxp + dx, f[i]);
+		}
+	}
+}
+
+// Per tile: sum over its cells of |u - u_prev|^2 and |u|^2 in FP64, then
+// u_prev = u.  Fixed reduction order (warp shuffle, then warps in order).
+__global__ void __launch_bounds__(512) k_batch_residual_partial(BatchParams p) {
+	__shared__ double sh[2][16];
+	const int c = p.block_ch[blockIdx.x];
+	double num = 0.0, den = 0.0;
+	if (p.active[c]) {
+		const ChannelRec ch = p.ch[c];
+		const int l = (blockIdx.x - ch.first_block) * blockDim.x + threadIdx.x;
+		if (l < ch.nxp * ch.ny) {
+			const int64_t cell = ch.off + l;
+			for (int d = 0; d < 2; ++d) {
+				const double a = p.u[d * p.plane + cell], b = p.u_prev[d * p.plane + cell];
+				num += (a - b) * (a - b);
+				den += a * a;
+				p.u_prev[d * p.plane + cell] = (float)a;
+			}
+		}
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		num += __shfl_down_sync(0xffffffffu, num, o);
+		den += __shfl_down_sync(0xffffffffu, den, o);
+	}
+	if ((threadIdx.x & 31) == 0) {
+		sh[0][threadIdx.x >> 5] = num;
+		sh[1][threadIdx.x >> 5] = den;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double a = 0.0, b = 0.0;
+		for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+			a += sh[0][w];
+			b += sh[1][w];
+		}
+		p.partial[blockIdx.x] = make_double2(a, b);
+	}
+}
+
+// Per channel: relative L2 change sqrt(sum|du|^2 / sum|u|^2) over its tiles
+// (in tile order); a channel below `tol` is deactivated.
+__global__ void k_batch_residual_final(BatchParams p, int n_channels, double tol, double *residual) {
+	const int c = blockIdx.x * blockDim.x + threadIdx.x;
+	if (c >= n_channels || !p.active[c]) return;
+	const ChannelRec ch = p.ch[c];
+	double a = 0.0, b = 0.0;
+	for (int k = 0; k < ch.nblocks; ++k) {
+		const double2 v = p.partial[ch.first_block + k];
+		a += v.x;
+		b += v.y;
+	}
+	const double r = b > 0.0 ? sqrt(a / b) : (a > 0.0 ? INFINITY : 0.0);
+	residual[c] = r;
+	if (r < tol) p.active[c] = 0;
+}
+
+__global__ void k_batch_init(BatchParams p, int64_t n) {
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+		for (int i = 0; i < 9; ++i) p.f[i * p.plane + k] = (float)D2Q9::w(i);
+		p.rho[k] = 1.f;
+		p.u[k] = p.u[p.plane + k] = 0.f;
+		p.u_prev[k] = p.u_prev[p.plane + k] = 0.f;
+	}
+}
+
+// packed host flags (nx*ny per channel, concatenated) -> padded device tiles
+__global__ void k_batch_flags(BatchParams p, const uint8_t *packed, const int64_t *src_off, int n_channels) {
+	const int c = blockIdx.y;
+	if (c >= n_channels) return;
+	const ChannelRec ch = p.ch[c];
+	const int64_t cells = (int64_t)ch.nxp * ch.ny;
+	uint8_t *dst = const_cast<uint8_t *>(p.flags);
+	for (int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; l < cells; l += (int64_t)gridDim.x * blockDim.x) {
+		const int y = (int)(l / ch.nxp), x = (int)(l - (int64_t)y * ch.nxp);
+		dst[ch.off + l] = x < ch.nx ? packed[src_off[c] + (int64_t)y * ch.nx + x] : 0;
+	}
+}
+
+// channel c -> host layouts (AoS populations, or rho / u)
+__global__ void k_batch_download(BatchParams p, ChannelRec ch, int odd, int what, float *out) {
+	const int64_t n = (int64_t)ch.nx * ch.ny;
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+		const int y = (int)(k / ch.nx), x = (int)(k - (int64_t)y * ch.nx);
+		const int64_t cell = ch.off + (int64_t)y * ch.nxp + x;
+		if (what == 0) {
+			for (int i = 0; i < 9; ++i) {
+				float v;
+				if (!odd) {
+					v = p.f[i * p.plane + cell];
+				} else {
+					const int sx = x - D2Q9::cx(i), sy = y - D2Q9::cy(i);
+					v = (sx >= 0 && sx < ch.nxp && sy >= 0 && sy < ch.ny)
+							? p.f[D2Q9::opp(i) * p.plane + ch.off + (int64_t)sy * ch.nxp + sx]
+							: 0.f;
+				}
+				out[k * 9 + i] = v;
+			}
+		} else {
+			out[k * 3 + 0] = p.rho[cell];
+			out[k * 3 + 1] = p.u[cell];
+			out[k * 3 + 2] = p.u[p.plane + cell];
+		}
+	}
+}
+
+} // namespace
+
+struct kel_batch {
+	int n = 0;
+	int tile = 256;
+	std::vector<kel_channel_desc> desc;
+	std::vector<ChannelRec> rec;
+	std::vector<int> block_ch;
+	std::vector<uint64_t> t;          // per-channel time step
+	std::vector<uint8_t> host_flags;  // packed copy (kept for re-layout)
+	std::vector<float> host_profiles; // packed inlet profiles
+	int64_t plane = 0;
+	int nblocks = 0;
+	int64_t profile_len = 0;
+	// device
+	float *f = nullptr, *rho = nullptr, *u = nullptr, *u_prev = nullptr, *profiles = nullptr;
+	uint8_t *flags = nullptr;
+	ChannelRec *d_rec = nullptr;
+	int *d_block_ch = nullptr, *d_active = nullptr;
+	double2 *partial = nullptr;
+	double *d_residual = nullptr;
+	OpEntry *ops = nullptr;
+	bool have_ops = false;
+	kel_step_program prog;
+	bool exact = false;
+	cudaStream_t stream = nullptr;
+	bool own_stream = false;
+	cudaGraphExec_t graph = nullptr;
+	int graph_check = 0;
+	double graph_tol = 0.0;
+};
+
+namespace {
+
+void free_device(kel_batch *B) {
+	cudaFree(B->f);
+	cudaFree(B->rho);
+	cudaFree(B->u);
+	cudaFree(B->u_prev);
+	cudaFree(B->profiles);
+	cudaFree(B->flags);
+	cudaFree(B->d_rec);
+	cudaFree(B->d_block_ch);
+	cudaFree(B->d_active);
+	cudaFree(B->partial);
+	cudaFree(B->d_residual);
+	B->f = B->rho = B->u = B->u_prev = B->profiles = nullptr;
+	B->flags = nullptr;
+	B->d_rec = nullptr;
+	B->d_block_ch = B->d_active = nullptr;
+	B->partial = nullptr;
+	B->d_residual = nullptr;
+	if (B->graph) cudaGraphExecDestroy(B->graph);
+	B->graph = nullptr;
+}
+
+BatchParams params(const kel_batch *B, int write_macros) {
+	BatchParams p;
+	memset(&p, 0, sizeof(p));
+	p.f = B->f;
+	p.plane = B->plane;
+	p.flags = B->flags;
+	p.rho = B->rho;
+	p.u = B->u;
+	p.u_prev = B->u_prev;
+	p.ops = B->ops;
+	p.profiles = B->profiles;
+	p.ch = B->d_rec;
+	p.block_ch = B->d_block_ch;
+	p.active = B->d_active;
+	p.partial = B->partial;
+	p.tile = B->tile;
+	p.write_macros = write_macros;
+	return p;
+}
+
+// Lay the channels out in tiles of `tile` cells and allocate the device side.
+int layout(kel_batch *B, int tile) {
+	free_device(B);
+	B->tile = tile;
+	B->rec.assign(B->n, ChannelRec{});
+	B->block_ch.clear();
+	int64_t off = 0;
+	int64_t poff = 0;
+	for (int c = 0; c < B->n; ++c) {
+		const kel_channel_desc &d = B->desc[c];
+		ChannelRec &r = B->rec[c];
+		r.nx = (int)d.nx;
+		r.nxp = (int)((d.nx + 3) / 4 * 4);
+		r.ny = (int)d.ny;
+		r.off = off;
+		r.first_block = (int)B->block_ch.size();
+		const int64_t cells = (int64_t)r.nxp * r.ny;
+		r.nblocks = (int)((cells + tile - 1) / tile);
+		for (int k = 0; k < r.nblocks; ++k) B->block_ch.push_back(c);
+		off += (int64_t)r.nblocks * tile;
+		r.prof_off = (int)poff;
+		poff += r.ny;
+		r.omega = 1.0f / (float)d.tau;
+		r.guo_scale = 1.0f - 0.5f * r.omega;
+	}
+	B->plane = off;
+	B->nblocks = (int)B->block_ch.size();
+	B->profile_len = poff;
+	KEL_CUDA(cudaMalloc(&B->f, sizeof(float) * 9 * B->plane));
+	KEL_CUDA(cudaMalloc(&B->rho, sizeof(float) * B->plane));
+	KEL_CUDA(cudaMalloc(&B->u, sizeof(float) * 2 * B->plane));
+	KEL_CUDA(cudaMalloc(&B->u_prev, sizeof(float) * 2 * B->plane));
+	KEL_CUDA(cudaMalloc(&B->profiles, sizeof(float) * (B->profile_len + 1)));
+	KEL_CUDA(cudaMalloc(&B->flags, B->plane));
+	KEL_CUDA(cudaMalloc(&B->d_rec, sizeof(ChannelRec) * B->n));
+	KEL_CUDA(cudaMalloc(&B->d_block_ch, sizeof(int) * B->nblocks));
+	KEL_CUDA(cudaMalloc(&B->d_active, sizeof(int) * B->n));
+	KEL_CUDA(cudaMalloc(&B->partial, sizeof(double2) * B->nblocks));
+	KEL_CUDA(cudaMalloc(&B->d_residual, sizeof(double) * B->n));
+	KEL_CUDA(cudaMemcpyAsync(B->d_rec, B->rec.data(), sizeof(ChannelRec) * B->n, cudaMemcpyHostToDevice, B->stream));
+	KEL_CUDA(cudaMemcpyAsync(B->d_block_ch, B->block_ch.data(), sizeof(int) * B->nblocks, cudaMemcpyHostToDevice,
+							 B->stream));
+	KEL_CUDA(cudaMemcpyAsync(B->profiles, B->host_profiles.data(), sizeof(float) * B->profile_len,
+							 cudaMemcpyHostToDevice, B->stream));
+	std::vector<int> ones(B->n, 1);
+	KEL_CUDA(cudaMemcpyAsync(B->d_active, ones.data(), sizeof(int) * B->n, cudaMemcpyHostToDevice, B->stream));
+	KEL_CUDA(cudaMemsetAsync(B->d_residual, 0, sizeof(double) * B->n, B->stream));
+	KEL_CUDA(cudaMemsetAsync(B->flags, 0, B->plane, B->stream));
+	BatchParams p = params(B, 0);
+	k_batch_init<<<grid_for(B->plane), 256, 0, B->stream>>>(p, B->plane);
+	KEL_CUDA(cudaGetLastError());
+	if (!B->host_flags.empty()) {
+		uint8_t *dpk = nullptr;
+		int64_t *doff = nullptr;
+		std::vector<int64_t> soff(B->n);
+		int64_t s = 0;
+		for (int c = 0; c < B->n; ++c) {
+			soff[c] = s;
+			s += B->desc[c].nx * B->desc[c].ny;
+		}
+		KEL_CUDA(cudaMalloc(&dpk, B->host_flags.size()));
+		KEL_CUDA(cudaMalloc(&doff, sizeof(int64_t) * B->n));
+		KEL_CUDA(cudaMemcpyAsync(dpk, B->host_flags.data(), B->host_flags.size(), cudaMemcpyHostToDevice, B->stream));
+		KEL_CUDA(cudaMemcpyAsync(doff, soff.data(), sizeof(int64_t) * B->n, cudaMemcpyHostToDevice, B->stream));
+		k_batch_flags<<<dim3(64, B->n), 256, 0, B->stream>>>(p, dpk, doff, B->n);
+		KEL_CUDA(cudaGetLastError());
+		KEL_CUDA(cudaStreamSynchronize(B->stream));
+		cudaFree(dpk);
+		cudaFree(doff);
+	}
+	KEL_CUDA(cudaStreamSynchronize(B->stream));
+	for (auto &tc : B->t) tc = 0;
+	return KEL_OK;
+}
+
+cudaError_t launch_sweep_batch(const kel_batch *B, bool odd, int write_macros) {
+	BatchParams p = params(B, write_macros);
+	if (B->exact) {
+		if (odd) k_batch_sweep<true, true><<<B->nblocks, B->tile, 0, B->stream>>>(p);
+		else k_batch_sweep<false, true><<<B->nblocks, B->tile, 0, B->stream>>>(p);
+	} else {
+		if (odd) k_batch_sweep<true, false><<<B->nblocks, B->tile, 0, B->stream>>>(p);
+		else k_batch_sweep<false, false><<<B->nblocks, B->tile, 0, B->stream>>>(p);
+	}
+	return cudaGetLastError();
+}
+
+cudaError_t launch_residual(const kel_batch *B, double tol) {
+	BatchParams p = params(B, 0);
+	k_batch_residual_partial<<<B->nblocks, B->tile, 0, B->stream>>>(p);
+	k_batch_residual_final<<<(B->n + 127) / 128, 128, 0, B->stream>>>(p, B->n, tol, B->d_residual);
+	return cudaGetLastError();
+}
+
+} // namespace
+
+extern "C" int kel_batch_create(int32_t n_channels, const kel_channel_desc *ch, int32_t tile, kel_batch **out) {
+	if (!out || !ch || n_channels < 1) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_create: bad arguments");
+	*out = nullptr;
+	if (tile == 0) tile = 256;
+	if (tile != 128 && tile != 256 && tile != 512)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_create: tile must be 128, 256 or 512");
+	for (int c = 0; c < n_channels; ++c) {
+		if (ch[c].nx < 3 || ch[c].ny < 3 || ch[c].nx > (1 << 20) || ch[c].ny > (1 << 20))
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_create: channel %d has bad extents", c);
+		if (!(ch[c].tau > 0.0)) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_create: channel %d tau", c);
+	}
+	kel_batch *B = new kel_batch();
+	B->n = n_channels;
+	B->desc.assign(ch, ch + n_channels);
+	B->t.assign(n_channels, 0);
+	// parabolic inlet per channel, as the single-lattice inlet profile (float)
+	for (int c = 0; c < n_channels; ++c) {
+		const int ny = (int)ch[c].ny;
+		for (int y = 0; y < ny; ++y) {
+			double eta = (y - 0.5) / (double)(ny - 2);
+			double u = (y == 0 || y == ny - 1) ? 0.0 : 4.0 * ch[c].u_max * eta * (1.0 - eta);
+			B->host_profiles.push_back((float)u);
+		}
+	}
+	if (cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking) != cudaSuccess) {
+		delete B;
+		return fail(KEL_ERR_CUDA, "kel_batch_create: stream creation failed");
+	}
+	B->own_stream = true;
+	if (cudaMalloc(&B->ops, sizeof(OpEntry) * MAX_FLAGS) != cudaSuccess) {
+		cudaStreamDestroy(B->stream);
+		delete B;
+		return fail(KEL_ERR_OUT_OF_MEMORY, "kel_batch_create: allocation failed");
+	}
+	int rc = layout(B, tile);
+	if (rc) {
+		kel_batch_destroy(B);
+		return rc;
+	}
+	*out = B;
+	return KEL_OK;
+}
+
+extern "C" int kel_batch_destroy(kel_batch *B) {
+	if (!B) return KEL_OK;
+	cudaStreamSynchronize(B->stream);
+	free_device(B);
+	cudaFree(B->ops);
+	if (B->own_stream) cudaStreamDestroy(B->stream);
+	delete B;
+	return KEL_OK;
+}
+
+extern "C" int kel_batch_upload_flags(kel_batch *B, const uint8_t *packed) {
+	if (!B || !packed) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_upload_flags: null argument");
+	int64_t total = 0;
+	for (int c = 0; c < B->n; ++c) total += B->desc[c].nx * B->desc[c].ny;
+	B->host_flags.assign(packed, packed + total);
+	return layout(B, B->tile);
+}
+
+extern "C" int kel_batch_set_program(kel_batch *B, const kel_step_program *P) {
+	if (!B || !P) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_set_program: null argument");
+	if (P->collision != KEL_COLL_BGK)
+		return fail(KEL_ERR_UNSUPPORTED, "kel_batch_set_program: channels run BGK (one tau per channel)");
+	OpEntry ops[MAX_FLAGS];
+	memset(ops, 0, sizeof(ops));
+	for (int fl = 0; fl < MAX_FLAGS; ++fl) {
+		const kel_flag_op &o = P->ops[fl];
+		if (o.bc == KEL_BC_MOVING_WALL || o.bc == KEL_BC_EQUILIBRIUM)
+			return fail(KEL_ERR_UNSUPPORTED, "kel_batch_set_program: flag %d: boundary %d not batched", fl, o.bc);
+		if (o.bc < KEL_BC_NONE || o.bc > KEL_BC_ANTI_BOUNCE_BACK)
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_set_program: flag %d: unknown boundary %d", fl, o.bc);
+		ops[fl].bc = o.bc;
+		ops[fl].collide = o.collide ? 1 : 0;
+		ops[fl].east = o.east ? 1 : 0;
+		ops[fl].use_profile = o.use_profile ? 1 : 0;
+		ops[fl].rho = (float)o.rho;
+		for (int k = 0; k < 3; ++k) ops[fl].u[k] = (float)o.u[k];
+	}
+	if (P->arithmetic != KEL_ARITH_FAST && P->arithmetic != KEL_ARITH_REFERENCE)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_set_program: unknown arithmetic");
+	B->exact = P->arithmetic == KEL_ARITH_REFERENCE;
+	KEL_CUDA(cudaMemcpyAsync(B->ops, ops, sizeof(ops), cudaMemcpyHostToDevice, B->stream));
+	KEL_CUDA(cudaStreamSynchronize(B->stream));
+	B->prog = *P;
+	B->have_ops = true;
+	if (B->graph) {
+		cudaGraphExecDestroy(B->graph);
+		B->graph = nullptr;
+	}
+	return KEL_OK;
+}
+
+static uint64_t global_t(const kel_batch *B) {
+	uint64_t t = 0;
+	for (auto v : B->t) t = v > t ? v : t;
+	return t;
+}
+
+extern "C" int kel_batch_step(kel_batch *B, uint64_t n_steps) {
+	if (!B) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_step: null batch");
+	if (!B->have_ops) return fail(KEL_ERR_STATE, "kel_batch_step: no program set");
+	std::vector<int> act(B->n);
+	KEL_CUDA(cudaMemcpyAsync(act.data(), B->d_active, sizeof(int) * B->n, cudaMemcpyDeviceToHost, B->stream));
+	KEL_CUDA(cudaStreamSynchronize(B->stream));
+	uint64_t t = global_t(B);
+	for (int c = 0; c < B->n; ++c)
+		if (act[c] && B->t[c] != t) return fail(KEL_ERR_STATE, "kel_batch_step: channel time steps diverged");
+	for (uint64_t s = 0; s < n_steps; ++s) {
+		cudaError_t e = launch_sweep_batch(B, ((t + s) & 1u) != 0, s + 1 == n_steps);
+		if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_batch_step: %s", cudaGetErrorString(e));
+	}
+	for (int c = 0; c < B->n; ++c)
+		if (act[c]) B->t[c] += n_steps;
+	KEL_CUDA(cudaStreamSynchronize(B->stream));
+	return KEL_OK;
+}
+
+// Capture `check` sweeps + the residual as one graph.
+static int build_graph(kel_batch *B, int check, double tol) {
+	if (B->graph && B->graph_check == check && B->graph_tol == tol) return KEL_OK;
+	if (B->graph) cudaGraphExecDestroy(B->graph);
+	B->graph = nullptr;
+	cudaGraph_t g;
+	KEL_CUDA(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+	cudaError_t e = cudaSuccess;
+	for (int s = 0; s < check && e == cudaSuccess; ++s) e = launch_sweep_batch(B, (s & 1) != 0, s + 1 == check);
+	if (e == cudaSuccess) e = launch_residual(B, tol);
+	cudaError_t e2 = cudaStreamEndCapture(B->stream, &g);
+	if (e != cudaSuccess || e2 != cudaSuccess)
+		return fail(KEL_ERR_CUDA, "kel_batch_run_until: graph capture failed: %s",
+					cudaGetErrorString(e != cudaSuccess ? e : e2));
+	e = cudaGraphInstantiate(&B->graph, g, 0);
+	cudaGraphDestroy(g);
+	if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_batch_run_until: instantiate: %s", cudaGetErrorString(e));
+	B->graph_check = check;
+	B->graph_tol = tol;
+	return KEL_OK;
+}
+
+extern "C" int kel_batch_run_until(kel_batch *B, double tol, uint64_t check_every, uint64_t max_steps,
+								   int32_t use_graph, uint64_t *steps_out, double *residual_out) {
+	if (!B) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_run_until: null batch");
+	if (!B->have_ops) return fail(KEL_ERR_STATE, "kel_batch_run_until: no program set");
+	if (check_every < 2 || (check_every & 1u) || check_every > 100000)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_run_until: check_every must be even, 2..100000");
+	uint64_t t0 = global_t(B);
+	if (t0 & 1u) return fail(KEL_ERR_STATE, "kel_batch_run_until: needs an even time step");
+	std::vector<int> act(B->n);
+	KEL_CUDA(cudaMemcpyAsync(act.data(), B->d_active, sizeof(int) * B->n, cudaMemcpyDeviceToHost, B->stream));
+	KEL_CUDA(cudaStreamSynchronize(B->stream));
+	int rc;
+	if (use_graph && (rc = build_graph(B, (int)check_every, tol))) return rc;
+	uint64_t done = 0;
+	int n_active = 0;
+	for (int c = 0; c < B->n; ++c) n_active += act[c] != 0;
+	while (n_active > 0 && done < max_steps) {
+		if (use_graph) {
+			KEL_CUDA(cudaGraphLaunch(B->graph, B->stream));
+		} else {
+			for (uint64_t s = 0; s < check_every; ++s) {
+				cudaError_t e = launch_sweep_batch(B, (s & 1u) != 0, s + 1 == check_every);
+				if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_batch_run_until: %s", cudaGetErrorString(e));
+			}
+			cudaError_t e = launch_residual(B, tol);
+			if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_batch_run_until: %s", cudaGetErrorString(e));
+		}
+		done += check_every;
+		for (int c = 0; c < B->n; ++c)
+			if (act[c]) B->t[c] += check_every;
+		KEL_CUDA(cudaMemcpyAsync(act.data(), B->d_active, sizeof(int) * B->n, cudaMemcpyDeviceToHost, B->stream));
+		KEL_CUDA(cudaStreamSynchronize(B->stream));
+		n_active = 0;
+		for (int c = 0; c < B->n; ++c) n_active += act[c] != 0;
+	}
+	if (steps_out)
+		for (int c = 0; c < B->n; ++c) steps_out[c] = B->t[c];
+	if (residual_out) {
+		KEL_CUDA(cudaMemcpyAsync(residual_out, B->d_residual, sizeof(double) * B->n, cudaMemcpyDeviceToHost, B->stream));
+		KEL_CUDA(cudaStreamSynchronize(B->stream));
+	}
+	return KEL_OK;
+}
+
+extern "C" int kel_batch_active_count(kel_batch *B, int32_t *count) {
+	if (!B || !count) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_active_count: null argument");
+	std::vector<int> act(B->n);
+	KEL_CUDA(cudaMemcpyAsync(act.data(), B->d_active, sizeof(int) * B->n, cudaMemcpyDeviceToHost, B->stream));
+	KEL_CUDA(cudaStreamSynchronize(B->stream));
+	int n = 0;
+	for (int c = 0; c < B->n; ++c) n += act[c] != 0;
+	*count = n;
+	return KEL_OK;
+}
+
+static int batch_download(kel_batch *B, int32_t channel, int what, float *host) {
+	if (!B || !host || channel < 0 || channel >= B->n)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_download: bad arguments");
+	const ChannelRec ch = B->rec[channel];
+	const int64_t n = (int64_t)ch.nx * ch.ny * (what == 0 ? 9 : 3);
+	float *d = nullptr;
+	KEL_CUDA(cudaMalloc(&d, sizeof(float) * n));
+	k_batch_download<<<grid_for((int64_t)ch.nx * ch.ny), 256, 0, B->stream>>>(params(B, 0), ch, (int)(B->t[channel] & 1u),
+																			  what, d);
+	cudaError_t e = cudaGetLastError();
+	if (e == cudaSuccess) e = cudaMemcpyAsync(host, d, sizeof(float) * n, cudaMemcpyDeviceToHost, B->stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+	cudaFree(d);
+	if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_batch_download: %s", cudaGetErrorString(e));
+	return KEL_OK;
+}
+
+extern "C" int kel_batch_download_populations(kel_batch *B, int32_t channel, float *host_aos) {
+	return batch_download(B, channel, 0, host_aos);
+}
+
+extern "C" int kel_batch_download_macros(kel_batch *B, int32_t channel, float *host_rho_u) {
+	return batch_download(B, channel, 1, host_rho_u);
+}
+
+extern "C" int kel_batch_channel_time_step(const kel_batch *B, int32_t channel, uint64_t *t) {
+	if (!B || !t || channel < 0 || channel >= B->n) return fail(KEL_ERR_INVALID_ARGUMENT, "bad arguments");
+	*t = B->t[channel];
+	return KEL_OK;
+}
+
+extern "C" int kel_batch_info(const kel_batch *B, int64_t *cells, int64_t *padded_cells, int32_t *tile) {
+	if (!B) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_info: null batch");
+	int64_t s = 0;
+	for (auto &d : B->desc) s += d.nx * d.ny;
+	if (cells) *cells = s;
+	if (padded_cells) *padded_cells = B->plane;
+	if (tile) *tile = B->tile;
+	return KEL_OK;
+}
+
+// Time `steps` sweeps for each candidate tile on the current flags and keep the
+// fastest; the state returns to rest equilibrium (call before stepping).
+extern "C" int kel_batch_autotune(kel_batch *B, int32_t steps, int32_t *chosen_tile, float *ms_per_step) {
+	if (!B || steps < 2) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_autotune: bad arguments");
+	if (!B->have_ops) return fail(KEL_ERR_STATE, "kel_batch_autotune: set a program first");
+	for (auto t : B->t)
+		if (t != 0) return fail(KEL_ERR_STATE, "kel_batch_autotune: only before the first step");
+	const int cand[3] = {128, 256, 512};
+	float best = 1e30f;
+	int best_tile = B->tile;
+	cudaEvent_t e0, e1;
+	KEL_CUDA(cudaEventCreate(&e0));
+	KEL_CUDA(cudaEventCreate(&e1));
+	for (int k = 0; k < 3; ++k) {
+		int rc = layout(B, cand[k]);
+		if (rc) return rc;
+		launch_sweep_batch(B, false, 0);
+		launch_sweep_batch(B, true, 0);
+		KEL_CUDA(cudaEventRecord(e0, B->stream));
+		for (int s = 0; s < steps; ++s) launch_sweep_batch(B, (s & 1) != 0, 0);
+		KEL_CUDA(cudaEventRecord(e1, B->stream));
+		KEL_CUDA(cudaEventSynchronize(e1));
+		float ms = 0.f;
+		KEL_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+		ms /= steps;
+		if (ms < best) {
+			best = ms;
+			best_tile = cand[k];
+		}
+	}
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	int rc = layout(B, best_tile);
+	if (rc) return rc;
+	if (chosen_tile) *chosen_tile = best_tile;
+	if (ms_per_step) *ms_per_step = best;
+	return KEL_OK;
+}

@@ -78,6 +78,28 @@ struct SweepParams {
 	int block;        // threads per block
 };
 
+// What the per-cell physics needs from a launch: the flag -> operation table,
+// the inlet profile and the collision constants.
+struct CellCtx {
+	const OpEntry *ops;
+	const float *profile;
+	float omega;
+	float guo_scale;
+	float g[3];
+};
+
+__device__ __forceinline__ CellCtx cell_ctx(const SweepParams &p) {
+	CellCtx c;
+	c.ops = p.ops;
+	c.profile = p.profile;
+	c.omega = p.omega;
+	c.guo_scale = p.guo_scale;
+	c.g[0] = p.g[0];
+	c.g[1] = p.g[1];
+	c.g[2] = p.g[2];
+	return c;
+}
+
 // ---------------------------------------------------------------------------
 // Arithmetic policy.  EXACT: the reference's rounding sequence (no fused
 // multiply-add, equilibrium bracket in double); otherwise plain float math.
@@ -208,28 +230,15 @@ __device__ __forceinline__ void equilibrium(float rho, const float (&u)[3], floa
 			eq[i] = __double2float_rn(__dmul_rn((double)wr, br));
 		}
 	} else {
-		// Float-float evaluation of w rho (1 + vcc - 1.5 vv + vcc^2/2) with the
-		// reference's float sub-terms (vcc, vcc^2, w rho) and a single final
-		// rounding: the correctly rounded value of the expression the reference
-		// evaluates in double, without the FP64 pipe.
-		const float h_hi = __fmul_rn(1.5f, vv);
-		const float h_lo = __fmaf_rn(1.5f, vv, -h_hi);
+		// w rho (1 + d), d = vcc + (vcc^2/2 - 1.5 vv), with the reference's float
+		// sub-terms and one fused rounding at the end.
+		const float h = __fmul_rn(1.5f, vv);
 #pragma unroll
 		for (int i = 0; i < L::Q; ++i) {
 			const float vcc = __fmul_rn(3.0f, cdot<L, true>(i, u));
-			const float ht = __fmul_rn(0.5f, __fmul_rn(vcc, vcc));
-			const float s1 = __fadd_rn(vcc, ht); // |vcc| >= |ht|: Fast2Sum
-			const float e1 = __fsub_rn(ht, __fsub_rn(s1, vcc));
-			const float s2 = __fsub_rn(s1, h_hi); // TwoSum(s1, -h_hi)
-			const float bb = __fsub_rn(s2, s1);
-			const float e2 = __fadd_rn(__fsub_rn(s1, __fsub_rn(s2, bb)), __fsub_rn(-h_hi, bb));
-			const float d_lo = __fsub_rn(__fadd_rn(e1, e2), h_lo);
+			const float d = vcc + __fmaf_rn(0.5f * vcc, vcc, -h);
 			const float wr = __fmul_rn((float)L::w(i), rho);
-			const float q_hi = __fmul_rn(wr, s2);
-			const float q_err = __fmaf_rn(wr, s2, -q_hi);
-			const float t_hi = __fadd_rn(wr, q_hi); // |wr| >= |q_hi|: Fast2Sum
-			const float t_lo = __fsub_rn(q_hi, __fsub_rn(t_hi, wr));
-			eq[i] = __fadd_rn(t_hi, __fadd_rn(__fmaf_rn(wr, d_lo, q_err), t_lo));
+			eq[i] = __fmaf_rn(wr, d, wr);
 		}
 	}
 }
@@ -359,7 +368,7 @@ __device__ __forceinline__ void zouhe_pressure_d3q27(float (&f)[27], bool east, 
 
 // The collision chosen by the program (BGK / BGKGuo / Psm / Psm + Guo).
 template <class L, int COLL, bool EXACT>
-__device__ __forceinline__ void collide(float (&f)[L::Q], const SweepParams &p, float por, const float (&Fc)[3],
+__device__ __forceinline__ void collide(float (&f)[L::Q], const CellCtx &p, float por, const float (&Fc)[3],
 										float &rho, float (&u)[3]) {
 	using A = Ar<true>;
 	moments<L, EXACT>(f, rho, u);
@@ -398,7 +407,7 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], const SweepParams &p, 
 // Boundary step + collision of one cell (the body of a driver's switch(info)).
 // Returns true when the cell collided (its moments go to the macro fields).
 template <class L, int COLL, bool EXACT>
-__device__ __forceinline__ bool cell_update(float (&f)[L::Q], int flag, int y, const SweepParams &p, float por,
+__device__ __forceinline__ bool cell_update(float (&f)[L::Q], int flag, int y, const CellCtx &p, float por,
 											const float (&Fc)[3], float &rho, float (&u)[3]) {
 	using A = Ar<true>;
 	if (flag == 0) { // outside the lattice: what the zero ghost ring supplies
@@ -533,6 +542,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ Swee
 #pragma unroll
 		for (int k = 0; k < L::D; ++k) fcv[k] = *reinterpret_cast<const float4 *>(p.force + k * p.plane + rbase + x0);
 	}
+	const CellCtx ctx = cell_ctx(p);
 	float4 rho4 = make_float4(0.f, 0.f, 0.f, 0.f);
 	float4 u4[3] = {rho4, rho4, rho4};
 	int collided = 0;
@@ -544,7 +554,7 @@ __global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ Swee
 		for (int i = 0; i < Q; ++i) c[i] = f[i][k];
 		float Fc[3] = {f4get(fcv[0], k), f4get(fcv[1], k), f4get(fcv[2], k)};
 		float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
-		const bool col = cell_update<L, COLL, EXACT>(c, flag, y, p, f4get(porv, k), Fc, rho, u);
+		const bool col = cell_update<L, COLL, EXACT>(c, flag, y, ctx, f4get(porv, k), Fc, rho, u);
 		collided |= (col ? 1 : 0) << k;
 		if (k == 0) { rho4.x = rho; u4[0].x = u[0]; u4[1].x = u[1]; u4[2].x = u[2]; }
 		if (k == 1) { rho4.y = rho; u4[0].y = u[0]; u4[1].y = u[1]; u4[2].y = u[2]; }
@@ -641,7 +651,11 @@ __global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ Swee
 // sweep_kernel, with 32-bit accesses: the x-shifted loads/stores of odd steps
 // are plain unit offsets, coalesced across the warp, and the register budget
 // (~70) leaves room for four times as many resident warps.
-// Grid: (ceil(nxp / blockDim.x), ny, nz).
+// Grid: (ceil(nxp / blockDim.x), ny, nz) -- a block never leaves its row, so
+// "the row and its y/z neighbours exist" is uniform over the block and
+// interior rows take a path with no per-direction bounds arithmetic: each
+// neighbour is the cell index plus a row offset, and only the first and last
+// cell of a row carry an x predicate.
 template <class L, int STORE, bool ODD, int COLL, bool EXACT>
 __global__ void __launch_bounds__(256) sweep1_kernel(const __grid_constant__ SweepParams p) {
 	using S = Store<STORE>;
@@ -651,20 +665,37 @@ __global__ void __launch_bounds__(256) sweep1_kernel(const __grid_constant__ Swe
 	const int y = blockIdx.y, z = blockIdx.z;
 	const int nxp = p.nxp;
 	const int64_t cell = (static_cast<int64_t>(z) * p.ny + y) * nxp + x;
+	const int64_t oy = nxp, oz = static_cast<int64_t>(nxp) * p.ny;
+	// neighbour x offsets (periodic rows wrap; nxp == nx then)
+	const bool has_xm = x > 0, has_xp = x + 1 < nxp;
+	const int xm = has_xm ? -1 : nxp - 1;     // offset of x - 1
+	const int xp = has_xp ? 1 : -(nxp - 1);   // offset of x + 1
+	const bool ok_xm = has_xm || p.periodic;  // x - 1 exists
+	const bool ok_xp = has_xp || p.periodic;  // x + 1 exists
+	const bool row_interior = y > 0 && y + 1 < p.ny && (L::D == 2 || (z > 0 && z + 1 < p.nz));
 
 	float f[Q];
+	if (!ODD) {
 #pragma unroll
-	for (int i = 0; i < Q; ++i) {
-		const float s = p.wshift[i];
-		if (!ODD) {
-			f[i] = S::ld1(p.f, i * p.plane + cell, s);
-		} else {
+		for (int i = 0; i < Q; ++i) f[i] = S::ld1(p.f, i * p.plane + cell, p.wshift[i]);
+	} else if (row_interior) {
+#pragma unroll
+		for (int i = 0; i < Q; ++i) {
+			// f_i(x) = A[opp i][x - c_i]
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int64_t off = (cx > 0 ? xm : (cx < 0 ? xp : 0)) - cy * oy - cz * oz;
+			const bool ok = cx > 0 ? ok_xm : (cx < 0 ? ok_xp : true);
+			f[i] = ok ? S::ld1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + cell + off, p.wshift[i]) : 0.f;
+		}
+	} else {
+#pragma unroll
+		for (int i = 0; i < Q; ++i) {
 			int sx = x - L::cx(i);
 			const int sy = y - L::cy(i), sz = z - L::cz(i);
 			if (p.periodic) sx = sx < 0 ? sx + nxp : (sx >= nxp ? sx - nxp : sx);
 			const bool in = sx >= 0 && sx < nxp && sy >= 0 && sy < p.ny && sz >= 0 && sz < p.nz;
 			f[i] = in ? S::ld1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane +
-									   (static_cast<int64_t>(sz) * p.ny + sy) * nxp + sx, s)
+										(static_cast<int64_t>(sz) * p.ny + sy) * nxp + sx, p.wshift[i])
 					  : 0.f;
 		}
 	}
@@ -676,30 +707,42 @@ __global__ void __launch_bounds__(256) sweep1_kernel(const __grid_constant__ Swe
 		for (int k = 0; k < L::D; ++k) Fc[k] = p.force[k * p.plane + cell];
 	}
 	float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
-	const bool col = cell_update<L, COLL, EXACT>(f, flag, y, p, por, Fc, rho, u);
+	const bool col = cell_update<L, COLL, EXACT>(f, flag, y, cell_ctx(p), por, Fc, rho, u);
 	if (p.write_macros && col) {
 		p.rho[cell] = rho;
 #pragma unroll
 		for (int k = 0; k < L::D; ++k) p.u[k * p.plane + cell] = u[k];
 	}
+	if (!ODD) {
 #pragma unroll
-	for (int i = 0; i < Q; ++i) {
-		const float s = p.wshift[i];
-		if (!ODD) {
-			S::st1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + cell, f[i], s);
-		} else {
+		for (int i = 0; i < Q; ++i) S::st1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + cell, f[i], p.wshift[i]);
+	} else if (row_interior) {
+#pragma unroll
+		for (int i = 0; i < Q; ++i) {
+			// f*_i(x) -> A[i][x + c_i]; the slot A[i][x] whose source x - c_i
+			// lies outside gets the ghost ring's zero
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int64_t pb = static_cast<int64_t>(i) * p.plane + cell;
+			if (cx > 0 && !ok_xm) S::st1(p.f, pb, 0.f, p.wshift[i]);
+			if (cx < 0 && !ok_xp) S::st1(p.f, pb, 0.f, p.wshift[i]);
+			const int64_t off = (cx > 0 ? xp : (cx < 0 ? xm : 0)) + cy * oy + cz * oz;
+			const bool ok = cx > 0 ? ok_xp : (cx < 0 ? ok_xm : true);
+			if (ok) S::st1(p.f, pb + off, f[i], p.wshift[i]);
+		}
+	} else {
+#pragma unroll
+		for (int i = 0; i < Q; ++i) {
 			const int64_t pb = static_cast<int64_t>(i) * p.plane;
-			// this cell's slot whose source lies outside: the ghost ring's zero
 			{
 				const int sx = x - L::cx(i), sy = y - L::cy(i), sz = z - L::cz(i);
 				const bool out_x = !p.periodic && (sx < 0 || sx >= nxp);
-				if (out_x || sy < 0 || sy >= p.ny || sz < 0 || sz >= p.nz) S::st1(p.f, pb + cell, 0.f, s);
+				if (out_x || sy < 0 || sy >= p.ny || sz < 0 || sz >= p.nz) S::st1(p.f, pb + cell, 0.f, p.wshift[i]);
 			}
 			int dx = x + L::cx(i);
 			const int dy = y + L::cy(i), dz = z + L::cz(i);
 			if (p.periodic) dx = dx < 0 ? dx + nxp : (dx >= nxp ? dx - nxp : dx);
 			if (dx >= 0 && dx < nxp && dy >= 0 && dy < p.ny && dz >= 0 && dz < p.nz)
-				S::st1(p.f, pb + (static_cast<int64_t>(dz) * p.ny + dy) * nxp + dx, f[i], s);
+				S::st1(p.f, pb + (static_cast<int64_t>(dz) * p.ny + dy) * nxp + dx, f[i], p.wshift[i]);
 		}
 	}
 }

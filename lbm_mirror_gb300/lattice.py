@@ -314,3 +314,76 @@ class Particles:
     def step(self, params, program, n_steps=1, write_macros=True):
         fl = K.KEL_STEP_WRITE_MACROS if write_macros else 0
         _check(self.lib.kel_particles_step(self._h, C.byref(params), C.byref(program), n_steps, fl), self.lib)
+
+
+class Batch:
+    """Many independent D2Q9 channels of uneven size in one launch
+    (C ABI kel_batch_*).  ``channels``: dicts with nx, ny, tau, u_max, flags."""
+
+    def __init__(self, channels, program, tile=0):
+        self.lib = K.load_library()
+        self.n = len(channels)
+        arr = (K.ChannelDesc * self.n)()
+        for a, c in zip(arr, channels):
+            a.nx, a.ny, a.tau, a.u_max = int(c["nx"]), int(c["ny"]), float(c["tau"]), float(c["u_max"])
+        h = C.c_void_p()
+        _check(self.lib.kel_batch_create(self.n, arr, int(tile), C.byref(h)), self.lib)
+        self._h = h
+        self.dims = [(int(c["nx"]), int(c["ny"])) for c in channels]
+        packed = np.concatenate([np.ascontiguousarray(c["flags"], dtype=np.uint8).reshape(-1) for c in channels])
+        _check(self.lib.kel_batch_upload_flags(self._h, _ptr(packed)), self.lib)
+        _check(self.lib.kel_batch_set_program(self._h, C.byref(program)), self.lib)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.kel_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def autotune(self, steps=6):
+        t, ms = C.c_int32(), C.c_float()
+        _check(self.lib.kel_batch_autotune(self._h, steps, C.byref(t), C.byref(ms)), self.lib)
+        return t.value, ms.value
+
+    def step(self, n=1):
+        _check(self.lib.kel_batch_step(self._h, n), self.lib)
+
+    def run_until(self, tol=1e-6, check_every=1000, max_steps=10**7, use_graph=True):
+        steps = np.zeros(self.n, dtype=np.uint64)
+        res = np.zeros(self.n, dtype=np.float64)
+        _check(self.lib.kel_batch_run_until(self._h, tol, check_every, max_steps, int(use_graph), _ptr(steps),
+                                            _ptr(res)), self.lib)
+        return steps, res
+
+    def active_count(self):
+        v = C.c_int32()
+        _check(self.lib.kel_batch_active_count(self._h, C.byref(v)), self.lib)
+        return v.value
+
+    def info(self):
+        a, b, t = C.c_int64(), C.c_int64(), C.c_int32()
+        _check(self.lib.kel_batch_info(self._h, C.byref(a), C.byref(b), C.byref(t)), self.lib)
+        return a.value, b.value, t.value
+
+    def time_step(self, channel):
+        v = C.c_uint64()
+        _check(self.lib.kel_batch_channel_time_step(self._h, channel, C.byref(v)), self.lib)
+        return v.value
+
+    def populations(self, channel):
+        nx, ny = self.dims[channel]
+        out = np.empty(nx * ny * 9, dtype=np.float32)
+        _check(self.lib.kel_batch_download_populations(self._h, channel, _ptr(out)), self.lib)
+        return out.reshape(nx * ny, 9)
+
+    def macros(self, channel):
+        nx, ny = self.dims[channel]
+        out = np.empty(nx * ny * 3, dtype=np.float32)
+        _check(self.lib.kel_batch_download_macros(self._h, channel, _ptr(out)), self.lib)
+        out = out.reshape(nx * ny, 3)
+        return out[:, 0].copy(), out[:, 1:3].copy()

@@ -205,3 +205,55 @@ def run_oracle(case):
     lat.run(case["program"], case["steps"])
     rho, vel = lat.macros()
     return lat.populations(), rho, vel
+
+
+def channel_geometry(nx, ny, rng):
+    """One config-C4 channel: rim walls, inlet 3 at x = 0, outlet 4 at
+    x = nx-1, and 1..8 seeded obstacles (disks r in [3, 12] or axis-aligned
+    rectangles) kept clear of the inlet/outlet columns and of the channel
+    height, so that the channel never closes."""
+    x, y, _ = cell_grid((nx, ny))
+    f = channel_flags((nx, ny))
+    n_obs = int(rng.integers(1, 9))
+    for _ in range(n_obs):
+        if rng.uniform() < 0.5:
+            r = float(rng.uniform(3.0, 12.0))
+            r = min(r, (ny - 6) / 2.0 - 1.0)
+            cx = float(rng.uniform(r + 6, nx - r - 6))
+            cy = float(rng.uniform(r + 1, ny - r - 2))
+            solid = (x - cx) ** 2 + (y - cy) ** 2 <= r * r
+        else:
+            w = int(rng.integers(2, max(3, nx // 8)))
+            h = int(rng.integers(2, max(3, ny // 2)))
+            x0 = int(rng.integers(6, max(7, nx - w - 6)))
+            y0 = int(rng.integers(1, max(2, ny - h - 1)))
+            solid = (x >= x0) & (x < x0 + w) & (y >= y0) & (y < y0 + h)
+        f[solid & (x > 2) & (x < nx - 3)] = 1
+    return f
+
+
+def batch_channels(n=1024, seed=4, nx_range=(64, 512), ny_range=(32, 128)):
+    """Config C4: n independent D2Q9 channels of uneven size, u_max ~ U[0.01,
+    0.08], tau ~ U[0.55, 1.0].  Returns a list of dicts (nx, ny, tau, u_max,
+    flags, profile)."""
+    rng = np.random.default_rng(SEED + 1000 + seed)
+    out = []
+    for _ in range(n):
+        nx = int(rng.integers(nx_range[0], nx_range[1] + 1))
+        ny = int(rng.integers(ny_range[0], ny_range[1] + 1))
+        u_max = float(rng.uniform(0.01, 0.08))
+        tau = float(rng.uniform(0.55, 1.0))
+        out.append(dict(nx=nx, ny=ny, tau=tau, u_max=u_max, flags=channel_geometry(nx, ny, rng),
+                        profile=parabolic_profile(ny, u_max)))
+    return out
+
+
+def channel_program(tau, arithmetic=K.KEL_ARITH_FAST):
+    """The per-flag program of a C4 channel (the stdkr_2d_bgk switch)."""
+    ops = {
+        1: dict(bc=K.KEL_BC_BOUNCE_BACK),
+        2: dict(bc=K.KEL_BC_FLUID, collide=1),
+        3: dict(bc=K.KEL_BC_ZOUHE_VELOCITY_X, collide=1, east=1, use_profile=1),
+        4: dict(bc=K.KEL_BC_ZOUHE_PRESSURE_X, collide=1, east=0, rho=1.0),
+    }
+    return K.make_program(tau, K.KEL_COLL_BGK, ops, arithmetic=arithmetic)
