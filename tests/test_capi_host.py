@@ -61,3 +61,11 @@ def test_program_dict_round_trip():
     d = K.program_to_dict(c["program"])
     p2 = K.program_from_dict(d)
     assert bytes(p2) == bytes(c["program"])
+
+
+def test_cpp_facade_driver_compiles_and_links(tmp_path):
+    """The reference-style C++ driver builds against the header-only face and
+    links the CUDA library (running it needs a GPU: tests/test_cpp_facade.py)."""
+    from tests.cpp_driver import build_driver
+    exe = build_driver(str(tmp_path))
+    assert os.path.exists(exe)
