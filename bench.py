@@ -262,13 +262,16 @@ def main():
     ncell = int(np.prod(dims))
     stream = torch.cuda.Stream()
     lat = Lattice(QNAME[q], dims, storage=args.storage, stream=stream.cuda_stream)
-    if args.cpt:
-        lat.set_launch(args.cpt, args.block)
-    cpt, block = lat.launch()
     lat.upload_flags(case["flags"])
     if case["profile"] is not None:
         lat.upload_inlet_profile(case["profile"])
     prog = case["program"]
+    if args.cpt:
+        lat.set_launch(args.cpt, args.block)
+        tuned = None
+    else:
+        tuned = lat.autotune(prog, steps=8)  # the project's launch-shape autotuner
+    cpt, block = lat.launch()
 
     # ---- device-resident throughput (value) and per-launch duration -------
     lat.step(prog, args.warmup, write_macros=False)
@@ -339,7 +342,8 @@ def main():
         "data": "synthetic",
         "config": {"workload": args.workload, "descriptor": f"D{D}Q{Q}", "dims": list(dims), "cells": ncell,
                    "storage": args.storage, "tau": float(prog.tau), "collision": "BGK", "arithmetic": "fast",
-                   "scheme": "AA in-place, SoA", "cells_per_thread": cpt, "block": block, "l2": "populations 1.27 GB >> 129 MB L2, no flush needed"
+                   "scheme": "AA in-place, SoA", "cells_per_thread": cpt, "block": block,
+                   "autotuned": tuned is not None, "l2": "populations 1.27 GB >> 129 MB L2, no flush needed"
                    if ncell * Q * 4 > 4e8 else "working set smaller than L2",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -253,6 +253,11 @@ int kel_batch_download_macros(kel_batch *b, int32_t channel, float *host_rho_u);
  * or 256).  Results do not depend on it. */
 int kel_lattice_set_launch(kel_lattice *lat, int32_t cells_per_thread, int32_t block_threads);
 int kel_lattice_get_launch(const kel_lattice *lat, int32_t *cells_per_thread, int32_t *block_threads);
+/* Time `steps` sweeps of `prog` with every launch shape on the lattice's
+ * current state and keep the fastest.  The populations are restored after
+ * each trial and the time step does not advance. */
+int kel_lattice_autotune(kel_lattice *lat, const kel_step_program *prog, int32_t steps, int32_t *cells_per_thread,
+						 int32_t *block_threads, float *ms_per_step);
 
 /* Synchronise the lattice's stream. */
 int kel_lattice_synchronize(kel_lattice *lat);

@@ -236,6 +236,8 @@ def load_library(path: str | None = None):
         "kel_batch_download_populations": ([vp, i32, vp], C.c_int),
         "kel_batch_download_macros": ([vp, i32, vp], C.c_int),
         "kel_lattice_get_launch": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
+        "kel_lattice_autotune": ([vp, C.POINTER(StepProgram), i32, C.POINTER(i32), C.POINTER(i32),
+                                  C.POINTER(C.c_float)], C.c_int),
         "kel_particles_create": ([vp, i32, C.POINTER(vp)], C.c_int),
         "kel_particles_destroy": ([vp], C.c_int),
         "kel_particles_upload": ([vp, vp], C.c_int),

@@ -525,24 +525,7 @@ extern "C" int kel_lattice_get_launch(const kel_lattice *L, int32_t *cells_per_t
 	return KEL_OK;
 }
 
-extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_steps, uint32_t step_flags) {
-	if (!L || !P) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: null argument");
-	if (step_flags & ~(KEL_STEP_WRITE_MACROS | KEL_STEP_ALL_MACROS))
-		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown step flags");
-	int rc;
-	if (!L->have_ops || memcmp(&L->last_prog, P, sizeof(*P)) != 0) {
-		OpEntry ops[MAX_FLAGS];
-		if ((rc = lower_program(L, P, ops))) return rc;
-		KEL_CUDA(cudaMemcpyAsync(L->ops, ops, sizeof(ops), cudaMemcpyHostToDevice, L->stream));
-		KEL_CUDA(cudaStreamSynchronize(L->stream));
-		L->last_prog = *P;
-		L->have_ops = true;
-	}
-	const bool psm = P->collision == KEL_COLL_PSM || P->collision == KEL_COLL_PSM_GUO;
-	const bool guo = P->collision == KEL_COLL_BGK_GUO || P->collision == KEL_COLL_PSM_GUO;
-	if (psm && (rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
-	if (guo && (rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
-
+static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	SweepParams p;
 	memset(&p, 0, sizeof(p));
 	p.f = L->f;
@@ -567,6 +550,88 @@ extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_st
 	for (int i = 0; i < 27; ++i) p.wshift[i] = L->wshift[i];
 	p.cpt = L->cpt;
 	p.block = L->block;
+	return p;
+}
+
+
+// Time every supported launch shape on the lattice's own state, then put the
+// state back: the populations are saved to a scratch copy first and restored
+// after each trial, macros are not written, the time step does not move.
+extern "C" int kel_lattice_autotune(kel_lattice *L, const kel_step_program *P, int32_t steps, int32_t *cells_per_thread,
+									int32_t *block_threads, float *ms_per_step) {
+	if (!L || !P || steps < 2) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_autotune: bad arguments");
+	int rc;
+	if ((rc = kel_step(L, P, 0, 0))) return rc; // validates and uploads the program
+	const bool psm = P->collision == KEL_COLL_PSM || P->collision == KEL_COLL_PSM_GUO;
+	const bool guo = P->collision == KEL_COLL_BGK_GUO || P->collision == KEL_COLL_PSM_GUO;
+	if (psm && (rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
+	if (guo && (rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
+	const size_t bytes = (size_t)L->d.Q * L->plane * L->elem;
+	void *save = nullptr;
+	KEL_CUDA(cudaMalloc(&save, bytes));
+	cudaEvent_t e0, e1;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	const int cands[6][2] = {{1, 64}, {1, 128}, {1, 256}, {4, 64}, {4, 128}, {4, 256}};
+	float best = 1e30f;
+	int bc = L->cpt, bb = L->block;
+	cudaError_t e = cudaMemcpyAsync(save, L->f, bytes, cudaMemcpyDeviceToDevice, L->stream);
+	SweepParams p = make_params(L, P);
+	p.write_macros = 0;
+	const bool exact = P->arithmetic == KEL_ARITH_REFERENCE;
+	for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
+		if (!launch_ok(L, cands[k][0], cands[k][1])) continue;
+		p.cpt = cands[k][0];
+		p.block = cands[k][1];
+		const bool odd0 = (L->t & 1u) != 0;
+		for (int s = 0; s < 2 && e == cudaSuccess; ++s) e = launch_one(L, p, P->collision, exact, odd0 != (s & 1));
+		cudaEventRecord(e0, L->stream);
+		for (int s = 0; s < steps && e == cudaSuccess; ++s) e = launch_one(L, p, P->collision, exact, odd0 != (s & 1));
+		cudaEventRecord(e1, L->stream);
+		if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+		float ms = 0.f;
+		cudaEventElapsedTime(&ms, e0, e1);
+		ms /= steps;
+		if (ms < best) {
+			best = ms;
+			bc = cands[k][0];
+			bb = cands[k][1];
+		}
+		if (e == cudaSuccess) e = cudaMemcpyAsync(L->f, save, bytes, cudaMemcpyDeviceToDevice, L->stream);
+	}
+	if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	cudaFree(save);
+	if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_lattice_autotune: %s", cudaGetErrorString(e));
+	L->cpt = bc;
+	L->block = bb;
+	L->tuned = true;
+	if (cells_per_thread) *cells_per_thread = bc;
+	if (block_threads) *block_threads = bb;
+	if (ms_per_step) *ms_per_step = best;
+	return KEL_OK;
+}
+
+extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_steps, uint32_t step_flags) {
+	if (!L || !P) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: null argument");
+	if (step_flags & ~(KEL_STEP_WRITE_MACROS | KEL_STEP_ALL_MACROS))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown step flags");
+	int rc;
+	if (!L->have_ops || memcmp(&L->last_prog, P, sizeof(*P)) != 0) {
+		OpEntry ops[MAX_FLAGS];
+		if ((rc = lower_program(L, P, ops))) return rc;
+		KEL_CUDA(cudaMemcpyAsync(L->ops, ops, sizeof(ops), cudaMemcpyHostToDevice, L->stream));
+		KEL_CUDA(cudaStreamSynchronize(L->stream));
+		L->last_prog = *P;
+		L->have_ops = true;
+	}
+	const bool psm = P->collision == KEL_COLL_PSM || P->collision == KEL_COLL_PSM_GUO;
+	const bool guo = P->collision == KEL_COLL_BGK_GUO || P->collision == KEL_COLL_PSM_GUO;
+	if (psm && (rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
+	if (guo && (rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
+
+	SweepParams p = make_params(L, P);
 	const bool exact = P->arithmetic == KEL_ARITH_REFERENCE;
 	for (uint64_t s = 0; s < n_steps; ++s) {
 		p.write_macros = (step_flags & KEL_STEP_ALL_MACROS) || ((step_flags & KEL_STEP_WRITE_MACROS) && s + 1 == n_steps);

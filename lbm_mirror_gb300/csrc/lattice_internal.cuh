@@ -59,6 +59,6 @@ struct kel_lattice {
 	kel_step_program last_prog;
 	int device = 0;
 	int cpt = 1;      // cells per thread of the sweep launch (1 or 4)
-	int block = 256;  // threads per block of the sweep launch
+	int block = 128;  // threads per block of the sweep launch
 	bool tuned = false;
 };

@@ -249,6 +249,14 @@ class Lattice:
     def set_launch(self, cells_per_thread, block_threads=256):
         _check(self.lib.kel_lattice_set_launch(self._h, cells_per_thread, block_threads), self.lib)
 
+    def autotune(self, program, steps=6):
+        """Time every launch shape on the current state (restored after each
+        trial) and keep the fastest; returns (cells_per_thread, block, ms)."""
+        a, b, ms = C.c_int32(), C.c_int32(), C.c_float()
+        _check(self.lib.kel_lattice_autotune(self._h, C.byref(program), steps, C.byref(a), C.byref(b), C.byref(ms)),
+               self.lib)
+        return a.value, b.value, ms.value
+
     def launch(self):
         a, b = C.c_int32(), C.c_int32()
         _check(self.lib.kel_lattice_get_launch(self._h, C.byref(a), C.byref(b)), self.lib)

@@ -218,7 +218,7 @@ def channel_geometry(nx, ny, rng):
     for _ in range(n_obs):
         if rng.uniform() < 0.5:
             r = float(rng.uniform(3.0, 12.0))
-            r = min(r, (ny - 6) / 2.0 - 1.0)
+            r = max(1.5, min(r, (ny - 6) / 2.0 - 1.0, (nx - 14) / 2.0))
             cx = float(rng.uniform(r + 6, nx - r - 6))
             cy = float(rng.uniform(r + 1, ny - r - 2))
             solid = (x - cx) ** 2 + (y - cy) ** 2 <= r * r

@@ -172,3 +172,18 @@ def test_invalid_arguments_return_errors():
     with pytest.raises(KelError):
         lat.set_launch(1, 100)
     lat.close()
+
+
+def test_autotune_restores_state_and_keeps_results():
+    case, dfs, rho, vel = G.load("cavity_d3q19")
+    prog = with_arith(case["program"], K.KEL_ARITH_REFERENCE)
+    lat = make_lattice(case)
+    lat.step(prog, 7)
+    before = lat.populations(np.float64)
+    t = lat.t
+    cpt, block, ms = lat.autotune(prog, steps=4)
+    assert (cpt, block) in [(1, 64), (1, 128), (1, 256), (4, 64), (4, 128), (4, 256)] and ms > 0
+    assert lat.t == t and lat.launch() == (cpt, block)
+    np.testing.assert_array_equal(lat.populations(np.float64), before)
+    lat.step(prog, case["steps"] - 7)
+    np.testing.assert_array_equal(lat.populations(np.float64), dfs)
