@@ -257,3 +257,37 @@ def channel_program(tau, arithmetic=K.KEL_ARITH_FAST):
         4: dict(bc=K.KEL_BC_ZOUHE_PRESSURE_X, collide=1, east=0, rho=1.0),
     }
     return K.make_program(tau, K.KEL_COLL_BGK, ops, arithmetic=arithmetic)
+
+
+def particle_channel(nx=2048, ny=512, n_particles=64, radius=8.0, density=1.5, seed=3):
+    """Config C3: periodic-x channel with walls at y = 0 and y = ny-1 and
+    n_particles discs of radius R placed by seeded uniform rejection sampling
+    (no overlap, at least one cell between discs and from the walls), at rest.
+    Returns (flags, states (P, 28))."""
+    rng = np.random.default_rng(SEED + 3000 + seed)
+    x, y, _ = cell_grid((nx, ny))
+    flags = np.full(nx * ny, 2, dtype=np.uint8)
+    flags[(y == 0) | (y == ny - 1)] = 1
+    pos = []
+    while len(pos) < n_particles:
+        px = rng.uniform(0.0, nx)
+        py = rng.uniform(radius + 2.0, ny - 1 - radius - 2.0)
+        ok = True
+        for (qx, qy) in pos:
+            dx = abs(px - qx)
+            dx = min(dx, nx - dx)
+            if dx * dx + (py - qy) ** 2 < (2 * radius + 1.0) ** 2:
+                ok = False
+                break
+        if ok:
+            pos.append((px, py))
+    st = np.zeros((n_particles, 28))
+    m = np.pi * radius * radius * density
+    for i, (px, py) in enumerate(pos):
+        st[i, 0:2] = (px, py)
+        st[i, 3:5] = (px, py)
+        st[i, 24] = m
+        st[i, 25] = 0.5 * m * radius * radius
+        st[i, 26] = radius
+        st[i, 27] = density
+    return flags, st
