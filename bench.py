@@ -37,6 +37,7 @@ WORKLOADS = {
     "d3q19_cavity_256": (19, (256, 256, 256), 0.55, "cavity"),
     "d3q27_cavity_256": (27, (256, 256, 256), 0.55, "cavity"),
     "d3q19_cavity_128": (19, (128, 128, 128), 0.55, "cavity"),
+    "d3q19_cavity_192": (19, (192, 192, 192), 0.55, "cavity"),
     "d2q9_poiseuille_256x64": (9, (256, 64), 0.8, "poiseuille"),
     "d2q9_channel_4096x4096": (9, (4096, 4096), 0.8, "poiseuille"),
     "d2q9_batch_1024": (9, None, None, "batch"),
