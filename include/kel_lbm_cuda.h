@@ -248,6 +248,39 @@ int kel_batch_info(const kel_batch *b, int64_t *cells, int64_t *padded_cells, in
 int kel_batch_download_populations(kel_batch *b, int32_t channel, float *host_aos);
 int kel_batch_download_macros(kel_batch *b, int32_t channel, float *host_rho_u);
 
+/* ---- learned warm start: conv U-Net (no counterpart in the reference) -- */
+
+typedef struct kel_unet_desc {
+	int32_t height, width;  /* grid (multiples of 8) */
+	int32_t in_channels;    /* 16: mask, u_max, tau planes, zero padding */
+	int32_t out_channels;   /* 3: u_x, u_y, rho (scaled) */
+	int32_t widths[4];      /* channels per level, multiples of 16 (32, 64, 128, 128) */
+	int32_t max_batch;
+	int32_t reserved;
+} kel_unet_desc;
+
+typedef struct kel_unet kel_unet;
+
+/* He-uniform initialisation from `seed`; FP32 master weights, bf16 copies. */
+int kel_unet_create(const kel_unet_desc *desc, uint64_t seed, kel_unet **out);
+int kel_unet_destroy(kel_unet *net);
+int kel_unet_param_count(const kel_unet *net, int64_t *n);
+int kel_unet_get_params(kel_unet *net, float *host);
+int kel_unet_set_params(kel_unet *net, const float *host);
+int kel_unet_get_grads(kel_unet *net, float *host);
+int kel_unet_set_stream(kel_unet *net, void *stream);
+int kel_unet_synchronize(kel_unet *net);
+/* Input planes from device data: mask (n*H*W bytes), u_max and tau (n floats each). */
+int kel_unet_make_input(kel_unet *net, const uint8_t *d_mask, const float *d_umax, const float *d_tau, int32_t n);
+/* Input directly: bf16 NHWC, 16 channels (device pointer). */
+int kel_unet_set_input(kel_unet *net, const uint16_t *d_input_bf16, int32_t n);
+/* Forward pass; d_out (device, may be NULL) receives n*H*W*out_channels floats (NHWC). */
+int kel_unet_forward(kel_unet *net, int32_t n, float *d_out);
+/* After a forward with the same n: loss = mean (y - target)^2 and every
+ * parameter gradient (FP32, overwritten).  *loss is written on the host. */
+int kel_unet_backward(kel_unet *net, const float *d_target, int32_t n, double *loss);
+int kel_unet_adam_step(kel_unet *net, float lr, float beta1, float beta2, float eps, int32_t step);
+
 /* Launch shape of the sweep: cells per thread (1: 32-bit accesses, one cell;
  * 4: 128-bit accesses, four consecutive cells) and threads per block (64, 128
  * or 256).  Results do not depend on it. */

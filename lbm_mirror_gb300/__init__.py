@@ -4,8 +4,8 @@ The compute path is libkel_lbm_cuda.so (hand-written sm_103a CUDA kernels behind
 the C ABI of include/kel_lbm_cuda.h); this package is the Python host mirror.
 """
 from . import capi
-from .lattice import (BGK, Batch, AntiBounceBack, BGKGuo, BounceBack, Equilibrium, KelError, Lattice, MovingWall, Particles, Psm,
+from .lattice import (BGK, Batch, UNet, AntiBounceBack, BGKGuo, BounceBack, Equilibrium, KelError, Lattice, MovingWall, Particles, Psm,
                       PsmGuo, ZouHePressureX, ZouHeVelocityX, program_from_switch)
 
-__all__ = ["capi", "Lattice", "Particles", "Batch", "KelError", "program_from_switch", "BGK", "BGKGuo", "Psm", "PsmGuo", "BounceBack",
+__all__ = ["capi", "Lattice", "Particles", "Batch", "UNet", "KelError", "program_from_switch", "BGK", "BGKGuo", "Psm", "PsmGuo", "BounceBack",
            "AntiBounceBack", "Equilibrium", "ZouHePressureX", "ZouHeVelocityX", "MovingWall"]

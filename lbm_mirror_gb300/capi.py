@@ -189,6 +189,12 @@ def states_from_array(a):
     return arr
 
 
+class UnetDesc(C.Structure):
+    _fields_ = [("height", C.c_int32), ("width", C.c_int32), ("in_channels", C.c_int32),
+                ("out_channels", C.c_int32), ("widths", C.c_int32 * 4), ("max_batch", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
 class ChannelDesc(C.Structure):
     _fields_ = [("nx", C.c_int64), ("ny", C.c_int64), ("tau", C.c_double), ("u_max", C.c_double)]
 
@@ -224,6 +230,19 @@ def load_library(path: str | None = None):
         "kel_lattice_synchronize": ([vp], C.c_int),
         "kel_lattice_set_launch": ([vp, i32, i32], C.c_int),
         "kel_batch_create": ([i32, C.POINTER(ChannelDesc), i32, C.POINTER(vp)], C.c_int),
+        "kel_unet_create": ([C.POINTER(UnetDesc), u64, C.POINTER(vp)], C.c_int),
+        "kel_unet_destroy": ([vp], C.c_int),
+        "kel_unet_param_count": ([vp, C.POINTER(i64)], C.c_int),
+        "kel_unet_get_params": ([vp, vp], C.c_int),
+        "kel_unet_set_params": ([vp, vp], C.c_int),
+        "kel_unet_get_grads": ([vp, vp], C.c_int),
+        "kel_unet_set_stream": ([vp, vp], C.c_int),
+        "kel_unet_synchronize": ([vp], C.c_int),
+        "kel_unet_make_input": ([vp, vp, vp, vp, i32], C.c_int),
+        "kel_unet_set_input": ([vp, vp, i32], C.c_int),
+        "kel_unet_forward": ([vp, i32, vp], C.c_int),
+        "kel_unet_backward": ([vp, vp, i32, C.POINTER(C.c_double)], C.c_int),
+        "kel_unet_adam_step": ([vp, C.c_float, C.c_float, C.c_float, C.c_float, i32], C.c_int),
         "kel_batch_destroy": ([vp], C.c_int),
         "kel_batch_upload_flags": ([vp, vp], C.c_int),
         "kel_batch_set_program": ([vp, C.POINTER(StepProgram)], C.c_int),

@@ -1,0 +1,877 @@
+// Warm-start U-Net: training and inference kernels (C ABI kel_unet_*).
+//
+// No counterpart in keldu/lbm_mirror (it has no learned component).  The
+// network maps an obstacle mask and the inlet amplitude / relaxation time of
+// a channel to (u_x, u_y, rho) on the lattice, which initialises the LBM.
+//
+// Layout: activations NHWC in bf16, channels a multiple of 16 (the input is
+// padded to 16); conv weights [c_out][ky][kx][c_in] with an FP32 master copy,
+// a bf16 copy for the forward GEMM and a flipped/transposed bf16 copy
+// [c_in][2-ky][2-kx][c_out] for the data gradient.  Architecture as in
+// oracle/unet_oracle.py (4 levels, concat skips, 1x1 head).
+//
+// Tensor-core GEMMs (bf16 in, FP32 accumulate, mma.sync m16n8k16):
+//   conv_igemm  implicit GEMM, M = pixels, N = c_out, K = 9 c_in; also the
+//               data gradient (same kernel on dY with the flipped weights);
+//               bias + ReLU fused into the epilogue;
+//   conv_wgrad  M = c_out, N = 9 c_in, K = pixels, split over pixel chunks
+//               into FP32 partial sums, reduced in fixed order (deterministic).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lattice_internal.cuh"
+
+using namespace kel::gb;
+
+namespace {
+
+typedef __nv_bfloat16 bf16;
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], const uint32_t (&b)[2]) {
+	asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+				 "{%0,%1,%2,%3};\n"
+				 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+				 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// ---- implicit-GEMM 3x3 convolution (forward and data gradient) -----------------
+
+constexpr int CB_M = 64, CB_N = 64, CB_K = 16, CPAD = 24; // tile + padded row pitch (bf16)
+
+struct ConvArgs {
+	const bf16 *x; // (N,H,W,Ci)
+	const bf16 *w; // (Co,3,3,Ci)
+	const float *bias;
+	bf16 *y;       // (N,H,W,Co)
+	int N, H, W, Ci, Co;
+	int relu, use_bias;
+};
+
+__global__ void __launch_bounds__(128) conv_igemm(ConvArgs a) {
+	__shared__ __align__(16) bf16 As[2][CB_M][CPAD];
+	__shared__ __align__(16) bf16 Bs[2][CB_N][CPAD];
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int wm = warp >> 1, wn = warp & 1;
+	const int g = lane >> 2, t = lane & 3;
+	const int64_t M = (int64_t)a.N * a.H * a.W;
+	const int64_t m0 = (int64_t)blockIdx.x * CB_M;
+	const int n0 = blockIdx.y * CB_N;
+	const int K = 9 * a.Ci;
+	const int ksteps = K / CB_K;
+	// this thread's load slots: one 16-byte vector of A and one of B per k-step
+	const int lrow = tid >> 1, lhalf = tid & 1;
+	const int64_t lm = m0 + lrow;
+	int ln = 0, ly = 0, lx = 0;
+	if (lm < M) {
+		ln = (int)(lm / ((int64_t)a.H * a.W));
+		const int r = (int)(lm - (int64_t)ln * a.H * a.W);
+		ly = r / a.W;
+		lx = r - ly * a.W;
+	}
+	const int lco = n0 + lrow;
+	auto load_a = [&](int ks) -> uint4 {
+		const int k0 = ks * CB_K;
+		const int tap = k0 / a.Ci, ci0 = k0 - tap * a.Ci + lhalf * 8;
+		const int yy = ly + tap / 3 - 1, xx = lx + tap % 3 - 1;
+		uint4 v = make_uint4(0, 0, 0, 0);
+		if (lm < M && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W)
+			v = *reinterpret_cast<const uint4 *>(a.x + (((int64_t)ln * a.H + yy) * a.W + xx) * a.Ci + ci0);
+		return v;
+	};
+	auto load_b = [&](int ks) -> uint4 {
+		uint4 v = make_uint4(0, 0, 0, 0);
+		if (lco < a.Co) v = *reinterpret_cast<const uint4 *>(a.w + (int64_t)lco * K + ks * CB_K + lhalf * 8);
+		return v;
+	};
+	float acc[2][4][4];
+#pragma unroll
+	for (int i = 0; i < 2; ++i)
+#pragma unroll
+		for (int j = 0; j < 4; ++j)
+#pragma unroll
+			for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+	uint4 ra = load_a(0), rb = load_b(0);
+	*reinterpret_cast<uint4 *>(&As[0][lrow][lhalf * 8]) = ra;
+	*reinterpret_cast<uint4 *>(&Bs[0][lrow][lhalf * 8]) = rb;
+	__syncthreads();
+	for (int ks = 0; ks < ksteps; ++ks) {
+		const int cur = ks & 1;
+		if (ks + 1 < ksteps) {
+			ra = load_a(ks + 1);
+			rb = load_b(ks + 1);
+		}
+		uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+		for (int i = 0; i < 2; ++i) {
+			const int r = wm * 32 + i * 16 + g;
+			af[i][0] = *reinterpret_cast<const uint32_t *>(&As[cur][r][2 * t]);
+			af[i][1] = *reinterpret_cast<const uint32_t *>(&As[cur][r + 8][2 * t]);
+			af[i][2] = *reinterpret_cast<const uint32_t *>(&As[cur][r][2 * t + 8]);
+			af[i][3] = *reinterpret_cast<const uint32_t *>(&As[cur][r + 8][2 * t + 8]);
+		}
+#pragma unroll
+		for (int j = 0; j < 4; ++j) {
+			const int c = wn * 32 + j * 8 + g;
+			bfr[j][0] = *reinterpret_cast<const uint32_t *>(&Bs[cur][c][2 * t]);
+			bfr[j][1] = *reinterpret_cast<const uint32_t *>(&Bs[cur][c][2 * t + 8]);
+		}
+#pragma unroll
+		for (int i = 0; i < 2; ++i)
+#pragma unroll
+			for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+		if (ks + 1 < ksteps) {
+			*reinterpret_cast<uint4 *>(&As[cur ^ 1][lrow][lhalf * 8]) = ra;
+			*reinterpret_cast<uint4 *>(&Bs[cur ^ 1][lrow][lhalf * 8]) = rb;
+		}
+		__syncthreads();
+	}
+	// epilogue: bias, ReLU, bf16 store
+#pragma unroll
+	for (int i = 0; i < 2; ++i) {
+#pragma unroll
+		for (int j = 0; j < 4; ++j) {
+			const int co = n0 + wn * 32 + j * 8 + 2 * t;
+			if (co >= a.Co) continue;
+			const float b0 = a.use_bias ? a.bias[co] : 0.f, b1 = a.use_bias ? a.bias[co + 1] : 0.f;
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const int64_t m = m0 + wm * 32 + i * 16 + g + h * 8;
+				if (m >= M) continue;
+				float v0 = acc[i][j][2 * h] + b0, v1 = acc[i][j][2 * h + 1] + b1;
+				if (a.relu) {
+					v0 = fmaxf(v0, 0.f);
+					v1 = fmaxf(v1, 0.f);
+				}
+				*reinterpret_cast<__nv_bfloat162 *>(a.y + m * a.Co + co) = __floats2bfloat162_rn(v0, v1);
+			}
+		}
+	}
+}
+
+// ---- weight gradient: dW[co][k] = sum_m dY[m][co] * im2col(X)[m][k] -------------
+
+struct WgradArgs {
+	const bf16 *x;  // (N,H,W,Ci) forward input
+	const bf16 *dy; // (N,H,W,Co) gradient at the pre-activation
+	float *partial; // (chunks, Co, 9 Ci)
+	int N, H, W, Ci, Co;
+	int64_t chunk; // pixels per chunk (multiple of 16)
+};
+
+__global__ void __launch_bounds__(128) conv_wgrad(WgradArgs a) {
+	__shared__ __align__(16) bf16 As[CB_M][CPAD]; // [co][pixel]
+	__shared__ __align__(16) bf16 Bs[CB_N][CPAD]; // [kcol][pixel]
+	const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+	const int wm = warp >> 1, wn = warp & 1;
+	const int g = lane >> 2, t = lane & 3;
+	const int64_t M = (int64_t)a.N * a.H * a.W;
+	const int K = 9 * a.Ci;
+	const int co0 = blockIdx.x * CB_M, k0 = blockIdx.y * CB_N;
+	const int64_t p_begin = (int64_t)blockIdx.z * a.chunk;
+	const int64_t p_end = p_begin + a.chunk < M ? p_begin + a.chunk : M;
+	float acc[2][4][4];
+#pragma unroll
+	for (int i = 0; i < 2; ++i)
+#pragma unroll
+		for (int j = 0; j < 4; ++j)
+#pragma unroll
+			for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
+	// per k-step of 16 pixels: thread -> (pixel = tid / 8, vector v = tid % 8 of 8 bf16)
+	const int lp = tid >> 3, lv = tid & 7;
+	for (int64_t pb = p_begin; pb < p_end; pb += 16) {
+		const int64_t m = pb + lp;
+		int n = 0, yy = 0, xx = 0;
+		const bool mv = m < p_end;
+		if (mv) {
+			n = (int)(m / ((int64_t)a.H * a.W));
+			const int r = (int)(m - (int64_t)n * a.H * a.W);
+			yy = r / a.W;
+			xx = r - yy * a.W;
+		}
+		// A: dY[m][co0 + 8 lv .. +7]
+		{
+			uint4 v = make_uint4(0, 0, 0, 0);
+			const int co = co0 + lv * 8;
+			if (mv && co < a.Co) v = *reinterpret_cast<const uint4 *>(a.dy + m * a.Co + co);
+			const bf16 *e = reinterpret_cast<const bf16 *>(&v);
+#pragma unroll
+			for (int q = 0; q < 8; ++q) As[lv * 8 + q][lp] = e[q];
+		}
+		// B: im2col(X)[m][k0 + 8 lv .. +7]
+		{
+			uint4 v = make_uint4(0, 0, 0, 0);
+			const int k = k0 + lv * 8;
+			if (mv && k < K) {
+				const int tap = k / a.Ci, ci = k - tap * a.Ci;
+				const int sy = yy + tap / 3 - 1, sx = xx + tap % 3 - 1;
+				if (sy >= 0 && sy < a.H && sx >= 0 && sx < a.W)
+					v = *reinterpret_cast<const uint4 *>(a.x + (((int64_t)n * a.H + sy) * a.W + sx) * a.Ci + ci);
+			}
+			const bf16 *e = reinterpret_cast<const bf16 *>(&v);
+#pragma unroll
+			for (int q = 0; q < 8; ++q) Bs[lv * 8 + q][lp] = e[q];
+		}
+		__syncthreads();
+		uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+		for (int i = 0; i < 2; ++i) {
+			const int r = wm * 32 + i * 16 + g;
+			af[i][0] = *reinterpret_cast<const uint32_t *>(&As[r][2 * t]);
+			af[i][1] = *reinterpret_cast<const uint32_t *>(&As[r + 8][2 * t]);
+			af[i][2] = *reinterpret_cast<const uint32_t *>(&As[r][2 * t + 8]);
+			af[i][3] = *reinterpret_cast<const uint32_t *>(&As[r + 8][2 * t + 8]);
+		}
+#pragma unroll
+		for (int j = 0; j < 4; ++j) {
+			const int c = wn * 32 + j * 8 + g;
+			bfr[j][0] = *reinterpret_cast<const uint32_t *>(&Bs[c][2 * t]);
+			bfr[j][1] = *reinterpret_cast<const uint32_t *>(&Bs[c][2 * t + 8]);
+		}
+#pragma unroll
+		for (int i = 0; i < 2; ++i)
+#pragma unroll
+			for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j]);
+		__syncthreads();
+	}
+	float *out = a.partial + (int64_t)blockIdx.z * a.Co * K;
+#pragma unroll
+	for (int i = 0; i < 2; ++i)
+#pragma unroll
+		for (int j = 0; j < 4; ++j)
+#pragma unroll
+			for (int h = 0; h < 2; ++h) {
+				const int co = co0 + wm * 32 + i * 16 + g + h * 8;
+				const int k = k0 + wn * 32 + j * 8 + 2 * t;
+				if (co < a.Co && k < K) {
+					out[(int64_t)co * K + k] = acc[i][j][2 * h];
+					if (k + 1 < K) out[(int64_t)co * K + k + 1] = acc[i][j][2 * h + 1];
+				}
+			}
+}
+
+// grad[j] += sum over chunks of partial[c][j], chunks in order
+__global__ void reduce_partials(const float *partial, int64_t per, int chunks, float *grad) {
+	for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < per; j += (int64_t)gridDim.x * blockDim.x) {
+		float s = 0.f;
+		for (int c = 0; c < chunks; ++c) s += partial[(int64_t)c * per + j];
+		grad[j] += s;
+	}
+}
+
+// db[co] += sum over pixels of dY[m][co] (one block per channel, fixed order)
+__global__ void bias_grad(const bf16 *dy, int64_t M, int Co, float *db) {
+	__shared__ float sh[256];
+	const int co = blockIdx.x;
+	float s = 0.f;
+	for (int64_t m = threadIdx.x; m < M; m += blockDim.x) s += __bfloat162float(dy[m * Co + co]);
+	sh[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) db[co] += sh[0];
+}
+
+// ---- element-wise pieces -----------------------------------------------------------
+
+__global__ void relu_backward(bf16 *dy, const bf16 *y, int64_t n) {
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+		if (!(__bfloat162float(y[i]) > 0.f)) dy[i] = __float2bfloat16(0.f);
+}
+
+__global__ void pool_forward(const bf16 *x, bf16 *y, int N, int H, int W, int C) {
+	const int64_t n = (int64_t)N * (H / 2) * (W / 2) * C;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const int c = (int)(i % C);
+		int64_t r = i / C;
+		const int xo = (int)(r % (W / 2));
+		r /= (W / 2);
+		const int yo = (int)(r % (H / 2));
+		const int b = (int)(r / (H / 2));
+		const int64_t base = (((int64_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
+		const float s = __bfloat162float(x[base]) + __bfloat162float(x[base + C]) +
+						__bfloat162float(x[base + (int64_t)W * C]) + __bfloat162float(x[base + (int64_t)W * C + C]);
+		y[i] = __float2bfloat16(0.25f * s);
+	}
+}
+
+// dx (N,H,W,C) = pool_backward(dy (N,H/2,W/2,C)) + skip_grad
+__global__ void pool_backward_add(const bf16 *dy, const bf16 *skip, bf16 *dx, int N, int H, int W, int C) {
+	const int64_t n = (int64_t)N * H * W * C;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const int c = (int)(i % C);
+		int64_t r = i / C;
+		const int x = (int)(r % W);
+		r /= W;
+		const int y = (int)(r % H);
+		const int b = (int)(r / H);
+		const float g = 0.25f * __bfloat162float(dy[(((int64_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c]);
+		dx[i] = __float2bfloat16(g + __bfloat162float(skip[i]));
+	}
+}
+
+// cat (N,H,W,Cu+Cs) = [upsample2(u (N,H/2,W/2,Cu)), s (N,H,W,Cs)]
+__global__ void upcat_forward(const bf16 *u, const bf16 *s, bf16 *cat, int N, int H, int W, int Cu, int Cs) {
+	const int C = Cu + Cs;
+	const int64_t n = (int64_t)N * H * W * C;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const int c = (int)(i % C);
+		const int64_t p = i / C;
+		const int x = (int)(p % W);
+		const int64_t r = p / W;
+		const int y = (int)(r % H);
+		const int b = (int)(r / H);
+		cat[i] = c < Cu ? u[(((int64_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * Cu + c] : s[p * Cs + (c - Cu)];
+	}
+}
+
+// split d(cat): d_up (N,H/2,W/2,Cu) = upsample_backward(first Cu), d_skip = last Cs
+__global__ void upcat_backward(const bf16 *dcat, bf16 *du, bf16 *ds, int N, int H, int W, int Cu, int Cs) {
+	const int C = Cu + Cs;
+	const int64_t nu = (int64_t)N * (H / 2) * (W / 2) * Cu;
+	const int64_t ns = (int64_t)N * H * W * Cs;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nu + ns; i += (int64_t)gridDim.x * blockDim.x) {
+		if (i < nu) {
+			const int c = (int)(i % Cu);
+			int64_t r = i / Cu;
+			const int xo = (int)(r % (W / 2));
+			r /= (W / 2);
+			const int yo = (int)(r % (H / 2));
+			const int b = (int)(r / (H / 2));
+			const int64_t base = (((int64_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
+			const float s = __bfloat162float(dcat[base]) + __bfloat162float(dcat[base + C]) +
+							__bfloat162float(dcat[base + (int64_t)W * C]) +
+							__bfloat162float(dcat[base + (int64_t)W * C + C]);
+			du[i] = __float2bfloat16(s);
+		} else {
+			const int64_t j = i - nu;
+			const int c = (int)(j % Cs);
+			const int64_t p = j / Cs;
+			ds[j] = dcat[p * C + Cu + c];
+		}
+	}
+}
+
+// 1x1 head: y (N,H,W,3) fp32 = x (.., Ci) * Wh^T + b
+__global__ void head_forward(const bf16 *x, const float *w, const float *b, float *y, int64_t M, int Ci, int Co) {
+	for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+		for (int co = 0; co < Co; ++co) {
+			float s = b[co];
+			for (int ci = 0; ci < Ci; ++ci) s += w[co * Ci + ci] * __bfloat162float(x[m * Ci + ci]);
+			y[m * Co + co] = s;
+		}
+	}
+}
+
+// masked-free MSE: loss = mean (y - t)^2, dy = 2 (y - t) / n; partial loss per block
+__global__ void mse_loss(const float *y, const float *tgt, float *dy, int64_t n, double *partial) {
+	__shared__ double sh[256];
+	double s = 0.0;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const float d = y[i] - tgt[i];
+		dy[i] = 2.f * d / (float)n;
+		s += (double)d * d;
+	}
+	sh[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
+}
+
+// head backward: dx (bf16) = dy * Wh, dW/db accumulated per block then reduced
+__global__ void head_backward_dx(const float *dy, const float *w, bf16 *dx, int64_t M, int Ci, int Co) {
+	for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x)
+		for (int ci = 0; ci < Ci; ++ci) {
+			float s = 0.f;
+			for (int co = 0; co < Co; ++co) s += dy[m * Co + co] * w[co * Ci + ci];
+			dx[m * Ci + ci] = __float2bfloat16(s);
+		}
+}
+
+__global__ void head_backward_dw(const float *dy, const bf16 *x, int64_t M, int Ci, int Co, float *partial) {
+	// one block per (co, ci) pair plus one per co for the bias; fixed-order reduction
+	__shared__ float sh[256];
+	const int j = blockIdx.x; // j < Co*Ci: weight, else bias
+	const int co = j < Co * Ci ? j / Ci : j - Co * Ci;
+	const int ci = j < Co * Ci ? j % Ci : -1;
+	float s = 0.f;
+	for (int64_t m = threadIdx.x; m < M; m += blockDim.x)
+		s += dy[m * Co + co] * (ci >= 0 ? __bfloat162float(x[m * Ci + ci]) : 1.f);
+	sh[threadIdx.x] = s;
+	__syncthreads();
+	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) partial[j] += sh[0];
+}
+
+// Adam on the FP32 master copy, then the bf16 copies: w (co,3,3,ci) and the
+// flipped/transposed wf (ci,3,3,co) used by the data gradient.
+__global__ void adam_update(float *p, const float *g, float *m, float *v, int64_t n, float lr, float b1, float b2,
+							float eps, float c1, float c2) {
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const float gi = g[i];
+		const float mi = b1 * m[i] + (1.f - b1) * gi;
+		const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+		m[i] = mi;
+		v[i] = vi;
+		p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+	}
+}
+
+__global__ void refresh_conv_weights(const float *w32, bf16 *w, bf16 *wf, int Co, int Ci, int k) {
+	const int64_t n = (int64_t)Co * k * k * Ci;
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const int ci = (int)(i % Ci);
+		int64_t r = i / Ci;
+		const int kx = (int)(r % k);
+		r /= k;
+		const int ky = (int)(r % k);
+		const int co = (int)(r / k);
+		const bf16 v = __float2bfloat16(w32[i]);
+		w[i] = v;
+		if (wf) wf[(((int64_t)ci * k + (k - 1 - ky)) * k + (k - 1 - kx)) * Co + co] = v;
+	}
+}
+
+// network input: ch0 = mask, ch1 = u_max / 0.08, ch2 = (tau - 0.55) / 0.45, rest 0
+__global__ void make_input(const uint8_t *mask, const float *umax, const float *tau, bf16 *x, int N, int H, int W,
+						   int C) {
+	const int64_t n = (int64_t)N * H * W;
+	for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+		const int b = (int)(p / ((int64_t)H * W));
+		bf16 *o = x + p * C;
+		for (int c = 0; c < C; ++c) o[c] = __float2bfloat16(0.f);
+		o[0] = __float2bfloat16((float)mask[p]);
+		o[1] = __float2bfloat16(umax[b] / 0.08f);
+		o[2] = __float2bfloat16((tau[b] - 0.55f) / 0.45f);
+	}
+}
+
+int grid_of(int64_t n) { return grid_for(n); }
+
+} // namespace
+
+// ----------------------------------------------------------------------------------
+// network object
+
+struct UnetLayer {
+	int co, ci, k;  // conv shape
+	int64_t woff;   // offset of the weights in the flat parameter vector (bias follows)
+	bf16 *w = nullptr, *wf = nullptr;
+	int level;      // spatial level (0 = full resolution)
+};
+
+struct kel_unet {
+	kel_unet_desc d;
+	std::vector<UnetLayer> L; // enc0a enc0b enc1a enc1b enc2a enc2b botta bottb dec2a dec2b dec1a dec1b dec0a dec0b head
+	int64_t nparam = 0;
+	float *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr;
+	float *partial = nullptr;
+	int64_t partial_len = 0;
+	double *loss_partial = nullptr;
+	cudaStream_t stream = nullptr;
+	// activations / gradients, one per named tensor
+	std::vector<bf16 *> act, grad;
+	bf16 *input = nullptr;
+	float *out = nullptr, *dout = nullptr;
+	int batch = 0;
+};
+
+namespace {
+
+// tensor ids
+enum { T_E0A, T_E0B, T_P0, T_E1A, T_E1B, T_P1, T_E2A, T_E2B, T_P2, T_BA, T_BB, T_C2, T_D2A, T_D2B, T_C1, T_D1A,
+	   T_D1B, T_C0, T_D0A, T_D0B, T_COUNT };
+
+struct TShape {
+	int level, ch;
+};
+
+TShape tshape(const kel_unet *U, int t) {
+	const int *w = U->d.widths;
+	switch (t) {
+	case T_E0A: case T_E0B: return {0, w[0]};
+	case T_P0: return {1, w[0]};
+	case T_E1A: case T_E1B: return {1, w[1]};
+	case T_P1: return {2, w[1]};
+	case T_E2A: case T_E2B: return {2, w[2]};
+	case T_P2: return {3, w[2]};
+	case T_BA: case T_BB: return {3, w[3]};
+	case T_C2: return {2, w[3] + w[2]};
+	case T_D2A: case T_D2B: return {2, w[2]};
+	case T_C1: return {1, w[2] + w[1]};
+	case T_D1A: case T_D1B: return {1, w[1]};
+	case T_C0: return {0, w[1] + w[0]};
+	default: return {0, w[0]};
+	}
+}
+
+int64_t telems(const kel_unet *U, int t, int n) {
+	const TShape s = tshape(U, t);
+	return (int64_t)n * (U->d.height >> s.level) * (U->d.width >> s.level) * s.ch;
+}
+
+int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y, int n, int level, int ci, int co,
+			 bool relu, bool bias) {
+	ConvArgs a;
+	a.x = x;
+	a.w = w;
+	a.bias = b;
+	a.y = y;
+	a.N = n;
+	a.H = U->d.height >> level;
+	a.W = U->d.width >> level;
+	a.Ci = ci;
+	a.Co = co;
+	a.relu = relu;
+	a.use_bias = bias;
+	const int64_t M = (int64_t)n * a.H * a.W;
+	dim3 grid((unsigned)((M + CB_M - 1) / CB_M), (unsigned)((co + CB_N - 1) / CB_N));
+	conv_igemm<<<grid, 128, 0, U->stream>>>(a);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+int conv_grads(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy, int n) {
+	WgradArgs a;
+	a.x = x;
+	a.dy = dy;
+	a.partial = U->partial;
+	a.N = n;
+	a.H = U->d.height >> l.level;
+	a.W = U->d.width >> l.level;
+	a.Ci = l.ci;
+	a.Co = l.co;
+	const int64_t M = (int64_t)n * a.H * a.W;
+	const int K = 9 * l.ci;
+	const int tiles = ((l.co + CB_M - 1) / CB_M) * ((K + CB_N - 1) / CB_N);
+	int64_t chunks = (600 + tiles - 1) / tiles;
+	const int64_t max_chunks = U->partial_len / ((int64_t)l.co * K);
+	if (chunks > max_chunks) chunks = max_chunks;
+	if (chunks > (M + 255) / 256) chunks = (M + 255) / 256;
+	if (chunks < 1) chunks = 1;
+	a.chunk = ((M + chunks - 1) / chunks + 15) / 16 * 16;
+	chunks = (M + a.chunk - 1) / a.chunk;
+	dim3 grid((unsigned)((l.co + CB_M - 1) / CB_M), (unsigned)((K + CB_N - 1) / CB_N), (unsigned)chunks);
+	conv_wgrad<<<grid, 128, 0, U->stream>>>(a);
+	const int64_t per = (int64_t)l.co * K;
+	reduce_partials<<<grid_of(per), 256, 0, U->stream>>>(U->partial, per, (int)chunks, U->g + l.woff);
+	bias_grad<<<l.co, 256, 0, U->stream>>>(dy, M, l.co, U->g + l.woff + per);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+void init_params(kel_unet *U, uint64_t seed, std::vector<float> &h) {
+	h.assign(U->nparam, 0.f);
+	uint64_t s = seed * 6364136223846793005ull + 1442695040888963407ull;
+	auto next = [&]() {
+		s = s * 6364136223846793005ull + 1442695040888963407ull;
+		return (double)((s >> 11) & ((1ull << 53) - 1)) / (double)(1ull << 53);
+	};
+	for (const auto &l : U->L) {
+		const int64_t fan_in = (int64_t)l.k * l.k * l.ci;
+		const double bound = std::sqrt(6.0 / (double)fan_in); // He-uniform
+		const int64_t nw = (int64_t)l.co * fan_in;
+		for (int64_t i = 0; i < nw; ++i) h[l.woff + i] = (float)((2.0 * next() - 1.0) * bound);
+	}
+}
+
+int refresh(kel_unet *U) {
+	for (auto &l : U->L) {
+		if (l.k != 3) continue;
+		refresh_conv_weights<<<grid_of((int64_t)l.co * 9 * l.ci), 256, 0, U->stream>>>(U->p + l.woff, l.w, l.wf, l.co,
+																						   l.ci, 3);
+	}
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+} // namespace
+
+extern "C" int kel_unet_create(const kel_unet_desc *desc, uint64_t seed, kel_unet **out) {
+	if (!desc || !out) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_create: null argument");
+	*out = nullptr;
+	if (desc->height % 8 || desc->width % 8 || desc->height < 8 || desc->width < 8)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_create: height and width must be multiples of 8");
+	if (desc->in_channels != 16 || desc->out_channels < 1 || desc->out_channels > 8 || desc->max_batch < 1)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_create: in_channels must be 16, out_channels 1..8");
+	for (int i = 0; i < 4; ++i)
+		if (desc->widths[i] < 16 || desc->widths[i] % 16)
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_create: widths must be multiples of 16");
+	kel_unet *U = new kel_unet();
+	U->d = *desc;
+	const int *w = desc->widths;
+	struct Spec {
+		int co, ci, k, level;
+	};
+	const Spec specs[15] = {{w[0], 16, 3, 0},		 {w[0], w[0], 3, 0}, {w[1], w[0], 3, 1},		{w[1], w[1], 3, 1},
+							{w[2], w[1], 3, 2},		 {w[2], w[2], 3, 2}, {w[3], w[2], 3, 3},		{w[3], w[3], 3, 3},
+							{w[2], w[3] + w[2], 3, 2}, {w[2], w[2], 3, 2}, {w[1], w[2] + w[1], 3, 1}, {w[1], w[1], 3, 1},
+							{w[0], w[1] + w[0], 3, 0}, {w[0], w[0], 3, 0}, {desc->out_channels, w[0], 1, 0}};
+	int64_t off = 0;
+	int64_t max_w = 0;
+	for (const auto &s : specs) {
+		UnetLayer l;
+		l.co = s.co;
+		l.ci = s.ci;
+		l.k = s.k;
+		l.level = s.level;
+		l.woff = off;
+		off += (int64_t)s.co * s.k * s.k * s.ci + s.co;
+		if ((int64_t)s.co * 9 * s.ci > max_w) max_w = (int64_t)s.co * 9 * s.ci;
+		U->L.push_back(l);
+	}
+	U->nparam = off;
+	cudaStreamCreateWithFlags(&U->stream, cudaStreamNonBlocking);
+	auto fail_out = [&](cudaError_t e) {
+		kel_unet_destroy(U);
+		return fail(e == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA, "kel_unet_create: %s",
+					cudaGetErrorString(e));
+	};
+	cudaError_t e;
+	if ((e = cudaMalloc(&U->p, sizeof(float) * off)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->g, sizeof(float) * off)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->m, sizeof(float) * off)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->v, sizeof(float) * off)) != cudaSuccess) return fail_out(e);
+	cudaMemsetAsync(U->m, 0, sizeof(float) * off, U->stream);
+	cudaMemsetAsync(U->v, 0, sizeof(float) * off, U->stream);
+	cudaMemsetAsync(U->g, 0, sizeof(float) * off, U->stream);
+	for (auto &l : U->L) {
+		if (l.k != 3) continue;
+		const int64_t nw = (int64_t)l.co * 9 * l.ci;
+		if ((e = cudaMalloc(&l.w, sizeof(bf16) * nw)) != cudaSuccess) return fail_out(e);
+		if ((e = cudaMalloc(&l.wf, sizeof(bf16) * nw)) != cudaSuccess) return fail_out(e);
+	}
+	U->partial_len = max_w * 64;
+	if ((e = cudaMalloc(&U->partial, sizeof(float) * U->partial_len)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->loss_partial, sizeof(double) * 1024)) != cudaSuccess) return fail_out(e);
+	const int n = desc->max_batch;
+	U->batch = n;
+	U->act.assign(T_COUNT, nullptr);
+	U->grad.assign(T_COUNT, nullptr);
+	for (int t = 0; t < T_COUNT; ++t) {
+		if ((e = cudaMalloc(&U->act[t], sizeof(bf16) * telems(U, t, n))) != cudaSuccess) return fail_out(e);
+		if ((e = cudaMalloc(&U->grad[t], sizeof(bf16) * telems(U, t, n))) != cudaSuccess) return fail_out(e);
+	}
+	const int64_t pix = (int64_t)n * desc->height * desc->width;
+	if ((e = cudaMalloc(&U->input, sizeof(bf16) * pix * 16)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->out, sizeof(float) * pix * desc->out_channels)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->dout, sizeof(float) * pix * desc->out_channels)) != cudaSuccess) return fail_out(e);
+	std::vector<float> h;
+	init_params(U, seed, h);
+	if ((e = cudaMemcpyAsync(U->p, h.data(), sizeof(float) * off, cudaMemcpyHostToDevice, U->stream)) != cudaSuccess)
+		return fail_out(e);
+	int rc = refresh(U);
+	if (rc) {
+		kel_unet_destroy(U);
+		return rc;
+	}
+	cudaStreamSynchronize(U->stream);
+	*out = U;
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_destroy(kel_unet *U) {
+	if (!U) return KEL_OK;
+	if (U->stream) cudaStreamSynchronize(U->stream);
+	for (auto &l : U->L) {
+		cudaFree(l.w);
+		cudaFree(l.wf);
+	}
+	for (auto *p : U->act) cudaFree(p);
+	for (auto *p : U->grad) cudaFree(p);
+	cudaFree(U->p);
+	cudaFree(U->g);
+	cudaFree(U->m);
+	cudaFree(U->v);
+	cudaFree(U->partial);
+	cudaFree(U->loss_partial);
+	cudaFree(U->input);
+	cudaFree(U->out);
+	cudaFree(U->dout);
+	if (U->stream) cudaStreamDestroy(U->stream);
+	delete U;
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_param_count(const kel_unet *U, int64_t *n) {
+	if (!U || !n) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_param_count: null argument");
+	*n = U->nparam;
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_get_params(kel_unet *U, float *host) {
+	if (!U || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_get_params: null argument");
+	KEL_CUDA(cudaMemcpyAsync(host, U->p, sizeof(float) * U->nparam, cudaMemcpyDeviceToHost, U->stream));
+	KEL_CUDA(cudaStreamSynchronize(U->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_set_params(kel_unet *U, const float *host) {
+	if (!U || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_set_params: null argument");
+	KEL_CUDA(cudaMemcpyAsync(U->p, host, sizeof(float) * U->nparam, cudaMemcpyHostToDevice, U->stream));
+	int rc = refresh(U);
+	if (rc) return rc;
+	KEL_CUDA(cudaStreamSynchronize(U->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_get_grads(kel_unet *U, float *host) {
+	if (!U || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_get_grads: null argument");
+	KEL_CUDA(cudaMemcpyAsync(host, U->g, sizeof(float) * U->nparam, cudaMemcpyDeviceToHost, U->stream));
+	KEL_CUDA(cudaStreamSynchronize(U->stream));
+	return KEL_OK;
+}
+
+static int check_batch(const kel_unet *U, int32_t n, const char *who) {
+	if (!U || n < 1 || n > U->batch) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: batch must be 1..max_batch", who);
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_make_input(kel_unet *U, const uint8_t *d_mask, const float *d_umax, const float *d_tau,
+								   int32_t n) {
+	int rc = check_batch(U, n, "kel_unet_make_input");
+	if (rc) return rc;
+	const int64_t pix = (int64_t)n * U->d.height * U->d.width;
+	make_input<<<grid_of(pix), 256, 0, U->stream>>>(d_mask, d_umax, d_tau, U->input, n, U->d.height, U->d.width, 16);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_forward(kel_unet *U, int32_t n, float *d_out) {
+	int rc = check_batch(U, n, "kel_unet_forward");
+	if (rc) return rc;
+	auto &A = U->act;
+	const auto &L = U->L;
+	const int *w = U->d.widths;
+	const int H = U->d.height, W = U->d.width;
+	auto cv = [&](int li, const bf16 *x, bf16 *y) {
+		const UnetLayer &l = L[li];
+		return conv_fwd(U, x, l.w, U->p + l.woff + (int64_t)l.co * 9 * l.ci, y, n, l.level, l.ci, l.co, true, true);
+	};
+	if ((rc = cv(0, U->input, A[T_E0A])) || (rc = cv(1, A[T_E0A], A[T_E0B]))) return rc;
+	pool_forward<<<grid_of(telems(U, T_P0, n)), 256, 0, U->stream>>>(A[T_E0B], A[T_P0], n, H, W, w[0]);
+	if ((rc = cv(2, A[T_P0], A[T_E1A])) || (rc = cv(3, A[T_E1A], A[T_E1B]))) return rc;
+	pool_forward<<<grid_of(telems(U, T_P1, n)), 256, 0, U->stream>>>(A[T_E1B], A[T_P1], n, H / 2, W / 2, w[1]);
+	if ((rc = cv(4, A[T_P1], A[T_E2A])) || (rc = cv(5, A[T_E2A], A[T_E2B]))) return rc;
+	pool_forward<<<grid_of(telems(U, T_P2, n)), 256, 0, U->stream>>>(A[T_E2B], A[T_P2], n, H / 4, W / 4, w[2]);
+	if ((rc = cv(6, A[T_P2], A[T_BA])) || (rc = cv(7, A[T_BA], A[T_BB]))) return rc;
+	upcat_forward<<<grid_of(telems(U, T_C2, n)), 256, 0, U->stream>>>(A[T_BB], A[T_E2B], A[T_C2], n, H / 4, W / 4, w[3],
+																	   w[2]);
+	if ((rc = cv(8, A[T_C2], A[T_D2A])) || (rc = cv(9, A[T_D2A], A[T_D2B]))) return rc;
+	upcat_forward<<<grid_of(telems(U, T_C1, n)), 256, 0, U->stream>>>(A[T_D2B], A[T_E1B], A[T_C1], n, H / 2, W / 2, w[2],
+																	   w[1]);
+	if ((rc = cv(10, A[T_C1], A[T_D1A])) || (rc = cv(11, A[T_D1A], A[T_D1B]))) return rc;
+	upcat_forward<<<grid_of(telems(U, T_C0, n)), 256, 0, U->stream>>>(A[T_D1B], A[T_E0B], A[T_C0], n, H, W, w[1], w[0]);
+	if ((rc = cv(12, A[T_C0], A[T_D0A])) || (rc = cv(13, A[T_D0A], A[T_D0B]))) return rc;
+	const UnetLayer &hd = L[14];
+	const int64_t M = (int64_t)n * H * W;
+	head_forward<<<grid_of(M), 256, 0, U->stream>>>(A[T_D0B], U->p + hd.woff, U->p + hd.woff + (int64_t)hd.co * hd.ci,
+													U->out, M, hd.ci, hd.co);
+	KEL_CUDA(cudaGetLastError());
+	if (d_out && d_out != U->out)
+		KEL_CUDA(cudaMemcpyAsync(d_out, U->out, sizeof(float) * M * hd.co, cudaMemcpyDeviceToDevice, U->stream));
+	return KEL_OK;
+}
+
+// After kel_unet_forward with the same n: masked-free MSE against d_target
+// (N,H,W,out_channels), all gradients into the FP32 gradient vector
+// (overwritten).  *loss receives the loss (host).
+extern "C" int kel_unet_backward(kel_unet *U, const float *d_target, int32_t n, double *loss) {
+	int rc = check_batch(U, n, "kel_unet_backward");
+	if (rc) return rc;
+	if (!d_target) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_backward: null target");
+	auto &A = U->act;
+	auto &G = U->grad;
+	const auto &L = U->L;
+	const int *w = U->d.widths;
+	const int H = U->d.height, W = U->d.width;
+	const UnetLayer &hd = L[14];
+	const int64_t M = (int64_t)n * H * W;
+	const int64_t nout = M * hd.co;
+	KEL_CUDA(cudaMemsetAsync(U->g, 0, sizeof(float) * U->nparam, U->stream));
+	const int lb = 512;
+	mse_loss<<<lb, 256, 0, U->stream>>>(U->out, d_target, U->dout, nout, U->loss_partial);
+	// head
+	head_backward_dx<<<grid_of(M), 256, 0, U->stream>>>(U->dout, U->p + hd.woff, G[T_D0B], M, hd.ci, hd.co);
+	head_backward_dw<<<hd.co * hd.ci + hd.co, 256, 0, U->stream>>>(U->dout, A[T_D0B], M, hd.ci, hd.co, U->g + hd.woff);
+	// one conv layer: relu backward on dy, weight/bias grads, data grad into dx
+	auto back = [&](int li, int t_in, const bf16 *x_in, int t_out, bf16 *dx) -> int {
+		const UnetLayer &l = L[li];
+		relu_backward<<<grid_of(telems(U, t_out, n)), 256, 0, U->stream>>>(G[t_out], A[t_out], telems(U, t_out, n));
+		int r = conv_grads(U, l, x_in, G[t_out], n);
+		if (r) return r;
+		if (dx) r = conv_fwd(U, G[t_out], l.wf, nullptr, dx, n, l.level, l.co, l.ci, false, false);
+		(void)t_in;
+		return r;
+	};
+	if ((rc = back(13, T_D0A, A[T_D0A], T_D0B, G[T_D0A])) || (rc = back(12, T_C0, A[T_C0], T_D0A, G[T_C0]))) return rc;
+	upcat_backward<<<grid_of(telems(U, T_C0, n)), 256, 0, U->stream>>>(G[T_C0], G[T_D1B], G[T_E0B], n, H, W, w[1], w[0]);
+	if ((rc = back(11, T_D1A, A[T_D1A], T_D1B, G[T_D1A])) || (rc = back(10, T_C1, A[T_C1], T_D1A, G[T_C1]))) return rc;
+	upcat_backward<<<grid_of(telems(U, T_C1, n)), 256, 0, U->stream>>>(G[T_C1], G[T_D2B], G[T_E1B], n, H / 2, W / 2, w[2],
+																		w[1]);
+	if ((rc = back(9, T_D2A, A[T_D2A], T_D2B, G[T_D2A])) || (rc = back(8, T_C2, A[T_C2], T_D2A, G[T_C2]))) return rc;
+	upcat_backward<<<grid_of(telems(U, T_C2, n)), 256, 0, U->stream>>>(G[T_C2], G[T_BB], G[T_E2B], n, H / 4, W / 4, w[3],
+																		w[2]);
+	if ((rc = back(7, T_BA, A[T_BA], T_BB, G[T_BA])) || (rc = back(6, T_P2, A[T_P2], T_BA, G[T_P2]))) return rc;
+	// encoder level 2: d(e2b) = pool_backward(d p2) + d skip2 (kept in G[T_E2B])
+	pool_backward_add<<<grid_of(telems(U, T_E2B, n)), 256, 0, U->stream>>>(G[T_P2], G[T_E2B], G[T_E2B], n, H / 4,
+																			 W / 4, w[2]);
+	if ((rc = back(5, T_E2A, A[T_E2A], T_E2B, G[T_E2A])) || (rc = back(4, T_P1, A[T_P1], T_E2A, G[T_P1]))) return rc;
+	pool_backward_add<<<grid_of(telems(U, T_E1B, n)), 256, 0, U->stream>>>(G[T_P1], G[T_E1B], G[T_E1B], n, H / 2,
+																			 W / 2, w[1]);
+	if ((rc = back(3, T_E1A, A[T_E1A], T_E1B, G[T_E1A])) || (rc = back(2, T_P0, A[T_P0], T_E1A, G[T_P0]))) return rc;
+	pool_backward_add<<<grid_of(telems(U, T_E0B, n)), 256, 0, U->stream>>>(G[T_P0], G[T_E0B], G[T_E0B], n, H, W, w[0]);
+	if ((rc = back(1, T_E0A, A[T_E0A], T_E0B, G[T_E0A])) || (rc = back(0, -1, U->input, T_E0A, nullptr))) return rc;
+	KEL_CUDA(cudaGetLastError());
+	if (loss) {
+		std::vector<double> part(lb);
+		KEL_CUDA(cudaMemcpyAsync(part.data(), U->loss_partial, sizeof(double) * lb, cudaMemcpyDeviceToHost, U->stream));
+		KEL_CUDA(cudaStreamSynchronize(U->stream));
+		double s = 0.0;
+		for (double p : part) s += p;
+		*loss = s / (double)nout;
+	}
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_adam_step(kel_unet *U, float lr, float beta1, float beta2, float eps, int32_t step) {
+	if (!U || step < 1) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_adam_step: bad arguments");
+	const float c1 = 1.f - powf(beta1, (float)step), c2 = 1.f - powf(beta2, (float)step);
+	adam_update<<<grid_of(U->nparam), 256, 0, U->stream>>>(U->p, U->g, U->m, U->v, U->nparam, lr, beta1, beta2, eps, c1,
+														   c2);
+	KEL_CUDA(cudaGetLastError());
+	return refresh(U);
+}
+
+extern "C" int kel_unet_set_stream(kel_unet *U, void *stream) {
+	if (!U) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_set_stream: null net");
+	U->stream = static_cast<cudaStream_t>(stream);
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_synchronize(kel_unet *U) {
+	if (!U) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_synchronize: null net");
+	KEL_CUDA(cudaStreamSynchronize(U->stream));
+	return KEL_OK;
+}
+
+// Direct input (bf16 NHWC, 16 channels) for tests: copies into the net's input.
+extern "C" int kel_unet_set_input(kel_unet *U, const uint16_t *d_input_bf16, int32_t n) {
+	int rc = check_batch(U, n, "kel_unet_set_input");
+	if (rc) return rc;
+	KEL_CUDA(cudaMemcpyAsync(U->input, d_input_bf16, sizeof(bf16) * (int64_t)n * U->d.height * U->d.width * 16,
+							 cudaMemcpyDeviceToDevice, U->stream));
+	return KEL_OK;
+}

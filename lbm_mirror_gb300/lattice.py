@@ -395,3 +395,76 @@ class Batch:
         _check(self.lib.kel_batch_download_macros(self._h, channel, _ptr(out)), self.lib)
         out = out.reshape(nx * ny, 3)
         return out[:, 0].copy(), out[:, 1:3].copy()
+
+
+class UNet:
+    """The warm-start U-Net (C ABI kel_unet_*): bf16 tensor-core convolutions,
+    FP32 accumulate, FP32 master weights and Adam.  Device buffers passed in
+    are raw device pointers (e.g. torch tensors' data_ptr())."""
+
+    def __init__(self, height=64, width=256, widths=(32, 64, 128, 128), out_channels=3, max_batch=32, seed=1):
+        self.lib = K.load_library()
+        d = K.UnetDesc()
+        d.height, d.width, d.in_channels, d.out_channels = height, width, 16, out_channels
+        for i in range(4):
+            d.widths[i] = widths[i]
+        d.max_batch = max_batch
+        h = C.c_void_p()
+        _check(self.lib.kel_unet_create(C.byref(d), seed, C.byref(h)), self.lib)
+        self._h = h
+        self.shape = (height, width, out_channels)
+        self.widths = tuple(widths)
+        n = C.c_int64()
+        _check(self.lib.kel_unet_param_count(self._h, C.byref(n)), self.lib)
+        self.n_params = n.value
+        self.step_count = 0
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.kel_unet_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        out = np.empty(self.n_params, dtype=np.float32)
+        _check(self.lib.kel_unet_get_params(self._h, _ptr(out)), self.lib)
+        return out
+
+    def set_params(self, p):
+        a = np.ascontiguousarray(p, dtype=np.float32)
+        _check(self.lib.kel_unet_set_params(self._h, _ptr(a)), self.lib)
+
+    def grads(self):
+        out = np.empty(self.n_params, dtype=np.float32)
+        _check(self.lib.kel_unet_get_grads(self._h, _ptr(out)), self.lib)
+        return out
+
+    def set_stream(self, stream):
+        _check(self.lib.kel_unet_set_stream(self._h, C.c_void_p(stream)), self.lib)
+
+    def synchronize(self):
+        _check(self.lib.kel_unet_synchronize(self._h), self.lib)
+
+    def make_input(self, d_mask, d_umax, d_tau, n):
+        _check(self.lib.kel_unet_make_input(self._h, C.c_void_p(d_mask), C.c_void_p(d_umax), C.c_void_p(d_tau), n),
+               self.lib)
+
+    def set_input(self, d_input_bf16, n):
+        _check(self.lib.kel_unet_set_input(self._h, C.c_void_p(d_input_bf16), n), self.lib)
+
+    def forward(self, n, d_out=None):
+        _check(self.lib.kel_unet_forward(self._h, n, C.c_void_p(d_out) if d_out else None), self.lib)
+
+    def backward(self, d_target, n):
+        loss = C.c_double()
+        _check(self.lib.kel_unet_backward(self._h, C.c_void_p(d_target), n, C.byref(loss)), self.lib)
+        return loss.value
+
+    def adam_step(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        self.step_count += 1
+        _check(self.lib.kel_unet_adam_step(self._h, lr, beta1, beta2, eps, self.step_count), self.lib)

@@ -63,8 +63,8 @@ def test_graph_replay_equals_plain_launches_and_converged_channels_freeze():
     prog = cases.channel_program(0.8)
     a = Batch(chans, prog)
     b = Batch(chans, prog)
-    sa, ra = a.run_until(tol=3e-3, check_every=50, max_steps=2000, use_graph=True)
-    sb, rb = b.run_until(tol=3e-3, check_every=50, max_steps=2000, use_graph=False)
+    sa, ra = a.run_until(tol=1e-2, check_every=50, max_steps=20000, use_graph=True)
+    sb, rb = b.run_until(tol=1e-2, check_every=50, max_steps=20000, use_graph=False)
     np.testing.assert_array_equal(sa, sb)
     np.testing.assert_array_equal(ra, rb)
     for i in range(len(chans)):

@@ -1,0 +1,89 @@
+"""The CUDA U-Net (bf16 tensor-core convolutions, FP32 accumulate) against the
+FP64 oracle of oracle/unet_oracle.py on the same bf16-rounded weights and
+inputs.  Bar (bf16 activations): forward relative L2 <= 3e-2; every layer's
+weight gradient relative L2 <= 8e-2 and cosine >= 0.995 against FP64."""
+import numpy as np
+import pytest
+
+from oracle import unet_oracle as U
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+H, W, WIDTHS, N = 16, 32, (16, 32, 32, 48), 2
+
+
+def bf16_round(a):
+    t = torch.tensor(np.asarray(a, dtype=np.float32)).to(torch.bfloat16)
+    return t.to(torch.float32).numpy().astype(np.float64)
+
+
+def _net():
+    from lbm_mirror_gb300 import UNet
+    return UNet(height=H, width=W, widths=WIDTHS, out_channels=3, max_batch=N, seed=7)
+
+
+def _inputs(rng):
+    x = np.zeros((N, H, W, 16))
+    x[..., :3] = rng.standard_normal((N, H, W, 3))
+    return bf16_round(x)
+
+
+def test_forward_and_gradients_vs_fp64_oracle():
+    rng = np.random.default_rng(1)
+    net = _net()
+    flat = net.params().astype(np.float64)
+    assert flat.size == U.param_count(16, 3, WIDTHS)
+    x = _inputs(rng)
+    tgt = rng.standard_normal((N, H, W, 3)) * 0.1
+    xin = torch.tensor(x, dtype=torch.bfloat16, device="cuda").contiguous()
+    tg = torch.tensor(tgt, dtype=torch.float32, device="cuda").contiguous()
+    out = torch.empty((N, H, W, 3), dtype=torch.float32, device="cuda")
+    net.set_input(xin.data_ptr(), N)
+    net.forward(N, out.data_ptr())
+    loss_gpu = net.backward(tg.data_ptr(), N)
+    net.synchronize()
+    g_gpu = net.grads().astype(np.float64)
+
+    # oracle on bf16 conv weights (what the tensor cores multiply); biases and
+    # the 1x1 head stay FP32 on the GPU
+    shapes = U.layer_shapes(16, 3, WIDTHS)
+    wq = flat.copy()
+    o = 0
+    for (name, co, k, ci) in shapes:
+        nw = co * k * k * ci
+        if k == 3:
+            wq[o:o + nw] = bf16_round(flat[o:o + nw])
+        o += nw + co
+    loss, y, g = U.loss_and_grads(wq, x, tgt, 16, 3, WIDTHS)
+    y_gpu = out.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(y_gpu - y) / np.linalg.norm(y) <= 3e-2
+    assert abs(loss_gpu - loss) <= 3e-2 * loss
+    o = 0
+    for (name, co, k, ci) in shapes:
+        nw = co * k * k * ci
+        for sl in (slice(o, o + nw), slice(o + nw, o + nw + co)):
+            a, b = g_gpu[sl], g[sl]
+            rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+            cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
+            assert rel <= 8e-2 and cos >= 0.995, (name, rel, cos)
+        o += nw + co
+
+
+def test_training_reduces_loss():
+    rng = np.random.default_rng(2)
+    net = _net()
+    x = _inputs(rng)
+    # a smooth target the net can fit: a function of the input planes
+    tgt = np.stack([np.tanh(x[..., 0]), 0.5 * x[..., 1], 0.1 * x[..., 0] * x[..., 2]], axis=-1)
+    xin = torch.tensor(x, dtype=torch.bfloat16, device="cuda").contiguous()
+    tg = torch.tensor(tgt, dtype=torch.float32, device="cuda").contiguous()
+    net.set_input(xin.data_ptr(), N)
+    losses = []
+    for _ in range(150):
+        net.forward(N)
+        losses.append(net.backward(tg.data_ptr(), N))
+        net.adam_step(lr=3e-3)
+    assert losses[-1] < 0.2 * losses[0], (losses[0], losses[-1])
+    assert np.isfinite(losses).all()
