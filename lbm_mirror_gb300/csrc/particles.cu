@@ -344,67 +344,96 @@ __device__ inline void pdiff(int D, const double *a, const double *b, int per, d
 	}
 }
 
+// Force and torque of the pair (self s, other j) on s, or false when they do
+// not touch (particle/contact.hpp:466-512 inner body).
+__device__ inline bool pair_response(const kel_particle_state &self, const kel_particle_state &other, int s, int j, int D,
+									 const kel_particle_params &prm, double steps, double Lx, int periodic, double *f,
+									 double *torque0) {
+	double dd[3] = {0, 0, 0};
+	pdiff(D, self.position, other.position, periodic, Lx, dd);
+	double n2 = 0.0;
+	for (int k = 0; k < D; ++k) n2 = n2 + dd[k] * dd[k];
+	const double rl = self.radius, rr = other.radius;
+	if (!(n2 < rl * rl + rr * rr + rr * rl * 2.0)) return false;
+	const bool self_is_lo = s < j;
+	const kel_particle_state &lo = self_is_lo ? self : other;
+	const kel_particle_state &hi = self_is_lo ? other : self;
+	double d[3] = {0, 0, 0};
+	pdiff(D, lo.position, hi.position, periodic, Lx, d);
+	double len2 = 0.0;
+	for (int k = 0; k < D; ++k) len2 = len2 + d[k] * d[k];
+	const double sum_r = lo.radius + hi.radius;
+	if (!(len2 < sum_r * sum_r)) return false;
+	const double len = sqrt(len2);
+	double depth = sum_r - len;
+	const double cap = (lo.radius < hi.radius) ? lo.radius : hi.radius;
+	if (depth > cap) depth = cap;
+	double n[3] = {0, 0, 0};
+	if (!safe_normalize(D, d, n)) {
+		for (int k = 0; k < D; ++k) n[k] = 0;
+		n[0] = 1;
+	}
+	double off[3] = {0, 0, 0};
+	for (int k = 0; k < D; ++k) off[k] = n[k] * (hi.radius - depth * 0.5);
+	if (!self_is_lo)
+		for (int k = 0; k < D; ++k) n[k] = -n[k];
+	double r_s[3] = {0, 0, 0}, r_o[3] = {0, 0, 0};
+	for (int k = 0; k < D; ++k) {
+		const double pt = hi.position[k] + off[k];
+		r_s[k] = pt - self.position[k];
+		r_o[k] = pt - other.position[k];
+	}
+	if (periodic) {
+		if (r_s[0] > 0.5 * Lx) r_s[0] -= Lx; else if (r_s[0] < -0.5 * Lx) r_s[0] += Lx;
+		if (r_o[0] > 0.5 * Lx) r_o[0] -= Lx; else if (r_o[0] < -0.5 * Lx) r_o[0] += Lx;
+	}
+	double v_s[3] = {0, 0, 0}, v_o[3] = {0, 0, 0}, v_rel[3] = {0, 0, 0};
+	surface_velocity(D, self, r_s, steps, v_s);
+	surface_velocity(D, other, r_o, steps, v_o);
+	for (int k = 0; k < D; ++k) v_rel[k] = v_s[k] - v_o[k];
+	const double m_eff = (self.mass * other.mass) / (self.mass + other.mass);
+	double t[3] = {0, 0, 0};
+	soft_shell(D, n, depth, r_s, v_rel, m_eff, prm, f, t);
+	*torque0 = t[0];
+	return true;
+}
+
+// One warp per body: the lanes evaluate its pairs 32 at a time, then lane 0
+// adds the contacts in index order (the reference's accumulation order, so
+// the FP64 result is bit-identical) and finally the box walls.
 __global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_params prm, int nx, int ny, int nz,
 						  int periodic) {
-	const int s = blockIdx.x * blockDim.x + threadIdx.x;
-	if (s >= np) return;
+	__shared__ double fs[4][32][4];
+	__shared__ int hs[4][32];
+	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int s = blockIdx.x * 4 + w;
+	if (s >= np) return; // warp-uniform
 	const double steps = (double)(prm.sub_steps == 0 ? 1 : prm.sub_steps);
 	const double Lx = (double)nx;
 	const double ext[3] = {(double)nx, (double)ny, (double)nz};
 	const kel_particle_state &self = P[s];
 	double force[3] = {self.force[0], self.force[1], self.force[2]};
 	double torque0 = self.torque[0];
-	for (int j = 0; j < np; ++j) {
-		if (j == s) continue;
-		const kel_particle_state &other = P[j];
-		double dd[3] = {0, 0, 0};
-		pdiff(D, self.position, other.position, periodic, Lx, dd);
-		double n2 = 0.0;
-		for (int k = 0; k < D; ++k) n2 = n2 + dd[k] * dd[k];
-		const double rl = self.radius, rr = other.radius;
-		if (!(n2 < rl * rl + rr * rr + rr * rl * 2.0)) continue;
-		const bool self_is_lo = s < j;
-		const kel_particle_state &lo = self_is_lo ? self : other;
-		const kel_particle_state &hi = self_is_lo ? other : self;
-		double d[3] = {0, 0, 0};
-		pdiff(D, lo.position, hi.position, periodic, Lx, d);
-		double len2 = 0.0;
-		for (int k = 0; k < D; ++k) len2 = len2 + d[k] * d[k];
-		const double sum_r = lo.radius + hi.radius;
-		if (!(len2 < sum_r * sum_r)) continue;
-		const double len = sqrt(len2);
-		double depth = sum_r - len;
-		const double cap = (lo.radius < hi.radius) ? lo.radius : hi.radius;
-		if (depth > cap) depth = cap;
-		double n[3] = {0, 0, 0};
-		if (!safe_normalize(D, d, n)) {
-			for (int k = 0; k < D; ++k) n[k] = 0;
-			n[0] = 1;
+	for (int j0 = 0; j0 < np; j0 += 32) {
+		const int j = j0 + lane;
+		double f[3] = {0, 0, 0}, t0 = 0.0;
+		const bool hit = j < np && j != s && pair_response(self, P[j], s, j, D, prm, steps, Lx, periodic, f, &t0);
+		fs[w][lane][0] = f[0];
+		fs[w][lane][1] = f[1];
+		fs[w][lane][2] = f[2];
+		fs[w][lane][3] = t0;
+		hs[w][lane] = hit ? 1 : 0;
+		__syncwarp();
+		if (lane == 0) {
+			for (int q = 0; q < 32; ++q) {
+				if (!hs[w][q]) continue;
+				for (int k = 0; k < D; ++k) force[k] = force[k] + fs[w][q][k];
+				if (D == 2) torque0 = torque0 + fs[w][q][3];
+			}
 		}
-		double off[3] = {0, 0, 0};
-		for (int k = 0; k < D; ++k) off[k] = n[k] * (hi.radius - depth * 0.5);
-		if (!self_is_lo)
-			for (int k = 0; k < D; ++k) n[k] = -n[k];
-		double r_s[3] = {0, 0, 0}, r_o[3] = {0, 0, 0};
-		for (int k = 0; k < D; ++k) {
-			const double pt = hi.position[k] + off[k];
-			r_s[k] = pt - self.position[k];
-			r_o[k] = pt - other.position[k];
-		}
-		if (periodic) {
-			if (r_s[0] > 0.5 * Lx) r_s[0] -= Lx; else if (r_s[0] < -0.5 * Lx) r_s[0] += Lx;
-			if (r_o[0] > 0.5 * Lx) r_o[0] -= Lx; else if (r_o[0] < -0.5 * Lx) r_o[0] += Lx;
-		}
-		double v_s[3] = {0, 0, 0}, v_o[3] = {0, 0, 0}, v_rel[3] = {0, 0, 0};
-		surface_velocity(D, self, r_s, steps, v_s);
-		surface_velocity(D, other, r_o, steps, v_o);
-		for (int k = 0; k < D; ++k) v_rel[k] = v_s[k] - v_o[k];
-		const double m_eff = (self.mass * other.mass) / (self.mass + other.mass);
-		double f[3] = {0, 0, 0}, t[3] = {0, 0, 0};
-		soft_shell(D, n, depth, r_s, v_rel, m_eff, prm, f, t);
-		for (int k = 0; k < D; ++k) force[k] = force[k] + f[k];
-		if (D == 2) torque0 = torque0 + t[0];
+		__syncwarp();
 	}
+	if (lane != 0) return;
 	for (int ax = 0; ax < D; ++ax) {
 		if (!(prm.wall_axes & (1u << ax))) continue;
 		const double x = self.position[ax], r = self.radius, hb = ext[ax];
@@ -425,7 +454,8 @@ __global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_par
 			if (D == 2) torque0 = torque0 + t[0];
 		}
 	}
-	// only this thread writes body s; the others read its position fields only
+	// only lane 0 of this warp writes body s; the other warps read its
+	// position fields only
 	P[s].force[0] = force[0];
 	P[s].force[1] = force[1];
 	P[s].force[2] = force[2];
@@ -600,7 +630,7 @@ static int particles_gather(kel_particles *ps, const kel_particle_params *prm, b
 
 static int particles_contact(kel_particles *ps, const kel_particle_params *prm) {
 	kel_lattice *L = ps->lat;
-	k_contact<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(ps->d, ps->n, L->d.D, *prm, (int)L->desc.nx, (int)L->desc.ny,
+	k_contact<<<(ps->n + 3) / 4, 128, 0, L->stream>>>(ps->d, ps->n, L->d.D, *prm, (int)L->desc.nx, (int)L->desc.ny,
 														   (int)L->desc.nz, (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
