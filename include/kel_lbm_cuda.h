@@ -248,6 +248,19 @@ int kel_batch_info(const kel_batch *b, int64_t *cells, int64_t *padded_cells, in
 int kel_batch_download_populations(kel_batch *b, int32_t channel, float *host_aos);
 int kel_batch_download_macros(kel_batch *b, int32_t channel, float *host_rho_u);
 
+/* Relative L2 change sqrt(sum |u - u_prev|^2 / sum |u|^2) of a velocity
+ * field, FP64 sums, written to *d_result (a device double) on `stream`.
+ * d_u and d_u_prev hold `comps` planes of n floats each (device pointers).
+ * No counterpart in the reference.  Allocates nothing: for callers that may
+ * not allocate device memory while they run (cudaMalloc/cudaFree synchronise
+ * the device and fail once a pooling allocator owns the memory).  Its scratch
+ * is a fixed device array of 65,536 tiles, so n is limited to 16,777,216
+ * cells; larger n is rejected with KEL_ERR_INVALID_ARGUMENT.  The first call
+ * on a device looks up the scratch address (make it before any stream
+ * capture).  Calls share the scratch: calls that overlap on the GPU race. */
+int kel_velocity_residual_noalloc(const float *d_u, const float *d_u_prev, int64_t n, int32_t comps,
+								  double *d_result, void *stream);
+
 /* ---- learned warm start: conv U-Net (no counterpart in the reference) -- */
 
 typedef struct kel_unet_desc {

@@ -230,6 +230,7 @@ def load_library(path: str | None = None):
         "kel_lattice_synchronize": ([vp], C.c_int),
         "kel_lattice_set_launch": ([vp, i32, i32], C.c_int),
         "kel_batch_create": ([i32, C.POINTER(ChannelDesc), i32, C.POINTER(vp)], C.c_int),
+        "kel_velocity_residual_noalloc": ([vp, vp, i64, i32, vp, vp], C.c_int),
         "kel_unet_create": ([C.POINTER(UnetDesc), u64, C.POINTER(vp)], C.c_int),
         "kel_unet_destroy": ([vp], C.c_int),
         "kel_unet_param_count": ([vp, C.POINTER(i64)], C.c_int),
