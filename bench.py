@@ -41,6 +41,8 @@ WORKLOADS = {
     "d2q9_poiseuille_256x64": (9, (256, 64), 0.8, "poiseuille"),
     "d2q9_channel_4096x4096": (9, (4096, 4096), 0.8, "poiseuille"),
     "d2q9_batch_1024": (9, None, None, "batch"),
+    "d2q9_batch_1024_converge": (9, None, None, "batch_converge"),
+    "d2q9_warm_start_256x64": (9, (256, 64), None, "warm_start"),
     "d2q9_psm_particles_2048x512": (9, (2048, 512), 0.7, "particles"),
 }
 
@@ -189,7 +191,7 @@ def run_reference(args, rank, world):
 
 
 def run_batch(args, rank, world):
-    """Config C4: 1024 seeded uneven D2Q9 channels in one batched launch."""
+    """1024 seeded uneven D2Q9 channels in one batched launch."""
     import torch
     from lbm_mirror_gb300 import Batch
     from tests import cases
@@ -218,8 +220,125 @@ def run_batch(args, rank, world):
         print(json.dumps(line))
 
 
+def run_batch_converge(args, rank, world):
+    """The 1024 seeded uneven channels run from rest until every channel's
+    relative L2 change of u over 1000 steps is below --tol (one persistent
+    CUDA-graph replay per 1000 steps; converged channels' tiles are dropped
+    from the launch).  value = wall seconds to the last channel."""
+    import torch
+    from lbm_mirror_gb300 import Batch
+    from lbm_mirror_gb300 import capi as K
+    from lbm_mirror_gb300.workloads import batch_channels, channel_program
+    chans = batch_channels()
+    b = Batch(chans, channel_program(0.8, K.KEL_ARITH_SHIFTED))
+    tile, _ = b.autotune(steps=6)
+    cells, padded, _ = b.info()
+    b.synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    steps, res = b.run_until(tol=args.tol, check_every=1000, max_steps=args.max_steps)
+    dt = time.perf_counter() - t0
+    sizes = np.array([c["nx"] * c["ny"] for c in chans], dtype=np.float64)
+    updates = float(np.sum(sizes * steps.astype(np.float64)))
+    bpu = bytes_per_update(9, "fp32")
+    peak, src = load_peaks()
+    line = {"metric": "time_to_steady_state_s", "value": dt, "unit": "s", "n_gpus": world, "steps": int(steps.max()),
+            "warmup": 0, "ms_per_step": None, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (shifted: g = f - w)", "data": "synthetic",
+            "config": {"workload": "d2q9_batch_1024_converge", "channels": len(chans), "cells": cells,
+                       "padded_cells": padded, "tile": tile, "tol": args.tol, "check_every": 1000,
+                       "max_steps": args.max_steps},
+            "channel_steps": {"mean": float(steps.mean()), "median": float(np.median(steps)),
+                              "max": int(steps.max()), "unconverged": int(np.sum(res >= args.tol))},
+            "active_MLUPS": updates / dt / 1e6,
+            "roofline": {"bound": "hbm", "achieved": bpu * updates / dt / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": bpu * updates / dt / 1e9 / peak, "traffic": None, "peak_source": src,
+                         "bytes_per_update": bpu, "kernel": "batched sweep, averaged over the whole run"},
+            "gpu_launches": int(steps.max() // 1000 * 1002)}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def unet_flops_per_sample(h, w, widths, in_ch=16, out_ch=3):
+    """Multiply-adds x 2 of one U-Net forward pass (3x3 convolutions and the
+    1x1 head) on an h x w grid."""
+    w0, w1, w2, w3 = widths
+    convs = [(0, in_ch, w0), (0, w0, w0), (1, w0, w1), (1, w1, w1), (2, w1, w2), (2, w2, w2), (3, w2, w3),
+             (3, w3, w3), (2, w3 + w2, w2), (2, w2, w2), (1, w2 + w1, w1), (1, w1, w1), (0, w1 + w0, w0), (0, w0, w0)]
+    f = sum(2 * 9 * ci * co * (h >> lv) * (w >> lv) for lv, ci, co in convs)
+    return f + 2 * w0 * out_ch * h * w
+
+
+def run_warm_start(args, rank, world):
+    """Learned warm start on 256x64 channels: --train seeded steady states
+    (batched runner to --tol), U-Net training on them, then --test held-out
+    geometries run to --tol from rest and from the network's prediction.
+    value = wall seconds of the warm-started runs (inference and population
+    reconstruction included); plain_seconds = the same from rest."""
+    import torch
+    from lbm_mirror_gb300 import warmstart as WS
+    nx, ny = WORKLOADS[args.workload][1]
+    widths = (32, 64, 128, 128)
+    train_ch = WS.fixed_size_channels(args.train, seed=5, nx=nx, ny=ny)
+    test_ch = WS.fixed_size_channels(args.test, seed=6, nx=nx, ny=ny)
+    states = WS.solve(train_ch, tol=args.tol, check_every=1000, max_steps=args.max_steps)
+    gen_updates = float(np.sum(states.steps.astype(np.float64)) * nx * ny)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    model = WS.train(states, epochs=args.epochs, batch=32, lr=2e-3, widths=widths, log_every=32)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    n_steps = args.epochs * (args.train // 32)
+    train_flops = 3 * unet_flops_per_sample(ny, nx, widths) * 32 * n_steps
+    r = WS.evaluate(model, test_ch, tol=args.tol, check_every=1000, max_steps=args.max_steps)
+    # inference alone, timed with CUDA events on the network's own stream path
+    mask, u_max, tau = WS.channel_inputs(test_ch)
+    d_mask = torch.from_numpy(mask).cuda()
+    d_umax = torch.from_numpy(u_max).cuda()
+    d_tau = torch.from_numpy(tau).cuda()
+    WS.predict(model, d_mask, d_umax, d_tau)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    WS.predict(model, d_mask, d_umax, d_tau)
+    t_inf = time.perf_counter() - t1
+    inf_flops = unet_flops_per_sample(ny, nx, widths) * args.test
+    bf16 = None
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        bf16 = json.load(open(pk)).get("bf16_tflops")
+    if rank == 0:
+        if args.save_dir:
+            np.save(os.path.join(args.save_dir, "warm_start_unet_params.npy"), model.net.params())
+        line = {"metric": "time_to_steady_state_s", "value": r["warm_seconds"], "unit": "s", "n_gpus": world,
+                "steps": r["warm_steps_max"], "warmup": 0, "ms_per_step": None, "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 lattice, bf16 network", "data": "synthetic",
+                "config": {"workload": "d2q9_warm_start_256x64", "train": args.train, "test": args.test,
+                           "tol": args.tol, "check_every": 1000, "epochs": args.epochs, "widths": list(widths),
+                           "params": model.net.n_params, "rho_scale": model.rho_scale},
+                "plain_seconds": r["plain_seconds"], "speedup": r["speedup"],
+                "channel_steps": {k: r[k] for k in ("plain_steps_mean", "warm_steps_mean", "plain_steps_max",
+                                                    "warm_steps_max", "plain_unconverged", "warm_unconverged")},
+                "final_u_rel_l2": {"mean": r["final_u_rel_l2_mean"], "max": r["final_u_rel_l2_max"]},
+                "prediction_u_rel_l2": {"mean": r["prediction_u_rel_l2_mean"], "max": r["prediction_u_rel_l2_max"]},
+                "training": {"seconds": t_train, "adam_steps": n_steps, "batch": 32,
+                             "loss_first": model.history[0][1] if model.history else None,
+                             "loss_last": model.history[-1][1] if model.history else None,
+                             "tflops": train_flops / t_train / 1e12},
+                "inference": {"seconds": t_inf, "samples": args.test, "tflops": inf_flops / t_inf / 1e12},
+                "data_generation": {"seconds": states.seconds, "channels": args.train,
+                                    "unconverged": int(np.sum(~states.converged)),
+                                    "active_MLUPS": gen_updates / states.seconds / 1e6},
+                "roofline": {"bound": "tensor", "achieved": train_flops / t_train / 1e12,
+                             "peak": bf16, "unit": "TFLOP/s",
+                             "frac": (train_flops / t_train / 1e12 / bf16) if bf16 else None, "traffic": None,
+                             "peak_source": "measured" if bf16 else None,
+                             "kernel": "U-Net training step (whole step, host loop included)"},
+                "gpu_launches": None}
+        print(json.dumps(line))
+
+
 def run_particles(args, rank, world):
-    """Config C3: 2048x512 periodic channel, PSM + Guo gravity, 64 discs R = 8,
+    """Particle-laden channel: 2048x512 periodic channel, PSM + Guo gravity, 64 discs R = 8,
     4x4 sub-cell solid fraction, DEM k = 100, damping 0.1, FP64 bodies."""
     import torch
     from lbm_mirror_gb300 import Lattice, Particles
@@ -279,6 +398,12 @@ def main():
     ap.add_argument("--e2e-lbm-steps", type=int, default=100)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tol", type=float, default=1e-6, help="steady-state residual (converge / warm-start workloads)")
+    ap.add_argument("--max-steps", type=int, default=2_000_000)
+    ap.add_argument("--train", type=int, default=4096, help="warm start: training steady states")
+    ap.add_argument("--test", type=int, default=512, help="warm start: held-out geometries")
+    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--save-dir", default="", help="warm start: directory for the trained parameters")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -299,6 +424,12 @@ def main():
         return
     if WORKLOADS[args.workload][3] == "particles":
         run_particles(args, rank, world)
+        return
+    if WORKLOADS[args.workload][3] == "batch_converge":
+        run_batch_converge(args, rank, world)
+        return
+    if WORKLOADS[args.workload][3] == "warm_start":
+        run_warm_start(args, rank, world)
         return
     dist = None
     if world > 1:

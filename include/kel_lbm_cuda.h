@@ -73,6 +73,7 @@ extern "C" {
 /* ---- arithmetic mode of the sweep -------------------------------------- */
 #define KEL_ARITH_FAST 0      /* float-float equilibrium bracket, fused BGK relaxation */
 #define KEL_ARITH_REFERENCE 1 /* the reference's rounding sequence (double equilibrium bracket): bit-exact */
+#define KEL_ARITH_SHIFTED 2   /* batches only: FP32 populations stored and relaxed as g = f - w_i (lower rounding noise) */
 
 #define KEL_MAX_FLAGS 8
 
@@ -238,12 +239,26 @@ int kel_batch_step(kel_batch *b, uint64_t n_steps);
  * below `tol`, or until `max_steps`.  With use_graph the `check_every` sweeps
  * and the residual are one captured CUDA graph, replayed.  steps_out and
  * residual_out (n values each, may be NULL) receive each channel's final time
- * step and last residual. */
+ * step and last residual.  A channel whose residual is not finite (diverged)
+ * stops too; its residual_out is NaN or inf.  Once the tiles of the active
+ * channels are at most half of those launched, later sweeps launch only them. */
 int kel_batch_run_until(kel_batch *b, double tol, uint64_t check_every, uint64_t max_steps, int32_t use_graph,
 						uint64_t *steps_out, double *residual_out);
 int kel_batch_active_count(kel_batch *b, int32_t *count);
 int kel_batch_channel_time_step(const kel_batch *b, int32_t channel, uint64_t *t);
 int kel_batch_info(const kel_batch *b, int64_t *cells, int64_t *padded_cells, int32_t *tile);
+/* Warm start of channels [first, first + count), all at an even time step,
+ * from a predicted field (no counterpart in the reference).  Channel
+ * first + j reads d_pred + j * pred_stride (device): 3 floats per cell, x
+ * fastest, physical (u_x, u_y, rho) = value * scale + offset with
+ * d_scale / d_offset (device, 3 floats per channel).  Fluid cells get
+ * f_eq(rho, u) plus, with with_neq, the non-equilibrium part
+ * -(tau w_i rho / cs^2) Q_i : grad u (central differences, u = 0 in walls);
+ * wall cells get the rest state at the mean density of their fluid
+ * neighbours.  The residual's previous velocity becomes the predicted u. */
+int kel_batch_warm_start(kel_batch *b, int32_t first, int32_t count, const float *d_pred, int64_t pred_stride,
+						 const float *d_scale, const float *d_offset, int32_t with_neq);
+int kel_batch_synchronize(kel_batch *b);
 /* One channel's populations (AoS, nx*ny*9) or macros (rho, u_x, u_y per cell). */
 int kel_batch_download_populations(kel_batch *b, int32_t channel, float *host_aos);
 int kel_batch_download_macros(kel_batch *b, int32_t channel, float *host_rho_u);
@@ -293,6 +308,14 @@ int kel_unet_forward(kel_unet *net, int32_t n, float *d_out);
  * parameter gradient (FP32, overwritten).  *loss is written on the host. */
 int kel_unet_backward(kel_unet *net, const float *d_target, int32_t n, double *loss);
 int kel_unet_adam_step(kel_unet *net, float lr, float beta1, float beta2, float eps, int32_t step);
+/* Convolution kernels: KEL_UNET_CONV_TCGEN05 (tcgen05.mma with the
+ * accumulator in tensor memory) or KEL_UNET_CONV_MMA_SYNC (default; warp-level
+ * mma.sync).  Both compute bf16 x bf16 -> FP32; results agree to FP32
+ * summation order.  kel_unet_synchronize / kel_unet_backward return
+ * KEL_ERR_TIMEOUT if a tensor-core kernel gave up on a bounded wait. */
+#define KEL_UNET_CONV_TCGEN05 0
+#define KEL_UNET_CONV_MMA_SYNC 1
+int kel_unet_set_conv_kernel(kel_unet *net, int32_t kind);
 
 /* Launch shape of the sweep: cells per thread (1: 32-bit accesses, one cell;
  * 4: 128-bit accesses, four consecutive cells) and threads per block (64, 128

@@ -40,13 +40,14 @@ KEL_BC_ANTI_BOUNCE_BACK = 6
 KEL_BC_EQUILIBRIUM = 7
 
 KEL_COLL_BGK, KEL_COLL_BGK_GUO, KEL_COLL_PSM, KEL_COLL_PSM_GUO = 0, 1, 2, 3
-KEL_ARITH_FAST, KEL_ARITH_REFERENCE = 0, 1
+KEL_ARITH_FAST, KEL_ARITH_REFERENCE, KEL_ARITH_SHIFTED = 0, 1, 2
 KEL_MAX_FLAGS = 8
 
 KEL_DTYPE_F32, KEL_DTYPE_F64 = 0, 1
 KEL_LAYOUT_AOS, KEL_LAYOUT_SOA = 0, 1
 KEL_FIELD_POROSITY, KEL_FIELD_FORCE = 1, 2
 KEL_STEP_WRITE_MACROS, KEL_STEP_ALL_MACROS = 1, 2
+KEL_UNET_CONV_TCGEN05, KEL_UNET_CONV_MMA_SYNC = 0, 1
 
 
 class FlagOp(C.Structure):
@@ -244,6 +245,7 @@ def load_library(path: str | None = None):
         "kel_unet_forward": ([vp, i32, vp], C.c_int),
         "kel_unet_backward": ([vp, vp, i32, C.POINTER(C.c_double)], C.c_int),
         "kel_unet_adam_step": ([vp, C.c_float, C.c_float, C.c_float, C.c_float, i32], C.c_int),
+        "kel_unet_set_conv_kernel": ([vp, i32], C.c_int),
         "kel_batch_destroy": ([vp], C.c_int),
         "kel_batch_upload_flags": ([vp, vp], C.c_int),
         "kel_batch_set_program": ([vp, C.POINTER(StepProgram)], C.c_int),
@@ -255,6 +257,8 @@ def load_library(path: str | None = None):
         "kel_batch_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i32)], C.c_int),
         "kel_batch_download_populations": ([vp, i32, vp], C.c_int),
         "kel_batch_download_macros": ([vp, i32, vp], C.c_int),
+        "kel_batch_warm_start": ([vp, i32, i32, vp, i64, vp, vp, i32], C.c_int),
+        "kel_batch_synchronize": ([vp], C.c_int),
         "kel_lattice_get_launch": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "kel_lattice_autotune": ([vp, C.POINTER(StepProgram), i32, C.POINTER(i32), C.POINTER(i32),
                                   C.POINTER(C.c_float)], C.c_int),

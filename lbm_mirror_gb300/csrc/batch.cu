@@ -45,19 +45,128 @@ struct BatchParams {
 	const float *profiles;
 	const ChannelRec *ch;
 	const int *block_ch;
+	const int *blist; // launched block -> tile (all tiles, or those of active channels)
 	int *active;
 	double2 *partial; // per-tile residual partial sums (scratch)
 	int tile;
 	int write_macros;
+	int shifted; // populations hold g = f - w_i (MODE_SHIFTED)
 };
 
-template <bool ODD, bool EXACT>
+// Arithmetic of a batch: the library's two (fast, reference rounding) on
+// populations f, or SHIFTED on g = f - w_i (FP32 storage of the deviation
+// from rest, "DDF shifting").  The rest populations (w_0 = 4/9 ...) dominate
+// the rounding error of f in FP32; g is of the order of the flow's own
+// deviation, so its rounding noise, which sets the floor of the relative
+// velocity change a run can reach, is one to two orders of magnitude lower.
+enum { MODE_FAST = 0, MODE_EXACT = 1, MODE_SHIFTED = 2 };
+
+// One D2Q9 cell in shifted form: the same operations as cell_update for the
+// boundaries a batch accepts, written on g.  Bounce-back and anti-bounce-back
+// permute directions of equal weight, so they act on g unchanged; Zou-He
+// keeps its linear updates (pairs of equal weight cancel) with the closure
+// sums taken on g (the weights of the summed populations add up to 1); BGK
+// relaxes g towards g_eq = w (rho - 1) + w rho (3 c.u + 4.5 (c.u)^2 - 1.5 u^2).
+__device__ __forceinline__ bool cell_update_shifted(float (&g)[9], int flag, int y, const CellCtx &p, float &rho,
+													float (&u)[3]) {
+	using L = D2Q9;
+	if (flag == 0) {
+#pragma unroll
+		for (int i = 0; i < 9; ++i) g[i] = 0.f;
+		return false;
+	}
+	if (flag >= MAX_FLAGS) return false;
+	const OpEntry *op = p.ops + flag;
+	const int bc = __ldg(&op->bc);
+	const float c23 = (float)(2.0 / 3.0), c16 = (float)(1.0 / 6.0);
+	float t;
+	switch (bc) {
+	case BC_BOUNCE_BACK:
+		t = g[1]; g[1] = g[2]; g[2] = t;
+		t = g[3]; g[3] = g[4]; g[4] = t;
+		t = g[5]; g[5] = g[8]; g[8] = t;
+		t = g[6]; g[6] = g[7]; g[7] = t;
+		break;
+	case BC_ANTI_BOUNCE_BACK:
+		t = g[3]; g[3] = g[4]; g[4] = t;
+		t = g[5]; g[5] = g[7]; g[7] = t;
+		t = g[6]; g[6] = g[8]; g[8] = t;
+		break;
+	case BC_ZOUHE_PRESSURE_X: {
+		const bool east = __ldg(&op->east) != 0;
+		const float drs = __ldg(&op->rho) - 1.0f;
+		if (east) {
+			const float Sg = (g[0] + g[3] + g[4]) + 2.f * (g[1] + g[5] + g[7]);
+			const float r = drs - Sg;
+			g[2] = g[1] + c23 * r;
+			g[6] = g[5] + c16 * r + 0.5f * (g[3] - g[4]);
+			g[8] = g[7] + c16 * r + 0.5f * (g[4] - g[3]);
+		} else {
+			const float Sg = (g[0] + g[3] + g[4]) + 2.f * (g[2] + g[6] + g[8]);
+			const float r = Sg - drs;
+			g[1] = g[2] - c23 * r;
+			g[5] = g[6] - c16 * r + 0.5f * (g[4] - g[3]);
+			g[7] = g[8] - c16 * r + 0.5f * (g[3] - g[4]);
+		}
+		break;
+	}
+	case BC_ZOUHE_VELOCITY_X: {
+		const bool east = __ldg(&op->east) != 0;
+		const float ux = __ldg(&op->use_profile) ? __ldg(p.profile + y) : __ldg(&op->u[0]);
+		const float uy = __ldg(&op->u[1]);
+		const float dg = east ? (g[1] + g[5] + g[7]) : (g[2] + g[6] + g[8]);
+		// rho = (f0 + f4 + f3 + 2 ds) / (u_x + 1) as the library's Zou-He inlet
+		const float r0 = (1.0f + ((g[0] + g[4] + g[3]) + 2.f * dg)) / (ux + 1.0f);
+		const float rux = c16 * r0 * ux, ruy = r0 * uy;
+		if (east) {
+			g[2] = g[1] + c23 * r0 * ux;
+			g[6] = g[5] + rux + 0.5f * (g[3] - g[4] + ruy);
+			g[8] = g[7] + rux + 0.5f * (g[4] - g[3] + ruy);
+		} else {
+			g[1] = g[2] + c23 * r0 * ux;
+			g[5] = g[6] + rux + 0.5f * (g[4] - g[3] + ruy);
+			g[7] = g[8] + rux + 0.5f * (g[3] - g[4] + ruy);
+		}
+		break;
+	}
+	default:
+		break;
+	}
+	if (!__ldg(&op->collide)) return false;
+	// moments on g: rho - 1 = sum g, rho u = sum c g
+	float drho = 0.f, jx = 0.f, jy = 0.f;
+#pragma unroll
+	for (int i = 0; i < 9; ++i) {
+		drho += g[i];
+		if (L::cx(i) > 0) jx += g[i];
+		if (L::cx(i) < 0) jx -= g[i];
+		if (L::cy(i) > 0) jy += g[i];
+		if (L::cy(i) < 0) jy -= g[i];
+	}
+	rho = 1.0f + drho;
+	const float ir = 1.0f / rho;
+	u[0] = jx * ir;
+	u[1] = jy * ir;
+	u[2] = 0.f;
+	const float h = 1.5f * (u[0] * u[0] + u[1] * u[1]);
+#pragma unroll
+	for (int i = 0; i < 9; ++i) {
+		const float w = (float)L::w(i);
+		const float vcc = 3.f * ((float)L::cx(i) * u[0] + (float)L::cy(i) * u[1]);
+		const float geq = __fmaf_rn(w * rho, vcc + __fmaf_rn(0.5f * vcc, vcc, -h), w * drho);
+		g[i] = __fmaf_rn(p.omega, geq - g[i], g[i]);
+	}
+	return true;
+}
+
+template <bool ODD, int MODE>
 __global__ void __launch_bounds__(512) k_batch_sweep(const __grid_constant__ BatchParams p) {
 	using L = D2Q9;
-	const int c = p.block_ch[blockIdx.x];
+	const int ob = p.blist[blockIdx.x];
+	const int c = p.block_ch[ob];
 	if (!p.active[c]) return;
 	const ChannelRec ch = p.ch[c];
-	const int l = (blockIdx.x - ch.first_block) * blockDim.x + threadIdx.x;
+	const int l = (ob - ch.first_block) * blockDim.x + threadIdx.x;
 	if (l >= ch.nxp * ch.ny) return;
 	const int y = l / ch.nxp, x = l - y * ch.nxp;
 	const int64_t cell = ch.off + l;
@@ -80,7 +189,9 @@ __global__ void __launch_bounds__(512) k_batch_sweep(const __grid_constant__ Bat
 	ctx.g[0] = ctx.g[1] = ctx.g[2] = 0.f;
 	const float Fc[3] = {0.f, 0.f, 0.f};
 	float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
-	const bool col = cell_update<L, COLL_BGK, EXACT>(f, p.flags[cell], y, ctx, 1.f, Fc, rho, u);
+	const bool col = MODE == MODE_SHIFTED
+						 ? cell_update_shifted(f, p.flags[cell], y, ctx, rho, u)
+						 : cell_update<L, COLL_BGK, MODE == MODE_EXACT>(f, p.flags[cell], y, ctx, 1.f, Fc, rho, u);
 	if (p.write_macros && col) {
 		p.rho[cell] = rho;
 		p.u[cell] = u[0];
@@ -104,11 +215,12 @@ __global__ void __launch_bounds__(512) k_batch_sweep(const __grid_constant__ Bat
 // u_prev = u.  Fixed reduction order (warp shuffle, then warps in order).
 __global__ void __launch_bounds__(512) k_batch_residual_partial(BatchParams p) {
 	__shared__ double sh[2][16];
-	const int c = p.block_ch[blockIdx.x];
+	const int ob = p.blist[blockIdx.x];
+	const int c = p.block_ch[ob];
 	double num = 0.0, den = 0.0;
 	if (p.active[c]) {
 		const ChannelRec ch = p.ch[c];
-		const int l = (blockIdx.x - ch.first_block) * blockDim.x + threadIdx.x;
+		const int l = (ob - ch.first_block) * blockDim.x + threadIdx.x;
 		if (l < ch.nxp * ch.ny) {
 			const int64_t cell = ch.off + l;
 			for (int d = 0; d < 2; ++d) {
@@ -134,12 +246,13 @@ __global__ void __launch_bounds__(512) k_batch_residual_partial(BatchParams p) {
 			a += sh[0][w];
 			b += sh[1][w];
 		}
-		p.partial[blockIdx.x] = make_double2(a, b);
+		p.partial[ob] = make_double2(a, b);
 	}
 }
 
 // Per channel: relative L2 change sqrt(sum|du|^2 / sum|u|^2) over its tiles
-// (in tile order); a channel below `tol` is deactivated.
+// (in tile order); a channel below `tol` is deactivated, and so is one whose
+// residual is not finite (a diverged run; its residual stays NaN / inf).
 __global__ void k_batch_residual_final(BatchParams p, int n_channels, double tol, double *residual) {
 	const int c = blockIdx.x * blockDim.x + threadIdx.x;
 	if (c >= n_channels || !p.active[c]) return;
@@ -152,12 +265,12 @@ __global__ void k_batch_residual_final(BatchParams p, int n_channels, double tol
 	}
 	const double r = b > 0.0 ? sqrt(a / b) : (a > 0.0 ? INFINITY : 0.0);
 	residual[c] = r;
-	if (r < tol) p.active[c] = 0;
+	if (r < tol || !isfinite(r)) p.active[c] = 0;
 }
 
 __global__ void k_batch_init(BatchParams p, int64_t n) {
 	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
-		for (int i = 0; i < 9; ++i) p.f[i * p.plane + k] = (float)D2Q9::w(i);
+		for (int i = 0; i < 9; ++i) p.f[i * p.plane + k] = p.shifted ? 0.f : (float)D2Q9::w(i);
 		p.rho[k] = 1.f;
 		p.u[k] = p.u[p.plane + k] = 0.f;
 		p.u_prev[k] = p.u_prev[p.plane + k] = 0.f;
@@ -186,12 +299,13 @@ __global__ void k_batch_download(BatchParams p, ChannelRec ch, int odd, int what
 		if (what == 0) {
 			for (int i = 0; i < 9; ++i) {
 				float v;
+				const float wi = p.shifted ? (float)D2Q9::w(i) : 0.f;
 				if (!odd) {
-					v = p.f[i * p.plane + cell];
+					v = p.f[i * p.plane + cell] + wi;
 				} else {
 					const int sx = x - D2Q9::cx(i), sy = y - D2Q9::cy(i);
 					v = (sx >= 0 && sx < ch.nxp && sy >= 0 && sy < ch.ny)
-							? p.f[D2Q9::opp(i) * p.plane + ch.off + (int64_t)sy * ch.nxp + sx]
+							? p.f[D2Q9::opp(i) * p.plane + ch.off + (int64_t)sy * ch.nxp + sx] + wi
 							: 0.f;
 				}
 				out[k * 9 + i] = v;
@@ -204,6 +318,82 @@ __global__ void k_batch_download(BatchParams p, ChannelRec ch, int odd, int what
 	}
 }
 
+// Warm start of channels [first, first + gridDim.y) at an even time step.
+// Channel first + j reads its predicted field at pred + j * pred_stride: three
+// values v per cell (x fastest), physical (u_x, u_y, rho) = v * scale + offset
+// with scale / offset = sc[3j..3j+2] / of[3j..3j+2].  A fluid cell gets
+//   f_i = f_eq(rho, u) - (tau w_i rho / cs^2) Q_i : grad u   (with_neq)
+// with Q_i = c_i c_i - cs^2 I and grad u by central differences (one-sided at
+// the channel ends; u = 0 in wall cells): the first-order Chapman-Enskog
+// population of the predicted field.  A wall cell (flag 1) gets the rest state
+// at the mean predicted density of its fluid neighbours; u_prev takes the
+// predicted u, so the first residual measures the change from the prediction.
+__global__ void k_batch_warm_start(BatchParams p, int first, const float *pred, int64_t pred_stride, const float *sc,
+								   const float *of, int with_neq) {
+	const int j = blockIdx.y;
+	const ChannelRec ch = p.ch[first + j];
+	const float *pr = pred + (int64_t)j * pred_stride;
+	const float s0 = sc[3 * j], s1 = sc[3 * j + 1], s2 = sc[3 * j + 2];
+	const float o0 = of[3 * j], o1 = of[3 * j + 1], o2 = of[3 * j + 2];
+	const float tau = 1.f / ch.omega;
+	const int64_t n = (int64_t)ch.nx * ch.ny;
+	auto is_fluid = [&](int xx, int yy) {
+		const uint8_t f2 = p.flags[ch.off + (int64_t)yy * ch.nxp + xx];
+		return f2 != 1 && f2 != 0;
+	};
+	auto ux_at = [&](int xx, int yy) {
+		return is_fluid(xx, yy) ? pr[((int64_t)yy * ch.nx + xx) * 3 + 0] * s0 + o0 : 0.f;
+	};
+	auto uy_at = [&](int xx, int yy) {
+		return is_fluid(xx, yy) ? pr[((int64_t)yy * ch.nx + xx) * 3 + 1] * s1 + o1 : 0.f;
+	};
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+		const int y = (int)(k / ch.nx), x = (int)(k - (int64_t)y * ch.nx);
+		const int64_t cell = ch.off + (int64_t)y * ch.nxp + x;
+		float f[9];
+		if (!is_fluid(x, y)) {
+			float rs = 0.f;
+			int cnt = 0;
+			for (int i = 1; i < 9; ++i) {
+				const int xx = x + D2Q9::cx(i), yy = y + D2Q9::cy(i);
+				if (xx >= 0 && xx < ch.nx && yy >= 0 && yy < ch.ny && is_fluid(xx, yy)) {
+					rs += pr[((int64_t)yy * ch.nx + xx) * 3 + 2] * s2 + o2;
+					++cnt;
+				}
+			}
+			const float rho = cnt ? rs / (float)cnt : 1.f;
+			for (int i = 0; i < 9; ++i) f[i] = (float)D2Q9::w(i) * rho;
+		} else {
+			float u[3] = {ux_at(x, y), uy_at(x, y), 0.f};
+			const float rho = pr[k * 3 + 2] * s2 + o2;
+			equilibrium<D2Q9, true>(rho, u, f);
+			if (with_neq) {
+				const int xm = x > 0 ? x - 1 : x, xp = x + 1 < ch.nx ? x + 1 : x;
+				const int ym = y > 0 ? y - 1 : y, yp = y + 1 < ch.ny ? y + 1 : y;
+				const float ix = 1.f / (float)(xp - xm), iy = 1.f / (float)(yp - ym);
+				const float dxu = (ux_at(xp, y) - ux_at(xm, y)) * ix, dxv = (uy_at(xp, y) - uy_at(xm, y)) * ix;
+				const float dyu = (ux_at(x, yp) - ux_at(x, ym)) * iy, dyv = (uy_at(x, yp) - uy_at(x, ym)) * iy;
+				const float sxy = 0.5f * (dxv + dyu);
+				for (int i = 0; i < 9; ++i) {
+					const float cx = (float)D2Q9::cx(i), cy = (float)D2Q9::cy(i);
+					const float qs = (cx * cx - 1.f / 3.f) * dxu + (cy * cy - 1.f / 3.f) * dyv + 2.f * cx * cy * sxy;
+					f[i] -= tau * (float)D2Q9::w(i) * rho * 3.f * qs;
+				}
+			}
+			p.u_prev[cell] = u[0];
+			p.u_prev[p.plane + cell] = u[1];
+		}
+		for (int i = 0; i < 9; ++i) p.f[i * p.plane + cell] = f[i] - (p.shifted ? (float)D2Q9::w(i) : 0.f);
+	}
+}
+
+// f <-> g = f - w_i on every slot (sign -1: to shifted, +1: back), when a
+// program switches between shifted and unshifted arithmetic
+__global__ void k_batch_shift(BatchParams p, float sign) {
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < p.plane; k += (int64_t)gridDim.x * blockDim.x)
+		for (int i = 0; i < 9; ++i) p.f[i * p.plane + k] += sign * (float)D2Q9::w(i);
+}
+
 } // namespace
 
 struct kel_batch {
@@ -212,6 +402,8 @@ struct kel_batch {
 	std::vector<kel_channel_desc> desc;
 	std::vector<ChannelRec> rec;
 	std::vector<int> block_ch;
+	std::vector<int> blist; // launched tiles (host copy of d_blist)
+	int nlaunch = 0;        // tiles launched per sweep
 	std::vector<uint64_t> t;          // per-channel time step
 	std::vector<uint8_t> host_flags;  // packed copy (kept for re-layout)
 	std::vector<float> host_profiles; // packed inlet profiles
@@ -222,13 +414,14 @@ struct kel_batch {
 	float *f = nullptr, *rho = nullptr, *u = nullptr, *u_prev = nullptr, *profiles = nullptr;
 	uint8_t *flags = nullptr;
 	ChannelRec *d_rec = nullptr;
-	int *d_block_ch = nullptr, *d_active = nullptr;
+	int *d_block_ch = nullptr, *d_active = nullptr, *d_blist = nullptr;
 	double2 *partial = nullptr;
 	double *d_residual = nullptr;
 	OpEntry *ops = nullptr;
 	bool have_ops = false;
 	kel_step_program prog;
-	bool exact = false;
+	int mode = MODE_FAST; // arithmetic of the sweep
+	bool shifted = false; // populations stored as g = f - w_i
 	cudaStream_t stream = nullptr;
 	bool own_stream = false;
 	cudaGraphExec_t graph = nullptr;
@@ -247,13 +440,14 @@ void free_device(kel_batch *B) {
 	cudaFree(B->flags);
 	cudaFree(B->d_rec);
 	cudaFree(B->d_block_ch);
+	cudaFree(B->d_blist);
 	cudaFree(B->d_active);
 	cudaFree(B->partial);
 	cudaFree(B->d_residual);
 	B->f = B->rho = B->u = B->u_prev = B->profiles = nullptr;
 	B->flags = nullptr;
 	B->d_rec = nullptr;
-	B->d_block_ch = B->d_active = nullptr;
+	B->d_block_ch = B->d_active = B->d_blist = nullptr;
 	B->partial = nullptr;
 	B->d_residual = nullptr;
 	if (B->graph) cudaGraphExecDestroy(B->graph);
@@ -273,10 +467,12 @@ BatchParams params(const kel_batch *B, int write_macros) {
 	p.profiles = B->profiles;
 	p.ch = B->d_rec;
 	p.block_ch = B->d_block_ch;
+	p.blist = B->d_blist;
 	p.active = B->d_active;
 	p.partial = B->partial;
 	p.tile = B->tile;
 	p.write_macros = write_macros;
+	p.shifted = B->shifted ? 1 : 0;
 	return p;
 }
 
@@ -316,6 +512,12 @@ int layout(kel_batch *B, int tile) {
 	KEL_CUDA(cudaMalloc(&B->flags, B->plane));
 	KEL_CUDA(cudaMalloc(&B->d_rec, sizeof(ChannelRec) * B->n));
 	KEL_CUDA(cudaMalloc(&B->d_block_ch, sizeof(int) * B->nblocks));
+	KEL_CUDA(cudaMalloc(&B->d_blist, sizeof(int) * B->nblocks));
+	B->blist.resize(B->nblocks);
+	for (int b = 0; b < B->nblocks; ++b) B->blist[b] = b;
+	B->nlaunch = B->nblocks;
+	KEL_CUDA(cudaMemcpyAsync(B->d_blist, B->blist.data(), sizeof(int) * B->nblocks, cudaMemcpyHostToDevice,
+							 B->stream));
 	KEL_CUDA(cudaMalloc(&B->d_active, sizeof(int) * B->n));
 	KEL_CUDA(cudaMalloc(&B->partial, sizeof(double2) * B->nblocks));
 	KEL_CUDA(cudaMalloc(&B->d_residual, sizeof(double) * B->n));
@@ -357,19 +559,26 @@ int layout(kel_batch *B, int tile) {
 
 cudaError_t launch_sweep_batch(const kel_batch *B, bool odd, int write_macros) {
 	BatchParams p = params(B, write_macros);
-	if (B->exact) {
-		if (odd) k_batch_sweep<true, true><<<B->nblocks, B->tile, 0, B->stream>>>(p);
-		else k_batch_sweep<false, true><<<B->nblocks, B->tile, 0, B->stream>>>(p);
-	} else {
-		if (odd) k_batch_sweep<true, false><<<B->nblocks, B->tile, 0, B->stream>>>(p);
-		else k_batch_sweep<false, false><<<B->nblocks, B->tile, 0, B->stream>>>(p);
+	const dim3 g(B->nlaunch), b(B->tile);
+	switch (B->mode) {
+	case MODE_EXACT:
+		if (odd) k_batch_sweep<true, MODE_EXACT><<<g, b, 0, B->stream>>>(p);
+		else k_batch_sweep<false, MODE_EXACT><<<g, b, 0, B->stream>>>(p);
+		break;
+	case MODE_SHIFTED:
+		if (odd) k_batch_sweep<true, MODE_SHIFTED><<<g, b, 0, B->stream>>>(p);
+		else k_batch_sweep<false, MODE_SHIFTED><<<g, b, 0, B->stream>>>(p);
+		break;
+	default:
+		if (odd) k_batch_sweep<true, MODE_FAST><<<g, b, 0, B->stream>>>(p);
+		else k_batch_sweep<false, MODE_FAST><<<g, b, 0, B->stream>>>(p);
 	}
 	return cudaGetLastError();
 }
 
 cudaError_t launch_residual(const kel_batch *B, double tol) {
 	BatchParams p = params(B, 0);
-	k_batch_residual_partial<<<B->nblocks, B->tile, 0, B->stream>>>(p);
+	k_batch_residual_partial<<<B->nlaunch, B->tile, 0, B->stream>>>(p);
 	k_batch_residual_final<<<(B->n + 127) / 128, 128, 0, B->stream>>>(p, B->n, tol, B->d_residual);
 	return cudaGetLastError();
 }
@@ -456,9 +665,16 @@ extern "C" int kel_batch_set_program(kel_batch *B, const kel_step_program *P) {
 		ops[fl].rho = (float)o.rho;
 		for (int k = 0; k < 3; ++k) ops[fl].u[k] = (float)o.u[k];
 	}
-	if (P->arithmetic != KEL_ARITH_FAST && P->arithmetic != KEL_ARITH_REFERENCE)
+	if (P->arithmetic != KEL_ARITH_FAST && P->arithmetic != KEL_ARITH_REFERENCE && P->arithmetic != KEL_ARITH_SHIFTED)
 		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_set_program: unknown arithmetic");
-	B->exact = P->arithmetic == KEL_ARITH_REFERENCE;
+	B->mode = P->arithmetic == KEL_ARITH_REFERENCE ? MODE_EXACT
+			  : (P->arithmetic == KEL_ARITH_SHIFTED ? MODE_SHIFTED : MODE_FAST);
+	const bool shifted = B->mode == MODE_SHIFTED;
+	if (shifted != B->shifted) { // re-express the stored populations
+		B->shifted = shifted;
+		k_batch_shift<<<grid_for(B->plane), 256, 0, B->stream>>>(params(B, 0), shifted ? -1.f : 1.f);
+		KEL_CUDA(cudaGetLastError());
+	}
 	KEL_CUDA(cudaMemcpyAsync(B->ops, ops, sizeof(ops), cudaMemcpyHostToDevice, B->stream));
 	KEL_CUDA(cudaStreamSynchronize(B->stream));
 	B->prog = *P;
@@ -492,6 +708,26 @@ extern "C" int kel_batch_step(kel_batch *B, uint64_t n_steps) {
 	for (int c = 0; c < B->n; ++c)
 		if (act[c]) B->t[c] += n_steps;
 	KEL_CUDA(cudaStreamSynchronize(B->stream));
+	return KEL_OK;
+}
+
+// Launch only the tiles of active channels once they are at most half of
+// the tiles launched so far (a converged channel's tiles otherwise still
+// cost a block launch each per sweep).  Any captured graph is dropped.
+static int compact(kel_batch *B, const std::vector<int> &act) {
+	int keep = 0;
+	for (int c = 0; c < B->n; ++c)
+		if (act[c]) keep += B->rec[c].nblocks;
+	if (keep == 0 || 2 * keep > B->nlaunch) return KEL_OK;
+	B->blist.clear();
+	for (int c = 0; c < B->n; ++c)
+		if (act[c])
+			for (int k = 0; k < B->rec[c].nblocks; ++k) B->blist.push_back(B->rec[c].first_block + k);
+	KEL_CUDA(cudaMemcpyAsync(B->d_blist, B->blist.data(), sizeof(int) * keep, cudaMemcpyHostToDevice, B->stream));
+	KEL_CUDA(cudaStreamSynchronize(B->stream));
+	B->nlaunch = keep;
+	if (B->graph) cudaGraphExecDestroy(B->graph);
+	B->graph = nullptr;
 	return KEL_OK;
 }
 
@@ -529,11 +765,12 @@ extern "C" int kel_batch_run_until(kel_batch *B, double tol, uint64_t check_ever
 	KEL_CUDA(cudaMemcpyAsync(act.data(), B->d_active, sizeof(int) * B->n, cudaMemcpyDeviceToHost, B->stream));
 	KEL_CUDA(cudaStreamSynchronize(B->stream));
 	int rc;
-	if (use_graph && (rc = build_graph(B, (int)check_every, tol))) return rc;
 	uint64_t done = 0;
 	int n_active = 0;
 	for (int c = 0; c < B->n; ++c) n_active += act[c] != 0;
 	while (n_active > 0 && done < max_steps) {
+		if ((rc = compact(B, act))) return rc;
+		if (use_graph && (rc = build_graph(B, (int)check_every, tol))) return rc;
 		if (use_graph) {
 			KEL_CUDA(cudaGraphLaunch(B->graph, B->stream));
 		} else {
@@ -586,6 +823,37 @@ static int batch_download(kel_batch *B, int32_t channel, int what, float *host) 
 	if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
 	cudaFree(d);
 	if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_batch_download: %s", cudaGetErrorString(e));
+	return KEL_OK;
+}
+
+extern "C" int kel_batch_warm_start(kel_batch *B, int32_t first, int32_t count, const float *d_pred,
+									int64_t pred_stride, const float *d_scale, const float *d_offset,
+									int32_t with_neq) {
+	if (!B || !d_pred || !d_scale || !d_offset)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_warm_start: null argument");
+	if (first < 0 || count < 1 || count > 65535 || first > B->n - count)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_warm_start: channels [%d, %d) outside [0, %d)", first,
+					first + count, B->n);
+	int64_t most = 0;
+	for (int c = first; c < first + count; ++c) {
+		if (B->t[c] & 1u)
+			return fail(KEL_ERR_STATE, "kel_batch_warm_start: channel %d is at an odd time step", c);
+		const int64_t cells = (int64_t)B->rec[c].nx * B->rec[c].ny;
+		if (cells * 3 > pred_stride)
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_warm_start: channel %d needs %lld floats > stride %lld", c,
+						(long long)(cells * 3), (long long)pred_stride);
+		most = cells > most ? cells : most;
+	}
+	const int bx = (int)((most + 255) / 256 < 1024 ? (most + 255) / 256 : 1024);
+	k_batch_warm_start<<<dim3(bx, count), 256, 0, B->stream>>>(params(B, 0), first, d_pred, pred_stride, d_scale,
+															   d_offset, with_neq);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+extern "C" int kel_batch_synchronize(kel_batch *B) {
+	if (!B) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_synchronize: null batch");
+	KEL_CUDA(cudaStreamSynchronize(B->stream));
 	return KEL_OK;
 }
 

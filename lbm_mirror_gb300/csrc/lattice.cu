@@ -307,6 +307,54 @@ __global__ void k_pop_convert(ConvArgs a, int upload) {
 	}
 }
 
+// Host AoS (Q values per cell, cells x fastest) <-> lattice, one tile of
+// CONV_TILE consecutive cells per block staged in shared memory as [cell][i]
+// (Q odd: a stride-Q walk is free of bank conflicts), so that the host-side
+// reads / writes and the per-plane lattice writes / reads are both coalesced.
+constexpr int CONV_TILE = 256;
+
+template <typename H>
+__global__ void __launch_bounds__(CONV_TILE) k_pop_aos(ConvArgs a, int upload) {
+	extern __shared__ float tile[];
+	const int64_t c0 = (int64_t)blockIdx.x * CONV_TILE;
+	const int n = (int)(a.ncell - c0 < CONV_TILE ? a.ncell - c0 : CONV_TILE);
+	const int Q = a.Q;
+	H *hb = static_cast<H *>(a.buf) + c0 * Q;
+	const int64_t c = c0 + threadIdx.x;
+	const int64_t row = c / a.nx;
+	const int x = (int)(c - row * a.nx);
+	const int y = (int)(row % a.ny);
+	const int z = (int)(row / a.ny);
+	if (upload) {
+		for (int k = threadIdx.x; k < n * Q; k += CONV_TILE) tile[k] = (float)hb[k];
+		__syncthreads();
+		if (threadIdx.x < n)
+			for (int i = 0; i < Q; ++i) {
+				int64_t idx;
+				if (pop_slot(a, x, y, z, i, idx)) stpop(a, idx, i, tile[threadIdx.x * Q + i]);
+			}
+	} else {
+		if (threadIdx.x < n)
+			for (int i = 0; i < Q; ++i) {
+				int64_t idx;
+				tile[threadIdx.x * Q + i] = pop_slot(a, x, y, z, i, idx) ? ldpop(a, idx, i) : 0.f;
+			}
+		__syncthreads();
+		for (int k = threadIdx.x; k < n * Q; k += CONV_TILE) hb[k] = (H)tile[k];
+	}
+}
+
+static void launch_pop_convert(const kel_lattice *L, const ConvArgs &a, int upload) {
+	if (a.layout == KEL_LAYOUT_AOS) {
+		const unsigned blocks = (unsigned)((a.ncell + CONV_TILE - 1) / CONV_TILE);
+		const size_t sm = sizeof(float) * CONV_TILE * a.Q;
+		if (a.dtype == KEL_DTYPE_F32) k_pop_aos<float><<<blocks, CONV_TILE, sm, L->stream>>>(a, upload);
+		else k_pop_aos<double><<<blocks, CONV_TILE, sm, L->stream>>>(a, upload);
+	} else {
+		k_pop_convert<<<grid_for(a.ncell * a.Q), 256, 0, L->stream>>>(a, upload);
+	}
+}
+
 static ConvArgs conv_args(const kel_lattice *L, int dtype, int layout) {
 	ConvArgs a;
 	memset(&a, 0, sizeof(a));
@@ -346,7 +394,7 @@ extern "C" int kel_upload_populations(kel_lattice *L, const void *host, int32_t 
 	const size_t bytes = (size_t)L->ncell * L->d.Q * (dtype == KEL_DTYPE_F32 ? 4 : 8);
 	if ((rc = ensure_staging(L, bytes))) return rc;
 	KEL_CUDA(cudaMemcpyAsync(L->staging, host, bytes, cudaMemcpyHostToDevice, L->stream));
-	k_pop_convert<<<grid_for(L->ncell * L->d.Q), 256, 0, L->stream>>>(conv_args(L, dtype, layout), 1);
+	launch_pop_convert(L, conv_args(L, dtype, layout), 1);
 	KEL_CUDA(cudaGetLastError());
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
 	return KEL_OK;
@@ -357,7 +405,7 @@ extern "C" int kel_download_populations(kel_lattice *L, void *host, int32_t dtyp
 	if (rc) return rc;
 	const size_t bytes = (size_t)L->ncell * L->d.Q * (dtype == KEL_DTYPE_F32 ? 4 : 8);
 	if ((rc = ensure_staging(L, bytes))) return rc;
-	k_pop_convert<<<grid_for(L->ncell * L->d.Q), 256, 0, L->stream>>>(conv_args(L, dtype, layout), 0);
+	launch_pop_convert(L, conv_args(L, dtype, layout), 0);
 	KEL_CUDA(cudaGetLastError());
 	KEL_CUDA(cudaMemcpyAsync(host, L->staging, bytes, cudaMemcpyDeviceToHost, L->stream));
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
@@ -367,18 +415,27 @@ extern "C" int kel_download_populations(kel_lattice *L, void *host, int32_t dtyp
 // ---------------------------------------------------------------------------
 // macros and per-cell fields: padded plane layout <-> host AoS
 
-__global__ void k_field_io(float *dev, float *buf, int64_t plane, int64_t ncell, int nx, int ny, int nxp, int comps,
-						   int upload) {
-	const int64_t total = ncell * comps;
-	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
-		const int64_t c = k / comps;
-		const int d = (int)(k % comps);
-		const int x = (int)(c % nx);
-		const int64_t row = c / nx;
-		const int64_t idx = (int64_t)d * plane + row * nxp + x;
-		(void)ny;
-		if (upload) dev[idx] = buf[k];
-		else buf[k] = dev[idx];
+// Padded planes (comps of them) <-> host AoS (comps values per cell), one
+// tile of CONV_TILE cells per block staged in shared memory as [cell][d].
+__global__ void __launch_bounds__(CONV_TILE) k_field_io(float *dev, float *buf, int64_t plane, int64_t ncell, int nx,
+														 int nxp, int comps, int upload) {
+	__shared__ float tile[CONV_TILE * 3];
+	const int64_t c0 = (int64_t)blockIdx.x * CONV_TILE;
+	const int n = (int)(ncell - c0 < CONV_TILE ? ncell - c0 : CONV_TILE);
+	float *hb = buf + c0 * comps;
+	const int64_t c = c0 + threadIdx.x;
+	const int64_t row = c / nx;
+	const int64_t idx = row * nxp + (c - row * nx);
+	if (upload) {
+		for (int k = threadIdx.x; k < n * comps; k += CONV_TILE) tile[k] = hb[k];
+		__syncthreads();
+		if (threadIdx.x < n)
+			for (int d = 0; d < comps; ++d) dev[d * plane + idx] = tile[threadIdx.x * comps + d];
+	} else {
+		if (threadIdx.x < n)
+			for (int d = 0; d < comps; ++d) tile[threadIdx.x * comps + d] = dev[d * plane + idx];
+		__syncthreads();
+		for (int k = threadIdx.x; k < n * comps; k += CONV_TILE) hb[k] = tile[k];
 	}
 }
 
@@ -388,8 +445,9 @@ static int field_io(kel_lattice *L, float *dev, float *host_out, const float *ho
 	if (rc) return rc;
 	float *buf = static_cast<float *>(L->staging);
 	if (host_in) KEL_CUDA(cudaMemcpyAsync(buf, host_in, bytes, cudaMemcpyHostToDevice, L->stream));
-	k_field_io<<<grid_for(L->ncell * comps), 256, 0, L->stream>>>(dev, buf, L->plane, L->ncell, (int)L->desc.nx,
-																   (int)L->desc.ny, L->nxp, comps, host_in ? 1 : 0);
+	if (comps < 1 || comps > 3) return fail(KEL_ERR_INVALID_ARGUMENT, "field_io: %d components", comps);
+	k_field_io<<<(unsigned)((L->ncell + CONV_TILE - 1) / CONV_TILE), CONV_TILE, 0, L->stream>>>(
+		dev, buf, L->plane, L->ncell, (int)L->desc.nx, L->nxp, comps, host_in ? 1 : 0);
 	KEL_CUDA(cudaGetLastError());
 	if (host_out) KEL_CUDA(cudaMemcpyAsync(host_out, buf, bytes, cudaMemcpyDeviceToHost, L->stream));
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
@@ -454,6 +512,8 @@ static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops
 	const HostDesc &d = L->d;
 	if (P->collision < KEL_COLL_BGK || P->collision > KEL_COLL_PSM_GUO)
 		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown collision %d", P->collision);
+	if (P->arithmetic == KEL_ARITH_SHIFTED)
+		return fail(KEL_ERR_UNSUPPORTED, "kel_step: shifted arithmetic is implemented for batches only");
 	if (P->arithmetic != KEL_ARITH_FAST && P->arithmetic != KEL_ARITH_REFERENCE)
 		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown arithmetic mode %d", P->arithmetic);
 	if (P->arithmetic == KEL_ARITH_REFERENCE && L->desc.storage != KEL_STORAGE_FP32)

@@ -153,6 +153,243 @@ __global__ void __launch_bounds__(128) conv_igemm(ConvArgs a) {
 	}
 }
 
+// ---- the same implicit-GEMM convolution on the 5th-generation tensor cores ------
+//
+// One CTA (4 warps) computes a 128-pixel x Co tile (M = 128 rows of the
+// accumulator in TMEM, N = Co columns, Co <= 256).  K = 9 Ci runs in chunks of
+// 64 through a TC_STAGES-deep ring of shared-memory stages filled by cp.async
+// (16-byte vectors; taps outside the image and rows past M are zero-filled).
+// One thread issues tcgen05.mma (kind::f16, bf16 x bf16 -> FP32, both operands
+// K-major, no swizzle) per 16-wide K step and commits each chunk to that
+// stage's mbarrier; a stage is refilled only after its mbarrier shows the MMAs
+// that read it are done.  The epilogue reads TMEM with tcgen05.ld, adds bias,
+// applies ReLU and stores bf16.  Every wait is bounded: on timeout the CTA
+// records the failure in *err, stops issuing, and still frees its TMEM.
+//
+// Shared-memory operand layout (K-major, no swizzle): 8-row x 16-byte core
+// matrices; element (r, k) at (r / 8) * 1024 + (k / 8) * 128 + (r % 8) * 16 +
+// (k % 8) * 2, i.e. leading-dimension (K) core-matrix stride 128 B and
+// stride-dimension (M/N) 8-row-group stride 1024 B.  The B stages come first
+// in shared memory so that every address a descriptor can form stays inside
+// the CTA's allocation.
+
+constexpr int TC_M = 128, TC_K = 64;
+
+struct TcArgs {
+	const bf16 *x; // (N,H,W,Ci)
+	const bf16 *w; // (Co,3,3,Ci)
+	const float *bias;
+	bf16 *y;       // (N,H,W,Co)
+	int N, H, W, Ci, Co;
+	int relu, use_bias;
+	int stages;
+	uint32_t tmem_cols;
+	int *err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+	return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+	uint64_t d = 0;
+	d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+	d |= (uint64_t)(128u >> 4) << 16;  // leading (K) core-matrix stride
+	d |= (uint64_t)(1024u >> 4) << 32; // stride (M/N) 8-row-group stride
+	d |= (uint64_t)1 << 46;            // descriptor version for tcgen05
+	return d;                          // base offset 0, no swizzle
+}
+
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void *g, bool valid) {
+	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(valid ? 16 : 0));
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+	asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t parity) {
+	uint32_t ok;
+	asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+				 : "=r"(ok)
+				 : "r"(addr), "r"(parity)
+				 : "memory");
+	return ok != 0;
+}
+
+// Bounded wait (about a second of SM clock); false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t parity) {
+	const long long t0 = clock64();
+	while (!mbar_try(addr, parity))
+		if (clock64() - t0 > 2000000000ll) return false;
+	return true;
+}
+
+__global__ void __launch_bounds__(128) conv_tc(TcArgs a) {
+	extern __shared__ __align__(1024) uint8_t sm[];
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int S = a.stages;
+	const uint32_t b_bytes = (uint32_t)a.Co * 128u; // one B stage: Co rows x 64 K
+	const uint32_t a_bytes = TC_M * 128u;           // one A stage
+	uint8_t *Bs = sm;
+	uint8_t *As = sm + (size_t)S * b_bytes;
+	uint64_t *mbar = reinterpret_cast<uint64_t *>(As + (size_t)S * a_bytes);
+	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + S);
+
+	const int64_t M = (int64_t)a.N * a.H * a.W;
+	const int64_t m0 = (int64_t)blockIdx.x * TC_M;
+	const int K = 9 * a.Ci;
+	const int nk = (K + TC_K - 1) / TC_K;
+
+	if (tid == 0) {
+		for (int s = 0; s < S; ++s)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar + s)));
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+					 "r"(a.tmem_cols));
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+	const uint32_t tmem = *tmem_slot;
+
+	// this thread's 8 A vectors per stage: v = tid + 128 i -> row v / 8, group v % 8
+	int64_t a_pix[8];
+	int a_y[8], a_x[8];
+#pragma unroll
+	for (int i = 0; i < 8; ++i) {
+		const int v = tid + 128 * i;
+		const int64_t m = m0 + (v >> 3);
+		a_pix[i] = -1;
+		a_y[i] = a_x[i] = 0;
+		if (m < M) {
+			const int64_t n = m / ((int64_t)a.H * a.W);
+			const int r = (int)(m - n * a.H * a.W);
+			a_y[i] = r / a.W;
+			a_x[i] = r - a_y[i] * a.W;
+			a_pix[i] = n * a.H * a.W;
+		}
+	}
+	auto load_chunk = [&](int c, int s) {
+		const uint32_t abase = smem_u32(As + (size_t)s * a_bytes);
+		const uint32_t bbase = smem_u32(Bs + (size_t)s * b_bytes);
+#pragma unroll
+		for (int i = 0; i < 8; ++i) {
+			const int v = tid + 128 * i, row = v >> 3, g = v & 7;
+			const int k = c * TC_K + g * 8;
+			if (k >= K) continue;
+			const int tap = k / a.Ci, ci = k - tap * a.Ci;
+			const int yy = a_y[i] + tap / 3 - 1, xx = a_x[i] + tap % 3 - 1;
+			const bool ok = a_pix[i] >= 0 && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+			const bf16 *src = ok ? a.x + (a_pix[i] + (int64_t)yy * a.W + xx) * a.Ci + ci : a.x;
+			cp_async16(abase + (row >> 3) * 1024 + g * 128 + (row & 7) * 16, src, ok);
+		}
+		for (int v = tid; v < a.Co * 8; v += 128) {
+			const int row = v >> 3, g = v & 7;
+			const int k = c * TC_K + g * 8;
+			if (k >= K) continue;
+			cp_async16(bbase + (row >> 3) * 1024 + g * 128 + (row & 7) * 16, a.w + (int64_t)row * K + k, true);
+		}
+	};
+
+	// instruction descriptor: D f32, A bf16, B bf16, both K-major, N = Co, M = 128
+	const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+
+	for (int c = 0; c < S - 1; ++c) {
+		if (c < nk) load_chunk(c, c);
+		cp_async_commit();
+	}
+	int issued = -1;  // last chunk whose MMAs were issued (the same in every thread)
+	int my_fail = 0;  // this thread saw a wait time out
+	for (int c = 0; c < nk; ++c) {
+		const int s = c % S;
+		// chunk c has landed once at most S - 2 younger groups are pending
+		if (S == 2) cp_async_wait<0>();
+		else if (S == 3) cp_async_wait<1>();
+		else cp_async_wait<2>();
+		asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+		if (__syncthreads_or(my_fail)) break; // the same decision in every thread
+		issued = c;
+		if (tid == 0) {
+			asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+			const int ksteps = (K - c * TC_K < TC_K ? K - c * TC_K : TC_K) / 16;
+			const uint32_t abase = smem_u32(As + (size_t)s * a_bytes);
+			const uint32_t bbase = smem_u32(Bs + (size_t)s * b_bytes);
+			for (int j = 0; j < ksteps; ++j) {
+				const uint64_t ad = umma_desc(abase + j * 256), bd = umma_desc(bbase + j * 256);
+				const uint32_t acc = (c > 0 || j > 0) ? 1u : 0u;
+				asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+							 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+							 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+			}
+			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+				smem_u32(mbar + s)));
+		}
+		// refill the stage chunk c - 1 used, once its MMAs are done
+		const int cn = c + S - 1;
+		if (cn < nk) {
+			if (c >= 1 && !mbar_wait(smem_u32(mbar + (c - 1) % S), (uint32_t)(((c - 1) / S) & 1))) my_fail = 1;
+			else load_chunk(cn, cn % S);
+		}
+		cp_async_commit();
+	}
+	cp_async_wait<0>();
+	// the commit of the last issued chunk covers every MMA issued before it;
+	// wait for it (bounded) even after a failure, before TMEM is freed
+	if (issued >= 0 && !mbar_wait(smem_u32(mbar + issued % S), (uint32_t)((issued / S) & 1))) my_fail = 1;
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+	const int failed = __syncthreads_or(my_fail || issued != nk - 1);
+	if (failed) {
+		if (tid == 0) atomicExch(a.err, 1);
+	} else {
+		// epilogue: warp w owns TMEM lanes (= tile rows) 32 w .. 32 w + 31
+		const int row = warp * 32 + lane;
+		const int64_t m = m0 + row;
+		for (int c0 = 0; c0 < a.Co; c0 += 16) {
+			uint32_t r[16];
+			const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+			asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+						 "[%16];\n"
+						 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+						   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+						   "=r"(r[14]), "=r"(r[15])
+						 : "r"(taddr));
+			asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+			if (m < M) {
+				__align__(16) __nv_bfloat162 o[8];
+#pragma unroll
+				for (int q = 0; q < 8; ++q) {
+					float v0 = __uint_as_float(r[2 * q]), v1 = __uint_as_float(r[2 * q + 1]);
+					if (a.use_bias) {
+						v0 += a.bias[c0 + 2 * q];
+						v1 += a.bias[c0 + 2 * q + 1];
+					}
+					if (a.relu) {
+						v0 = fmaxf(v0, 0.f);
+						v1 = fmaxf(v1, 0.f);
+					}
+					o[q] = __floats2bfloat162_rn(v0, v1);
+				}
+				uint4 *dst = reinterpret_cast<uint4 *>(a.y + m * a.Co + c0);
+				dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
+				dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
+			}
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	if (warp == 0) {
+		asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tmem_cols));
+	}
+}
+
 // ---- weight gradient: dW[co][k] = sum_m dY[m][co] * im2col(X)[m][k] -------------
 
 struct WgradArgs {
@@ -486,6 +723,8 @@ struct kel_unet {
 	bf16 *input = nullptr;
 	float *out = nullptr, *dout = nullptr;
 	int batch = 0;
+	int conv_kernel = KEL_UNET_CONV_MMA_SYNC;
+	int *d_err = nullptr; // set by a tensor-core kernel whose bounded wait ran out
 };
 
 namespace {
@@ -537,6 +776,35 @@ int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
 	a.relu = relu;
 	a.use_bias = bias;
 	const int64_t M = (int64_t)n * a.H * a.W;
+	if (U->conv_kernel == KEL_UNET_CONV_TCGEN05) {
+		if (ci % 16 || co % 16 || co < 16 || co > 256)
+			return fail(KEL_ERR_UNSUPPORTED, "conv: tensor-core path needs c_in, c_out multiples of 16, c_out <= 256");
+		TcArgs t;
+		t.x = x;
+		t.w = w;
+		t.bias = b;
+		t.y = y;
+		t.N = n;
+		t.H = a.H;
+		t.W = a.W;
+		t.Ci = ci;
+		t.Co = co;
+		t.relu = relu;
+		t.use_bias = bias;
+		t.stages = co <= 64 ? 4 : (co <= 128 ? 3 : 2);
+		t.tmem_cols = 32;
+		while (t.tmem_cols < (uint32_t)co) t.tmem_cols <<= 1;
+		t.err = U->d_err;
+		const size_t smem = (size_t)t.stages * ((size_t)co * 128 + (size_t)TC_M * 128) + (size_t)t.stages * 8 + 16;
+		static bool attr_set = false;
+		if (!attr_set) {
+			KEL_CUDA(cudaFuncSetAttribute(conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+			attr_set = true;
+		}
+		conv_tc<<<(unsigned)((M + TC_M - 1) / TC_M), 128, smem, U->stream>>>(t);
+		KEL_CUDA(cudaGetLastError());
+		return KEL_OK;
+	}
 	dim3 grid((unsigned)((M + CB_M - 1) / CB_M), (unsigned)((co + CB_N - 1) / CB_N));
 	conv_igemm<<<grid, 128, 0, U->stream>>>(a);
 	KEL_CUDA(cudaGetLastError());
@@ -599,6 +867,19 @@ int refresh(kel_unet *U) {
 
 } // namespace
 
+// After a stream synchronisation: KEL_ERR_TIMEOUT if a tensor-core kernel
+// gave up on a bounded wait since the last check (its output is not valid).
+static int check_device_error(kel_unet *U, const char *who) {
+	int e = 0;
+	KEL_CUDA(cudaMemcpyAsync(&e, U->d_err, sizeof(int), cudaMemcpyDeviceToHost, U->stream));
+	KEL_CUDA(cudaStreamSynchronize(U->stream));
+	if (e) {
+		KEL_CUDA(cudaMemsetAsync(U->d_err, 0, sizeof(int), U->stream));
+		return fail(KEL_ERR_TIMEOUT, "%s: a tensor-core pipeline wait timed out", who);
+	}
+	return KEL_OK;
+}
+
 extern "C" int kel_unet_create(const kel_unet_desc *desc, uint64_t seed, kel_unet **out) {
 	if (!desc || !out) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_create: null argument");
 	*out = nullptr;
@@ -656,6 +937,8 @@ extern "C" int kel_unet_create(const kel_unet_desc *desc, uint64_t seed, kel_une
 	U->partial_len = max_w * 64;
 	if ((e = cudaMalloc(&U->partial, sizeof(float) * U->partial_len)) != cudaSuccess) return fail_out(e);
 	if ((e = cudaMalloc(&U->loss_partial, sizeof(double) * 1024)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->d_err, sizeof(int))) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMemsetAsync(U->d_err, 0, sizeof(int), U->stream)) != cudaSuccess) return fail_out(e);
 	const int n = desc->max_batch;
 	U->batch = n;
 	U->act.assign(T_COUNT, nullptr);
@@ -700,6 +983,7 @@ extern "C" int kel_unet_destroy(kel_unet *U) {
 	cudaFree(U->input);
 	cudaFree(U->out);
 	cudaFree(U->dout);
+	cudaFree(U->d_err);
 	if (U->stream) cudaStreamDestroy(U->stream);
 	delete U;
 	return KEL_OK;
@@ -839,6 +1123,7 @@ extern "C" int kel_unet_backward(kel_unet *U, const float *d_target, int32_t n, 
 		std::vector<double> part(lb);
 		KEL_CUDA(cudaMemcpyAsync(part.data(), U->loss_partial, sizeof(double) * lb, cudaMemcpyDeviceToHost, U->stream));
 		KEL_CUDA(cudaStreamSynchronize(U->stream));
+		if ((rc = check_device_error(U, "kel_unet_backward"))) return rc;
 		double s = 0.0;
 		for (double p : part) s += p;
 		*loss = s / (double)nout;
@@ -864,6 +1149,14 @@ extern "C" int kel_unet_set_stream(kel_unet *U, void *stream) {
 extern "C" int kel_unet_synchronize(kel_unet *U) {
 	if (!U) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_synchronize: null net");
 	KEL_CUDA(cudaStreamSynchronize(U->stream));
+	return check_device_error(U, "kel_unet_synchronize");
+}
+
+extern "C" int kel_unet_set_conv_kernel(kel_unet *U, int32_t kind) {
+	if (!U) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_set_conv_kernel: null net");
+	if (kind != KEL_UNET_CONV_TCGEN05 && kind != KEL_UNET_CONV_MMA_SYNC)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_set_conv_kernel: unknown kind %d", kind);
+	U->conv_kernel = kind;
 	return KEL_OK;
 }
 

@@ -396,6 +396,16 @@ class Batch:
         out = out.reshape(nx * ny, 3)
         return out[:, 0].copy(), out[:, 1:3].copy()
 
+    def warm_start(self, first, count, d_pred, pred_stride, d_scale, d_offset, with_neq=True):
+        """Populations of channels [first, first + count) from a predicted
+        (u_x, u_y, rho) field (device pointers; see kel_batch_warm_start)."""
+        _check(self.lib.kel_batch_warm_start(self._h, int(first), int(count), C.c_void_p(d_pred), int(pred_stride),
+                                             C.c_void_p(d_scale), C.c_void_p(d_offset), int(bool(with_neq))),
+               self.lib)
+
+    def synchronize(self):
+        _check(self.lib.kel_batch_synchronize(self._h), self.lib)
+
 
 class UNet:
     """The warm-start U-Net (C ABI kel_unet_*): bf16 tensor-core convolutions,
@@ -414,6 +424,7 @@ class UNet:
         self._h = h
         self.shape = (height, width, out_channels)
         self.widths = tuple(widths)
+        self.max_batch = max_batch
         n = C.c_int64()
         _check(self.lib.kel_unet_param_count(self._h, C.byref(n)), self.lib)
         self.n_params = n.value
@@ -443,6 +454,10 @@ class UNet:
         out = np.empty(self.n_params, dtype=np.float32)
         _check(self.lib.kel_unet_get_grads(self._h, _ptr(out)), self.lib)
         return out
+
+    def set_conv_kernel(self, kind):
+        """K.KEL_UNET_CONV_TCGEN05 or K.KEL_UNET_CONV_MMA_SYNC (default)."""
+        _check(self.lib.kel_unet_set_conv_kernel(self._h, int(kind)), self.lib)
 
     def set_stream(self, stream):
         _check(self.lib.kel_unet_set_stream(self._h, C.c_void_p(stream)), self.lib)

@@ -1,0 +1,288 @@
+"""Learned warm start of batched D2Q9 channels (no counterpart in
+keldu/lbm_mirror, whose drivers always start from rest equilibrium,
+examples/stdkr_2d_bgk/init.hpp:16-54).
+
+Pipeline, all on one GPU:
+  1. steady states: seeded channels of one size run in the batched runner
+     (kel_batch_run_until) from rest until the relative L2 change of u over
+     `check_every` steps is below `tol`, in shifted FP32 arithmetic (with f
+     itself in FP32 the rounding noise of slow channels stalls above 1e-6);
+  2. training: the conv U-Net (kel_unet_*, bf16 tensor-core convolutions,
+     FP32 accumulate, Adam on FP32 master weights) maps the obstacle mask,
+     u_max and tau planes to the normalised steady field
+     (u_x / u_max, u_y / u_max, (rho - 1) / (u_max * rho_scale));
+  3. warm start: inference on new geometries, then kel_batch_warm_start
+     builds f_eq + f_neq (Chapman-Enskog) populations from the prediction and
+     the same runner continues to the same residual.  The plain run from rest
+     stays the judge of convergence: a warm-started channel stops by the same
+     residual test.
+
+Device memory is held in torch tensors (plumbing only); every kernel on the
+path is this library's.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import capi as K
+from .lattice import Batch, UNet
+from .workloads import batch_channels, channel_program
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("the warm-start pipeline needs a CUDA device")
+    return torch
+
+
+def fixed_size_channels(n, seed, nx=256, ny=64):
+    """n seeded channels of one size (nx x ny): obstacles, u_max and tau as
+    the batched-channel workload draws them."""
+    return batch_channels(n=n, seed=seed, nx_range=(nx, nx), ny_range=(ny, ny))
+
+
+def channel_inputs(channels):
+    """Host arrays of the network inputs: mask (n, ny, nx) uint8 (1 = wall or
+    obstacle), u_max (n,) and tau (n,) float32."""
+    ny, nx = channels[0]["ny"], channels[0]["nx"]
+    mask = np.stack([(np.asarray(c["flags"]).reshape(ny, nx) == 1).astype(np.uint8) for c in channels])
+    u_max = np.array([c["u_max"] for c in channels], dtype=np.float32)
+    tau = np.array([c["tau"] for c in channels], dtype=np.float32)
+    return mask, u_max, tau
+
+
+@dataclass
+class SteadyStates:
+    """Steady fields of a set of channels: rho (n, ny, nx), u (n, ny, nx, 2),
+    steps to convergence and the last residual per channel, wall seconds."""
+    channels: list
+    rho: np.ndarray
+    u: np.ndarray
+    steps: np.ndarray
+    residual: np.ndarray
+    seconds: float
+    tol: float = 1e-6
+
+    @property
+    def converged(self):
+        return self.residual < self.tol  # False for NaN / inf (diverged)
+
+
+def solve(channels, tol=1e-6, check_every=1000, max_steps=600_000, tile=128, chunk=1024, arithmetic=K.KEL_ARITH_SHIFTED):
+    """Run the channels from rest to the residual `tol` in batches of `chunk`
+    channels; returns SteadyStates (fields downloaded to the host)."""
+    n = len(channels)
+    ny, nx = channels[0]["ny"], channels[0]["nx"]
+    rho = np.empty((n, ny, nx), np.float32)
+    u = np.empty((n, ny, nx, 2), np.float32)
+    steps = np.empty(n, np.uint64)
+    res = np.empty(n, np.float64)
+    t0 = time.perf_counter()
+    for a in range(0, n, chunk):
+        part = channels[a:a + chunk]
+        b = Batch(part, channel_program(0.8, arithmetic), tile=tile)
+        s, r = b.run_until(tol=tol, check_every=check_every, max_steps=max_steps)
+        steps[a:a + len(part)] = s
+        res[a:a + len(part)] = r
+        for k in range(len(part)):
+            rr, uu = b.macros(k)
+            rho[a + k] = rr.reshape(ny, nx)
+            u[a + k] = uu.reshape(ny, nx, 2)
+        b.close()
+    return SteadyStates(channels, rho, u, steps, res, time.perf_counter() - t0, tol)
+
+
+def steady_subset(states: SteadyStates):
+    """The channels that reached the residual (unsteady or diverged ones are
+    no steady states and are left out of training)."""
+    k = np.flatnonzero(states.converged)
+    return SteadyStates([states.channels[i] for i in k], states.rho[k], states.u[k], states.steps[k],
+                        states.residual[k], states.seconds, states.tol)
+
+
+@dataclass
+class WarmStartNet:
+    """The trained U-Net plus the density normalisation it was trained with."""
+    net: UNet
+    rho_scale: float
+    history: list = field(default_factory=list)
+
+    @property
+    def shape(self):
+        return self.net.shape
+
+
+def targets(states: SteadyStates, rho_scale=None):
+    """Normalised training targets (n, ny, nx, 3) float32 and the density
+    scale (RMS of (rho - 1) / u_max over non-wall cells unless given)."""
+    _, u_max, _ = channel_inputs(states.channels)
+    um = u_max[:, None, None]
+    drho = (states.rho - 1.0) / um
+    if rho_scale is None:
+        mask, _, _ = channel_inputs(states.channels)
+        fluid = mask == 0
+        rho_scale = float(np.sqrt(np.mean(drho[fluid] ** 2))) or 1.0
+    t = np.empty(states.u.shape[:3] + (3,), np.float32)
+    t[..., 0] = states.u[..., 0] / um
+    t[..., 1] = states.u[..., 1] / um
+    t[..., 2] = drho / rho_scale
+    return t, rho_scale
+
+
+def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, warmup=100, seed=1,
+          widths=(32, 64, 128, 128), log_every=0):
+    """Train the U-Net on the steady states with Adam (cosine schedule).
+    Returns a WarmStartNet; its history holds (step, loss) pairs."""
+    torch = _torch()
+    ny, nx = states.rho.shape[1:]
+    mask, u_max, tau = channel_inputs(states.channels)
+    tgt, rho_scale = targets(states)
+    dev = torch.device("cuda")
+    d_mask = torch.from_numpy(mask).to(dev)
+    d_umax = torch.from_numpy(u_max).to(dev)
+    d_tau = torch.from_numpy(tau).to(dev)
+    d_tgt = torch.from_numpy(tgt).to(dev)
+    n = mask.shape[0]
+    net = UNet(height=ny, width=nx, widths=widths, out_channels=3, max_batch=batch, seed=seed)
+    model = WarmStartNet(net, rho_scale)
+    steps_per_epoch = n // batch
+    total = max(1, epochs * steps_per_epoch)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    step = 0
+    for _ in range(epochs):
+        perm = torch.randperm(n, device=dev, generator=gen)
+        for i in range(steps_per_epoch):
+            idx = perm[i * batch:(i + 1) * batch]
+            mb_mask = d_mask.index_select(0, idx).contiguous()
+            mb_umax = d_umax.index_select(0, idx).contiguous()
+            mb_tau = d_tau.index_select(0, idx).contiguous()
+            mb_tgt = d_tgt.index_select(0, idx).contiguous()
+            torch.cuda.synchronize()
+            net.make_input(mb_mask.data_ptr(), mb_umax.data_ptr(), mb_tau.data_ptr(), batch)
+            net.forward(batch)
+            loss = net.backward(mb_tgt.data_ptr(), batch)
+            if step < warmup:
+                rate = lr * (step + 1) / warmup
+            else:
+                q = (step - warmup) / max(1, total - warmup)
+                rate = lr * (lr_min_frac + (1 - lr_min_frac) * 0.5 * (1 + math.cos(math.pi * q)))
+            net.adam_step(lr=rate)
+            step += 1
+            if log_every and step % log_every == 0:
+                model.history.append((step, loss))
+            elif not log_every:
+                model.history.append((step, loss))
+    net.synchronize()
+    return model
+
+
+def predict(model: WarmStartNet, d_mask, d_umax, d_tau):
+    """Normalised prediction (n, ny, nx, 3) float32 on the device for device
+    inputs (mask uint8 (n, ny, nx), u_max and tau float32 (n,))."""
+    torch = _torch()
+    n = d_mask.shape[0]
+    ny, nx, oc = model.shape
+    out = torch.empty((n, ny, nx, oc), dtype=torch.float32, device=d_mask.device)
+    mb = model.net.max_batch
+    torch.cuda.synchronize()
+    for a in range(0, n, mb):
+        k = min(mb, n - a)
+        model.net.make_input(d_mask[a:].data_ptr(), d_umax[a:].data_ptr(), d_tau[a:].data_ptr(), k)
+        model.net.forward(k, out[a:].data_ptr())
+    model.net.synchronize()
+    return out
+
+
+def warm_start(batch: Batch, model: WarmStartNet, d_mask, d_umax, d_tau, with_neq=True):
+    """Inference for every channel of `batch` (all of the network's size,
+    in channel order) and the populations built from it."""
+    torch = _torch()
+    pred = predict(model, d_mask, d_umax, d_tau)
+    n = pred.shape[0]
+    um = d_umax.to(torch.float32)
+    scale = torch.stack([um, um, um * model.rho_scale], dim=1).contiguous()
+    offset = torch.zeros((n, 3), dtype=torch.float32, device=pred.device)
+    offset[:, 2] = 1.0
+    torch.cuda.synchronize()
+    ny, nx, oc = model.shape
+    batch.warm_start(0, n, pred.data_ptr(), ny * nx * oc, scale.data_ptr(), offset.data_ptr(), with_neq)
+    return pred
+
+
+def _rel_l2(a, b):
+    d = float(np.sqrt(np.sum((a - b) ** 2)))
+    r = float(np.sqrt(np.sum(b ** 2)))
+    return d / r if r > 0 else d
+
+
+def time_to_steady(channels, model: WarmStartNet | None, tol=1e-6, check_every=1000, max_steps=600_000, tile=128,
+                   with_neq=True, arithmetic=K.KEL_ARITH_SHIFTED):
+    """One batched run of `channels` to the residual `tol`, from rest
+    (model None) or warm-started.  The timed region holds inference, the
+    population reconstruction and every sweep; the batch set-up (flags and
+    the rest state) is outside it for both.  Returns (seconds, steps,
+    residual, u (n, ny, nx, 2), prediction or None)."""
+    torch = _torch()
+    ny, nx = channels[0]["ny"], channels[0]["nx"]
+    b = Batch(channels, channel_program(0.8, arithmetic), tile=tile)
+    mask, u_max, tau = channel_inputs(channels)
+    dev = torch.device("cuda")
+    d_mask = torch.from_numpy(mask).to(dev)
+    d_umax = torch.from_numpy(u_max).to(dev)
+    d_tau = torch.from_numpy(tau).to(dev)
+    b.synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    pred = None
+    if model is not None:
+        pred = warm_start(b, model, d_mask, d_umax, d_tau, with_neq)
+    steps, res = b.run_until(tol=tol, check_every=check_every, max_steps=max_steps)
+    seconds = time.perf_counter() - t0
+    u = np.empty((len(channels), ny, nx, 2), np.float32)
+    for k in range(len(channels)):
+        u[k] = b.macros(k)[1].reshape(ny, nx, 2)
+    b.close()
+    pred_np = None
+    if pred is not None:
+        pred_np = pred.cpu().numpy()
+    return seconds, steps, res, u, pred_np
+
+
+def evaluate(model: WarmStartNet, channels, tol=1e-6, check_every=1000, max_steps=600_000, tile=128,
+             with_neq=True):
+    """Plain (rest) vs warm-started runs of the same channels.  Channels whose
+    run from rest does not reach `tol` within max_steps (unsteady flow: vortex
+    shedding behind an obstacle; or diverged) have no time to steady state;
+    they are counted and left out, and both arms are timed on the rest.
+    Returns a dict with wall seconds, steps per channel, the final-field
+    error of the warm run against the plain run and the prediction's own
+    error."""
+    t_plain, s_plain, r_plain, u_plain, _ = time_to_steady(channels, None, tol, check_every, max_steps, tile)
+    ok = np.flatnonzero(r_plain < tol)
+    excluded = len(channels) - len(ok)
+    if excluded:
+        channels = [channels[k] for k in ok]
+        t_plain, s_plain, r_plain, u_plain, _ = time_to_steady(channels, None, tol, check_every, max_steps, tile)
+    t_warm, s_warm, r_warm, u_warm, pred = time_to_steady(channels, model, tol, check_every, max_steps, tile,
+                                                           with_neq)
+    mask, u_max, _ = channel_inputs(channels)
+    final_err = np.array([_rel_l2(u_warm[k], u_plain[k]) for k in range(len(channels))])
+    pred_u = pred[..., :2] * u_max[:, None, None, None]
+    pred_u[mask == 1] = 0.0
+    pred_err = np.array([_rel_l2(pred_u[k], u_plain[k]) for k in range(len(channels))])
+    return dict(
+        channels=len(channels), excluded_unsteady=excluded, tol=tol, check_every=check_every,
+        plain_seconds=t_plain, warm_seconds=t_warm, speedup=t_plain / t_warm,
+        plain_steps_mean=float(np.mean(s_plain)), warm_steps_mean=float(np.mean(s_warm)),
+        plain_steps_max=int(np.max(s_plain)), warm_steps_max=int(np.max(s_warm)),
+        plain_unconverged=int(np.sum(~(r_plain < tol))), warm_unconverged=int(np.sum(~(r_warm < tol))),
+        final_u_rel_l2_mean=float(np.mean(final_err)), final_u_rel_l2_max=float(np.max(final_err)),
+        prediction_u_rel_l2_mean=float(np.mean(pred_err)), prediction_u_rel_l2_max=float(np.max(pred_err)),
+        steps_plain=s_plain, steps_warm=s_warm,
+    )

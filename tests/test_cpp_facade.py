@@ -1,4 +1,4 @@
-"""The C++ face run as a reference-style driver (config C1 in small) on the
+"""The C++ face run as a reference-style driver (the 256x64 Poiseuille channel in small) on the
 GPU: with reference arithmetic its macros equal the reference's bit for bit."""
 import os
 import subprocess

@@ -1,0 +1,108 @@
+"""Learned warm start on the GPU: the population reconstruction of
+kel_batch_warm_start against the FP64 oracle, its argument checks, and a
+small end-to-end run showing what the trained network gains over the rest
+start (same residual test for both)."""
+import numpy as np
+import pytest
+
+from lbm_mirror_gb300 import capi as K
+from oracle import warmstart_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _batch(chans):
+    from lbm_mirror_gb300 import Batch
+    from lbm_mirror_gb300.workloads import channel_program
+    return Batch(chans, channel_program(0.8), tile=128)
+
+
+def _uneven_channels():
+    from lbm_mirror_gb300.workloads import batch_channels
+    return batch_channels(n=3, seed=41, nx_range=(30, 70), ny_range=(12, 30))
+
+
+def test_reconstruction_matches_fp64_oracle():
+    rng = np.random.default_rng(3)
+    chans = _uneven_channels()
+    b = _batch(chans)
+    cells = [c["nx"] * c["ny"] for c in chans]
+    stride = max(cells) * 3 + 5
+    pred = np.zeros((3, stride), np.float32)
+    for k, n in enumerate(cells):
+        pred[k, :n * 3] = rng.uniform(-1, 1, n * 3)
+    scale = np.array([[c["u_max"], c["u_max"], 0.02] for c in chans], np.float32)
+    offset = np.tile(np.array([0.0, 0.0, 1.0], np.float32), (3, 1))
+    d_pred = torch.from_numpy(pred).cuda()
+    d_scale = torch.from_numpy(scale).cuda()
+    d_off = torch.from_numpy(offset).cuda()
+    torch.cuda.synchronize()
+    for with_neq in (False, True):
+        b.warm_start(0, 3, d_pred.data_ptr(), stride, d_scale.data_ptr(), d_off.data_ptr(), with_neq)
+        b.synchronize()
+        for k, c in enumerate(chans):
+            got = b.populations(k).astype(np.float64)
+            p = pred[k, :cells[k] * 3].reshape(c["ny"], c["nx"], 3)
+            want = O.warm_start_populations(np.asarray(c["flags"]).reshape(c["ny"], c["nx"]), p, scale[k], offset[k],
+                                            np.float32(1.0 / np.float32(1.0 / c["tau"])), with_neq)
+            assert np.max(np.abs(got - want)) <= 2e-6, (k, with_neq, np.max(np.abs(got - want)))
+
+
+def test_subrange_leaves_other_channels_at_rest():
+    chans = _uneven_channels()
+    b = _batch(chans)
+    stride = max(c["nx"] * c["ny"] for c in chans) * 3
+    d_pred = torch.full((2, stride), 0.3, dtype=torch.float32, device="cuda")
+    d_scale = torch.full((2, 3), 0.05, dtype=torch.float32, device="cuda")
+    d_off = torch.zeros((2, 3), dtype=torch.float32, device="cuda")
+    d_off[:, 2] = 1.0
+    torch.cuda.synchronize()
+    b.warm_start(1, 2, d_pred.data_ptr(), stride, d_scale.data_ptr(), d_off.data_ptr(), True)
+    b.synchronize()
+    f0 = b.populations(0)
+    assert np.array_equal(f0, np.tile(O.W.astype(np.float32), (f0.shape[0], 1)))
+    assert not np.array_equal(b.populations(1), np.tile(O.W.astype(np.float32), (b.populations(1).shape[0], 1)))
+
+
+def test_invalid_arguments():
+    from lbm_mirror_gb300.lattice import KelError
+    chans = _uneven_channels()
+    b = _batch(chans)
+    n = max(c["nx"] * c["ny"] for c in chans)
+    d = torch.zeros((3, n * 3), dtype=torch.float32, device="cuda")
+    s = torch.ones((3, 3), dtype=torch.float32, device="cuda")
+    with pytest.raises(KelError) as e:
+        b.warm_start(2, 2, d.data_ptr(), n * 3, s.data_ptr(), s.data_ptr())
+    assert e.value.code == K.KEL_ERR_INVALID_ARGUMENT
+    with pytest.raises(KelError) as e:
+        b.warm_start(0, 3, d.data_ptr(), n * 3 - 1, s.data_ptr(), s.data_ptr())
+    assert e.value.code == K.KEL_ERR_INVALID_ARGUMENT
+    b.step(1)
+    with pytest.raises(KelError) as e:
+        b.warm_start(0, 1, d.data_ptr(), n * 3, s.data_ptr(), s.data_ptr())
+    assert e.value.code == K.KEL_ERR_STATE
+
+
+def test_trained_network_reaches_steady_state_in_fewer_steps():
+    """Train on 256 seeded 64x32 channels, test on 32 held-out ones: the
+    warm-started runs reach the residual 1e-5 (per 200 steps) in fewer steps
+    than the runs from rest, and end on the same field."""
+    from lbm_mirror_gb300 import warmstart as WS
+    train_ch = WS.fixed_size_channels(256, seed=51, nx=64, ny=32)
+    test_ch = WS.fixed_size_channels(32, seed=52, nx=64, ny=32)
+    tol, check = 1e-5, 200
+    states = WS.solve(train_ch, tol=tol, check_every=check, max_steps=100_000)
+    # channels with shedding or a diverged run are not steady states
+    assert states.converged.mean() >= 0.5, states.residual
+    model = WS.train(WS.steady_subset(states), epochs=40, batch=32, lr=2e-3, widths=(16, 32, 64, 64))
+    first = np.mean([l for _, l in model.history[:8]])
+    last = np.mean([l for _, l in model.history[-8:]])
+    assert last < 0.1 * first, (first, last)
+    r = WS.evaluate(model, test_ch, tol=tol, check_every=check, max_steps=100_000)
+    assert r["channels"] >= 8, r
+    assert r["plain_unconverged"] == 0 and r["warm_unconverged"] == 0, r
+    assert r["prediction_u_rel_l2_mean"] < 0.2, r
+    assert r["warm_steps_mean"] < 0.9 * r["plain_steps_mean"], r
+    assert r["final_u_rel_l2_max"] < 1e-2, r
