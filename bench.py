@@ -285,7 +285,8 @@ def run_warm_start(args, rank, world):
     gen_updates = float(np.sum(states.steps.astype(np.float64)) * nx * ny)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    model = WS.train(states, epochs=args.epochs, batch=32, lr=2e-3, widths=widths, log_every=32)
+    model = WS.train(WS.steady_subset(states), epochs=args.epochs, batch=32, lr=2e-3, widths=widths,
+                     log_every=32)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     n_steps = args.epochs * (args.train // 32)
@@ -327,6 +328,8 @@ def run_warm_start(args, rank, world):
                 "inference": {"seconds": t_inf, "samples": args.test, "tflops": inf_flops / t_inf / 1e12},
                 "data_generation": {"seconds": states.seconds, "channels": args.train,
                                     "unconverged": int(np.sum(~states.converged)),
+                                    "residual_max_converged": float(np.max(states.residual[states.converged]))
+                                    if states.converged.any() else None,
                                     "active_MLUPS": gen_updates / states.seconds / 1e6},
                 "roofline": {"bound": "tensor", "achieved": train_flops / t_train / 1e12,
                              "peak": bf16, "unit": "TFLOP/s",
@@ -517,6 +520,21 @@ def main():
         e2e_s = float(t.item())
     e2e_value = world * ncell * args.e2e_lbm_steps * args.e2e_iters / e2e_s / 1e6
     mass = float(h_rho.numpy()[case["flags"] == 2].astype(np.float64).mean())
+    # one more pass, each call timed alone (not part of the e2e value)
+    phases = {}
+    tp = time.perf_counter()
+    lib.kel_upload_flags(lat.handle, C.c_void_p(h_flags.data_ptr()))
+    phases["upload_flags"] = (time.perf_counter() - tp) * 1e3
+    tp = time.perf_counter()
+    lib.kel_upload_populations(lat.handle, C.c_void_p(h_pop.data_ptr()), K.KEL_DTYPE_F32, K.KEL_LAYOUT_AOS)
+    phases["upload_populations"] = (time.perf_counter() - tp) * 1e3
+    tp = time.perf_counter()
+    lib.kel_step(lat.handle, C.byref(prog), args.e2e_lbm_steps, K.KEL_STEP_WRITE_MACROS)
+    lib.kel_lattice_synchronize(lat.handle)
+    phases["steps"] = (time.perf_counter() - tp) * 1e3
+    tp = time.perf_counter()
+    lib.kel_download_macros(lat.handle, C.c_void_p(h_rho.data_ptr()), C.c_void_p(h_u.data_ptr()))
+    phases["download_macros"] = (time.perf_counter() - tp) * 1e3
 
     line = {
         "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
@@ -534,7 +552,7 @@ def main():
                      "per_launch_ms": per_launch_s * 1e3},
         "e2e": {"value": e2e_value, "unit": "MLUPS", "h2d_bytes_per_step": int(ncell + ncell * Q * 4),
                 "d2h_bytes_per_step": int(ncell * 4 * (1 + D)), "lbm_steps_per_step": args.e2e_lbm_steps,
-                "iters": args.e2e_iters, "mean_rho_fluid": mass},
+                "iters": args.e2e_iters, "mean_rho_fluid": mass, "phases_ms": phases},
         "gpu_launches": args.steps,
         "clocks": clk,
     }

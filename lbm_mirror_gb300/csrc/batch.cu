@@ -15,6 +15,7 @@
 // FP64 convergence residual per channel; converged channels drop out (their
 // blocks return at once) and the graph is replayed until none is left.
 #include <cuda_runtime.h>
+#include <math_constants.h>
 
 #include <cmath>
 #include <cstring>
@@ -229,6 +230,8 @@ __global__ void __launch_bounds__(512) k_batch_residual_partial(BatchParams p) {
 				den += a * a;
 				p.u_prev[d * p.plane + cell] = (float)a;
 			}
+			// a density that overflowed (u may still read 0) marks the run diverged
+			if (!isfinite(p.rho[cell])) num = CUDART_NAN;
 		}
 	}
 	for (int o = 16; o > 0; o >>= 1) {

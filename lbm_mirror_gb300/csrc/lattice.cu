@@ -193,6 +193,7 @@ extern "C" int kel_lattice_destroy(kel_lattice *L) {
 	else cudaDeviceSynchronize();
 	cudaFree(L->f);
 	cudaFree(L->flags);
+	cudaFree(L->d_seen);
 	cudaFree(L->rho);
 	cudaFree(L->u);
 	cudaFree(L->por);
@@ -225,16 +226,36 @@ extern "C" int kel_lattice_synchronize(kel_lattice *L) {
 // ---------------------------------------------------------------------------
 // flags
 
+// Which flag values occur in the lattice's own cells (the row padding x >= nx
+// is skipped): one bit per value, OR-ed per block in shared memory, then
+// into `seen`.
+__global__ void k_flag_presence(const uint8_t *flags, int64_t n, int nx, int nxp, unsigned *seen) {
+	__shared__ unsigned blk[8];
+	if (threadIdx.x < 8) blk[threadIdx.x] = 0u;
+	__syncthreads();
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+		if ((int)(k % nxp) >= nx) continue;
+		const unsigned v = flags[k];
+		atomicOr(&blk[v >> 5], 1u << (v & 31));
+	}
+	__syncthreads();
+	if (threadIdx.x < 8 && blk[threadIdx.x]) atomicOr(&seen[threadIdx.x], blk[threadIdx.x]);
+}
+
 extern "C" int kel_upload_flags(kel_lattice *L, const uint8_t *host) {
 	if (!L || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_upload_flags: null argument");
 	const auto &D = L->desc;
 	KEL_CUDA(cudaMemcpy2DAsync(L->flags, (size_t)L->nxp, host, (size_t)D.nx, (size_t)D.nx, (size_t)(D.ny * D.nz),
 							   cudaMemcpyHostToDevice, L->stream));
-	bool seen[256] = {false};
-	for (int64_t c = 0; c < L->ncell; ++c) seen[host[c]] = true;
-	for (int fl = 0; fl < MAX_FLAGS; ++fl) L->present[fl] = seen[fl] ? 1 : 0;
-	L->have_ops = false; // re-validate the program against the new flag set
+	if (!L->d_seen) KEL_CUDA(cudaMalloc(&L->d_seen, 8 * sizeof(unsigned)));
+	KEL_CUDA(cudaMemsetAsync(L->d_seen, 0, 8 * sizeof(unsigned), L->stream));
+	k_flag_presence<<<grid_for(L->plane), 256, 0, L->stream>>>(L->flags, L->plane, (int)D.nx, L->nxp, L->d_seen);
+	KEL_CUDA(cudaGetLastError());
+	unsigned seen[8];
+	KEL_CUDA(cudaMemcpyAsync(seen, L->d_seen, sizeof(seen), cudaMemcpyDeviceToHost, L->stream));
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	for (int fl = 0; fl < MAX_FLAGS; ++fl) L->present[fl] = (seen[fl >> 5] >> (fl & 31)) & 1u;
+	L->have_ops = false; // re-validate the program against the new flag set
 	return KEL_OK;
 }
 

@@ -56,6 +56,7 @@ struct kel_lattice {
 	float wshift[27];
 	bool have_ops = false;
 	uint8_t present[kel::gb::MAX_FLAGS] = {0}; // flag values present in the uploaded flag field
+	unsigned *d_seen = nullptr;                 // device scratch of the flag-presence scan (8 words)
 	kel_step_program last_prog;
 	int device = 0;
 	int cpt = 1;      // cells per thread of the sweep launch (1 or 4)

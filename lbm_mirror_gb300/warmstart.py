@@ -70,7 +70,9 @@ class SteadyStates:
 
     @property
     def converged(self):
-        return self.residual < self.tol  # False for NaN / inf (diverged)
+        """Reached the residual with finite fields (False for diverged runs)."""
+        finite = np.isfinite(self.rho).all(axis=(1, 2)) & np.isfinite(self.u).all(axis=(1, 2, 3))
+        return (self.residual < self.tol) & finite
 
 
 def solve(channels, tol=1e-6, check_every=1000, max_steps=600_000, tile=128, chunk=1024, arithmetic=K.KEL_ARITH_SHIFTED):
