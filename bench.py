@@ -291,7 +291,7 @@ def run_warm_start(args, rank, world):
     t_train = time.perf_counter() - t0
     n_steps = args.epochs * (args.train // 32)
     train_flops = 3 * unet_flops_per_sample(ny, nx, widths) * 32 * n_steps
-    r = WS.evaluate(model, test_ch, tol=args.tol, check_every=1000, max_steps=args.max_steps)
+    r = WS.evaluate(model, test_ch, tol=args.tol, check_every=1000, max_steps=args.max_steps, variants=True)
     # inference alone, timed with CUDA events on the network's own stream path
     mask, u_max, tau = WS.channel_inputs(test_ch)
     d_mask = torch.from_numpy(mask).cuda()
@@ -321,6 +321,10 @@ def run_warm_start(args, rank, world):
                                                     "warm_steps_max", "plain_unconverged", "warm_unconverged")},
                 "final_u_rel_l2": {"mean": r["final_u_rel_l2_mean"], "max": r["final_u_rel_l2_max"]},
                 "prediction_u_rel_l2": {"mean": r["prediction_u_rel_l2_mean"], "max": r["prediction_u_rel_l2_max"]},
+                "prediction_drho_rel_l2_mean": r["prediction_drho_rel_l2_mean"],
+                "init_variants_steps_mean": {"steady_state_itself": r["steady_init_steps_mean"],
+                                             "net_u_rho_one": r["rho_one_steps_mean"],
+                                             "net_without_neq": r["no_neq_steps_mean"]},
                 "training": {"seconds": t_train, "adam_steps": n_steps, "batch": 32,
                              "loss_first": model.history[0][1] if model.history else None,
                              "loss_last": model.history[-1][1] if model.history else None,

@@ -298,8 +298,14 @@ int kel_unet_set_params(kel_unet *net, const float *host);
 int kel_unet_get_grads(kel_unet *net, float *host);
 int kel_unet_set_stream(kel_unet *net, void *stream);
 int kel_unet_synchronize(kel_unet *net);
-/* Input planes from device data: mask (n*H*W bytes), u_max and tau (n floats each). */
+/* Input planes from device data: mask (n*H*W bytes, 1 = solid), u_max and tau
+ * (n floats each).  Channels: mask, u_max / 0.08, (tau - 0.55) / 0.45, y and x
+ * coordinates, the column's open fraction, the downstream resistance
+ * sum 1/open^3 / W, the vertical gap height, 4 s (1 - s) across the gap and
+ * the lubrication estimate of u_x / u_max (halved); the rest zero. */
 int kel_unet_make_input(kel_unet *net, const uint8_t *d_mask, const float *d_umax, const float *d_tau, int32_t n);
+/* The current input (bf16 NHWC, 16 channels) copied to a device buffer. */
+int kel_unet_get_input(kel_unet *net, uint16_t *d_out_bf16, int32_t n);
 /* Input directly: bf16 NHWC, 16 channels (device pointer). */
 int kel_unet_set_input(kel_unet *net, const uint16_t *d_input_bf16, int32_t n);
 /* Forward pass; d_out (device, may be NULL) receives n*H*W*out_channels floats (NHWC). */
@@ -308,8 +314,8 @@ int kel_unet_forward(kel_unet *net, int32_t n, float *d_out);
  * parameter gradient (FP32, overwritten).  *loss is written on the host. */
 int kel_unet_backward(kel_unet *net, const float *d_target, int32_t n, double *loss);
 int kel_unet_adam_step(kel_unet *net, float lr, float beta1, float beta2, float eps, int32_t step);
-/* Convolution kernels: KEL_UNET_CONV_TCGEN05 (tcgen05.mma with the
- * accumulator in tensor memory) or KEL_UNET_CONV_MMA_SYNC (default; warp-level
+/* Convolution kernels: KEL_UNET_CONV_TCGEN05 (default; tcgen05.mma with the
+ * accumulator in tensor memory) or KEL_UNET_CONV_MMA_SYNC (warp-level
  * mma.sync).  Both compute bf16 x bf16 -> FP32; results agree to FP32
  * summation order.  kel_unet_synchronize / kel_unet_backward return
  * KEL_ERR_TIMEOUT if a tensor-core kernel gave up on a bounded wait. */

@@ -242,6 +242,7 @@ def load_library(path: str | None = None):
         "kel_unet_synchronize": ([vp], C.c_int),
         "kel_unet_make_input": ([vp, vp, vp, vp, i32], C.c_int),
         "kel_unet_set_input": ([vp, vp, i32], C.c_int),
+        "kel_unet_get_input": ([vp, vp, i32], C.c_int),
         "kel_unet_forward": ([vp, i32, vp], C.c_int),
         "kel_unet_backward": ([vp, vp, i32, C.POINTER(C.c_double)], C.c_int),
         "kel_unet_adam_step": ([vp, C.c_float, C.c_float, C.c_float, C.c_float, i32], C.c_int),

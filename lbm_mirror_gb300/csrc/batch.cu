@@ -82,12 +82,14 @@ __device__ __forceinline__ bool cell_update_shifted(float (&g)[9], int flag, int
 	const float c23 = (float)(2.0 / 3.0), c16 = (float)(1.0 / 6.0);
 	float t;
 	switch (bc) {
-	case BC_BOUNCE_BACK:
-		t = g[1]; g[1] = g[2]; g[2] = t;
-		t = g[3]; g[3] = g[4]; g[4] = t;
-		t = g[5]; g[5] = g[8]; g[8] = t;
-		t = g[6]; g[6] = g[7]; g[7] = t;
+	case BC_BOUNCE_BACK: {
+		float cpy[9];
+#pragma unroll
+		for (int i = 0; i < 9; ++i) cpy[i] = g[i];
+#pragma unroll
+		for (int i = 0; i < 9; ++i) g[i] = cpy[L::opp(i)];
 		break;
+	}
 	case BC_ANTI_BOUNCE_BACK:
 		t = g[3]; g[3] = g[4]; g[4] = t;
 		t = g[5]; g[5] = g[7]; g[7] = t;
@@ -328,9 +330,12 @@ __global__ void k_batch_download(BatchParams p, ChannelRec ch, int odd, int what
 //   f_i = f_eq(rho, u) - (tau w_i rho / cs^2) Q_i : grad u   (with_neq)
 // with Q_i = c_i c_i - cs^2 I and grad u by central differences (one-sided at
 // the channel ends; u = 0 in wall cells): the first-order Chapman-Enskog
-// population of the predicted field.  A wall cell (flag 1) gets the rest state
-// at the mean predicted density of its fluid neighbours; u_prev takes the
-// predicted u, so the first residual measures the change from the prediction.
+// population of the predicted field.  A wall cell (flag 1) holds, in each
+// slot i whose source x - c_i is fluid, that neighbour's post-collision
+// population f_eq + (1 - omega) f_neq (what the last stream step would have
+// brought), and the rest state at the mean predicted density of its fluid
+// neighbours in the other slots; u_prev takes the predicted u, so the first
+// residual measures the change from the prediction.
 __global__ void k_batch_warm_start(BatchParams p, int first, const float *pred, int64_t pred_stride, const float *sc,
 								   const float *of, int with_neq) {
 	const int j = blockIdx.y;
@@ -339,6 +344,7 @@ __global__ void k_batch_warm_start(BatchParams p, int first, const float *pred, 
 	const float s0 = sc[3 * j], s1 = sc[3 * j + 1], s2 = sc[3 * j + 2];
 	const float o0 = of[3 * j], o1 = of[3 * j + 1], o2 = of[3 * j + 2];
 	const float tau = 1.f / ch.omega;
+	const float post = 1.f - ch.omega; // f_neq factor after a BGK collision
 	const int64_t n = (int64_t)ch.nx * ch.ny;
 	auto is_fluid = [&](int xx, int yy) {
 		const uint8_t f2 = p.flags[ch.off + (int64_t)yy * ch.nxp + xx];
@@ -350,11 +356,33 @@ __global__ void k_batch_warm_start(BatchParams p, int first, const float *pred, 
 	auto uy_at = [&](int xx, int yy) {
 		return is_fluid(xx, yy) ? pr[((int64_t)yy * ch.nx + xx) * 3 + 1] * s1 + o1 : 0.f;
 	};
+	// population i of fluid cell (xx, yy): f_eq + fac f_neq (fac = 1: before,
+	// 1 - omega: after its collision)
+	auto pop = [&](int xx, int yy, int i, float fac) {
+		float u[3] = {ux_at(xx, yy), uy_at(xx, yy), 0.f};
+		const float rho = pr[((int64_t)yy * ch.nx + xx) * 3 + 2] * s2 + o2;
+		float eq[9];
+		equilibrium<D2Q9, true>(rho, u, eq);
+		float v = eq[i];
+		if (with_neq) {
+			const int xm = xx > 0 ? xx - 1 : xx, xp = xx + 1 < ch.nx ? xx + 1 : xx;
+			const int ym = yy > 0 ? yy - 1 : yy, yp = yy + 1 < ch.ny ? yy + 1 : yy;
+			const float ix = 1.f / (float)(xp - xm), iy = 1.f / (float)(yp - ym);
+			const float dxu = (ux_at(xp, yy) - ux_at(xm, yy)) * ix, dxv = (uy_at(xp, yy) - uy_at(xm, yy)) * ix;
+			const float dyu = (ux_at(xx, yp) - ux_at(xx, ym)) * iy, dyv = (uy_at(xx, yp) - uy_at(xx, ym)) * iy;
+			const float cx = (float)D2Q9::cx(i), cy = (float)D2Q9::cy(i);
+			const float qs = (cx * cx - 1.f / 3.f) * dxu + (cy * cy - 1.f / 3.f) * dyv + cx * cy * (dxv + dyu);
+			v -= fac * tau * (float)D2Q9::w(i) * rho * 3.f * qs;
+		}
+		return v;
+	};
 	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
 		const int y = (int)(k / ch.nx), x = (int)(k - (int64_t)y * ch.nx);
 		const int64_t cell = ch.off + (int64_t)y * ch.nxp + x;
 		float f[9];
 		if (!is_fluid(x, y)) {
+			// what streamed in from fluid neighbours: their post-collision
+			// populations; the rest of the slots at the mean neighbour density
 			float rs = 0.f;
 			int cnt = 0;
 			for (int i = 1; i < 9; ++i) {
@@ -365,26 +393,15 @@ __global__ void k_batch_warm_start(BatchParams p, int first, const float *pred, 
 				}
 			}
 			const float rho = cnt ? rs / (float)cnt : 1.f;
-			for (int i = 0; i < 9; ++i) f[i] = (float)D2Q9::w(i) * rho;
-		} else {
-			float u[3] = {ux_at(x, y), uy_at(x, y), 0.f};
-			const float rho = pr[k * 3 + 2] * s2 + o2;
-			equilibrium<D2Q9, true>(rho, u, f);
-			if (with_neq) {
-				const int xm = x > 0 ? x - 1 : x, xp = x + 1 < ch.nx ? x + 1 : x;
-				const int ym = y > 0 ? y - 1 : y, yp = y + 1 < ch.ny ? y + 1 : y;
-				const float ix = 1.f / (float)(xp - xm), iy = 1.f / (float)(yp - ym);
-				const float dxu = (ux_at(xp, y) - ux_at(xm, y)) * ix, dxv = (uy_at(xp, y) - uy_at(xm, y)) * ix;
-				const float dyu = (ux_at(x, yp) - ux_at(x, ym)) * iy, dyv = (uy_at(x, yp) - uy_at(x, ym)) * iy;
-				const float sxy = 0.5f * (dxv + dyu);
-				for (int i = 0; i < 9; ++i) {
-					const float cx = (float)D2Q9::cx(i), cy = (float)D2Q9::cy(i);
-					const float qs = (cx * cx - 1.f / 3.f) * dxu + (cy * cy - 1.f / 3.f) * dyv + 2.f * cx * cy * sxy;
-					f[i] -= tau * (float)D2Q9::w(i) * rho * 3.f * qs;
-				}
+			for (int i = 0; i < 9; ++i) {
+				const int xs = x - D2Q9::cx(i), ys = y - D2Q9::cy(i);
+				const bool from_fluid = i > 0 && xs >= 0 && xs < ch.nx && ys >= 0 && ys < ch.ny && is_fluid(xs, ys);
+				f[i] = from_fluid ? pop(xs, ys, i, post) : (float)D2Q9::w(i) * rho;
 			}
-			p.u_prev[cell] = u[0];
-			p.u_prev[p.plane + cell] = u[1];
+		} else {
+			for (int i = 0; i < 9; ++i) f[i] = pop(x, y, i, 1.f);
+			p.u_prev[cell] = ux_at(x, y);
+			p.u_prev[p.plane + cell] = uy_at(x, y);
 		}
 		for (int i = 0; i < 9; ++i) p.f[i * p.plane + cell] = f[i] - (p.shifted ? (float)D2Q9::w(i) : 0.f);
 	}

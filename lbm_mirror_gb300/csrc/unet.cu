@@ -191,13 +191,15 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) {
 	return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr) {
+// Shared-memory matrix descriptor, no swizzle: start address, leading and
+// stride byte offsets (16-byte units), version 1 (tcgen05), base offset 0.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo = 128u, uint32_t sbo = 1024u) {
 	uint64_t d = 0;
 	d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
-	d |= (uint64_t)(128u >> 4) << 16;  // leading (K) core-matrix stride
-	d |= (uint64_t)(1024u >> 4) << 32; // stride (M/N) 8-row-group stride
-	d |= (uint64_t)1 << 46;            // descriptor version for tcgen05
-	return d;                          // base offset 0, no swizzle
+	d |= (uint64_t)((lbo & 0x3FFFFu) >> 4) << 16;
+	d |= (uint64_t)((sbo & 0x3FFFFu) >> 4) << 32;
+	d |= (uint64_t)1 << 46;
+	return d;
 }
 
 __device__ __forceinline__ void cp_async16(uint32_t saddr, const void *g, bool valid) {
@@ -380,6 +382,169 @@ __global__ void __launch_bounds__(128) conv_tc(TcArgs a) {
 				dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
 				dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
 			}
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	if (warp == 0) {
+		asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tmem_cols));
+	}
+}
+
+// ---- weight gradient on the tensor cores -----------------------------------------
+//
+// D[kcol][co] = sum over a chunk of pixels m of im2col(X)[m][kcol] dY[m][co]:
+// M = 128 columns kcol = tap * Ci + ci of the weight, N = Co, K = pixels.  In
+// NHWC memory both operands run along M/N (8 consecutive kcol of one pixel,
+// or 8 consecutive co, are 16 contiguous bytes), so they are staged
+// MN-major: core matrices of 8 pixels (16-byte rows) x 8 elements; element
+// (r, m) of a stage at (r / 8) * 1024 + (m / 8) * 128 + (m % 8) * 16 +
+// (r % 8) * 2.  For the no-swizzle MN-major layout the descriptor's leading
+// byte offset is the K-direction stride (128 B between 8-pixel groups) and
+// its stride byte offset the M/N-direction stride (1024 B).  Pipeline, bounded waits
+// and TMEM handling as conv_tc; the epilogue writes this chunk's FP32
+// partial sums partial[chunk][co][kcol], reduced later in fixed chunk order.
+
+struct TcWgradArgs {
+	const bf16 *x;  // (N,H,W,Ci) forward input
+	const bf16 *dy; // (N,H,W,Co) gradient at the pre-activation
+	float *partial; // (chunks, Co, 9 Ci)
+	int N, H, W, Ci, Co;
+	int64_t chunk;  // pixels per chunk (multiple of 64)
+	int stages;
+	uint32_t tmem_cols;
+	int *err;
+};
+
+__global__ void __launch_bounds__(128) conv_wgrad_tc(TcWgradArgs a) {
+	extern __shared__ __align__(1024) uint8_t sm[];
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int S = a.stages;
+	const uint32_t b_bytes = (uint32_t)a.Co * 128u;
+	const uint32_t a_bytes = TC_M * 128u;
+	uint8_t *Bs = sm;
+	uint8_t *As = sm + (size_t)S * b_bytes;
+	uint64_t *mbar = reinterpret_cast<uint64_t *>(As + (size_t)S * a_bytes);
+	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + S);
+
+	const int64_t M = (int64_t)a.N * a.H * a.W;
+	const int K = 9 * a.Ci;
+	const int kc0 = blockIdx.x * TC_M;
+	const int64_t p_begin = (int64_t)blockIdx.y * a.chunk;
+	const int64_t p_end = p_begin + a.chunk < M ? p_begin + a.chunk : M;
+	const int nk = (int)((p_end - p_begin + TC_K - 1) / TC_K);
+	const int HW = a.H * a.W;
+
+	if (tid == 0) {
+		for (int s = 0; s < S; ++s)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(mbar + s)));
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+					 "r"(a.tmem_cols));
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+	const uint32_t tmem = *tmem_slot;
+
+	const int cog = a.Co >> 3; // 16-byte groups of dY per pixel
+	auto load_chunk = [&](int c, int s) {
+		const uint32_t abase = smem_u32(As + (size_t)s * a_bytes);
+		const uint32_t bbase = smem_u32(Bs + (size_t)s * b_bytes);
+		const int64_t q0 = p_begin + (int64_t)c * TC_K;
+		// A: 64 pixels x 16 groups of 8 kcol
+#pragma unroll
+		for (int i = 0; i < 8; ++i) {
+			const int v = tid + 128 * i, g = v & 15, pp = v >> 4;
+			const int64_t m = q0 + pp;
+			const int k = kc0 + g * 8;
+			bool ok = m < p_end && k < K;
+			const bf16 *src = a.x;
+			if (ok) {
+				const int tap = k / a.Ci, ci = k - tap * a.Ci;
+				const int64_t n = m / HW;
+				const int r = (int)(m - n * HW);
+				const int yy = r / a.W + tap / 3 - 1, xx = r % a.W + tap % 3 - 1;
+				ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+				if (ok) src = a.x + ((n * a.H + yy) * (int64_t)a.W + xx) * a.Ci + ci;
+			}
+			cp_async16(abase + g * 1024 + (pp >> 3) * 128 + (pp & 7) * 16, src, ok);
+		}
+		// B: 64 pixels x Co / 8 groups of dY
+		for (int v = tid; v < TC_K * cog; v += 128) {
+			const int g = v % cog, pp = v / cog;
+			const int64_t m = q0 + pp;
+			const bool ok = m < p_end;
+			cp_async16(bbase + g * 1024 + (pp >> 3) * 128 + (pp & 7) * 16, ok ? a.dy + m * a.Co + g * 8 : a.dy, ok);
+		}
+	};
+
+	// D f32, A bf16, B bf16, A and B MN-major, N = Co, M = 128
+	const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+						   ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+
+	for (int c = 0; c < S - 1; ++c) {
+		if (c < nk) load_chunk(c, c);
+		cp_async_commit();
+	}
+	int issued = -1;
+	int my_fail = 0;
+	for (int c = 0; c < nk; ++c) {
+		const int s = c % S;
+		if (S == 2) cp_async_wait<0>();
+		else if (S == 3) cp_async_wait<1>();
+		else cp_async_wait<2>();
+		asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+		if (__syncthreads_or(my_fail)) break;
+		issued = c;
+		if (tid == 0) {
+			asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+			const uint32_t abase = smem_u32(As + (size_t)s * a_bytes);
+			const uint32_t bbase = smem_u32(Bs + (size_t)s * b_bytes);
+			for (int j = 0; j < TC_K / 16; ++j) {
+				const uint64_t ad = umma_desc(abase + j * 256, 128u, 1024u);
+				const uint64_t bd = umma_desc(bbase + j * 256, 128u, 1024u);
+				const uint32_t acc = (c > 0 || j > 0) ? 1u : 0u;
+				asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+							 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+							 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+			}
+			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+				smem_u32(mbar + s)));
+		}
+		const int cn = c + S - 1;
+		if (cn < nk) {
+			if (c >= 1 && !mbar_wait(smem_u32(mbar + (c - 1) % S), (uint32_t)(((c - 1) / S) & 1))) my_fail = 1;
+			else load_chunk(cn, cn % S);
+		}
+		cp_async_commit();
+	}
+	cp_async_wait<0>();
+	if (issued >= 0 && !mbar_wait(smem_u32(mbar + issued % S), (uint32_t)((issued / S) & 1))) my_fail = 1;
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+	const int failed = __syncthreads_or(my_fail || issued != nk - 1);
+	if (failed) {
+		if (tid == 0) atomicExch(a.err, 1);
+	} else {
+		const int kcol = kc0 + warp * 32 + lane;
+		float *out = a.partial + (int64_t)blockIdx.y * a.Co * K;
+		for (int c0 = 0; c0 < a.Co; c0 += 16) {
+			uint32_t r[16];
+			const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+			asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+						 "[%16];\n"
+						 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+						   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+						   "=r"(r[14]), "=r"(r[15])
+						 : "r"(taddr));
+			asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+			if (kcol < K)
+#pragma unroll
+				for (int q = 0; q < 16; ++q) out[(int64_t)(c0 + q) * K + kcol] = __uint_as_float(r[q]);
 		}
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -681,17 +846,85 @@ __global__ void refresh_conv_weights(const float *w32, bf16 *w, bf16 *wf, int Co
 	}
 }
 
-// network input: ch0 = mask, ch1 = u_max / 0.08, ch2 = (tau - 0.55) / 0.45, rest 0
-__global__ void make_input(const uint8_t *mask, const float *umax, const float *tau, bf16 *x, int N, int H, int W,
-						   int C) {
+// Network input (16 channels, bf16).  From the obstacle mask (1 = solid) and
+// the two flow parameters:
+//   0 mask, 1 u_max / 0.08, 2 (tau - 0.55) / 0.45, 3 y / (H - 1), 4 x / (W - 1),
+//   5 open fraction of the column (fluid cells / (H - 2)),
+//   6 downstream resistance: sum over columns x' >= x of 1 / open^3, / W,
+//   7 height of the vertical gap holding the cell / (H - 2),
+//   8 4 s (1 - s), s the cell's position across that gap,
+//   9 lubrication estimate of u_x / u_max, halved: with the inlet flux
+//     Q = 2/3 u_max (H - 2) split over a column's gaps as h^3, the gap's
+//     Poiseuille profile gives u_x / u_max = (H - 2) h^2 / sum h^3 4 s (1 - s),
+//   10-15 zero.
+// Solid cells carry only channels 0-4.
+
+// per (sample, column): fluid-cell count and sum of the cubes of its gap heights
+__global__ void column_features(const uint8_t *mask, int N, int H, int W, float *open, float *h3) {
+	const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+	if (idx >= N * W) return;
+	const int b = idx / W, x = idx - b * W;
+	const uint8_t *m = mask + (int64_t)b * H * W;
+	int cnt = 0, run = 0;
+	float s3 = 0.f;
+	for (int y = 0; y < H; ++y) {
+		if (!m[(int64_t)y * W + x]) {
+			++cnt;
+			++run;
+		} else {
+			s3 += (float)run * run * run;
+			run = 0;
+		}
+	}
+	s3 += (float)run * run * run;
+	open[idx] = fminf((float)cnt / (float)(H > 2 ? H - 2 : H), 1.f);
+	h3[idx] = s3;
+}
+
+// per sample: suffix sums of the column resistance 1 / max(open, 1/8)^3
+__global__ void column_resistance(const float *open, int N, int W, float *R) {
+	const int b = blockIdx.x * blockDim.x + threadIdx.x;
+	if (b >= N) return;
+	float acc = 0.f;
+	for (int x = W - 1; x >= 0; --x) {
+		const float o = fmaxf(open[(int64_t)b * W + x], 0.125f);
+		acc += 1.f / (o * o * o);
+		R[(int64_t)b * W + x] = acc / (float)W;
+	}
+}
+
+__global__ void make_input(const uint8_t *mask, const float *umax, const float *tau, const float *open,
+						   const float *h3, const float *R, bf16 *x, int N, int H, int W, int C) {
 	const int64_t n = (int64_t)N * H * W;
 	for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
 		const int b = (int)(p / ((int64_t)H * W));
+		const int r = (int)(p - (int64_t)b * H * W);
+		const int yy = r / W, xx = r - yy * W;
+		const uint8_t *m = mask + (int64_t)b * H * W;
+		float v[16];
+		for (int c = 0; c < 16; ++c) v[c] = 0.f;
+		v[0] = (float)m[r];
+		v[1] = umax[b] / 0.08f;
+		v[2] = (tau[b] - 0.55f) / 0.45f;
+		v[3] = (float)yy / (float)(H - 1);
+		v[4] = (float)xx / (float)(W - 1);
+		if (!m[r]) {
+			const int64_t col = (int64_t)b * W + xx;
+			int lo = yy, hi = yy;
+			while (lo > 0 && !m[(int64_t)(lo - 1) * W + xx]) --lo;
+			while (hi + 1 < H && !m[(int64_t)(hi + 1) * W + xx]) ++hi;
+			const float h = (float)(hi - lo + 1);
+			const float sp = ((float)(yy - lo) + 0.5f) / h;
+			const float shape = 4.f * sp * (1.f - sp);
+			const float hin = (float)(H > 2 ? H - 2 : H);
+			v[5] = open[col];
+			v[6] = R[col];
+			v[7] = h / hin;
+			v[8] = shape;
+			v[9] = 0.5f * fminf(hin * h * h / fmaxf(h3[col], 1.f) * shape, 8.f);
+		}
 		bf16 *o = x + p * C;
-		for (int c = 0; c < C; ++c) o[c] = __float2bfloat16(0.f);
-		o[0] = __float2bfloat16((float)mask[p]);
-		o[1] = __float2bfloat16(umax[b] / 0.08f);
-		o[2] = __float2bfloat16((tau[b] - 0.55f) / 0.45f);
+		for (int c = 0; c < C; ++c) o[c] = __float2bfloat16(c < 16 ? v[c] : 0.f);
 	}
 }
 
@@ -723,8 +956,9 @@ struct kel_unet {
 	bf16 *input = nullptr;
 	float *out = nullptr, *dout = nullptr;
 	int batch = 0;
-	int conv_kernel = KEL_UNET_CONV_MMA_SYNC;
+	int conv_kernel = KEL_UNET_CONV_TCGEN05;
 	int *d_err = nullptr; // set by a tensor-core kernel whose bounded wait ran out
+	float *col_open = nullptr, *col_h3 = nullptr, *col_res = nullptr; // input-feature scratch (max_batch x W)
 };
 
 namespace {
@@ -811,7 +1045,48 @@ int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
 	return KEL_OK;
 }
 
+int conv_grads_tc(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy, int n) {
+	if (l.ci % 16 || l.co % 16 || l.co > 256)
+		return fail(KEL_ERR_UNSUPPORTED, "wgrad: tensor-core path needs c_in, c_out multiples of 16, c_out <= 256");
+	TcWgradArgs a;
+	a.x = x;
+	a.dy = dy;
+	a.partial = U->partial;
+	a.N = n;
+	a.H = U->d.height >> l.level;
+	a.W = U->d.width >> l.level;
+	a.Ci = l.ci;
+	a.Co = l.co;
+	const int64_t M = (int64_t)n * a.H * a.W;
+	const int K = 9 * l.ci;
+	const int tiles = (K + TC_M - 1) / TC_M;
+	int64_t chunks = (608 + tiles - 1) / tiles;
+	const int64_t max_chunks = U->partial_len / ((int64_t)l.co * K);
+	if (chunks > max_chunks) chunks = max_chunks;
+	if (chunks > (M + 255) / 256) chunks = (M + 255) / 256;
+	if (chunks < 1) chunks = 1;
+	a.chunk = ((M + chunks - 1) / chunks + TC_K - 1) / TC_K * TC_K;
+	chunks = (M + a.chunk - 1) / a.chunk;
+	a.stages = l.co <= 64 ? 4 : (l.co <= 128 ? 3 : 2);
+	a.tmem_cols = 32;
+	while (a.tmem_cols < (uint32_t)l.co) a.tmem_cols <<= 1;
+	a.err = U->d_err;
+	const size_t smem = (size_t)a.stages * ((size_t)l.co * 128 + (size_t)TC_M * 128) + (size_t)a.stages * 8 + 16;
+	static bool attr_set = false;
+	if (!attr_set) {
+		KEL_CUDA(cudaFuncSetAttribute(conv_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+		attr_set = true;
+	}
+	conv_wgrad_tc<<<dim3((unsigned)tiles, (unsigned)chunks), 128, smem, U->stream>>>(a);
+	const int64_t per = (int64_t)l.co * K;
+	reduce_partials<<<grid_of(per), 256, 0, U->stream>>>(U->partial, per, (int)chunks, U->g + l.woff);
+	bias_grad<<<l.co, 256, 0, U->stream>>>(dy, M, l.co, U->g + l.woff + per);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
 int conv_grads(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy, int n) {
+	if (U->conv_kernel == KEL_UNET_CONV_TCGEN05) return conv_grads_tc(U, l, x, dy, n);
 	WgradArgs a;
 	a.x = x;
 	a.dy = dy;
@@ -949,6 +1224,10 @@ extern "C" int kel_unet_create(const kel_unet_desc *desc, uint64_t seed, kel_une
 	}
 	const int64_t pix = (int64_t)n * desc->height * desc->width;
 	if ((e = cudaMalloc(&U->input, sizeof(bf16) * pix * 16)) != cudaSuccess) return fail_out(e);
+	const size_t colb = sizeof(float) * (size_t)desc->max_batch * desc->width;
+	if ((e = cudaMalloc(&U->col_open, colb)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->col_h3, colb)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->col_res, colb)) != cudaSuccess) return fail_out(e);
 	if ((e = cudaMalloc(&U->out, sizeof(float) * pix * desc->out_channels)) != cudaSuccess) return fail_out(e);
 	if ((e = cudaMalloc(&U->dout, sizeof(float) * pix * desc->out_channels)) != cudaSuccess) return fail_out(e);
 	std::vector<float> h;
@@ -984,6 +1263,9 @@ extern "C" int kel_unet_destroy(kel_unet *U) {
 	cudaFree(U->out);
 	cudaFree(U->dout);
 	cudaFree(U->d_err);
+	cudaFree(U->col_open);
+	cudaFree(U->col_h3);
+	cudaFree(U->col_res);
 	if (U->stream) cudaStreamDestroy(U->stream);
 	delete U;
 	return KEL_OK;
@@ -1028,7 +1310,11 @@ extern "C" int kel_unet_make_input(kel_unet *U, const uint8_t *d_mask, const flo
 	int rc = check_batch(U, n, "kel_unet_make_input");
 	if (rc) return rc;
 	const int64_t pix = (int64_t)n * U->d.height * U->d.width;
-	make_input<<<grid_of(pix), 256, 0, U->stream>>>(d_mask, d_umax, d_tau, U->input, n, U->d.height, U->d.width, 16);
+	const int H = U->d.height, W = U->d.width;
+	column_features<<<(n * W + 127) / 128, 128, 0, U->stream>>>(d_mask, n, H, W, U->col_open, U->col_h3);
+	column_resistance<<<(n + 63) / 64, 64, 0, U->stream>>>(U->col_open, n, W, U->col_res);
+	make_input<<<grid_of(pix), 256, 0, U->stream>>>(d_mask, d_umax, d_tau, U->col_open, U->col_h3, U->col_res,
+													 U->input, n, H, W, 16);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
@@ -1161,6 +1447,16 @@ extern "C" int kel_unet_set_conv_kernel(kel_unet *U, int32_t kind) {
 }
 
 // Direct input (bf16 NHWC, 16 channels) for tests: copies into the net's input.
+extern "C" int kel_unet_get_input(kel_unet *U, uint16_t *d_out_bf16, int32_t n) {
+	int rc = check_batch(U, n, "kel_unet_get_input");
+	if (rc) return rc;
+	if (!d_out_bf16) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_get_input: null output");
+	KEL_CUDA(cudaMemcpyAsync(d_out_bf16, U->input, sizeof(bf16) * (int64_t)n * U->d.height * U->d.width * 16,
+							 cudaMemcpyDeviceToDevice, U->stream));
+	KEL_CUDA(cudaStreamSynchronize(U->stream));
+	return KEL_OK;
+}
+
 extern "C" int kel_unet_set_input(kel_unet *U, const uint16_t *d_input_bf16, int32_t n) {
 	int rc = check_batch(U, n, "kel_unet_set_input");
 	if (rc) return rc;

@@ -456,7 +456,7 @@ class UNet:
         return out
 
     def set_conv_kernel(self, kind):
-        """K.KEL_UNET_CONV_TCGEN05 or K.KEL_UNET_CONV_MMA_SYNC (default)."""
+        """K.KEL_UNET_CONV_TCGEN05 (default) or K.KEL_UNET_CONV_MMA_SYNC."""
         _check(self.lib.kel_unet_set_conv_kernel(self._h, int(kind)), self.lib)
 
     def set_stream(self, stream):
@@ -468,6 +468,9 @@ class UNet:
     def make_input(self, d_mask, d_umax, d_tau, n):
         _check(self.lib.kel_unet_make_input(self._h, C.c_void_p(d_mask), C.c_void_p(d_umax), C.c_void_p(d_tau), n),
                self.lib)
+
+    def get_input(self, d_out_bf16, n):
+        _check(self.lib.kel_unet_get_input(self._h, C.c_void_p(d_out_bf16), n), self.lib)
 
     def set_input(self, d_input_bf16, n):
         _check(self.lib.kel_unet_set_input(self._h, C.c_void_p(d_input_bf16), n), self.lib)

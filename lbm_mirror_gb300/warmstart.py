@@ -119,16 +119,18 @@ class WarmStartNet:
         return self.net.shape
 
 
-def targets(states: SteadyStates, rho_scale=None):
+def targets(states: SteadyStates, rho_scale=None, rho_target_rms=0.25):
     """Normalised training targets (n, ny, nx, 3) float32 and the density
-    scale (RMS of (rho - 1) / u_max over non-wall cells unless given)."""
+    scale: (rho - 1) / u_max over non-wall cells is scaled to RMS
+    rho_target_rms (unless rho_scale is given), which weights the density in
+    the squared-error loss below the velocity (u / u_max is of order 1)."""
     _, u_max, _ = channel_inputs(states.channels)
     um = u_max[:, None, None]
     drho = (states.rho - 1.0) / um
     if rho_scale is None:
         mask, _, _ = channel_inputs(states.channels)
         fluid = mask == 0
-        rho_scale = float(np.sqrt(np.mean(drho[fluid] ** 2))) or 1.0
+        rho_scale = float(np.sqrt(np.mean(drho[fluid] ** 2)) / rho_target_rms) or 1.0
     t = np.empty(states.u.shape[:3] + (3,), np.float32)
     t[..., 0] = states.u[..., 0] / um
     t[..., 1] = states.u[..., 1] / um
@@ -201,14 +203,16 @@ def predict(model: WarmStartNet, d_mask, d_umax, d_tau):
     return out
 
 
-def warm_start(batch: Batch, model: WarmStartNet, d_mask, d_umax, d_tau, with_neq=True):
+def warm_start(batch: Batch, model: WarmStartNet, d_mask, d_umax, d_tau, with_neq=True, rho_from_net=True):
     """Inference for every channel of `batch` (all of the network's size,
-    in channel order) and the populations built from it."""
+    in channel order) and the populations built from it.  With
+    rho_from_net False the density starts at 1 (only u is predicted)."""
     torch = _torch()
     pred = predict(model, d_mask, d_umax, d_tau)
     n = pred.shape[0]
     um = d_umax.to(torch.float32)
-    scale = torch.stack([um, um, um * model.rho_scale], dim=1).contiguous()
+    rs = um * model.rho_scale if rho_from_net else torch.zeros_like(um)
+    scale = torch.stack([um, um, rs], dim=1).contiguous()
     offset = torch.zeros((n, 3), dtype=torch.float32, device=pred.device)
     offset[:, 2] = 1.0
     torch.cuda.synchronize()
@@ -217,19 +221,43 @@ def warm_start(batch: Batch, model: WarmStartNet, d_mask, d_umax, d_tau, with_ne
     return pred
 
 
+def model_init(model: WarmStartNet, with_neq=True, rho_from_net=True):
+    """Initialiser for time_to_steady: the network's prediction."""
+    def init(batch, d_mask, d_umax, d_tau):
+        return warm_start(batch, model, d_mask, d_umax, d_tau, with_neq, rho_from_net)
+    return init
+
+
+def field_init(fields, with_neq=True):
+    """Initialiser for time_to_steady from given physical fields (n, ny, nx, 3)
+    = (u_x, u_y, rho) per cell, e.g. a known steady state (diagnostics)."""
+    def init(batch, d_mask, d_umax, d_tau):
+        torch = _torch()
+        n = fields.shape[0]
+        d = torch.from_numpy(np.ascontiguousarray(fields, dtype=np.float32)).cuda()
+        one = torch.ones((n, 3), dtype=torch.float32, device="cuda")
+        zero = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        batch.warm_start(0, n, d.data_ptr(), d[0].numel(), one.data_ptr(), zero.data_ptr(), with_neq)
+        batch.synchronize()
+        return d
+    return init
+
+
 def _rel_l2(a, b):
     d = float(np.sqrt(np.sum((a - b) ** 2)))
     r = float(np.sqrt(np.sum(b ** 2)))
     return d / r if r > 0 else d
 
 
-def time_to_steady(channels, model: WarmStartNet | None, tol=1e-6, check_every=1000, max_steps=600_000, tile=128,
-                   with_neq=True, arithmetic=K.KEL_ARITH_SHIFTED):
-    """One batched run of `channels` to the residual `tol`, from rest
-    (model None) or warm-started.  The timed region holds inference, the
-    population reconstruction and every sweep; the batch set-up (flags and
+def time_to_steady(channels, init=None, tol=1e-6, check_every=1000, max_steps=600_000, tile=128,
+                   arithmetic=K.KEL_ARITH_SHIFTED):
+    """One batched run of `channels` to the residual `tol`, from rest (init
+    None) or from init(batch, d_mask, d_umax, d_tau) (model_init /
+    field_init).  The timed region holds the initialiser (inference and
+    population reconstruction) and every sweep; the batch set-up (flags and
     the rest state) is outside it for both.  Returns (seconds, steps,
-    residual, u (n, ny, nx, 2), prediction or None)."""
+    residual, u (n, ny, nx, 2), rho (n, ny, nx), initialiser output or None)."""
     torch = _torch()
     ny, nx = channels[0]["ny"], channels[0]["nx"]
     b = Batch(channels, channel_program(0.8, arithmetic), tile=tile)
@@ -242,43 +270,51 @@ def time_to_steady(channels, model: WarmStartNet | None, tol=1e-6, check_every=1
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     pred = None
-    if model is not None:
-        pred = warm_start(b, model, d_mask, d_umax, d_tau, with_neq)
+    if init is not None:
+        pred = init(b, d_mask, d_umax, d_tau)
     steps, res = b.run_until(tol=tol, check_every=check_every, max_steps=max_steps)
     seconds = time.perf_counter() - t0
     u = np.empty((len(channels), ny, nx, 2), np.float32)
+    rho = np.empty((len(channels), ny, nx), np.float32)
     for k in range(len(channels)):
-        u[k] = b.macros(k)[1].reshape(ny, nx, 2)
+        r, uu = b.macros(k)
+        u[k] = uu.reshape(ny, nx, 2)
+        rho[k] = r.reshape(ny, nx)
     b.close()
-    pred_np = None
-    if pred is not None:
-        pred_np = pred.cpu().numpy()
-    return seconds, steps, res, u, pred_np
+    pred_np = pred.cpu().numpy() if pred is not None else None
+    return seconds, steps, res, u, rho, pred_np
 
 
 def evaluate(model: WarmStartNet, channels, tol=1e-6, check_every=1000, max_steps=600_000, tile=128,
-             with_neq=True):
+             with_neq=True, variants=False):
     """Plain (rest) vs warm-started runs of the same channels.  Channels whose
     run from rest does not reach `tol` within max_steps (unsteady flow: vortex
     shedding behind an obstacle; or diverged) have no time to steady state;
     they are counted and left out, and both arms are timed on the rest.
     Returns a dict with wall seconds, steps per channel, the final-field
     error of the warm run against the plain run and the prediction's own
-    error."""
-    t_plain, s_plain, r_plain, u_plain, _ = time_to_steady(channels, None, tol, check_every, max_steps, tile)
+    error.  With variants, also the mean steps from the plain run's own
+    steady state (the floor any prediction can reach), from the network's
+    u with rho = 1, and without the non-equilibrium part."""
+    t_plain, s_plain, r_plain, u_plain, rho_plain, _ = time_to_steady(channels, None, tol, check_every, max_steps,
+                                                                      tile)
     ok = np.flatnonzero(r_plain < tol)
     excluded = len(channels) - len(ok)
     if excluded:
         channels = [channels[k] for k in ok]
-        t_plain, s_plain, r_plain, u_plain, _ = time_to_steady(channels, None, tol, check_every, max_steps, tile)
-    t_warm, s_warm, r_warm, u_warm, pred = time_to_steady(channels, model, tol, check_every, max_steps, tile,
-                                                           with_neq)
+        t_plain, s_plain, r_plain, u_plain, rho_plain, _ = time_to_steady(channels, None, tol, check_every,
+                                                                          max_steps, tile)
+    t_warm, s_warm, r_warm, u_warm, _, pred = time_to_steady(channels, model_init(model, with_neq), tol,
+                                                             check_every, max_steps, tile)
     mask, u_max, _ = channel_inputs(channels)
     final_err = np.array([_rel_l2(u_warm[k], u_plain[k]) for k in range(len(channels))])
     pred_u = pred[..., :2] * u_max[:, None, None, None]
     pred_u[mask == 1] = 0.0
     pred_err = np.array([_rel_l2(pred_u[k], u_plain[k]) for k in range(len(channels))])
-    return dict(
+    pred_rho = pred[..., 2] * (u_max[:, None, None] * model.rho_scale) + 1.0
+    fl = mask == 0
+    rho_err = np.array([_rel_l2(pred_rho[k][fl[k]] - 1, rho_plain[k][fl[k]] - 1) for k in range(len(channels))])
+    out = dict(
         channels=len(channels), excluded_unsteady=excluded, tol=tol, check_every=check_every,
         plain_seconds=t_plain, warm_seconds=t_warm, speedup=t_plain / t_warm,
         plain_steps_mean=float(np.mean(s_plain)), warm_steps_mean=float(np.mean(s_warm)),
@@ -286,5 +322,16 @@ def evaluate(model: WarmStartNet, channels, tol=1e-6, check_every=1000, max_step
         plain_unconverged=int(np.sum(~(r_plain < tol))), warm_unconverged=int(np.sum(~(r_warm < tol))),
         final_u_rel_l2_mean=float(np.mean(final_err)), final_u_rel_l2_max=float(np.max(final_err)),
         prediction_u_rel_l2_mean=float(np.mean(pred_err)), prediction_u_rel_l2_max=float(np.max(pred_err)),
+        prediction_drho_rel_l2_mean=float(np.mean(rho_err)),
         steps_plain=s_plain, steps_warm=s_warm,
     )
+    if variants:
+        exact = np.concatenate([u_plain, rho_plain[..., None]], axis=-1)
+        _, s_ex, _, _, _, _ = time_to_steady(channels, field_init(exact, with_neq), tol, check_every, max_steps,
+                                             tile)
+        _, s_r1, _, _, _, _ = time_to_steady(channels, model_init(model, with_neq, rho_from_net=False), tol,
+                                             check_every, max_steps, tile)
+        _, s_nn, _, _, _, _ = time_to_steady(channels, model_init(model, False), tol, check_every, max_steps, tile)
+        out.update(steady_init_steps_mean=float(np.mean(s_ex)), rho_one_steps_mean=float(np.mean(s_r1)),
+                   no_neq_steps_mean=float(np.mean(s_nn)))
+    return out

@@ -106,3 +106,23 @@ def test_trained_network_reaches_steady_state_in_fewer_steps():
     assert r["prediction_u_rel_l2_mean"] < 0.2, r
     assert r["warm_steps_mean"] < 0.9 * r["plain_steps_mean"], r
     assert r["final_u_rel_l2_max"] < 1e-2, r
+
+
+def test_network_input_planes_match_oracle():
+    """kel_unet_make_input (mask, flow parameters, coordinates, column open
+    fraction, downstream resistance, gap height and position, lubrication
+    estimate) against the FP64 restatement, to bf16 rounding."""
+    from lbm_mirror_gb300 import UNet
+    from lbm_mirror_gb300 import warmstart as WS
+    chans = WS.fixed_size_channels(3, seed=61, nx=64, ny=32)
+    mask, u_max, tau = WS.channel_inputs(chans)
+    net = UNet(height=32, width=64, widths=(16, 32, 32, 32), max_batch=4, seed=1)
+    dm, du, dt = (torch.from_numpy(a).cuda() for a in (mask, u_max, tau))
+    torch.cuda.synchronize()
+    net.make_input(dm.data_ptr(), du.data_ptr(), dt.data_ptr(), 3)
+    got = torch.empty((3, 32, 64, 16), dtype=torch.bfloat16, device="cuda")
+    net.get_input(got.data_ptr(), 3)
+    want = O.unet_input(mask, u_max.astype(np.float64), tau.astype(np.float64))
+    want_bf = torch.tensor(want, dtype=torch.float32).to(torch.bfloat16).float().numpy()
+    g = got.float().cpu().numpy()
+    assert np.max(np.abs(g - want_bf) / np.maximum(np.abs(want_bf), 1e-3)) <= 1e-2

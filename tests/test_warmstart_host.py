@@ -50,15 +50,24 @@ def test_oracle_moments_are_chapman_enskog():
             assert abs(pxy - (-r * tau * (dxv + dyu) / 3)) < 1e-12
 
 
-def test_oracle_wall_cells_rest_at_neighbour_density():
+def test_oracle_wall_cells_hold_neighbours_post_collision_populations():
     rng = np.random.default_rng(6)
     flags, pred = _field(rng, 8, 10)
-    f = O.warm_start_populations(flags, pred, (1, 1, 0.1), (0, 0, 1), 0.6).reshape(8, 10, 9)
-    # a bottom-wall cell below fluid: mean density of its 3 fluid neighbours
+    tau = 0.6
+    scale, offset = (1, 1, 0.1), (0, 0, 1)
+    f = O.warm_start_populations(flags, pred, scale, offset, tau).reshape(8, 10, 9)
+    fneq0 = O.warm_start_populations(flags, pred, scale, offset, tau, with_neq=False).reshape(8, 10, 9)
     rho = pred[..., 2] * 0.1 + 1
     x = 5
-    want = np.mean([rho[1, x - 1], rho[1, x], rho[1, x + 1]])
-    assert np.allclose(f[0, x], O.W * want, rtol=0, atol=1e-14)
+    # bottom-wall cell (0, x): slots pointing up from the fluid row above come
+    # from there; the others hold the rest state at the neighbours' density
+    want_rest = np.mean([rho[1, x - 1], rho[1, x], rho[1, x + 1]])
+    for i in range(9):
+        if O.CY[i] < 0:  # source (x - cx, 1) is fluid
+            post = fneq0[1, x - O.CX[i], i] + (1 - 1 / tau) * (f[1, x - O.CX[i], i] - fneq0[1, x - O.CX[i], i])
+            assert abs(f[0, x, i] - post) < 1e-14
+        else:
+            assert abs(f[0, x, i] - O.W[i] * want_rest) < 1e-14
 
 
 def test_targets_normalisation_round_trip():
@@ -74,4 +83,35 @@ def test_targets_normalisation_round_trip():
     assert np.allclose(t[..., 2] * um * s + 1, rho, rtol=1e-6, atol=1e-6)
     mask, _, _ = WS.channel_inputs(chans)
     assert mask.shape == (4, 16, 32) and set(np.unique(mask)) <= {0, 1}
-    assert abs(np.sqrt(np.mean(t[..., 2][mask == 0] ** 2)) - 1.0) < 1e-5
+    assert abs(np.sqrt(np.mean(t[..., 2][mask == 0] ** 2)) - 0.25) < 1e-5
+
+
+def test_lubrication_input_is_the_poiseuille_profile_in_an_empty_channel():
+    """Without obstacles the lubrication channel is the inlet's parabola
+    (u_x / u_max = 4 eta (1 - eta), halved) and the downstream resistance
+    falls linearly to 1 / W at the outlet column."""
+    H, W = 10, 12
+    mask = np.zeros((1, H, W), np.uint8)
+    mask[0, 0, :] = mask[0, -1, :] = 1
+    x = O.unet_input(mask, np.array([0.05]), np.array([0.8]))
+    eta = (np.arange(1, H - 1) - 0.5) / (H - 2)
+    np.testing.assert_allclose(x[0, 1:H - 1, 3, 9], 0.5 * 4 * eta * (1 - eta), rtol=1e-12)
+    np.testing.assert_allclose(x[0, 1:H - 1, :, 6][0], (W - np.arange(W)) / W, rtol=1e-12)
+    assert (x[0, 0, :, 5:] == 0).all()
+
+
+def test_lubrication_input_splits_flux_as_gap_cubes():
+    """An obstacle splitting a column into gaps of h1 = 3 and h2 = 5 cells:
+    each gap's estimate is h^2 / (h1^3 + h2^3) times its own profile, so the
+    summed estimates are in the ratio h1^2 S1 : h2^2 S2 (S = the sum of
+    4 s (1 - s) over the gap's cell midpoints, about 2 h / 3)."""
+    H, W = 12, 4
+    mask = np.zeros((1, H, W), np.uint8)
+    mask[0, 0, :] = mask[0, -1, :] = 1
+    mask[0, 4:6, 2] = 1  # gaps of 3 (y 1..3) and 5 (y 6..10) cells in column 2
+    x = O.unet_input(mask, np.array([0.05]), np.array([0.8]))
+    u = 2 * x[0, :, 2, 9]  # u_x / u_max estimate
+    q1, q2 = u[1:4].sum(), u[6:11].sum()
+    s1 = sum(4 * ((k + 0.5) / 3) * (1 - (k + 0.5) / 3) for k in range(3))
+    s2 = sum(4 * ((k + 0.5) / 5) * (1 - (k + 0.5) / 5) for k in range(5))
+    np.testing.assert_allclose(q1 / q2, (3 ** 2 * s1) / (5 ** 2 * s2), rtol=1e-12)
