@@ -43,6 +43,7 @@ WORKLOADS = {
     "d2q9_batch_1024": (9, None, None, "batch"),
     "d2q9_batch_1024_converge": (9, None, None, "batch_converge"),
     "d2q9_warm_start_256x64": (9, (256, 64), None, "warm_start"),
+    "unet_train_256x64": (9, (256, 64), None, "unet_train"),
     "d2q9_psm_particles_2048x512": (9, (2048, 512), 0.7, "particles"),
 }
 
@@ -322,6 +323,8 @@ def run_warm_start(args, rank, world):
                 "final_u_rel_l2": {"mean": r["final_u_rel_l2_mean"], "max": r["final_u_rel_l2_max"]},
                 "prediction_u_rel_l2": {"mean": r["prediction_u_rel_l2_mean"], "max": r["prediction_u_rel_l2_max"]},
                 "prediction_drho_rel_l2_mean": r["prediction_drho_rel_l2_mean"],
+                "nonfinite_channels": r["nonfinite_channels"],
+                "warm_fallbacks_to_rest": r["warm_fallbacks_to_rest"],
                 "init_variants_steps_mean": {"steady_state_itself": r["steady_init_steps_mean"],
                                              "net_u_rho_one": r["rho_one_steps_mean"],
                                              "net_without_neq": r["no_neq_steps_mean"]},
@@ -341,6 +344,60 @@ def run_warm_start(args, rank, world):
                              "peak_source": "measured" if bf16 else None,
                              "kernel": "U-Net training step (whole step, host loop included)"},
                 "gpu_launches": None}
+        print(json.dumps(line))
+
+
+def run_unet_train(args, rank, world):
+    """Training steps of the warm-start U-Net (widths 32, 64, 128, 128; 256x64
+    grids; batch 32) on the input planes of seeded channels and a synthetic
+    target: make_input + forward + backward (loss read back) + Adam per step.
+    value = model TFLOP/s of the whole step (3 x the forward FLOPs)."""
+    import torch
+    from lbm_mirror_gb300 import UNet
+    from lbm_mirror_gb300 import warmstart as WS
+    nx, ny = WORKLOADS[args.workload][1]
+    n, widths = 32, (32, 64, 128, 128)
+    chans = WS.fixed_size_channels(n, seed=77, nx=nx, ny=ny)
+    mask, umax, tau = WS.channel_inputs(chans)
+    dm, du, dt = (torch.from_numpy(a).cuda() for a in (mask, umax, tau))
+    tgt = torch.randn((n, ny, nx, 3), device="cuda", generator=torch.Generator(device="cuda").manual_seed(5)) * 0.1
+    net = UNet(height=ny, width=nx, widths=widths, max_batch=n, seed=1)
+
+    def step():
+        net.make_input(dm.data_ptr(), du.data_ptr(), dt.data_ptr(), n)
+        net.forward(n)
+        loss = net.backward(tgt.data_ptr(), n)
+        net.adam_step(lr=1e-3)
+        return loss
+
+    for _ in range(args.warmup):
+        step()
+    net.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        loss = step()
+    net.synchronize()
+    dt_s = (time.perf_counter() - t0) / args.steps
+    flops = 3 * unet_flops_per_sample(ny, nx, widths) * n
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    bf16 = json.load(open(pk)).get("bf16_tflops") if os.path.exists(pk) else None
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        net.forward(n)
+    net.synchronize()
+    fwd_s = (time.perf_counter() - t0) / args.steps
+    line = {"metric": "unet_train_tflops", "value": flops / dt_s / 1e12, "unit": "TFLOP/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt_s * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16 x bf16 -> fp32", "data": "synthetic",
+            "config": {"workload": "unet_train_256x64", "batch": n, "widths": list(widths),
+                       "params": net.n_params, "conv": "tcgen05"},
+            "forward_ms": fwd_s * 1e3, "forward_tflops": unet_flops_per_sample(ny, nx, widths) * n / fwd_s / 1e12,
+            "loss": loss,
+            "roofline": {"bound": "tensor", "achieved": flops / dt_s / 1e12, "peak": bf16, "unit": "TFLOP/s",
+                         "frac": flops / dt_s / 1e12 / bf16 if bf16 else None, "traffic": None,
+                         "peak_source": "measured" if bf16 else None, "kernel": "whole training step"},
+            "gpu_launches": None}
+    if rank == 0:
         print(json.dumps(line))
 
 
@@ -437,6 +494,9 @@ def main():
         return
     if WORKLOADS[args.workload][3] == "warm_start":
         run_warm_start(args, rank, world)
+        return
+    if WORKLOADS[args.workload][3] == "unet_train":
+        run_unet_train(args, rank, world)
         return
     dist = None
     if world > 1:

@@ -268,7 +268,8 @@ __global__ void k_batch_residual_final(BatchParams p, int n_channels, double tol
 		a += v.x;
 		b += v.y;
 	}
-	const double r = b > 0.0 ? sqrt(a / b) : (a > 0.0 ? INFINITY : 0.0);
+	// NaN sums (a NaN or overflowed field) give a NaN residual: diverged
+	const double r = (isnan(a) || isnan(b)) ? (double)NAN : (b > 0.0 ? sqrt(a / b) : (a > 0.0 ? INFINITY : 0.0));
 	residual[c] = r;
 	if (r < tol || !isfinite(r)) p.active[c] = 0;
 }

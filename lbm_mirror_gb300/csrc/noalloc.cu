@@ -81,7 +81,9 @@ __global__ void __launch_bounds__(1024) na_final(const double2 *partial, int til
 		}
 		__syncthreads();
 	}
-	if (threadIdx.x == 0) *result = sb[0] > 0.0 ? sqrt(sa[0] / sb[0]) : (sa[0] > 0.0 ? INFINITY : 0.0);
+	if (threadIdx.x == 0)
+		*result = (isnan(sa[0]) || isnan(sb[0])) ? (double)NAN
+											   : (sb[0] > 0.0 ? sqrt(sa[0] / sb[0]) : (sa[0] > 0.0 ? INFINITY : 0.0));
 }
 
 // Device address of the scratch array, looked up once per device with that

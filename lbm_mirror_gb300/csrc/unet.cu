@@ -680,6 +680,43 @@ __global__ void bias_grad(const bf16 *dy, int64_t M, int Co, float *db) {
 	if (threadIdx.x == 0) db[co] += sh[0];
 }
 
+// Per-channel sums over pixels, in parallel over pixel chunks: block b sums
+// pixels [b * chunk, (b + 1) * chunk) of dY (M x Co, bf16); thread t owns
+// channel t % Co and every (blockDim / Co)-th pixel of the chunk (coalesced
+// rows), then the threads of one channel are added in thread order.
+// partial[b][co] is reduced over blocks in order by reduce_partials.
+__global__ void __launch_bounds__(256) channel_sums_partial(const bf16 *dy, int64_t M, int Co, int64_t chunk,
+															 float *partial) {
+	__shared__ float sh[256];
+	const int per = blockDim.x / Co; // pixels in flight per block (Co divides 256)
+	const int c = threadIdx.x % Co, r = threadIdx.x / Co;
+	const int64_t m0 = (int64_t)blockIdx.x * chunk;
+	const int64_t m1 = m0 + chunk < M ? m0 + chunk : M;
+	float s = 0.f;
+	if (r < per)
+		for (int64_t m = m0 + r; m < m1; m += per) s += __bfloat162float(dy[m * Co + c]);
+	sh[threadIdx.x] = s;
+	__syncthreads();
+	if (threadIdx.x < Co) {
+		float t = 0.f;
+		for (int k = 0; k < per; ++k) t += sh[k * Co + threadIdx.x];
+		partial[(int64_t)blockIdx.x * Co + threadIdx.x] = t;
+	}
+}
+
+// db[co] += sum over pixels of dY[m][co], deterministic (fixed chunks and order)
+void bias_grads(const bf16 *dy, int64_t M, int Co, float *scratch, float *db, cudaStream_t st) {
+	if (Co > 256) {
+		bias_grad<<<Co, 256, 0, st>>>(dy, M, Co, db);
+		return;
+	}
+	const int blocks = 304;
+	const int64_t chunk = (M + blocks - 1) / blocks;
+	const int nb = (int)((M + chunk - 1) / chunk);
+	channel_sums_partial<<<nb, 256, 0, st>>>(dy, M, Co, chunk, scratch);
+	reduce_partials<<<(Co + 127) / 128, 128, 0, st>>>(scratch, Co, nb, db);
+}
+
 // ---- element-wise pieces -----------------------------------------------------------
 
 __global__ void relu_backward(bf16 *dy, const bf16 *y, int64_t n) {
@@ -815,6 +852,46 @@ __global__ void head_backward_dw(const float *dy, const bf16 *x, int64_t M, int 
 		__syncthreads();
 	}
 	if (threadIdx.x == 0) partial[j] += sh[0];
+}
+
+// The same sums in parallel over pixel chunks (Ci divides 256, Co <= 8):
+// block b covers pixels [b * chunk, ...); thread t owns input channel t % Ci
+// and every (256 / Ci)-th pixel; partial[b][co * Ci + ci] and, for the bias,
+// partial[b][Co * Ci + co]; reduced over blocks in order by reduce_partials.
+__global__ void __launch_bounds__(256) head_dw_partial(const float *dy, const bf16 *x, int64_t M, int Ci, int Co,
+														int64_t chunk, float *partial) {
+	__shared__ float sh[2][256];
+	const int per = blockDim.x / Ci;
+	const int ci = threadIdx.x % Ci, r = threadIdx.x / Ci;
+	const int64_t m0 = (int64_t)blockIdx.x * chunk;
+	const int64_t m1 = m0 + chunk < M ? m0 + chunk : M;
+	float acc[8], bacc[8];
+	for (int k = 0; k < 8; ++k) acc[k] = bacc[k] = 0.f;
+	if (r < per)
+		for (int64_t m = m0 + r; m < m1; m += per) {
+			const float xv = __bfloat162float(x[m * Ci + ci]);
+			for (int co = 0; co < Co; ++co) {
+				const float d = dy[m * Co + co];
+				acc[co] += d * xv;
+				bacc[co] += d;
+			}
+		}
+	const int64_t base = (int64_t)blockIdx.x * (Co * Ci + Co);
+	for (int co = 0; co < Co; ++co) {
+		sh[0][threadIdx.x] = acc[co];
+		sh[1][threadIdx.x] = bacc[co];
+		__syncthreads();
+		if (threadIdx.x < Ci) {
+			float t = 0.f, tb = 0.f;
+			for (int k = 0; k < per; ++k) {
+				t += sh[0][k * Ci + threadIdx.x];
+				tb += sh[1][k * Ci + threadIdx.x];
+			}
+			partial[base + co * Ci + threadIdx.x] = t;
+			if (threadIdx.x == 0) partial[base + Co * Ci + co] = tb; // ci == 0 threads saw every pixel once
+		}
+		__syncthreads();
+	}
 }
 
 // Adam on the FP32 master copy, then the bf16 copies: w (co,3,3,ci) and the
@@ -1080,7 +1157,7 @@ int conv_grads_tc(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy
 	conv_wgrad_tc<<<dim3((unsigned)tiles, (unsigned)chunks), 128, smem, U->stream>>>(a);
 	const int64_t per = (int64_t)l.co * K;
 	reduce_partials<<<grid_of(per), 256, 0, U->stream>>>(U->partial, per, (int)chunks, U->g + l.woff);
-	bias_grad<<<l.co, 256, 0, U->stream>>>(dy, M, l.co, U->g + l.woff + per);
+	bias_grads(dy, M, l.co, U->partial, U->g + l.woff + per, U->stream);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
@@ -1110,7 +1187,7 @@ int conv_grads(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy, i
 	conv_wgrad<<<grid, 128, 0, U->stream>>>(a);
 	const int64_t per = (int64_t)l.co * K;
 	reduce_partials<<<grid_of(per), 256, 0, U->stream>>>(U->partial, per, (int)chunks, U->g + l.woff);
-	bias_grad<<<l.co, 256, 0, U->stream>>>(dy, M, l.co, U->g + l.woff + per);
+	bias_grads(dy, M, l.co, U->partial, U->g + l.woff + per, U->stream);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
@@ -1375,7 +1452,16 @@ extern "C" int kel_unet_backward(kel_unet *U, const float *d_target, int32_t n, 
 	mse_loss<<<lb, 256, 0, U->stream>>>(U->out, d_target, U->dout, nout, U->loss_partial);
 	// head
 	head_backward_dx<<<grid_of(M), 256, 0, U->stream>>>(U->dout, U->p + hd.woff, G[T_D0B], M, hd.ci, hd.co);
-	head_backward_dw<<<hd.co * hd.ci + hd.co, 256, 0, U->stream>>>(U->dout, A[T_D0B], M, hd.ci, hd.co, U->g + hd.woff);
+	if (hd.co <= 8 && 256 % hd.ci == 0) {
+		const int64_t chunk = (M + 303) / 304;
+		const int nb = (int)((M + chunk - 1) / chunk);
+		const int64_t per = (int64_t)hd.co * hd.ci + hd.co;
+		head_dw_partial<<<nb, 256, 0, U->stream>>>(U->dout, A[T_D0B], M, hd.ci, hd.co, chunk, U->partial);
+		reduce_partials<<<grid_of(per), 256, 0, U->stream>>>(U->partial, per, nb, U->g + hd.woff);
+	} else {
+		head_backward_dw<<<hd.co * hd.ci + hd.co, 256, 0, U->stream>>>(U->dout, A[T_D0B], M, hd.ci, hd.co,
+																	   U->g + hd.woff);
+	}
 	// one conv layer: relu backward on dy, weight/bias grads, data grad into dx
 	auto back = [&](int li, int t_in, const bf16 *x_in, int t_out, bf16 *dx) -> int {
 		const UnetLayer &l = L[li];

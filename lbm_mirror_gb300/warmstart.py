@@ -250,14 +250,27 @@ def _rel_l2(a, b):
     return d / r if r > 0 else d
 
 
+@dataclass
+class SteadyRun:
+    """One timed run: wall seconds, steps and last residual per channel, the
+    final u (n, ny, nx, 2) and rho (n, ny, nx), the initialiser's output (or
+    None) and how many channels fell back to a run from rest."""
+    seconds: float
+    steps: np.ndarray
+    residual: np.ndarray
+    u: np.ndarray
+    rho: np.ndarray
+    pred: np.ndarray | None
+    fell_back: int = 0
+
+
 def time_to_steady(channels, init=None, tol=1e-6, check_every=1000, max_steps=600_000, tile=128,
                    arithmetic=K.KEL_ARITH_SHIFTED):
     """One batched run of `channels` to the residual `tol`, from rest (init
     None) or from init(batch, d_mask, d_umax, d_tau) (model_init /
     field_init).  The timed region holds the initialiser (inference and
     population reconstruction) and every sweep; the batch set-up (flags and
-    the rest state) is outside it for both.  Returns (seconds, steps,
-    residual, u (n, ny, nx, 2), rho (n, ny, nx), initialiser output or None)."""
+    the rest state) is outside it for both.  Returns a SteadyRun."""
     torch = _torch()
     ny, nx = channels[0]["ny"], channels[0]["nx"]
     b = Batch(channels, channel_program(0.8, arithmetic), tile=tile)
@@ -273,16 +286,35 @@ def time_to_steady(channels, init=None, tol=1e-6, check_every=1000, max_steps=60
     if init is not None:
         pred = init(b, d_mask, d_umax, d_tau)
     steps, res = b.run_until(tol=tol, check_every=check_every, max_steps=max_steps)
-    seconds = time.perf_counter() - t0
     u = np.empty((len(channels), ny, nx, 2), np.float32)
     rho = np.empty((len(channels), ny, nx), np.float32)
+    fell_back = np.zeros(len(channels), bool)
+    if init is not None:
+        # the plain run from rest is the fallback: a warm-started channel
+        # that diverged (NaN / inf residual) is run again from rest, in the
+        # timed region, its steps added to those it spent
+        bad = np.flatnonzero(~np.isfinite(res))
+        if len(bad):
+            fb = Batch([channels[k] for k in bad], channel_program(0.8, arithmetic), tile=tile)
+            s2, r2 = fb.run_until(tol=tol, check_every=check_every, max_steps=max_steps)
+            for j, k in enumerate(bad):
+                steps[k] += s2[j]
+                res[k] = r2[j]
+                r_, uu = fb.macros(j)
+                u[k] = uu.reshape(ny, nx, 2)
+                rho[k] = r_.reshape(ny, nx)
+            fb.close()
+            fell_back[bad] = True
+    seconds = time.perf_counter() - t0
     for k in range(len(channels)):
+        if fell_back[k]:
+            continue
         r, uu = b.macros(k)
         u[k] = uu.reshape(ny, nx, 2)
         rho[k] = r.reshape(ny, nx)
     b.close()
     pred_np = pred.cpu().numpy() if pred is not None else None
-    return seconds, steps, res, u, rho, pred_np
+    return SteadyRun(seconds, steps, res, u, rho, pred_np, int(fell_back.sum()))
 
 
 def evaluate(model: WarmStartNet, channels, tol=1e-6, check_every=1000, max_steps=600_000, tile=128,
@@ -296,16 +328,15 @@ def evaluate(model: WarmStartNet, channels, tol=1e-6, check_every=1000, max_step
     error.  With variants, also the mean steps from the plain run's own
     steady state (the floor any prediction can reach), from the network's
     u with rho = 1, and without the non-equilibrium part."""
-    t_plain, s_plain, r_plain, u_plain, rho_plain, _ = time_to_steady(channels, None, tol, check_every, max_steps,
-                                                                      tile)
-    ok = np.flatnonzero(r_plain < tol)
+    pr = time_to_steady(channels, None, tol, check_every, max_steps, tile)
+    ok = np.flatnonzero(pr.residual < tol)
     excluded = len(channels) - len(ok)
     if excluded:
         channels = [channels[k] for k in ok]
-        t_plain, s_plain, r_plain, u_plain, rho_plain, _ = time_to_steady(channels, None, tol, check_every,
-                                                                          max_steps, tile)
-    t_warm, s_warm, r_warm, u_warm, _, pred = time_to_steady(channels, model_init(model, with_neq), tol,
-                                                             check_every, max_steps, tile)
+        pr = time_to_steady(channels, None, tol, check_every, max_steps, tile)
+    t_plain, s_plain, r_plain, u_plain, rho_plain = pr.seconds, pr.steps, pr.residual, pr.u, pr.rho
+    wr = time_to_steady(channels, model_init(model, with_neq), tol, check_every, max_steps, tile)
+    t_warm, s_warm, r_warm, u_warm, pred, fallbacks = wr.seconds, wr.steps, wr.residual, wr.u, wr.pred, wr.fell_back
     mask, u_max, _ = channel_inputs(channels)
     final_err = np.array([_rel_l2(u_warm[k], u_plain[k]) for k in range(len(channels))])
     pred_u = pred[..., :2] * u_max[:, None, None, None]
@@ -314,24 +345,27 @@ def evaluate(model: WarmStartNet, channels, tol=1e-6, check_every=1000, max_step
     pred_rho = pred[..., 2] * (u_max[:, None, None] * model.rho_scale) + 1.0
     fl = mask == 0
     rho_err = np.array([_rel_l2(pred_rho[k][fl[k]] - 1, rho_plain[k][fl[k]] - 1) for k in range(len(channels))])
+    nonfinite = dict(pred=int(sum(not np.isfinite(pred[k][fl[k]]).all() for k in range(len(channels)))),
+                     u_warm=int(sum(not np.isfinite(u_warm[k]).all() for k in range(len(channels)))),
+                     u_plain=int(sum(not np.isfinite(u_plain[k]).all() for k in range(len(channels)))))
     out = dict(
         channels=len(channels), excluded_unsteady=excluded, tol=tol, check_every=check_every,
         plain_seconds=t_plain, warm_seconds=t_warm, speedup=t_plain / t_warm,
         plain_steps_mean=float(np.mean(s_plain)), warm_steps_mean=float(np.mean(s_warm)),
         plain_steps_max=int(np.max(s_plain)), warm_steps_max=int(np.max(s_warm)),
         plain_unconverged=int(np.sum(~(r_plain < tol))), warm_unconverged=int(np.sum(~(r_warm < tol))),
-        final_u_rel_l2_mean=float(np.mean(final_err)), final_u_rel_l2_max=float(np.max(final_err)),
-        prediction_u_rel_l2_mean=float(np.mean(pred_err)), prediction_u_rel_l2_max=float(np.max(pred_err)),
-        prediction_drho_rel_l2_mean=float(np.mean(rho_err)),
+        final_u_rel_l2_mean=float(np.nanmean(final_err)), final_u_rel_l2_max=float(np.nanmax(final_err)),
+        prediction_u_rel_l2_mean=float(np.nanmean(pred_err)), prediction_u_rel_l2_max=float(np.nanmax(pred_err)),
+        prediction_drho_rel_l2_mean=float(np.nanmean(rho_err)), nonfinite_channels=nonfinite,
+        warm_fallbacks_to_rest=fallbacks,
         steps_plain=s_plain, steps_warm=s_warm,
     )
     if variants:
         exact = np.concatenate([u_plain, rho_plain[..., None]], axis=-1)
-        _, s_ex, _, _, _, _ = time_to_steady(channels, field_init(exact, with_neq), tol, check_every, max_steps,
-                                             tile)
-        _, s_r1, _, _, _, _ = time_to_steady(channels, model_init(model, with_neq, rho_from_net=False), tol,
-                                             check_every, max_steps, tile)
-        _, s_nn, _, _, _, _ = time_to_steady(channels, model_init(model, False), tol, check_every, max_steps, tile)
+        s_ex = time_to_steady(channels, field_init(exact, with_neq), tol, check_every, max_steps, tile).steps
+        s_r1 = time_to_steady(channels, model_init(model, with_neq, rho_from_net=False), tol, check_every,
+                              max_steps, tile).steps
+        s_nn = time_to_steady(channels, model_init(model, False), tol, check_every, max_steps, tile).steps
         out.update(steady_init_steps_mean=float(np.mean(s_ex)), rho_one_steps_mean=float(np.mean(s_r1)),
                    no_neq_steps_mean=float(np.mean(s_nn)))
     return out

@@ -1,0 +1,52 @@
+"""Full-size lid-driven cavity (256^3, tau 0.55, lid u = (0.1, 0, 0), rest
+start, 5,000 steps) on the GPU in FP32 and FP16-shifted storage against the
+FP64 oracle run of the same case (tests/golden/cavity256_d3q*_fp64_5000_sub8.npz,
+made by tests/golden/make_cavity_fp64.py), compared at the fixture's 32^3
+sub-sampled cells.  Bars: FP16-shifted relative L2 velocity error <= 1e-3;
+FP32 <= 1e-4."""
+import os
+
+import numpy as np
+import pytest
+
+from lbm_mirror_gb300 import capi as K
+from tests import cases
+from tests.gpu_util import make_lattice, rel_l2, with_arith
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def fixture(q):
+    p = os.path.join(HERE, "golden", f"cavity256_d3q{q}_fp64_5000_sub8.npz")
+    if not os.path.exists(p):
+        pytest.skip(f"{os.path.basename(p)} not generated")
+    return np.load(p)
+
+
+def errors_vs_fp64(q, storage):
+    """(relative L2 of u, relative L2 of rho - 1) at the fixture's cells."""
+    g = fixture(q)
+    n, st, off, steps = int(g["n"]), int(g["stride"]), int(g["offset"]), int(g["steps"])
+    case = cases.cavity_3d(q, dims=(n, n, n), steps=steps)
+    lat = make_lattice(case, storage)
+    prog = with_arith(case["program"], K.KEL_ARITH_FAST)
+    lat.step(prog, steps - 1, write_macros=False)
+    lat.step(prog, 1, write_macros=True)
+    rho, u = lat.macros()
+    lat.close()
+    rho = rho.reshape(n, n, n)
+    u = u.reshape(n, n, n, 3)
+    sl = (slice(off, n, st),) * 3
+    fl = case["flags"].reshape(n, n, n)[sl] == 2
+    return (rel_l2(u[sl][fl], g["u"][fl]), rel_l2(rho[sl][fl] - 1.0, g["rho"][fl] - 1.0))
+
+
+@pytest.mark.parametrize("q", [19, 27])
+def test_fp32_and_fp16s_vs_fp64_oracle_full_size(q):
+    e32 = errors_vs_fp64(q, "fp32")
+    e16 = errors_vs_fp64(q, "fp16s")
+    print(f"D3Q{q} 256^3 x 5000: FP32 u {e32[0]:.3e} rho-1 {e32[1]:.3e}; FP16S u {e16[0]:.3e} rho-1 {e16[1]:.3e}")
+    assert e16[0] <= 1e-3, e16
+    assert e32[0] <= 1e-4, e32
