@@ -334,6 +334,45 @@ int kel_lattice_get_launch(const kel_lattice *lat, int32_t *cells_per_thread, in
 int kel_lattice_autotune(kel_lattice *lat, const kel_step_program *prog, int32_t steps, int32_t *cells_per_thread,
 						 int32_t *block_threads, float *ms_per_step);
 
+/* ---- field output and checkpoints -------------------------------------
+ * Host writers in the reference's formats (write_vtk.hpp, write_csv.hpp,
+ * abstract/forst.hpp + forst_chunk.hpp): cells x fastest over dims; each
+ * field one member of the reference's Struct of Chunks, in order. */
+#define KEL_VALUE_U8 0
+#define KEL_VALUE_F32 1
+#define KEL_VALUE_F64 2
+typedef struct kel_field_view {
+	const char *name;   /* member key, e.g. "velocity", "density", "info" */
+	int32_t value_type; /* KEL_VALUE_* */
+	int32_t components; /* values per cell */
+	int32_t ghost;      /* Forst only: the chunk's ghost width (zeros) */
+	int32_t vector;     /* VTK: VECTORS even with one component */
+	const void *data;   /* host, n_cells * components values */
+} kel_field_view;
+/* <out_dir>/vtk/<file_name>_<t>.vtk: ASCII STRUCTURED_POINTS, all fields. */
+int kel_write_vtk(const char *out_dir, const char *file_name, uint64_t t, const int64_t *dims, int32_t n_dims,
+				  const kel_field_view *fields, int32_t n_fields);
+/* <out_dir>/csv/<file_name>_<name>_<t>.csv per field. */
+int kel_write_csv(const char *out_dir, const char *file_name, uint64_t t, const int64_t *dims, int32_t n_dims,
+				  const kel_field_view *fields, int32_t n_fields);
+/* Forst encoding of the Struct of the fields' chunks (packed, no framing). */
+int kel_write_forst(const char *path, const int64_t *dims, int32_t n_dims, const kel_field_view *fields,
+					int32_t n_fields);
+/* Inverse of kel_write_forst into the views' (writable) buffers; the file
+ * size must match the layout exactly. */
+int kel_read_forst(const char *path, const int64_t *dims, int32_t n_dims, kel_field_view *fields, int32_t n_fields);
+#define KEL_WRITE_VTK 1
+#define KEL_WRITE_CSV 2
+#define KEL_WRITE_FORST 4
+/* The drivers' macro output (MacroStruct {velocity, density}) of the last
+ * step that wrote macros, as VTK / CSV / <out_dir>/forst/<name>_<t>.forst. */
+int kel_lattice_write_fields(kel_lattice *lat, int32_t formats, const char *out_dir, const char *file_name, uint64_t t);
+/* Checkpoint: Forst of {time_step UInt64, info Chunk<UInt8,0>, dfs
+ * Chunk<FixedArray<Float32,Q>,1>} at the current time step; load restores
+ * flags, populations and time step into a lattice of the same shape. */
+int kel_lattice_save(kel_lattice *lat, const char *path);
+int kel_lattice_load(kel_lattice *lat, const char *path);
+
 /* Synchronise the lattice's stream. */
 int kel_lattice_synchronize(kel_lattice *lat);
 

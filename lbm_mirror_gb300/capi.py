@@ -48,6 +48,8 @@ KEL_LAYOUT_AOS, KEL_LAYOUT_SOA = 0, 1
 KEL_FIELD_POROSITY, KEL_FIELD_FORCE = 1, 2
 KEL_STEP_WRITE_MACROS, KEL_STEP_ALL_MACROS = 1, 2
 KEL_UNET_CONV_TCGEN05, KEL_UNET_CONV_MMA_SYNC = 0, 1
+KEL_VALUE_U8, KEL_VALUE_F32, KEL_VALUE_F64 = 0, 1, 2
+KEL_WRITE_VTK, KEL_WRITE_CSV, KEL_WRITE_FORST = 1, 2, 4
 
 
 class FlagOp(C.Structure):
@@ -196,6 +198,11 @@ class UnetDesc(C.Structure):
                 ("reserved", C.c_int32)]
 
 
+class FieldView(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("value_type", C.c_int32), ("components", C.c_int32), ("ghost", C.c_int32),
+                ("vector", C.c_int32), ("data", C.c_void_p)]
+
+
 class ChannelDesc(C.Structure):
     _fields_ = [("nx", C.c_int64), ("ny", C.c_int64), ("tau", C.c_double), ("u_max", C.c_double)]
 
@@ -260,6 +267,13 @@ def load_library(path: str | None = None):
         "kel_batch_download_macros": ([vp, i32, vp], C.c_int),
         "kel_batch_warm_start": ([vp, i32, i32, vp, i64, vp, vp, i32], C.c_int),
         "kel_batch_synchronize": ([vp], C.c_int),
+        "kel_write_vtk": ([C.c_char_p, C.c_char_p, u64, C.POINTER(i64), i32, C.POINTER(FieldView), i32], C.c_int),
+        "kel_write_csv": ([C.c_char_p, C.c_char_p, u64, C.POINTER(i64), i32, C.POINTER(FieldView), i32], C.c_int),
+        "kel_write_forst": ([C.c_char_p, C.POINTER(i64), i32, C.POINTER(FieldView), i32], C.c_int),
+        "kel_read_forst": ([C.c_char_p, C.POINTER(i64), i32, C.POINTER(FieldView), i32], C.c_int),
+        "kel_lattice_write_fields": ([vp, i32, C.c_char_p, C.c_char_p, u64], C.c_int),
+        "kel_lattice_save": ([vp, C.c_char_p], C.c_int),
+        "kel_lattice_load": ([vp, C.c_char_p], C.c_int),
         "kel_lattice_get_launch": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "kel_lattice_autotune": ([vp, C.POINTER(StepProgram), i32, C.POINTER(i32), C.POINTER(i32),
                                   C.POINTER(C.c_float)], C.c_int),

@@ -206,6 +206,12 @@ __device__ __forceinline__ void cp_async16(uint32_t saddr, const void *g, bool v
 	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(valid ? 16 : 0));
 }
 
+// the same through L1: the nine taps of an implicit-GEMM tile re-read the same
+// input rows, which L1 then serves
+__device__ __forceinline__ void cp_async16_l1(uint32_t saddr, const void *g, bool valid) {
+	asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(valid ? 16 : 0));
+}
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
 
 template <int N>
@@ -290,7 +296,7 @@ __global__ void __launch_bounds__(128) conv_tc(TcArgs a) {
 			const int yy = a_y[i] + tap / 3 - 1, xx = a_x[i] + tap % 3 - 1;
 			const bool ok = a_pix[i] >= 0 && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
 			const bf16 *src = ok ? a.x + (a_pix[i] + (int64_t)yy * a.W + xx) * a.Ci + ci : a.x;
-			cp_async16(abase + (row >> 3) * 1024 + g * 128 + (row & 7) * 16, src, ok);
+			cp_async16_l1(abase + (row >> 3) * 1024 + g * 128 + (row & 7) * 16, src, ok);
 		}
 		for (int v = tid; v < a.Co * 8; v += 128) {
 			const int row = v >> 3, g = v & 7;
@@ -452,34 +458,45 @@ __global__ void __launch_bounds__(128) conv_wgrad_tc(TcWgradArgs a) {
 	const uint32_t tmem = *tmem_slot;
 
 	const int cog = a.Co >> 3; // 16-byte groups of dY per pixel
+	// This thread's A vectors: kcol group g = tid % 16 (the same in every
+	// chunk, so its tap and channel are fixed) and pixels tid / 16 + 8 i.
+	const int ga = tid & 15, pa = tid >> 4;
+	const int ka = kc0 + ga * 8;
+	const int tap_a = ka < K ? ka / a.Ci : 0, ci_a = ka - tap_a * a.Ci;
+	const int dy_a = tap_a / 3 - 1, dx_a = tap_a % 3 - 1;
 	auto load_chunk = [&](int c, int s) {
 		const uint32_t abase = smem_u32(As + (size_t)s * a_bytes);
 		const uint32_t bbase = smem_u32(Bs + (size_t)s * b_bytes);
 		const int64_t q0 = p_begin + (int64_t)c * TC_K;
-		// A: 64 pixels x 16 groups of 8 kcol
+		// A: 64 pixels x 16 groups of 8 kcol; (n, y, x) of the first pixel by
+		// one division, then stepped by 8 pixels with carries
+		int64_t m = q0 + pa;
+		int64_t n = m / HW;
+		int r = (int)(m - n * HW);
+		int y = r / a.W, x = r - (r / a.W) * a.W;
 #pragma unroll
 		for (int i = 0; i < 8; ++i) {
-			const int v = tid + 128 * i, g = v & 15, pp = v >> 4;
-			const int64_t m = q0 + pp;
-			const int k = kc0 + g * 8;
-			bool ok = m < p_end && k < K;
-			const bf16 *src = a.x;
-			if (ok) {
-				const int tap = k / a.Ci, ci = k - tap * a.Ci;
-				const int64_t n = m / HW;
-				const int r = (int)(m - n * HW);
-				const int yy = r / a.W + tap / 3 - 1, xx = r % a.W + tap % 3 - 1;
-				ok = yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
-				if (ok) src = a.x + ((n * a.H + yy) * (int64_t)a.W + xx) * a.Ci + ci;
+			const int pp = pa + 8 * i;
+			const int yy = y + dy_a, xx = x + dx_a;
+			const bool ok = m < p_end && ka < K && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
+			const bf16 *src = ok ? a.x + ((n * a.H + yy) * (int64_t)a.W + xx) * a.Ci + ci_a : a.x;
+			cp_async16(abase + ga * 1024 + (pp >> 3) * 128 + (pp & 7) * 16, src, ok);
+			m += 8;
+			x += 8;
+			while (x >= a.W) {
+				x -= a.W;
+				if (++y == a.H) {
+					y = 0;
+					++n;
+				}
 			}
-			cp_async16(abase + g * 1024 + (pp >> 3) * 128 + (pp & 7) * 16, src, ok);
 		}
 		// B: 64 pixels x Co / 8 groups of dY
 		for (int v = tid; v < TC_K * cog; v += 128) {
 			const int g = v % cog, pp = v / cog;
-			const int64_t m = q0 + pp;
-			const bool ok = m < p_end;
-			cp_async16(bbase + g * 1024 + (pp >> 3) * 128 + (pp & 7) * 16, ok ? a.dy + m * a.Co + g * 8 : a.dy, ok);
+			const int64_t mb = q0 + pp;
+			const bool ok = mb < p_end;
+			cp_async16(bbase + g * 1024 + (pp >> 3) * 128 + (pp & 7) * 16, ok ? a.dy + mb * a.Co + g * 8 : a.dy, ok);
 		}
 	};
 
@@ -1102,7 +1119,7 @@ int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
 		t.Co = co;
 		t.relu = relu;
 		t.use_bias = bias;
-		t.stages = co <= 64 ? 4 : (co <= 128 ? 3 : 2);
+		t.stages = co <= 128 ? 3 : 2; // 2-3 CTAs per SM by shared memory
 		t.tmem_cols = 32;
 		while (t.tmem_cols < (uint32_t)co) t.tmem_cols <<= 1;
 		t.err = U->d_err;
@@ -1144,7 +1161,7 @@ int conv_grads_tc(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy
 	if (chunks < 1) chunks = 1;
 	a.chunk = ((M + chunks - 1) / chunks + TC_K - 1) / TC_K * TC_K;
 	chunks = (M + a.chunk - 1) / a.chunk;
-	a.stages = l.co <= 64 ? 4 : (l.co <= 128 ? 3 : 2);
+	a.stages = l.co <= 128 ? 3 : 2;
 	a.tmem_cols = 32;
 	while (a.tmem_cols < (uint32_t)l.co) a.tmem_cols <<= 1;
 	a.err = U->d_err;

@@ -246,6 +246,20 @@ class Lattice:
         fl = (K.KEL_STEP_WRITE_MACROS if write_macros else 0) | (K.KEL_STEP_ALL_MACROS if all_macros else 0)
         _check(self.lib.kel_step(self._h, C.byref(program), n_steps, fl), self.lib)
 
+    def write_fields(self, out_dir, file_name, t, formats=K.KEL_WRITE_VTK):
+        """The macro output (velocity, density) as the reference's VTK / CSV /
+        Forst files under out_dir (kel_lattice_write_fields)."""
+        _check(self.lib.kel_lattice_write_fields(self._h, int(formats), str(out_dir).encode(),
+                                                 str(file_name).encode(), int(t)), self.lib)
+
+    def save(self, path):
+        """Checkpoint (Forst: time step, flags, populations)."""
+        _check(self.lib.kel_lattice_save(self._h, str(path).encode()), self.lib)
+
+    def load(self, path):
+        """Restore a checkpoint written by save() (same descriptor and extents)."""
+        _check(self.lib.kel_lattice_load(self._h, str(path).encode()), self.lib)
+
     def set_launch(self, cells_per_thread, block_threads=256):
         _check(self.lib.kel_lattice_set_launch(self._h, cells_per_thread, block_threads), self.lib)
 

@@ -32,12 +32,17 @@
  *   out_dir/rho.f64, out_dir/vel.f64   macros of the last collide
  */
 #include "lbm.hpp" /* modules/core/c++/lbm.hpp, via -I */
+#include "forst_chunk.hpp"
+#include "write_csv.hpp"
+#include "write_vtk.hpp"
 
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <filesystem>
 #include <map>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -520,6 +525,67 @@ struct ParticleCase {
 	}
 };
 
+/*
+ * Field writers of the reference on given values: write_vtk_file /
+ * write_csv_file (modules/core/c++/write_vtk.hpp, write_csv.hpp) of the
+ * drivers' MacroStruct {velocity, density} and of the lattice struct {info,
+ * dfs, dfs_old}, and the Forst encoding (abstract/forst.hpp, forst_chunk.hpp)
+ * of both, for byte comparison with the library's writers.
+ *   in_dir/flags.u8, dfs.f64 (AoS, Q per cell), rho.f64, vel.f64 (D per cell)
+ *   out_dir/vtk/m_37.vtk, out_dir/vtk/initial_state_0.vtk,
+ *   out_dir/csv/m_velocity_37.csv, out_dir/csv/m_density_37.csv,
+ *   out_dir/m.forst, out_dir/lattice.forst
+ */
+template <typename T, typename Desc, uint64_t... Dims>
+struct WriterCase {
+	using B = Case<T, Desc, Dims...>;
+	static constexpr uint64_t D = Desc::D, Q = Desc::Q, N = B::N;
+	using NT = typename native_data_type<T>::type;
+	using Macro = sch::Struct<sch::Member<sch::Chunk<sch::Vector<T, D>, 0u, Dims...>, "velocity">,
+							  sch::Member<sch::Chunk<sch::Scalar<T>, 0u, Dims...>, "density">>;
+
+	template <typename Sch>
+	static int encode(const data<Sch> &from, const std::string &path) {
+		codec<Sch, enc::Forst> c;
+		data<Sch, enc::Forst> bytes;
+		auto eov = c.encode(from, bytes);
+		if (eov.is_error()) return 3;
+		std::ofstream f(path, std::ios::binary);
+		f.write(reinterpret_cast<const char *>(bytes.raw()), (std::streamsize)bytes.size().get());
+		return 0;
+	}
+
+	static int run(const std::string &in, const std::string &out) {
+		auto flags = read_file(in + "/flags.u8", true);
+		auto dfs = read_file(in + "/dfs.f64", true);
+		auto rho = read_file(in + "/rho.f64", true);
+		auto vel = read_file(in + "/vel.f64", true);
+		const double *pd = reinterpret_cast<const double *>(dfs.data());
+		const double *pr = reinterpret_cast<const double *>(rho.data());
+		const double *pv = reinterpret_cast<const double *>(vel.data());
+		auto macros = std::make_unique<data<Macro>>();
+		auto fields = std::make_unique<data<typename B::ChunkStruct>>();
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = B::unflat(c);
+			for (uint64_t d = 0; d < D; ++d)
+				macros->template get<"velocity">().at(idx).at({{d}}).set(static_cast<NT>(pv[c * D + d]));
+			macros->template get<"density">().at(idx).at({}).set(static_cast<NT>(pr[c]));
+			fields->template get<"info">().at(idx).set(static_cast<uint8_t>(flags[c]));
+			for (uint64_t i = 0; i < Q; ++i) {
+				fields->template get<"dfs">().at(idx).at({i}).set(static_cast<NT>(pd[c * Q + i]));
+				fields->template get<"dfs_old">().at(idx).at({i}).set(static_cast<NT>(-pd[c * Q + i]));
+			}
+		}
+		std::filesystem::path od(out);
+		if (write_vtk_file(od, "m", 37u, *macros).is_error()) return 4;
+		if (write_csv_file(od, "m", 37u, *macros).is_error()) return 4;
+		if (write_vtk_file(od, "initial_state", 0u, *fields).is_error()) return 4;
+		if (encode(*macros, out + "/m.forst")) return 3;
+		if (encode(*fields, out + "/lattice.forst")) return 3;
+		return 0;
+	}
+};
+
 int main(int argc, char **argv) {
 	if (argc != 4) {
 		std::fprintf(stderr, "usage: %s <case> <in_dir> <out_dir>\n", argv[0]);
@@ -537,6 +603,8 @@ int main(int argc, char **argv) {
 	if (c == "particles_d2q9_f64_64x48x5") return ParticleCase<F64, sch::D2Q9, 64, 48, 5>::run(argv[2], argv[3]);
 	if (c == "particles_d2q9_f32_64x48x5") return ParticleCase<F32, sch::D2Q9, 64, 48, 5>::run(argv[2], argv[3]);
 	if (c == "d3q27_f64_16x12x10") return Case<F64, sch::D3Q27, 16, 12, 10>::run(argv[2], argv[3]);
+	if (c == "writers_d2q9_f32_12x7") return WriterCase<F32, sch::D2Q9, 12, 7>::run(argv[2], argv[3]);
+	if (c == "writers_d3q19_f64_5x4x3") return WriterCase<F64, sch::D3Q19, 5, 4, 3>::run(argv[2], argv[3]);
 	std::fprintf(stderr, "unknown case %s\n", c.c_str());
 	return 1;
 }

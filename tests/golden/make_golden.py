@@ -172,7 +172,43 @@ def load_particles(name):
 
 
 def names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("particles_"))
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.endswith(".npz") and not f.startswith(("particles_", "writers_", "cavity256_")))
+
+
+WRITER_CASES = {"writers_d2q9_f32_12x7": (9, (12, 7), np.float32),
+                "writers_d3q19_f64_5x4x3": (19, (5, 4, 3), np.float64)}
+WRITER_FILES = ("vtk/m_37.vtk", "vtk/initial_state_0.vtk", "csv/m_velocity_37.csv", "csv/m_density_37.csv",
+                "m.forst", "lattice.forst")
+
+
+def writer_inputs(q, dims, dtype, seed=21):
+    """Values that exercise the number formatting: magnitudes from 1e-9 to 1e3,
+    both signs, exact zeros and integers."""
+    rng = np.random.default_rng(seed)
+    n = int(np.prod(dims))
+    d = 2 if q == 9 else 3
+
+    def vals(shape):
+        v = rng.standard_normal(shape) * 10.0 ** rng.integers(-9, 4, shape)
+        v[rng.random(shape) < 0.05] = 0.0
+        v[rng.random(shape) < 0.05] = 1.0
+        v[rng.random(shape) < 0.05] = -250.0
+        return v.astype(dtype).astype(np.float64)
+
+    flags = rng.integers(0, 6, n).astype(np.uint8)
+    return dict(flags=flags, dfs=vals((n, q)), rho=1.0 + vals(n), vel=vals((n, d)))
+
+
+def run_writer_harness(name, inp, workdir):
+    ind, outd = os.path.join(workdir, "in"), os.path.join(workdir, "out")
+    os.makedirs(ind)
+    os.makedirs(outd)
+    inp["flags"].tofile(os.path.join(ind, "flags.u8"))
+    for k in ("dfs", "rho", "vel"):
+        inp[k].astype(np.float64).tofile(os.path.join(ind, k + ".f64"))
+    subprocess.check_call([HARNESS, name, ind, outd])
+    return {f: np.frombuffer(open(os.path.join(outd, f), "rb").read(), np.uint8) for f in WRITER_FILES}
 
 
 def main():
@@ -190,6 +226,15 @@ def main():
         np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), bodies=bodies, init=init.astype(np.float32),
                             params=np.array(json.dumps(PART_PARAMS)), **out)
         print(f"{name:28s} particles: force after gather {out['after_gather'][:, 18:20].ravel()[:4]}")
+    for name, (q, dims, dtype) in WRITER_CASES.items():
+        if args.only and args.only not in name:
+            continue
+        inp = writer_inputs(q, dims, dtype)
+        with tempfile.TemporaryDirectory() as td:
+            files = run_writer_harness(name, inp, td)
+        np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), **inp,
+                            **{"file:" + f: v for f, v in files.items()})
+        print(f"{name:28s} writers: " + ", ".join(f"{f} {len(v)} B" for f, v in files.items()))
     for name, (hcase, case) in registry().items():
         if args.only and args.only not in name:
             continue
