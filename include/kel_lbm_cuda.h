@@ -69,6 +69,7 @@ extern "C" {
 #define KEL_COLL_BGK_GUO 1 /* cmpt::BGKGuo (collision.hpp:99-205) */
 #define KEL_COLL_PSM 2     /* cmpt::Psm (psm.hpp:37-90) */
 #define KEL_COLL_PSM_GUO 3 /* cmpt::Psm followed by the BGKGuo forcing term */
+#define KEL_COLL_HLBM 4    /* cmpt::Hlbm (hlbm.hpp:53-101), D2Q9: u <- u por + (D > 0 ? N (1 - por) / D : N) */
 
 /* ---- arithmetic mode of the sweep -------------------------------------- */
 #define KEL_ARITH_FAST 0      /* float-float equilibrium bracket, fused BGK relaxation */

@@ -115,6 +115,8 @@ typedef struct ko_lattice {
 		(L)->vel = (REALT *)calloc((size_t)((L)->n * (L)->d.D), sizeof(REALT));          \
 		(L)->por = (REALT *)calloc((size_t)(L)->n, sizeof(REALT));                       \
 		(L)->force = (REALT *)calloc((size_t)((L)->n * (L)->d.D), sizeof(REALT));        \
+		(L)->hN = (REALT *)calloc((size_t)((L)->n * (L)->d.D), sizeof(REALT));           \
+		(L)->hD = (REALT *)calloc((size_t)(L)->n, sizeof(REALT));                        \
 	} while (0)
 
 #define KO_FREE_FIELDS(L)                                                               \
@@ -126,6 +128,8 @@ typedef struct ko_lattice {
 		free((L)->vel);                                                                 \
 		free((L)->por);                                                                 \
 		free((L)->force);                                                               \
+		free((L)->hN);                                                                  \
+		free((L)->hD);                                                                  \
 	} while (0)
 
 /* Rest-equilibrium initial state as in every reference driver's setup:
@@ -281,6 +285,48 @@ void ko_lattice_set_porosity_at(ko_lattice *h, int64_t c, double v) {
 
 double ko_lattice_porosity_at(const ko_lattice *h, int64_t c) {
 	return h->is_f64 ? h->f64.por[c] : (double)h->f32.por[c];
+}
+
+/* HLBM per-cell accumulators (particle_N: D values, particle_D) */
+void ko_lattice_hlbm_add_at(ko_lattice *h, int64_t c, const double *vflip, double flip) {
+	if (h->is_f64) {
+		for (int k = 0; k < h->f64.d.D; ++k) h->f64.hN[c * h->f64.d.D + k] = h->f64.hN[c * h->f64.d.D + k] + vflip[k];
+		h->f64.hD[c] = h->f64.hD[c] + flip;
+	} else {
+		for (int k = 0; k < h->f32.d.D; ++k)
+			h->f32.hN[c * h->f32.d.D + k] = h->f32.hN[c * h->f32.d.D + k] + (float)vflip[k];
+		h->f32.hD[c] = h->f32.hD[c] + (float)flip;
+	}
+}
+
+void ko_lattice_hlbm_reset(ko_lattice *h) {
+	if (h->is_f64) {
+		for (int64_t c = 0; c < h->f64.n; ++c) h->f64.por[c] = 1.0, h->f64.hD[c] = 0.0;
+		memset(h->f64.hN, 0, sizeof(double) * (size_t)(h->f64.n * h->f64.d.D));
+	} else {
+		for (int64_t c = 0; c < h->f32.n; ++c) h->f32.por[c] = 1.0f, h->f32.hD[c] = 0.0f;
+		memset(h->f32.hN, 0, sizeof(float) * (size_t)(h->f32.n * h->f32.d.D));
+	}
+}
+
+void ko_get_hlbm(ko_lattice *h, double *N, double *Dv) {
+	if (h->is_f64) {
+		get_vec_f64(h->f64.hN, N, h->f64.n * h->f64.d.D);
+		get_vec_f64(h->f64.hD, Dv, h->f64.n);
+	} else {
+		get_vec_f32(h->f32.hN, N, h->f32.n * h->f32.d.D);
+		get_vec_f32(h->f32.hD, Dv, h->f32.n);
+	}
+}
+
+void ko_set_hlbm(ko_lattice *h, const double *N, const double *Dv) {
+	if (h->is_f64) {
+		set_vec_f64(h->f64.hN, N, h->f64.n * h->f64.d.D);
+		set_vec_f64(h->f64.hD, Dv, h->f64.n);
+	} else {
+		set_vec_f32(h->f32.hN, N, h->f32.n * h->f32.d.D);
+		set_vec_f32(h->f32.hD, Dv, h->f32.n);
+	}
 }
 
 void ko_get_porosity(ko_lattice *h, double *out) {

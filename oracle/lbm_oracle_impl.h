@@ -23,6 +23,7 @@ typedef struct KO(ko_lat) {
 	uint8_t *info;
 	REAL *dfs[2]; /* [0] = "dfs_old", [1] = "dfs" (ghost-padded AoS) */
 	REAL *rho, *vel, *por, *force;
+	REAL *hN, *hD; /* HLBM "particle_N" (D per cell) and "particle_D" */
 	const double *profile;
 	uint64_t t;
 } KO(ko_lat);
@@ -100,6 +101,19 @@ static void KO(collide)(KO(ko_lat) * L, const kel_step_program *P, REAL *f, int6
 			f[i] = f[i] + freq * (eq[i] - f[i]) + Fi * ((REAL)1 - (REAL)0.5f * freq);
 		}
 		break;
+	case KEL_COLL_HLBM: { /* hlbm.hpp:66-101: convex combination of velocities, then BGK */
+		REAL por = L->por[c];
+		REAL flip = (REAL)1.0 - por;
+		REAL Dv = L->hD[c];
+		for (int k = 0; k < d->D; ++k) {
+			REAL Nk = L->hN[c * d->D + k];
+			REAL add = (Dv > 0.0) ? Nk * flip / Dv : Nk;
+			u[k] = u[k] * por + add;
+			L->vel[c * d->D + k] = u[k];
+		}
+		KO(equilibrium)(d, rho, u, eq);
+		for (int i = 0; i < d->Q; ++i) f[i] = f[i] + freq * (eq[i] - f[i]);
+	} break;
 	case KEL_COLL_PSM:
 	case KEL_COLL_PSM_GUO: { /* psm.hpp:79-88 */
 		REAL por = L->por[c];

@@ -67,6 +67,11 @@ def lib():
         L.ko_particles_reset.argtypes = [vp, C.c_int]
         L.ko_particles_contact.argtypes = [vp, C.c_int, C.c_int, vp, vp, C.c_int]
         L.ko_particles_integrate.argtypes = [vp, C.c_int, C.c_int, vp, vp, C.c_int]
+        L.ko_particles_hlbm_couple.argtypes = [vp, vp, C.c_int, vp]
+        L.ko_particles_hlbm_gather.argtypes = [vp, vp, C.c_int, vp, vp]
+        L.ko_particles_hlbm_stamp.argtypes = [vp, vp, C.c_int, vp]
+        L.ko_get_hlbm.argtypes = [vp, vp, vp]
+        L.ko_set_hlbm.argtypes = [vp, vp, vp]
         _lib = L
     return _lib
 
@@ -157,6 +162,30 @@ class OracleLattice:
         lib().ko_particles_gather(self._h, C.byref(states), len(states), C.byref(params),
                                   _ptr(cf) if cf is not None else None)
         return cf
+
+
+    def hlbm_couple(self, states, params):
+        lib().ko_particles_hlbm_couple(self._h, C.byref(states), len(states), C.byref(params))
+
+    def hlbm_gather(self, states, params, want_cell_force=False):
+        cf = np.zeros(self.n * self.D, dtype=np.float64) if want_cell_force else None
+        lib().ko_particles_hlbm_gather(self._h, C.byref(states), len(states), C.byref(params),
+                                       _ptr(cf) if cf is not None else None)
+        return cf
+
+    def hlbm_stamp(self, states, params):
+        lib().ko_particles_hlbm_stamp(self._h, C.byref(states), len(states), C.byref(params))
+
+    def hlbm_fields(self):
+        N = np.empty(self.n * self.D, dtype=np.float64)
+        Dv = np.empty(self.n, dtype=np.float64)
+        lib().ko_get_hlbm(self._h, _ptr(N), _ptr(Dv))
+        return N.reshape(self.n, self.D), Dv
+
+    def set_hlbm_fields(self, N, Dv):
+        N = np.ascontiguousarray(N, dtype=np.float64).reshape(-1)
+        Dv = np.ascontiguousarray(Dv, dtype=np.float64)
+        lib().ko_set_hlbm(self._h, _ptr(N), _ptr(Dv))
 
 
 def particles_reset(states):

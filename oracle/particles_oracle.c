@@ -215,6 +215,144 @@ void ko_particles_gather(ko_lattice *h, kel_particle_state *P, int np, const kel
 	}
 }
 
+/* ---- HLBM (hlbm.hpp) ---------------------------------------------------- */
+
+void ko_lattice_hlbm_reset(ko_lattice *h);
+void ko_lattice_hlbm_add_at(ko_lattice *h, int64_t c, const double *vflip, double flip);
+
+/* HlbmReset (hlbm.hpp:27-47) on every cell, then the porosity each
+ * HlbmOneParticleGather writes over its AABB (hlbm.hpp:178-186, the reference
+ * ramp with eps = 1.5), bodies in index order: a cell inside several AABBs
+ * keeps the last body's value, 1 included. */
+void ko_particles_hlbm_couple(ko_lattice *h, const kel_particle_state *P, int np, const kel_particle_params *prm) {
+	int D, Q, f64, per;
+	int64_t nx, ny, nz;
+	ko_lattice_info(h, &D, &Q, &nx, &ny, &nz, &f64, &per);
+	int64_t ext[3] = {nx, ny, nz};
+	ko_lattice_hlbm_reset(h);
+	for (int p = 0; p < np; ++p) {
+		int64_t a[3] = {0, 0, 0}, b[3] = {1, 1, 1};
+		aabb(D, &P[p], ext, per, 0, a, b);
+		for (int64_t ix = a[0]; ix < b[0]; ++ix)
+			for (int64_t iy = a[1]; iy < b[1]; ++iy)
+				for (int64_t iz = (D == 3 ? a[2] : 0); iz < (D == 3 ? b[2] : 1); ++iz) {
+					int64_t x = per ? ((ix % nx) + nx) % nx : ix;
+					double rel[3] = {rel_coord((double)x, P[p].position[0], per, nx), (double)iy - P[p].position[1],
+									 D == 3 ? (double)iz - P[p].position[2] : 0.0};
+					double s2 = 0.0;
+					for (int k = 0; k < D; ++k) s2 = s2 + rel[k] * rel[k];
+					ko_lattice_set_porosity_at(h, x + nx * (iy + ny * iz), ramp(sqrt(s2), P[p].radius, prm->eps));
+				}
+	}
+}
+
+/* HlbmOneParticleGather (hlbm.hpp:119-260): momentum exchange with the body's
+ * pre-move velocity over the cells of its AABB where its own porosity is
+ * below 1, no solid-fraction weight; the cell force (last body wins) is that
+ * momentum, the body takes minus the sum and minus the r x momentum torque. */
+#define KO_HLBM_GATHER_BODY(REALT, POP)                                                                      \
+	for (int p = 0; p < np; ++p) {                                                                           \
+		kel_particle_state *pp = &P[p];                                                                      \
+		int64_t a[3] = {0, 0, 0}, b[3] = {1, 1, 1};                                                          \
+		aabb(D, pp, ext, per, 0, a, b);                                                                      \
+		double ts = 1.0 / (double)steps;                                                                     \
+		double vp[3] = {0, 0, 0};                                                                            \
+		for (int k = 0; k < D; ++k) vp[k] = (pp->position[k] - pp->position_old[k]) / ts;                    \
+		double fsum[3] = {0, 0, 0}, tsum[3] = {0, 0, 0};                                                     \
+		for (int64_t ix = a[0]; ix < b[0]; ++ix)                                                             \
+			for (int64_t iy = a[1]; iy < b[1]; ++iy)                                                         \
+				for (int64_t iz = (D == 3 ? a[2] : 0); iz < (D == 3 ? b[2] : 1); ++iz) {                     \
+					int64_t x = per ? ((ix % nx) + nx) % nx : ix;                                            \
+					int64_t c = x + nx * (iy + ny * iz);                                                     \
+					double r[3] = {rel_coord((double)x, pp->position[0], per, nx), (double)iy - pp->position[1], \
+								   D == 3 ? (double)iz - pp->position[2] : 0.0};                             \
+					double s2 = 0.0;                                                                         \
+					for (int k = 0; k < D; ++k) s2 = s2 + r[k] * r[k];                                       \
+					REALT por = (REALT)ramp(sqrt(s2), pp->radius, prm->eps);                                 \
+					if (por >= (REALT)1.0) continue;                                                         \
+					REALT mom[3] = {0, 0, 0};                                                                \
+					for (int i = 0; i < Q; ++i) {                                                            \
+						int e0 = ko_lattice_dir(h, i, 0), e1 = ko_lattice_dir(h, i, 1), e2 = ko_lattice_dir(h, i, 2); \
+						double upe_d = 0.0;                                                                  \
+						upe_d = upe_d + (double)e0 * vp[0];                                                  \
+						upe_d = upe_d + (double)e1 * vp[1];                                                  \
+						if (D == 3) upe_d = upe_d + (double)e2 * vp[2];                                      \
+						REALT upe = (REALT)upe_d;                                                            \
+						int64_t nx_ = x + e0, ny_ = iy + e1, nz_ = iz + e2;                                  \
+						if (per) nx_ = (nx_ + nx) % nx;                                                      \
+						REALT fi = POP(h, x, iy, iz, i);                                                     \
+						REALT fo = POP(h, nx_, ny_, nz_, ko_lattice_opp(h, i));                              \
+						REALT da = fi * ((REALT)1.0 - upe) + fo * ((REALT)1.0 + upe);                        \
+						mom[0] = mom[0] + (REALT)e0 * da;                                                    \
+						mom[1] = mom[1] + (REALT)e1 * da;                                                    \
+						if (D == 3) mom[2] = mom[2] + (REALT)e2 * da;                                        \
+					}                                                                                        \
+					double F[3] = {0, 0, 0};                                                                 \
+					for (int k = 0; k < D; ++k) F[k] = (double)mom[k];                                       \
+					if (cell_force)                                                                          \
+						for (int k = 0; k < D; ++k) cell_force[c * D + k] = F[k];                            \
+					for (int k = 0; k < D; ++k) fsum[k] = fsum[k] - F[k];                                    \
+					if (D == 2) {                                                                            \
+						tsum[0] = tsum[0] - (r[0] * F[1] - r[1] * F[0]);                                     \
+					} else {                                                                                 \
+						tsum[0] = tsum[0] - (r[1] * F[2] - r[2] * F[1]);                                     \
+						tsum[1] = tsum[1] - (r[2] * F[0] - r[0] * F[2]);                                     \
+						tsum[2] = tsum[2] - (r[0] * F[1] - r[1] * F[0]);                                     \
+					}                                                                                        \
+				}                                                                                            \
+		for (int k = 0; k < D; ++k) pp->force[k] = pp->force[k] + fsum[k];                                   \
+		for (int k = 0; k < (D == 2 ? 1 : 3); ++k) pp->torque[k] = pp->torque[k] + tsum[k];                  \
+	}
+
+void ko_particles_hlbm_gather(ko_lattice *h, kel_particle_state *P, int np, const kel_particle_params *prm,
+							  double *cell_force) {
+	int D, Q, f64, per;
+	int64_t nx, ny, nz;
+	ko_lattice_info(h, &D, &Q, &nx, &ny, &nz, &f64, &per);
+	int64_t ext[3] = {nx, ny, nz};
+	int steps = prm->sub_steps == 0 ? 1 : prm->sub_steps; /* hlbm.hpp:148-151 */
+	if (f64) {
+		KO_HLBM_GATHER_BODY(double, ko_lattice_pop)
+	} else {
+		KO_HLBM_GATHER_BODY(float, ko_lattice_pop_f32)
+	}
+}
+
+/* HlbmOneParticleStamp (hlbm.hpp:269-311), after the integrate: over each
+ * body's (post-move) AABB, in body order, D += 1 - por and N += u_p (1 - por)
+ * with u_p = (X - X_old) sub_steps and por the porosity field. */
+void ko_particles_hlbm_stamp(ko_lattice *h, const kel_particle_state *P, int np, const kel_particle_params *prm) {
+	int D, Q, f64, per;
+	int64_t nx, ny, nz;
+	ko_lattice_info(h, &D, &Q, &nx, &ny, &nz, &f64, &per);
+	int64_t ext[3] = {nx, ny, nz};
+	int steps = prm->sub_steps == 0 ? 1 : prm->sub_steps;
+	double ts = 1.0 / (double)steps;
+	for (int p = 0; p < np; ++p) {
+		int64_t a[3] = {0, 0, 0}, b[3] = {1, 1, 1};
+		aabb(D, &P[p], ext, per, 0, a, b);
+		double vp[3] = {0, 0, 0};
+		for (int k = 0; k < D; ++k) vp[k] = (P[p].position[k] - P[p].position_old[k]) / ts;
+		for (int64_t ix = a[0]; ix < b[0]; ++ix)
+			for (int64_t iy = a[1]; iy < b[1]; ++iy)
+				for (int64_t iz = (D == 3 ? a[2] : 0); iz < (D == 3 ? b[2] : 1); ++iz) {
+					int64_t x = per ? ((ix % nx) + nx) % nx : ix;
+					int64_t c = x + nx * (iy + ny * iz);
+					double flip;
+					double vf[3] = {0, 0, 0};
+					if (f64) {
+						flip = 1.0 - ko_lattice_porosity_at(h, c);
+						for (int k = 0; k < D; ++k) vf[k] = vp[k] * flip;
+					} else {
+						float fl = 1.0f - (float)ko_lattice_porosity_at(h, c);
+						flip = fl;
+						for (int k = 0; k < D; ++k) vf[k] = (double)((float)vp[k] * fl);
+					}
+					ko_lattice_hlbm_add_at(h, c, vf, flip);
+				}
+	}
+}
+
 /* reset_particle_accumulators, integrate.hpp:195-212 */
 void ko_particles_reset(kel_particle_state *P, int np) {
 	for (int p = 0; p < np; ++p)

@@ -526,6 +526,149 @@ struct ParticleCase {
 };
 
 /*
+ * HLBM coupling, one time step phase by phase, driving the reference's own
+ * components (hlbm.hpp): HlbmReset on every cell, ParticleForceReset,
+ * HlbmOneParticleGather, ParticleIntegrate and HlbmOneParticleStamp for every
+ * particle (each phase over all particles before the next), then the sweep
+ * of examples/moving_poiseulle_particles_2d_hlbm_gpu/sim.cpp:237-262
+ * (BounceBack on info 1, Hlbm collision on info 2) and the pull Stream.
+ * in_dir: pparams.txt (sub_steps gx gy tau), particles.f64 (8 per body as
+ *   ParticleCase), init.f64, flags.u8
+ * out_dir: porosity.f64, force_field.f64, after_gather.f64,
+ *   after_integrate.f64, hlbm_N.f64, hlbm_D.f64, dfs.f64 (t = 1), rho.f64,
+ *   vel.f64
+ */
+template <typename T, typename Desc, uint64_t NX, uint64_t NY, uint64_t NP>
+struct HlbmCase {
+	using Base = Case<T, Desc, NX, NY>;
+	using PC = ParticleCase<T, Desc, NX, NY, NP>;
+	using NT = typename native_data_type<T>::type;
+	static constexpr uint64_t D = 2, Q = Desc::Q, N = NX * NY;
+	using GroupSch = sch::ParticleGroup<T, D, NP, coll::Spheroid<T>>;
+	using Fields = sch::Struct<sch::Member<typename Base::InfoChunk, "info">,
+							   sch::Member<typename Base::DfChunk, "dfs">,
+							   sch::Member<typename Base::DfChunk, "dfs_old">,
+							   sch::Member<sch::Chunk<sch::Vector<T, D>, 0u, NX, NY>, "particle_N">,
+							   sch::Member<sch::Chunk<sch::Scalar<T>, 0u, NX, NY>, "particle_D">>;
+
+	static int run(const std::string &in, const std::string &out) {
+		std::ifstream pf(in + "/pparams.txt");
+		uint64_t sub_steps;
+		double gx, gy, tau;
+		pf >> sub_steps >> gx >> gy >> tau;
+		auto pv = read_file(in + "/particles.f64", true);
+		auto init = read_file(in + "/init.f64", true);
+		auto flags = read_file(in + "/flags.u8", true);
+		if (pv.size() != NP * 8 * 8 || init.size() != N * Q * 8 || flags.size() != N) return 5;
+		const double *P = reinterpret_cast<const double *>(pv.data());
+		const double *I = reinterpret_cast<const double *>(init.data());
+
+		auto fields_own = heap<data<Fields>>();
+		auto macros_own = heap<data<typename Base::MacroStruct>>();
+		data<sch::Ptr<Fields>> fields{*fields_own};
+		data<sch::Ptr<typename Base::MacroStruct>> macros{*macros_own};
+		auto &dfs_old_f = fields.template get<"dfs_old">();
+		auto &info_f = fields.template get<"info">();
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			info_f.at(idx).set(static_cast<uint8_t>(flags[c]));
+			for (uint64_t i = 0; i < Q; ++i) dfs_old_f.at(idx).at({i}).set(static_cast<NT>(I[c * Q + i]));
+			macros.template get<"density">().at(idx).at({}).set(NT(1));
+		}
+		data<sch::LbmMeter<sch::Scalar<T>>> r0;
+		r0.at({}).set(static_cast<NT>(P[6]));
+		data<sch::Scalar<T>> d0;
+		d0.at({}).set(static_cast<NT>(P[7]));
+		auto g = create_spheroid_particle_group<T, D, NP>(r0, d0, {4u});
+		auto &parts = g.template get<"particles">();
+		for (uint64_t p = 0; p < NP; ++p) {
+			const double *q = P + p * 8;
+			auto &pi = parts.at({p});
+			auto &rb = pi.template get<"rigid_body">();
+			rb.template get<"position">().at({{0u}}).set(static_cast<NT>(q[0]));
+			rb.template get<"position">().at({{1u}}).set(static_cast<NT>(q[1]));
+			rb.template get<"position_old">().at({{0u}}).set(static_cast<NT>(q[2]));
+			rb.template get<"position_old">().at({{1u}}).set(static_cast<NT>(q[3]));
+			rb.template get<"rotation">().at({}).set(static_cast<NT>(q[4]));
+			rb.template get<"rotation_old">().at({}).set(static_cast<NT>(q[5]));
+			constexpr NT pi_c = 3.14159265358979323846;
+			NT r = static_cast<NT>(q[6]), rho = static_cast<NT>(q[7]);
+			NT m = pi_c * r * r * rho;
+			pi.template get<"collision">().template get<"radius">().at({}).set(r);
+			rb.template get<"mass">().at({}).set(m);
+			rb.template get<"inertia">().at({}).set(NT(0.5) * m * r * r);
+			rb.template get<"density">().at({}).set(rho);
+		}
+		data<sch::Ptr<GroupSch>, enc::Native> view{g};
+
+		component<T, Desc, cmpt::HlbmReset> hreset;
+		component<T, Desc, cmpt::ParticleForceReset> reset;
+		component<T, Desc, cmpt::HlbmOneParticleGather> gather;
+		component<T, Desc, cmpt::HlbmOneParticleStamp> stamp;
+		data<sch::LbmAcceleration<sch::Vector<T, D>>> grav;
+		grav.at({{0u}}).set(static_cast<NT>(gx));
+		grav.at({{1u}}).set(static_cast<NT>(gy));
+		component<T, Desc, cmpt::ParticleIntegrate> integrate{grav};
+		data<sch::UInt64> t0{0u}, ss{sub_steps};
+
+		for (uint64_t c = 0; c < N; ++c) hreset.apply(fields, macros, Base::unflat(c), t0);
+		for (uint64_t p = 0; p < NP; ++p) reset.apply(view, {{p}}, t0);
+		for (uint64_t p = 0; p < NP; ++p) gather.apply(fields, macros, view, {{p}}, t0, ss);
+		PC::dump(out + "/after_gather.f64", g);
+		{
+			std::vector<double> por(N), ff(N * D);
+			for (uint64_t c = 0; c < N; ++c) {
+				auto idx = Base::unflat(c);
+				por[c] = macros.template get<"porosity">().at(idx).at({}).get();
+				for (uint64_t k = 0; k < D; ++k) ff[c * D + k] = macros.template get<"force">().at(idx).at({{k}}).get();
+			}
+			write_f64(out + "/porosity.f64", por);
+			write_f64(out + "/force_field.f64", ff);
+		}
+		for (uint64_t p = 0; p < NP; ++p) integrate.apply(view, {{p}}, t0, ss);
+		PC::dump(out + "/after_integrate.f64", g);
+		for (uint64_t p = 0; p < NP; ++p) stamp.apply(fields, macros, view, {{p}}, t0, ss);
+		{
+			std::vector<double> hn(N * D), hd(N);
+			for (uint64_t c = 0; c < N; ++c) {
+				auto idx = Base::unflat(c);
+				hd[c] = fields.template get<"particle_D">().at(idx).at({}).get();
+				for (uint64_t k = 0; k < D; ++k) hn[c * D + k] = fields.template get<"particle_N">().at(idx).at({{k}}).get();
+			}
+			write_f64(out + "/hlbm_N.f64", hn);
+			write_f64(out + "/hlbm_D.f64", hd);
+		}
+		component<T, Desc, cmpt::Hlbm> collision{static_cast<NT>(tau)};
+		component<T, Desc, cmpt::BounceBack> bb;
+		component<T, Desc, cmpt::Stream> stream;
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			switch (info_f.at(idx).get()) {
+			case 1u: bb.apply(fields, idx, t0); break;
+			case 2u: collision.apply(fields, macros, idx, t0); break;
+			default: break;
+			}
+		}
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			if (info_f.at(idx).get() > 0u) stream.apply(fields, idx, t0);
+		}
+		auto &final_f = fields.template get<"dfs">();
+		std::vector<double> dfs(N * Q), rho(N), vel(N * D);
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			for (uint64_t i = 0; i < Q; ++i) dfs[c * Q + i] = static_cast<double>(final_f.at(idx).at({i}).get());
+			rho[c] = static_cast<double>(macros.template get<"density">().at(idx).at({}).get());
+			for (uint64_t d = 0; d < D; ++d) vel[c * D + d] = static_cast<double>(macros.template get<"velocity">().at(idx).at({{d}}).get());
+		}
+		write_f64(out + "/dfs.f64", dfs);
+		write_f64(out + "/rho.f64", rho);
+		write_f64(out + "/vel.f64", vel);
+		return 0;
+	}
+};
+
+/*
  * Field writers of the reference on given values: write_vtk_file /
  * write_csv_file (modules/core/c++/write_vtk.hpp, write_csv.hpp) of the
  * drivers' MacroStruct {velocity, density} and of the lattice struct {info,
@@ -603,6 +746,8 @@ int main(int argc, char **argv) {
 	if (c == "particles_d2q9_f64_64x48x5") return ParticleCase<F64, sch::D2Q9, 64, 48, 5>::run(argv[2], argv[3]);
 	if (c == "particles_d2q9_f32_64x48x5") return ParticleCase<F32, sch::D2Q9, 64, 48, 5>::run(argv[2], argv[3]);
 	if (c == "d3q27_f64_16x12x10") return Case<F64, sch::D3Q27, 16, 12, 10>::run(argv[2], argv[3]);
+	if (c == "hlbm_d2q9_f64_48x40x3") return HlbmCase<F64, sch::D2Q9, 48, 40, 3>::run(argv[2], argv[3]);
+	if (c == "hlbm_d2q9_f32_48x40x3") return HlbmCase<F32, sch::D2Q9, 48, 40, 3>::run(argv[2], argv[3]);
 	if (c == "writers_d2q9_f32_12x7") return WriterCase<F32, sch::D2Q9, 12, 7>::run(argv[2], argv[3]);
 	if (c == "writers_d3q19_f64_5x4x3") return WriterCase<F64, sch::D3Q19, 5, 4, 3>::run(argv[2], argv[3]);
 	std::fprintf(stderr, "unknown case %s\n", c.c_str());

@@ -158,6 +158,49 @@ def run_particle_harness(hcase, bodies, init, workdir):
     return out
 
 
+HLBM_DIMS = (48, 40)
+HLBM_PARAMS = dict(sub_steps=2, gravity=(0.0, -1e-4), tau=0.8)
+HLBM_CASES = {"hlbm_d2q9_f64_48x40x3": np.float64, "hlbm_d2q9_f32_48x40x3": np.float32}
+
+
+def hlbm_inputs(seed=31):
+    """Three moving discs in a walled 48x40 box (rim flag 1, fluid 2), two of
+    them with overlapping AABBs (the last body's porosity wins there), and
+    near-equilibrium populations."""
+    rng = np.random.default_rng(cases.SEED + seed)
+    xy = [(14.3, 13.6, 5.0), (22.8, 15.1, 4.5), (33.4, 27.2, 6.0)]
+    bodies = []
+    for (x, y, r) in xy:
+        vx, vy = 0.02 * rng.standard_normal(2)
+        rot = 0.05 * rng.standard_normal()
+        bodies.append([x, y, x - vx, y - vy, rot, rot - 0.002 * rng.standard_normal(), r, 1.5])
+    bodies = np.array(bodies, dtype=np.float64)
+    nx, ny = HLBM_DIMS
+    x, y, _ = cases.cell_grid(HLBM_DIMS)
+    flags = np.full(nx * ny, 2, np.uint8)
+    flags[(x == 0) | (x == nx - 1) | (y == 0) | (y == ny - 1)] = 1
+    init = cases.random_populations(9, nx * ny, rng, amp=0.05).astype(np.float32).astype(np.float64)
+    return bodies, init, flags
+
+
+def run_hlbm_harness(hcase, bodies, init, flags, workdir):
+    ind, outd = os.path.join(workdir, "in"), os.path.join(workdir, "out")
+    os.makedirs(ind, exist_ok=True)
+    os.makedirs(outd, exist_ok=True)
+    P = HLBM_PARAMS
+    open(os.path.join(ind, "pparams.txt"), "w").write(
+        f"{P['sub_steps']} {P['gravity'][0]!r} {P['gravity'][1]!r} {P['tau']!r}\n")
+    bodies.astype(np.float64).tofile(os.path.join(ind, "particles.f64"))
+    init.astype(np.float64).tofile(os.path.join(ind, "init.f64"))
+    flags.astype(np.uint8).tofile(os.path.join(ind, "flags.u8"))
+    subprocess.check_call([HARNESS, hcase, ind, outd])
+    out = {}
+    for k in ("porosity", "force_field", "after_gather", "after_integrate", "hlbm_N", "hlbm_D", "dfs", "rho", "vel"):
+        a = np.fromfile(os.path.join(outd, k + ".f64"))
+        out[k] = a.reshape(-1, 28) if k.startswith("after") else a
+    return out
+
+
 def particle_registry():
     return {
         "particles_gather_f64": ("particles_d2q9_f64_64x48x5", "gather"),
@@ -173,7 +216,7 @@ def load_particles(name):
 
 def names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and not f.startswith(("particles_", "writers_", "cavity256_")))
+                  if f.endswith(".npz") and not f.startswith(("particles_", "writers_", "cavity256_", "hlbm_")))
 
 
 WRITER_CASES = {"writers_d2q9_f32_12x7": (9, (12, 7), np.float32),
@@ -226,6 +269,15 @@ def main():
         np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), bodies=bodies, init=init.astype(np.float32),
                             params=np.array(json.dumps(PART_PARAMS)), **out)
         print(f"{name:28s} particles: force after gather {out['after_gather'][:, 18:20].ravel()[:4]}")
+    for name in HLBM_CASES:
+        if args.only and args.only not in name:
+            continue
+        bodies, init, flags = hlbm_inputs()
+        with tempfile.TemporaryDirectory() as td:
+            out = run_hlbm_harness(name, bodies, init, flags, td)
+        np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), bodies=bodies, init=init, flags=flags,
+                            params=np.array(json.dumps(HLBM_PARAMS)), **out)
+        print(f"{name:28s} hlbm: body force after gather {out['after_gather'][:, 18:20].ravel()[:4]}")
     for name, (q, dims, dtype) in WRITER_CASES.items():
         if args.only and args.only not in name:
             continue
