@@ -131,6 +131,7 @@ struct BGK {};
 struct BGKGuo {};
 struct Psm {};
 struct PsmGuo {};
+struct Hlbm {};
 struct BounceBack {};
 template <uint64_t I>
 struct AntiBounceBack {};
@@ -181,6 +182,20 @@ public:
 	explicit component(double relaxation__) : relaxation{relaxation__} {}
 	void lower(kel_step_program &p) const {
 		p.collision = KEL_COLL_PSM;
+		p.tau = relaxation;
+	}
+};
+
+// cmpt::Hlbm (hlbm.hpp:53-101), D2Q9: the collision of the HLBM coupling;
+// the per-cell porosity / particle_N / particle_D it reads come from
+// kel_particles_* with KEL_COUPLING_HLBM.
+template <typename T, typename Desc>
+class component<T, Desc, cmpt::Hlbm> {
+public:
+	double relaxation;
+	explicit component(double relaxation__) : relaxation{relaxation__} {}
+	void lower(kel_step_program &p) const {
+		p.collision = KEL_COLL_HLBM;
 		p.tau = relaxation;
 	}
 };

@@ -114,6 +114,8 @@ typedef struct kel_lattice kel_lattice;
 /* Field selectors. */
 #define KEL_FIELD_POROSITY 1 /* macros "porosity" (psm.hpp:20-32), 1 fluid .. 0 solid */
 #define KEL_FIELD_FORCE 2    /* macros "force" per cell, D values (collision.hpp:148-151) */
+#define KEL_FIELD_HLBM_N 3   /* HLBM "particle_N" per cell, D values (hlbm.hpp:37-46) */
+#define KEL_FIELD_HLBM_D 4   /* HLBM "particle_D" per cell */
 
 /* Replaces data<ChunkStruct, encode::Sycl<>> construction + malloc_device
  * (modules/sycl/c++/data.hpp:23-61).  Initial state: every cell flag 0,
@@ -179,8 +181,14 @@ typedef struct kel_particle_params {
 	double k_n, zeta_n, gamma_t, mu; /* dem_params (particle/contact.hpp:36-61) */
 	double body_acceleration[3];     /* ParticleIntegrate(g) (particle/integrate.hpp:263-296) */
 	uint32_t wall_axes;    /* DEM box walls at 0 and the extent on these axes (bit a = axis a) */
-	uint32_t reserved;
+	int32_t coupling;      /* KEL_COUPLING_PSM (0) or KEL_COUPLING_HLBM (D2Q9) */
 } kel_particle_params;
+#define KEL_COUPLING_PSM 0
+/* HLBM (hlbm.hpp): couple = HlbmReset + the gathers' porosity (last body
+ * wins), gather = momentum exchange without solid weight, stamp = the
+ * particle_N / particle_D accumulators after the integrate, and the lattice
+ * steps with KEL_COLL_HLBM. */
+#define KEL_COUPLING_HLBM 1
 
 typedef struct kel_particles kel_particles;
 
@@ -205,8 +213,13 @@ int kel_particles_gather(kel_particles *ps, const kel_particle_params *prm, floa
 int kel_particles_contact(kel_particles *ps, const kel_particle_params *prm);
 /* ParticleIntegrate (particle/integrate.hpp:45-83,263-296): position Verlet. */
 int kel_particles_integrate(kel_particles *ps, const kel_particle_params *prm);
+/* HLBM only: HlbmOneParticleStamp of every body (after the integrate). */
+int kel_particles_stamp(kel_particles *ps, const kel_particle_params *prm);
 /* One coupled time step, n times: reset, couple, gather, contact, integrate,
- * then the sweep (examples/moving_poiseulle_particles_2d_psm_gpu/sim.cpp:176-260). */
+ * (HLBM: stamp,) then the sweep
+ * (examples/moving_poiseulle_particles_2d_psm_gpu/sim.cpp:176-260,
+ * examples/moving_poiseulle_particles_2d_hlbm_gpu/sim.cpp:195-262).  With
+ * HLBM coupling the program's collision must be KEL_COLL_HLBM. */
 int kel_particles_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
 					   uint64_t n_steps, uint32_t step_flags);
 

@@ -45,7 +45,7 @@ KEL_MAX_FLAGS = 8
 
 KEL_DTYPE_F32, KEL_DTYPE_F64 = 0, 1
 KEL_LAYOUT_AOS, KEL_LAYOUT_SOA = 0, 1
-KEL_FIELD_POROSITY, KEL_FIELD_FORCE = 1, 2
+KEL_FIELD_POROSITY, KEL_FIELD_FORCE, KEL_FIELD_HLBM_N, KEL_FIELD_HLBM_D = 1, 2, 3, 4
 KEL_STEP_WRITE_MACROS, KEL_STEP_ALL_MACROS = 1, 2
 KEL_UNET_CONV_TCGEN05, KEL_UNET_CONV_MMA_SYNC = 0, 1
 KEL_VALUE_U8, KEL_VALUE_F32, KEL_VALUE_F64 = 0, 1, 2
@@ -132,6 +132,7 @@ def program_from_dict(d):
 
 
 KEL_POROSITY_RAMP, KEL_POROSITY_SUBCELL = 0, 1
+KEL_COUPLING_PSM, KEL_COUPLING_HLBM = 0, 1
 
 
 class ParticleState(C.Structure):
@@ -163,13 +164,14 @@ class ParticleParams(C.Structure):
         ("mu", C.c_double),
         ("body_acceleration", C.c_double * 3),
         ("wall_axes", C.c_uint32),
-        ("reserved", C.c_uint32),
+        ("coupling", C.c_int32),
     ]
 
 
 def make_particle_params(porosity_mode=KEL_POROSITY_RAMP, sub_steps=1, eps=1.5, k_n=1.0, zeta_n=0.3, gamma_t=0.0,
-                         mu=0.0, body_acceleration=(0.0, 0.0, 0.0), wall_axes=0):
+                         mu=0.0, body_acceleration=(0.0, 0.0, 0.0), wall_axes=0, coupling=KEL_COUPLING_PSM):
     p = ParticleParams()
+    p.coupling = coupling
     p.porosity_mode, p.sub_steps, p.eps = porosity_mode, sub_steps, eps
     p.k_n, p.zeta_n, p.gamma_t, p.mu = k_n, zeta_n, gamma_t, mu
     for k in range(3):
@@ -274,6 +276,7 @@ def load_library(path: str | None = None):
         "kel_lattice_write_fields": ([vp, i32, C.c_char_p, C.c_char_p, u64], C.c_int),
         "kel_lattice_save": ([vp, C.c_char_p], C.c_int),
         "kel_lattice_load": ([vp, C.c_char_p], C.c_int),
+        "kel_particles_stamp": ([vp, C.POINTER(ParticleParams)], C.c_int),
         "kel_lattice_get_launch": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "kel_lattice_autotune": ([vp, C.POINTER(StepProgram), i32, C.POINTER(i32), C.POINTER(i32),
                                   C.POINTER(C.c_float)], C.c_int),

@@ -198,6 +198,8 @@ extern "C" int kel_lattice_destroy(kel_lattice *L) {
 	cudaFree(L->u);
 	cudaFree(L->por);
 	cudaFree(L->force);
+	cudaFree(L->hN);
+	cudaFree(L->hD);
 	cudaFree(L->profile);
 	cudaFree(L->ops);
 	cudaFree(L->staging);
@@ -498,6 +500,14 @@ extern "C" int kel_upload_field(kel_lattice *L, int32_t field, const float *host
 		if ((rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
 		return field_io(L, L->force, nullptr, host, L->d.D);
 	}
+	if (field == KEL_FIELD_HLBM_N) {
+		if ((rc = ensure_field(L, &L->hN, L->plane * L->d.D, 0.0f))) return rc;
+		return field_io(L, L->hN, nullptr, host, L->d.D);
+	}
+	if (field == KEL_FIELD_HLBM_D) {
+		if ((rc = ensure_field(L, &L->hD, L->plane, 0.0f))) return rc;
+		return field_io(L, L->hD, nullptr, host, 1);
+	}
 	return fail(KEL_ERR_INVALID_ARGUMENT, "kel_upload_field: unknown field %d", field);
 }
 
@@ -511,6 +521,14 @@ extern "C" int kel_download_field(kel_lattice *L, int32_t field, float *host) {
 	if (field == KEL_FIELD_FORCE) {
 		if ((rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
 		return field_io(L, L->force, host, nullptr, L->d.D);
+	}
+	if (field == KEL_FIELD_HLBM_N) {
+		if ((rc = ensure_field(L, &L->hN, L->plane * L->d.D, 0.0f))) return rc;
+		return field_io(L, L->hN, host, nullptr, L->d.D);
+	}
+	if (field == KEL_FIELD_HLBM_D) {
+		if ((rc = ensure_field(L, &L->hD, L->plane, 0.0f))) return rc;
+		return field_io(L, L->hD, host, nullptr, 1);
 	}
 	return fail(KEL_ERR_INVALID_ARGUMENT, "kel_download_field: unknown field %d", field);
 }
@@ -531,8 +549,10 @@ extern "C" int kel_upload_inlet_profile(kel_lattice *L, const double *host_ux, i
 
 static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops) {
 	const HostDesc &d = L->d;
-	if (P->collision < KEL_COLL_BGK || P->collision > KEL_COLL_PSM_GUO)
+	if (P->collision < KEL_COLL_BGK || P->collision > KEL_COLL_HLBM)
 		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown collision %d", P->collision);
+	if (P->collision == KEL_COLL_HLBM && d.Q != 9)
+		return fail(KEL_ERR_UNSUPPORTED, "kel_step: the HLBM collision is D2Q9 only");
 	if (P->arithmetic == KEL_ARITH_SHIFTED)
 		return fail(KEL_ERR_UNSUPPORTED, "kel_step: shifted arithmetic is implemented for batches only");
 	if (P->arithmetic != KEL_ARITH_FAST && P->arithmetic != KEL_ARITH_REFERENCE)
@@ -606,6 +626,21 @@ extern "C" int kel_lattice_get_launch(const kel_lattice *L, int32_t *cells_per_t
 	return KEL_OK;
 }
 
+// The per-cell fields a collision reads, allocated on first use: porosity
+// (1 = fluid), force (0), and for HLBM particle_N / particle_D (0).
+static int ensure_collision_fields(kel_lattice *L, int coll) {
+	int rc;
+	const bool por = coll == KEL_COLL_PSM || coll == KEL_COLL_PSM_GUO || coll == KEL_COLL_HLBM;
+	const bool guo = coll == KEL_COLL_BGK_GUO || coll == KEL_COLL_PSM_GUO;
+	if (por && (rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
+	if (guo && (rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
+	if (coll == KEL_COLL_HLBM) {
+		if ((rc = ensure_field(L, &L->hN, L->plane * L->d.D, 0.0f))) return rc;
+		if ((rc = ensure_field(L, &L->hD, L->plane, 0.0f))) return rc;
+	}
+	return KEL_OK;
+}
+
 static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	SweepParams p;
 	memset(&p, 0, sizeof(p));
@@ -616,6 +651,8 @@ static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	p.u = L->u;
 	p.por = L->por;
 	p.force = L->force;
+	p.hN = L->hN;
+	p.hD = L->hD;
 	p.profile = L->profile;
 	p.ops = L->ops;
 	p.nxp = L->nxp;
@@ -643,10 +680,7 @@ extern "C" int kel_lattice_autotune(kel_lattice *L, const kel_step_program *P, i
 	if (!L || !P || steps < 2) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_autotune: bad arguments");
 	int rc;
 	if ((rc = kel_step(L, P, 0, 0))) return rc; // validates and uploads the program
-	const bool psm = P->collision == KEL_COLL_PSM || P->collision == KEL_COLL_PSM_GUO;
-	const bool guo = P->collision == KEL_COLL_BGK_GUO || P->collision == KEL_COLL_PSM_GUO;
-	if (psm && (rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
-	if (guo && (rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
+	if ((rc = ensure_collision_fields(L, P->collision))) return rc;
 	const size_t bytes = (size_t)L->d.Q * L->plane * L->elem;
 	void *save = nullptr;
 	KEL_CUDA(cudaMalloc(&save, bytes));
@@ -707,10 +741,7 @@ extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_st
 		L->last_prog = *P;
 		L->have_ops = true;
 	}
-	const bool psm = P->collision == KEL_COLL_PSM || P->collision == KEL_COLL_PSM_GUO;
-	const bool guo = P->collision == KEL_COLL_BGK_GUO || P->collision == KEL_COLL_PSM_GUO;
-	if (psm && (rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
-	if (guo && (rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
+	if ((rc = ensure_collision_fields(L, P->collision))) return rc;
 
 	SweepParams p = make_params(L, P);
 	const bool exact = P->arithmetic == KEL_ARITH_REFERENCE;

@@ -48,6 +48,7 @@ struct kel_lattice {
 	void *f = nullptr;
 	uint8_t *flags = nullptr;
 	float *rho = nullptr, *u = nullptr, *por = nullptr, *force = nullptr, *profile = nullptr;
+	float *hN = nullptr, *hD = nullptr; // HLBM particle_N (D planes) and particle_D, on first use
 	kel::gb::OpEntry *ops = nullptr;
 	void *staging = nullptr;
 	size_t staging_bytes = 0;

@@ -49,6 +49,7 @@ struct PView {
 	int odd, periodic;
 	float *por;
 	float *cell_force;
+	float *hN, *hD; // HLBM particle_N (D planes) and particle_D
 	float wshift[27];
 };
 
@@ -208,8 +209,13 @@ __device__ inline float pop_post(const PView &v, int x, int y, int z, int i) {
 
 constexpr int GT = 256;
 
-template <class L, int STORE>
-__global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, int steps, int mode) {
+// PSM (HLBM false): psm.hpp:101-446, the porosity field the couple pass
+// wrote, cell force = momentum x (1 - porosity).  HLBM: hlbm.hpp:119-260,
+// the body's own ramp porosity (eps) decides which cells count and the cell
+// momentum enters unweighted; the cell force field is written by the HLBM
+// couple pass instead (the last body wins there).
+template <class L, int STORE, bool HLBM>
+__global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, int steps, int mode, double eps) {
 	constexpr int D = L::D;
 	__shared__ double part[GT / 32][6];
 	kel_particle_state &p = P[blockIdx.x];
@@ -228,7 +234,16 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, i
 		const int iz = D == 3 ? (int)(a[2] + k / (ex * ey)) : 0;
 		const int x = v.periodic ? ((ix % v.nx) + v.nx) % v.nx : ix;
 		const int64_t pc = ((int64_t)iz * v.ny + iy) * v.nxp + x;
-		const float por = v.por[pc];
+		const double r[3] = {rel_coord((double)x, p.position[0], v.periodic, v.nx), (double)iy - p.position[1],
+							 D == 3 ? (double)iz - p.position[2] : 0.0};
+		float por;
+		if (HLBM) {
+			double s2 = 0.0;
+			for (int d = 0; d < D; ++d) s2 = s2 + r[d] * r[d];
+			por = (float)ramp(sqrt(s2), p.radius, eps);
+		} else {
+			por = v.por[pc];
+		}
 		if (por >= 1.0f) continue;
 		float mom[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -247,12 +262,10 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, i
 		}
 		const float flip = __fsub_rn(1.0f, por);
 		double F[3] = {0.0, 0.0, 0.0};
-		for (int d = 0; d < D; ++d) F[d] = (double)__fmul_rn(mom[d], flip);
-		if (v.cell_force)
+		for (int d = 0; d < D; ++d) F[d] = HLBM ? (double)mom[d] : (double)__fmul_rn(mom[d], flip);
+		if (!HLBM && v.cell_force)
 			for (int d = 0; d < D; ++d) v.cell_force[(int64_t)d * v.plane + pc] = (float)F[d];
 		for (int d = 0; d < D; ++d) acc[d] -= F[d];
-		const double r[3] = {rel_coord((double)x, p.position[0], v.periodic, v.nx), (double)iy - p.position[1],
-							 D == 3 ? (double)iz - p.position[2] : 0.0};
 		if (D == 2) {
 			acc[3] -= r[0] * F[1] - r[1] * F[0];
 		} else {
@@ -276,6 +289,145 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, i
 		for (int d = 0; d < D; ++d) p.force[d] = p.force[d] + tot[d];
 		for (int d = 0; d < (D == 2 ? 1 : 3); ++d) p.torque[d] = p.torque[d] + tot[3 + d];
 	}
+}
+
+// ---- HLBM per-cell passes ----------------------------------------------------------
+
+// Indices (ascending) of the bodies among [c0, c0 + TT) whose AABB touches
+// this tile, into cand[0 .. *ncand); every thread of the block calls it.
+__device__ inline void cull_tile(const PView &v, const kel_particle_state *P, int np, int c0, int x0, int y0, int z,
+								 int *cand, int *warp_count, int *ncand) {
+	const int tid = threadIdx.y * TX + threadIdx.x;
+	bool hit = false;
+	const int pi = c0 + tid;
+	if (pi < np) {
+		int64_t a[3], b[3];
+		body_aabb(v.D, P[pi], v.nx, v.ny, v.nz, v.periodic, 0, a, b);
+		const bool yz = a[1] < y0 + TY && b[1] > y0 && (v.D == 2 || (a[2] <= z && b[2] > z));
+		bool xs = a[0] < x0 + TX && b[0] > x0;
+		if (v.periodic)
+			xs = xs || (a[0] < x0 + TX - v.nx && b[0] > x0 - v.nx) || (a[0] < x0 + TX + v.nx && b[0] > x0 + v.nx);
+		hit = yz && xs;
+	}
+	const unsigned m = __ballot_sync(0xffffffffu, hit);
+	if ((tid & 31) == 0) warp_count[tid >> 5] = __popc(m);
+	__syncthreads();
+	if (tid == 0) {
+		int s = 0;
+		for (int w = 0; w < TT / 32; ++w) {
+			const int c = warp_count[w];
+			warp_count[w] = s;
+			s += c;
+		}
+		*ncand = s;
+	}
+	__syncthreads();
+	if (hit) cand[warp_count[tid >> 5] + __popc(m & ((1u << (tid & 31)) - 1u))] = pi;
+	__syncthreads();
+}
+
+// Does body p's AABB hold cell (x, y, z)?  Returns its offset r from the body.
+__device__ inline bool in_aabb(const PView &v, const kel_particle_state &p, int x, int y, int z, double *r) {
+	int64_t a[3], b[3];
+	body_aabb(v.D, p, v.nx, v.ny, v.nz, v.periodic, 0, a, b);
+	r[0] = rel_coord((double)x, p.position[0], v.periodic, v.nx);
+	r[1] = (double)y - p.position[1];
+	r[2] = v.D == 3 ? (double)z - p.position[2] : 0.0;
+	const int64_t xc = v.periodic ? (int64_t)llround(p.position[0] + r[0]) : x;
+	return !(xc < a[0] || xc >= b[0] || y < a[1] || y >= b[1] || (v.D == 3 && (z < a[2] || z >= b[2])));
+}
+
+// HlbmReset (hlbm.hpp:27-47) and the porosity of the HLBM gathers
+// (hlbm.hpp:178-186): per cell the ramp of the last body (index order) whose
+// AABB holds it; with a cell-force buffer, that body's momentum exchange
+// (pre-move velocity) where its porosity is below 1, as the last gather
+// writing the cell leaves it.
+template <int STORE>
+__global__ void __launch_bounds__(TT) k_hlbm_couple(PView v, const kel_particle_state *P, int np, double eps,
+													int steps) {
+	__shared__ int cand[TT];
+	__shared__ int warp_count[TT / 32];
+	__shared__ int ncand;
+	const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z = blockIdx.z;
+	const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+	double por = 1.0;
+	int owner = -1; // last body whose gather counts this cell (its porosity below 1)
+	for (int c0 = 0; c0 < np; c0 += TT) {
+		cull_tile(v, P, np, c0, x0, y0, z, cand, warp_count, &ncand);
+		if (x < v.nx && y < v.ny)
+			for (int k = 0; k < ncand; ++k) {
+				double r[3];
+				if (!in_aabb(v, P[cand[k]], x, y, z, r)) continue;
+				double s2 = 0.0;
+				for (int d = 0; d < v.D; ++d) s2 = s2 + r[d] * r[d];
+				por = ramp(sqrt(s2), P[cand[k]].radius, eps);
+				if ((float)por < 1.0f) owner = cand[k];
+			}
+		__syncthreads();
+	}
+	if (x >= v.nx || y >= v.ny) return;
+	const int64_t pc = ((int64_t)z * v.ny + y) * v.nxp + x;
+	v.por[pc] = (float)por;
+	v.hD[pc] = 0.f;
+	for (int d = 0; d < v.D; ++d) v.hN[(int64_t)d * v.plane + pc] = 0.f;
+	if (!v.cell_force) return;
+	float mom[2] = {0.f, 0.f};
+	if (owner >= 0) {
+		const kel_particle_state &p = P[owner];
+		const double ts = 1.0 / (double)steps;
+		double vp[2];
+		for (int k = 0; k < 2; ++k) vp[k] = (p.position[k] - p.position_old[k]) / ts;
+#pragma unroll
+		for (int i = 1; i < 9; ++i) {
+			double upe_d = 0.0;
+			upe_d = upe_d + (double)D2Q9::cx(i) * vp[0];
+			upe_d = upe_d + (double)D2Q9::cy(i) * vp[1];
+			const float upe = (float)upe_d;
+			const float fi = pop_post<D2Q9, STORE>(v, x, y, z, i);
+			const float fo = pop_post<D2Q9, STORE>(v, x + D2Q9::cx(i), y + D2Q9::cy(i), z, D2Q9::opp(i));
+			const float da = __fadd_rn(__fmul_rn(fi, __fsub_rn(1.0f, upe)), __fmul_rn(fo, __fadd_rn(1.0f, upe)));
+			mom[0] = __fadd_rn(mom[0], __fmul_rn((float)D2Q9::cx(i), da));
+			mom[1] = __fadd_rn(mom[1], __fmul_rn((float)D2Q9::cy(i), da));
+		}
+	}
+	for (int d = 0; d < 2; ++d) v.cell_force[(int64_t)d * v.plane + pc] = mom[d];
+}
+
+// HlbmOneParticleStamp (hlbm.hpp:269-311) of every body, after the
+// integrate: per cell, over the bodies (index order) whose post-move AABB
+// holds it, D += 1 - por and N += u_p (1 - por), u_p = (X - X_old) sub_steps.
+__global__ void __launch_bounds__(TT) k_hlbm_stamp(PView v, const kel_particle_state *P, int np, int steps) {
+	__shared__ int cand[TT];
+	__shared__ int warp_count[TT / 32];
+	__shared__ int ncand;
+	const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z = blockIdx.z;
+	const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+	const bool inside = x < v.nx && y < v.ny;
+	const int64_t pc = ((int64_t)z * v.ny + y) * v.nxp + x;
+	const float flip = inside ? __fsub_rn(1.0f, v.por[pc]) : 0.f;
+	float Dv = inside ? v.hD[pc] : 0.f;
+	float N[3] = {0.f, 0.f, 0.f};
+	if (inside)
+		for (int d = 0; d < v.D; ++d) N[d] = v.hN[(int64_t)d * v.plane + pc];
+	const double ts = 1.0 / (double)steps;
+	for (int c0 = 0; c0 < np; c0 += TT) {
+		cull_tile(v, P, np, c0, x0, y0, z, cand, warp_count, &ncand);
+		if (inside)
+			for (int k = 0; k < ncand; ++k) {
+				const kel_particle_state &p = P[cand[k]];
+				double r[3];
+				if (!in_aabb(v, p, x, y, z, r)) continue;
+				Dv = __fadd_rn(Dv, flip);
+				for (int d = 0; d < v.D; ++d) {
+					const float up = (float)((p.position[d] - p.position_old[d]) / ts);
+					N[d] = __fadd_rn(N[d], __fmul_rn(up, flip));
+				}
+			}
+		__syncthreads();
+	}
+	if (!inside) return;
+	v.hD[pc] = Dv;
+	for (int d = 0; d < v.D; ++d) v.hN[(int64_t)d * v.plane + pc] = N[d];
 }
 
 // ---- DEM contact (contact.hpp) ----------------------------------------------------
@@ -522,6 +674,8 @@ PView make_view(kel_lattice *L) {
 	v.odd = (int)(L->t & 1u);
 	v.periodic = (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0;
 	v.por = L->por;
+	v.hN = L->hN;
+	v.hD = L->hD;
 	for (int i = 0; i < 27; ++i) v.wshift[i] = L->wshift[i];
 	return v;
 }
@@ -531,8 +685,16 @@ int check_params(const kel_particles *ps, const kel_particle_params *prm, const 
 	if (prm->porosity_mode != KEL_POROSITY_RAMP && prm->porosity_mode != KEL_POROSITY_SUBCELL)
 		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: unknown porosity mode %d", who, prm->porosity_mode);
 	if (prm->sub_steps < 0) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: negative sub_steps", who);
-	if (prm->porosity_mode == KEL_POROSITY_RAMP && !(prm->eps > 0))
+	if ((prm->porosity_mode == KEL_POROSITY_RAMP || prm->coupling == KEL_COUPLING_HLBM) && !(prm->eps > 0))
 		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: eps must be positive", who);
+	if (prm->coupling != KEL_COUPLING_PSM && prm->coupling != KEL_COUPLING_HLBM)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: unknown coupling %d", who, prm->coupling);
+	if (prm->coupling == KEL_COUPLING_HLBM) {
+		if (ps->lat->d.Q != 9) return fail(KEL_ERR_UNSUPPORTED, "%s: HLBM coupling is D2Q9 only", who);
+		int rc;
+		if ((rc = ensure_field(ps->lat, &ps->lat->hN, ps->lat->plane * ps->lat->d.D, 0.0f))) return rc;
+		if ((rc = ensure_field(ps->lat, &ps->lat->hD, ps->lat->plane, 0.0f))) return rc;
+	}
 	return KEL_OK;
 }
 
@@ -593,23 +755,64 @@ static int particles_reset(kel_particles *ps) {
 	return KEL_OK;
 }
 
-static int particles_couple(kel_particles *ps, const kel_particle_params *prm) {
+static dim3 cell_grid(const kel_lattice *L) {
+	return dim3((unsigned)((L->desc.nx + TX - 1) / TX), (unsigned)((L->desc.ny + TY - 1) / TY), (unsigned)L->desc.nz);
+}
+
+static int hlbm_steps(const kel_particle_params *prm) { return prm->sub_steps == 0 ? 1 : prm->sub_steps; }
+
+// HLBM: porosity, reset of N / D and (with a buffer) the cell force field
+static int particles_hlbm_couple(kel_particles *ps, const kel_particle_params *prm, bool want_cell_force) {
 	kel_lattice *L = ps->lat;
 	PView v = make_view(L);
-	dim3 grid((unsigned)((L->desc.nx + TX - 1) / TX), (unsigned)((L->desc.ny + TY - 1) / TY), (unsigned)L->desc.nz);
-	k_couple<<<grid, dim3(TX, TY), 0, L->stream>>>(v, ps->d, ps->n, prm->porosity_mode, prm->eps);
+	if (want_cell_force) {
+		if (!ps->cell_force) KEL_CUDA(cudaMalloc(&ps->cell_force, sizeof(float) * L->plane * L->d.D));
+		v.cell_force = ps->cell_force;
+	}
+	if (L->desc.storage == KEL_STORAGE_FP32)
+		k_hlbm_couple<STORE_FP32><<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, ps->n, prm->eps,
+																				 hlbm_steps(prm));
+	else
+		k_hlbm_couple<STORE_FP16S><<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, ps->n, prm->eps,
+																				  hlbm_steps(prm));
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+static int particles_couple(kel_particles *ps, const kel_particle_params *prm) {
+	kel_lattice *L = ps->lat;
+	if (prm->coupling == KEL_COUPLING_HLBM) return particles_hlbm_couple(ps, prm, false);
+	PView v = make_view(L);
+	k_couple<<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, ps->n, prm->porosity_mode, prm->eps);
+	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+static int particles_stamp(kel_particles *ps, const kel_particle_params *prm) {
+	kel_lattice *L = ps->lat;
+	k_hlbm_stamp<<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(make_view(L), ps->d, ps->n, hlbm_steps(prm));
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
 
 template <class Lc, int STORE>
 static void launch_gather(const PView &v, kel_particles *ps, int steps, int mode) {
-	k_gather<Lc, STORE><<<ps->n, GT, 0, ps->lat->stream>>>(v, ps->d, steps, mode);
+	k_gather<Lc, STORE, false><<<ps->n, GT, 0, ps->lat->stream>>>(v, ps->d, steps, mode, 1.5);
 }
 
 static int particles_gather(kel_particles *ps, const kel_particle_params *prm, bool want_cell_force) {
 	kel_lattice *L = ps->lat;
 	PView v = make_view(L);
+	if (prm->coupling == KEL_COUPLING_HLBM) { // D2Q9 (checked); the couple pass wrote the cell forces
+		if (L->desc.storage == KEL_STORAGE_FP32)
+			k_gather<D2Q9, STORE_FP32, true><<<ps->n, GT, 0, L->stream>>>(v, ps->d, hlbm_steps(prm), KEL_POROSITY_RAMP,
+																		   prm->eps);
+		else
+			k_gather<D2Q9, STORE_FP16S, true><<<ps->n, GT, 0, L->stream>>>(v, ps->d, hlbm_steps(prm),
+																			KEL_POROSITY_RAMP, prm->eps);
+		KEL_CUDA(cudaGetLastError());
+		return KEL_OK;
+	}
 	if (want_cell_force) {
 		if (!ps->cell_force) KEL_CUDA(cudaMalloc(&ps->cell_force, sizeof(float) * L->plane * L->d.D));
 		KEL_CUDA(cudaMemsetAsync(ps->cell_force, 0, sizeof(float) * L->plane * L->d.D, L->stream));
@@ -661,7 +864,12 @@ extern "C" int kel_particles_couple(kel_particles *ps, const kel_particle_params
 
 extern "C" int kel_particles_gather(kel_particles *ps, const kel_particle_params *prm, float *host_cell_force) {
 	int rc = check_params(ps, prm, "kel_particles_gather");
-	if (rc || (rc = particles_gather(ps, prm, host_cell_force != nullptr))) return rc;
+	if (rc) return rc;
+	// HLBM: the cell force is the momentum of the last gather writing each
+	// cell, computed on the populations before the bodies move
+	if (prm->coupling == KEL_COUPLING_HLBM && host_cell_force && (rc = particles_hlbm_couple(ps, prm, true)))
+		return rc;
+	if ((rc = particles_gather(ps, prm, host_cell_force != nullptr))) return rc;
 	if (host_cell_force) {
 		kel_lattice *L = ps->lat;
 		if ((rc = field_to_host(L, ps->cell_force, host_cell_force, L->d.D))) return rc;
@@ -684,15 +892,29 @@ extern "C" int kel_particles_integrate(kel_particles *ps, const kel_particle_par
 	return KEL_OK;
 }
 
+extern "C" int kel_particles_stamp(kel_particles *ps, const kel_particle_params *prm) {
+	int rc = check_params(ps, prm, "kel_particles_stamp");
+	if (rc) return rc;
+	if (prm->coupling != KEL_COUPLING_HLBM)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_stamp: HLBM coupling only");
+	if ((rc = particles_stamp(ps, prm))) return rc;
+	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	return KEL_OK;
+}
+
 extern "C" int kel_particles_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
 								  uint64_t n_steps, uint32_t step_flags) {
 	int rc = check_params(ps, prm, "kel_particles_step");
 	if (rc) return rc;
 	if (!prog) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_step: null program");
+	const bool hlbm = prm->coupling == KEL_COUPLING_HLBM;
+	if (hlbm != (prog->collision == KEL_COLL_HLBM))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_step: HLBM coupling goes with the KEL_COLL_HLBM collision");
 	for (uint64_t s = 0; s < n_steps; ++s) {
 		if ((rc = particles_reset(ps)) || (rc = particles_couple(ps, prm)) || (rc = particles_gather(ps, prm, false)) ||
 			(rc = particles_contact(ps, prm)) || (rc = particles_integrate(ps, prm)))
 			return rc;
+		if (hlbm && (rc = particles_stamp(ps, prm))) return rc;
 		const uint32_t fl = (s + 1 == n_steps) ? step_flags : (step_flags & KEL_STEP_ALL_MACROS);
 		if ((rc = kel_step(ps->lat, prog, 1, fl))) return rc;
 	}

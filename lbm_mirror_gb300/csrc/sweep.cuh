@@ -33,7 +33,7 @@ namespace kel {
 namespace gb {
 
 enum : int { STORE_FP32 = 0, STORE_FP16S = 1 };
-enum : int { COLL_BGK = 0, COLL_BGK_GUO = 1, COLL_PSM = 2, COLL_PSM_GUO = 3 };
+enum : int { COLL_BGK = 0, COLL_BGK_GUO = 1, COLL_PSM = 2, COLL_PSM_GUO = 3, COLL_HLBM = 4 };
 enum : int {
 	BC_NONE = 0,
 	BC_BOUNCE_BACK = 1,
@@ -63,6 +63,8 @@ struct SweepParams {
 	float *u;         // macros "velocity", D planes
 	const float *por; // macros "porosity"
 	const float *force; // macros "force", D planes
+	const float *hN;    // HLBM "particle_N", D planes
+	const float *hD;    // HLBM "particle_D"
 	const float *profile; // inlet u_x per y
 	const OpEntry *ops;
 	int nxp, ny, nz;
@@ -367,11 +369,22 @@ __device__ __forceinline__ void zouhe_pressure_d3q27(float (&f)[27], bool east, 
 }
 
 // The collision chosen by the program (BGK / BGKGuo / Psm / Psm + Guo).
+// For COLL_HLBM the force argument carries the cell's HLBM accumulators
+// (N_x, N_y, D) and por its porosity.
 template <class L, int COLL, bool EXACT>
 __device__ __forceinline__ void collide(float (&f)[L::Q], const CellCtx &p, float por, const float (&Fc)[3],
 										float &rho, float (&u)[3]) {
 	using A = Ar<true>;
 	moments<L, EXACT>(f, rho, u);
+	if (COLL == COLL_HLBM) {
+		// hlbm.hpp:86-96: u <- u por + (D > 0 ? N (1 - por) / D : N)
+		const float flip = A::sub(1.0f, por), Dv = Fc[2];
+#pragma unroll
+		for (int k = 0; k < 2; ++k) {
+			const float add = Dv > 0.f ? A::div(A::mul(Fc[k], flip), Dv) : Fc[k];
+			u[k] = A::add(A::mul(u[k], por), add);
+		}
+	}
 	float eq[L::Q];
 	equilibrium<L, EXACT>(rho, u, eq);
 	float F[3] = {0.f, 0.f, 0.f};
@@ -379,7 +392,7 @@ __device__ __forceinline__ void collide(float (&f)[L::Q], const CellCtx &p, floa
 #pragma unroll
 		for (int k = 0; k < L::D; ++k) F[k] = A::add(Fc[k], p.g[k]);
 	}
-	if (COLL == COLL_BGK) {
+	if (COLL == COLL_BGK || COLL == COLL_HLBM) {
 #pragma unroll
 		for (int i = 0; i < L::Q; ++i)
 			f[i] = EXACT ? A::add(f[i], A::mul(p.omega, A::sub(eq[i], f[i]))) : __fmaf_rn(p.omega, A::sub(eq[i], f[i]), f[i]);
@@ -700,11 +713,16 @@ __global__ void __launch_bounds__(256) sweep1_kernel(const __grid_constant__ Swe
 		}
 	}
 	const int flag = p.flags[cell];
-	const float por = (COLL == COLL_PSM || COLL == COLL_PSM_GUO) ? p.por[cell] : 1.f;
+	const float por = (COLL == COLL_PSM || COLL == COLL_PSM_GUO || COLL == COLL_HLBM) ? p.por[cell] : 1.f;
 	float Fc[3] = {0.f, 0.f, 0.f};
 	if (COLL == COLL_BGK_GUO || COLL == COLL_PSM_GUO) {
 #pragma unroll
 		for (int k = 0; k < L::D; ++k) Fc[k] = p.force[k * p.plane + cell];
+	}
+	if (COLL == COLL_HLBM) {
+		Fc[0] = p.hN[cell];
+		Fc[1] = p.hN[p.plane + cell];
+		Fc[2] = p.hD[cell];
 	}
 	float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
 	const bool col = cell_update<L, COLL, EXACT>(f, flag, y, cell_ctx(p), por, Fc, rho, u);

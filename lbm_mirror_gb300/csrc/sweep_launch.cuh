@@ -13,7 +13,10 @@ namespace gb {
 template <class L, int STORE, bool ODD, int COLL, bool EXACT>
 static cudaError_t launch_variant(const SweepParams &p, cudaStream_t st) {
 	const int block = p.block > 0 ? p.block : 256;
-	if (p.cpt == 1) {
+	if constexpr (COLL == COLL_HLBM) { // one cell per thread only
+		dim3 grid((p.nxp + block - 1) / block, p.ny, p.nz);
+		sweep1_kernel<L, STORE, ODD, COLL, EXACT><<<grid, block, 0, st>>>(p);
+	} else if (p.cpt == 1) {
 		dim3 grid((p.nxp + block - 1) / block, p.ny, p.nz);
 		sweep1_kernel<L, STORE, ODD, COLL, EXACT><<<grid, block, 0, st>>>(p);
 	} else {
@@ -31,6 +34,9 @@ static cudaError_t launch_coll(const SweepParams &p, int coll, cudaStream_t st) 
 	case COLL_BGK_GUO: return launch_variant<L, STORE, ODD, COLL_BGK_GUO, EXACT>(p, st);
 	case COLL_PSM: return launch_variant<L, STORE, ODD, COLL_PSM, EXACT>(p, st);
 	case COLL_PSM_GUO: return launch_variant<L, STORE, ODD, COLL_PSM_GUO, EXACT>(p, st);
+	case COLL_HLBM:
+		if constexpr (L::Q == 9) return launch_variant<L, STORE, ODD, COLL_HLBM, EXACT>(p, st);
+		return cudaErrorInvalidValue;
 	}
 	return cudaErrorInvalidValue;
 }

@@ -330,6 +330,10 @@ class Particles:
     def contact(self, params):
         _check(self.lib.kel_particles_contact(self._h, C.byref(params)), self.lib)
 
+    def stamp(self, params):
+        """HLBM coupling: the particle_N / particle_D accumulators (after integrate)."""
+        _check(self.lib.kel_particles_stamp(self._h, C.byref(params)), self.lib)
+
     def integrate(self, params):
         _check(self.lib.kel_particles_integrate(self._h, C.byref(params)), self.lib)
 
