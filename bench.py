@@ -38,6 +38,7 @@ WORKLOADS = {
     "d3q27_cavity_256": (27, (256, 256, 256), 0.55, "cavity"),
     "d3q19_cavity_128": (19, (128, 128, 128), 0.55, "cavity"),
     "d3q19_cavity_192": (19, (192, 192, 192), 0.55, "cavity"),
+    "d3q27_cavity_128": (27, (128, 128, 128), 0.55, "cavity"),
     "d2q9_poiseuille_256x64": (9, (256, 64), 0.8, "poiseuille"),
     "d2q9_channel_4096x4096": (9, (4096, 4096), 0.8, "poiseuille"),
     "d2q9_batch_1024": (9, None, None, "batch"),
@@ -46,6 +47,22 @@ WORKLOADS = {
     "unet_train_256x64": (9, (256, 64), None, "unet_train"),
     "d2q9_psm_particles_2048x512": (9, (2048, 512), 0.7, "particles"),
 }
+
+
+def max_over_ranks(x, dist, device="cuda"):
+    """The slowest rank's time (barrier-bracketed timing reports the max)."""
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)], device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, seconds):
+    """Replicas: every rank processes units_per_rank; the whole job's rate is
+    all ranks' units over the slowest rank's time."""
+    return world * units_per_rank / seconds
 
 
 def bytes_per_update(q, storage):
@@ -539,13 +556,9 @@ def main():
     ev1.synchronize()
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist)
     per_launch_s = ms / 1e3 / args.steps
-    value = world * ncell * args.steps / (ms / 1e3) / 1e6
+    value = whole_job_rate(ncell * args.steps, world, ms / 1e3) / 1e6
 
     bpu = bytes_per_update(q, args.storage)
     peak, peak_src = load_peaks()
@@ -577,12 +590,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.e2e_iters):
         e2e_once()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * ncell * args.e2e_lbm_steps * args.e2e_iters / e2e_s / 1e6
+    e2e_s = max_over_ranks(time.perf_counter() - t0, dist)
+    e2e_value = whole_job_rate(ncell * args.e2e_lbm_steps * args.e2e_iters, world, e2e_s) / 1e6
     mass = float(h_rho.numpy()[case["flags"] == 2].astype(np.float64).mean())
     # one more pass, each call timed alone (not part of the e2e value)
     phases = {}

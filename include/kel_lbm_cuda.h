@@ -348,6 +348,30 @@ int kel_lattice_get_launch(const kel_lattice *lat, int32_t *cells_per_thread, in
 int kel_lattice_autotune(kel_lattice *lat, const kel_step_program *prog, int32_t steps, int32_t *cells_per_thread,
 						 int32_t *block_threads, float *ms_per_step);
 
+/* ---- geometry and initial state on the device --------------------------
+ * The drivers' setup_initial_conditions (e.g. examples/poiseulle_2d_gpu/
+ * poiseulle_2d_gpu.cpp:55-156) paint flags cell by cell and set
+ * dfs_old = equilibrium(rho, u) on the host; here both run on the device. */
+#define KEL_PAINT_BOX 0
+#define KEL_PAINT_SPHERE 1
+typedef struct kel_paint_op {
+	int32_t shape;        /* KEL_PAINT_BOX or KEL_PAINT_SPHERE */
+	int32_t flag;         /* value written (0..255) */
+	int64_t lo[3], hi[3]; /* cells with lo <= x < hi on every axis: the box, or the sphere's clip */
+	double center[3];     /* sphere: sum over axes (x - center)^2 <= radius^2 */
+	double radius;
+} kel_paint_op;
+/* Apply the ops in order to the flag field (later ops win). */
+int kel_lattice_paint(kel_lattice *lat, const kel_paint_op *ops, int32_t n_ops);
+int kel_download_flags(kel_lattice *lat, uint8_t *host);
+/* f_i(x) = equilibrium(rho, u) with the reference's rounding at the current
+ * time step; rho and u from device fields (n_cells floats, x fastest; u one
+ * such plane per component) or, where a pointer is NULL, from rho0 / u0 (u0
+ * may be NULL: zero).  At an odd time step a boundary cell's populations that
+ * come from outside the lattice have no slot (they are the zero ghost ring). */
+int kel_lattice_init_equilibrium(kel_lattice *lat, const float *d_rho, const float *d_u, double rho0,
+								 const double *u0);
+
 /* ---- field output and checkpoints -------------------------------------
  * Host writers in the reference's formats (write_vtk.hpp, write_csv.hpp,
  * abstract/forst.hpp + forst_chunk.hpp): cells x fastest over dims; each

@@ -49,6 +49,7 @@ KEL_FIELD_POROSITY, KEL_FIELD_FORCE, KEL_FIELD_HLBM_N, KEL_FIELD_HLBM_D = 1, 2, 
 KEL_STEP_WRITE_MACROS, KEL_STEP_ALL_MACROS = 1, 2
 KEL_UNET_CONV_TCGEN05, KEL_UNET_CONV_MMA_SYNC = 0, 1
 KEL_VALUE_U8, KEL_VALUE_F32, KEL_VALUE_F64 = 0, 1, 2
+KEL_PAINT_BOX, KEL_PAINT_SPHERE = 0, 1
 KEL_WRITE_VTK, KEL_WRITE_CSV, KEL_WRITE_FORST = 1, 2, 4
 
 
@@ -200,6 +201,11 @@ class UnetDesc(C.Structure):
                 ("reserved", C.c_int32)]
 
 
+class PaintOp(C.Structure):
+    _fields_ = [("shape", C.c_int32), ("flag", C.c_int32), ("lo", C.c_int64 * 3), ("hi", C.c_int64 * 3),
+                ("center", C.c_double * 3), ("radius", C.c_double)]
+
+
 class FieldView(C.Structure):
     _fields_ = [("name", C.c_char_p), ("value_type", C.c_int32), ("components", C.c_int32), ("ghost", C.c_int32),
                 ("vector", C.c_int32), ("data", C.c_void_p)]
@@ -276,6 +282,9 @@ def load_library(path: str | None = None):
         "kel_lattice_write_fields": ([vp, i32, C.c_char_p, C.c_char_p, u64], C.c_int),
         "kel_lattice_save": ([vp, C.c_char_p], C.c_int),
         "kel_lattice_load": ([vp, C.c_char_p], C.c_int),
+        "kel_lattice_paint": ([vp, C.POINTER(PaintOp), i32], C.c_int),
+        "kel_download_flags": ([vp, vp], C.c_int),
+        "kel_lattice_init_equilibrium": ([vp, vp, vp, C.c_double, C.POINTER(C.c_double)], C.c_int),
         "kel_particles_stamp": ([vp, C.POINTER(ParticleParams)], C.c_int),
         "kel_lattice_get_launch": ([vp, C.POINTER(i32), C.POINTER(i32)], C.c_int),
         "kel_lattice_autotune": ([vp, C.POINTER(StepProgram), i32, C.POINTER(i32), C.POINTER(i32),

@@ -378,6 +378,64 @@ static void launch_pop_convert(const kel_lattice *L, const ConvArgs &a, int uplo
 	}
 }
 
+// ---------------------------------------------------------------------------
+// geometry and initial state on the device
+
+// Flag painting: each op writes `flag` into the cells of its box (lo <= x < hi
+// per axis) -- for a sphere only those with sum (x - c)^2 <= r^2, cell centres
+// at integer coordinates -- applied in order, one cell per thread.
+__global__ void k_paint(uint8_t *flags, int nx, int ny, int nz, int nxp, const kel_paint_op *ops, int n_ops) {
+	const int64_t n = (int64_t)nx * ny * nz;
+	for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+		const int x = (int)(c % nx);
+		const int64_t r = c / nx;
+		const int y = (int)(r % ny), z = (int)(r / ny);
+		const int64_t pos[3] = {x, y, z};
+		const int64_t at = r * nxp + x;
+		uint8_t v = flags[at];
+		for (int k = 0; k < n_ops; ++k) {
+			const kel_paint_op &o = ops[k];
+			bool in = true;
+			for (int d = 0; d < 3; ++d) in = in && pos[d] >= o.lo[d] && pos[d] < o.hi[d];
+			if (in && o.shape == KEL_PAINT_SPHERE) {
+				double s2 = 0.0;
+				for (int d = 0; d < 3; ++d) {
+					const double dd = (double)pos[d] - o.center[d];
+					s2 = s2 + dd * dd;
+				}
+				in = s2 <= o.radius * o.radius;
+			}
+			if (in) v = (uint8_t)o.flag;
+		}
+		flags[at] = v;
+	}
+}
+
+// Populations f_i(x) = equilibrium(rho, u) with the reference's rounding
+// (equilibrium.hpp:7-48), placed for the lattice's current time step; rho and
+// u per cell from the fields (cells x fastest; u one plane per component) or
+// the constants.
+template <class L>
+__global__ void k_init_equilibrium(ConvArgs a, const float *rho_f, const float *u_f, float rho0, float u0x, float u0y,
+								   float u0z) {
+	for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < a.ncell; c += (int64_t)gridDim.x * blockDim.x) {
+		const int x = (int)(c % a.nx);
+		const int64_t r = c / a.nx;
+		const int y = (int)(r % a.ny), z = (int)(r / a.ny);
+		const float rho = rho_f ? rho_f[c] : rho0;
+		float u[3] = {u0x, u0y, u0z};
+		if (u_f)
+			for (int d = 0; d < L::D; ++d) u[d] = u_f[(int64_t)d * a.ncell + c];
+		if (L::D == 2) u[2] = 0.f;
+		float eq[L::Q];
+		equilibrium<L, true>(rho, u, eq);
+		for (int i = 0; i < L::Q; ++i) {
+			int64_t idx;
+			if (pop_slot(a, x, y, z, i, idx)) stpop(a, idx, i, eq[i]);
+		}
+	}
+}
+
 static ConvArgs conv_args(const kel_lattice *L, int dtype, int layout) {
 	ConvArgs a;
 	memset(&a, 0, sizeof(a));
@@ -431,6 +489,73 @@ extern "C" int kel_download_populations(kel_lattice *L, void *host, int32_t dtyp
 	launch_pop_convert(L, conv_args(L, dtype, layout), 0);
 	KEL_CUDA(cudaGetLastError());
 	KEL_CUDA(cudaMemcpyAsync(host, L->staging, bytes, cudaMemcpyDeviceToHost, L->stream));
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_lattice_paint(kel_lattice *L, const kel_paint_op *ops, int32_t n_ops) {
+	if (!L || !ops || n_ops < 1 || n_ops > 4096)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_paint: bad arguments");
+	for (int k = 0; k < n_ops; ++k) {
+		if (ops[k].shape != KEL_PAINT_BOX && ops[k].shape != KEL_PAINT_SPHERE)
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_paint: op %d: unknown shape %d", k, ops[k].shape);
+		if (ops[k].flag < 0 || ops[k].flag > 255)
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_paint: op %d: flag %d outside 0..255", k, ops[k].flag);
+	}
+	kel_paint_op *d_ops = nullptr;
+	KEL_CUDA(cudaMalloc(&d_ops, sizeof(kel_paint_op) * n_ops));
+	cudaError_t e = cudaMemcpyAsync(d_ops, ops, sizeof(kel_paint_op) * n_ops, cudaMemcpyHostToDevice, L->stream);
+	if (e == cudaSuccess) {
+		k_paint<<<grid_for(L->ncell), 256, 0, L->stream>>>(L->flags, (int)L->desc.nx, (int)L->desc.ny,
+														   (int)L->desc.nz, L->nxp, d_ops, n_ops);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+	cudaFree(d_ops);
+	if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_lattice_paint: %s", cudaGetErrorString(e));
+	// the program is validated against the flags present: rescan them
+	if (!L->d_seen) KEL_CUDA(cudaMalloc(&L->d_seen, 8 * sizeof(unsigned)));
+	KEL_CUDA(cudaMemsetAsync(L->d_seen, 0, 8 * sizeof(unsigned), L->stream));
+	k_flag_presence<<<grid_for(L->plane), 256, 0, L->stream>>>(L->flags, L->plane, (int)L->desc.nx, L->nxp, L->d_seen);
+	KEL_CUDA(cudaGetLastError());
+	unsigned seen[8];
+	KEL_CUDA(cudaMemcpyAsync(seen, L->d_seen, sizeof(seen), cudaMemcpyDeviceToHost, L->stream));
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	for (int fl = 0; fl < MAX_FLAGS; ++fl) L->present[fl] = (seen[fl >> 5] >> (fl & 31)) & 1u;
+	L->have_ops = false;
+	return KEL_OK;
+}
+
+extern "C" int kel_download_flags(kel_lattice *L, uint8_t *host) {
+	if (!L || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_download_flags: null argument");
+	const auto &D = L->desc;
+	KEL_CUDA(cudaMemcpy2DAsync(host, (size_t)D.nx, L->flags, (size_t)L->nxp, (size_t)D.nx, (size_t)(D.ny * D.nz),
+							   cudaMemcpyDeviceToHost, L->stream));
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_lattice_init_equilibrium(kel_lattice *L, const float *d_rho, const float *d_u, double rho0,
+											const double *u0) {
+	if (!L) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_init_equilibrium: null lattice");
+	const double z[3] = {0.0, 0.0, 0.0};
+	const double *u = u0 ? u0 : z;
+	const ConvArgs a = conv_args(L, KEL_DTYPE_F32, KEL_LAYOUT_AOS);
+	const unsigned g = grid_for(L->ncell);
+	switch (L->d.Q) {
+	case 9:
+		k_init_equilibrium<D2Q9><<<g, 256, 0, L->stream>>>(a, d_rho, d_u, (float)rho0, (float)u[0], (float)u[1], 0.f);
+		break;
+	case 19:
+		k_init_equilibrium<D3Q19><<<g, 256, 0, L->stream>>>(a, d_rho, d_u, (float)rho0, (float)u[0], (float)u[1],
+															(float)u[2]);
+		break;
+	default:
+		k_init_equilibrium<D3Q27><<<g, 256, 0, L->stream>>>(a, d_rho, d_u, (float)rho0, (float)u[0], (float)u[1],
+															(float)u[2]);
+		break;
+	}
+	KEL_CUDA(cudaGetLastError());
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
 	return KEL_OK;
 }
@@ -667,6 +792,7 @@ static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	for (int k = 0; k < 3; ++k) p.g[k] = (float)P->global_force[k];
 	for (int i = 0; i < 27; ++i) p.wshift[i] = L->wshift[i];
 	p.cpt = L->cpt;
+	p.idx32 = (int64_t)L->d.Q * L->plane < ((int64_t)1 << 31) ? 1 : 0;
 	p.block = L->block;
 	return p;
 }

@@ -77,6 +77,7 @@ struct SweepParams {
 	float g[3];       // global force
 	float wshift[27]; // FP16S: stored value is f - wshift[i]
 	int cpt;          // cells per thread: 4 (sweep_kernel) or 1 (sweep1_kernel)
+	int idx32;        // Q * plane < 2^31: offsets from a cell fit 32-bit arithmetic
 	int block;        // threads per block
 };
 
@@ -175,8 +176,10 @@ struct Store<STORE_FP16S> {
 // ---------------------------------------------------------------------------
 // Cell physics (one cell, populations in registers).
 
-// compute_rho_u, modules/core/c++/macroscopic.hpp:10-35
-template <class L, bool EXACT_UNUSED>
+// compute_rho_u, modules/core/c++/macroscopic.hpp:10-35: the reference's
+// summation order; EXACT divides each component by rho, the fast arithmetic
+// multiplies by the correctly rounded reciprocal of rho (one rounding more).
+template <class L, bool EXACT>
 __device__ __forceinline__ void moments(const float (&f)[L::Q], float &rho, float (&u)[3]) {
 	using A = Ar<true>;
 	float r = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f;
@@ -193,9 +196,16 @@ __device__ __forceinline__ void moments(const float (&f)[L::Q], float &rho, floa
 		}
 	}
 	rho = r;
-	u[0] = A::div(v0, r);
-	u[1] = A::div(v1, r);
-	u[2] = L::D == 3 ? A::div(v2, r) : 0.f;
+	if (EXACT) {
+		u[0] = A::div(v0, r);
+		u[1] = A::div(v1, r);
+		u[2] = L::D == 3 ? A::div(v2, r) : 0.f;
+	} else {
+		const float ir = __frcp_rn(r);
+		u[0] = v0 * ir;
+		u[1] = v1 * ir;
+		u[2] = L::D == 3 ? v2 * ir : 0.f;
+	}
 }
 
 // c_i . u with the reference's summation order (0 + u_0 c_0 + u_1 c_1 ...)
@@ -686,11 +696,27 @@ __global__ void __launch_bounds__(256) sweep1_kernel(const __grid_constant__ Swe
 	const bool ok_xm = has_xm || p.periodic;  // x - 1 exists
 	const bool ok_xp = has_xp || p.periodic;  // x + 1 exists
 	const bool row_interior = y > 0 && y + 1 < p.ny && (L::D == 2 || (z > 0 && z + 1 < p.nz));
+	// 32-bit offsets from this cell's slot in plane 0 (when they fit): one
+	// 32-bit multiply-add per population instead of 64-bit index arithmetic
+	using ST = typename S::T;
+	ST *const fc = static_cast<ST *>(p.f) + cell;
+	const int pl32 = (int)p.plane, oy32 = nxp, oz32 = nxp * p.ny;
 
 	float f[Q];
-	if (!ODD) {
+	if (!ODD && p.idx32) {
+#pragma unroll
+		for (int i = 0; i < Q; ++i) f[i] = S::ld1(fc, i * pl32, p.wshift[i]);
+	} else if (!ODD) {
 #pragma unroll
 		for (int i = 0; i < Q; ++i) f[i] = S::ld1(p.f, i * p.plane + cell, p.wshift[i]);
+	} else if (row_interior && p.idx32) {
+#pragma unroll
+		for (int i = 0; i < Q; ++i) {
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int off = L::opp(i) * pl32 + (cx > 0 ? xm : (cx < 0 ? xp : 0)) - cy * oy32 - cz * oz32;
+			const bool ok = cx > 0 ? ok_xm : (cx < 0 ? ok_xp : true);
+			f[i] = ok ? S::ld1(fc, off, p.wshift[i]) : 0.f;
+		}
 	} else if (row_interior) {
 #pragma unroll
 		for (int i = 0; i < Q; ++i) {
@@ -733,7 +759,21 @@ __global__ void __launch_bounds__(256) sweep1_kernel(const __grid_constant__ Swe
 	}
 	if (!ODD) {
 #pragma unroll
-		for (int i = 0; i < Q; ++i) S::st1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + cell, f[i], p.wshift[i]);
+		for (int i = 0; i < Q; ++i) {
+			if (p.idx32) S::st1(fc, L::opp(i) * pl32, f[i], p.wshift[i]);
+			else S::st1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + cell, f[i], p.wshift[i]);
+		}
+	} else if (row_interior && p.idx32) {
+#pragma unroll
+		for (int i = 0; i < Q; ++i) {
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int pb = i * pl32;
+			if (cx > 0 && !ok_xm) S::st1(fc, pb, 0.f, p.wshift[i]);
+			if (cx < 0 && !ok_xp) S::st1(fc, pb, 0.f, p.wshift[i]);
+			const int off = (cx > 0 ? xp : (cx < 0 ? xm : 0)) + cy * oy32 + cz * oz32;
+			const bool ok = cx > 0 ? ok_xp : (cx < 0 ? ok_xm : true);
+			if (ok) S::st1(fc, pb + off, f[i], p.wshift[i]);
+		}
 	} else if (row_interior) {
 #pragma unroll
 		for (int i = 0; i < Q; ++i) {

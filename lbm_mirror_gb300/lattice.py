@@ -246,6 +246,37 @@ class Lattice:
         fl = (K.KEL_STEP_WRITE_MACROS if write_macros else 0) | (K.KEL_STEP_ALL_MACROS if all_macros else 0)
         _check(self.lib.kel_step(self._h, C.byref(program), n_steps, fl), self.lib)
 
+    def paint(self, ops):
+        """Flag painting on the device: ops are dicts with shape ("box" or
+        "sphere"), flag, lo, hi (cell bounds, lo <= x < hi) and, for spheres,
+        center and radius; applied in order."""
+        arr = (K.PaintOp * len(ops))()
+        for a, o in zip(arr, ops):
+            a.shape = K.KEL_PAINT_SPHERE if o.get("shape", "box") == "sphere" else K.KEL_PAINT_BOX
+            a.flag = int(o["flag"])
+            big = 1 << 40
+            lo = list(o.get("lo", (0, 0, 0))) + [0] * 3
+            hi = list(o.get("hi", (big, big, big))) + [big] * 3
+            for d in range(3):
+                a.lo[d], a.hi[d] = int(lo[d]), int(hi[d])
+            c = list(o.get("center", (0.0, 0.0, 0.0))) + [0.0] * 3
+            for d in range(3):
+                a.center[d] = float(c[d])
+            a.radius = float(o.get("radius", 0.0))
+        _check(self.lib.kel_lattice_paint(self._h, arr, len(ops)), self.lib)
+
+    def flags(self):
+        out = np.empty(self.n, dtype=np.uint8)
+        _check(self.lib.kel_download_flags(self._h, _ptr(out)), self.lib)
+        return out
+
+    def init_equilibrium(self, rho=1.0, u=(0.0, 0.0, 0.0), d_rho=None, d_u=None):
+        """Populations = equilibrium(rho, u) on the device (reference rounding);
+        d_rho / d_u: optional device pointers to per-cell fields."""
+        u3 = (C.c_double * 3)(*(list(u) + [0.0] * 3)[:3])
+        _check(self.lib.kel_lattice_init_equilibrium(self._h, C.c_void_p(d_rho) if d_rho else None,
+                                                     C.c_void_p(d_u) if d_u else None, float(rho), u3), self.lib)
+
     def write_fields(self, out_dir, file_name, t, formats=K.KEL_WRITE_VTK):
         """The macro output (velocity, density) as the reference's VTK / CSV /
         Forst files under out_dir (kel_lattice_write_fields)."""
