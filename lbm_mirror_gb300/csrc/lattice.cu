@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "lattice_internal.cuh"
+#include "sweep_rows.cuh"
 
 using namespace kel::gb;
 
@@ -144,13 +145,19 @@ extern "C" int kel_lattice_create(const kel_lattice_desc *desc, kel_lattice **ou
 	kel_lattice *L = new kel_lattice();
 	L->desc = *desc;
 	L->d = d;
-	L->nxp = (int)((desc->nx + 3) / 4 * 4);
+	// rows padded to 16 bytes (FP32: 4 cells, FP16S: 8 cells) so that every row
+	// starts on a bulk-copy boundary; periodic rows are not padded (nxp == nx)
+	const bool periodic = (desc->flags & KEL_LATTICE_PERIODIC_X) != 0;
+	const int64_t pad = (desc->storage == KEL_STORAGE_FP16S && !periodic) ? 8 : 4;
+	L->nxp = (int)((desc->nx + pad - 1) / pad * pad);
 	L->nq = L->nxp / 4;
 	L->wpr = (L->nq + 31) / 32;
 	L->ncell = desc->nx * desc->ny * desc->nz;
 	L->plane = (int64_t)L->nxp * desc->ny * desc->nz;
 	L->elem = desc->storage == KEL_STORAGE_FP32 ? 4 : 2;
 	cudaGetDevice(&L->device);
+	cudaDeviceGetAttribute(&L->sms, cudaDevAttrMultiProcessorCount, L->device);
+	if (L->sms < 1) L->sms = 1;
 	for (int i = 0; i < 27; ++i) L->wshift[i] = 0.f;
 	if (desc->storage == KEL_STORAGE_FP16S)
 		for (int i = 0; i < d.Q; ++i) L->wshift[i] = __half2float(__float2half_rn((float)d.w[i]));
@@ -161,7 +168,10 @@ extern "C" int kel_lattice_create(const kel_lattice_desc *desc, kel_lattice **ou
 	};
 	cudaError_t e;
 	if ((e = cudaMalloc(&L->f, (size_t)d.Q * L->plane * L->elem)) != cudaSuccess ||
-		(e = cudaMalloc(&L->flags, (size_t)L->plane)) != cudaSuccess ||
+		// 64 bytes past the last row: the row pipeline widens its flag copies
+		// to 16-byte boundaries
+		(e = cudaMalloc(&L->flags, (size_t)L->plane + 64)) != cudaSuccess ||
+		(e = cudaMalloc(&L->d_err, sizeof(unsigned))) != cudaSuccess ||
 		(e = cudaMalloc(&L->rho, (size_t)L->plane * sizeof(float))) != cudaSuccess ||
 		(e = cudaMalloc(&L->u, (size_t)d.D * L->plane * sizeof(float))) != cudaSuccess ||
 		(e = cudaMalloc(&L->profile, (size_t)desc->ny * sizeof(float))) != cudaSuccess ||
@@ -178,7 +188,8 @@ extern "C" int kel_lattice_create(const kel_lattice_desc *desc, kel_lattice **ou
 	k_fill_f32<<<grid_for(L->plane), 256, 0, L->stream>>>(L->rho, L->plane, 1.0f);
 	k_fill_f32<<<grid_for(d.D * L->plane), 256, 0, L->stream>>>(L->u, d.D * L->plane, 0.0f);
 	k_fill_f32<<<grid_for(desc->ny), 256, 0, L->stream>>>(L->profile, desc->ny, 0.0f);
-	if ((e = cudaMemsetAsync(L->flags, 0, (size_t)L->plane, L->stream)) != cudaSuccess ||
+	if ((e = cudaMemsetAsync(L->flags, 0, (size_t)L->plane + 64, L->stream)) != cudaSuccess ||
+		(e = cudaMemsetAsync(L->d_err, 0, sizeof(unsigned), L->stream)) != cudaSuccess ||
 		(e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamSynchronize(L->stream)) != cudaSuccess) {
 		int rc = fail(KEL_ERR_CUDA, "kel_lattice_create: %s", cudaGetErrorString(e));
 		return cleanup(rc);
@@ -194,6 +205,7 @@ extern "C" int kel_lattice_destroy(kel_lattice *L) {
 	cudaFree(L->f);
 	cudaFree(L->flags);
 	cudaFree(L->d_seen);
+	cudaFree(L->d_err);
 	cudaFree(L->rho);
 	cudaFree(L->u);
 	cudaFree(L->por);
@@ -219,10 +231,24 @@ extern "C" int kel_lattice_time_step(const kel_lattice *L, uint64_t *t) {
 	return KEL_OK;
 }
 
+// After the lattice's stream has drained: did a row-pipeline sweep give up on
+// a bounded wait?  The flag is cleared when reported.
+static int check_sweep_error(kel_lattice *L, const char *who) {
+	if (!L->rows_used) return KEL_OK;
+	unsigned err = 0;
+	KEL_CUDA(cudaMemcpyAsync(&err, L->d_err, sizeof(err), cudaMemcpyDeviceToHost, L->stream));
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	if (err == 0) return KEL_OK;
+	KEL_CUDA(cudaMemsetAsync(L->d_err, 0, sizeof(unsigned), L->stream));
+	KEL_CUDA(cudaStreamSynchronize(L->stream));
+	return fail(KEL_ERR_TIMEOUT, "%s: a row-pipeline sweep gave up waiting for its row copies; the populations are invalid",
+				who);
+}
+
 extern "C" int kel_lattice_synchronize(kel_lattice *L) {
 	if (!L) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_lattice_synchronize: null lattice");
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
-	return KEL_OK;
+	return check_sweep_error(L, "kel_lattice_synchronize");
 }
 
 // ---------------------------------------------------------------------------
@@ -490,7 +516,7 @@ extern "C" int kel_download_populations(kel_lattice *L, void *host, int32_t dtyp
 	KEL_CUDA(cudaGetLastError());
 	KEL_CUDA(cudaMemcpyAsync(host, L->staging, bytes, cudaMemcpyDeviceToHost, L->stream));
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
-	return KEL_OK;
+	return check_sweep_error(L, "kel_download_populations");
 }
 
 extern "C" int kel_lattice_paint(kel_lattice *L, const kel_paint_op *ops, int32_t n_ops) {
@@ -611,7 +637,7 @@ extern "C" int kel_download_macros(kel_lattice *L, float *host_rho, float *host_
 	int rc;
 	if (host_rho && (rc = field_io(L, L->rho, host_rho, nullptr, 1))) return rc;
 	if (host_u && (rc = field_io(L, L->u, host_u, nullptr, L->d.D))) return rc;
-	return KEL_OK;
+	return check_sweep_error(L, "kel_download_macros");
 }
 
 extern "C" int kel_upload_field(kel_lattice *L, int32_t field, const float *host) {
@@ -727,6 +753,13 @@ static cudaError_t launch_one(const kel_lattice *L, const SweepParams &p, int co
 }
 
 static bool launch_ok(const kel_lattice *L, int cpt, int block) {
+	if (cpt == 2) { // row pipeline: block = row stages
+		if (block < 2 || block > ROWS_MAX_STAGES) return false;
+		if (L->nxp > ROWS_MAX_NXP || ((int64_t)L->nxp * (int64_t)L->elem) % 16 != 0) return false;
+		int optin = 0;
+		if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, L->device) != cudaSuccess) return false;
+		return rows_smem_bytes(L->d.Q, L->nxp, (int)L->elem, block) <= optin;
+	}
 	if (cpt != 1 && cpt != 4) return false;
 	if (block != 64 && block != 128 && block != 256) return false;
 	if (cpt == 1 && (L->desc.ny > 65535 || L->desc.nz > 65535)) return false;
@@ -794,6 +827,10 @@ static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	p.cpt = L->cpt;
 	p.idx32 = (int64_t)L->d.Q * L->plane < ((int64_t)1 << 31) ? 1 : 0;
 	p.block = L->block;
+	p.stages = L->cpt == 2 ? L->block : 0;
+	p.sms = L->sms;
+	p.err = L->d_err;
+	if (L->cpt == 2) L->rows_used = true;
 	return p;
 }
 
@@ -813,17 +850,19 @@ extern "C" int kel_lattice_autotune(kel_lattice *L, const kel_step_program *P, i
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
-	const int cands[6][2] = {{1, 64}, {1, 128}, {1, 256}, {4, 64}, {4, 128}, {4, 256}};
+	const int cands[9][2] = {{1, 64}, {1, 128}, {1, 256}, {4, 64}, {4, 128}, {4, 256}, {2, 3}, {2, 4}, {2, 6}};
 	float best = 1e30f;
 	int bc = L->cpt, bb = L->block;
 	cudaError_t e = cudaMemcpyAsync(save, L->f, bytes, cudaMemcpyDeviceToDevice, L->stream);
 	SweepParams p = make_params(L, P);
 	p.write_macros = 0;
 	const bool exact = P->arithmetic == KEL_ARITH_REFERENCE;
-	for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
+	for (int k = 0; k < 9 && e == cudaSuccess; ++k) {
 		if (!launch_ok(L, cands[k][0], cands[k][1])) continue;
 		p.cpt = cands[k][0];
 		p.block = cands[k][1];
+		p.stages = p.cpt == 2 ? p.block : 0;
+		if (p.cpt == 2) L->rows_used = true;
 		const bool odd0 = (L->t & 1u) != 0;
 		for (int s = 0; s < 2 && e == cudaSuccess; ++s) e = launch_one(L, p, P->collision, exact, odd0 != (s & 1));
 		cudaEventRecord(e0, L->stream);
@@ -845,6 +884,7 @@ extern "C" int kel_lattice_autotune(kel_lattice *L, const kel_step_program *P, i
 	cudaEventDestroy(e1);
 	cudaFree(save);
 	if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_lattice_autotune: %s", cudaGetErrorString(e));
+	if ((rc = check_sweep_error(L, "kel_lattice_autotune"))) return rc;
 	L->cpt = bc;
 	L->block = bb;
 	L->tuned = true;

@@ -60,7 +60,10 @@ struct kel_lattice {
 	unsigned *d_seen = nullptr;                 // device scratch of the flag-presence scan (8 words)
 	kel_step_program last_prog;
 	int device = 0;
-	int cpt = 1;      // cells per thread of the sweep launch (1 or 4)
-	int block = 128;  // threads per block of the sweep launch
+	int cpt = 1;      // sweep launch: cells per thread (1 or 4), or 2 for the row pipeline
+	int block = 128;  // threads per block of the sweep launch (row pipeline: row stages)
+	int sms = 1;      // multiprocessors of the lattice's device
+	unsigned *d_err = nullptr; // set by the row pipeline when a bounded wait gave up
+	bool rows_used = false;    // a row-pipeline sweep was launched (d_err worth reading)
 	bool tuned = false;
 };

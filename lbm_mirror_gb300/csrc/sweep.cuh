@@ -76,9 +76,12 @@ struct SweepParams {
 	float guo_scale;  // 1 - 0.5 * omega
 	float g[3];       // global force
 	float wshift[27]; // FP16S: stored value is f - wshift[i]
-	int cpt;          // cells per thread: 4 (sweep_kernel) or 1 (sweep1_kernel)
+	int cpt;          // cells per thread: 4 (sweep_kernel), 1 (sweep1_kernel), 2 (sweep_rows_kernel)
 	int idx32;        // Q * plane < 2^31: offsets from a cell fit 32-bit arithmetic
 	int block;        // threads per block
+	int stages;       // sweep_rows_kernel: row stages in shared memory
+	int sms;          // multiprocessors of the device (persistent grid of sweep_rows_kernel)
+	unsigned *err;    // sweep_rows_kernel: set to 1 when a bounded wait gave up
 };
 
 // What the per-cell physics needs from a launch: the flag -> operation table,

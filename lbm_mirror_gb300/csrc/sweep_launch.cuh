@@ -5,14 +5,58 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
+#include <cstdint>
+
 #include "sweep.cuh"
+#include "sweep_rows.cuh"
 
 namespace kel {
 namespace gb {
 
+// Row pipeline: persistent grid of (resident CTAs per SM) x SMs, capped at the
+// row count.  The shared-memory opt-in and the occupancy query run once per
+// kernel variant, device, row length and stage count (one cached entry).
+// Any grid size is correct (rows are dealt round-robin to the CTAs); the
+// occupancy only makes all CTAs resident at once.
+template <class L, int STORE, bool ODD, int COLL, bool EXACT>
+static cudaError_t launch_rows(const SweepParams &p, cudaStream_t st) {
+	auto kern = sweep_rows_kernel<L, STORE, ODD, COLL, EXACT>;
+	const int smem = rows_smem_bytes(L::Q, p.nxp, (int)sizeof(typename Store<STORE>::T), p.stages);
+	const int threads = ((p.nxp + 31) & ~31) + 32; // consumers (one per cell) + the producer warp
+	// one atomic word: device + 1 (bits 48-63), stages (40-47), nxp (16-39), CTAs per SM (0-15)
+	static std::atomic<uint64_t> cached{0};
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
+	const uint64_t key = (static_cast<uint64_t>(dev + 1) << 48) | (static_cast<uint64_t>(p.stages & 0xff) << 40) |
+						 (static_cast<uint64_t>(p.nxp & 0xffffff) << 16);
+	const uint64_t hit = cached.load();
+	int per_sm = 0;
+	if ((hit & ~static_cast<uint64_t>(0xffff)) == key) {
+		per_sm = static_cast<int>(hit & 0xffff);
+	} else {
+		// opt in to the device's whole per-block shared memory, so that no
+		// later call with a smaller footprint can lower it under another thread
+		int optin = 0;
+		if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
+		if (smem > optin) return cudaErrorInvalidConfiguration;
+		if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin)) != cudaSuccess) return e;
+		if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem)) != cudaSuccess) return e;
+		if (per_sm < 1) return cudaErrorInvalidConfiguration;
+		cached.store(key | static_cast<uint64_t>(per_sm & 0xffff));
+	}
+	const int64_t rows = static_cast<int64_t>(p.ny) * p.nz;
+	const int64_t slots = static_cast<int64_t>(per_sm) * (p.sms > 0 ? p.sms : 1);
+	const unsigned grid = static_cast<unsigned>(rows < slots ? rows : slots);
+	kern<<<grid, threads, smem, st>>>(p);
+	return cudaGetLastError();
+}
+
 template <class L, int STORE, bool ODD, int COLL, bool EXACT>
 static cudaError_t launch_variant(const SweepParams &p, cudaStream_t st) {
 	const int block = p.block > 0 ? p.block : 256;
+	if (p.cpt == 2) return launch_rows<L, STORE, ODD, COLL, EXACT>(p, st);
 	if constexpr (COLL == COLL_HLBM) { // one cell per thread only
 		dim3 grid((p.nxp + block - 1) / block, p.ny, p.nz);
 		sweep1_kernel<L, STORE, ODD, COLL, EXACT><<<grid, block, 0, st>>>(p);

@@ -19,10 +19,12 @@ pytestmark = pytest.mark.gpu
 OPS = {1: dict(bc=K.KEL_BC_BOUNCE_BACK), 2: dict(bc=K.KEL_BC_FLUID, collide=1)}
 
 
-def setup(g):
+def setup(g, launch=None):
     prm, P = params(g)
     prm.coupling = K.KEL_COUPLING_HLBM
     lat = Lattice("D2Q9", G.HLBM_DIMS)
+    if launch is not None:
+        lat.set_launch(*launch)
     lat.upload_flags(g["flags"])
     lat.upload_populations(g["init"].astype(np.float32))
     ps = Particles(lat, initial_states(g))
@@ -33,9 +35,10 @@ def setup(g):
     return prm, P, lat, ps, o, st
 
 
-def test_hlbm_phases_vs_oracle():
+@pytest.mark.parametrize("launch", [None, (K.KEL_LAUNCH_ROWS, 3)], ids=["default", "rows"])
+def test_hlbm_phases_vs_oracle(launch):
     g = load("hlbm_d2q9_f32_48x40x3")
-    prm, P, lat, ps, o, st = setup(g)
+    prm, P, lat, ps, o, st = setup(g, launch)
     ps.reset()
     ps.couple(prm)
     cf = ps.gather(prm, cell_force=True).astype(np.float64)
@@ -71,9 +74,10 @@ def test_hlbm_phases_vs_oracle():
     np.testing.assert_array_equal(u[fl].astype(np.float64), ou[fl])
 
 
-def test_hlbm_coupled_steps_vs_oracle():
+@pytest.mark.parametrize("launch", [None, (K.KEL_LAUNCH_ROWS, 4)], ids=["default", "rows"])
+def test_hlbm_coupled_steps_vs_oracle(launch):
     g = load("hlbm_d2q9_f32_48x40x3")
-    prm, P, lat, ps, o, st = setup(g)
+    prm, P, lat, ps, o, st = setup(g, launch)
     prog = K.make_program(P["tau"], K.KEL_COLL_HLBM, OPS, arithmetic=K.KEL_ARITH_REFERENCE)
     ps.step(prm, prog, 25)
     for _ in range(25):

@@ -119,7 +119,8 @@ def _periodic_bodies():
     return st
 
 
-def test_coupled_periodic_run_vs_oracle():
+@pytest.mark.parametrize("launch", [None, (K.KEL_LAUNCH_ROWS, 3)], ids=["default", "rows"])
+def test_coupled_periodic_run_vs_oracle(launch):
     """Config-3 shape in small: periodic x, walls in y, PSM + Guo gravity,
     bodies straddling the periodic seam, 40 coupled steps (reset, couple,
     gather, contact, integrate, sweep) against the oracle stepping the same."""
@@ -135,6 +136,8 @@ def test_coupled_periodic_run_vs_oracle():
                                  body_acceleration=(0.0, -1e-5), wall_axes=0b10)
     st0 = _periodic_bodies()
     lat = Lattice("D2Q9", dims, periodic_x=True)
+    if launch is not None:
+        lat.set_launch(*launch)
     lat.upload_flags(flags)
     ps = Particles(lat, st0)
     ps.step(prm, prog, 40)

@@ -21,13 +21,19 @@ FAST_TOL = 1e-5
 F32_NAMES = [n for n in G.names() if not n.endswith("_f64")]
 
 
-LAUNCHES = [(1, 256), (4, 256), (1, 64), (4, 128)]
+# (cells per thread, threads per block); (KEL_LAUNCH_ROWS, stages) is the row pipeline
+ROWS = K.KEL_LAUNCH_ROWS
+LAUNCHES = [(1, 256), (4, 256), (1, 64), (4, 128), (ROWS, 2), (ROWS, 4)]
 
 
-@pytest.mark.parametrize("launch", LAUNCHES, ids=lambda l: f"{l[0]}cell_{l[1]}thr")
+def launch_id(l):
+    return f"rows_{l[1]}stages" if l[0] == ROWS else f"{l[0]}cell_{l[1]}thr"
+
+
+@pytest.mark.parametrize("launch", LAUNCHES, ids=launch_id)
 @pytest.mark.parametrize("name", F32_NAMES)
 def test_reference_arithmetic_bit_exact(name, launch):
-    """Bit-exact for every launch shape (one or four cells per thread)."""
+    """Bit-exact for every launch shape (one or four cells per thread, row pipeline)."""
     case, dfs, rho, vel = G.load(name)
     f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE, launch=launch)
     np.testing.assert_array_equal(f, dfs)
@@ -35,22 +41,24 @@ def test_reference_arithmetic_bit_exact(name, launch):
     np.testing.assert_array_equal(v, vel)
 
 
+@pytest.mark.parametrize("launch", [None, (ROWS, 3)], ids=lambda l: "default" if l is None else launch_id(l))
 @pytest.mark.parametrize("name", F32_NAMES)
-def test_fast_arithmetic_within_1e5(name):
+def test_fast_arithmetic_within_1e5(name, launch):
     case, dfs, rho, vel = G.load(name)
-    f, r, v = run_gpu(case, K.KEL_ARITH_FAST)
+    f, r, v = run_gpu(case, K.KEL_ARITH_FAST, launch=launch)
     assert rel_l2(f, dfs) < FAST_TOL
     assert rel_l2(r, rho) < FAST_TOL
     assert rel_l2(v, vel) < FAST_TOL
     assert rel_err(v, vel) < 5 * FAST_TOL  # max-norm stays in the same range
 
 
+@pytest.mark.parametrize("launch", [None, (ROWS, 3)], ids=lambda l: "default" if l is None else launch_id(l))
 @pytest.mark.parametrize("chunks", [[1, 1, 1, 18], [2, 7, 12], [21]])
-def test_step_chunking_and_parity(chunks):
+def test_step_chunking_and_parity(chunks, launch):
     """Stepping 1, 2, 7 ... at a time (odd and even entry parities) gives the
     same bits as one call."""
     case, dfs, rho, vel = G.load("mixed3d_d3q19_guo")
-    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE, chunks=chunks)
+    f, r, v = run_gpu(case, K.KEL_ARITH_REFERENCE, chunks=chunks, launch=launch)
     np.testing.assert_array_equal(f, dfs)
 
 
@@ -71,7 +79,7 @@ def test_upload_at_odd_time_step():
     np.testing.assert_array_equal(b.populations(np.float64), ref)
 
 
-@pytest.mark.parametrize("launch", [(1, 256), (4, 256)], ids=lambda l: f"{l[0]}cell")
+@pytest.mark.parametrize("launch", [(1, 256), (4, 256), (ROWS, 3)], ids=launch_id)
 @pytest.mark.parametrize("q", [9, 27])
 def test_periodic_x_matches_oracle(q, launch):
     if q == 9:
@@ -84,7 +92,7 @@ def test_periodic_x_matches_oracle(q, launch):
     np.testing.assert_array_equal(v, ovel)
 
 
-@pytest.mark.parametrize("launch", [(1, 64), (4, 256)], ids=lambda l: f"{l[0]}cell")
+@pytest.mark.parametrize("launch", [(1, 64), (4, 256), (ROWS, 4)], ids=launch_id)
 @pytest.mark.parametrize("nx", [5, 37, 130, 131])
 def test_ragged_widths_match_oracle(nx, launch):
     """Row widths that are not multiples of 4 or of a warp's 128 cells."""
@@ -106,18 +114,34 @@ def test_config1_full_size_bit_exact():
     assert rel_l2(r2, rho) < FAST_TOL
 
 
+@pytest.mark.parametrize("launch", [None, (ROWS, 4)], ids=lambda l: "default" if l is None else launch_id(l))
 @pytest.mark.parametrize("q", [19, 27])
-def test_fp16s_velocity_error_vs_fp64(q):
+def test_fp16s_velocity_error_vs_fp64(q, launch):
     """FP16-shifted storage: relative L2 velocity error against the FP64 oracle
     of the same cavity below 1e-3."""
     case = cases.cavity_3d(q, dims=(32, 32, 32), steps=400)
     c64 = dict(case, f64=True)
     _, rho64, vel64 = cases.run_oracle(c64)
-    _, r16, v16 = run_gpu(case, K.KEL_ARITH_FAST, storage="fp16s")
+    _, r16, v16 = run_gpu(case, K.KEL_ARITH_FAST, storage="fp16s", launch=launch)
     err = np.linalg.norm(v16 - vel64) / np.linalg.norm(vel64)
     assert err < 1e-3, err
-    _, r32, v32 = run_gpu(case, K.KEL_ARITH_FAST, storage="fp32")
+    _, r32, v32 = run_gpu(case, K.KEL_ARITH_FAST, storage="fp32", launch=launch)
     assert np.linalg.norm(v32 - vel64) / np.linalg.norm(vel64) < 1e-4
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16s"])
+@pytest.mark.parametrize("q", [19, 27])
+def test_row_pipeline_same_bits_as_one_cell_sweep(q, storage):
+    """The row pipeline runs the same per-cell arithmetic as the one-cell
+    sweep: fast arithmetic, FP32 and FP16S storage, identical populations,
+    with rows of 72 cells (FP16S rows padded to 16 bytes) and
+    boundary rows in every direction."""
+    case = cases.cavity_3d(q, dims=(72, 20, 13), steps=31)
+    a = run_gpu(case, K.KEL_ARITH_FAST, storage=storage, launch=(1, 128))
+    for stages in (2, 3, 6):
+        b = run_gpu(case, K.KEL_ARITH_FAST, storage=storage, launch=(ROWS, stages))
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
 
 
 def test_closed_box_mass_conservation_and_determinism():
@@ -170,8 +194,15 @@ def test_invalid_arguments_return_errors():
     with pytest.raises(KelError):
         lat.set_launch(2, 256)
     with pytest.raises(KelError):
+        lat.set_launch(ROWS, 7)
+    with pytest.raises(KelError):
         lat.set_launch(1, 100)
+    lat.set_launch(ROWS, 2)
     lat.close()
+    wide = Lattice("D2Q9", (300, 4))  # rows longer than 256 cells: no row pipeline
+    with pytest.raises(KelError):
+        wide.set_launch(ROWS, 3)
+    wide.close()
 
 
 def test_autotune_restores_state_and_keeps_results():
@@ -182,7 +213,8 @@ def test_autotune_restores_state_and_keeps_results():
     before = lat.populations(np.float64)
     t = lat.t
     cpt, block, ms = lat.autotune(prog, steps=4)
-    assert (cpt, block) in [(1, 64), (1, 128), (1, 256), (4, 64), (4, 128), (4, 256)] and ms > 0
+    assert (cpt, block) in [(1, 64), (1, 128), (1, 256), (4, 64), (4, 128), (4, 256), (ROWS, 3), (ROWS, 4),
+                            (ROWS, 6)] and ms > 0
     assert lat.t == t and lat.launch() == (cpt, block)
     np.testing.assert_array_equal(lat.populations(np.float64), before)
     lat.step(prog, case["steps"] - 7)
