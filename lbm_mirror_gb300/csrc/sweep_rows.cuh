@@ -143,6 +143,10 @@ __global__ void __launch_bounds__(ROWS_MAX_NXP + 32, 2) sweep_rows_kernel(const 
 	const int64_t K = static_cast<int64_t>(blockIdx.x) < R ? (R - 1 - blockIdx.x) / G + 1 : 0;
 	ST *const f = static_cast<ST *>(p.f);
 
+	if (blockDim.x != static_cast<unsigned>(C + 32) || NS < 1 || NS > ROWS_MAX_STAGES) { // launch does not match the layout
+		if (tid == 0) atomicOr(p.err, 2u);
+		return;
+	}
 	if (tid == 0) {
 		for (int s = 0; s < NS; ++s) {
 			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(rows_saddr(full + s)));
