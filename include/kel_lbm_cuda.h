@@ -337,9 +337,10 @@ int kel_unet_adam_step(kel_unet *net, float lr, float beta1, float beta2, float 
 #define KEL_UNET_CONV_MMA_SYNC 1
 int kel_unet_set_conv_kernel(kel_unet *net, int32_t kind);
 
-/* Launch shape of the sweep: cells per thread (1: 32-bit accesses, one cell;
- * 4: 128-bit accesses, four consecutive cells) and threads per block (64, 128
- * or 256); or KEL_LAUNCH_ROWS with block_threads = row stages (2-6): the row
+/* Launch shape of the sweep: cells per thread (1: one cell, 32-bit FP32 /
+ * 16-bit FP16S accesses; 2: two consecutive cells, 64-bit / 32-bit accesses;
+ * 4: four consecutive cells, 128-bit / 64-bit accesses) and threads per block
+ * (64, 128 or 256); or KEL_LAUNCH_ROWS with block_threads = row stages (2-6): the row
  * pipeline, one thread per cell of a row, whole rows moved between HBM and
  * shared memory by bulk asynchronous copies, for rows of at most 256 cells
  * whose padded length is a multiple of 16 bytes (KEL_ERR_INVALID_ARGUMENT
@@ -347,7 +348,7 @@ int kel_unet_set_conv_kernel(kel_unet *net, int32_t kind);
  * gives up on its bounded wait for a row copy, the next
  * kel_lattice_synchronize / kel_download_populations / kel_download_macros
  * returns KEL_ERR_TIMEOUT. */
-#define KEL_LAUNCH_ROWS 2
+#define KEL_LAUNCH_ROWS (-1)
 int kel_lattice_set_launch(kel_lattice *lat, int32_t cells_per_thread, int32_t block_threads);
 int kel_lattice_get_launch(const kel_lattice *lat, int32_t *cells_per_thread, int32_t *block_threads);
 /* Time `steps` sweeps of `prog` with every launch shape on the lattice's

@@ -29,7 +29,7 @@ KEL_D2Q9, KEL_D3Q19, KEL_D3Q27 = 9, 19, 27
 KEL_STORAGE_FP32, KEL_STORAGE_FP16S = 0, 1
 KEL_LATTICE_PERIODIC_X = 1
 # kel_lattice_set_launch: cells_per_thread value of the row pipeline (block_threads = row stages)
-KEL_LAUNCH_ROWS = 2
+KEL_LAUNCH_ROWS = -1
 
 # ---- boundary ops (values of kel_flag_op.bc) -------------------------------
 KEL_BC_NONE = 0

@@ -15,16 +15,11 @@
 #include <vector>
 
 #include "lattice_internal.cuh"
+#include "sweep_dispatch.cuh"
 #include "sweep_rows.cuh"
 
 using namespace kel::gb;
 
-namespace kel {
-namespace gb {
-template <class L>
-cudaError_t launch_sweep(const SweepParams &p, int storage, bool odd, int coll, bool exact, cudaStream_t st);
-} // namespace gb
-} // namespace kel
 
 // ---------------------------------------------------------------------------
 // errors
@@ -753,14 +748,14 @@ static cudaError_t launch_one(const kel_lattice *L, const SweepParams &p, int co
 }
 
 static bool launch_ok(const kel_lattice *L, int cpt, int block) {
-	if (cpt == 2) { // row pipeline: block = row stages
+	if (cpt == CPT_ROWS) { // row pipeline: block = row stages
 		if (block < 2 || block > ROWS_MAX_STAGES) return false;
 		if (L->nxp > ROWS_MAX_NXP || ((int64_t)L->nxp * (int64_t)L->elem) % 16 != 0) return false;
 		int optin = 0;
 		if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, L->device) != cudaSuccess) return false;
 		return rows_smem_bytes(L->d.Q, L->nxp, (int)L->elem, block) <= optin;
 	}
-	if (cpt != 1 && cpt != 4) return false;
+	if (cpt != 1 && cpt != 2 && cpt != 4) return false;
 	if (block != 64 && block != 128 && block != 256) return false;
 	if (cpt == 1 && (L->desc.ny > 65535 || L->desc.nz > 65535)) return false;
 	return true;
@@ -818,6 +813,7 @@ static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	p.nz = (int)L->desc.nz;
 	p.nq = L->nq;
 	p.wpr = L->wpr;
+	p.wpr2 = (L->nxp / 2 + 31) / 32;
 	p.periodic = (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0;
 	const float tau = (float)P->tau;
 	p.omega = 1.0f / tau;
@@ -827,10 +823,10 @@ static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	p.cpt = L->cpt;
 	p.idx32 = (int64_t)L->d.Q * L->plane < ((int64_t)1 << 31) ? 1 : 0;
 	p.block = L->block;
-	p.stages = L->cpt == 2 ? L->block : 0;
+	p.stages = L->cpt == CPT_ROWS ? L->block : 0;
 	p.sms = L->sms;
 	p.err = L->d_err;
-	if (L->cpt == 2) L->rows_used = true;
+	if (L->cpt == CPT_ROWS) L->rows_used = true;
 	return p;
 }
 
@@ -850,19 +846,21 @@ extern "C" int kel_lattice_autotune(kel_lattice *L, const kel_step_program *P, i
 	cudaEvent_t e0, e1;
 	cudaEventCreate(&e0);
 	cudaEventCreate(&e1);
-	const int cands[9][2] = {{1, 64}, {1, 128}, {1, 256}, {4, 64}, {4, 128}, {4, 256}, {2, 3}, {2, 4}, {2, 6}};
+	const int cands[][2] = {{1, 64},  {1, 128}, {1, 256}, {2, 64},        {2, 128},       {2, 256},
+	                        {4, 64},  {4, 128}, {4, 256}, {CPT_ROWS, 3}, {CPT_ROWS, 4}, {CPT_ROWS, 6}};
+	const int ncand = (int)(sizeof(cands) / sizeof(cands[0]));
 	float best = 1e30f;
 	int bc = L->cpt, bb = L->block;
 	cudaError_t e = cudaMemcpyAsync(save, L->f, bytes, cudaMemcpyDeviceToDevice, L->stream);
 	SweepParams p = make_params(L, P);
 	p.write_macros = 0;
 	const bool exact = P->arithmetic == KEL_ARITH_REFERENCE;
-	for (int k = 0; k < 9 && e == cudaSuccess; ++k) {
+	for (int k = 0; k < ncand && e == cudaSuccess; ++k) {
 		if (!launch_ok(L, cands[k][0], cands[k][1])) continue;
 		p.cpt = cands[k][0];
 		p.block = cands[k][1];
-		p.stages = p.cpt == 2 ? p.block : 0;
-		if (p.cpt == 2) L->rows_used = true;
+		p.stages = p.cpt == CPT_ROWS ? p.block : 0;
+		if (p.cpt == CPT_ROWS) L->rows_used = true;
 		const bool odd0 = (L->t & 1u) != 0;
 		for (int s = 0; s < 2 && e == cudaSuccess; ++s) e = launch_one(L, p, P->collision, exact, odd0 != (s & 1));
 		cudaEventRecord(e0, L->stream);

@@ -45,6 +45,7 @@ enum : int {
 	BC_EQUILIBRIUM = 7
 };
 constexpr int MAX_FLAGS = 8;
+constexpr int CPT_ROWS = -1; // launch shape of the row pipeline (KEL_LAUNCH_ROWS)
 
 // Per-flag operation, resident in device memory (read through the read-only path).
 struct OpEntry {
@@ -76,9 +77,10 @@ struct SweepParams {
 	float guo_scale;  // 1 - 0.5 * omega
 	float g[3];       // global force
 	float wshift[27]; // FP16S: stored value is f - wshift[i]
-	int cpt;          // cells per thread: 4 (sweep_kernel), 1 (sweep1_kernel), 2 (sweep_rows_kernel)
+	int cpt;          // cells per thread: 1 (sweep1_kernel), 2 (sweep2_kernel), 4 (sweep_kernel), CPT_ROWS (sweep_rows_kernel)
 	int idx32;        // Q * plane < 2^31: offsets from a cell fit 32-bit arithmetic
 	int block;        // threads per block
+	int wpr2;         // sweep2_kernel: warps per row (32 cell pairs per warp)
 	int stages;       // sweep_rows_kernel: row stages in shared memory
 	int sms;          // multiprocessors of the device (persistent grid of sweep_rows_kernel)
 	unsigned *err;    // sweep_rows_kernel: set to 1 when a bounded wait gave up
@@ -148,6 +150,12 @@ struct Store<STORE_FP32> {
 	__device__ static __forceinline__ void st1(void *base, int64_t idx, float v, float) {
 		__stcs(static_cast<float *>(base) + idx, v);
 	}
+	__device__ static __forceinline__ float2 ld2(const void *base, int64_t idx, float) {
+		return __ldcs(reinterpret_cast<const float2 *>(static_cast<const float *>(base) + idx));
+	}
+	__device__ static __forceinline__ void st2(void *base, int64_t idx, float2 v, float) {
+		__stcs(reinterpret_cast<float2 *>(static_cast<float *>(base) + idx), v);
+	}
 };
 
 template <>
@@ -173,6 +181,15 @@ struct Store<STORE_FP16S> {
 	}
 	__device__ static __forceinline__ void st1(void *base, int64_t idx, float v, float s) {
 		static_cast<__half *>(base)[idx] = __float2half_rn(v - s);
+	}
+	__device__ static __forceinline__ float2 ld2(const void *base, int64_t idx, float s) {
+		unsigned r = __ldcs(reinterpret_cast<const unsigned *>(static_cast<const __half *>(base) + idx));
+		const float2 v = __half22float2(*reinterpret_cast<__half2 *>(&r));
+		return make_float2(v.x + s, v.y + s);
+	}
+	__device__ static __forceinline__ void st2(void *base, int64_t idx, float2 v, float s) {
+		__half2 h = __floats2half2_rn(v.x - s, v.y - s);
+		__stcs(reinterpret_cast<unsigned *>(static_cast<__half *>(base) + idx), *reinterpret_cast<unsigned *>(&h));
 	}
 };
 
@@ -661,6 +678,180 @@ __global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ Swee
 						S::st1(p.f, db + x0 + 1, f[i][2], s);
 						S::st1(p.f, db + x0 + 2, f[i][3], s);
 					}
+					if (x0 > 0) {
+						if (lane == 0) S::st1(p.f, db + x0 - 1, f[i][0], s);
+					} else if (p.periodic) {
+						S::st1(p.f, db + nxp - 1, f[i][0], s);
+					}
+				}
+			}
+		}
+	}
+}
+
+
+// Two consecutive cells per thread (x0 = 2 * pair), 64-bit FP32 / 32-bit
+// FP16S accesses: half the load/store instructions of the one-cell sweep and,
+// in FP16S, one register per population pair in flight.  A warp covers 32
+// pairs of one row; the x-shifted accesses of odd steps are realigned with
+// one warp shuffle per direction, and only the lanes at a warp's or row's end
+// touch the neighbouring pair with a scalar access (as sweep_kernel does
+// with four cells).
+template <class L, int STORE, bool ODD, int COLL, bool EXACT>
+__global__ void __launch_bounds__(256) sweep2_kernel(const __grid_constant__ SweepParams p) {
+	using S = Store<STORE>;
+	constexpr int Q = L::Q;
+	const int lane = threadIdx.x & 31;
+	const int64_t gwarp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+	const int64_t row = gwarp / p.wpr2;
+	const int64_t nrows = static_cast<int64_t>(p.ny) * p.nz;
+	if (row >= nrows) return; // warp-uniform: a warp never spans rows
+	const int nxp = p.nxp;
+	const int pr = static_cast<int>(gwarp % p.wpr2) * 32 + lane;
+	const bool active = 2 * pr < nxp;
+	const int x0 = 2 * pr;
+	const int y = static_cast<int>(row % p.ny);
+	const int z = static_cast<int>(row / p.ny);
+	const int64_t rbase = row * nxp; // first cell of this row
+	const unsigned FULL = 0xffffffffu;
+
+	float f[Q][2];
+
+	// ---- gather the post-stream populations f_i of the 2 cells -------------
+#pragma unroll
+	for (int i = 0; i < Q; ++i) {
+		const float s = p.wshift[i];
+		if (!ODD) {
+			const float2 v = active ? S::ld2(p.f, i * p.plane + rbase + x0, s) : make_float2(0.f, 0.f);
+			f[i][0] = v.x;
+			f[i][1] = v.y;
+		} else {
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int sy = y - cy, sz = z - cz;
+			const bool row_in = (sy >= 0) && (sy < p.ny) && (sz >= 0) && (sz < p.nz);
+			const int64_t sb = static_cast<int64_t>(L::opp(i)) * p.plane + (static_cast<int64_t>(sz) * p.ny + sy) * nxp;
+			float2 v = make_float2(0.f, 0.f);
+			if (row_in && active) v = S::ld2(p.f, sb + x0, s);
+			if (cx == 0) {
+				f[i][0] = v.x;
+				f[i][1] = v.y;
+			} else if (cx > 0) { // source x - 1
+				float prev = __shfl_up_sync(FULL, v.y, 1);
+				if (lane == 0 || x0 == 0) {
+					prev = 0.f;
+					if (row_in && active) {
+						if (x0 > 0) prev = S::ld1(p.f, sb + x0 - 1, s);
+						else if (p.periodic) prev = S::ld1(p.f, sb + nxp - 1, s);
+					}
+				}
+				f[i][0] = prev;
+				f[i][1] = v.x;
+			} else { // source x + 1
+				float next = __shfl_down_sync(FULL, v.x, 1);
+				if (lane == 31 || x0 + 2 >= nxp) {
+					next = 0.f;
+					if (row_in && active) {
+						if (x0 + 2 < nxp) next = S::ld1(p.f, sb + x0 + 2, s);
+						else if (p.periodic) next = S::ld1(p.f, sb, s);
+					}
+				}
+				f[i][0] = v.y;
+				f[i][1] = next;
+			}
+		}
+	}
+
+	// ---- boundary step + collision per cell ---------------------------------
+	uchar2 fl = make_uchar2(0, 0);
+	if (active) fl = *reinterpret_cast<const uchar2 *>(p.flags + rbase + x0);
+	float2 porv = make_float2(1.f, 1.f);
+	if ((COLL == COLL_PSM || COLL == COLL_PSM_GUO || COLL == COLL_HLBM) && active)
+		porv = *reinterpret_cast<const float2 *>(p.por + rbase + x0);
+	float2 fcv[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+	if ((COLL == COLL_BGK_GUO || COLL == COLL_PSM_GUO) && active) {
+#pragma unroll
+		for (int k = 0; k < L::D; ++k) fcv[k] = *reinterpret_cast<const float2 *>(p.force + k * p.plane + rbase + x0);
+	}
+	if (COLL == COLL_HLBM && active) {
+		fcv[0] = *reinterpret_cast<const float2 *>(p.hN + rbase + x0);
+		fcv[1] = *reinterpret_cast<const float2 *>(p.hN + p.plane + rbase + x0);
+		fcv[2] = *reinterpret_cast<const float2 *>(p.hD + rbase + x0);
+	}
+	const CellCtx ctx = cell_ctx(p);
+	float2 rho2 = make_float2(0.f, 0.f);
+	float2 u2[3] = {rho2, rho2, rho2};
+	int collided = 0;
+#pragma unroll
+	for (int k = 0; k < 2; ++k) {
+		const int flag = k == 0 ? fl.x : fl.y;
+		float c[Q];
+#pragma unroll
+		for (int i = 0; i < Q; ++i) c[i] = f[i][k];
+		float Fc[3] = {k ? fcv[0].y : fcv[0].x, k ? fcv[1].y : fcv[1].x, k ? fcv[2].y : fcv[2].x};
+		float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
+		const bool col = cell_update<L, COLL, EXACT>(c, flag, y, ctx, k ? porv.y : porv.x, Fc, rho, u);
+		collided |= (col ? 1 : 0) << k;
+		if (k == 0) { rho2.x = rho; u2[0].x = u[0]; u2[1].x = u[1]; u2[2].x = u[2]; }
+		else { rho2.y = rho; u2[0].y = u[0]; u2[1].y = u[1]; u2[2].y = u[2]; }
+#pragma unroll
+		for (int i = 0; i < Q; ++i) f[i][k] = c[i];
+	}
+
+	// ---- macros of collided cells (collision.hpp:83-89) ---------------------
+	if (p.write_macros && active && collided) {
+		if (collided == 3) {
+			*reinterpret_cast<float2 *>(p.rho + rbase + x0) = rho2;
+#pragma unroll
+			for (int k = 0; k < L::D; ++k) *reinterpret_cast<float2 *>(p.u + k * p.plane + rbase + x0) = u2[k];
+		} else {
+			const int k = collided == 1 ? 0 : 1;
+			p.rho[rbase + x0 + k] = k ? rho2.y : rho2.x;
+#pragma unroll
+			for (int d = 0; d < L::D; ++d) p.u[d * p.plane + rbase + x0 + k] = k ? u2[d].y : u2[d].x;
+		}
+	}
+
+	// ---- scatter the post-collision populations -----------------------------
+#pragma unroll
+	for (int i = 0; i < Q; ++i) {
+		const float s = p.wshift[i];
+		if (!ODD) {
+			if (active) S::st2(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + rbase + x0, make_float2(f[i][0], f[i][1]), s);
+		} else {
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int64_t pb = static_cast<int64_t>(i) * p.plane;
+			// slots of this row whose source lies outside: the ghost ring's zero
+			{
+				const int sy = y - cy, sz = z - cz;
+				const bool src_row_in = (sy >= 0) && (sy < p.ny) && (sz >= 0) && (sz < p.nz);
+				if (!src_row_in) {
+					if (active) S::st2(p.f, pb + rbase + x0, make_float2(0.f, 0.f), s);
+				} else if (!p.periodic && active) {
+					if (cx > 0 && x0 == 0) S::st1(p.f, pb + rbase, 0.f, s);
+					if (cx < 0 && x0 + 2 == nxp) S::st1(p.f, pb + rbase + nxp - 1, 0.f, s);
+				}
+			}
+			const int dy = y + cy, dz = z + cz;
+			const bool row_in = (dy >= 0) && (dy < p.ny) && (dz >= 0) && (dz < p.nz);
+			const int64_t db = pb + (static_cast<int64_t>(dz) * p.ny + dy) * nxp;
+			if (cx == 0) {
+				if (row_in && active) S::st2(p.f, db + x0, make_float2(f[i][0], f[i][1]), s);
+			} else if (cx > 0) { // destination x + 1
+				const float q = __shfl_up_sync(FULL, f[i][1], 1);
+				if (row_in && active) {
+					if (lane > 0) S::st2(p.f, db + x0, make_float2(q, f[i][0]), s);
+					else S::st1(p.f, db + x0 + 1, f[i][0], s); // element x0: previous warp, or the ghost slot
+					if (x0 + 2 < nxp) {
+						if (lane == 31) S::st1(p.f, db + x0 + 2, f[i][1], s);
+					} else if (p.periodic) {
+						S::st1(p.f, db, f[i][1], s);
+					}
+				}
+			} else { // destination x - 1
+				const float r = __shfl_down_sync(FULL, f[i][0], 1);
+				if (row_in && active) {
+					if (lane < 31 && x0 + 2 < nxp) S::st2(p.f, db + x0, make_float2(f[i][1], r), s);
+					else S::st1(p.f, db + x0, f[i][1], s); // element x0 + 1: next warp, or the ghost slot
 					if (x0 > 0) {
 						if (lane == 0) S::st1(p.f, db + x0 - 1, f[i][0], s);
 					} else if (p.periodic) {

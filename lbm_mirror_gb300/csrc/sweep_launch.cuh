@@ -1,6 +1,6 @@
-// Instantiation and launch of the sweep kernel for one descriptor; included
-// once per descriptor translation unit (sweep_d2q9.cu, sweep_d3q19.cu,
-// sweep_d3q27.cu) so the three compile in parallel.
+// Launch of the sweep kernels; included by the nine translation units
+// sweep_<descriptor>_<fast|exact|fp16s>.cu, each of which instantiates one
+// part (sweep_dispatch.cuh picks the part at run time).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -9,6 +9,7 @@
 #include <cstdint>
 
 #include "sweep.cuh"
+#include "sweep_dispatch.cuh"
 #include "sweep_rows.cuh"
 
 namespace kel {
@@ -56,7 +57,13 @@ static cudaError_t launch_rows(const SweepParams &p, cudaStream_t st) {
 template <class L, int STORE, bool ODD, int COLL, bool EXACT>
 static cudaError_t launch_variant(const SweepParams &p, cudaStream_t st) {
 	const int block = p.block > 0 ? p.block : 256;
-	if (p.cpt == 2) return launch_rows<L, STORE, ODD, COLL, EXACT>(p, st);
+	if (p.cpt == CPT_ROWS) return launch_rows<L, STORE, ODD, COLL, EXACT>(p, st);
+	if (p.cpt == 2) {
+		const int64_t threads = static_cast<int64_t>(p.ny) * p.nz * p.wpr2 * 32;
+		const int64_t blocks = (threads + block - 1) / block;
+		sweep2_kernel<L, STORE, ODD, COLL, EXACT><<<static_cast<unsigned>(blocks), block, 0, st>>>(p);
+		return cudaGetLastError();
+	}
 	if constexpr (COLL == COLL_HLBM) { // one cell per thread only
 		dim3 grid((p.nxp + block - 1) / block, p.ny, p.nz);
 		sweep1_kernel<L, STORE, ODD, COLL, EXACT><<<grid, block, 0, st>>>(p);
@@ -85,17 +92,17 @@ static cudaError_t launch_coll(const SweepParams &p, int coll, cudaStream_t st) 
 	return cudaErrorInvalidValue;
 }
 
-template <class L>
-cudaError_t launch_sweep(const SweepParams &p, int storage, bool odd, int coll, bool exact, cudaStream_t st) {
-	if (storage == STORE_FP32) {
-		if (exact) return odd ? launch_coll<L, STORE_FP32, true, true>(p, coll, st)
-							  : launch_coll<L, STORE_FP32, false, true>(p, coll, st);
-		return odd ? launch_coll<L, STORE_FP32, true, false>(p, coll, st)
-				   : launch_coll<L, STORE_FP32, false, false>(p, coll, st);
-	}
-	if (exact) return cudaErrorInvalidValue;
-	return odd ? launch_coll<L, STORE_FP16S, true, false>(p, coll, st)
-			   : launch_coll<L, STORE_FP16S, false, false>(p, coll, st);
+// One part of the variant set (the translation units compile one part each,
+// in parallel): FP32 fast arithmetic, FP32 reference arithmetic, FP16S.
+template <class L, int PART>
+cudaError_t launch_sweep_part(const SweepParams &p, bool odd, int coll, cudaStream_t st) {
+	if constexpr (PART == PART_FAST32)
+		return odd ? launch_coll<L, STORE_FP32, true, false>(p, coll, st) : launch_coll<L, STORE_FP32, false, false>(p, coll, st);
+	else if constexpr (PART == PART_EXACT32)
+		return odd ? launch_coll<L, STORE_FP32, true, true>(p, coll, st) : launch_coll<L, STORE_FP32, false, true>(p, coll, st);
+	else
+		return odd ? launch_coll<L, STORE_FP16S, true, false>(p, coll, st)
+				   : launch_coll<L, STORE_FP16S, false, false>(p, coll, st);
 }
 
 } // namespace gb

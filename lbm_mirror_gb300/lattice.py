@@ -292,7 +292,7 @@ class Lattice:
         _check(self.lib.kel_lattice_load(self._h, str(path).encode()), self.lib)
 
     def set_launch(self, cells_per_thread, block_threads=256):
-        """Sweep launch shape: (1 or 4 cells per thread, 64/128/256 threads per
+        """Sweep launch shape: (1, 2 or 4 cells per thread, 64/128/256 threads per
         block), or (KEL_LAUNCH_ROWS, row stages 2-6) for the row pipeline."""
         _check(self.lib.kel_lattice_set_launch(self._h, cells_per_thread, block_threads), self.lib)
 

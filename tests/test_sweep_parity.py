@@ -23,7 +23,7 @@ F32_NAMES = [n for n in G.names() if not n.endswith("_f64")]
 
 # (cells per thread, threads per block); (KEL_LAUNCH_ROWS, stages) is the row pipeline
 ROWS = K.KEL_LAUNCH_ROWS
-LAUNCHES = [(1, 256), (4, 256), (1, 64), (4, 128), (ROWS, 2), (ROWS, 4)]
+LAUNCHES = [(1, 256), (2, 256), (4, 256), (1, 64), (2, 64), (4, 128), (ROWS, 2), (ROWS, 4)]
 
 
 def launch_id(l):
@@ -79,7 +79,7 @@ def test_upload_at_odd_time_step():
     np.testing.assert_array_equal(b.populations(np.float64), ref)
 
 
-@pytest.mark.parametrize("launch", [(1, 256), (4, 256), (ROWS, 3)], ids=launch_id)
+@pytest.mark.parametrize("launch", [(1, 256), (2, 128), (4, 256), (ROWS, 3)], ids=launch_id)
 @pytest.mark.parametrize("q", [9, 27])
 def test_periodic_x_matches_oracle(q, launch):
     if q == 9:
@@ -92,7 +92,7 @@ def test_periodic_x_matches_oracle(q, launch):
     np.testing.assert_array_equal(v, ovel)
 
 
-@pytest.mark.parametrize("launch", [(1, 64), (4, 256), (ROWS, 4)], ids=launch_id)
+@pytest.mark.parametrize("launch", [(1, 64), (2, 64), (4, 256), (ROWS, 4)], ids=launch_id)
 @pytest.mark.parametrize("nx", [5, 37, 130, 131])
 def test_ragged_widths_match_oracle(nx, launch):
     """Row widths that are not multiples of 4 or of a warp's 128 cells."""
@@ -114,7 +114,7 @@ def test_config1_full_size_bit_exact():
     assert rel_l2(r2, rho) < FAST_TOL
 
 
-@pytest.mark.parametrize("launch", [None, (ROWS, 4)], ids=lambda l: "default" if l is None else launch_id(l))
+@pytest.mark.parametrize("launch", [None, (2, 128), (ROWS, 4)], ids=lambda l: "default" if l is None else launch_id(l))
 @pytest.mark.parametrize("q", [19, 27])
 def test_fp16s_velocity_error_vs_fp64(q, launch):
     """FP16-shifted storage: relative L2 velocity error against the FP64 oracle
@@ -131,15 +131,16 @@ def test_fp16s_velocity_error_vs_fp64(q, launch):
 
 @pytest.mark.parametrize("storage", ["fp32", "fp16s"])
 @pytest.mark.parametrize("q", [19, 27])
-def test_row_pipeline_same_bits_as_one_cell_sweep(q, storage):
-    """The row pipeline runs the same per-cell arithmetic as the one-cell
-    sweep: fast arithmetic, FP32 and FP16S storage, identical populations,
+def test_row_pipeline_and_two_cell_sweep_same_bits_as_one_cell_sweep(q, storage):
+    """The row pipeline and the two-cell sweep run the same per-cell
+    arithmetic as the one-cell sweep: fast arithmetic, FP32 and FP16S
+    storage, identical populations,
     with rows of 72 cells (FP16S rows padded to 16 bytes) and
     boundary rows in every direction."""
     case = cases.cavity_3d(q, dims=(72, 20, 13), steps=31)
     a = run_gpu(case, K.KEL_ARITH_FAST, storage=storage, launch=(1, 128))
-    for stages in (2, 3, 6):
-        b = run_gpu(case, K.KEL_ARITH_FAST, storage=storage, launch=(ROWS, stages))
+    for launch in [(ROWS, 2), (ROWS, 3), (ROWS, 6), (2, 64), (2, 256)]:
+        b = run_gpu(case, K.KEL_ARITH_FAST, storage=storage, launch=launch)
         for x, y in zip(a, b):
             np.testing.assert_array_equal(x, y)
 
@@ -192,7 +193,7 @@ def test_invalid_arguments_return_errors():
     with pytest.raises(KelError):
         lat.step(K.make_program(-1.0), 1)
     with pytest.raises(KelError):
-        lat.set_launch(2, 256)
+        lat.set_launch(3, 256)
     with pytest.raises(KelError):
         lat.set_launch(ROWS, 7)
     with pytest.raises(KelError):
@@ -213,8 +214,8 @@ def test_autotune_restores_state_and_keeps_results():
     before = lat.populations(np.float64)
     t = lat.t
     cpt, block, ms = lat.autotune(prog, steps=4)
-    assert (cpt, block) in [(1, 64), (1, 128), (1, 256), (4, 64), (4, 128), (4, 256), (ROWS, 3), (ROWS, 4),
-                            (ROWS, 6)] and ms > 0
+    assert (cpt, block) in [(1, 64), (1, 128), (1, 256), (2, 64), (2, 128), (2, 256), (4, 64), (4, 128), (4, 256),
+                            (ROWS, 3), (ROWS, 4), (ROWS, 6)] and ms > 0
     assert lat.t == t and lat.launch() == (cpt, block)
     np.testing.assert_array_equal(lat.populations(np.float64), before)
     lat.step(prog, case["steps"] - 7)
