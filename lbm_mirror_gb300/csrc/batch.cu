@@ -8,7 +8,8 @@
 //   - populations: 9 planes over the packed cells of every channel; channel c
 //     owns [off_c, off_c + nxp_c * ny_c), padded up to whole tiles;
 //   - one tile (= one thread block, `tile` cells, one cell per thread) never
-//     spans two channels: block b reads its channel from block_ch[b];
+//     spans two channels: a launched block reads its (tile, channel) pair
+//     from the launch list;
 //   - per-channel relaxation rate and parabolic inlet profile come from the
 //     channel table; the flag -> operation table is shared.
 // Steps run as a captured CUDA graph of `check_every` sweeps followed by the
@@ -46,12 +47,13 @@ struct BatchParams {
 	const float *profiles;
 	const ChannelRec *ch;
 	const int *block_ch;
-	const int *blist; // launched block -> tile (all tiles, or those of active channels)
+	const int2 *blist; // launched block -> (tile, channel): all tiles, or those of active channels
 	int *active;
 	double2 *partial; // per-tile residual partial sums (scratch)
 	int tile;
 	int write_macros;
 	int shifted; // populations hold g = f - w_i (MODE_SHIFTED)
+	int idx32;   // 9 * plane < 2^31: population offsets from a cell fit 32-bit arithmetic
 };
 
 // Arithmetic of a batch: the library's two (fast, reference rounding) on
@@ -165,23 +167,34 @@ __device__ __forceinline__ bool cell_update_shifted(float (&g)[9], int flag, int
 template <bool ODD, int MODE>
 __global__ void __launch_bounds__(512) k_batch_sweep(const __grid_constant__ BatchParams p) {
 	using L = D2Q9;
-	const int ob = p.blist[blockIdx.x];
-	const int c = p.block_ch[ob];
+	const int2 tc = p.blist[blockIdx.x]; // (tile, channel)
+	const int ob = tc.x, c = tc.y;
 	if (!p.active[c]) return;
 	const ChannelRec ch = p.ch[c];
 	const int l = (ob - ch.first_block) * blockDim.x + threadIdx.x;
 	if (l >= ch.nxp * ch.ny) return;
 	const int y = l / ch.nxp, x = l - y * ch.nxp;
 	const int64_t cell = ch.off + l;
+	// interior cells: every neighbour inside the channel, offsets from the
+	// cell in 32-bit arithmetic
+	const bool fast = p.idx32 && x > 0 && x + 1 < ch.nxp && y > 0 && y + 1 < ch.ny;
+	const float *const fc = p.f + cell;
+	const int pl32 = static_cast<int>(p.plane), nxp = ch.nxp;
 	float f[9];
+	if (fast) {
 #pragma unroll
-	for (int i = 0; i < 9; ++i) {
-		if (!ODD) {
-			f[i] = __ldcs(p.f + i * p.plane + cell);
-		} else {
-			const int sx = x - L::cx(i), sy = y - L::cy(i);
-			const bool in = sx >= 0 && sx < ch.nxp && sy >= 0 && sy < ch.ny;
-			f[i] = in ? __ldcs(p.f + L::opp(i) * p.plane + ch.off + sy * ch.nxp + sx) : 0.f;
+		for (int i = 0; i < 9; ++i)
+			f[i] = ODD ? __ldcs(fc + (L::opp(i) * pl32 - L::cx(i) - L::cy(i) * nxp)) : __ldcs(fc + i * pl32);
+	} else {
+#pragma unroll
+		for (int i = 0; i < 9; ++i) {
+			if (!ODD) {
+				f[i] = __ldcs(p.f + i * p.plane + cell);
+			} else {
+				const int sx = x - L::cx(i), sy = y - L::cy(i);
+				const bool in = sx >= 0 && sx < ch.nxp && sy >= 0 && sy < ch.ny;
+				f[i] = in ? __ldcs(p.f + L::opp(i) * p.plane + ch.off + sy * ch.nxp + sx) : 0.f;
+			}
 		}
 	}
 	CellCtx ctx;
@@ -199,6 +212,13 @@ __global__ void __launch_bounds__(512) k_batch_sweep(const __grid_constant__ Bat
 		p.rho[cell] = rho;
 		p.u[cell] = u[0];
 		p.u[p.plane + cell] = u[1];
+	}
+	float *const fw = p.f + cell;
+	if (fast) {
+#pragma unroll
+		for (int i = 0; i < 9; ++i)
+			__stcs(fw + (ODD ? i * pl32 + L::cx(i) + L::cy(i) * nxp : L::opp(i) * pl32), f[i]);
+		return;
 	}
 #pragma unroll
 	for (int i = 0; i < 9; ++i) {
@@ -218,8 +238,8 @@ __global__ void __launch_bounds__(512) k_batch_sweep(const __grid_constant__ Bat
 // u_prev = u.  Fixed reduction order (warp shuffle, then warps in order).
 __global__ void __launch_bounds__(512) k_batch_residual_partial(BatchParams p) {
 	__shared__ double sh[2][16];
-	const int ob = p.blist[blockIdx.x];
-	const int c = p.block_ch[ob];
+	const int2 tc = p.blist[blockIdx.x];
+	const int ob = tc.x, c = tc.y;
 	double num = 0.0, den = 0.0;
 	if (p.active[c]) {
 		const ChannelRec ch = p.ch[c];
@@ -423,7 +443,7 @@ struct kel_batch {
 	std::vector<kel_channel_desc> desc;
 	std::vector<ChannelRec> rec;
 	std::vector<int> block_ch;
-	std::vector<int> blist; // launched tiles (host copy of d_blist)
+	std::vector<int2> blist; // launched (tile, channel) pairs (host copy of d_blist)
 	int nlaunch = 0;        // tiles launched per sweep
 	std::vector<uint64_t> t;          // per-channel time step
 	std::vector<uint8_t> host_flags;  // packed copy (kept for re-layout)
@@ -435,7 +455,8 @@ struct kel_batch {
 	float *f = nullptr, *rho = nullptr, *u = nullptr, *u_prev = nullptr, *profiles = nullptr;
 	uint8_t *flags = nullptr;
 	ChannelRec *d_rec = nullptr;
-	int *d_block_ch = nullptr, *d_active = nullptr, *d_blist = nullptr;
+	int *d_block_ch = nullptr, *d_active = nullptr;
+	int2 *d_blist = nullptr;
 	double2 *partial = nullptr;
 	double *d_residual = nullptr;
 	OpEntry *ops = nullptr;
@@ -468,7 +489,8 @@ void free_device(kel_batch *B) {
 	B->f = B->rho = B->u = B->u_prev = B->profiles = nullptr;
 	B->flags = nullptr;
 	B->d_rec = nullptr;
-	B->d_block_ch = B->d_active = B->d_blist = nullptr;
+	B->d_block_ch = B->d_active = nullptr;
+	B->d_blist = nullptr;
 	B->partial = nullptr;
 	B->d_residual = nullptr;
 	if (B->graph) cudaGraphExecDestroy(B->graph);
@@ -494,6 +516,7 @@ BatchParams params(const kel_batch *B, int write_macros) {
 	p.tile = B->tile;
 	p.write_macros = write_macros;
 	p.shifted = B->shifted ? 1 : 0;
+	p.idx32 = 9 * B->plane < ((int64_t)1 << 31) ? 1 : 0;
 	return p;
 }
 
@@ -533,11 +556,11 @@ int layout(kel_batch *B, int tile) {
 	KEL_CUDA(cudaMalloc(&B->flags, B->plane));
 	KEL_CUDA(cudaMalloc(&B->d_rec, sizeof(ChannelRec) * B->n));
 	KEL_CUDA(cudaMalloc(&B->d_block_ch, sizeof(int) * B->nblocks));
-	KEL_CUDA(cudaMalloc(&B->d_blist, sizeof(int) * B->nblocks));
+	KEL_CUDA(cudaMalloc(&B->d_blist, sizeof(int2) * B->nblocks));
 	B->blist.resize(B->nblocks);
-	for (int b = 0; b < B->nblocks; ++b) B->blist[b] = b;
+	for (int b = 0; b < B->nblocks; ++b) B->blist[b] = make_int2(b, B->block_ch[b]);
 	B->nlaunch = B->nblocks;
-	KEL_CUDA(cudaMemcpyAsync(B->d_blist, B->blist.data(), sizeof(int) * B->nblocks, cudaMemcpyHostToDevice,
+	KEL_CUDA(cudaMemcpyAsync(B->d_blist, B->blist.data(), sizeof(int2) * B->nblocks, cudaMemcpyHostToDevice,
 							 B->stream));
 	KEL_CUDA(cudaMalloc(&B->d_active, sizeof(int) * B->n));
 	KEL_CUDA(cudaMalloc(&B->partial, sizeof(double2) * B->nblocks));
@@ -743,8 +766,8 @@ static int compact(kel_batch *B, const std::vector<int> &act) {
 	B->blist.clear();
 	for (int c = 0; c < B->n; ++c)
 		if (act[c])
-			for (int k = 0; k < B->rec[c].nblocks; ++k) B->blist.push_back(B->rec[c].first_block + k);
-	KEL_CUDA(cudaMemcpyAsync(B->d_blist, B->blist.data(), sizeof(int) * keep, cudaMemcpyHostToDevice, B->stream));
+			for (int k = 0; k < B->rec[c].nblocks; ++k) B->blist.push_back(make_int2(B->rec[c].first_block + k, c));
+	KEL_CUDA(cudaMemcpyAsync(B->d_blist, B->blist.data(), sizeof(int2) * keep, cudaMemcpyHostToDevice, B->stream));
 	KEL_CUDA(cudaStreamSynchronize(B->stream));
 	B->nlaunch = keep;
 	if (B->graph) cudaGraphExecDestroy(B->graph);
