@@ -39,6 +39,7 @@ WORKLOADS = {
     "d3q19_cavity_128": (19, (128, 128, 128), 0.55, "cavity"),
     "d3q19_cavity_192": (19, (192, 192, 192), 0.55, "cavity"),
     "d3q27_cavity_128": (27, (128, 128, 128), 0.55, "cavity"),
+    "d3q27_cavity_192": (27, (192, 192, 192), 0.55, "cavity"),
     "d2q9_poiseuille_256x64": (9, (256, 64), 0.8, "poiseuille"),
     "d2q9_channel_4096x4096": (9, (4096, 4096), 0.8, "poiseuille"),
     "d2q9_batch_1024": (9, None, None, "batch"),
@@ -465,6 +466,20 @@ def run_particles(args, rank, world):
         print(json.dumps(line))
 
 
+# DRAM bytes (read + write) per cell update of the one-cell sweep, from ncu
+# dram__bytes_read.sum + dram__bytes_write.sum on the 192^3 cavity (both
+# parities averaged; profiles/sweep1_cavity192_traffic.md).  The 256^3 bench
+# lattice is too large to capture under ncu's memory save/restore, so its
+# per-launch traffic is this figure times the cells (traffic grows with the
+# cells: every population is read and written once).
+SWEEP1_TRAFFIC_PER_CELL = {(19, "fp32"): 144.6, (19, "fp16s"): 69.1, (27, "fp32"): 213.2}
+
+
+def sweep_traffic(q, storage, cpt, cells):
+    per = SWEEP1_TRAFFIC_PER_CELL.get((q, storage))
+    return per * cells if (per is not None and cpt == 1) else None
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -621,8 +636,8 @@ def main():
                    if ncell * Q * 4 > 4e8 else "working set smaller than L2",
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_source": peak_src, "bytes_per_update": bpu,
-                     "per_launch_ms": per_launch_s * 1e3},
+                     "traffic": sweep_traffic(Q, args.storage, cpt, ncell), "peak_source": peak_src,
+                     "bytes_per_update": bpu, "per_launch_ms": per_launch_s * 1e3},
         "e2e": {"value": e2e_value, "unit": "MLUPS", "h2d_bytes_per_step": int(ncell + ncell * Q * 4),
                 "d2h_bytes_per_step": int(ncell * 4 * (1 + D)), "lbm_steps_per_step": args.e2e_lbm_steps,
                 "iters": args.e2e_iters, "mean_rho_fluid": mass, "phases_ms": phases},

@@ -35,6 +35,7 @@ struct kel_particles {
 	int n = 0;
 	kel_particle_state *d = nullptr; // device copy of the bodies
 	float *cell_force = nullptr;     // D planes, allocated on first request
+	void *boxes = nullptr;           // per-body integer boxes of the couple pass (n BodyBox)
 };
 
 namespace {
@@ -122,25 +123,64 @@ __device__ inline double subcell_porosity(int D, const double *x, const double *
 
 constexpr int TX = 32, TY = 8, TT = TX * TY;
 
-__global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state *P, int np, int mode, double eps) {
+// Every body's box (body_aabb) once per couple, as integers: the tile cull
+// and the per-cell box test then need no FP64 arithmetic (FP64 issues at a
+// small fraction of the FP32 rate on this GPU, and the per-tile FP64 cull
+// of every body bounded the couple pass).
+struct BodyBox {
+	int a[3], b[3];
+};
+
+__global__ void k_body_boxes(PView v, const kel_particle_state *P, int np, int sub, BodyBox *box) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= np) return;
+	int64_t a[3], b[3];
+	body_aabb(v.D, P[i], v.nx, v.ny, v.nz, v.periodic, sub, a, b);
+	BodyBox r;
+	for (int k = 0; k < 3; ++k) {
+		r.a[k] = (int)a[k];
+		r.b[k] = (int)b[k];
+	}
+	box[i] = r;
+}
+
+// Per tile of TX x TY cells: an ordered cull of the bodies whose box touches
+// the tile (their data staged in shared memory), then per cell the product of
+// the candidates' complements in body order, each complement computed as the
+// reference computes it.  Two exact shortcuts skip the FP64 sampling:
+//   sub-cell mode: the 16 (64) samples lie within 3 sqrt(D) / 8 of the cell
+//     centre, so a centre farther than R + that radius (+ 1e-6) from the body
+//     centre has no sample inside (factor 1) and one nearer than R - radius
+//     (- 1e-6) has all inside (factor 0);
+//   ramp mode: |r|^2 below (R - eps/2)^2 - 1e-6 gives 0, above
+//     (R + eps/2)^2 + 1e-6 gives 1.
+// The margins are far above the FP64 rounding of the coordinates, so the
+// factors equal those of the full computation bit for bit.
+__global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state *P, const BodyBox *box, int np,
+											   int mode, double eps) {
 	__shared__ int cand[TT];
+	__shared__ BodyBox cbox[TT];
+	__shared__ double cpos[TT][3];
+	__shared__ double crad[TT];
 	__shared__ int warp_count[TT / 32];
 	__shared__ int ncand;
 	const int tid = threadIdx.y * TX + threadIdx.x;
 	const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z = blockIdx.z;
 	const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
 	const int sub = mode == KEL_POROSITY_SUBCELL;
+	const double reach = sub ? (v.D == 3 ? 0.6495190528383290 : 0.5303300858899106) : 0.0; // 3 sqrt(D) / 8
 	double por = 1.0;
 	for (int c0 = 0; c0 < np; c0 += TT) {
-		// cull: does body c0+tid's AABB touch this tile?  (ordered compaction)
+		// cull: does body c0+tid's box touch this tile?  (ordered compaction)
 		bool hit = false;
 		const int pi = c0 + tid;
+		BodyBox bb;
 		if (pi < np) {
-			int64_t a[3], b[3];
-			body_aabb(v.D, P[pi], v.nx, v.ny, v.nz, v.periodic, sub, a, b);
-			bool yz = a[1] < y0 + TY && b[1] > y0 && (v.D == 2 || (a[2] <= z && b[2] > z));
-			bool xs = a[0] < x0 + TX && b[0] > x0;
-			if (v.periodic) xs = xs || (a[0] < x0 + TX - v.nx && b[0] > x0 - v.nx) || (a[0] < x0 + TX + v.nx && b[0] > x0 + v.nx);
+			bb = box[pi];
+			const bool yz = bb.a[1] < y0 + TY && bb.b[1] > y0 && (v.D == 2 || (bb.a[2] <= z && bb.b[2] > z));
+			bool xs = bb.a[0] < x0 + TX && bb.b[0] > x0;
+			if (v.periodic)
+				xs = xs || (bb.a[0] < x0 + TX - v.nx && bb.b[0] > x0 - v.nx) || (bb.a[0] < x0 + TX + v.nx && bb.b[0] > x0 + v.nx);
 			hit = yz && xs;
 		}
 		const unsigned m = __ballot_sync(0xffffffffu, hit);
@@ -156,26 +196,42 @@ __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state
 			ncand = s;
 		}
 		__syncthreads();
-		if (hit) cand[warp_count[tid >> 5] + __popc(m & ((1u << (tid & 31)) - 1u))] = pi;
+		if (hit) {
+			const int slot = warp_count[tid >> 5] + __popc(m & ((1u << (tid & 31)) - 1u));
+			cand[slot] = pi;
+			cbox[slot] = bb;
+			for (int d = 0; d < 3; ++d) cpos[slot][d] = P[pi].position[d];
+			crad[slot] = P[pi].radius;
+		}
 		__syncthreads();
 		if (x < v.nx && y < v.ny) {
 			for (int k = 0; k < ncand; ++k) {
-				const kel_particle_state &p = P[cand[k]];
-				int64_t a[3], b[3];
-				body_aabb(v.D, p, v.nx, v.ny, v.nz, v.periodic, sub, a, b);
-				double rel[3] = {rel_coord((double)x, p.position[0], v.periodic, v.nx), (double)y - p.position[1],
-								 v.D == 3 ? (double)z - p.position[2] : 0.0};
-				const double xi = p.position[0] + rel[0];
+				const BodyBox &q = cbox[k];
+				const double X0 = cpos[k][0], X1 = cpos[k][1], X2 = cpos[k][2], R = crad[k];
+				double rel[3] = {rel_coord((double)x, X0, v.periodic, v.nx), (double)y - X1, v.D == 3 ? (double)z - X2 : 0.0};
+				const double xi = X0 + rel[0];
 				const int64_t xc = v.periodic ? (int64_t)llround(xi) : x;
-				if (xc < a[0] || xc >= b[0] || y < a[1] || y >= b[1] || (v.D == 3 && (z < a[2] || z >= b[2]))) continue;
+				if (xc < q.a[0] || xc >= q.b[0] || y < q.a[1] || y >= q.b[1] || (v.D == 3 && (z < q.a[2] || z >= q.b[2])))
+					continue;
+				double s2 = 0.0;
+				for (int d = 0; d < v.D; ++d) s2 = s2 + rel[d] * rel[d];
 				double pp;
 				if (sub) {
-					const double xs[3] = {xi, (double)y, (double)z};
-					pp = subcell_porosity(v.D, xs, p.position, p.radius);
+					const double out_r = R + reach + 1e-6, in_r = R - reach - 1e-6;
+					if (s2 > out_r * out_r) {
+						continue; // no sample inside: factor 1
+					} else if (in_r > 0.0 && s2 < in_r * in_r) {
+						pp = 0.0;
+					} else {
+						const double xs[3] = {xi, (double)y, (double)z};
+						const double Xs[3] = {X0, X1, X2};
+						pp = subcell_porosity(v.D, xs, Xs, R);
+					}
 				} else {
-					double s2 = 0.0;
-					for (int d = 0; d < v.D; ++d) s2 = s2 + rel[d] * rel[d];
-					pp = ramp(sqrt(s2), p.radius, eps);
+					const double lo = R - eps / 2, hi = R + eps / 2;
+					if (lo > 0.0 && s2 < lo * lo - 1e-6) pp = 0.0;
+					else if (s2 > hi * hi + 1e-6) continue;
+					else pp = ramp(sqrt(s2), R, eps);
 				}
 				por = por * pp;
 			}
@@ -731,6 +787,7 @@ extern "C" int kel_particles_destroy(kel_particles *ps) {
 	cudaStreamSynchronize(ps->lat->stream);
 	cudaFree(ps->d);
 	cudaFree(ps->cell_force);
+	cudaFree(ps->boxes);
 	delete ps;
 	return KEL_OK;
 }
@@ -783,7 +840,11 @@ static int particles_couple(kel_particles *ps, const kel_particle_params *prm) {
 	kel_lattice *L = ps->lat;
 	if (prm->coupling == KEL_COUPLING_HLBM) return particles_hlbm_couple(ps, prm, false);
 	PView v = make_view(L);
-	k_couple<<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, ps->n, prm->porosity_mode, prm->eps);
+	if (!ps->boxes) KEL_CUDA(cudaMalloc(&ps->boxes, sizeof(BodyBox) * ps->n));
+	BodyBox *box = static_cast<BodyBox *>(ps->boxes);
+	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
+	k_body_boxes<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, sub, box);
+	k_couple<<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, box, ps->n, prm->porosity_mode, prm->eps);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
