@@ -155,7 +155,8 @@ __global__ void k_body_boxes(PView v, const kel_particle_state *P, int np, int s
 //   ramp mode: |r|^2 below (R - eps/2)^2 - 1e-6 gives 0, above
 //     (R + eps/2)^2 + 1e-6 gives 1.
 // The margins are far above the FP64 rounding of the coordinates, so the
-// factors equal those of the full computation bit for bit.
+// factors equal those of the full computation bit for bit.  Cells with no
+// image inside a candidate's box skip it before any FP64 arithmetic.
 __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state *P, const BodyBox *box, int np,
 											   int mode, double eps) {
 	__shared__ int cand[TT];
@@ -170,6 +171,7 @@ __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state
 	const int sub = mode == KEL_POROSITY_SUBCELL;
 	const double reach = sub ? (v.D == 3 ? 0.6495190528383290 : 0.5303300858899106) : 0.0; // 3 sqrt(D) / 8
 	double por = 1.0;
+	bool touched = false; // some body's box holds the cell (otherwise por stays exactly 1)
 	for (int c0 = 0; c0 < np; c0 += TT) {
 		// cull: does body c0+tid's box touch this tile?  (ordered compaction)
 		bool hit = false;
@@ -207,6 +209,14 @@ __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state
 		if (x < v.nx && y < v.ny) {
 			for (int k = 0; k < ncand; ++k) {
 				const BodyBox &q = cbox[k];
+				// integer pre-filter: no image of the cell (x, x -/+ nx when
+				// periodic) in the box means the nearest image is not either
+				if (y < q.a[1] || y >= q.b[1] || (v.D == 3 && (z < q.a[2] || z >= q.b[2]))) continue;
+				const bool in0 = x >= q.a[0] && x < q.b[0];
+				const bool inm = v.periodic && x - v.nx >= q.a[0] && x - v.nx < q.b[0];
+				const bool inp = v.periodic && x + v.nx >= q.a[0] && x + v.nx < q.b[0];
+				if (!(in0 || inm || inp)) continue;
+				touched = true;
 				const double X0 = cpos[k][0], X1 = cpos[k][1], X2 = cpos[k][2], R = crad[k];
 				double rel[3] = {rel_coord((double)x, X0, v.periodic, v.nx), (double)y - X1, v.D == 3 ? (double)z - X2 : 0.0};
 				const double xi = X0 + rel[0];
@@ -238,7 +248,7 @@ __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state
 		}
 		__syncthreads();
 	}
-	if (x < v.nx && y < v.ny) v.por[((int64_t)z * v.ny + y) * v.nxp + x] = (float)por;
+	if (x < v.nx && y < v.ny) v.por[((int64_t)z * v.ny + y) * v.nxp + x] = touched ? (float)por : 1.0f;
 }
 
 // ---- gather ---------------------------------------------------------------------
@@ -283,11 +293,33 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, i
 	const double ts = 1.0 / (double)steps;
 	double vp[3] = {0.0, 0.0, 0.0};
 	for (int k = 0; k < D; ++k) vp[k] = (p.position[k] - p.position_old[k]) / ts;
+	// c_i . u_p per direction, rounded to float as the reference rounds it: the
+	// same for every cell of the body, so computed once (FP64 is slow here)
+	float upe[L::Q];
+#pragma unroll
+	for (int i = 1; i < L::Q; ++i) {
+		double upe_d = 0.0;
+		upe_d = upe_d + (double)L::cx(i) * vp[0];
+		upe_d = upe_d + (double)L::cy(i) * vp[1];
+		if (D == 3) upe_d = upe_d + (double)L::cz(i) * vp[2];
+		upe[i] = (float)upe_d;
+	}
 	double acc[6] = {0, 0, 0, 0, 0, 0}; // force[3], torque[3] (sums of minus the cell forces)
+	// 32-bit index arithmetic unless the box holds 2^31 cells or more
+	const bool small = ncell < ((int64_t)1 << 31);
+	const int ex32 = (int)ex, ey32 = (int)ey, exy32 = small ? (int)(ex * ey) : 0;
 	for (int64_t k = threadIdx.x; k < ncell; k += GT) {
-		const int ix = (int)(a[0] + k % ex);
-		const int iy = (int)(a[1] + (k / ex) % ey);
-		const int iz = D == 3 ? (int)(a[2] + k / (ex * ey)) : 0;
+		int ix, iy, iz;
+		if (small) {
+			const int k32 = (int)k;
+			ix = (int)a[0] + k32 % ex32;
+			iy = (int)a[1] + (k32 / ex32) % ey32;
+			iz = D == 3 ? (int)a[2] + k32 / exy32 : 0;
+		} else {
+			ix = (int)(a[0] + k % ex);
+			iy = (int)(a[1] + (k / ex) % ey);
+			iz = D == 3 ? (int)(a[2] + k / (ex * ey)) : 0;
+		}
 		const int x = v.periodic ? ((ix % v.nx) + v.nx) % v.nx : ix;
 		const int64_t pc = ((int64_t)iz * v.ny + iy) * v.nxp + x;
 		const double r[3] = {rel_coord((double)x, p.position[0], v.periodic, v.nx), (double)iy - p.position[1],
@@ -304,14 +336,9 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, i
 		float mom[3] = {0.f, 0.f, 0.f};
 #pragma unroll
 		for (int i = 1; i < L::Q; ++i) {
-			double upe_d = 0.0;
-			upe_d = upe_d + (double)L::cx(i) * vp[0];
-			upe_d = upe_d + (double)L::cy(i) * vp[1];
-			if (D == 3) upe_d = upe_d + (double)L::cz(i) * vp[2];
-			const float upe = (float)upe_d;
 			const float fi = pop_post<L, STORE>(v, x, iy, iz, i);
 			const float fo = pop_post<L, STORE>(v, x + L::cx(i), iy + L::cy(i), iz + L::cz(i), L::opp(i));
-			const float da = __fadd_rn(__fmul_rn(fi, __fsub_rn(1.0f, upe)), __fmul_rn(fo, __fadd_rn(1.0f, upe)));
+			const float da = __fadd_rn(__fmul_rn(fi, __fsub_rn(1.0f, upe[i])), __fmul_rn(fo, __fadd_rn(1.0f, upe[i])));
 			mom[0] = __fadd_rn(mom[0], __fmul_rn((float)L::cx(i), da));
 			mom[1] = __fadd_rn(mom[1], __fmul_rn((float)L::cy(i), da));
 			if (D == 3) mom[2] = __fadd_rn(mom[2], __fmul_rn((float)L::cz(i), da));
