@@ -490,13 +490,33 @@ static int check_io(kel_lattice *L, const void *host, int32_t dtype, int32_t lay
 	return KEL_OK;
 }
 
+// A page-locked host buffer the device can address directly (cudaHostAlloc /
+// cudaHostRegister; with NVLink-C2C the GPU reads and writes it at several
+// hundred GB/s): the conversion kernels then read or write it in place, with
+// no staging copy.  Other host memory (pageable) goes through the staging
+// buffer and one cudaMemcpyAsync.
+static void *mapped_host(const void *host) {
+	cudaPointerAttributes at;
+	if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+		cudaGetLastError(); // an unregistered pointer is not an error here
+		return nullptr;
+	}
+	return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 extern "C" int kel_upload_populations(kel_lattice *L, const void *host, int32_t dtype, int32_t layout) {
 	int rc = check_io(L, host, dtype, layout, "kel_upload_populations");
 	if (rc) return rc;
 	const size_t bytes = (size_t)L->ncell * L->d.Q * (dtype == KEL_DTYPE_F32 ? 4 : 8);
-	if ((rc = ensure_staging(L, bytes))) return rc;
-	KEL_CUDA(cudaMemcpyAsync(L->staging, host, bytes, cudaMemcpyHostToDevice, L->stream));
-	launch_pop_convert(L, conv_args(L, dtype, layout), 1);
+	ConvArgs a = conv_args(L, dtype, layout);
+	if (void *m = mapped_host(host)) {
+		a.buf = m;
+	} else {
+		if ((rc = ensure_staging(L, bytes))) return rc;
+		a.buf = L->staging;
+		KEL_CUDA(cudaMemcpyAsync(L->staging, host, bytes, cudaMemcpyHostToDevice, L->stream));
+	}
+	launch_pop_convert(L, a, 1);
 	KEL_CUDA(cudaGetLastError());
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
 	return KEL_OK;
@@ -506,10 +526,17 @@ extern "C" int kel_download_populations(kel_lattice *L, void *host, int32_t dtyp
 	int rc = check_io(L, host, dtype, layout, "kel_download_populations");
 	if (rc) return rc;
 	const size_t bytes = (size_t)L->ncell * L->d.Q * (dtype == KEL_DTYPE_F32 ? 4 : 8);
-	if ((rc = ensure_staging(L, bytes))) return rc;
-	launch_pop_convert(L, conv_args(L, dtype, layout), 0);
+	ConvArgs a = conv_args(L, dtype, layout);
+	void *m = mapped_host(host);
+	if (m) {
+		a.buf = m;
+	} else {
+		if ((rc = ensure_staging(L, bytes))) return rc;
+		a.buf = L->staging;
+	}
+	launch_pop_convert(L, a, 0);
 	KEL_CUDA(cudaGetLastError());
-	KEL_CUDA(cudaMemcpyAsync(host, L->staging, bytes, cudaMemcpyDeviceToHost, L->stream));
+	if (!m) KEL_CUDA(cudaMemcpyAsync(host, L->staging, bytes, cudaMemcpyDeviceToHost, L->stream));
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
 	return check_sweep_error(L, "kel_download_populations");
 }
@@ -610,15 +637,20 @@ __global__ void __launch_bounds__(CONV_TILE) k_field_io(float *dev, float *buf, 
 
 static int field_io(kel_lattice *L, float *dev, float *host_out, const float *host_in, int comps) {
 	const size_t bytes = (size_t)L->ncell * comps * sizeof(float);
-	int rc = ensure_staging(L, bytes);
-	if (rc) return rc;
-	float *buf = static_cast<float *>(L->staging);
-	if (host_in) KEL_CUDA(cudaMemcpyAsync(buf, host_in, bytes, cudaMemcpyHostToDevice, L->stream));
 	if (comps < 1 || comps > 3) return fail(KEL_ERR_INVALID_ARGUMENT, "field_io: %d components", comps);
+	// page-locked host buffers are read / written in place (mapped_host)
+	float *buf = static_cast<float *>(mapped_host(host_in ? static_cast<const void *>(host_in) : host_out));
+	const bool staged = buf == nullptr;
+	if (staged) {
+		int rc = ensure_staging(L, bytes);
+		if (rc) return rc;
+		buf = static_cast<float *>(L->staging);
+		if (host_in) KEL_CUDA(cudaMemcpyAsync(buf, host_in, bytes, cudaMemcpyHostToDevice, L->stream));
+	}
 	k_field_io<<<(unsigned)((L->ncell + CONV_TILE - 1) / CONV_TILE), CONV_TILE, 0, L->stream>>>(
 		dev, buf, L->plane, L->ncell, (int)L->desc.nx, L->nxp, comps, host_in ? 1 : 0);
 	KEL_CUDA(cudaGetLastError());
-	if (host_out) KEL_CUDA(cudaMemcpyAsync(host_out, buf, bytes, cudaMemcpyDeviceToHost, L->stream));
+	if (host_out && staged) KEL_CUDA(cudaMemcpyAsync(host_out, buf, bytes, cudaMemcpyDeviceToHost, L->stream));
 	KEL_CUDA(cudaStreamSynchronize(L->stream));
 	return KEL_OK;
 }

@@ -139,13 +139,14 @@ def targets(states: SteadyStates, rho_scale=None, rho_target_rms=0.25):
 
 
 def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, warmup=100, seed=1,
-          widths=(32, 64, 128, 128), log_every=0):
+          widths=(32, 64, 128, 128), log_every=0, rho_target_rms=0.25):
     """Train the U-Net on the steady states with Adam (cosine schedule).
+    rho_target_rms sets the weight of the density in the loss (see targets).
     Returns a WarmStartNet; its history holds (step, loss) pairs."""
     torch = _torch()
     ny, nx = states.rho.shape[1:]
     mask, u_max, tau = channel_inputs(states.channels)
-    tgt, rho_scale = targets(states)
+    tgt, rho_scale = targets(states, rho_target_rms=rho_target_rms)
     dev = torch.device("cuda")
     d_mask = torch.from_numpy(mask).to(dev)
     d_umax = torch.from_numpy(u_max).to(dev)
@@ -366,6 +367,14 @@ def evaluate(model: WarmStartNet, channels, tol=1e-6, check_every=1000, max_step
         s_r1 = time_to_steady(channels, model_init(model, with_neq, rho_from_net=False), tol, check_every,
                               max_steps, tile).steps
         s_nn = time_to_steady(channels, model_init(model, False), tol, check_every, max_steps, tile).steps
+        # which predicted field limits: the exact u with the predicted rho,
+        # and the predicted u with the exact rho
+        phys = np.concatenate([pred_u, pred_rho[..., None]], axis=-1)
+        u_ex = np.concatenate([u_plain, pred_rho[..., None]], axis=-1)
+        rho_ex = np.concatenate([phys[..., :2], rho_plain[..., None]], axis=-1)
+        s_uex = time_to_steady(channels, field_init(u_ex, with_neq), tol, check_every, max_steps, tile).steps
+        s_rex = time_to_steady(channels, field_init(rho_ex, with_neq), tol, check_every, max_steps, tile).steps
         out.update(steady_init_steps_mean=float(np.mean(s_ex)), rho_one_steps_mean=float(np.mean(s_r1)),
-                   no_neq_steps_mean=float(np.mean(s_nn)))
+                   no_neq_steps_mean=float(np.mean(s_nn)), exact_u_net_rho_steps_mean=float(np.mean(s_uex)),
+                   net_u_exact_rho_steps_mean=float(np.mean(s_rex)))
     return out
