@@ -336,6 +336,13 @@ int kel_unet_adam_step(kel_unet *net, float lr, float beta1, float beta2, float 
 #define KEL_UNET_CONV_TCGEN05 0
 #define KEL_UNET_CONV_MMA_SYNC 1
 int kel_unet_set_conv_kernel(kel_unet *net, int32_t kind);
+/* Residual head (no counterpart in the reference): output channel
+ * `out_channel` becomes the head's value plus `scale` times input plane
+ * `in_channel`, so the network learns the correction to that plane (the
+ * warm start adds the local Poiseuille estimate of u_x / u_max this way).
+ * out_channel < 0 turns it off (the default).  Training and inference use
+ * the same setting. */
+int kel_unet_set_residual(kel_unet *net, int32_t out_channel, int32_t in_channel, float scale);
 
 /* Launch shape of the sweep: cells per thread (1: one cell, 32-bit FP32 /
  * 16-bit FP16S accesses; 2: two consecutive cells, 64-bit / 32-bit accesses;

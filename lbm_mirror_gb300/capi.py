@@ -264,6 +264,7 @@ def load_library(path: str | None = None):
         "kel_unet_backward": ([vp, vp, i32, C.POINTER(C.c_double)], C.c_int),
         "kel_unet_adam_step": ([vp, C.c_float, C.c_float, C.c_float, C.c_float, i32], C.c_int),
         "kel_unet_set_conv_kernel": ([vp, i32], C.c_int),
+        "kel_unet_set_residual": ([vp, i32, i32, C.c_float], C.c_int),
         "kel_batch_destroy": ([vp], C.c_int),
         "kel_batch_upload_flags": ([vp, vp], C.c_int),
         "kel_batch_set_program": ([vp, C.POINTER(StepProgram)], C.c_int),

@@ -814,12 +814,17 @@ __global__ void upcat_backward(const bf16 *dcat, bf16 *du, bf16 *ds, int N, int 
 	}
 }
 
-// 1x1 head: y (N,H,W,3) fp32 = x (.., Ci) * Wh^T + b
-__global__ void head_forward(const bf16 *x, const float *w, const float *b, float *y, int64_t M, int Ci, int Co) {
+// 1x1 head: y (N,H,W,3) fp32 = x (.., Ci) * Wh^T + b, plus (res_out >= 0)
+// res_scale times input plane res_in of the network input `in` (Cin planes)
+// on output channel res_out: the network then learns the correction to that
+// plane (a residual target).
+__global__ void head_forward(const bf16 *x, const float *w, const float *b, float *y, int64_t M, int Ci, int Co,
+							 const bf16 *in, int Cin, int res_out, int res_in, float res_scale) {
 	for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
 		for (int co = 0; co < Co; ++co) {
 			float s = b[co];
 			for (int ci = 0; ci < Ci; ++ci) s += w[co * Ci + ci] * __bfloat162float(x[m * Ci + ci]);
+			if (co == res_out) s += res_scale * __bfloat162float(in[m * Cin + res_in]);
 			y[m * Co + co] = s;
 		}
 	}
@@ -1053,6 +1058,8 @@ struct kel_unet {
 	int conv_kernel = KEL_UNET_CONV_TCGEN05;
 	int *d_err = nullptr; // set by a tensor-core kernel whose bounded wait ran out
 	float *col_open = nullptr, *col_h3 = nullptr, *col_res = nullptr; // input-feature scratch (max_batch x W)
+	int res_out = -1, res_in = 0; // residual head (kel_unet_set_residual); res_out < 0: none
+	float res_scale = 0.f;
 };
 
 namespace {
@@ -1442,7 +1449,8 @@ extern "C" int kel_unet_forward(kel_unet *U, int32_t n, float *d_out) {
 	const UnetLayer &hd = L[14];
 	const int64_t M = (int64_t)n * H * W;
 	head_forward<<<grid_of(M), 256, 0, U->stream>>>(A[T_D0B], U->p + hd.woff, U->p + hd.woff + (int64_t)hd.co * hd.ci,
-													U->out, M, hd.ci, hd.co);
+													U->out, M, hd.ci, hd.co, U->input, U->d.in_channels, U->res_out,
+													U->res_in, U->res_scale);
 	KEL_CUDA(cudaGetLastError());
 	if (d_out && d_out != U->out)
 		KEL_CUDA(cudaMemcpyAsync(d_out, U->out, sizeof(float) * M * hd.co, cudaMemcpyDeviceToDevice, U->stream));
@@ -1539,6 +1547,17 @@ extern "C" int kel_unet_synchronize(kel_unet *U) {
 	if (!U) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_synchronize: null net");
 	KEL_CUDA(cudaStreamSynchronize(U->stream));
 	return check_device_error(U, "kel_unet_synchronize");
+}
+
+extern "C" int kel_unet_set_residual(kel_unet *U, int32_t out_channel, int32_t in_channel, float scale) {
+	if (!U) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_set_residual: null net");
+	if (out_channel >= U->d.out_channels || (out_channel >= 0 && (in_channel < 0 || in_channel >= U->d.in_channels)))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_set_residual: channels %d <- %d out of range", out_channel,
+					in_channel);
+	U->res_out = out_channel < 0 ? -1 : out_channel;
+	U->res_in = in_channel;
+	U->res_scale = scale;
+	return KEL_OK;
 }
 
 extern "C" int kel_unet_set_conv_kernel(kel_unet *U, int32_t kind) {

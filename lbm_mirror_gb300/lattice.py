@@ -510,6 +510,11 @@ class UNet:
         """K.KEL_UNET_CONV_TCGEN05 (default) or K.KEL_UNET_CONV_MMA_SYNC."""
         _check(self.lib.kel_unet_set_conv_kernel(self._h, int(kind)), self.lib)
 
+    def set_residual(self, out_channel, in_channel=0, scale=1.0):
+        """Output channel out_channel = head + scale * input plane in_channel
+        (out_channel < 0: off)."""
+        _check(self.lib.kel_unet_set_residual(self._h, int(out_channel), int(in_channel), float(scale)), self.lib)
+
     def set_stream(self, stream):
         _check(self.lib.kel_unet_set_stream(self._h, C.c_void_p(stream)), self.lib)
 

@@ -139,9 +139,12 @@ def targets(states: SteadyStates, rho_scale=None, rho_target_rms=0.25):
 
 
 def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, warmup=100, seed=1,
-          widths=(32, 64, 128, 128), log_every=0, rho_target_rms=0.25):
+          widths=(32, 64, 128, 128), log_every=0, rho_target_rms=0.25, residual=False):
     """Train the U-Net on the steady states with Adam (cosine schedule).
     rho_target_rms sets the weight of the density in the loss (see targets).
+    With `residual` the u_x output is the correction to the local Poiseuille
+    estimate the input planes carry (2 x plane 9 = u_x / u_max of the column's
+    gap, its flux share by h^3): kel_unet_set_residual(0, 9, 2).
     Returns a WarmStartNet; its history holds (step, loss) pairs."""
     torch = _torch()
     ny, nx = states.rho.shape[1:]
@@ -154,6 +157,8 @@ def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, 
     d_tgt = torch.from_numpy(tgt).to(dev)
     n = mask.shape[0]
     net = UNet(height=ny, width=nx, widths=widths, out_channels=3, max_batch=batch, seed=seed)
+    if residual:
+        net.set_residual(0, 9, 2.0)
     model = WarmStartNet(net, rho_scale)
     steps_per_epoch = n // batch
     total = max(1, epochs * steps_per_epoch)

@@ -124,3 +124,36 @@ def test_tcgen05_and_mma_sync_kernels_agree_at_full_size():
     assert abs(la - lb) <= 1e-2 * lb
     assert np.linalg.norm(ga - gb) / np.linalg.norm(gb) <= 1e-2
 
+
+
+def test_residual_head_adds_the_input_plane():
+    """kel_unet_set_residual: output channel 0 = the plain head + 2 x input
+    plane 9 (the warm start's local Poiseuille estimate); the other output
+    channels and the gradients' path are unchanged; out_channel -1 turns it
+    off; out-of-range channels are rejected."""
+    from lbm_mirror_gb300 import KelError
+    rng = np.random.default_rng(4)
+    net = _net()
+    x = np.zeros((N, H, W, 16))
+    x[..., :3] = rng.standard_normal((N, H, W, 3))
+    x[..., 9] = rng.uniform(0.0, 4.0, (N, H, W))
+    x = bf16_round(x)
+    xin = torch.tensor(x, dtype=torch.bfloat16, device="cuda").contiguous()
+    base = torch.empty((N, H, W, 3), dtype=torch.float32, device="cuda")
+    res = torch.empty_like(base)
+    net.set_input(xin.data_ptr(), N)
+    net.forward(N, base.data_ptr())
+    net.set_residual(0, 9, 2.0)
+    net.forward(N, res.data_ptr())
+    net.synchronize()
+    b, r = base.cpu().numpy(), res.cpu().numpy()
+    np.testing.assert_allclose(r[..., 0], b[..., 0] + 2.0 * x[..., 9], rtol=0, atol=1e-5)
+    np.testing.assert_array_equal(r[..., 1:], b[..., 1:])
+    net.set_residual(-1)
+    net.forward(N, res.data_ptr())
+    net.synchronize()
+    np.testing.assert_array_equal(res.cpu().numpy(), b)
+    with pytest.raises(KelError):
+        net.set_residual(3, 9, 1.0)
+    with pytest.raises(KelError):
+        net.set_residual(0, 16, 1.0)
