@@ -63,6 +63,13 @@ extern "C" {
 #define KEL_BC_MOVING_WALL 5       /* lid: f_i = f_opp + 2 w_i (c_i.u_w)/cs^2 (cavity_2d_gpu.cpp:204-235) */
 #define KEL_BC_ANTI_BOUNCE_BACK 6  /* cmpt::AntiBounceBack, D2Q9 y-mirror (boundary.hpp:81-133) */
 #define KEL_BC_EQUILIBRIUM 7       /* cmpt::Equilibrium(rho,u) (boundary.hpp:135-161) */
+/* Half-way bounce-back wall (no counterpart in the reference, whose walls
+ * are full-way): a cell with this op is solid and computes nothing; a
+ * population a computed cell sends towards it returns to that cell in the
+ * opposite direction in the same step (the wall sits half way between the
+ * two cell centres).  Populations stored at such cells are undefined.
+ * Sweeps with one cell per thread; batches reject it. */
+#define KEL_BC_HALFWAY_WALL 8
 
 /* ---- collision operator applied to cells whose op has .collide = 1 ------ */
 #define KEL_COLL_BGK 0     /* cmpt::BGK (collision.hpp:19-97) */

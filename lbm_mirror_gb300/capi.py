@@ -40,6 +40,7 @@ KEL_BC_ZOUHE_PRESSURE_X = 4
 KEL_BC_MOVING_WALL = 5
 KEL_BC_ANTI_BOUNCE_BACK = 6
 KEL_BC_EQUILIBRIUM = 7
+KEL_BC_HALFWAY_WALL = 8
 
 KEL_COLL_BGK, KEL_COLL_BGK_GUO, KEL_COLL_PSM, KEL_COLL_PSM_GUO, KEL_COLL_HLBM = 0, 1, 2, 3, 4
 KEL_ARITH_FAST, KEL_ARITH_REFERENCE, KEL_ARITH_SHIFTED = 0, 1, 2

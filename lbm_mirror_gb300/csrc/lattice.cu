@@ -201,6 +201,7 @@ extern "C" int kel_lattice_destroy(kel_lattice *L) {
 	cudaFree(L->flags);
 	cudaFree(L->d_seen);
 	cudaFree(L->d_err);
+	cudaFree(L->hw_mask);
 	cudaFree(L->rho);
 	cudaFree(L->u);
 	cudaFree(L->por);
@@ -742,7 +743,7 @@ static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops
 	for (int fl = 0; fl < MAX_FLAGS; ++fl) {
 		const kel_flag_op &o = P->ops[fl];
 		OpEntry &e = ops[fl];
-		if (o.bc < KEL_BC_NONE || o.bc > KEL_BC_EQUILIBRIUM)
+		if (o.bc < KEL_BC_NONE || o.bc > KEL_BC_HALFWAY_WALL)
 			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: flag %d: unknown boundary op %d", fl, o.bc);
 		// A boundary the descriptor has no reference specialisation for is an
 		// error only where a cell carries that flag.
@@ -754,7 +755,7 @@ static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops
 		if (used && o.bc == KEL_BC_ANTI_BOUNCE_BACK && d.Q != 9)
 			return fail(KEL_ERR_UNSUPPORTED, "kel_step: AntiBounceBack is D2Q9 only (boundary.hpp:117)");
 		e.bc = used ? o.bc : KEL_BC_NONE;
-		e.collide = o.collide ? 1 : 0;
+		e.collide = o.collide && o.bc != KEL_BC_HALFWAY_WALL ? 1 : 0; // a half-way wall is solid
 		e.east = o.east ? 1 : 0;
 		e.use_profile = o.use_profile ? 1 : 0;
 		e.rho = (float)o.rho;
@@ -768,6 +769,53 @@ static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops
 		float uf[3] = {(float)o.u[0], (float)o.u[1], (float)o.u[2]};
 		host_equilibrium(d, (float)o.rho, uf, e.eq);
 	}
+	return KEL_OK;
+}
+
+// Half-way walls: per cell, bit i set where the neighbour x + c_i is a cell
+// whose flag has the half-way wall op (periodic rows wrap); zero for wall
+// cells, flag-0 cells and cells with no wall neighbour.
+template <class Lc>
+__global__ void k_hw_mask(const uint8_t *flags, unsigned hw_flags, int nxp, int ny, int nz, int periodic, int64_t plane,
+						  uint32_t *mask) {
+	for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < plane; c += (int64_t)gridDim.x * blockDim.x) {
+		const int x = (int)(c % nxp);
+		const int64_t r = c / nxp;
+		const int y = (int)(r % ny), z = (int)(r / ny);
+		const unsigned f = flags[c];
+		uint32_t m = 0;
+		if (f != 0u && !(f < MAX_FLAGS && ((hw_flags >> f) & 1u))) {
+#pragma unroll
+			for (int i = 1; i < Lc::Q; ++i) {
+				int nx = x + Lc::cx(i);
+				const int ny2 = y + Lc::cy(i), nz2 = z + Lc::cz(i);
+				if (periodic) nx = nx < 0 ? nx + nxp : (nx >= nxp ? nx - nxp : nx);
+				if (nx < 0 || nx >= nxp || ny2 < 0 || ny2 >= ny || nz2 < 0 || nz2 >= nz) continue;
+				const unsigned g = flags[((int64_t)nz2 * ny + ny2) * nxp + nx];
+				if (g < MAX_FLAGS && ((hw_flags >> g) & 1u)) m |= 1u << i;
+			}
+		}
+		mask[c] = m;
+	}
+}
+
+// After a program is lowered: the half-way wall mask, when a flag present in
+// the lattice has the op (else the sweeps run without it).
+static int update_halfway(kel_lattice *L, const kel_step_program *P) {
+	unsigned hw = 0;
+	for (int fl = 1; fl < MAX_FLAGS; ++fl)
+		if (P->ops[fl].bc == KEL_BC_HALFWAY_WALL && L->present[fl]) hw |= 1u << fl;
+	L->hw_active = hw != 0;
+	if (!hw) return KEL_OK;
+	if (!L->hw_mask) KEL_CUDA(cudaMalloc(&L->hw_mask, sizeof(uint32_t) * (size_t)L->plane));
+	const int periodic = (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0;
+	const int ny = (int)L->desc.ny, nz = (int)L->desc.nz;
+	switch (L->d.Q) {
+	case 9: k_hw_mask<D2Q9><<<grid_for(L->plane), 256, 0, L->stream>>>(L->flags, hw, L->nxp, ny, nz, periodic, L->plane, L->hw_mask); break;
+	case 19: k_hw_mask<D3Q19><<<grid_for(L->plane), 256, 0, L->stream>>>(L->flags, hw, L->nxp, ny, nz, periodic, L->plane, L->hw_mask); break;
+	default: k_hw_mask<D3Q27><<<grid_for(L->plane), 256, 0, L->stream>>>(L->flags, hw, L->nxp, ny, nz, periodic, L->plane, L->hw_mask); break;
+	}
+	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
 
@@ -855,6 +903,7 @@ static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	p.cpt = L->cpt;
 	p.idx32 = (int64_t)L->d.Q * L->plane < ((int64_t)1 << 31) ? 1 : 0;
 	p.block = L->block;
+	p.hw_mask = L->hw_active ? L->hw_mask : nullptr;
 	p.stages = L->cpt == CPT_ROWS ? L->block : 0;
 	p.sms = L->sms;
 	p.err = L->d_err;
@@ -933,6 +982,7 @@ extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_st
 		OpEntry ops[MAX_FLAGS];
 		if ((rc = lower_program(L, P, ops))) return rc;
 		KEL_CUDA(cudaMemcpyAsync(L->ops, ops, sizeof(ops), cudaMemcpyHostToDevice, L->stream));
+		if ((rc = update_halfway(L, P))) return rc;
 		KEL_CUDA(cudaStreamSynchronize(L->stream));
 		L->last_prog = *P;
 		L->have_ops = true;

@@ -65,5 +65,7 @@ struct kel_lattice {
 	int sms = 1;      // multiprocessors of the lattice's device
 	unsigned *d_err = nullptr; // set by the row pipeline when a bounded wait gave up
 	bool rows_used = false;    // a row-pipeline sweep was launched (d_err worth reading)
+	uint32_t *hw_mask = nullptr; // half-way wall neighbour bits per cell (allocated on first use)
+	bool hw_active = false;      // the current program has half-way walls present in the lattice
 	bool tuned = false;
 };

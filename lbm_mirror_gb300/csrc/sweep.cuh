@@ -42,7 +42,8 @@ enum : int {
 	BC_ZOUHE_PRESSURE_X = 4,
 	BC_MOVING_WALL = 5,
 	BC_ANTI_BOUNCE_BACK = 6,
-	BC_EQUILIBRIUM = 7
+	BC_EQUILIBRIUM = 7,
+	BC_HALFWAY_WALL = 8
 };
 constexpr int MAX_FLAGS = 8;
 constexpr int CPT_ROWS = -1; // launch shape of the row pipeline (KEL_LAUNCH_ROWS)
@@ -81,6 +82,7 @@ struct SweepParams {
 	int idx32;        // Q * plane < 2^31: offsets from a cell fit 32-bit arithmetic
 	int block;        // threads per block
 	int wpr2;         // sweep2_kernel: warps per row (32 cell pairs per warp)
+	const uint32_t *hw_mask; // half-way walls: per cell, bit i = the neighbour x + c_i is one (null: none)
 	int stages;       // sweep_rows_kernel: row stages in shared memory
 	int sms;          // multiprocessors of the device (persistent grid of sweep_rows_kernel)
 	unsigned *err;    // sweep_rows_kernel: set to 1 when a bounded wait gave up
@@ -461,6 +463,7 @@ __device__ __forceinline__ bool cell_update(float (&f)[L::Q], int flag, int y, c
 	if (flag >= MAX_FLAGS) return false; // the drivers' `default: break;`
 	const OpEntry *op = p.ops + flag;
 	const int bc = __ldg(&op->bc);
+	if (bc == BC_HALFWAY_WALL) return false; // solid: the sweep writes nothing for it
 	float cpy[L::Q];
 	switch (bc) {
 	case BC_BOUNCE_BACK: // boundary.hpp:58-75 (full-way)
@@ -954,6 +957,40 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 		p.rho[cell] = rho;
 #pragma unroll
 		for (int k = 0; k < L::D; ++k) p.u[k * p.plane + cell] = u[k];
+	}
+	if (p.hw_mask) {
+		// half-way bounce-back: a wall cell writes nothing; a population sent
+		// towards a wall goes to the slot this cell reads f_opp(i) from next
+		// step (even: A[i][x + c_i], which the odd step reads as
+		// A[opp(opp i)][x - c_opp i]; odd: A[opp i][x], read by the even step)
+		if (flag > 0 && flag < MAX_FLAGS && __ldg(&p.ops[flag].bc) == BC_HALFWAY_WALL) return;
+		const uint32_t hw = p.hw_mask[cell];
+		if (hw) {
+#pragma unroll
+			for (int i = 0; i < Q; ++i) {
+				const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+				const int64_t pb = static_cast<int64_t>(i) * p.plane;
+				const int64_t po = static_cast<int64_t>(L::opp(i)) * p.plane;
+				int dx = x + cx;
+				if (p.periodic) dx = dx < 0 ? dx + nxp : (dx >= nxp ? dx - nxp : dx);
+				const int dy = y + cy, dz = z + cz;
+				const int64_t dcell = (static_cast<int64_t>(dz) * p.ny + dy) * nxp + dx;
+				const bool wall = (hw >> i) & 1u;
+				if (!ODD) {
+					S::st1(p.f, wall ? pb + dcell : po + cell, f[i], p.wshift[i]);
+				} else {
+					int sx = x - cx;
+					const int sy = y - cy, sz = z - cz;
+					if (p.periodic) sx = sx < 0 ? sx + nxp : (sx >= nxp ? sx - nxp : sx);
+					if (sx < 0 || sx >= nxp || sy < 0 || sy >= p.ny || sz < 0 || sz >= p.nz)
+						S::st1(p.f, pb + cell, 0.f, p.wshift[i]); // ghost ring's zero
+					if (wall) S::st1(p.f, po + cell, f[i], p.wshift[i]);
+					else if (dx >= 0 && dx < nxp && dy >= 0 && dy < p.ny && dz >= 0 && dz < p.nz)
+						S::st1(p.f, pb + dcell, f[i], p.wshift[i]);
+				}
+			}
+			return;
+		}
 	}
 	if (!ODD) {
 #pragma unroll

@@ -206,6 +206,7 @@ static int KO(cell_step)(KO(ko_lat) * L, const kel_step_program *P, int64_t c, i
 	/* `case 0u: break;` and `default: break;` of the drivers' switch(info) */
 	if (info == 0u || info >= KEL_MAX_FLAGS) return 0;
 	const kel_flag_op *o = &P->ops[info];
+	if (o->bc == KEL_BC_HALFWAY_WALL) return 0; /* solid: computes nothing */
 	REAL *f = buf + KO(gidx)(L, x, y, z) * d->Q;
 	REAL cpy[27];
 	switch (o->bc) {
@@ -255,12 +256,36 @@ static int KO(cell_step)(KO(ko_lat) * L, const kel_step_program *P, int64_t c, i
 	return 0;
 }
 
-static void KO(stream_cell)(KO(ko_lat) * L, int64_t x, int64_t y, int64_t z, const REAL *src, REAL *dst) {
+/* Does program P give any flag the half-way wall op?  (Only then does the
+ * stream look at its neighbours' flags; P = NULL below means "none".) */
+static const kel_step_program *KO(halfway_program)(const kel_step_program *P) {
+	for (int k = 1; k < KEL_MAX_FLAGS; ++k)
+		if (P->ops[k].bc == KEL_BC_HALFWAY_WALL) return P;
+	return 0;
+}
+
+/* Is interior cell (x, y, z) a half-way wall of program P? */
+static int KO(is_halfway)(const KO(ko_lat) * L, const kel_step_program *P, int64_t x, int64_t y, int64_t z) {
+	if (!P || x < 0 || x >= L->nx || y < 0 || y >= L->ny || z < 0 || z >= L->nz) return 0;
+	const uint8_t info = L->info[x + L->nx * (y + L->ny * z)];
+	return info > 0u && info < KEL_MAX_FLAGS && P->ops[info].bc == KEL_BC_HALFWAY_WALL;
+}
+
+/* Pull stream of one cell.  Half-way bounce-back (no counterpart in the
+ * reference): where the source x - c_i is a half-way wall, f_i(x) takes the
+ * post-collision f_opp(i) that x itself sent towards the wall. */
+static void KO(stream_cell)(KO(ko_lat) * L, const kel_step_program *P, int64_t x, int64_t y, int64_t z,
+							const REAL *src, REAL *dst) {
 	const ko_desc *d = &L->d;
+	if (P && KO(is_halfway)(L, P, x, y, z)) return; /* solid */
 	REAL *out = dst + KO(gidx)(L, x, y, z) * d->Q;
 	for (int i = 0; i < d->Q; ++i) {
 		int64_t sx = x - d->c[i][0], sy = y - d->c[i][1], sz = z - (d->D == 3 ? d->c[i][2] : 0);
 		if (L->periodic_x) sx = (sx + L->nx) % L->nx;
+		if (P && KO(is_halfway)(L, P, sx, sy, sz)) {
+			out[i] = src[KO(gidx)(L, x, y, z) * d->Q + d->opp[i]];
+			continue;
+		}
 		/* stream.hpp:256-264: ghost_at(g_index - c_i), the ghost ring holds zeros */
 		out[i] = src[((sx + 1) + L->gx * ((sy + 1) + L->gy * (sz + (d->D == 3 ? 1 : 0)))) * d->Q + i];
 	}
@@ -268,6 +293,7 @@ static void KO(stream_cell)(KO(ko_lat) * L, int64_t x, int64_t y, int64_t z, con
 
 static int KO(run)(KO(ko_lat) * L, const kel_step_program *P, uint64_t steps) {
 	const ko_desc *d = &L->d;
+	const kel_step_program *hw = KO(halfway_program)(P);
 	for (uint64_t s = 0; s < steps; ++s) {
 		int even = (L->t % 2u) == 0u;
 		REAL *old = even ? L->dfs[0] : L->dfs[1];
@@ -287,7 +313,7 @@ static int KO(run)(KO(ko_lat) * L, const kel_step_program *P, uint64_t steps) {
 			int64_t z = zy / L->ny, y = zy % L->ny;
 			for (int64_t x = 0; x < L->nx; ++x) {
 				int64_t c = x + L->nx * (y + L->ny * z);
-				if (L->info[c] > 0u) KO(stream_cell)(L, x, y, z, old, nw);
+				if (L->info[c] > 0u) KO(stream_cell)(L, hw, x, y, z, old, nw);
 			}
 		}
 		(void)d;
@@ -301,6 +327,7 @@ static int KO(run)(KO(ko_lat) * L, const kel_step_program *P, uint64_t steps) {
  * counter does not advance; used only to time the reference algorithm on a
  * bounded part of a large lattice. */
 static int KO(run_rows)(KO(ko_lat) * L, const kel_step_program *P, int64_t r0, int64_t r1) {
+	const kel_step_program *hw = KO(halfway_program)(P);
 	int even = (L->t % 2u) == 0u;
 	REAL *old = even ? L->dfs[0] : L->dfs[1];
 	REAL *nw = even ? L->dfs[1] : L->dfs[0];
@@ -315,7 +342,7 @@ static int KO(run_rows)(KO(ko_lat) * L, const kel_step_program *P, int64_t r0, i
 	for (int64_t zy = r0; zy < r1; ++zy) {
 		int64_t z = zy / L->ny, y = zy % L->ny;
 		for (int64_t x = 0; x < L->nx; ++x)
-			if (L->info[x + L->nx * zy] > 0u) KO(stream_cell)(L, x, y, z, old, nw);
+			if (L->info[x + L->nx * zy] > 0u) KO(stream_cell)(L, hw, x, y, z, old, nw);
 	}
 	return 0;
 }

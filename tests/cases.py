@@ -145,6 +145,58 @@ def mixed_3d(q, collision, dims=(16, 12, 10), steps=21, seed=2, arithmetic=K.KEL
                 porosity=por, force=force)
 
 
+def halfway_poiseuille_2d(nx=8, ny=22, steps=6000, tau=0.8, g=1e-6, arithmetic=K.KEL_ARITH_FAST, f64=False):
+    """Force-driven D2Q9 channel, periodic in x, half-way bounce-back walls
+    at y = 0 and y = ny - 1 (the wall planes sit at y = 1/2 and y = ny - 3/2),
+    BGK + Guo body force g along x, rest start.  Steady state:
+    u_x(y) = g_eff / (2 nu) (y - 1/2) (ny - 3/2 - y), nu = (tau - 1/2) / 3,
+    g_eff = (1 - 1/(2 tau)) g (the reference's Guo term without the
+    half-force velocity shift)."""
+    dims = (nx, ny)
+    x, y, _ = cell_grid(dims)
+    flags = np.full(nx * ny, 2, dtype=np.uint8)
+    flags[(y == 0) | (y == ny - 1)] = 1
+    ops = {1: dict(bc=K.KEL_BC_HALFWAY_WALL), 2: dict(bc=K.KEL_BC_FLUID, collide=1)}
+    return dict(q=9, dims=dims, f64=f64, periodic=True, steps=steps,
+                program=K.make_program(tau, K.KEL_COLL_BGK_GUO, ops, global_force=(g, 0.0, 0.0),
+                                       arithmetic=arithmetic),
+                flags=flags, init=None, profile=None, porosity=None, force=None)
+
+
+def halfway_mixed(q, dims, steps=23, seed=3, arithmetic=K.KEL_ARITH_REFERENCE, f64=False, periodic=False):
+    """Half-way walls (flag 6: the rim in y and z, an obstacle block and an
+    isolated wall cell) beside full-way walls (flag 1: the x ends), a moving
+    lid (flag 5), fluid, random populations."""
+    rng = np.random.default_rng(SEED + seed)
+    x, y, z = cell_grid(dims)
+    nx, ny = dims[0], dims[1]
+    nz = dims[2] if len(dims) == 3 else 1
+    n = nx * ny * nz
+    flags = np.full(n, 2, dtype=np.uint8)
+    rim = (y == 0) | (y == ny - 1)
+    if q != 9:
+        rim |= (z == 0) | (z == nz - 1)
+    flags[rim] = 6
+    if not periodic:
+        flags[(x == 0) | (x == nx - 1)] = 1
+    flags[(y == ny - 1) & (x > 2) & (x < nx - 3) & ((z > 1) & (z < nz - 2) if q != 9 else True)] = 5
+    blk = (x > 5) & (x < 9) & (y > 3) & (y < 7)
+    if q != 9:
+        blk &= (z > 2) & (z < 6)
+    flags[blk] = 6
+    flags[(x == nx - 5) & (y == ny // 2) & (z == nz // 2)] = 6
+    ops = {
+        1: dict(bc=K.KEL_BC_BOUNCE_BACK),
+        2: dict(bc=K.KEL_BC_FLUID, collide=1),
+        5: dict(bc=K.KEL_BC_MOVING_WALL, u=(0.06, 0.0, 0.02) if q != 9 else (0.06, 0.0, 0.0)),
+        6: dict(bc=K.KEL_BC_HALFWAY_WALL),
+    }
+    return dict(q=q, dims=tuple(dims), f64=f64, periodic=periodic, steps=steps,
+                program=K.make_program(0.7, K.KEL_COLL_BGK_GUO, ops, global_force=(2e-5, -1e-5, 0.0),
+                                       arithmetic=arithmetic),
+                flags=flags, init=random_populations(q, n, rng), profile=None, porosity=None, force=None)
+
+
 def run_oracle(case):
     """Run a case on the CPU oracle; returns (populations AoS, rho, vel)."""
     from oracle.oracle import OracleLattice
