@@ -462,8 +462,7 @@ __device__ __forceinline__ bool cell_update(float (&f)[L::Q], int flag, int y, c
 	}
 	if (flag >= MAX_FLAGS) return false; // the drivers' `default: break;`
 	const OpEntry *op = p.ops + flag;
-	const int bc = __ldg(&op->bc);
-	if (bc == BC_HALFWAY_WALL) return false; // solid: the sweep writes nothing for it
+	const int bc = __ldg(&op->bc); // BC_HALFWAY_WALL: no boundary step and collide = 0 (lower_program)
 	float cpy[L::Q];
 	switch (bc) {
 	case BC_BOUNCE_BACK: // boundary.hpp:58-75 (full-way)
@@ -880,7 +879,10 @@ __global__ void __launch_bounds__(256) sweep2_kernel(const __grid_constant__ Swe
 // global-load latency, and 32 resident warps per SM keep more loads in
 // flight than 24 at 80 registers (measured +3 % FP32, +6 % FP16S at 256^3;
 // the few spilled words stay in L1).
-template <class L, int STORE, bool ODD, int COLL, bool EXACT>
+// HW: the lattice has half-way walls (p.hw_mask set); a separate
+// instantiation, so that the stores' redirection costs the common case
+// nothing.
+template <class L, int STORE, bool ODD, int COLL, bool EXACT, bool HW = false>
 __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ SweepParams p) {
 	using S = Store<STORE>;
 	constexpr int Q = L::Q;
@@ -958,7 +960,7 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 #pragma unroll
 		for (int k = 0; k < L::D; ++k) p.u[k * p.plane + cell] = u[k];
 	}
-	if (p.hw_mask) {
+	if (HW) {
 		// half-way bounce-back: a wall cell writes nothing; a population sent
 		// towards a wall goes to the slot this cell reads f_opp(i) from next
 		// step (even: A[i][x + c_i], which the odd step reads as

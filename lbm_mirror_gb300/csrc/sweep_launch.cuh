@@ -60,7 +60,7 @@ static cudaError_t launch_variant(const SweepParams &p, cudaStream_t st) {
 	if (p.hw_mask) { // half-way walls: the one-cell sweep only (other shapes fall back to it)
 		const int b1 = p.cpt == 1 ? block : 256;
 		dim3 grid((p.nxp + b1 - 1) / b1, p.ny, p.nz);
-		sweep1_kernel<L, STORE, ODD, COLL, EXACT><<<grid, b1, 0, st>>>(p);
+		sweep1_kernel<L, STORE, ODD, COLL, EXACT, true><<<grid, b1, 0, st>>>(p);
 		return cudaGetLastError();
 	}
 	if (p.cpt == CPT_ROWS) return launch_rows<L, STORE, ODD, COLL, EXACT>(p, st);
