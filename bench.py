@@ -305,7 +305,8 @@ def run_warm_start(args, rank, world):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     model = WS.train(WS.steady_subset(states), epochs=args.epochs, batch=32, lr=2e-3, widths=widths,
-                     log_every=32, rho_target_rms=args.rho_rms, residual=args.residual)
+                     log_every=32, rho_target_rms=args.rho_rms, residual=args.residual,
+                     weight_by_steps=args.weight_by_steps)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     n_steps = args.epochs * (args.train // 32)
@@ -333,7 +334,7 @@ def run_warm_start(args, rank, world):
                 "steps": r["warm_steps_max"], "warmup": 0, "ms_per_step": None, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 lattice, bf16 network", "data": "synthetic",
                 "config": {"workload": "d2q9_warm_start_256x64", "train": args.train, "test": args.test,
-                           "tol": args.tol, "check_every": 1000, "epochs": args.epochs, "rho_target_rms": args.rho_rms, "residual_u": args.residual,
+                           "tol": args.tol, "check_every": 1000, "epochs": args.epochs, "rho_target_rms": args.rho_rms, "residual_u": args.residual, "weight_by_steps": args.weight_by_steps,
                            "widths": list(widths),
                            "params": model.net.n_params, "rho_scale": model.rho_scale},
                 "plain_seconds": r["plain_seconds"], "speedup": r["speedup"],
@@ -504,6 +505,8 @@ def main():
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--rho-rms", type=float, default=0.25,
                     help="warm start: RMS of the normalised density target (its weight in the loss)")
+    ap.add_argument("--weight-by-steps", action="store_true",
+                    help="warm start: draw training channels in proportion to their steps from rest")
     ap.add_argument("--residual", action="store_true",
                     help="warm start: predict the correction to the local Poiseuille estimate of u_x")
     ap.add_argument("--save-dir", default="", help="warm start: directory for the trained parameters")

@@ -139,9 +139,12 @@ def targets(states: SteadyStates, rho_scale=None, rho_target_rms=0.25):
 
 
 def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, warmup=100, seed=1,
-          widths=(32, 64, 128, 128), log_every=0, rho_target_rms=0.25, residual=False):
+          widths=(32, 64, 128, 128), log_every=0, rho_target_rms=0.25, residual=False, weight_by_steps=False):
     """Train the U-Net on the steady states with Adam (cosine schedule).
     rho_target_rms sets the weight of the density in the loss (see targets).
+    With weight_by_steps the minibatches draw channels with probability
+    proportional to the steps their run from rest took (the slow channels
+    dominate the time to steady state), instead of a permutation per epoch.
     With `residual` the u_x output is the correction to the local Poiseuille
     estimate the input planes carry (2 x plane 9 = u_x / u_max of the column's
     gap, its flux share by h^3): kel_unet_set_residual(0, 9, 2).
@@ -165,8 +168,15 @@ def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, 
     gen = torch.Generator(device=dev)
     gen.manual_seed(seed)
     step = 0
+    pw = None
+    if weight_by_steps:
+        w = np.asarray(states.steps, dtype=np.float64)
+        pw = torch.from_numpy(w / w.sum()).to(dev)
     for _ in range(epochs):
-        perm = torch.randperm(n, device=dev, generator=gen)
+        if pw is None:
+            perm = torch.randperm(n, device=dev, generator=gen)
+        else:
+            perm = torch.multinomial(pw, n, replacement=True, generator=gen)
         for i in range(steps_per_epoch):
             idx = perm[i * batch:(i + 1) * batch]
             mb_mask = d_mask.index_select(0, idx).contiguous()
