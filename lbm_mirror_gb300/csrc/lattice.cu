@@ -202,6 +202,7 @@ extern "C" int kel_lattice_destroy(kel_lattice *L) {
 	cudaFree(L->d_seen);
 	cudaFree(L->d_err);
 	cudaFree(L->hw_mask);
+	if (L->graph) cudaGraphExecDestroy(L->graph);
 	cudaFree(L->rho);
 	cudaFree(L->u);
 	cudaFree(L->por);
@@ -973,6 +974,38 @@ extern "C" int kel_lattice_autotune(kel_lattice *L, const kel_step_program *P, i
 	return KEL_OK;
 }
 
+constexpr int GRAPH_STEPS = 64;
+
+// The captured graph of GRAPH_STEPS sweeps from an even step, for launch
+// parameters p (compared bit for bit with those of the cached graph; a
+// change re-captures).  A failed capture leaves the caller on plain launches.
+static int ensure_step_graph(kel_lattice *L, const SweepParams &p, int coll, bool exact) {
+	if (L->graph && L->graph_coll == coll && L->graph_exact == exact && memcmp(&L->graph_params, &p, sizeof(p)) == 0)
+		return KEL_OK;
+	if (L->graph) cudaGraphExecDestroy(L->graph);
+	L->graph = nullptr;
+	cudaGraph_t g = nullptr;
+	if (cudaStreamBeginCapture(L->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+		cudaGetLastError();
+		return KEL_ERR_CUDA;
+	}
+	cudaError_t e = cudaSuccess;
+	for (int k = 0; k < GRAPH_STEPS && e == cudaSuccess; ++k) e = launch_one(L, p, coll, exact, (k & 1) != 0);
+	cudaError_t e2 = cudaStreamEndCapture(L->stream, &g);
+	if (e == cudaSuccess && e2 == cudaSuccess && g) e = cudaGraphInstantiate(&L->graph, g, 0);
+	else if (e == cudaSuccess) e = e2;
+	if (g) cudaGraphDestroy(g);
+	if (e != cudaSuccess || !L->graph) {
+		cudaGetLastError();
+		L->graph = nullptr;
+		return KEL_ERR_CUDA;
+	}
+	L->graph_params = p;
+	L->graph_coll = coll;
+	L->graph_exact = exact;
+	return KEL_OK;
+}
+
 extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_steps, uint32_t step_flags) {
 	if (!L || !P) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: null argument");
 	if (step_flags & ~(KEL_STEP_WRITE_MACROS | KEL_STEP_ALL_MACROS))
@@ -991,7 +1024,30 @@ extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_st
 
 	SweepParams p = make_params(L, P);
 	const bool exact = P->arithmetic == KEL_ARITH_REFERENCE;
-	for (uint64_t s = 0; s < n_steps; ++s) {
+	uint64_t s = 0;
+	// Long runs without macro output replay a captured graph of GRAPH_STEPS
+	// sweeps (starting at an even step): one launch per block of steps
+	// instead of one per step, which is what bounds small lattices.
+	const uint64_t plain = (step_flags & KEL_STEP_ALL_MACROS)
+							   ? 0
+							   : ((step_flags & KEL_STEP_WRITE_MACROS) && n_steps > 0 ? n_steps - 1 : n_steps);
+	if (L->stream != nullptr && L->cpt != CPT_ROWS && plain >= 2 * GRAPH_STEPS) {
+		p.write_macros = 0;
+		for (; (L->t & 1u) && s < plain; ++s, ++L->t) {
+			cudaError_t e = launch_one(L, p, P->collision, exact, true);
+			if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_step: launch failed: %s", cudaGetErrorString(e));
+		}
+		const uint64_t reps = (plain - s) / GRAPH_STEPS;
+		if (reps > 0 && ensure_step_graph(L, p, P->collision, exact) == KEL_OK) {
+			for (uint64_t r = 0; r < reps; ++r) {
+				cudaError_t e = cudaGraphLaunch(L->graph, L->stream);
+				if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_step: graph launch failed: %s", cudaGetErrorString(e));
+			}
+			s += reps * GRAPH_STEPS;
+			L->t += reps * GRAPH_STEPS;
+		}
+	}
+	for (; s < n_steps; ++s) {
 		p.write_macros = (step_flags & KEL_STEP_ALL_MACROS) || ((step_flags & KEL_STEP_WRITE_MACROS) && s + 1 == n_steps);
 		const bool odd = (L->t & 1u) != 0;
 		cudaError_t e = launch_one(L, p, P->collision, exact, odd);

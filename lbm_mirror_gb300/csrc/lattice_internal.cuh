@@ -67,5 +67,9 @@ struct kel_lattice {
 	bool rows_used = false;    // a row-pipeline sweep was launched (d_err worth reading)
 	uint32_t *hw_mask = nullptr; // half-way wall neighbour bits per cell (allocated on first use)
 	bool hw_active = false;      // the current program has half-way walls present in the lattice
+	cudaGraphExec_t graph = nullptr;    // GRAPH_STEPS captured sweeps (kel_step), for graph_params
+	kel::gb::SweepParams graph_params;
+	int graph_coll = -1;
+	bool graph_exact = false;
 	bool tuned = false;
 };

@@ -220,3 +220,26 @@ def test_autotune_restores_state_and_keeps_results():
     np.testing.assert_array_equal(lat.populations(np.float64), before)
     lat.step(prog, case["steps"] - 7)
     np.testing.assert_array_equal(lat.populations(np.float64), dfs)
+
+
+@pytest.mark.parametrize("chunks", [[10000], [3, 9997], [1, 130, 9869]])
+def test_graph_replay_on_a_stream_bit_exact(chunks):
+    """On a non-default stream, long kel_step calls replay a captured graph
+    of sweeps (entered at even or odd steps): config C1 at full size stays
+    bit-exact against the reference."""
+    torch = pytest.importorskip("torch")
+    from lbm_mirror_gb300 import Lattice
+    case, dfs, rho, vel = G.load("poiseuille_256x64")
+    prog = with_arith(case["program"], K.KEL_ARITH_REFERENCE)
+    st = torch.cuda.Stream()
+    lat = Lattice("D2Q9", case["dims"], stream=st.cuda_stream)
+    lat.upload_flags(case["flags"])
+    if case["profile"] is not None:
+        lat.upload_inlet_profile(case["profile"])
+    for c in chunks:
+        lat.step(prog, c)
+    f = lat.populations(np.float64)
+    r, v = lat.macros()
+    lat.close()
+    np.testing.assert_array_equal(f, dfs)
+    np.testing.assert_array_equal(v.astype(np.float64), vel)
