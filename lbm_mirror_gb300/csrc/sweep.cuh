@@ -333,9 +333,11 @@ __device__ __forceinline__ void zouhe_velocity_d2q9(float (&f)[9], bool east, fl
 	}
 }
 
-// D3Q27 ZouHePressureX<East>, modules/core/c++/boundary.hpp:229-756
-template <bool EXACT>
-__device__ __forceinline__ void zouhe_pressure_d3q27(float (&f)[27], bool east, float rs) {
+// D3Q27 ZouHePressureX<East>, modules/core/c++/boundary.hpp:229-756.  The
+// side is a template argument: a run-time side would index f with a run-time
+// offset and move the whole population array to local memory.
+template <bool EXACT, bool east>
+__device__ __forceinline__ void zouhe_pressure_d3q27(float (&f)[27], float rs) {
 	using A = Ar<true>;
 	const float a = (float)(4.0 / 9.0), b = (float)(1.0 / 9.0), e = (float)(1.0 / 36.0);
 	float S = f[0];
@@ -348,7 +350,7 @@ __device__ __forceinline__ void zouhe_pressure_d3q27(float (&f)[27], bool east, 
 	S = A::add(S, f[21]);
 	S = A::add(S, f[24]);
 	// known side: cx = +1 at x = max (east = false), cx = -1 at x = 0 (east = true)
-	const int k0 = east ? 1 : 2;
+	constexpr int k0 = east ? 1 : 2;
 	float K = f[k0];
 #pragma unroll
 	for (int j = 1; j < 9; ++j) K = A::add(K, f[k0 + 3 * j]);
@@ -377,7 +379,7 @@ __device__ __forceinline__ void zouhe_pressure_d3q27(float (&f)[27], bool east, 
 	tz = A::add(tz, f[k0 + 21]);
 	tz = A::add(tz, f[k0 + 24]);
 	ruz = A::add(ruz, A::mul(2.f, tz));
-	if (!east) {
+	if constexpr (!east) {
 		f[1] = A::sub(f[2], A::mul(a, rux));
 		f[4] = A::sub(f[5], A::mul(b, A::add(rux, ruy)));
 		f[7] = A::add(f[8], A::mul(b, A::add(-rux, ruy)));
@@ -491,7 +493,10 @@ __device__ __forceinline__ bool cell_update(float (&f)[L::Q], int flag, int y, c
 		break;
 	case BC_ZOUHE_PRESSURE_X:
 		if constexpr (L::Q == 9) zouhe_pressure_d2q9<EXACT>(f, __ldg(&op->east) != 0, __ldg(&op->rho));
-		if constexpr (L::Q == 27) zouhe_pressure_d3q27<EXACT>(f, __ldg(&op->east) != 0, __ldg(&op->rho));
+		if constexpr (L::Q == 27) {
+			if (__ldg(&op->east) != 0) zouhe_pressure_d3q27<EXACT, true>(f, __ldg(&op->rho));
+			else zouhe_pressure_d3q27<EXACT, false>(f, __ldg(&op->rho));
+		}
 		break;
 	case BC_ZOUHE_VELOCITY_X:
 		if constexpr (L::Q == 9) {
