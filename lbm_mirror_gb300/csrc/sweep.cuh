@@ -871,6 +871,182 @@ __global__ void __launch_bounds__(256) sweep2_kernel(const __grid_constant__ Swe
 }
 
 
+// Two consecutive cells per thread in FP16S storage, the pair held as raw
+// halves: one 32-bit register per population (cell x0 in the low half, x0 + 1
+// in the high half) from the load to the store, so each 32-bit access moves
+// two cells' populations and the pair costs what one cell of sweep1_kernel
+// costs in registers.  The two cells are collided one after the other (the
+// loop over them is not unrolled): one cell's FP32 populations are live at a
+// time.  A warp covers 32 pairs of one row (nxp is even in FP16S storage);
+// x-shifted odd-step accesses are realigned with one warp shuffle per
+// direction, and the lanes at a warp's or row's end touch the neighbouring
+// pair with a 16-bit access.  Per cell the arithmetic is that of
+// sweep1_kernel: f_i = half(A) + w_i on load (0 for the ghost ring),
+// A = half_rn(f_i - w_i) on store.
+template <class L, bool ODD, int COLL, bool EXACT>
+__global__ void __launch_bounds__(256, 4) sweep2h_kernel(const __grid_constant__ SweepParams p) {
+	constexpr int Q = L::Q;
+	static_assert(Q <= 32, "one zero bit per population");
+	const int lane = threadIdx.x & 31;
+	const int64_t gwarp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+	const int64_t row = gwarp / p.wpr2;
+	const int64_t nrows = static_cast<int64_t>(p.ny) * p.nz;
+	if (row >= nrows) return; // warp-uniform: a warp never spans rows
+	const int nxp = p.nxp;
+	const int x0 = 2 * (static_cast<int>(gwarp % p.wpr2) * 32 + lane);
+	const bool active = x0 < nxp; // nxp even: x0 + 1 < nxp too
+	const int y = static_cast<int>(row % p.ny);
+	const int z = static_cast<int>(row / p.ny);
+	const int64_t rbase = row * nxp;
+	const int64_t oy = nxp, oz = static_cast<int64_t>(nxp) * p.ny;
+	const unsigned FULL = 0xffffffffu;
+	unsigned short *const A = static_cast<unsigned short *>(p.f);
+	auto ld2h = [&](int64_t idx) { return __ldcs(reinterpret_cast<const unsigned *>(A + idx)); };
+	auto st2h = [&](int64_t idx, unsigned v) { __stcs(reinterpret_cast<unsigned *>(A + idx), v); };
+	auto ld1h = [&](int64_t idx) { return static_cast<unsigned>(__ldcs(A + idx)); };
+	auto st1h = [&](int64_t idx, unsigned v) { __stcs(A + idx, static_cast<unsigned short>(v)); };
+
+	uint32_t h[Q];
+	uint32_t zero0 = 0u, zero1 = 0u; // bit i: f_i of cell x0 / x0 + 1 is the ghost ring's zero
+
+	// ---- gather the post-stream populations of the pair ---------------------
+#pragma unroll
+	for (int i = 0; i < Q; ++i) {
+		if (!ODD) {
+			h[i] = active ? ld2h(static_cast<int64_t>(i) * p.plane + rbase + x0) : 0u;
+		} else {
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int sy = y - cy, sz = z - cz;
+			const bool row_in = (sy >= 0) && (sy < p.ny) && (sz >= 0) && (sz < p.nz);
+			const int64_t sb = static_cast<int64_t>(L::opp(i)) * p.plane + rbase - cy * oy - cz * oz;
+			const unsigned w = (row_in && active) ? ld2h(sb + x0) : 0u;
+			if (!row_in) {
+				zero0 |= 1u << i;
+				zero1 |= 1u << i;
+			}
+			if (cx == 0) {
+				h[i] = w;
+			} else if (cx > 0) { // sources x0 - 1, x0
+				unsigned lo = __shfl_up_sync(FULL, w, 1) >> 16;
+				if (lane == 0 || x0 == 0) {
+					lo = 0u;
+					if (row_in && active) {
+						if (x0 > 0) lo = ld1h(sb + x0 - 1);
+						else if (p.periodic) lo = ld1h(sb + nxp - 1);
+						else zero0 |= 1u << i;
+					}
+				}
+				h[i] = lo | (w << 16);
+			} else { // sources x0 + 1, x0 + 2
+				unsigned hi = __shfl_down_sync(FULL, w, 1) & 0xffffu;
+				if (lane == 31 || x0 + 2 >= nxp) {
+					hi = 0u;
+					if (row_in && active) {
+						if (x0 + 2 < nxp) hi = ld1h(sb + x0 + 2);
+						else if (p.periodic) hi = ld1h(sb);
+						else zero1 |= 1u << i;
+					}
+				}
+				h[i] = (w >> 16) | (hi << 16);
+			}
+		}
+	}
+
+	// ---- boundary step + collision, one cell after the other ----------------
+	uchar2 fl = make_uchar2(0, 0);
+	if (active) fl = *reinterpret_cast<const uchar2 *>(p.flags + rbase + x0);
+	float2 porv = make_float2(1.f, 1.f);
+	if ((COLL == COLL_PSM || COLL == COLL_PSM_GUO || COLL == COLL_HLBM) && active)
+		porv = *reinterpret_cast<const float2 *>(p.por + rbase + x0);
+	float2 fcv[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+	if ((COLL == COLL_BGK_GUO || COLL == COLL_PSM_GUO) && active) {
+#pragma unroll
+		for (int k = 0; k < L::D; ++k) fcv[k] = *reinterpret_cast<const float2 *>(p.force + k * p.plane + rbase + x0);
+	}
+	if (COLL == COLL_HLBM && active) {
+		fcv[0] = *reinterpret_cast<const float2 *>(p.hN + rbase + x0);
+		fcv[1] = *reinterpret_cast<const float2 *>(p.hN + p.plane + rbase + x0);
+		fcv[2] = *reinterpret_cast<const float2 *>(p.hD + rbase + x0);
+	}
+	const CellCtx ctx = cell_ctx(p);
+#pragma unroll 1
+	for (int k = 0; k < 2; ++k) {
+		const int sh = 16 * k;
+		const uint32_t zm = k ? zero1 : zero0;
+		float c[Q];
+#pragma unroll
+		for (int i = 0; i < Q; ++i) {
+			const float v = __half2float(__ushort_as_half(static_cast<unsigned short>(h[i] >> sh)));
+			c[i] = ((zm >> i) & 1u) ? 0.f : v + p.wshift[i];
+		}
+		const float Fc[3] = {k ? fcv[0].y : fcv[0].x, k ? fcv[1].y : fcv[1].x, k ? fcv[2].y : fcv[2].x};
+		float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
+		const bool col = cell_update<L, COLL, EXACT>(c, k ? fl.y : fl.x, y, ctx, k ? porv.y : porv.x, Fc, rho, u);
+		if (p.write_macros && col && active) {
+			p.rho[rbase + x0 + k] = rho;
+#pragma unroll
+			for (int d = 0; d < L::D; ++d) p.u[d * p.plane + rbase + x0 + k] = u[d];
+		}
+		const uint32_t keep = k ? 0x0000ffffu : 0xffff0000u;
+#pragma unroll
+		for (int i = 0; i < Q; ++i) {
+			const uint32_t b = __half_as_ushort(__float2half_rn(c[i] - p.wshift[i]));
+			h[i] = (h[i] & keep) | (b << sh);
+		}
+	}
+
+	// ---- scatter the post-collision populations -----------------------------
+#pragma unroll
+	for (int i = 0; i < Q; ++i) {
+		if (!ODD) {
+			if (active) st2h(static_cast<int64_t>(L::opp(i)) * p.plane + rbase + x0, h[i]);
+		} else {
+			const int cx = L::cx(i), cy = L::cy(i), cz = L::cz(i);
+			const int64_t pb = static_cast<int64_t>(i) * p.plane;
+			// slots of this row whose source lies outside: the ghost ring's zero
+			{
+				const uint32_t zh = __half_as_ushort(__float2half_rn(0.f - p.wshift[i]));
+				const int sy = y - cy, sz = z - cz;
+				const bool src_row_in = (sy >= 0) && (sy < p.ny) && (sz >= 0) && (sz < p.nz);
+				if (!src_row_in) {
+					if (active) st2h(pb + rbase + x0, zh | (zh << 16));
+				} else if (!p.periodic && active) {
+					if (cx > 0 && x0 == 0) st1h(pb + rbase, zh);
+					if (cx < 0 && x0 + 2 == nxp) st1h(pb + rbase + nxp - 1, zh);
+				}
+			}
+			const int dy = y + cy, dz = z + cz;
+			const bool row_in = (dy >= 0) && (dy < p.ny) && (dz >= 0) && (dz < p.nz);
+			const int64_t db = pb + rbase + cy * oy + cz * oz;
+			if (cx == 0) {
+				if (row_in && active) st2h(db + x0, h[i]);
+			} else if (cx > 0) { // destinations x0 + 1, x0 + 2
+				const unsigned q = __shfl_up_sync(FULL, h[i], 1);
+				if (row_in && active) {
+					if (lane > 0) st2h(db + x0, (q >> 16) | (h[i] << 16));
+					else st1h(db + x0 + 1, h[i] & 0xffffu); // element x0: previous warp, or the ghost slot
+					if (x0 + 2 < nxp) {
+						if (lane == 31) st1h(db + x0 + 2, h[i] >> 16);
+					} else if (p.periodic) {
+						st1h(db, h[i] >> 16);
+					}
+				}
+			} else { // destinations x0 - 1, x0
+				const unsigned r = __shfl_down_sync(FULL, h[i], 1);
+				if (row_in && active) {
+					if (lane < 31 && x0 + 2 < nxp) st2h(db + x0, (h[i] >> 16) | (r << 16));
+					else st1h(db + x0, h[i] >> 16); // element x0 + 1: next warp, or the ghost slot
+					if (x0 > 0) {
+						if (lane == 0) st1h(db + x0 - 1, h[i] & 0xffffu);
+					} else if (p.periodic) {
+						st1h(db + nxp - 1, h[i] & 0xffffu);
+					}
+				}
+			}
+		}
+	}
+}
+
 // One cell per thread.  Same physics and the same AA addressing as
 // sweep_kernel, with 32-bit accesses: the x-shifted loads/stores of odd steps
 // are plain unit offsets, coalesced across the warp, and the register budget

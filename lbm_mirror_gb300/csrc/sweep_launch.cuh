@@ -67,7 +67,10 @@ static cudaError_t launch_variant(const SweepParams &p, cudaStream_t st) {
 	if (p.cpt == 2) {
 		const int64_t threads = static_cast<int64_t>(p.ny) * p.nz * p.wpr2 * 32;
 		const int64_t blocks = (threads + block - 1) / block;
-		sweep2_kernel<L, STORE, ODD, COLL, EXACT><<<static_cast<unsigned>(blocks), block, 0, st>>>(p);
+		if constexpr (STORE == STORE_FP16S) // nxp is even in FP16S storage
+			sweep2h_kernel<L, ODD, COLL, EXACT><<<static_cast<unsigned>(blocks), block, 0, st>>>(p);
+		else
+			sweep2_kernel<L, STORE, ODD, COLL, EXACT><<<static_cast<unsigned>(blocks), block, 0, st>>>(p);
 		return cudaGetLastError();
 	}
 	if constexpr (COLL == COLL_HLBM) { // one cell per thread only

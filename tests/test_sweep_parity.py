@@ -145,6 +145,22 @@ def test_row_pipeline_and_two_cell_sweep_same_bits_as_one_cell_sweep(q, storage)
             np.testing.assert_array_equal(x, y)
 
 
+@pytest.mark.parametrize("periodic", [False, True], ids=["bounded", "periodic"])
+@pytest.mark.parametrize("coll", [K.KEL_COLL_BGK, K.KEL_COLL_BGK_GUO, K.KEL_COLL_PSM, K.KEL_COLL_PSM_GUO])
+def test_two_cell_fp16s_same_bits_mixed(coll, periodic):
+    """FP16S two-cell sweep (packed half pairs) against the one-cell sweep:
+    every boundary op, random populations and fields, rows of 2-3 warps of
+    pairs, bounded and periodic x, identical populations and macros."""
+    for case in (G.normalise(cases.mixed_2d(coll, dims=(160, 20), periodic=periodic, steps=23)),
+                 G.normalise(cases.mixed_3d(19, coll, dims=(72, 12, 10), periodic=periodic, steps=15)),
+                 G.normalise(cases.mixed_3d(27, coll, dims=(136, 6, 5), periodic=periodic, steps=15))):
+        a = run_gpu(case, K.KEL_ARITH_FAST, storage="fp16s", launch=(1, 128))
+        for launch in [(2, 64), (2, 256)]:
+            b = run_gpu(case, K.KEL_ARITH_FAST, storage="fp16s", launch=launch)
+            for x, y in zip(a, b):
+                np.testing.assert_array_equal(x, y)
+
+
 def test_closed_box_mass_conservation_and_determinism():
     """Full-size property (C2 extents): 256^3 D3Q19 closed box, all walls
     full-way bounce-back, walls start empty so no population ever leaves the
