@@ -265,14 +265,19 @@ __device__ __forceinline__ void equilibrium(float rho, const float (&u)[3], floa
 		}
 	} else {
 		// w rho (1 + d), d = vcc + (vcc^2/2 - 1.5 vv), with the reference's float
-		// sub-terms and one fused rounding at the end.
+		// sub-terms and one fused rounding at the end.  Opposite directions
+		// share w, and their c.u and vcc are exact negatives (IEEE rounding is
+		// sign-symmetric), so vcc, the symmetric part and w rho are computed
+		// once per pair: the same bits as computing each direction alone.
 		const float h = __fmul_rn(1.5f, vv);
 #pragma unroll
 		for (int i = 0; i < L::Q; ++i) {
+			if (L::opp(i) < i) continue; // done with its partner
 			const float vcc = __fmul_rn(3.0f, cdot<L, true>(i, u));
-			const float d = vcc + __fmaf_rn(0.5f * vcc, vcc, -h);
+			const float sym = __fmaf_rn(0.5f * vcc, vcc, -h);
 			const float wr = __fmul_rn((float)L::w(i), rho);
-			eq[i] = __fmaf_rn(wr, d, wr);
+			eq[i] = __fmaf_rn(wr, vcc + sym, wr);
+			if (L::opp(i) != i) eq[L::opp(i)] = __fmaf_rn(wr, sym - vcc, wr);
 		}
 	}
 }
