@@ -476,7 +476,7 @@ def run_particles(args, rank, world):
 # lattice is too large to capture under ncu's memory save/restore, so its
 # per-launch traffic is this figure times the cells (traffic grows with the
 # cells: every population is read and written once).
-SWEEP1_TRAFFIC_PER_CELL = {(19, "fp32"): 144.6, (19, "fp16s"): 69.1, (27, "fp32"): 213.2}
+SWEEP1_TRAFFIC_PER_CELL = {(19, "fp32"): 144.6, (19, "fp16s"): 69.1, (27, "fp32"): 208.8}
 
 
 def sweep_traffic(q, storage, cpt, cells):
