@@ -165,7 +165,7 @@ __device__ __forceinline__ bool cell_update_shifted(float (&g)[9], int flag, int
 }
 
 template <bool ODD, int MODE>
-__global__ void __launch_bounds__(512) k_batch_sweep(const __grid_constant__ BatchParams p) {
+__global__ void __launch_bounds__(512, MODE == MODE_EXACT ? 1 : 4) k_batch_sweep(const __grid_constant__ BatchParams p) {
 	using L = D2Q9;
 	const int2 tc = p.blist[blockIdx.x]; // (tile, channel)
 	const int ob = tc.x, c = tc.y;
