@@ -13,8 +13,8 @@ Pipeline, all on one GPU:
      (u_x / u_max, u_y / u_max, (rho - 1) / (u_max * rho_scale));
   3. warm start: inference on new geometries, then kel_batch_warm_start
      builds f_eq + f_neq (Chapman-Enskog) populations from the prediction and
-     the same runner continues to the same residual.  The plain run from rest
-     stays the judge of convergence: a warm-started channel stops by the same
+     the same runner continues to the same residual.  Convergence is tested
+     as in the plain run from rest: a warm-started channel stops by the same
      residual test.
 
 Device memory is held in torch tensors (plumbing only); every kernel on the
