@@ -88,40 +88,79 @@ def make_case(name):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled while the GPU is busy.
+
+    The GPU is named by its UUID (an ordinal would name another GPU under
+    CUDA_VISIBLE_DEVICES remapping).  A timed region of a few milliseconds is
+    shorter than the 200 ms sampling period, so the bench brackets it with
+    back-to-back untimed sweeps: the samples cover a window of about a second
+    of sustained load that contains the timed region."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index):
-        self.gpu = gpu_index
+    def __init__(self, device):
+        self.gpu = self.gpu_id(device)
         self.proc = None
         self.file = None
+        self.t0 = None
+
+    @staticmethod
+    def gpu_id(device):
+        try:
+            import torch
+            u = getattr(torch.cuda.get_device_properties(device), "uuid", None)
+            if u is not None:
+                u = str(u)
+                return u if u.startswith("GPU-") else "GPU-" + u
+        except Exception:
+            pass
+        return str(device)
 
     def start(self):
         try:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                ["nvidia-smi", "-i", self.gpu, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                  "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+            self.t0 = time.perf_counter()
         except Exception:
             self.proc = None
 
-    def stop(self):
-        if self.proc is None:
-            return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
+    def _rows(self):
+        if self.file is None:
+            return []
         self.file.flush()
         rows = []
         for line in open(self.file.name):
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 9:
                 rows.append(parts)
+        return rows
+
+    def keep_busy(self, work, seconds):
+        """Run work() back to back (each call ends with a device sync) until
+        `seconds` have passed and at least one sample has been written (at
+        most 5 s more).  Returns the number of calls."""
+        n, t0 = 0, time.perf_counter()
+        while True:
+            work()
+            n += 1
+            dt = time.perf_counter() - t0
+            if dt >= seconds and (self.proc is None or self._rows() or dt >= seconds + 5.0):
+                return n
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        window = time.perf_counter() - self.t0
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = self._rows()
         os.unlink(self.file.name)
         if not rows:
             return None
@@ -130,7 +169,7 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "window_s": round(window, 3), "gpu": self.gpu}
 
 
 def cpu_baseline_sample(name, seconds=10.0):
@@ -306,7 +345,8 @@ def run_warm_start(args, rank, world):
     t0 = time.perf_counter()
     model = WS.train(WS.steady_subset(states), epochs=args.epochs, batch=32, lr=2e-3, widths=widths,
                      log_every=32, rho_target_rms=args.rho_rms, residual=args.residual,
-                     weight_by_steps=args.weight_by_steps)
+                     weight_by_steps=args.weight_by_steps, rho_norm=args.rho_norm,
+                     rho_residual=args.rho_residual)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     n_steps = args.epochs * (args.train // 32)
@@ -334,7 +374,10 @@ def run_warm_start(args, rank, world):
                 "steps": r["warm_steps_max"], "warmup": 0, "ms_per_step": None, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 lattice, bf16 network", "data": "synthetic",
                 "config": {"workload": "d2q9_warm_start_256x64", "train": args.train, "test": args.test,
-                           "tol": args.tol, "check_every": 1000, "epochs": args.epochs, "rho_target_rms": args.rho_rms, "residual_u": args.residual, "weight_by_steps": args.weight_by_steps,
+                           "tol": args.tol, "check_every": 1000, "epochs": args.epochs,
+                           "rho_target_rms": args.rho_rms, "residual_u": args.residual,
+                           "weight_by_steps": args.weight_by_steps, "rho_norm": args.rho_norm,
+                           "rho_residual": args.rho_residual,
                            "widths": list(widths),
                            "params": model.net.n_params, "rho_scale": model.rho_scale},
                 "plain_seconds": r["plain_seconds"], "speedup": r["speedup"],
@@ -442,7 +485,8 @@ def run_particles(args, rank, world):
     lat.upload_flags(flags)
     ps = Particles(lat, st)
     tuned = lat.autotune(prog, steps=8)
-    ps.step(prm, prog, args.warmup, write_macros=False)
+    # warm-up long enough to capture the two-step graph the coupled step replays
+    ps.step(prm, prog, max(args.warmup, 8), write_macros=False)
     lat.synchronize()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     ev[0].record(stream)
@@ -465,14 +509,16 @@ def run_particles(args, rank, world):
             "roofline": {"bound": "hbm", "achieved": bpu * cells / (sweep_ms / 1e3) / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": bpu * cells / (sweep_ms / 1e3) / 1e9 / peak, "traffic": None,
                          "peak_source": src, "bytes_per_update": bpu, "kernel": "PSM+Guo sweep"},
-            "gpu_launches": args.steps * 6}
+            "gpu_launches": args.steps * 6,
+            "launches_per_step": "reset+boxes, couple (bodies' boxes only), gather (blocks per body), "
+                                 "contact (+ gather sums), integrate, sweep; graph-replayed in pairs of steps"}
     if rank == 0:
         print(json.dumps(line))
 
 
 # DRAM bytes (read + write) per cell update of the one-cell sweep, from ncu
 # dram__bytes_read.sum + dram__bytes_write.sum on the 192^3 cavity (both
-# parities averaged; profiles/sweep1_cavity192_traffic.md).  The 256^3 bench
+# parities averaged).  The 256^3 bench
 # lattice is too large to capture under ncu's memory save/restore, so its
 # per-launch traffic is this figure times the cells (traffic grows with the
 # cells: every population is read and written once).
@@ -492,6 +538,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="d3q19_cavity_256", choices=sorted(WORKLOADS))
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16s"])
+    ap.add_argument("--arith", default="fast", choices=["fast", "reference"],
+                    help="collision arithmetic of the headline sweep (reference: the reference's own rounding, "
+                         "bit-exact with it)")
     ap.add_argument("--cpt", type=int, default=0, help="cells per thread of the sweep (0: library default)")
     ap.add_argument("--block", type=int, default=256)
     ap.add_argument("--e2e-iters", type=int, default=3)
@@ -510,6 +559,11 @@ def main():
     ap.add_argument("--residual", action="store_true",
                     help="warm start: predict the correction to the local Poiseuille estimate of u_x")
     ap.add_argument("--save-dir", default="", help="warm start: directory for the trained parameters")
+    ap.add_argument("--rho-norm", default="global", choices=["global", "lubrication"],
+                    help="warm start: density target over u_max (global) or over the channel's lubrication "
+                         "pressure drop")
+    ap.add_argument("--rho-residual", action="store_true",
+                    help="warm start: the density output corrects the lubrication pressure plane")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -547,7 +601,7 @@ def main():
 
     from lbm_mirror_gb300 import Lattice
     from lbm_mirror_gb300 import capi as K
-    from tests.gpu_util import QNAME
+    from tests.gpu_util import QNAME, with_arith
 
     case = make_case(args.workload)
     q, dims = case["q"], case["dims"]
@@ -557,7 +611,8 @@ def main():
     lat.upload_flags(case["flags"])
     if case["profile"] is not None:
         lat.upload_inlet_profile(case["profile"])
-    prog = case["program"]
+    arith = {"fast": K.KEL_ARITH_FAST, "reference": K.KEL_ARITH_REFERENCE}
+    prog = with_arith(case["program"], arith[args.arith])
     if args.cpt:
         lat.set_launch(args.cpt, args.block)
         tuned = None
@@ -571,16 +626,26 @@ def main():
     clocks = ClockSampler(torch.cuda.current_device())
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+
+    def busy():  # untimed sweeps around the timed region (also warms kel_step's graph)
+        lat.step(prog, 256, write_macros=False)
+        lat.synchronize()
+
+    clocks.start()
+    soak = clocks.keep_busy(busy, 0.5)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
     ev0.record(stream)
     lat.step(prog, args.steps, write_macros=False)
     ev1.record(stream)
     ev1.synchronize()
     torch.cuda.synchronize()
+    soak += clocks.keep_busy(busy, 0.5)
     clk = clocks.stop()
+    if clk is not None:
+        clk["note"] = (f"sampled over back-to-back sweeps containing the timed region "
+                       f"({soak} x 256 untimed sweeps around it)")
     ms = max_over_ranks(ev0.elapsed_time(ev1), dist)
     per_launch_s = ms / 1e3 / args.steps
     value = whole_job_rate(ncell * args.steps, world, ms / 1e3) / 1e6
@@ -588,6 +653,23 @@ def main():
     bpu = bytes_per_update(q, args.storage)
     peak, peak_src = load_peaks()
     achieved = bpu * ncell / per_launch_s / 1e9
+
+    # ---- the other collision arithmetic, same lattice, same step count -----
+    other = "reference" if args.arith == "fast" else "fast"
+    oprog = with_arith(case["program"], arith[other])
+    lat.step(oprog, args.warmup, write_macros=False)
+    lat.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    lat.step(oprog, args.steps, write_macros=False)
+    ev1.record(stream)
+    ev1.synchronize()
+    oms = max_over_ranks(ev0.elapsed_time(ev1), dist)
+    other_line = {"arithmetic": other, "value": whole_job_rate(ncell * args.steps, world, oms / 1e3) / 1e6,
+                  "unit": "MLUPS", "ms_per_step": oms / args.steps,
+                  "hbm_frac": bpu * ncell / (oms / 1e3 / args.steps) / 1e9 / peak}
 
     # ---- end to end through the C ABI with pinned host buffers ------------
     Q, D = q, (2 if q == 9 else 3)
@@ -640,7 +722,7 @@ def main():
         "vs_baseline": None, "dtype": "f32" if args.storage == "fp32" else "f16-shifted storage, f32 arithmetic",
         "data": "synthetic",
         "config": {"workload": args.workload, "descriptor": f"D{D}Q{Q}", "dims": list(dims), "cells": ncell,
-                   "storage": args.storage, "tau": float(prog.tau), "collision": "BGK", "arithmetic": "fast",
+                   "storage": args.storage, "tau": float(prog.tau), "collision": "BGK", "arithmetic": args.arith,
                    "scheme": "AA in-place, SoA", "cells_per_thread": cpt, "block": block,
                    "autotuned": tuned is not None, "l2": "populations 1.27 GB >> 129 MB L2, no flush needed"
                    if ncell * Q * 4 > 4e8 else "working set smaller than L2",
@@ -653,6 +735,7 @@ def main():
                 "iters": args.e2e_iters, "mean_rho_fluid": mass, "phases_ms": phases},
         "gpu_launches": args.steps,
         "clocks": clk,
+        "other_arithmetic": other_line,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample(args.workload, args.cpu_seconds)

@@ -2,10 +2,15 @@
 
 Runs oracle/_ref/ref_harness (built by oracle/Makefile from the reference's
 headers, unchanged) on every case below and stores inputs + outputs as
-tests/golden/<name>.npz.  Needs the reference tree, so it runs only where the
-reference is mounted; the committed .npz files are what the tests read.
+tests/golden/<name>.npz.  Needs the reference tree, named by the environment
+variable KEL_REFERENCE_ROOT (the harness is built from
+$KEL_REFERENCE_ROOT/modules/core/c++), so it runs only where the reference is
+mounted; the committed .npz files are what the tests read.
 
-    python tests/golden/make_golden.py [--check]
+    KEL_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py [--only NAME] [--check]
+
+--check regenerates every selected fixture and compares it array for array
+with the committed file instead of writing it (exit status 1 on a difference).
 
 Inputs are rounded to float32 before use so that the stored float32 copy is
 exactly what both the reference and the implementations under test consume.
@@ -87,6 +92,30 @@ def run_harness(hcase, case, workdir):
     return dfs, rho, vel
 
 
+CHECK = {"on": False, "bad": []}
+
+
+def emit(name, **arrays):
+    """Write tests/golden/<name>.npz, or with --check compare with it."""
+    path = os.path.join(GOLDEN, name + ".npz")
+    if not CHECK["on"]:
+        np.savez_compressed(path, **arrays)
+        return
+    old = np.load(path)
+    same = set(old.files) == set(arrays) and all(
+        np.array_equal(np.asarray(arrays[k]), old[k]) for k in arrays)
+    if not same:
+        CHECK["bad"].append(name)
+    print(f"{name:28s} check: {'identical' if same else 'DIFFERS'}")
+
+
+def build_harness():
+    ref = os.environ.get("KEL_REFERENCE_ROOT", "")
+    if not ref:
+        raise SystemExit("set KEL_REFERENCE_ROOT to the reference checkout (modules/core/c++ below it)")
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), f"REF={ref}"])
+
+
 def save(name, case, dfs, rho, vel):
     odt = np.float64 if case["f64"] else np.float32
     arrays = dict(
@@ -98,7 +127,7 @@ def save(name, case, dfs, rho, vel):
     for k in ("init", "profile", "porosity", "force"):
         if case[k] is not None:
             arrays[k] = np.asarray(case[k]).astype(np.float32)
-    np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), **arrays)
+    emit(name, **arrays)
 
 
 def load(name):
@@ -257,16 +286,18 @@ def run_writer_harness(name, inp, workdir):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--only", default=None)
+    ap.add_argument("--check", action="store_true", help="compare with the committed fixtures, write nothing")
     args = ap.parse_args()
+    CHECK["on"] = args.check
     if not os.path.exists(HARNESS):
-        subprocess.check_call(["make", "-C", os.path.join(ROOT, "oracle")])
+        build_harness()
     for name, (hcase, kind) in particle_registry().items():
         if args.only and args.only not in name:
             continue
         bodies, init = particle_inputs(kind)
         with tempfile.TemporaryDirectory() as td:
             out = run_particle_harness(hcase, bodies, init, td)
-        np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), bodies=bodies, init=init.astype(np.float32),
+        emit(name, bodies=bodies, init=init.astype(np.float32),
                             params=np.array(json.dumps(PART_PARAMS)), **out)
         print(f"{name:28s} particles: force after gather {out['after_gather'][:, 18:20].ravel()[:4]}")
     for name in HLBM_CASES:
@@ -275,7 +306,7 @@ def main():
         bodies, init, flags = hlbm_inputs()
         with tempfile.TemporaryDirectory() as td:
             out = run_hlbm_harness(name, bodies, init, flags, td)
-        np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), bodies=bodies, init=init, flags=flags,
+        emit(name, bodies=bodies, init=init, flags=flags,
                             params=np.array(json.dumps(HLBM_PARAMS)), **out)
         print(f"{name:28s} hlbm: body force after gather {out['after_gather'][:, 18:20].ravel()[:4]}")
     for name, (q, dims, dtype) in WRITER_CASES.items():
@@ -284,7 +315,7 @@ def main():
         inp = writer_inputs(q, dims, dtype)
         with tempfile.TemporaryDirectory() as td:
             files = run_writer_harness(name, inp, td)
-        np.savez_compressed(os.path.join(GOLDEN, name + ".npz"), **inp,
+        emit(name, **inp,
                             **{"file:" + f: v for f, v in files.items()})
         print(f"{name:28s} writers: " + ", ".join(f"{f} {len(v)} B" for f, v in files.items()))
     for name, (hcase, case) in registry().items():
@@ -298,6 +329,9 @@ def main():
         same = np.array_equal(odfs, dfs) and np.array_equal(orho, rho) and np.array_equal(ovel, vel)
         print(f"{name:28s} steps={case['steps']:6d}  oracle bit-exact: {same}  "
               f"max|dfs diff|={np.abs(odfs - dfs).max():.3e}")
+    if CHECK["bad"]:
+        print("differing fixtures: " + ", ".join(CHECK["bad"]))
+        raise SystemExit(1)
 
 
 if __name__ == "__main__":
