@@ -154,7 +154,14 @@ int kel_upload_inlet_profile(kel_lattice *lat, const double *host_ux, int64_t n)
 
 /* Replaces one iteration of the drivers' loop: the collide+BC
  * parallel_for (e.g. examples/poiseulle_2d_gpu/poiseulle_2d_gpu.cpp:169-224)
- * followed by the Stream parallel_for (:384-399), n_steps times. */
+ * followed by the Stream parallel_for (:384-399), n_steps times.
+ * Asynchronous on the lattice's stream.  The stream may be under a caller's
+ * CUDA graph capture: the sweeps then go into that capture one launch per
+ * step, and the program must have been passed to kel_step once before the
+ * capture (a new program during capture is rejected).  The lattice's time
+ * step advances when kel_step is called, not when a graph is replayed, so a
+ * captured sequence should hold an even number of steps (the AA layout
+ * depends on the parity of the time step). */
 int kel_step(kel_lattice *lat, const kel_step_program *prog, uint64_t n_steps, uint32_t step_flags);
 
 /* ---- particles: spheres (3D) / discs (2D) coupled by PSM -------------- */
@@ -279,6 +286,16 @@ int kel_batch_info(const kel_batch *b, int64_t *cells, int64_t *padded_cells, in
  * neighbours.  The residual's previous velocity becomes the predicted u. */
 int kel_batch_warm_start(kel_batch *b, int32_t first, int32_t count, const float *d_pred, int64_t pred_stride,
 						 const float *d_scale, const float *d_offset, int32_t with_neq);
+/* Refinement of a warm start (no counterpart in the reference), same
+ * prediction arguments: `iterations` times, two sweeps of every active
+ * channel of the batch, then every fluid cell of channels [first, first +
+ * count) keeps the non-equilibrium part of its populations and gets the
+ * predicted field back: f_i <- f_i - f_eq(moments of f) + f_eq(rho_p, u_p)
+ * (rho_p = the cell's own density with keep_rho).  The non-equilibrium part
+ * is then the one the lattice and its boundary rules produce for the
+ * predicted field.  The sweeps count as steps of the channels. */
+int kel_batch_warm_refine(kel_batch *b, int32_t first, int32_t count, const float *d_pred, int64_t pred_stride,
+						  const float *d_scale, const float *d_offset, int32_t iterations, int32_t keep_rho);
 int kel_batch_synchronize(kel_batch *b);
 /* One channel's populations (AoS, nx*ny*9) or macros (rho, u_x, u_y per cell). */
 int kel_batch_download_populations(kel_batch *b, int32_t channel, float *host_aos);
@@ -322,8 +339,10 @@ int kel_unet_synchronize(kel_unet *net);
 /* Input planes from device data: mask (n*H*W bytes, 1 = solid), u_max and tau
  * (n floats each).  Channels: mask, u_max / 0.08, (tau - 0.55) / 0.45, y and x
  * coordinates, the column's open fraction, the downstream resistance
- * sum 1/open^3 / W, the vertical gap height, 4 s (1 - s) across the gap and
- * the lubrication estimate of u_x / u_max (halved); the rest zero. */
+ * sum 1/open^3 / W, the vertical gap height, 4 s (1 - s) across the gap,
+ * the lubrication estimate of u_x / u_max (halved) and the lubrication
+ * pressure S(x) / S(0), S(x) the suffix sum of 1 / sum h^3 over the columns
+ * from x to the outlet; the rest zero. */
 int kel_unet_make_input(kel_unet *net, const uint8_t *d_mask, const float *d_umax, const float *d_tau, int32_t n);
 /* The current input (bf16 NHWC, 16 channels) copied to a device buffer. */
 int kel_unet_get_input(kel_unet *net, uint16_t *d_out_bf16, int32_t n);
@@ -346,9 +365,10 @@ int kel_unet_set_conv_kernel(kel_unet *net, int32_t kind);
 /* Residual head (no counterpart in the reference): output channel
  * `out_channel` becomes the head's value plus `scale` times input plane
  * `in_channel`, so the network learns the correction to that plane (the
- * warm start adds the local Poiseuille estimate of u_x / u_max this way).
- * out_channel < 0 turns it off (the default).  Training and inference use
- * the same setting. */
+ * warm start adds the local Poiseuille estimate of u_x / u_max and the
+ * lubrication pressure this way).  Each call sets one output channel (up to
+ * 8); out_channel < 0 turns all of them off (the default).  Training and
+ * inference use the same setting. */
 int kel_unet_set_residual(kel_unet *net, int32_t out_channel, int32_t in_channel, float scale);
 
 /* Launch shape of the sweep: cells per thread (1: one cell, 32-bit FP32 /

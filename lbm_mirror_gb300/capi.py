@@ -278,6 +278,7 @@ def load_library(path: str | None = None):
         "kel_batch_download_populations": ([vp, i32, vp], C.c_int),
         "kel_batch_download_macros": ([vp, i32, vp], C.c_int),
         "kel_batch_warm_start": ([vp, i32, i32, vp, i64, vp, vp, i32], C.c_int),
+        "kel_batch_warm_refine": ([vp, i32, i32, vp, i64, vp, vp, i32, i32], C.c_int),
         "kel_batch_synchronize": ([vp], C.c_int),
         "kel_write_vtk": ([C.c_char_p, C.c_char_p, u64, C.POINTER(i64), i32, C.POINTER(FieldView), i32], C.c_int),
         "kel_write_csv": ([C.c_char_p, C.c_char_p, u64, C.POINTER(i64), i32, C.POINTER(FieldView), i32], C.c_int),

@@ -428,6 +428,43 @@ __global__ void k_batch_warm_start(BatchParams p, int first, const float *pred, 
 	}
 }
 
+// Refinement of a warm start, channels [first, first + gridDim.y) at an even
+// time step, same prediction arguments as k_batch_warm_start: every fluid cell
+// keeps the non-equilibrium part of its current populations and gets the
+// predicted macroscopic field back,
+//   f_i <- f_i - f_eq(rho_f, u_f) + f_eq(rho_p, u_p),
+// rho_f, u_f the moments of f and (rho_p, u_p) the prediction (rho_p = rho_f
+// with keep_rho).  After a few sweeps from the first-order reconstruction,
+// the non-equilibrium part is the one the lattice dynamics and its boundary
+// rules produce for this field, not a finite-difference estimate.
+__global__ void k_batch_reimpose(BatchParams p, int first, const float *pred, int64_t pred_stride, const float *sc,
+								 const float *of, int keep_rho) {
+	const int j = blockIdx.y;
+	const ChannelRec ch = p.ch[first + j];
+	const float *pr = pred + (int64_t)j * pred_stride;
+	const float s0 = sc[3 * j], s1 = sc[3 * j + 1], s2 = sc[3 * j + 2];
+	const float o0 = of[3 * j], o1 = of[3 * j + 1], o2 = of[3 * j + 2];
+	const int64_t n = (int64_t)ch.nx * ch.ny;
+	for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+		const int y = (int)(k / ch.nx), x = (int)(k - (int64_t)y * ch.nx);
+		const int64_t cell = ch.off + (int64_t)y * ch.nxp + x;
+		const uint8_t fl = p.flags[cell];
+		if (fl == 1 || fl == 0) continue;
+		float f[9];
+		for (int i = 0; i < 9; ++i) f[i] = p.f[i * p.plane + cell] + (p.shifted ? (float)D2Q9::w(i) : 0.f);
+		float rho_f, u_f[3];
+		moments<D2Q9, true>(f, rho_f, u_f);
+		const float *v = pr + k * 3;
+		float u_p[3] = {v[0] * s0 + o0, v[1] * s1 + o1, 0.f};
+		const float rho_p = keep_rho ? rho_f : v[2] * s2 + o2;
+		float eq_f[9], eq_p[9];
+		equilibrium<D2Q9, true>(rho_f, u_f, eq_f);
+		equilibrium<D2Q9, true>(rho_p, u_p, eq_p);
+		for (int i = 0; i < 9; ++i)
+			p.f[i * p.plane + cell] = f[i] - eq_f[i] + eq_p[i] - (p.shifted ? (float)D2Q9::w(i) : 0.f);
+	}
+}
+
 // f <-> g = f - w_i on every slot (sign -1: to shifted, +1: back), when a
 // program switches between shifted and unshifted arithmetic
 __global__ void k_batch_shift(BatchParams p, float sign) {
@@ -892,6 +929,34 @@ extern "C" int kel_batch_warm_start(kel_batch *B, int32_t first, int32_t count, 
 	k_batch_warm_start<<<dim3(bx, count), 256, 0, B->stream>>>(params(B, 0), first, d_pred, pred_stride, d_scale,
 															   d_offset, with_neq);
 	KEL_CUDA(cudaGetLastError());
+	return KEL_OK;
+}
+
+extern "C" int kel_batch_warm_refine(kel_batch *B, int32_t first, int32_t count, const float *d_pred,
+									 int64_t pred_stride, const float *d_scale, const float *d_offset,
+									 int32_t iterations, int32_t keep_rho) {
+	if (!B || !d_pred || !d_scale || !d_offset)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_warm_refine: null argument");
+	if (first < 0 || count < 1 || count > 65535 || first > B->n - count || iterations < 0)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_warm_refine: channels [%d, %d) outside [0, %d)", first,
+					first + count, B->n);
+	int64_t most = 0;
+	for (int c = first; c < first + count; ++c) {
+		if (B->t[c] & 1u) return fail(KEL_ERR_STATE, "kel_batch_warm_refine: channel %d is at an odd time step", c);
+		const int64_t cells = (int64_t)B->rec[c].nx * B->rec[c].ny;
+		if (cells * 3 > pred_stride)
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_batch_warm_refine: channel %d needs %lld floats > stride %lld",
+						c, (long long)(cells * 3), (long long)pred_stride);
+		most = cells > most ? cells : most;
+	}
+	const int bx = (int)((most + 255) / 256 < 1024 ? (most + 255) / 256 : 1024);
+	int rc;
+	for (int it = 0; it < iterations; ++it) {
+		if ((rc = kel_batch_step(B, 2))) return rc;
+		k_batch_reimpose<<<dim3(bx, count), 256, 0, B->stream>>>(params(B, 0), first, d_pred, pred_stride, d_scale,
+																 d_offset, keep_rho);
+		KEL_CUDA(cudaGetLastError());
+	}
 	return KEL_OK;
 }
 

@@ -674,6 +674,7 @@ extern "C" int kel_upload_field(kel_lattice *L, int32_t field, const float *host
 	int rc;
 	if (field == KEL_FIELD_POROSITY) {
 		if ((rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
+		++L->por_epoch;
 		return field_io(L, L->por, nullptr, host, 1);
 	}
 	if (field == KEL_FIELD_FORCE) {
@@ -912,6 +913,11 @@ static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	return p;
 }
 
+namespace kel {
+namespace gb {
+SweepParams sweep_params(kel_lattice *L, const kel_step_program *P) { return make_params(L, P); }
+} // namespace gb
+} // namespace kel
 
 // Time every supported launch shape on the lattice's own state, then put the
 // state back: the populations are saved to a scratch copy first and restored
@@ -1011,7 +1017,18 @@ extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_st
 	if (step_flags & ~(KEL_STEP_WRITE_MACROS | KEL_STEP_ALL_MACROS))
 		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown step flags");
 	int rc;
+	// A caller may capture its own loop of kel_step calls into a graph.  Then
+	// kel_step must neither synchronise nor capture a graph of its own (both
+	// are illegal on a capturing stream): the launches go into the caller's
+	// graph one by one, and the program must have been uploaded before.
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+	if (L->stream != nullptr) KEL_CUDA(cudaStreamIsCapturing(L->stream, &cap));
+	const bool capturing = cap != cudaStreamCaptureStatusNone;
 	if (!L->have_ops || memcmp(&L->last_prog, P, sizeof(*P)) != 0) {
+		if (capturing)
+			return fail(KEL_ERR_INVALID_ARGUMENT,
+						"kel_step: a new step program during stream capture; call kel_step with this program once "
+						"before capturing");
 		OpEntry ops[MAX_FLAGS];
 		if ((rc = lower_program(L, P, ops))) return rc;
 		KEL_CUDA(cudaMemcpyAsync(L->ops, ops, sizeof(ops), cudaMemcpyHostToDevice, L->stream));
@@ -1031,7 +1048,7 @@ extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_st
 	const uint64_t plain = (step_flags & KEL_STEP_ALL_MACROS)
 							   ? 0
 							   : ((step_flags & KEL_STEP_WRITE_MACROS) && n_steps > 0 ? n_steps - 1 : n_steps);
-	if (L->stream != nullptr && L->cpt != CPT_ROWS && plain >= 2 * GRAPH_STEPS) {
+	if (L->stream != nullptr && !capturing && L->cpt != CPT_ROWS && plain >= 2 * GRAPH_STEPS) {
 		p.write_macros = 0;
 		for (; (L->t & 1u) && s < plain; ++s, ++L->t) {
 			cudaError_t e = launch_one(L, p, P->collision, exact, true);

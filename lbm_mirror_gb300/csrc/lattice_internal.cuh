@@ -32,6 +32,8 @@ struct HostDesc {
 };
 
 int grid_for(int64_t n);
+// Launch parameters of the sweep kel_step runs for program P on lattice L.
+SweepParams sweep_params(kel_lattice *L, const kel_step_program *P);
 int ensure_field(kel_lattice *L, float **ptr, int64_t count, float init);
 // Copy `comps` device planes (padded plane layout) to host AoS (N*comps).
 int field_to_host(kel_lattice *L, const float *dev, float *host, int comps);
@@ -49,6 +51,10 @@ struct kel_lattice {
 	uint8_t *flags = nullptr;
 	float *rho = nullptr, *u = nullptr, *por = nullptr, *force = nullptr, *profile = nullptr;
 	float *hN = nullptr, *hD = nullptr; // HLBM particle_N (D planes) and particle_D, on first use
+	// Counts writes of the porosity field: an uploaded field, an HLBM couple
+	// and every PSM couple advance it, so a particle set sees whether the
+	// field still is the one its own last couple left.
+	uint64_t por_epoch = 1;
 	kel::gb::OpEntry *ops = nullptr;
 	void *staging = nullptr;
 	size_t staging_bytes = 0;

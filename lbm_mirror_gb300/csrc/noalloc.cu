@@ -14,6 +14,7 @@
 // hundred steps between its own kernels -- or code that manages all device
 // memory through its own pool -- cannot afford either.  The caller passes the
 // inputs and the output; this entry point adds nothing to the device heap.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -86,11 +87,47 @@ __global__ void __launch_bounds__(1024) na_final(const double2 *partial, int til
 											   : (sb[0] > 0.0 ? sqrt(sa[0] / sb[0]) : (sa[0] > 0.0 ? INFINITY : 0.0));
 }
 
-// Device address of the scratch array, looked up once per device with that
-// device current (in host code the array's name is only a host-side stand-in).
+// Device address of the scratch array, looked up with the device current (in
+// host code the array's name is only a host-side stand-in).  The address is
+// cached per device together with the id of the context it was resolved in:
+// after a cudaDeviceReset the runtime creates a new context, whose module
+// holds the array at another address, and the id tells the two apart.  The
+// context id comes from the driver through the runtime's entry-point lookup,
+// so the library needs no link against the driver library.
 constexpr int NA_MAX_DEVICES = 64;
-double2 *g_scratch_ptr[NA_MAX_DEVICES] = {nullptr};
+struct ScratchSlot {
+	double2 *ptr = nullptr;
+	unsigned long long ctx_id = 0;
+};
+ScratchSlot g_scratch[NA_MAX_DEVICES];
 std::mutex g_scratch_mutex;
+
+typedef CUresult (*PFN_ctx_get_current)(CUcontext *);
+typedef CUresult (*PFN_ctx_get_id)(CUcontext, unsigned long long *);
+PFN_ctx_get_current g_ctx_get_current = nullptr;
+PFN_ctx_get_id g_ctx_get_id = nullptr;
+bool g_ctx_lookup_done = false;
+
+// Id of the calling thread's current context, false when it is unknown.
+bool current_context_id(unsigned long long *id) {
+	if (!g_ctx_lookup_done) {
+		g_ctx_lookup_done = true;
+		void *a = nullptr, *b = nullptr;
+		cudaDriverEntryPointQueryResult qa, qb;
+		if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+			qa == cudaDriverEntryPointSuccess &&
+			cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+			qb == cudaDriverEntryPointSuccess) {
+			g_ctx_get_current = reinterpret_cast<PFN_ctx_get_current>(a);
+			g_ctx_get_id = reinterpret_cast<PFN_ctx_get_id>(b);
+		}
+		cudaGetLastError();
+	}
+	if (!g_ctx_get_current || !g_ctx_get_id) return false;
+	CUcontext c = nullptr;
+	if (g_ctx_get_current(&c) != CUDA_SUCCESS || !c) return false;
+	return g_ctx_get_id(c, id) == CUDA_SUCCESS;
+}
 
 int scratch_for_current_device(double2 **out) {
 	int dev = 0;
@@ -99,15 +136,20 @@ int scratch_for_current_device(double2 **out) {
 	if (dev < 0 || dev >= NA_MAX_DEVICES)
 		return fail(KEL_ERR_UNSUPPORTED, "kel_velocity_residual_noalloc: device %d beyond %d", dev, NA_MAX_DEVICES);
 	std::lock_guard<std::mutex> lock(g_scratch_mutex);
-	if (!g_scratch_ptr[dev]) {
+	unsigned long long id = 0;
+	const bool known = current_context_id(&id);
+	ScratchSlot &slot = g_scratch[dev];
+	if (!slot.ptr || !known || slot.ctx_id != id) {
 		void *p = nullptr;
 		e = cudaGetSymbolAddress(&p, g_noalloc_partials);
 		if (e != cudaSuccess || !p)
 			return fail(KEL_ERR_CUDA, "kel_velocity_residual_noalloc: cudaGetSymbolAddress failed: %s",
 						cudaGetErrorString(e));
-		g_scratch_ptr[dev] = static_cast<double2 *>(p);
+		slot.ptr = static_cast<double2 *>(p);
+		// the lookup made the device's context current if it was not yet
+		slot.ctx_id = current_context_id(&id) ? id : 0;
 	}
-	*out = g_scratch_ptr[dev];
+	*out = slot.ptr;
 	return KEL_OK;
 }
 

@@ -30,12 +30,29 @@
 
 using namespace kel::gb;
 
+// Key of the captured coupled step: everything its launches bake in.
+struct ParticleGraphKey {
+	kel_particle_params prm;
+	kel_step_program prog;
+	kel::gb::SweepParams sweep;
+	void *f, *por, *force, *bodies, *boxes, *partial;
+	int n, gather_g, couple_g, cpt, block;
+};
+
 struct kel_particles {
 	kel_lattice *lat = nullptr;
 	int n = 0;
 	kel_particle_state *d = nullptr; // device copy of the bodies
 	float *cell_force = nullptr;     // D planes, allocated on first request
-	void *boxes = nullptr;           // per-body integer boxes of the couple pass (n BodyBox)
+	void *boxes = nullptr;           // per-body integer boxes: current [0, n), previous couple [n, 2n)
+	double *partial = nullptr;       // gather partial sums, n x gather_g x 6
+	int partial_cap = 0;             // blocks per body the partial buffer holds
+	double max_radius = 0.0;         // largest radius of the uploaded bodies (sizes the launches)
+	// value of lat->por_epoch after this set's last PSM couple (0: none); the
+	// incremental couple needs the field to be untouched since then
+	uint64_t epoch = 0;
+	cudaGraphExec_t graph = nullptr; // two coupled steps from an even time step
+	ParticleGraphKey key;
 };
 
 namespace {
@@ -131,9 +148,22 @@ struct BodyBox {
 	int a[3], b[3];
 };
 
-__global__ void k_body_boxes(PView v, const kel_particle_state *P, int np, int sub, BodyBox *box) {
+// Per body: its box for the current position into cur[i].  With shift, the
+// box the previous couple used moves to prev[i] first (the incremental
+// couple restores the cells it no longer covers).  With reset, the body's
+// force and torque accumulators are zeroed as well (ParticleForceReset,
+// integrate.hpp:195-261), which saves a launch per coupled step.
+__global__ void k_pre(PView v, kel_particle_state *P, int np, int sub, BodyBox *cur, BodyBox *prev, int boxes,
+					  int shift, int reset) {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= np) return;
+	if (reset)
+		for (int k = 0; k < 3; ++k) {
+			P[i].force[k] = 0.0;
+			P[i].torque[k] = 0.0;
+		}
+	if (!boxes) return;
+	if (shift) prev[i] = cur[i];
 	int64_t a[3], b[3];
 	body_aabb(v.D, P[i], v.nx, v.ny, v.nz, v.periodic, sub, a, b);
 	BodyBox r;
@@ -141,13 +171,20 @@ __global__ void k_body_boxes(PView v, const kel_particle_state *P, int np, int s
 		r.a[k] = (int)a[k];
 		r.b[k] = (int)b[k];
 	}
-	box[i] = r;
+	cur[i] = r;
 }
 
-// Per tile of TX x TY cells: an ordered cull of the bodies whose box touches
-// the tile (their data staged in shared memory), then per cell the product of
-// the candidates' complements in body order, each complement computed as the
-// reference computes it.  Two exact shortcuts skip the FP64 sampling:
+// Candidate body of a couple pass, staged in shared memory.
+struct Cand {
+	BodyBox box;
+	double X[3];
+	double R;
+};
+
+// Body q's factor on the porosity of cell (x, y, z), multiplied into por
+// (product of complements, bodies in index order, as couple.hpp:26-58 takes
+// it).  A cell none of whose images lies in the body's box is left alone.
+// Two exact shortcuts skip the FP64 sampling:
 //   sub-cell mode: the 16 (64) samples lie within 3 sqrt(D) / 8 of the cell
 //     centre, so a centre farther than R + that radius (+ 1e-6) from the body
 //     centre has no sample inside (factor 1) and one nearer than R - radius
@@ -155,25 +192,91 @@ __global__ void k_body_boxes(PView v, const kel_particle_state *P, int np, int s
 //   ramp mode: |r|^2 below (R - eps/2)^2 - 1e-6 gives 0, above
 //     (R + eps/2)^2 + 1e-6 gives 1.
 // The margins are far above the FP64 rounding of the coordinates, so the
-// factors equal those of the full computation bit for bit.  Cells with no
-// image inside a candidate's box skip it before any FP64 arithmetic.
+// factors equal those of the full computation bit for bit.
+__device__ inline void body_factor(const PView &v, int x, int y, int z, const Cand &c, int sub, double reach,
+								   double eps, double &por, bool &touched) {
+	const BodyBox &q = c.box;
+	// integer pre-filter: no image of the cell (x, x -/+ nx when periodic) in
+	// the box means the nearest image is not either
+	if (y < q.a[1] || y >= q.b[1] || (v.D == 3 && (z < q.a[2] || z >= q.b[2]))) return;
+	const bool in0 = x >= q.a[0] && x < q.b[0];
+	const bool inm = v.periodic && x - v.nx >= q.a[0] && x - v.nx < q.b[0];
+	const bool inp = v.periodic && x + v.nx >= q.a[0] && x + v.nx < q.b[0];
+	if (!(in0 || inm || inp)) return;
+	touched = true;
+	const double X0 = c.X[0], X1 = c.X[1], X2 = c.X[2], R = c.R;
+	double rel[3] = {rel_coord((double)x, X0, v.periodic, v.nx), (double)y - X1, v.D == 3 ? (double)z - X2 : 0.0};
+	const double xi = X0 + rel[0];
+	const int64_t xc = v.periodic ? (int64_t)llround(xi) : x;
+	if (xc < q.a[0] || xc >= q.b[0]) return;
+	double s2 = 0.0;
+	for (int d = 0; d < v.D; ++d) s2 = s2 + rel[d] * rel[d];
+	double pp;
+	if (sub) {
+		const double out_r = R + reach + 1e-6, in_r = R - reach - 1e-6;
+		if (s2 > out_r * out_r) {
+			return; // no sample inside: factor 1
+		} else if (in_r > 0.0 && s2 < in_r * in_r) {
+			pp = 0.0;
+		} else {
+			const double xs[3] = {xi, (double)y, (double)z};
+			const double Xs[3] = {X0, X1, X2};
+			pp = subcell_porosity(v.D, xs, Xs, R);
+		}
+	} else {
+		const double lo = R - eps / 2, hi = R + eps / 2;
+		if (lo > 0.0 && s2 < lo * lo - 1e-6) pp = 0.0;
+		else if (s2 > hi * hi + 1e-6) return;
+		else pp = ramp(sqrt(s2), R, eps);
+	}
+	por = por * pp;
+}
+
+__device__ inline double subcell_reach(int D) { return D == 3 ? 0.6495190528383290 : 0.5303300858899106; } // 3 sqrt(D) / 8
+
+// Ordered compaction of the bodies [c0, c0 + TT) for which hit is true (one
+// thread per body, TT threads) into cand[0 .. *ncand).
+__device__ inline void compact_cands(bool hit, int pi, const BodyBox &bb, const kel_particle_state *P, Cand *cand,
+									 int *warp_count, int *ncand) {
+	const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+	const unsigned m = __ballot_sync(0xffffffffu, hit);
+	if ((tid & 31) == 0) warp_count[tid >> 5] = __popc(m);
+	__syncthreads();
+	if (tid == 0) {
+		int s = 0;
+		for (int w = 0; w < TT / 32; ++w) {
+			const int c = warp_count[w];
+			warp_count[w] = s;
+			s += c;
+		}
+		*ncand = s;
+	}
+	__syncthreads();
+	if (hit) {
+		Cand &c = cand[warp_count[tid >> 5] + __popc(m & ((1u << (tid & 31)) - 1u))];
+		c.box = bb;
+		for (int d = 0; d < 3; ++d) c.X[d] = P[pi].position[d];
+		c.R = P[pi].radius;
+	}
+	__syncthreads();
+}
+
+// Full couple pass.  Per tile of TX x TY cells: an ordered cull of the
+// bodies whose box touches the tile, then per cell the product of the
+// candidates' factors in body order (body_factor).  Every cell is written.
 __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state *P, const BodyBox *box, int np,
 											   int mode, double eps) {
-	__shared__ int cand[TT];
-	__shared__ BodyBox cbox[TT];
-	__shared__ double cpos[TT][3];
-	__shared__ double crad[TT];
+	__shared__ Cand cand[TT];
 	__shared__ int warp_count[TT / 32];
 	__shared__ int ncand;
 	const int tid = threadIdx.y * TX + threadIdx.x;
 	const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z = blockIdx.z;
 	const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
 	const int sub = mode == KEL_POROSITY_SUBCELL;
-	const double reach = sub ? (v.D == 3 ? 0.6495190528383290 : 0.5303300858899106) : 0.0; // 3 sqrt(D) / 8
+	const double reach = sub ? subcell_reach(v.D) : 0.0;
 	double por = 1.0;
 	bool touched = false; // some body's box holds the cell (otherwise por stays exactly 1)
 	for (int c0 = 0; c0 < np; c0 += TT) {
-		// cull: does body c0+tid's box touch this tile?  (ordered compaction)
 		bool hit = false;
 		const int pi = c0 + tid;
 		BodyBox bb;
@@ -185,70 +288,92 @@ __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state
 				xs = xs || (bb.a[0] < x0 + TX - v.nx && bb.b[0] > x0 - v.nx) || (bb.a[0] < x0 + TX + v.nx && bb.b[0] > x0 + v.nx);
 			hit = yz && xs;
 		}
-		const unsigned m = __ballot_sync(0xffffffffu, hit);
-		if ((tid & 31) == 0) warp_count[tid >> 5] = __popc(m);
-		__syncthreads();
-		if (tid == 0) {
-			int s = 0;
-			for (int w = 0; w < TT / 32; ++w) {
-				const int c = warp_count[w];
-				warp_count[w] = s;
-				s += c;
-			}
-			ncand = s;
-		}
-		__syncthreads();
-		if (hit) {
-			const int slot = warp_count[tid >> 5] + __popc(m & ((1u << (tid & 31)) - 1u));
-			cand[slot] = pi;
-			cbox[slot] = bb;
-			for (int d = 0; d < 3; ++d) cpos[slot][d] = P[pi].position[d];
-			crad[slot] = P[pi].radius;
-		}
-		__syncthreads();
-		if (x < v.nx && y < v.ny) {
-			for (int k = 0; k < ncand; ++k) {
-				const BodyBox &q = cbox[k];
-				// integer pre-filter: no image of the cell (x, x -/+ nx when
-				// periodic) in the box means the nearest image is not either
-				if (y < q.a[1] || y >= q.b[1] || (v.D == 3 && (z < q.a[2] || z >= q.b[2]))) continue;
-				const bool in0 = x >= q.a[0] && x < q.b[0];
-				const bool inm = v.periodic && x - v.nx >= q.a[0] && x - v.nx < q.b[0];
-				const bool inp = v.periodic && x + v.nx >= q.a[0] && x + v.nx < q.b[0];
-				if (!(in0 || inm || inp)) continue;
-				touched = true;
-				const double X0 = cpos[k][0], X1 = cpos[k][1], X2 = cpos[k][2], R = crad[k];
-				double rel[3] = {rel_coord((double)x, X0, v.periodic, v.nx), (double)y - X1, v.D == 3 ? (double)z - X2 : 0.0};
-				const double xi = X0 + rel[0];
-				const int64_t xc = v.periodic ? (int64_t)llround(xi) : x;
-				if (xc < q.a[0] || xc >= q.b[0] || y < q.a[1] || y >= q.b[1] || (v.D == 3 && (z < q.a[2] || z >= q.b[2])))
-					continue;
-				double s2 = 0.0;
-				for (int d = 0; d < v.D; ++d) s2 = s2 + rel[d] * rel[d];
-				double pp;
-				if (sub) {
-					const double out_r = R + reach + 1e-6, in_r = R - reach - 1e-6;
-					if (s2 > out_r * out_r) {
-						continue; // no sample inside: factor 1
-					} else if (in_r > 0.0 && s2 < in_r * in_r) {
-						pp = 0.0;
-					} else {
-						const double xs[3] = {xi, (double)y, (double)z};
-						const double Xs[3] = {X0, X1, X2};
-						pp = subcell_porosity(v.D, xs, Xs, R);
-					}
-				} else {
-					const double lo = R - eps / 2, hi = R + eps / 2;
-					if (lo > 0.0 && s2 < lo * lo - 1e-6) pp = 0.0;
-					else if (s2 > hi * hi + 1e-6) continue;
-					else pp = ramp(sqrt(s2), R, eps);
-				}
-				por = por * pp;
-			}
-		}
+		compact_cands(hit, pi, bb, P, cand, warp_count, &ncand);
+		if (x < v.nx && y < v.ny)
+			for (int k = 0; k < ncand; ++k) body_factor(v, x, y, z, cand[k], sub, reach, eps, por, touched);
 		__syncthreads();
 	}
 	if (x < v.nx && y < v.ny) v.por[((int64_t)z * v.ny + y) * v.nxp + x] = touched ? (float)por : 1.0f;
+}
+
+__device__ inline int64_t box_cells(const BodyBox &q, int D) {
+	const int64_t e0 = q.b[0] - q.a[0], e1 = q.b[1] - q.a[1], e2 = D == 3 ? q.b[2] - q.a[2] : 1;
+	return (e0 > 0 && e1 > 0 && e2 > 0) ? e0 * e1 * e2 : 0;
+}
+
+// Do boxes p and q share a cell (some periodic image of p when periodic)?
+__device__ inline bool boxes_touch(const BodyBox &p, const BodyBox &q, const PView &v) {
+	if (!(p.a[1] < q.b[1] && p.b[1] > q.a[1])) return false;
+	if (v.D == 3 && !(p.a[2] < q.b[2] && p.b[2] > q.a[2])) return false;
+	for (int s = v.periodic ? -1 : 0; s <= (v.periodic ? 1 : 0); ++s)
+		if (p.a[0] + s * v.nx < q.b[0] && p.b[0] + s * v.nx > q.a[0]) return true;
+	return false;
+}
+
+constexpr int RC_CPT = 4; // cells per thread and pass of the region couple
+
+// Incremental couple pass.  Only cells inside some body's box can have a
+// porosity other than 1, so after a couple whose boxes were prev[], the new
+// field differs from the old one only inside the boxes cur[] u prev[].
+// Block (b, .) recomputes the cells of body b's current box and, where it
+// moved, of its previous box: each such cell gets the full product over the
+// bodies (index order) whose current box holds it, or 1 when none does --
+// the same value the full pass writes.  A cell in several bodies' regions is
+// written by several blocks with that same value.
+__global__ void __launch_bounds__(TT) k_couple_regions(PView v, const kel_particle_state *P, const BodyBox *cur,
+													   const BodyBox *prev, int np, int mode, double eps) {
+	__shared__ Cand cand[TT];
+	__shared__ int warp_count[TT / 32];
+	__shared__ int ncand;
+	const int tid = threadIdx.x;
+	const int b = blockIdx.x;
+	const BodyBox A = cur[b], B = prev[b];
+	const bool same = A.a[0] == B.a[0] && A.b[0] == B.b[0] && A.a[1] == B.a[1] && A.b[1] == B.b[1] &&
+					  (v.D == 2 || (A.a[2] == B.a[2] && A.b[2] == B.b[2]));
+	const int64_t n0 = box_cells(A, v.D), n1 = same ? 0 : box_cells(B, v.D);
+	const int sub = mode == KEL_POROSITY_SUBCELL;
+	const double reach = sub ? subcell_reach(v.D) : 0.0;
+	for (int64_t base = (int64_t)blockIdx.y * TT * RC_CPT; base < n0 + n1; base += (int64_t)gridDim.y * TT * RC_CPT) {
+		int cx[RC_CPT], cy[RC_CPT], cz[RC_CPT];
+		bool ok[RC_CPT], touched[RC_CPT];
+		double por[RC_CPT];
+#pragma unroll
+		for (int j = 0; j < RC_CPT; ++j) {
+			const int64_t idx = base + (int64_t)j * TT + tid;
+			ok[j] = idx < n0 + n1;
+			touched[j] = false;
+			por[j] = 1.0;
+			cx[j] = cy[j] = cz[j] = 0;
+			if (!ok[j]) continue;
+			const BodyBox &q = idx < n0 ? A : B;
+			const int64_t k = idx < n0 ? idx : idx - n0;
+			const int64_t ex = q.b[0] - q.a[0], ey = q.b[1] - q.a[1];
+			int ix = q.a[0] + (int)(k % ex);
+			cy[j] = q.a[1] + (int)((k / ex) % ey);
+			cz[j] = v.D == 3 ? q.a[2] + (int)(k / (ex * ey)) : 0;
+			if (v.periodic) ix = ((ix % v.nx) + v.nx) % v.nx;
+			cx[j] = ix;
+		}
+		for (int c0 = 0; c0 < np; c0 += TT) {
+			bool hit = false;
+			const int pi = c0 + tid;
+			BodyBox bb;
+			if (pi < np) {
+				bb = cur[pi];
+				hit = boxes_touch(bb, A, v) || (!same && boxes_touch(bb, B, v));
+			}
+			compact_cands(hit, pi, bb, P, cand, warp_count, &ncand);
+#pragma unroll
+			for (int j = 0; j < RC_CPT; ++j)
+				if (ok[j])
+					for (int k = 0; k < ncand; ++k)
+						body_factor(v, cx[j], cy[j], cz[j], cand[k], sub, reach, eps, por[j], touched[j]);
+			__syncthreads();
+		}
+#pragma unroll
+		for (int j = 0; j < RC_CPT; ++j)
+			if (ok[j]) v.por[((int64_t)cz[j] * v.ny + cy[j]) * v.nxp + cx[j]] = touched[j] ? (float)por[j] : 1.0f;
+	}
 }
 
 // ---- gather ---------------------------------------------------------------------
@@ -273,18 +398,24 @@ __device__ inline float pop_post(const PView &v, int x, int y, int z, int i) {
 	return __half2float(static_cast<const __half *>(v.f)[idx]) + v.wshift[i];
 }
 
-constexpr int GT = 256;
+constexpr int GT = 128;
 
 // PSM (HLBM false): psm.hpp:101-446, the porosity field the couple pass
 // wrote, cell force = momentum x (1 - porosity).  HLBM: hlbm.hpp:119-260,
 // the body's own ramp porosity (eps) decides which cells count and the cell
 // momentum enters unweighted; the cell force field is written by the HLBM
 // couple pass instead (the last body wins there).
+// Grid (bodies, G): block (b, g) takes the cells g, g + G, g + 2G, ... (in
+// blocks of GT) of body b's box and writes its FP64 force/torque sums, after
+// a fixed-order warp-shuffle and shared-memory reduction, to
+// partial[(b * G + g) * 6 ..]; k_gather_finish or the contact pass adds the G
+// partials of a body in order g = 0 .. G-1.  Deterministic for a given G.
 template <class L, int STORE, bool HLBM>
-__global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, int steps, int mode, double eps) {
+__global__ void __launch_bounds__(GT) k_gather(PView v, const kel_particle_state *P, int steps, int mode, double eps,
+											   double *partial) {
 	constexpr int D = L::D;
 	__shared__ double part[GT / 32][6];
-	kel_particle_state &p = P[blockIdx.x];
+	const kel_particle_state &p = P[blockIdx.x];
 	int64_t a[3], b[3];
 	body_aabb(D, p, v.nx, v.ny, v.nz, v.periodic, mode == KEL_POROSITY_SUBCELL, a, b);
 	const int64_t ex = b[0] - a[0], ey = b[1] - a[1], ez = D == 3 ? b[2] - a[2] : 1;
@@ -308,7 +439,8 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, i
 	// 32-bit index arithmetic unless the box holds 2^31 cells or more
 	const bool small = ncell < ((int64_t)1 << 31);
 	const int ex32 = (int)ex, ey32 = (int)ey, exy32 = small ? (int)(ex * ey) : 0;
-	for (int64_t k = threadIdx.x; k < ncell; k += GT) {
+	const int64_t stride = (int64_t)gridDim.y * GT;
+	for (int64_t k = (int64_t)blockIdx.y * GT + threadIdx.x; k < ncell; k += stride) {
 		int ix, iy, iz;
 		if (small) {
 			const int k32 = (int)k;
@@ -365,13 +497,28 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, kel_particle_state *P, i
 		if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5][q] = s;
 	}
 	__syncthreads();
-	if (threadIdx.x == 0) {
-		double tot[6] = {0, 0, 0, 0, 0, 0};
-		for (int w = 0; w < GT / 32; ++w)
-			for (int q = 0; q < 6; ++q) tot[q] += part[w][q];
-		for (int d = 0; d < D; ++d) p.force[d] = p.force[d] + tot[d];
-		for (int d = 0; d < (D == 2 ? 1 : 3); ++d) p.torque[d] = p.torque[d] + tot[3 + d];
+	if (threadIdx.x < 6) {
+		double tot = 0.0;
+		for (int w = 0; w < GT / 32; ++w) tot += part[w][threadIdx.x];
+		partial[((int64_t)blockIdx.x * gridDim.y + blockIdx.y) * 6 + threadIdx.x] = tot;
 	}
+}
+
+// Sum of body i's G gather partials, g = 0 .. G-1 in order.
+__device__ inline void gather_total(const double *partial, int i, int G, double *tot) {
+	for (int q = 0; q < 6; ++q) tot[q] = 0.0;
+	for (int g = 0; g < G; ++g)
+		for (int q = 0; q < 6; ++q) tot[q] += partial[((int64_t)i * G + g) * 6 + q];
+}
+
+// The gather's sums into the bodies' accumulators (force += F, torque += T).
+__global__ void k_gather_finish(kel_particle_state *P, int np, int D, const double *partial, int G) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= np) return;
+	double tot[6];
+	gather_total(partial, i, G, tot);
+	for (int d = 0; d < D; ++d) P[i].force[d] = P[i].force[d] + tot[d];
+	for (int d = 0; d < (D == 2 ? 1 : 3); ++d) P[i].torque[d] = P[i].torque[d] + tot[3 + d];
 }
 
 // ---- HLBM per-cell passes ----------------------------------------------------------
@@ -635,9 +782,11 @@ __device__ inline bool pair_response(const kel_particle_state &self, const kel_p
 
 // One warp per body: the lanes evaluate its pairs 32 at a time, then lane 0
 // adds the contacts in index order (the reference's accumulation order, so
-// the FP64 result is bit-identical) and finally the box walls.
+// the FP64 result is bit-identical) and finally the box walls.  With a gather
+// partial buffer, the body's gather sums are added first, exactly as
+// k_gather_finish would add them (one launch fewer per coupled step).
 __global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_params prm, int nx, int ny, int nz,
-						  int periodic) {
+						  int periodic, const double *partial, int G) {
 	__shared__ double fs[4][32][4];
 	__shared__ int hs[4][32];
 	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -649,6 +798,17 @@ __global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_par
 	const kel_particle_state &self = P[s];
 	double force[3] = {self.force[0], self.force[1], self.force[2]};
 	double torque0 = self.torque[0];
+	double torque12[2] = {self.torque[1], self.torque[2]};
+	if (partial) {
+		double tot[6];
+		gather_total(partial, s, G, tot);
+		for (int d = 0; d < D; ++d) force[d] = force[d] + tot[d];
+		torque0 = torque0 + tot[3];
+		if (D == 3) {
+			torque12[0] = torque12[0] + tot[4];
+			torque12[1] = torque12[1] + tot[5];
+		}
+	}
 	for (int j0 = 0; j0 < np; j0 += 32) {
 		const int j = j0 + lane;
 		double f[3] = {0, 0, 0}, t0 = 0.0;
@@ -694,7 +854,11 @@ __global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_par
 	P[s].force[0] = force[0];
 	P[s].force[1] = force[1];
 	P[s].force[2] = force[2];
-	if (D == 2) P[s].torque[0] = torque0;
+	if (D == 2 || partial) P[s].torque[0] = torque0;
+	if (D == 3 && partial) {
+		P[s].torque[1] = torque12[0];
+		P[s].torque[2] = torque12[1];
+	}
 }
 
 // integrate_particle + verlet_step_lambda (integrate.hpp:45-83, particle.hpp:171-211)
@@ -731,15 +895,6 @@ __global__ void k_integrate(kel_particle_state *P, int np, int D, kel_particle_p
 		}
 	}
 	P[pi] = q;
-}
-
-__global__ void k_reset(kel_particle_state *P, int np) {
-	const int pi = blockIdx.x * blockDim.x + threadIdx.x;
-	if (pi >= np) return;
-	for (int k = 0; k < 3; ++k) {
-		P[pi].force[k] = 0.0;
-		P[pi].torque[k] = 0.0;
-	}
 }
 
 PView make_view(kel_lattice *L) {
@@ -786,6 +941,24 @@ int check_params(const kel_particles *ps, const kel_particle_params *prm, const 
 // ---------------------------------------------------------------------------
 // C ABI
 
+// Cells of a body's box per axis, at most: 2 r + 2 (ramp) or 2 r + 3 (sub-cell)
+static int64_t box_cells_max(const kel_particles *ps) {
+	const int64_t e = 2 * (int64_t)ceil(ps->max_radius) + 4;
+	return ps->lat->d.D == 3 ? e * e * e : e * e;
+}
+
+// Blocks per body of the gather: about one thread per box cell, 1 .. 64.
+static int gather_blocks(const kel_particles *ps) {
+	const int64_t g = (box_cells_max(ps) + GT - 1) / GT;
+	return (int)(g < 1 ? 1 : (g > 64 ? 64 : g));
+}
+
+// Blocks per body of the region couple (two boxes, RC_CPT cells per thread).
+static int couple_blocks(const kel_particles *ps) {
+	const int64_t g = (2 * box_cells_max(ps) + TT * RC_CPT - 1) / (TT * RC_CPT);
+	return (int)(g < 1 ? 1 : (g > 64 ? 64 : g));
+}
+
 extern "C" int kel_particles_create(kel_lattice *lat, int32_t count, kel_particles **out) {
 	if (!lat || !out || count < 1) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_create: bad arguments");
 	*out = nullptr;
@@ -793,7 +966,9 @@ extern "C" int kel_particles_create(kel_lattice *lat, int32_t count, kel_particl
 	ps->lat = lat;
 	ps->n = count;
 	cudaError_t e = cudaMalloc(&ps->d, sizeof(kel_particle_state) * count);
+	if (e == cudaSuccess) e = cudaMalloc(&ps->boxes, sizeof(BodyBox) * 2 * (size_t)count);
 	if (e != cudaSuccess) {
+		cudaFree(ps->d);
 		delete ps;
 		return fail(e == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA, "kel_particles_create: %s",
 					cudaGetErrorString(e));
@@ -802,6 +977,7 @@ extern "C" int kel_particles_create(kel_lattice *lat, int32_t count, kel_particl
 	int rc = ensure_field(lat, &lat->por, lat->plane, 1.0f);
 	if (rc) {
 		cudaFree(ps->d);
+		cudaFree(ps->boxes);
 		delete ps;
 		return rc;
 	}
@@ -812,17 +988,27 @@ extern "C" int kel_particles_create(kel_lattice *lat, int32_t count, kel_particl
 extern "C" int kel_particles_destroy(kel_particles *ps) {
 	if (!ps) return KEL_OK;
 	cudaStreamSynchronize(ps->lat->stream);
+	if (ps->graph) cudaGraphExecDestroy(ps->graph);
 	cudaFree(ps->d);
 	cudaFree(ps->cell_force);
 	cudaFree(ps->boxes);
+	cudaFree(ps->partial);
 	delete ps;
 	return KEL_OK;
 }
 
 extern "C" int kel_particles_upload(kel_particles *ps, const kel_particle_state *host) {
 	if (!ps || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_upload: null argument");
+	double rmax = 0.0;
+	for (int i = 0; i < ps->n; ++i) {
+		const double r = host[i].radius;
+		if (!(r >= 0.0) || !std::isfinite(r))
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_upload: body %d has radius %g", i, r);
+		if (r > rmax) rmax = r;
+	}
 	KEL_CUDA(cudaMemcpyAsync(ps->d, host, sizeof(kel_particle_state) * ps->n, cudaMemcpyHostToDevice, ps->lat->stream));
 	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	ps->max_radius = rmax;
 	return KEL_OK;
 }
 
@@ -833,8 +1019,13 @@ extern "C" int kel_particles_download(kel_particles *ps, kel_particle_state *hos
 	return KEL_OK;
 }
 
+static BodyBox *cur_boxes(kel_particles *ps) { return static_cast<BodyBox *>(ps->boxes); }
+static BodyBox *prev_boxes(kel_particles *ps) { return static_cast<BodyBox *>(ps->boxes) + ps->n; }
+
 static int particles_reset(kel_particles *ps) {
-	k_reset<<<(ps->n + 127) / 128, 128, 0, ps->lat->stream>>>(ps->d, ps->n);
+	kel_lattice *L = ps->lat;
+	k_pre<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(make_view(L), ps->d, ps->n, 0, cur_boxes(ps), prev_boxes(ps), 0,
+													   0, 1);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
@@ -860,19 +1051,36 @@ static int particles_hlbm_couple(kel_particles *ps, const kel_particle_params *p
 		k_hlbm_couple<STORE_FP16S><<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, ps->n, prm->eps,
 																				  hlbm_steps(prm));
 	KEL_CUDA(cudaGetLastError());
+	++L->por_epoch;
+	ps->epoch = 0;
 	return KEL_OK;
 }
 
-static int particles_couple(kel_particles *ps, const kel_particle_params *prm) {
+// PsmReset + couple.  The first couple of a particle set, and any couple
+// after someone else wrote the porosity field, recomputes every cell; later
+// ones only the cells of the bodies' current and previous boxes (identical
+// field).  With reset, the bodies' force and torque are zeroed in the same
+// launch.
+static int particles_couple(kel_particles *ps, const kel_particle_params *prm, bool reset) {
 	kel_lattice *L = ps->lat;
-	if (prm->coupling == KEL_COUPLING_HLBM) return particles_hlbm_couple(ps, prm, false);
+	if (prm->coupling == KEL_COUPLING_HLBM) {
+		int rc;
+		if (reset && (rc = particles_reset(ps))) return rc;
+		return particles_hlbm_couple(ps, prm, false);
+	}
 	PView v = make_view(L);
-	if (!ps->boxes) KEL_CUDA(cudaMalloc(&ps->boxes, sizeof(BodyBox) * ps->n));
-	BodyBox *box = static_cast<BodyBox *>(ps->boxes);
 	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
-	k_body_boxes<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, sub, box);
-	k_couple<<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, box, ps->n, prm->porosity_mode, prm->eps);
+	const bool incremental = ps->epoch != 0 && ps->epoch == L->por_epoch;
+	k_pre<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, sub, cur_boxes(ps), prev_boxes(ps), 1,
+													   incremental ? 1 : 0, reset ? 1 : 0);
+	if (incremental)
+		k_couple_regions<<<dim3((unsigned)ps->n, (unsigned)couple_blocks(ps)), TT, 0, L->stream>>>(
+			v, ps->d, cur_boxes(ps), prev_boxes(ps), ps->n, prm->porosity_mode, prm->eps);
+	else
+		k_couple<<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, cur_boxes(ps), ps->n, prm->porosity_mode,
+															 prm->eps);
 	KEL_CUDA(cudaGetLastError());
+	ps->epoch = ++L->por_epoch;
 	return KEL_OK;
 }
 
@@ -883,46 +1091,68 @@ static int particles_stamp(kel_particles *ps, const kel_particle_params *prm) {
 	return KEL_OK;
 }
 
-template <class Lc, int STORE>
-static void launch_gather(const PView &v, kel_particles *ps, int steps, int mode) {
-	k_gather<Lc, STORE, false><<<ps->n, GT, 0, ps->lat->stream>>>(v, ps->d, steps, mode, 1.5);
+static int ensure_partials(kel_particles *ps, int G) {
+	if (ps->partial && ps->partial_cap >= G) return KEL_OK;
+	if (ps->partial) {
+		KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+		cudaFree(ps->partial);
+		ps->partial = nullptr;
+	}
+	KEL_CUDA(cudaMalloc(&ps->partial, sizeof(double) * 6 * (size_t)ps->n * G));
+	ps->partial_cap = G;
+	return KEL_OK;
 }
 
-static int particles_gather(kel_particles *ps, const kel_particle_params *prm, bool want_cell_force) {
+template <class Lc, int STORE>
+static void launch_gather(const PView &v, kel_particles *ps, int steps, int mode, int G) {
+	k_gather<Lc, STORE, false><<<dim3((unsigned)ps->n, (unsigned)G), GT, 0, ps->lat->stream>>>(v, ps->d, steps, mode,
+																							  1.5, ps->partial);
+}
+
+// The gather's per-block sums into ps->partial (G blocks per body); with
+// finish, they are added to the bodies' accumulators here, otherwise the
+// contact pass adds them.
+static int particles_gather(kel_particles *ps, const kel_particle_params *prm, bool want_cell_force, bool finish) {
 	kel_lattice *L = ps->lat;
 	PView v = make_view(L);
+	const int G = gather_blocks(ps);
+	int rc;
+	if ((rc = ensure_partials(ps, G))) return rc;
 	if (prm->coupling == KEL_COUPLING_HLBM) { // D2Q9 (checked); the couple pass wrote the cell forces
+		const dim3 grid((unsigned)ps->n, (unsigned)G);
 		if (L->desc.storage == KEL_STORAGE_FP32)
-			k_gather<D2Q9, STORE_FP32, true><<<ps->n, GT, 0, L->stream>>>(v, ps->d, hlbm_steps(prm), KEL_POROSITY_RAMP,
-																		   prm->eps);
+			k_gather<D2Q9, STORE_FP32, true><<<grid, GT, 0, L->stream>>>(v, ps->d, hlbm_steps(prm), KEL_POROSITY_RAMP,
+																		  prm->eps, ps->partial);
 		else
-			k_gather<D2Q9, STORE_FP16S, true><<<ps->n, GT, 0, L->stream>>>(v, ps->d, hlbm_steps(prm),
-																			KEL_POROSITY_RAMP, prm->eps);
-		KEL_CUDA(cudaGetLastError());
-		return KEL_OK;
+			k_gather<D2Q9, STORE_FP16S, true><<<grid, GT, 0, L->stream>>>(v, ps->d, hlbm_steps(prm),
+																		   KEL_POROSITY_RAMP, prm->eps, ps->partial);
+	} else {
+		if (want_cell_force) {
+			if (!ps->cell_force) KEL_CUDA(cudaMalloc(&ps->cell_force, sizeof(float) * L->plane * L->d.D));
+			KEL_CUDA(cudaMemsetAsync(ps->cell_force, 0, sizeof(float) * L->plane * L->d.D, L->stream));
+			v.cell_force = ps->cell_force;
+		}
+		const bool f32 = L->desc.storage == KEL_STORAGE_FP32;
+		switch (L->d.Q) {
+		case 9: f32 ? launch_gather<D2Q9, STORE_FP32>(v, ps, prm->sub_steps, prm->porosity_mode, G)
+					: launch_gather<D2Q9, STORE_FP16S>(v, ps, prm->sub_steps, prm->porosity_mode, G); break;
+		case 19: f32 ? launch_gather<D3Q19, STORE_FP32>(v, ps, prm->sub_steps, prm->porosity_mode, G)
+					 : launch_gather<D3Q19, STORE_FP16S>(v, ps, prm->sub_steps, prm->porosity_mode, G); break;
+		default: f32 ? launch_gather<D3Q27, STORE_FP32>(v, ps, prm->sub_steps, prm->porosity_mode, G)
+					 : launch_gather<D3Q27, STORE_FP16S>(v, ps, prm->sub_steps, prm->porosity_mode, G); break;
+		}
 	}
-	if (want_cell_force) {
-		if (!ps->cell_force) KEL_CUDA(cudaMalloc(&ps->cell_force, sizeof(float) * L->plane * L->d.D));
-		KEL_CUDA(cudaMemsetAsync(ps->cell_force, 0, sizeof(float) * L->plane * L->d.D, L->stream));
-		v.cell_force = ps->cell_force;
-	}
-	const bool f32 = L->desc.storage == KEL_STORAGE_FP32;
-	switch (L->d.Q) {
-	case 9: f32 ? launch_gather<D2Q9, STORE_FP32>(v, ps, prm->sub_steps, prm->porosity_mode)
-				: launch_gather<D2Q9, STORE_FP16S>(v, ps, prm->sub_steps, prm->porosity_mode); break;
-	case 19: f32 ? launch_gather<D3Q19, STORE_FP32>(v, ps, prm->sub_steps, prm->porosity_mode)
-				 : launch_gather<D3Q19, STORE_FP16S>(v, ps, prm->sub_steps, prm->porosity_mode); break;
-	default: f32 ? launch_gather<D3Q27, STORE_FP32>(v, ps, prm->sub_steps, prm->porosity_mode)
-				 : launch_gather<D3Q27, STORE_FP16S>(v, ps, prm->sub_steps, prm->porosity_mode); break;
-	}
+	if (finish) k_gather_finish<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(ps->d, ps->n, L->d.D, ps->partial, G);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
 
-static int particles_contact(kel_particles *ps, const kel_particle_params *prm) {
+// ParticleContact; with fold, the gather partials are added first.
+static int particles_contact(kel_particles *ps, const kel_particle_params *prm, bool fold) {
 	kel_lattice *L = ps->lat;
 	k_contact<<<(ps->n + 3) / 4, 128, 0, L->stream>>>(ps->d, ps->n, L->d.D, *prm, (int)L->desc.nx, (int)L->desc.ny,
-														   (int)L->desc.nz, (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0);
+													   (int)L->desc.nz, (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0,
+													   fold ? ps->partial : nullptr, gather_blocks(ps));
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
@@ -945,7 +1175,7 @@ extern "C" int kel_particles_reset(kel_particles *ps) {
 
 extern "C" int kel_particles_couple(kel_particles *ps, const kel_particle_params *prm) {
 	int rc = check_params(ps, prm, "kel_particles_couple");
-	if (rc || (rc = particles_couple(ps, prm))) return rc;
+	if (rc || (rc = particles_couple(ps, prm, false))) return rc;
 	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
 	return KEL_OK;
 }
@@ -957,7 +1187,7 @@ extern "C" int kel_particles_gather(kel_particles *ps, const kel_particle_params
 	// cell, computed on the populations before the bodies move
 	if (prm->coupling == KEL_COUPLING_HLBM && host_cell_force && (rc = particles_hlbm_couple(ps, prm, true)))
 		return rc;
-	if ((rc = particles_gather(ps, prm, host_cell_force != nullptr))) return rc;
+	if ((rc = particles_gather(ps, prm, host_cell_force != nullptr, true))) return rc;
 	if (host_cell_force) {
 		kel_lattice *L = ps->lat;
 		if ((rc = field_to_host(L, ps->cell_force, host_cell_force, L->d.D))) return rc;
@@ -968,7 +1198,7 @@ extern "C" int kel_particles_gather(kel_particles *ps, const kel_particle_params
 
 extern "C" int kel_particles_contact(kel_particles *ps, const kel_particle_params *prm) {
 	int rc = check_params(ps, prm, "kel_particles_contact");
-	if (rc || (rc = particles_contact(ps, prm))) return rc;
+	if (rc || (rc = particles_contact(ps, prm, false))) return rc;
 	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
 	return KEL_OK;
 }
@@ -990,6 +1220,74 @@ extern "C" int kel_particles_stamp(kel_particles *ps, const kel_particle_params 
 	return KEL_OK;
 }
 
+// One coupled step: reset + couple (one launch), gather, contact (adding the
+// gather sums), integrate, (HLBM: stamp,) sweep.
+static int coupled_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
+						uint32_t flags) {
+	int rc;
+	if ((rc = particles_couple(ps, prm, true)) || (rc = particles_gather(ps, prm, false, false)) ||
+		(rc = particles_contact(ps, prm, true)) || (rc = particles_integrate(ps, prm)))
+		return rc;
+	if (prm->coupling == KEL_COUPLING_HLBM && (rc = particles_stamp(ps, prm))) return rc;
+	return kel_step(ps->lat, prog, 1, flags);
+}
+
+static ParticleGraphKey graph_key(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog) {
+	ParticleGraphKey k;
+	memset(&k, 0, sizeof(k));
+	kel_lattice *L = ps->lat;
+	k.prm = *prm;
+	k.prog = *prog;
+	k.sweep = sweep_params(L, prog);
+	k.f = L->f;
+	k.por = L->por;
+	k.force = L->force;
+	k.bodies = ps->d;
+	k.boxes = ps->boxes;
+	k.partial = ps->partial;
+	k.n = ps->n;
+	k.gather_g = gather_blocks(ps);
+	k.couple_g = couple_blocks(ps);
+	k.cpt = L->cpt;
+	k.block = L->block;
+	return k;
+}
+
+// The captured graph of two coupled PSM steps starting at an even time step
+// (incremental couples), re-captured when anything it bakes in changed.  The
+// host bookkeeping the captured calls do (time step, porosity epoch) is put
+// back, since nothing ran.
+static int ensure_particle_graph(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog) {
+	kel_lattice *L = ps->lat;
+	int rc;
+	if ((rc = ensure_partials(ps, gather_blocks(ps)))) return rc; // no allocation inside the capture
+	const ParticleGraphKey k = graph_key(ps, prm, prog);
+	if (ps->graph && memcmp(&k, &ps->key, sizeof(k)) == 0) return KEL_OK;
+	if (ps->graph) cudaGraphExecDestroy(ps->graph);
+	ps->graph = nullptr;
+	const uint64_t t0 = L->t, e0 = L->por_epoch, pe0 = ps->epoch;
+	if (cudaStreamBeginCapture(L->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+		cudaGetLastError();
+		return KEL_ERR_CUDA;
+	}
+	rc = coupled_step(ps, prm, prog, 0);
+	if (rc == KEL_OK) rc = coupled_step(ps, prm, prog, 0);
+	cudaGraph_t g = nullptr;
+	cudaError_t e = cudaStreamEndCapture(L->stream, &g);
+	L->t = t0;
+	L->por_epoch = e0;
+	ps->epoch = pe0;
+	if (rc == KEL_OK && e == cudaSuccess && g) e = cudaGraphInstantiate(&ps->graph, g, 0);
+	if (g) cudaGraphDestroy(g);
+	if (rc != KEL_OK || e != cudaSuccess || !ps->graph) {
+		cudaGetLastError();
+		ps->graph = nullptr;
+		return KEL_ERR_CUDA;
+	}
+	ps->key = k;
+	return KEL_OK;
+}
+
 extern "C" int kel_particles_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
 								  uint64_t n_steps, uint32_t step_flags) {
 	int rc = check_params(ps, prm, "kel_particles_step");
@@ -998,13 +1296,40 @@ extern "C" int kel_particles_step(kel_particles *ps, const kel_particle_params *
 	const bool hlbm = prm->coupling == KEL_COUPLING_HLBM;
 	if (hlbm != (prog->collision == KEL_COLL_HLBM))
 		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_step: HLBM coupling goes with the KEL_COLL_HLBM collision");
-	for (uint64_t s = 0; s < n_steps; ++s) {
-		if ((rc = particles_reset(ps)) || (rc = particles_couple(ps, prm)) || (rc = particles_gather(ps, prm, false)) ||
-			(rc = particles_contact(ps, prm)) || (rc = particles_integrate(ps, prm)))
-			return rc;
-		if (hlbm && (rc = particles_stamp(ps, prm))) return rc;
+	kel_lattice *L = ps->lat;
+	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+	if (L->stream != nullptr) KEL_CUDA(cudaStreamIsCapturing(L->stream, &cap));
+	// Steps without macro output replay a captured graph of two coupled steps
+	// (PSM coupling, non-default stream, one-cell-per-thread style sweeps) once
+	// the set is on incremental couples at an even time step.
+	const uint64_t plain = (step_flags & KEL_STEP_ALL_MACROS)
+							   ? 0
+							   : ((step_flags & KEL_STEP_WRITE_MACROS) && n_steps > 0 ? n_steps - 1 : n_steps);
+	const bool graphable = !hlbm && L->stream != nullptr && cap == cudaStreamCaptureStatusNone && L->cpt != CPT_ROWS;
+	uint64_t s = 0;
+	for (; s < n_steps; ++s) {
+		if (graphable && s < plain && plain - s >= 4 && (L->t & 1u) == 0 && ps->epoch != 0 &&
+			ps->epoch == L->por_epoch && L->have_ops && memcmp(&L->last_prog, prog, sizeof(*prog)) == 0)
+			break;
 		const uint32_t fl = (s + 1 == n_steps) ? step_flags : (step_flags & KEL_STEP_ALL_MACROS);
-		if ((rc = kel_step(ps->lat, prog, 1, fl))) return rc;
+		if ((rc = coupled_step(ps, prm, prog, fl))) return rc;
+	}
+	if (s < n_steps) {
+		const uint64_t reps = (plain - s) / 2;
+		if (ensure_particle_graph(ps, prm, prog) == KEL_OK) {
+			for (uint64_t r = 0; r < reps; ++r) {
+				cudaError_t e = cudaGraphLaunch(ps->graph, L->stream);
+				if (e != cudaSuccess)
+					return fail(KEL_ERR_CUDA, "kel_particles_step: graph launch failed: %s", cudaGetErrorString(e));
+			}
+			s += 2 * reps;
+			L->t += 2 * reps;
+			ps->epoch = ++L->por_epoch; // the replays left the field of their last couple
+		}
+		for (; s < n_steps; ++s) {
+			const uint32_t fl = (s + 1 == n_steps) ? step_flags : (step_flags & KEL_STEP_ALL_MACROS);
+			if ((rc = coupled_step(ps, prm, prog, fl))) return rc;
+		}
 	}
 	return KEL_OK;
 }

@@ -814,17 +814,24 @@ __global__ void upcat_backward(const bf16 *dcat, bf16 *du, bf16 *ds, int N, int 
 	}
 }
 
-// 1x1 head: y (N,H,W,3) fp32 = x (.., Ci) * Wh^T + b, plus (res_out >= 0)
-// res_scale times input plane res_in of the network input `in` (Cin planes)
-// on output channel res_out: the network then learns the correction to that
-// plane (a residual target).
+// Residual inputs of the head, per output channel: in[co] < 0 for none.
+constexpr int MAX_RES = 8;
+struct HeadRes {
+	int in[MAX_RES];
+	float scale[MAX_RES];
+};
+
+// 1x1 head: y (N,H,W,3) fp32 = x (.., Ci) * Wh^T + b, plus, on an output
+// channel co with r.in[co] >= 0, r.scale[co] times input plane r.in[co] of the
+// network input `in` (Cin planes): the network then learns the correction to
+// that plane (a residual target).
 __global__ void head_forward(const bf16 *x, const float *w, const float *b, float *y, int64_t M, int Ci, int Co,
-							 const bf16 *in, int Cin, int res_out, int res_in, float res_scale) {
+							 const bf16 *in, int Cin, HeadRes r) {
 	for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
 		for (int co = 0; co < Co; ++co) {
 			float s = b[co];
 			for (int ci = 0; ci < Ci; ++ci) s += w[co * Ci + ci] * __bfloat162float(x[m * Ci + ci]);
-			if (co == res_out) s += res_scale * __bfloat162float(in[m * Cin + res_in]);
+			if (co < MAX_RES && r.in[co] >= 0) s += r.scale[co] * __bfloat162float(in[m * Cin + r.in[co]]);
 			y[m * Co + co] = s;
 		}
 	}
@@ -955,7 +962,11 @@ __global__ void refresh_conv_weights(const float *w32, bf16 *w, bf16 *wf, int Co
 //   9 lubrication estimate of u_x / u_max, halved: with the inlet flux
 //     Q = 2/3 u_max (H - 2) split over a column's gaps as h^3, the gap's
 //     Poiseuille profile gives u_x / u_max = (H - 2) h^2 / sum h^3 4 s (1 - s),
-//   10-15 zero.
+//   10 lubrication pressure, normalised: each column's Poiseuille pressure
+//     gradient is 12 nu Q / sum h^3, so the pressure above the outlet is
+//     proportional to the suffix sum S(x) of 1 / sum h^3 over columns
+//     x' >= x; the plane holds S(x) / S(0) (1 at the inlet),
+//   11-15 zero.
 // Solid cells carry only channels 0-4.
 
 // per (sample, column): fluid-cell count and sum of the cubes of its gap heights
@@ -980,20 +991,25 @@ __global__ void column_features(const uint8_t *mask, int N, int H, int W, float 
 	h3[idx] = s3;
 }
 
-// per sample: suffix sums of the column resistance 1 / max(open, 1/8)^3
-__global__ void column_resistance(const float *open, int N, int W, float *R) {
+// per sample: suffix sums of the column resistance 1 / max(open, 1/8)^3, and
+// of the lubrication resistance 1 / max(sum h^3, 1) normalised by its total
+__global__ void column_resistance(const float *open, const float *h3, int N, int W, float *R, float *PL) {
 	const int b = blockIdx.x * blockDim.x + threadIdx.x;
 	if (b >= N) return;
-	float acc = 0.f;
+	float acc = 0.f, acc2 = 0.f;
 	for (int x = W - 1; x >= 0; --x) {
 		const float o = fmaxf(open[(int64_t)b * W + x], 0.125f);
 		acc += 1.f / (o * o * o);
 		R[(int64_t)b * W + x] = acc / (float)W;
+		acc2 += 1.f / fmaxf(h3[(int64_t)b * W + x], 1.f);
+		PL[(int64_t)b * W + x] = acc2;
 	}
+	const float inv = 1.f / acc2;
+	for (int x = 0; x < W; ++x) PL[(int64_t)b * W + x] *= inv;
 }
 
 __global__ void make_input(const uint8_t *mask, const float *umax, const float *tau, const float *open,
-						   const float *h3, const float *R, bf16 *x, int N, int H, int W, int C) {
+						   const float *h3, const float *R, const float *PL, bf16 *x, int N, int H, int W, int C) {
 	const int64_t n = (int64_t)N * H * W;
 	for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
 		const int b = (int)(p / ((int64_t)H * W));
@@ -1021,6 +1037,7 @@ __global__ void make_input(const uint8_t *mask, const float *umax, const float *
 			v[7] = h / hin;
 			v[8] = shape;
 			v[9] = 0.5f * fminf(hin * h * h / fmaxf(h3[col], 1.f) * shape, 8.f);
+			v[10] = PL[col];
 		}
 		bf16 *o = x + p * C;
 		for (int c = 0; c < C; ++c) o[c] = __float2bfloat16(c < 16 ? v[c] : 0.f);
@@ -1057,9 +1074,8 @@ struct kel_unet {
 	int batch = 0;
 	int conv_kernel = KEL_UNET_CONV_TCGEN05;
 	int *d_err = nullptr; // set by a tensor-core kernel whose bounded wait ran out
-	float *col_open = nullptr, *col_h3 = nullptr, *col_res = nullptr; // input-feature scratch (max_batch x W)
-	int res_out = -1, res_in = 0; // residual head (kel_unet_set_residual); res_out < 0: none
-	float res_scale = 0.f;
+	float *col_open = nullptr, *col_h3 = nullptr, *col_res = nullptr, *col_pl = nullptr; // input-feature scratch (max_batch x W)
+	HeadRes res; // residual head per output channel (kel_unet_set_residual)
 };
 
 namespace {
@@ -1268,6 +1284,10 @@ extern "C" int kel_unet_create(const kel_unet_desc *desc, uint64_t seed, kel_une
 			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_create: widths must be multiples of 16");
 	kel_unet *U = new kel_unet();
 	U->d = *desc;
+	for (int k = 0; k < MAX_RES; ++k) {
+		U->res.in[k] = -1;
+		U->res.scale[k] = 0.f;
+	}
 	const int *w = desc->widths;
 	struct Spec {
 		int co, ci, k, level;
@@ -1329,6 +1349,7 @@ extern "C" int kel_unet_create(const kel_unet_desc *desc, uint64_t seed, kel_une
 	if ((e = cudaMalloc(&U->col_open, colb)) != cudaSuccess) return fail_out(e);
 	if ((e = cudaMalloc(&U->col_h3, colb)) != cudaSuccess) return fail_out(e);
 	if ((e = cudaMalloc(&U->col_res, colb)) != cudaSuccess) return fail_out(e);
+	if ((e = cudaMalloc(&U->col_pl, colb)) != cudaSuccess) return fail_out(e);
 	if ((e = cudaMalloc(&U->out, sizeof(float) * pix * desc->out_channels)) != cudaSuccess) return fail_out(e);
 	if ((e = cudaMalloc(&U->dout, sizeof(float) * pix * desc->out_channels)) != cudaSuccess) return fail_out(e);
 	std::vector<float> h;
@@ -1367,6 +1388,7 @@ extern "C" int kel_unet_destroy(kel_unet *U) {
 	cudaFree(U->col_open);
 	cudaFree(U->col_h3);
 	cudaFree(U->col_res);
+	cudaFree(U->col_pl);
 	if (U->stream) cudaStreamDestroy(U->stream);
 	delete U;
 	return KEL_OK;
@@ -1413,9 +1435,9 @@ extern "C" int kel_unet_make_input(kel_unet *U, const uint8_t *d_mask, const flo
 	const int64_t pix = (int64_t)n * U->d.height * U->d.width;
 	const int H = U->d.height, W = U->d.width;
 	column_features<<<(n * W + 127) / 128, 128, 0, U->stream>>>(d_mask, n, H, W, U->col_open, U->col_h3);
-	column_resistance<<<(n + 63) / 64, 64, 0, U->stream>>>(U->col_open, n, W, U->col_res);
+	column_resistance<<<(n + 63) / 64, 64, 0, U->stream>>>(U->col_open, U->col_h3, n, W, U->col_res, U->col_pl);
 	make_input<<<grid_of(pix), 256, 0, U->stream>>>(d_mask, d_umax, d_tau, U->col_open, U->col_h3, U->col_res,
-													 U->input, n, H, W, 16);
+													 U->col_pl, U->input, n, H, W, 16);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
@@ -1449,8 +1471,7 @@ extern "C" int kel_unet_forward(kel_unet *U, int32_t n, float *d_out) {
 	const UnetLayer &hd = L[14];
 	const int64_t M = (int64_t)n * H * W;
 	head_forward<<<grid_of(M), 256, 0, U->stream>>>(A[T_D0B], U->p + hd.woff, U->p + hd.woff + (int64_t)hd.co * hd.ci,
-													U->out, M, hd.ci, hd.co, U->input, U->d.in_channels, U->res_out,
-													U->res_in, U->res_scale);
+													U->out, M, hd.ci, hd.co, U->input, U->d.in_channels, U->res);
 	KEL_CUDA(cudaGetLastError());
 	if (d_out && d_out != U->out)
 		KEL_CUDA(cudaMemcpyAsync(d_out, U->out, sizeof(float) * M * hd.co, cudaMemcpyDeviceToDevice, U->stream));
@@ -1551,12 +1572,16 @@ extern "C" int kel_unet_synchronize(kel_unet *U) {
 
 extern "C" int kel_unet_set_residual(kel_unet *U, int32_t out_channel, int32_t in_channel, float scale) {
 	if (!U) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_set_residual: null net");
-	if (out_channel >= U->d.out_channels || (out_channel >= 0 && (in_channel < 0 || in_channel >= U->d.in_channels)))
+	if (out_channel >= U->d.out_channels || out_channel >= MAX_RES ||
+		(out_channel >= 0 && (in_channel < 0 || in_channel >= U->d.in_channels)))
 		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_set_residual: channels %d <- %d out of range", out_channel,
 					in_channel);
-	U->res_out = out_channel < 0 ? -1 : out_channel;
-	U->res_in = in_channel;
-	U->res_scale = scale;
+	if (out_channel < 0) {
+		for (int k = 0; k < MAX_RES; ++k) U->res.in[k] = -1;
+		return KEL_OK;
+	}
+	U->res.in[out_channel] = in_channel;
+	U->res.scale[out_channel] = scale;
 	return KEL_OK;
 }
 

@@ -454,6 +454,14 @@ class Batch:
                                              C.c_void_p(d_scale), C.c_void_p(d_offset), int(bool(with_neq))),
                self.lib)
 
+    def warm_refine(self, first, count, d_pred, pred_stride, d_scale, d_offset, iterations, keep_rho=False):
+        """Refinement after warm_start (see kel_batch_warm_refine): `iterations`
+        times two sweeps, then the predicted field is put back while the
+        non-equilibrium part the sweeps produced is kept."""
+        _check(self.lib.kel_batch_warm_refine(self._h, int(first), int(count), C.c_void_p(d_pred), int(pred_stride),
+                                              C.c_void_p(d_scale), C.c_void_p(d_offset), int(iterations),
+                                              int(bool(keep_rho))), self.lib)
+
     def synchronize(self):
         _check(self.lib.kel_batch_synchronize(self._h), self.lib)
 

@@ -109,26 +109,63 @@ def steady_subset(states: SteadyStates):
 
 @dataclass
 class WarmStartNet:
-    """The trained U-Net plus the density normalisation it was trained with."""
+    """The trained U-Net plus the density normalisation it was trained with:
+    rho_norm "global": rho - 1 = target x u_max x rho_scale;
+    rho_norm "lubrication": rho - 1 = target x rho_scale x the channel's
+    lubrication pressure drop (lubrication_drho)."""
     net: UNet
     rho_scale: float
     history: list = field(default_factory=list)
+    rho_norm: str = "global"
 
     @property
     def shape(self):
         return self.net.shape
 
 
-def targets(states: SteadyStates, rho_scale=None, rho_target_rms=0.25):
+def _gap_h3(fluid):
+    """Per (channel, column): sum over the column's vertical runs of fluid
+    cells of the run length cubed.  fluid: (n, ny, nx) bool numpy array or
+    torch tensor."""
+    run = fluid[:, 0] * 0.0
+    s3 = fluid[:, 0] * 0.0
+    for y in range(fluid.shape[1]):
+        f = fluid[:, y] * 1.0
+        s3 = s3 + run ** 3 * (1.0 - f)
+        run = (run + 1.0) * f
+    return s3 + run ** 3
+
+
+def lubrication_drho(mask, u_max, tau):
+    """Pressure drop (as rho) from inlet to outlet that lubrication theory
+    gives for each channel: each column's Poiseuille gradient is
+    dp/dx = 12 nu Q / sum h^3 (gaps of height h, flux Q = 2/3 u_max (ny - 2)
+    of the parabolic inlet), p = rho / 3, so
+    drho = 36 nu Q sum_x 1 / sum h^3.  Works on numpy arrays or torch tensors
+    (mask (n, ny, nx), 1 = solid; u_max and tau (n,))."""
+    fluid = mask == 0
+    ny = mask.shape[1]
+    S0 = (1.0 / _gap_h3(fluid).clip(min=1.0)).sum(1)
+    nu = (tau - 0.5) / 3.0
+    Q = 2.0 / 3.0 * u_max * (ny - 2)
+    return 36.0 * nu * Q * S0
+
+
+def targets(states: SteadyStates, rho_scale=None, rho_target_rms=0.25, rho_norm="global"):
     """Normalised training targets (n, ny, nx, 3) float32 and the density
-    scale: (rho - 1) / u_max over non-wall cells is scaled to RMS
-    rho_target_rms (unless rho_scale is given), which weights the density in
-    the squared-error loss below the velocity (u / u_max is of order 1)."""
-    _, u_max, _ = channel_inputs(states.channels)
+    scale.  rho_norm "global": (rho - 1) / u_max over non-wall cells is scaled
+    to RMS rho_target_rms (unless rho_scale is given), which weights the
+    density in the squared-error loss below the velocity (u / u_max is of
+    order 1).  rho_norm "lubrication": (rho - 1) over each channel's
+    lubrication pressure drop (about 1 at the inlet, 0 at the outlet), times
+    1 / rho_scale, rho_scale set the same way."""
+    mask, u_max, tau = channel_inputs(states.channels)
     um = u_max[:, None, None]
-    drho = (states.rho - 1.0) / um
+    if rho_norm == "lubrication":
+        drho = (states.rho - 1.0) / lubrication_drho(mask, u_max, tau)[:, None, None]
+    else:
+        drho = (states.rho - 1.0) / um
     if rho_scale is None:
-        mask, _, _ = channel_inputs(states.channels)
         fluid = mask == 0
         rho_scale = float(np.sqrt(np.mean(drho[fluid] ** 2)) / rho_target_rms) or 1.0
     t = np.empty(states.u.shape[:3] + (3,), np.float32)
@@ -138,8 +175,19 @@ def targets(states: SteadyStates, rho_scale=None, rho_target_rms=0.25):
     return t, rho_scale
 
 
+def rho_denominator(model, d_mask, d_umax, d_tau):
+    """Per-channel factor turning the network's density output into rho - 1
+    (torch tensor on the inputs' device)."""
+    torch = _torch()
+    um = d_umax.to(torch.float32)
+    if model.rho_norm == "lubrication":
+        return (lubrication_drho(d_mask, um, d_tau.to(torch.float32)) * model.rho_scale).to(torch.float32)
+    return um * model.rho_scale
+
+
 def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, warmup=100, seed=1,
-          widths=(32, 64, 128, 128), log_every=0, rho_target_rms=0.25, residual=False, weight_by_steps=False):
+          widths=(32, 64, 128, 128), log_every=0, rho_target_rms=0.25, residual=False, weight_by_steps=False,
+          rho_norm="global", rho_residual=False):
     """Train the U-Net on the steady states with Adam (cosine schedule).
     rho_target_rms sets the weight of the density in the loss (see targets).
     With weight_by_steps the minibatches draw channels with probability
@@ -147,12 +195,15 @@ def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, 
     dominate the time to steady state), instead of a permutation per epoch.
     With `residual` the u_x output is the correction to the local Poiseuille
     estimate the input planes carry (2 x plane 9 = u_x / u_max of the column's
-    gap, its flux share by h^3): kel_unet_set_residual(0, 9, 2).
+    gap, its flux share by h^3): kel_unet_set_residual(0, 9, 2).  rho_norm
+    selects the density target (see targets); with rho_residual (lubrication
+    norm) the density output is the correction to the lubrication pressure
+    plane 10 (scaled to the target): kel_unet_set_residual(2, 10, 1 / rho_scale).
     Returns a WarmStartNet; its history holds (step, loss) pairs."""
     torch = _torch()
     ny, nx = states.rho.shape[1:]
     mask, u_max, tau = channel_inputs(states.channels)
-    tgt, rho_scale = targets(states, rho_target_rms=rho_target_rms)
+    tgt, rho_scale = targets(states, rho_target_rms=rho_target_rms, rho_norm=rho_norm)
     dev = torch.device("cuda")
     d_mask = torch.from_numpy(mask).to(dev)
     d_umax = torch.from_numpy(u_max).to(dev)
@@ -162,7 +213,11 @@ def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, 
     net = UNet(height=ny, width=nx, widths=widths, out_channels=3, max_batch=batch, seed=seed)
     if residual:
         net.set_residual(0, 9, 2.0)
-    model = WarmStartNet(net, rho_scale)
+    if rho_residual:
+        if rho_norm != "lubrication":
+            raise ValueError("rho_residual goes with rho_norm='lubrication'")
+        net.set_residual(2, 10, 1.0 / rho_scale)
+    model = WarmStartNet(net, rho_scale, rho_norm=rho_norm)
     steps_per_epoch = n // batch
     total = max(1, epochs * steps_per_epoch)
     gen = torch.Generator(device=dev)
@@ -219,32 +274,36 @@ def predict(model: WarmStartNet, d_mask, d_umax, d_tau):
     return out
 
 
-def warm_start(batch: Batch, model: WarmStartNet, d_mask, d_umax, d_tau, with_neq=True, rho_from_net=True):
+def warm_start(batch: Batch, model: WarmStartNet, d_mask, d_umax, d_tau, with_neq=True, rho_from_net=True,
+               refine=0, keep_rho=False):
     """Inference for every channel of `batch` (all of the network's size,
     in channel order) and the populations built from it.  With
-    rho_from_net False the density starts at 1 (only u is predicted)."""
+    rho_from_net False the density starts at 1 (only u is predicted).  With
+    refine > 0, that many refinement passes (kel_batch_warm_refine) follow."""
     torch = _torch()
     pred = predict(model, d_mask, d_umax, d_tau)
     n = pred.shape[0]
     um = d_umax.to(torch.float32)
-    rs = um * model.rho_scale if rho_from_net else torch.zeros_like(um)
+    rs = rho_denominator(model, d_mask, d_umax, d_tau) if rho_from_net else torch.zeros_like(um)
     scale = torch.stack([um, um, rs], dim=1).contiguous()
     offset = torch.zeros((n, 3), dtype=torch.float32, device=pred.device)
     offset[:, 2] = 1.0
     torch.cuda.synchronize()
     ny, nx, oc = model.shape
     batch.warm_start(0, n, pred.data_ptr(), ny * nx * oc, scale.data_ptr(), offset.data_ptr(), with_neq)
+    if refine:
+        batch.warm_refine(0, n, pred.data_ptr(), ny * nx * oc, scale.data_ptr(), offset.data_ptr(), refine, keep_rho)
     return pred
 
 
-def model_init(model: WarmStartNet, with_neq=True, rho_from_net=True):
+def model_init(model: WarmStartNet, with_neq=True, rho_from_net=True, refine=0, keep_rho=False):
     """Initialiser for time_to_steady: the network's prediction."""
     def init(batch, d_mask, d_umax, d_tau):
-        return warm_start(batch, model, d_mask, d_umax, d_tau, with_neq, rho_from_net)
+        return warm_start(batch, model, d_mask, d_umax, d_tau, with_neq, rho_from_net, refine, keep_rho)
     return init
 
 
-def field_init(fields, with_neq=True):
+def field_init(fields, with_neq=True, refine=0, keep_rho=False):
     """Initialiser for time_to_steady from given physical fields (n, ny, nx, 3)
     = (u_x, u_y, rho) per cell, e.g. a known steady state (diagnostics)."""
     def init(batch, d_mask, d_umax, d_tau):
@@ -255,6 +314,8 @@ def field_init(fields, with_neq=True):
         zero = torch.zeros((n, 3), dtype=torch.float32, device="cuda")
         torch.cuda.synchronize()
         batch.warm_start(0, n, d.data_ptr(), d[0].numel(), one.data_ptr(), zero.data_ptr(), with_neq)
+        if refine:
+            batch.warm_refine(0, n, d.data_ptr(), d[0].numel(), one.data_ptr(), zero.data_ptr(), refine, keep_rho)
         batch.synchronize()
         return d
     return init
@@ -358,7 +419,12 @@ def evaluate(model: WarmStartNet, channels, tol=1e-6, check_every=1000, max_step
     pred_u = pred[..., :2] * u_max[:, None, None, None]
     pred_u[mask == 1] = 0.0
     pred_err = np.array([_rel_l2(pred_u[k], u_plain[k]) for k in range(len(channels))])
-    pred_rho = pred[..., 2] * (u_max[:, None, None] * model.rho_scale) + 1.0
+    if model.rho_norm == "lubrication":
+        _, _, tau_h = channel_inputs(channels)
+        den = lubrication_drho(mask, u_max, tau_h) * model.rho_scale
+    else:
+        den = u_max * model.rho_scale
+    pred_rho = pred[..., 2] * den[:, None, None] + 1.0
     fl = mask == 0
     rho_err = np.array([_rel_l2(pred_rho[k][fl[k]] - 1, rho_plain[k][fl[k]] - 1) for k in range(len(channels))])
     nonfinite = dict(pred=int(sum(not np.isfinite(pred[k][fl[k]]).all() for k in range(len(channels)))),

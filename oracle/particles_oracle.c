@@ -109,37 +109,48 @@ static void aabb(int D, const kel_particle_state *p, const int64_t *ext, int per
 
 /* Porosity of every cell: product over bodies (couple.hpp:26-58), 1 = fluid.
  * Each body contributes only inside its AABB, which is where the reference's
- * gather stamps it (psm.hpp:198-265); outside every AABB the cell is fluid. */
+ * gather stamps it (psm.hpp:198-265); outside every AABB the cell is fluid.
+ * A cell counts for a body when the image of the cell nearest the body lies
+ * in the body's AABB.  Walked body by body (index order) over the cells of
+ * each AABB, with the products kept in double until every body is done: the
+ * same factors multiplied in the same order as a loop over the bodies per
+ * cell, in time proportional to the AABBs rather than cells x bodies. */
 void ko_particles_couple(ko_lattice *h, const kel_particle_state *P, int np, const kel_particle_params *prm) {
 	int D, Q, f64, per;
 	int64_t nx, ny, nz;
 	ko_lattice_info(h, &D, &Q, &nx, &ny, &nz, &f64, &per);
 	int64_t ext[3] = {nx, ny, nz};
 	int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
-	for (int64_t c = 0; c < nx * ny * nz; ++c) {
-		int64_t x = c % nx, y = (c / nx) % ny, z = c / (nx * ny);
-		double por = 1.0;
-		for (int p = 0; p < np; ++p) {
-			int64_t a[3] = {0, 0, 0}, b[3] = {1, 1, 1};
-			aabb(D, &P[p], ext, per, sub, a, b);
-			double rel[3] = {rel_coord((double)x, P[p].position[0], per, nx), (double)y - P[p].position[1],
-							 D == 3 ? (double)z - P[p].position[2] : 0.0};
-			double xi = P[p].position[0] + rel[0]; /* the image of x nearest the body */
-			int64_t xc = per ? (int64_t)llround(xi) : x;
-			if (xc < a[0] || xc >= b[0] || y < a[1] || y >= b[1] || (D == 3 && (z < a[2] || z >= b[2]))) continue;
-			double pp;
-			if (sub) {
-				double xs[3] = {xi, (double)y, (double)z};
-				pp = subcell(D, xs, P[p].position, P[p].radius);
-			} else {
-				double s2 = 0.0;
-				for (int k = 0; k < D; ++k) s2 = s2 + rel[k] * rel[k];
-				pp = ramp(sqrt(s2), P[p].radius, prm->eps);
-			}
-			por = por * pp;
-		}
-		ko_lattice_set_porosity_at(h, c, por);
+	int64_t n = nx * ny * nz;
+	double *por = (double *)malloc(sizeof(double) * (size_t)n);
+	for (int64_t c = 0; c < n; ++c) por[c] = 1.0;
+	for (int p = 0; p < np; ++p) {
+		int64_t a[3] = {0, 0, 0}, b[3] = {1, 1, 1};
+		aabb(D, &P[p], ext, per, sub, a, b);
+		for (int64_t iz = a[2]; iz < b[2]; ++iz)
+			for (int64_t iy = a[1]; iy < b[1]; ++iy)
+				for (int64_t ix = a[0]; ix < b[0]; ++ix) {
+					int64_t x = per ? ((ix % nx) + nx) % nx : ix, y = iy, z = D == 3 ? iz : 0;
+					double rel[3] = {rel_coord((double)x, P[p].position[0], per, nx), (double)y - P[p].position[1],
+									 D == 3 ? (double)z - P[p].position[2] : 0.0};
+					double xi = P[p].position[0] + rel[0]; /* the image of x nearest the body */
+					int64_t xc = per ? (int64_t)llround(xi) : x;
+					if (xc != ix) continue; /* this image is not the nearest one (or lies outside the AABB) */
+					double pp;
+					if (sub) {
+						double xs[3] = {xi, (double)y, (double)z};
+						pp = subcell(D, xs, P[p].position, P[p].radius);
+					} else {
+						double s2 = 0.0;
+						for (int k = 0; k < D; ++k) s2 = s2 + rel[k] * rel[k];
+						pp = ramp(sqrt(s2), P[p].radius, prm->eps);
+					}
+					int64_t c = x + nx * (y + ny * z);
+					por[c] = por[c] * pp;
+				}
 	}
+	for (int64_t c = 0; c < n; ++c) ko_lattice_set_porosity_at(h, c, por[c]);
+	free(por);
 }
 
 #define KO_GATHER_BODY(REALT, POP)                                                                           \

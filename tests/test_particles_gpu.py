@@ -158,3 +158,108 @@ def test_coupled_periodic_run_vs_oracle(launch):
     assert np.abs(got[:, 0:2] - ref[:, 0:2]).max() < 1e-9
     assert np.abs(f_gpu - o.populations()).max() < 1e-5
     assert np.all((got[:, 0] >= 0) & (got[:, 0] < nx))
+
+
+def _config3(nsteps_seed=7):
+    """Config C3 at its stated size: 2048 x 512 periodic channel, walls in y,
+    PSM + Guo gravity (g = 1e-6 in -y), tau 0.7, 64 seeded discs R = 8 of
+    density 1.5, 4x4 sub-cell solid fraction, DEM k = 100, damping 0.1.  The
+    real run starts from rest, where 500 steps move nothing; here the bodies
+    get seeded velocities and spins and the populations a seeded
+    perturbation of the rest state, so that forces, contacts and moving
+    porosity are all exercised."""
+    from lbm_mirror_gb300.workloads import particle_channel
+    dims = (2048, 512)
+    flags, st = particle_channel(*dims)
+    rng = np.random.default_rng(nsteps_seed)
+    v = rng.uniform(-0.05, 0.05, (st.shape[0], 2))
+    st[:, 3:5] = st[:, 0:2] - v                         # position_old: velocity v
+    st[:, 9] = st[:, 6] - rng.uniform(-0.01, 0.01, st.shape[0])  # rotation_old: spin
+    w = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+    init = w[None, :] * (1.0 + rng.uniform(-0.02, 0.02, (dims[0] * dims[1], 9)))
+    ops = {1: dict(bc=K.KEL_BC_BOUNCE_BACK), 2: dict(bc=K.KEL_BC_FLUID, collide=1)}
+    prog = K.make_program(0.7, K.KEL_COLL_PSM_GUO, ops, global_force=(0.0, -1e-6, 0.0),
+                          arithmetic=K.KEL_ARITH_REFERENCE)
+    prm = K.make_particle_params(K.KEL_POROSITY_SUBCELL, sub_steps=1, k_n=100.0, zeta_n=0.1,
+                                 body_acceleration=(0.0, -1e-6), wall_axes=0b10)
+    return dims, flags, st, init.astype(np.float32), prog, prm
+
+
+def _gpu_config3(dims, flags, st, init, prog, prm, steps, stream=None):
+    lat = Lattice("D2Q9", dims, periodic_x=True, stream=stream)
+    lat.upload_flags(flags)
+    lat.upload_populations(init)
+    ps = Particles(lat, st)
+    ps.step(prm, prog, steps)
+    out = (ps.download(), lat.populations(np.float64), lat.download_field(K.KEL_FIELD_POROSITY, 1))
+    ps.close()
+    lat.close()
+    return out
+
+
+def test_config3_full_size_vs_oracle():
+    """500 coupled steps of config C3 at 2048 x 512 with 64 bodies, in the
+    reference's arithmetic, on a stream (the captured two-step graph and the
+    incremental couple) against the oracle stepping the same: body positions
+    and velocities within 1e-9, populations within 1e-5, the porosity field
+    (4x4 sub-cell counts) bit-exact."""
+    torch = pytest.importorskip("torch")
+    dims, flags, st0, init, prog, prm = _config3()
+    steps = 500
+    stream = torch.cuda.Stream()
+    got, f_gpu, por_gpu = _gpu_config3(dims, flags, st0, init, prog, prm, steps, stream.cuda_stream)
+
+    o = O.OracleLattice(9, dims, periodic_x=True)
+    o.set_flags(flags)
+    o.set_populations(init.astype(np.float64))
+    st = K.states_from_array(st0)
+    for _ in range(steps):
+        O.particles_reset(st)
+        o.particles_couple(st, prm)
+        o.particles_gather(st, prm)
+        O.particles_contact(st, 2, prm, dims, periodic_x=True)
+        O.particles_integrate(st, 2, prm, dims, periodic_x=True)
+        o.run(prog, 1)
+    ref = K.states_to_array(st)
+    moved = np.abs(ref[:, 0:2] - st0[:, 0:2]).max()
+    assert moved > 1.0  # the bodies did travel
+    np.testing.assert_array_equal(por_gpu.astype(np.float64), o.porosity())
+    assert np.abs(got[:, 0:2] - ref[:, 0:2]).max() < 1e-9
+    vel_gpu, vel_ref = got[:, 0:2] - got[:, 3:5], ref[:, 0:2] - ref[:, 3:5]
+    assert np.abs(vel_gpu - vel_ref).max() < 1e-9
+    assert np.abs(f_gpu - o.populations()).max() < 1e-5
+
+
+def test_coupled_graph_replay_equals_plain_launches():
+    """kel_particles_step on a stream replays a captured graph of two coupled
+    steps; on the legacy stream every launch is issued one by one.  Both give
+    the same bits (64 bodies, 2048 x 512, 61 steps: odd count, macro step)."""
+    torch = pytest.importorskip("torch")
+    dims, flags, st0, init, prog, prm = _config3(11)
+    a = _gpu_config3(dims, flags, st0, init, prog, prm, 61, torch.cuda.Stream().cuda_stream)
+    b = _gpu_config3(dims, flags, st0, init, prog, prm, 61, None)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
+
+
+def test_couple_after_porosity_upload_recomputes_every_cell():
+    """The couple only revisits the bodies' current and previous boxes while
+    the porosity field is the one its last couple left; after an upload of
+    the field it recomputes every cell (equal to the oracle's full pass)."""
+    dims, flags, st0, init, prog, prm = _config3(5)
+    lat = Lattice("D2Q9", dims, periodic_x=True)
+    lat.upload_flags(flags)
+    ps = Particles(lat, st0)
+    ps.couple(prm)
+    st1 = st0.copy()
+    st1[:, 0] = (st1[:, 0] + 37.5) % dims[0]
+    ps.upload(st1)
+    ps.couple(prm)  # incremental: the old boxes go back to 1
+    lat.upload_porosity(np.full(dims[0] * dims[1], 0.25, dtype=np.float32))
+    ps.couple(prm)  # after the upload: every cell
+    por = lat.download_field(K.KEL_FIELD_POROSITY, 1).astype(np.float64)
+    o = O.OracleLattice(9, dims, periodic_x=True)
+    o.particles_couple(K.states_from_array(st1), prm)
+    np.testing.assert_array_equal(por, o.porosity())
+    ps.close()
+    lat.close()

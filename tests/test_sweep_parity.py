@@ -259,3 +259,33 @@ def test_graph_replay_on_a_stream_bit_exact(chunks):
     lat.close()
     np.testing.assert_array_equal(f, dfs)
     np.testing.assert_array_equal(v.astype(np.float64), vel)
+
+
+def test_caller_captured_kel_step_bit_exact():
+    """A caller may capture kel_step into a CUDA graph of its own.  kel_step
+    then launches its sweeps into that capture one by one (it neither nests a
+    capture of its own nor synchronises), and replays of the caller's graph
+    (an even number of steps, so the AA parity the host records stays right)
+    give config C1 bit for bit."""
+    torch = pytest.importorskip("torch")
+    from lbm_mirror_gb300 import Lattice
+    case, dfs, rho, vel = G.load("poiseuille_256x64")
+    prog = with_arith(case["program"], K.KEL_ARITH_REFERENCE)
+    st = torch.cuda.Stream()
+    lat = Lattice("D2Q9", case["dims"], stream=st.cuda_stream)
+    lat.upload_flags(case["flags"])
+    lat.upload_inlet_profile(case["profile"])
+    lat.step(prog, 16, write_macros=False)  # the program is uploaded outside the capture
+    lat.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=st, capture_error_mode="global"):
+        lat.step(prog, 256, write_macros=False)
+    with torch.cuda.stream(st):
+        for _ in range(38):
+            g.replay()
+    lat.step(prog, case["steps"] - 16 - 38 * 256)
+    f = lat.populations(np.float64)
+    r, v = lat.macros()
+    lat.close()
+    np.testing.assert_array_equal(f, dfs)
+    np.testing.assert_array_equal(v.astype(np.float64), vel)

@@ -37,12 +37,19 @@ def test_noalloc_residual_matches_batch_residual_twice():
     n = us[0].shape[0]
     stream = torch.cuda.current_stream().cuda_stream
     out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    planes = [(_planes(us[k]), _planes(us[k - 1])) for k in (1, 2)]
+    torch.cuda.synchronize()
+    free_before = None
     for k in (1, 2):  # two calls in a row, scratch shared between them
-        ua, ub = _planes(us[k]), _planes(us[k - 1])
+        ua, ub = planes[k - 1]
         rc = lib.kel_velocity_residual_noalloc(C.c_void_p(ua.data_ptr()), C.c_void_p(ub.data_ptr()), n, 2,
                                                C.c_void_p(out.data_ptr() + 8 * (k - 1)), C.c_void_p(stream))
         assert rc == K.KEL_OK, lib.kel_last_error_string().decode()
-    torch.cuda.synchronize()
+        torch.cuda.synchronize()
+        if k == 1:  # the first call may load the module that holds the scratch
+            free_before = torch.cuda.mem_get_info()[0]
+    # the second call allocated no device memory
+    assert torch.cuda.mem_get_info()[0] == free_before
     got = out.cpu().numpy()
     for k in (1, 2):
         assert abs(got[k - 1] - res[k]) <= 1e-12 * res[k], (got[k - 1], res[k])
