@@ -77,6 +77,13 @@ extern "C" {
 #define KEL_COLL_PSM 2     /* cmpt::Psm (psm.hpp:37-90) */
 #define KEL_COLL_PSM_GUO 3 /* cmpt::Psm followed by the BGKGuo forcing term */
 #define KEL_COLL_HLBM 4    /* cmpt::Hlbm (hlbm.hpp:53-101), D2Q9: u <- u por + (D > 0 ? N (1 - por) / D : N) */
+/* cmpt::FpLbm (fplbm.hpp:57-128) on cells whose op has no boundary step: BGK
+ * plus the Guo forcing term of the cell's "force" field (the coupling force
+ * the FPLBM particle pass wrote), velocity = momentum / density of the
+ * populations, no global force; the density / velocity macros are left as
+ * FpLbmReset wrote them (density and momentum).  Cells with a boundary step
+ * collide with plain BGK (the drivers' ZouHe + BGK cases). */
+#define KEL_COLL_FPLBM 5
 
 /* ---- arithmetic mode of the sweep -------------------------------------- */
 #define KEL_ARITH_FAST 0      /* float-float equilibrium bracket, fused BGK relaxation */
@@ -195,7 +202,7 @@ typedef struct kel_particle_params {
 	double k_n, zeta_n, gamma_t, mu; /* dem_params (particle/contact.hpp:36-61) */
 	double body_acceleration[3];     /* ParticleIntegrate(g) (particle/integrate.hpp:263-296) */
 	uint32_t wall_axes;    /* DEM box walls at 0 and the extent on these axes (bit a = axis a) */
-	int32_t coupling;      /* KEL_COUPLING_PSM (0) or KEL_COUPLING_HLBM (D2Q9) */
+	int32_t coupling;      /* KEL_COUPLING_PSM (0), KEL_COUPLING_HLBM, KEL_COUPLING_FPLBM(_OWN) (D2Q9) */
 } kel_particle_params;
 #define KEL_COUPLING_PSM 0
 /* HLBM (hlbm.hpp): couple = HlbmReset + the gathers' porosity (last body
@@ -203,6 +210,21 @@ typedef struct kel_particle_params {
  * particle_N / particle_D accumulators after the integrate, and the lattice
  * steps with KEL_COLL_HLBM. */
 #define KEL_COUPLING_HLBM 1
+/* FPLBM (fplbm.hpp), D2Q9, non-periodic lattices: couple = FpLbmReset
+ * (porosity 1 and force 0 everywhere; density and momentum of the cells
+ * whose op has no boundary step) + the particle pass of FpLbmOneParticle:
+ * every body writes, over the cells of an AABB, the sin^2 ramp porosity
+ * (eps 1.5) of its distance and the force (v_body - momentum) (1 - porosity)
+ * (bodies in index order, the last one wins a cell); gather = each body's
+ * FP64 sum of minus those forces, acceleration = sum / mass + the body
+ * acceleration (force and torque are not written); integrate = the Verlet
+ * sub-steps with that acceleration; no contact.  The lattice steps with
+ * KEL_COLL_FPLBM.  KEL_COUPLING_FPLBM keeps the reference's choice of body
+ * 0's AABB and body 0's radius (the group radius) for every body
+ * (fplbm.hpp:186,194), which couples only body 0's neighbourhood;
+ * KEL_COUPLING_FPLBM_OWN uses each body's own AABB and radius. */
+#define KEL_COUPLING_FPLBM 2
+#define KEL_COUPLING_FPLBM_OWN 3
 
 typedef struct kel_particles kel_particles;
 

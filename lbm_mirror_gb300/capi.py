@@ -42,7 +42,7 @@ KEL_BC_ANTI_BOUNCE_BACK = 6
 KEL_BC_EQUILIBRIUM = 7
 KEL_BC_HALFWAY_WALL = 8
 
-KEL_COLL_BGK, KEL_COLL_BGK_GUO, KEL_COLL_PSM, KEL_COLL_PSM_GUO, KEL_COLL_HLBM = 0, 1, 2, 3, 4
+KEL_COLL_BGK, KEL_COLL_BGK_GUO, KEL_COLL_PSM, KEL_COLL_PSM_GUO, KEL_COLL_HLBM, KEL_COLL_FPLBM = 0, 1, 2, 3, 4, 5
 KEL_ARITH_FAST, KEL_ARITH_REFERENCE, KEL_ARITH_SHIFTED = 0, 1, 2
 KEL_MAX_FLAGS = 8
 
@@ -136,7 +136,7 @@ def program_from_dict(d):
 
 
 KEL_POROSITY_RAMP, KEL_POROSITY_SUBCELL = 0, 1
-KEL_COUPLING_PSM, KEL_COUPLING_HLBM = 0, 1
+KEL_COUPLING_PSM, KEL_COUPLING_HLBM, KEL_COUPLING_FPLBM, KEL_COUPLING_FPLBM_OWN = 0, 1, 2, 3
 
 
 class ParticleState(C.Structure):

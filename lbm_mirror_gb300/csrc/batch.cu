@@ -38,7 +38,23 @@ struct ChannelRec {
 	float guo_scale; // 1 - omega / 2
 };
 
+// What one launched block of the sweep needs, in one 32-byte record read at
+// the block's start (the block's tile and its channel's extents, relaxation
+// rate and inlet profile), so that its population loads follow a single
+// load instead of a chain (launch list -> channel record).  `live` drops to
+// 0 when the channel converges (k_batch_residual_final).
+struct __align__(16) TileRec {
+	int64_t cell0; // packed index of the tile's first cell
+	int l0;        // index of that cell within its channel
+	int nxp, ny;   // channel extents
+	float omega;   // channel relaxation rate
+	int prof_off;  // channel inlet profile offset
+	int live;      // channel still running
+};
+
 struct BatchParams {
+	TileRec *trec;   // per launched block
+	int *lfirst;     // per channel: index of its first tile in the launch list (-1: not launched)
 	float *f;
 	int64_t plane;
 	const uint8_t *flags;
@@ -167,14 +183,21 @@ __device__ __forceinline__ bool cell_update_shifted(float (&g)[9], int flag, int
 template <bool ODD, int MODE>
 __global__ void __launch_bounds__(512, MODE == MODE_EXACT ? 1 : 4) k_batch_sweep(const __grid_constant__ BatchParams p) {
 	using L = D2Q9;
-	const int2 tc = p.blist[blockIdx.x]; // (tile, channel)
-	const int ob = tc.x, c = tc.y;
-	if (!p.active[c]) return;
-	const ChannelRec ch = p.ch[c];
-	const int l = (ob - ch.first_block) * blockDim.x + threadIdx.x;
+	const int4 *tr = reinterpret_cast<const int4 *>(p.trec + blockIdx.x);
+	const int4 r0 = __ldg(tr), r1 = __ldg(tr + 1);
+	TileRec ch;
+	ch.cell0 = (int64_t)(((uint64_t)(uint32_t)r0.y << 32) | (uint32_t)r0.x);
+	ch.l0 = r0.z;
+	ch.nxp = r0.w;
+	ch.ny = r1.x;
+	ch.omega = __int_as_float(r1.y);
+	ch.prof_off = r1.z;
+	if (!r1.w) return; // converged channel
+	const int l = ch.l0 + (int)threadIdx.x;
 	if (l >= ch.nxp * ch.ny) return;
 	const int y = l / ch.nxp, x = l - y * ch.nxp;
-	const int64_t cell = ch.off + l;
+	const int64_t cell = ch.cell0 + threadIdx.x;
+	const int64_t ch_off = ch.cell0 - ch.l0; // the channel's first cell
 	// interior cells: every neighbour inside the channel, offsets from the
 	// cell in 32-bit arithmetic
 	const bool fast = p.idx32 && x > 0 && x + 1 < ch.nxp && y > 0 && y + 1 < ch.ny;
@@ -193,7 +216,7 @@ __global__ void __launch_bounds__(512, MODE == MODE_EXACT ? 1 : 4) k_batch_sweep
 			} else {
 				const int sx = x - L::cx(i), sy = y - L::cy(i);
 				const bool in = sx >= 0 && sx < ch.nxp && sy >= 0 && sy < ch.ny;
-				f[i] = in ? __ldcs(p.f + L::opp(i) * p.plane + ch.off + sy * ch.nxp + sx) : 0.f;
+				f[i] = in ? __ldcs(p.f + L::opp(i) * p.plane + ch_off + sy * ch.nxp + sx) : 0.f;
 			}
 		}
 	}
@@ -201,7 +224,7 @@ __global__ void __launch_bounds__(512, MODE == MODE_EXACT ? 1 : 4) k_batch_sweep
 	ctx.ops = p.ops;
 	ctx.profile = p.profiles + ch.prof_off;
 	ctx.omega = ch.omega;
-	ctx.guo_scale = ch.guo_scale;
+	ctx.guo_scale = 1.0f - 0.5f * ch.omega; // unused by BGK
 	ctx.g[0] = ctx.g[1] = ctx.g[2] = 0.f;
 	const float Fc[3] = {0.f, 0.f, 0.f};
 	float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
@@ -229,7 +252,7 @@ __global__ void __launch_bounds__(512, MODE == MODE_EXACT ? 1 : 4) k_batch_sweep
 			const int sx = x - L::cx(i), sy = y - L::cy(i);
 			if (sx < 0 || sx >= ch.nxp || sy < 0 || sy >= ch.ny) __stcs(p.f + pb + cell, 0.f);
 			const int dx = x + L::cx(i), dy = y + L::cy(i);
-			if (dx >= 0 && dx < ch.nxp && dy >= 0 && dy < ch.ny) __stcs(p.f + pb + ch.off + dy * ch.nxp + dx, f[i]);
+			if (dx >= 0 && dx < ch.nxp && dy >= 0 && dy < ch.ny) __stcs(p.f + pb + ch_off + dy * ch.nxp + dx, f[i]);
 		}
 	}
 }
@@ -291,7 +314,12 @@ __global__ void k_batch_residual_final(BatchParams p, int n_channels, double tol
 	// NaN sums (a NaN or overflowed field) give a NaN residual: diverged
 	const double r = (isnan(a) || isnan(b)) ? (double)NAN : (b > 0.0 ? sqrt(a / b) : (a > 0.0 ? INFINITY : 0.0));
 	residual[c] = r;
-	if (r < tol || !isfinite(r)) p.active[c] = 0;
+	if (r < tol || !isfinite(r)) {
+		p.active[c] = 0;
+		const int lf = p.lfirst[c];
+		if (lf >= 0)
+			for (int k = 0; k < ch.nblocks; ++k) p.trec[lf + k].live = 0;
+	}
 }
 
 __global__ void k_batch_init(BatchParams p, int64_t n) {
@@ -494,6 +522,8 @@ struct kel_batch {
 	ChannelRec *d_rec = nullptr;
 	int *d_block_ch = nullptr, *d_active = nullptr;
 	int2 *d_blist = nullptr;
+	TileRec *d_trec = nullptr; // per launched block (same order as d_blist)
+	int *d_lfirst = nullptr;   // per channel: first launch index of its tiles, -1 if not launched
 	double2 *partial = nullptr;
 	double *d_residual = nullptr;
 	OpEntry *ops = nullptr;
@@ -520,6 +550,10 @@ void free_device(kel_batch *B) {
 	cudaFree(B->d_rec);
 	cudaFree(B->d_block_ch);
 	cudaFree(B->d_blist);
+	cudaFree(B->d_trec);
+	cudaFree(B->d_lfirst);
+	B->d_trec = nullptr;
+	B->d_lfirst = nullptr;
 	cudaFree(B->d_active);
 	cudaFree(B->partial);
 	cudaFree(B->d_residual);
@@ -537,6 +571,8 @@ void free_device(kel_batch *B) {
 BatchParams params(const kel_batch *B, int write_macros) {
 	BatchParams p;
 	memset(&p, 0, sizeof(p));
+	p.trec = B->d_trec;
+	p.lfirst = B->d_lfirst;
 	p.f = B->f;
 	p.plane = B->plane;
 	p.flags = B->flags;
@@ -555,6 +591,30 @@ BatchParams params(const kel_batch *B, int write_macros) {
 	p.shifted = B->shifted ? 1 : 0;
 	p.idx32 = 9 * B->plane < ((int64_t)1 << 31) ? 1 : 0;
 	return p;
+}
+
+// Tile records and per-channel launch offsets for the current launch list
+// (B->blist, B->nlaunch; every listed channel is running).
+int upload_tile_records(kel_batch *B) {
+	std::vector<TileRec> tr(B->nlaunch);
+	std::vector<int> lf(B->n, -1);
+	for (int k = 0; k < B->nlaunch; ++k) {
+		const int tile = B->blist[k].x, c = B->blist[k].y;
+		const ChannelRec &r = B->rec[c];
+		if (lf[c] < 0) lf[c] = k;
+		TileRec &t = tr[k];
+		t.l0 = (tile - r.first_block) * B->tile;
+		t.cell0 = r.off + t.l0;
+		t.nxp = r.nxp;
+		t.ny = r.ny;
+		t.omega = r.omega;
+		t.prof_off = r.prof_off;
+		t.live = 1;
+	}
+	KEL_CUDA(cudaMemcpyAsync(B->d_trec, tr.data(), sizeof(TileRec) * B->nlaunch, cudaMemcpyHostToDevice, B->stream));
+	KEL_CUDA(cudaMemcpyAsync(B->d_lfirst, lf.data(), sizeof(int) * B->n, cudaMemcpyHostToDevice, B->stream));
+	KEL_CUDA(cudaStreamSynchronize(B->stream));
+	return KEL_OK;
 }
 
 // Lay the channels out in tiles of `tile` cells and allocate the device side.
@@ -594,11 +654,17 @@ int layout(kel_batch *B, int tile) {
 	KEL_CUDA(cudaMalloc(&B->d_rec, sizeof(ChannelRec) * B->n));
 	KEL_CUDA(cudaMalloc(&B->d_block_ch, sizeof(int) * B->nblocks));
 	KEL_CUDA(cudaMalloc(&B->d_blist, sizeof(int2) * B->nblocks));
+	KEL_CUDA(cudaMalloc(&B->d_trec, sizeof(TileRec) * B->nblocks));
+	KEL_CUDA(cudaMalloc(&B->d_lfirst, sizeof(int) * B->n));
 	B->blist.resize(B->nblocks);
 	for (int b = 0; b < B->nblocks; ++b) B->blist[b] = make_int2(b, B->block_ch[b]);
 	B->nlaunch = B->nblocks;
 	KEL_CUDA(cudaMemcpyAsync(B->d_blist, B->blist.data(), sizeof(int2) * B->nblocks, cudaMemcpyHostToDevice,
 							 B->stream));
+	{
+		int rc2 = upload_tile_records(B);
+		if (rc2) return rc2;
+	}
 	KEL_CUDA(cudaMalloc(&B->d_active, sizeof(int) * B->n));
 	KEL_CUDA(cudaMalloc(&B->partial, sizeof(double2) * B->nblocks));
 	KEL_CUDA(cudaMalloc(&B->d_residual, sizeof(double) * B->n));
@@ -807,6 +873,8 @@ static int compact(kel_batch *B, const std::vector<int> &act) {
 	KEL_CUDA(cudaMemcpyAsync(B->d_blist, B->blist.data(), sizeof(int2) * keep, cudaMemcpyHostToDevice, B->stream));
 	KEL_CUDA(cudaStreamSynchronize(B->stream));
 	B->nlaunch = keep;
+	int rc = upload_tile_records(B);
+	if (rc) return rc;
 	if (B->graph) cudaGraphExecDestroy(B->graph);
 	B->graph = nullptr;
 	return KEL_OK;

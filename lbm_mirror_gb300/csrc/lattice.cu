@@ -906,6 +906,7 @@ static SweepParams make_params(kel_lattice *L, const kel_step_program *P) {
 	p.idx32 = (int64_t)L->d.Q * L->plane < ((int64_t)1 << 31) ? 1 : 0;
 	p.block = L->block;
 	p.hw_mask = L->hw_active ? L->hw_mask : nullptr;
+	p.plain = L->plain_flags;
 	p.stages = L->cpt == CPT_ROWS ? L->block : 0;
 	p.sms = L->sms;
 	p.err = L->d_err;
@@ -1031,6 +1032,10 @@ extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_st
 						"before capturing");
 		OpEntry ops[MAX_FLAGS];
 		if ((rc = lower_program(L, P, ops))) return rc;
+		uint32_t plain = 0;
+		for (int fl = 1; fl < MAX_FLAGS; ++fl)
+			if ((ops[fl].bc == KEL_BC_NONE || ops[fl].bc == KEL_BC_FLUID) && ops[fl].collide) plain |= 1u << fl;
+		L->plain_flags = plain;
 		KEL_CUDA(cudaMemcpyAsync(L->ops, ops, sizeof(ops), cudaMemcpyHostToDevice, L->stream));
 		if ((rc = update_halfway(L, P))) return rc;
 		KEL_CUDA(cudaStreamSynchronize(L->stream));

@@ -62,6 +62,7 @@ struct kel_lattice {
 	uint64_t t = 0;
 	float wshift[27];
 	bool have_ops = false;
+	uint32_t plain_flags = 0; // SweepParams::plain of the current program
 	uint8_t present[kel::gb::MAX_FLAGS] = {0}; // flag values present in the uploaded flag field
 	unsigned *d_seen = nullptr;                 // device scratch of the flag-presence scan (8 words)
 	kel_step_program last_prog;

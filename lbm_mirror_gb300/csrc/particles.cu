@@ -51,6 +51,12 @@ struct kel_particles {
 	// value of lat->por_epoch after this set's last PSM couple (0: none); the
 	// incremental couple needs the field to be untouched since then
 	uint64_t epoch = 0;
+	// box bookkeeping between couples: prev_is_last -- prev[] holds the boxes of
+	// the last couple (the fused contact + integrate moved them there);
+	// cur_fresh -- cur[] holds the boxes of the current positions, for
+	// porosity mode cur_sub
+	bool prev_is_last = false, cur_fresh = false;
+	int cur_sub = 0;
 	cudaGraphExec_t graph = nullptr; // two coupled steps from an even time step
 	ParticleGraphKey key;
 };
@@ -179,7 +185,24 @@ struct Cand {
 	BodyBox box;
 	double X[3];
 	double R;
+	// squared-distance limits of the exact shortcuts (see body_factor),
+	// formed once per body with the same operations
+	double lim_in2, lim_out2;
 };
+
+// The shortcut limits of body_factor for a body of radius R.
+__device__ inline void cand_limits(Cand &c, int sub, double reach, double eps) {
+	const double R = c.R;
+	if (sub) {
+		const double out_r = R + reach + 1e-6, in_r = R - reach - 1e-6;
+		c.lim_out2 = out_r * out_r;
+		c.lim_in2 = in_r > 0.0 ? in_r * in_r : -1.0;
+	} else {
+		const double lo = R - eps / 2, hi = R + eps / 2;
+		c.lim_in2 = lo > 0.0 ? lo * lo - 1e-6 : -1.0;
+		c.lim_out2 = hi * hi + 1e-6;
+	}
+}
 
 // Body q's factor on the porosity of cell (x, y, z), multiplied into por
 // (product of complements, bodies in index order, as couple.hpp:26-58 takes
@@ -213,10 +236,9 @@ __device__ inline void body_factor(const PView &v, int x, int y, int z, const Ca
 	for (int d = 0; d < v.D; ++d) s2 = s2 + rel[d] * rel[d];
 	double pp;
 	if (sub) {
-		const double out_r = R + reach + 1e-6, in_r = R - reach - 1e-6;
-		if (s2 > out_r * out_r) {
+		if (s2 > c.lim_out2) {
 			return; // no sample inside: factor 1
-		} else if (in_r > 0.0 && s2 < in_r * in_r) {
+		} else if (s2 < c.lim_in2) {
 			pp = 0.0;
 		} else {
 			const double xs[3] = {xi, (double)y, (double)z};
@@ -224,12 +246,12 @@ __device__ inline void body_factor(const PView &v, int x, int y, int z, const Ca
 			pp = subcell_porosity(v.D, xs, Xs, R);
 		}
 	} else {
-		const double lo = R - eps / 2, hi = R + eps / 2;
-		if (lo > 0.0 && s2 < lo * lo - 1e-6) pp = 0.0;
-		else if (s2 > hi * hi + 1e-6) return;
+		if (s2 < c.lim_in2) pp = 0.0;
+		else if (s2 > c.lim_out2) return;
 		else pp = ramp(sqrt(s2), R, eps);
 	}
 	por = por * pp;
+	(void)reach;
 }
 
 __device__ inline double subcell_reach(int D) { return D == 3 ? 0.6495190528383290 : 0.5303300858899106; } // 3 sqrt(D) / 8
@@ -237,7 +259,7 @@ __device__ inline double subcell_reach(int D) { return D == 3 ? 0.64951905283832
 // Ordered compaction of the bodies [c0, c0 + TT) for which hit is true (one
 // thread per body, TT threads) into cand[0 .. *ncand).
 __device__ inline void compact_cands(bool hit, int pi, const BodyBox &bb, const kel_particle_state *P, Cand *cand,
-									 int *warp_count, int *ncand) {
+									 int *warp_count, int *ncand, int sub, double reach, double eps) {
 	const int tid = threadIdx.x + threadIdx.y * blockDim.x;
 	const unsigned m = __ballot_sync(0xffffffffu, hit);
 	if ((tid & 31) == 0) warp_count[tid >> 5] = __popc(m);
@@ -257,6 +279,7 @@ __device__ inline void compact_cands(bool hit, int pi, const BodyBox &bb, const 
 		c.box = bb;
 		for (int d = 0; d < 3; ++d) c.X[d] = P[pi].position[d];
 		c.R = P[pi].radius;
+		cand_limits(c, sub, reach, eps);
 	}
 	__syncthreads();
 }
@@ -288,7 +311,7 @@ __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state
 				xs = xs || (bb.a[0] < x0 + TX - v.nx && bb.b[0] > x0 - v.nx) || (bb.a[0] < x0 + TX + v.nx && bb.b[0] > x0 + v.nx);
 			hit = yz && xs;
 		}
-		compact_cands(hit, pi, bb, P, cand, warp_count, &ncand);
+		compact_cands(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
 		if (x < v.nx && y < v.ny)
 			for (int k = 0; k < ncand; ++k) body_factor(v, x, y, z, cand[k], sub, reach, eps, por, touched);
 		__syncthreads();
@@ -310,7 +333,7 @@ __device__ inline bool boxes_touch(const BodyBox &p, const BodyBox &q, const PVi
 	return false;
 }
 
-constexpr int RC_CPT = 4; // cells per thread and pass of the region couple
+constexpr int RC_CPT = 1; // cells per thread and pass of the region couple (more blocks per body instead)
 
 // Incremental couple pass.  Only cells inside some body's box can have a
 // porosity other than 1, so after a couple whose boxes were prev[], the new
@@ -362,7 +385,7 @@ __global__ void __launch_bounds__(TT) k_couple_regions(PView v, const kel_partic
 				bb = cur[pi];
 				hit = boxes_touch(bb, A, v) || (!same && boxes_touch(bb, B, v));
 			}
-			compact_cands(hit, pi, bb, P, cand, warp_count, &ncand);
+			compact_cands(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
 #pragma unroll
 			for (int j = 0; j < RC_CPT; ++j)
 				if (ok[j])
@@ -780,18 +803,17 @@ __device__ inline bool pair_response(const kel_particle_state &self, const kel_p
 	return true;
 }
 
-// One warp per body: the lanes evaluate its pairs 32 at a time, then lane 0
-// adds the contacts in index order (the reference's accumulation order, so
-// the FP64 result is bit-identical) and finally the box walls.  With a gather
-// partial buffer, the body's gather sums are added first, exactly as
-// k_gather_finish would add them (one launch fewer per coupled step).
-__global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_params prm, int nx, int ny, int nz,
-						  int periodic, const double *partial, int G) {
-	__shared__ double fs[4][32][4];
-	__shared__ int hs[4][32];
-	const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int s = blockIdx.x * 4 + w;
-	if (s >= np) return; // warp-uniform
+// Contact of body s, by one warp (every lane calls it): the lanes evaluate
+// its pairs 32 at a time, then lane 0 adds the contacts in index order (the
+// reference's accumulation order, so the FP64 result is bit-identical) and
+// finally the box walls, and writes the body's force (and 2D torque).  The
+// sums start from the body's accumulators, or from zero with zero_start;
+// with a gather partial buffer the body's gather sums are added first,
+// exactly as k_gather_finish would add them.  fs / hs: this warp's scratch.
+__device__ inline void contact_one(kel_particle_state *P, int s, int np, int D, const kel_particle_params &prm, int nx,
+								   int ny, int nz, int periodic, const double *partial, int G, bool zero_start,
+								   double (*fs)[4], int *hs) {
+	const int lane = threadIdx.x & 31;
 	const double steps = (double)(prm.sub_steps == 0 ? 1 : prm.sub_steps);
 	const double Lx = (double)nx;
 	const double ext[3] = {(double)nx, (double)ny, (double)nz};
@@ -799,6 +821,10 @@ __global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_par
 	double force[3] = {self.force[0], self.force[1], self.force[2]};
 	double torque0 = self.torque[0];
 	double torque12[2] = {self.torque[1], self.torque[2]};
+	if (zero_start) {
+		force[0] = force[1] = force[2] = 0.0;
+		torque0 = torque12[0] = torque12[1] = 0.0;
+	}
 	if (partial) {
 		double tot[6];
 		gather_total(partial, s, G, tot);
@@ -813,17 +839,17 @@ __global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_par
 		const int j = j0 + lane;
 		double f[3] = {0, 0, 0}, t0 = 0.0;
 		const bool hit = j < np && j != s && pair_response(self, P[j], s, j, D, prm, steps, Lx, periodic, f, &t0);
-		fs[w][lane][0] = f[0];
-		fs[w][lane][1] = f[1];
-		fs[w][lane][2] = f[2];
-		fs[w][lane][3] = t0;
-		hs[w][lane] = hit ? 1 : 0;
+		fs[lane][0] = f[0];
+		fs[lane][1] = f[1];
+		fs[lane][2] = f[2];
+		fs[lane][3] = t0;
+		hs[lane] = hit ? 1 : 0;
 		__syncwarp();
 		if (lane == 0) {
 			for (int q = 0; q < 32; ++q) {
-				if (!hs[w][q]) continue;
-				for (int k = 0; k < D; ++k) force[k] = force[k] + fs[w][q][k];
-				if (D == 2) torque0 = torque0 + fs[w][q][3];
+				if (!hs[q]) continue;
+				for (int k = 0; k < D; ++k) force[k] = force[k] + fs[q][k];
+				if (D == 2) torque0 = torque0 + fs[q][3];
 			}
 		}
 		__syncwarp();
@@ -854,17 +880,27 @@ __global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_par
 	P[s].force[0] = force[0];
 	P[s].force[1] = force[1];
 	P[s].force[2] = force[2];
-	if (D == 2 || partial) P[s].torque[0] = torque0;
-	if (D == 3 && partial) {
+	if (D == 2 || partial || zero_start) P[s].torque[0] = torque0;
+	if (D == 3 && (partial || zero_start)) {
 		P[s].torque[1] = torque12[0];
 		P[s].torque[2] = torque12[1];
 	}
 }
 
+// One warp per body (four per block).
+__global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_params prm, int nx, int ny, int nz,
+						  int periodic, const double *partial, int G) {
+	__shared__ double fs[4][32][4];
+	__shared__ int hs[4][32];
+	const int w = threadIdx.x >> 5;
+	const int s = blockIdx.x * 4 + w;
+	if (s >= np) return; // warp-uniform
+	contact_one(P, s, np, D, prm, nx, ny, nz, periodic, partial, G, false, fs[w], hs[w]);
+}
+
 // integrate_particle + verlet_step_lambda (integrate.hpp:45-83, particle.hpp:171-211)
-__global__ void k_integrate(kel_particle_state *P, int np, int D, kel_particle_params prm, int nx, int periodic) {
-	const int pi = blockIdx.x * blockDim.x + threadIdx.x;
-	if (pi >= np) return;
+__device__ inline void integrate_one(kel_particle_state *P, int pi, int D, const kel_particle_params &prm, int nx,
+									 int periodic) {
 	kel_particle_state q = P[pi];
 	const int steps = prm.sub_steps == 0 ? 1 : prm.sub_steps;
 	const double ts = 1.0 / (double)steps;
@@ -895,6 +931,43 @@ __global__ void k_integrate(kel_particle_state *P, int np, int D, kel_particle_p
 		}
 	}
 	P[pi] = q;
+}
+
+__global__ void k_integrate(kel_particle_state *P, int np, int D, kel_particle_params prm, int nx, int periodic) {
+	const int pi = blockIdx.x * blockDim.x + threadIdx.x;
+	if (pi >= np) return;
+	integrate_one(P, pi, D, prm, nx, periodic);
+}
+
+constexpr int CI_MAX = 1024; // bodies the fused contact + integrate kernel takes (one CTA)
+
+// Contact and integrate of every body in one CTA, for the coupled step.  Warp
+// w takes bodies w, w + 32, ...: the gather sums and its contacts from a
+// zero force (contact_one), so no reset of the accumulators is needed; after
+// a barrier every thread integrates its bodies and, for the next step's
+// couple, moves each body's box to prev and writes the box of its new
+// position to cur (the shift k_pre would do).
+__global__ void __launch_bounds__(CI_MAX) k_contact_integrate(PView v, kel_particle_state *P, int np,
+															  kel_particle_params prm, const double *partial, int G,
+															  BodyBox *cur, BodyBox *prev, int sub) {
+	__shared__ double fs[CI_MAX / 32][32][4];
+	__shared__ int hs[CI_MAX / 32][32];
+	const int w = threadIdx.x >> 5;
+	for (int s = w; s < np; s += CI_MAX / 32) // warp-uniform
+		contact_one(P, s, np, v.D, prm, v.nx, v.ny, v.nz, v.periodic, partial, G, true, fs[w], hs[w]);
+	__syncthreads();
+	for (int i = threadIdx.x; i < np; i += CI_MAX) {
+		integrate_one(P, i, v.D, prm, v.nx, v.periodic);
+		int64_t a[3], b[3];
+		body_aabb(v.D, P[i], v.nx, v.ny, v.nz, v.periodic, sub, a, b);
+		BodyBox r;
+		for (int k = 0; k < 3; ++k) {
+			r.a[k] = (int)a[k];
+			r.b[k] = (int)b[k];
+		}
+		prev[i] = cur[i];
+		cur[i] = r;
+	}
 }
 
 PView make_view(kel_lattice *L) {
@@ -998,6 +1071,7 @@ extern "C" int kel_particles_destroy(kel_particles *ps) {
 }
 
 extern "C" int kel_particles_upload(kel_particles *ps, const kel_particle_state *host) {
+	if (ps) ps->cur_fresh = false;
 	if (!ps || !host) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_upload: null argument");
 	double rmax = 0.0;
 	for (int i = 0; i < ps->n; ++i) {
@@ -1066,13 +1140,21 @@ static int particles_couple(kel_particles *ps, const kel_particle_params *prm, b
 	if (prm->coupling == KEL_COUPLING_HLBM) {
 		int rc;
 		if (reset && (rc = particles_reset(ps))) return rc;
+		ps->prev_is_last = ps->cur_fresh = false;
 		return particles_hlbm_couple(ps, prm, false);
 	}
 	PView v = make_view(L);
 	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
 	const bool incremental = ps->epoch != 0 && ps->epoch == L->por_epoch;
-	k_pre<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, sub, cur_boxes(ps), prev_boxes(ps), 1,
-													   incremental ? 1 : 0, reset ? 1 : 0);
+	// after the fused contact + integrate, the boxes are ready and nothing
+	// needs resetting: no launch
+	const bool ready = incremental && ps->prev_is_last && ps->cur_fresh && ps->cur_sub == sub && !reset;
+	if (!ready)
+		k_pre<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, sub, cur_boxes(ps), prev_boxes(ps), 1,
+														   incremental && !ps->prev_is_last ? 1 : 0, reset ? 1 : 0);
+	ps->prev_is_last = false;
+	ps->cur_fresh = true;
+	ps->cur_sub = sub;
 	if (incremental)
 		k_couple_regions<<<dim3((unsigned)ps->n, (unsigned)couple_blocks(ps)), TT, 0, L->stream>>>(
 			v, ps->d, cur_boxes(ps), prev_boxes(ps), ps->n, prm->porosity_mode, prm->eps);
@@ -1162,6 +1244,21 @@ static int particles_integrate(kel_particles *ps, const kel_particle_params *prm
 	k_integrate<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(ps->d, ps->n, L->d.D, *prm, (int)L->desc.nx,
 															 (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0);
 	KEL_CUDA(cudaGetLastError());
+	ps->cur_fresh = false; // the bodies moved
+	return KEL_OK;
+}
+
+// Contact (with the gather sums) and integrate of every body in one launch,
+// which also prepares the next couple's boxes.
+static int particles_contact_integrate(kel_particles *ps, const kel_particle_params *prm) {
+	kel_lattice *L = ps->lat;
+	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
+	k_contact_integrate<<<1, CI_MAX, 0, L->stream>>>(make_view(L), ps->d, ps->n, *prm, ps->partial, gather_blocks(ps),
+													 cur_boxes(ps), prev_boxes(ps), sub);
+	KEL_CUDA(cudaGetLastError());
+	ps->prev_is_last = true;
+	ps->cur_fresh = true;
+	ps->cur_sub = sub;
 	return KEL_OK;
 }
 
@@ -1221,13 +1318,20 @@ extern "C" int kel_particles_stamp(kel_particles *ps, const kel_particle_params 
 }
 
 // One coupled step: reset + couple (one launch), gather, contact (adding the
-// gather sums), integrate, (HLBM: stamp,) sweep.
+// gather sums), integrate, (HLBM: stamp,) sweep.  With PSM coupling and up to
+// CI_MAX bodies, contact and integrate are one launch that also prepares the
+// next couple's boxes, so from the second step on a step is couple, gather,
+// contact + integrate and the sweep.
 static int coupled_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
 						uint32_t flags) {
 	int rc;
-	if ((rc = particles_couple(ps, prm, true)) || (rc = particles_gather(ps, prm, false, false)) ||
-		(rc = particles_contact(ps, prm, true)) || (rc = particles_integrate(ps, prm)))
+	const bool fused = prm->coupling == KEL_COUPLING_PSM && ps->n <= CI_MAX;
+	if ((rc = particles_couple(ps, prm, !fused)) || (rc = particles_gather(ps, prm, false, false))) return rc;
+	if (fused) {
+		if ((rc = particles_contact_integrate(ps, prm))) return rc;
+	} else if ((rc = particles_contact(ps, prm, true)) || (rc = particles_integrate(ps, prm))) {
 		return rc;
+	}
 	if (prm->coupling == KEL_COUPLING_HLBM && (rc = particles_stamp(ps, prm))) return rc;
 	return kel_step(ps->lat, prog, 1, flags);
 }
@@ -1266,6 +1370,8 @@ static int ensure_particle_graph(kel_particles *ps, const kel_particle_params *p
 	if (ps->graph) cudaGraphExecDestroy(ps->graph);
 	ps->graph = nullptr;
 	const uint64_t t0 = L->t, e0 = L->por_epoch, pe0 = ps->epoch;
+	const bool pl0 = ps->prev_is_last, cf0 = ps->cur_fresh;
+	const int cs0 = ps->cur_sub;
 	if (cudaStreamBeginCapture(L->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
 		cudaGetLastError();
 		return KEL_ERR_CUDA;
@@ -1277,6 +1383,9 @@ static int ensure_particle_graph(kel_particles *ps, const kel_particle_params *p
 	L->t = t0;
 	L->por_epoch = e0;
 	ps->epoch = pe0;
+	ps->prev_is_last = pl0;
+	ps->cur_fresh = cf0;
+	ps->cur_sub = cs0;
 	if (rc == KEL_OK && e == cudaSuccess && g) e = cudaGraphInstantiate(&ps->graph, g, 0);
 	if (g) cudaGraphDestroy(g);
 	if (rc != KEL_OK || e != cudaSuccess || !ps->graph) {
@@ -1308,8 +1417,11 @@ extern "C" int kel_particles_step(kel_particles *ps, const kel_particle_params *
 	const bool graphable = !hlbm && L->stream != nullptr && cap == cudaStreamCaptureStatusNone && L->cpt != CPT_ROWS;
 	uint64_t s = 0;
 	for (; s < n_steps; ++s) {
+		// the captured steps must find what the replayed ones leave: an
+		// incremental couple and (fused path) boxes prepared by the previous step
+		const bool steady = ps->n > CI_MAX || (ps->prev_is_last && ps->cur_fresh);
 		if (graphable && s < plain && plain - s >= 4 && (L->t & 1u) == 0 && ps->epoch != 0 &&
-			ps->epoch == L->por_epoch && L->have_ops && memcmp(&L->last_prog, prog, sizeof(*prog)) == 0)
+			ps->epoch == L->por_epoch && steady && L->have_ops && memcmp(&L->last_prog, prog, sizeof(*prog)) == 0)
 			break;
 		const uint32_t fl = (s + 1 == n_steps) ? step_flags : (step_flags & KEL_STEP_ALL_MACROS);
 		if ((rc = coupled_step(ps, prm, prog, fl))) return rc;

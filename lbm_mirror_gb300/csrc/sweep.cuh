@@ -86,6 +86,9 @@ struct SweepParams {
 	int stages;       // sweep_rows_kernel: row stages in shared memory
 	int sms;          // multiprocessors of the device (persistent grid of sweep_rows_kernel)
 	unsigned *err;    // sweep_rows_kernel: set to 1 when a bounded wait gave up
+	// bit f: flag value f (1 .. MAX_FLAGS-1) has no boundary step and collides,
+	// so its cells skip the operation-table dispatch (same result)
+	uint32_t plain;
 };
 
 // What the per-cell physics needs from a launch: the flag -> operation table,
@@ -170,8 +173,14 @@ struct Store<STORE_FP16S> {
 		float2 fa = __half22float2(a), fb = __half22float2(b);
 		return make_float4(fa.x + s, fa.y + s, fb.x + s, fb.y + s);
 	}
+	// f = float(h) + s with one rounding, as one mixed-precision add (the
+	// exact conversion of h, then the float add: the same bits as
+	// __half2float(h) + s)
 	__device__ static __forceinline__ float ld1(const void *base, int64_t idx, float s) {
-		return __half2float(static_cast<const __half *>(base)[idx]) + s;
+		const unsigned short h = __half_as_ushort(static_cast<const __half *>(base)[idx]);
+		float r;
+		asm("add.rn.f32.f16 %0, %1, %2;" : "=f"(r) : "h"(h), "f"(s));
+		return r;
 	}
 	__device__ static __forceinline__ void st4(void *base, int64_t idx, float4 v, float s) {
 		__half2 a = __floats2half2_rn(v.x - s, v.y - s);
@@ -1098,6 +1107,11 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 	} else if (!ODD) {
 #pragma unroll
 		for (int i = 0; i < Q; ++i) f[i] = S::ld1(p.f, i * p.plane + cell, p.wshift[i]);
+	} else if (row_interior && p.idx32 && has_xm && has_xp) {
+		// every neighbour exists: unit x offsets, no predicates
+#pragma unroll
+		for (int i = 0; i < Q; ++i)
+			f[i] = S::ld1(fc, L::opp(i) * pl32 - L::cx(i) - L::cy(i) * oy32 - L::cz(i) * oz32, p.wshift[i]);
 	} else if (row_interior && p.idx32) {
 #pragma unroll
 		for (int i = 0; i < Q; ++i) {
@@ -1140,7 +1154,13 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 		Fc[2] = p.hD[cell];
 	}
 	float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
-	const bool col = cell_update<L, COLL, EXACT>(f, flag, y, cell_ctx(p), por, Fc, rho, u);
+	bool col;
+	if (flag < MAX_FLAGS && ((p.plain >> flag) & 1u)) { // no boundary step: straight to the collision
+		collide<L, COLL, EXACT>(f, cell_ctx(p), por, Fc, rho, u);
+		col = true;
+	} else {
+		col = cell_update<L, COLL, EXACT>(f, flag, y, cell_ctx(p), por, Fc, rho, u);
+	}
 	if (p.write_macros && col) {
 		p.rho[cell] = rho;
 #pragma unroll
@@ -1186,6 +1206,11 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 			if (p.idx32) S::st1(fc, L::opp(i) * pl32, f[i], p.wshift[i]);
 			else S::st1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + cell, f[i], p.wshift[i]);
 		}
+	} else if (row_interior && p.idx32 && has_xm && has_xp) {
+		// every destination exists and no source lies outside: no predicates
+#pragma unroll
+		for (int i = 0; i < Q; ++i)
+			S::st1(fc, i * pl32 + L::cx(i) + L::cy(i) * oy32 + L::cz(i) * oz32, f[i], p.wshift[i]);
 	} else if (row_interior && p.idx32) {
 #pragma unroll
 		for (int i = 0; i < Q; ++i) {

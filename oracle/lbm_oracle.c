@@ -329,6 +329,23 @@ void ko_set_hlbm(ko_lattice *h, const double *N, const double *Dv) {
 	}
 }
 
+/* FPLBM (fplbm.hpp): FpLbmReset on every cell, then FpLbmOneParticle for
+ * every body (see lbm_oracle_impl.h) */
+void ko_fplbm_reset(ko_lattice *h, uint32_t plain_mask) {
+	if (h->is_f64) fplbm_reset_f64(&h->f64, plain_mask);
+	else fplbm_reset_f32(&h->f32, plain_mask);
+}
+
+void ko_fplbm_particles(ko_lattice *h, kel_particle_state *P, int np, const kel_particle_params *prm, int own) {
+	if (h->is_f64) fplbm_particles_f64(&h->f64, P, np, prm, own);
+	else fplbm_particles_f32(&h->f32, P, np, prm, own);
+}
+
+void ko_get_force(ko_lattice *h, double *out) {
+	if (h->is_f64) get_vec_f64(h->f64.force, out, h->f64.n * h->f64.d.D);
+	else get_vec_f32(h->f32.force, out, h->f32.n * h->f32.d.D);
+}
+
 void ko_get_porosity(ko_lattice *h, double *out) {
 	if (h->is_f64) get_vec_f64(h->f64.por, out, h->f64.n);
 	else get_vec_f32(h->f32.por, out, h->f32.n);

@@ -84,12 +84,17 @@ static void KO(collide)(KO(ko_lat) * L, const kel_step_program *P, REAL *f, int6
 	REAL pre[27];
 	for (int i = 0; i < d->Q; ++i) pre[i] = f[i];
 	KO(rho_u)(d, f, &rho, u);
-	L->rho[c] = rho;
-	for (int k = 0; k < d->D; ++k) L->vel[c * d->D + k] = u[k];
+	if (P->collision != KEL_COLL_FPLBM) { /* FpLbm leaves FpLbmReset's density and momentum */
+		L->rho[c] = rho;
+		for (int k = 0; k < d->D; ++k) L->vel[c * d->D + k] = u[k];
+	}
 	KO(equilibrium)(d, rho, u, eq);
 	REAL F[3] = {0, 0, 0};
 	if (P->collision == KEL_COLL_BGK_GUO || P->collision == KEL_COLL_PSM_GUO) {
 		for (int k = 0; k < d->D; ++k) F[k] = L->force[c * d->D + k] + (REAL)P->global_force[k];
+	}
+	if (P->collision == KEL_COLL_FPLBM) {
+		for (int k = 0; k < d->D; ++k) F[k] = L->force[c * d->D + k];
 	}
 	switch (P->collision) {
 	case KEL_COLL_BGK: /* collision.hpp:93-95 */
@@ -114,6 +119,12 @@ static void KO(collide)(KO(ko_lat) * L, const kel_step_program *P, REAL *f, int6
 		KO(equilibrium)(d, rho, u, eq);
 		for (int i = 0; i < d->Q; ++i) f[i] = f[i] + freq * (eq[i] - f[i]);
 	} break;
+	case KEL_COLL_FPLBM: /* fplbm.hpp:79-127: BGK + Guo term of the cell force, macros left alone */
+		for (int i = 0; i < d->Q; ++i) {
+			REAL Fi = KO(guo_term)(d, i, u, F);
+			f[i] = f[i] + freq * (eq[i] - f[i]) + Fi * ((REAL)1 - (REAL)0.5f * freq);
+		}
+		break;
 	case KEL_COLL_PSM:
 	case KEL_COLL_PSM_GUO: { /* psm.hpp:79-88 */
 		REAL por = L->por[c];
@@ -252,7 +263,16 @@ static int KO(cell_step)(KO(ko_lat) * L, const kel_step_program *P, int64_t c, i
 	default:
 		return -1;
 	}
-	if (o->collide) KO(collide)(L, P, f, c);
+	if (o->collide) {
+		if (P->collision == KEL_COLL_FPLBM && o->bc != KEL_BC_NONE && o->bc != KEL_BC_FLUID) {
+			/* the FPLBM drivers' boundary cases collide with BGK */
+			kel_step_program bgk = *P;
+			bgk.collision = KEL_COLL_BGK;
+			KO(collide)(L, &bgk, f, c);
+		} else {
+			KO(collide)(L, P, f, c);
+		}
+	}
 	return 0;
 }
 
@@ -365,6 +385,110 @@ static void KO(get_pops)(KO(ko_lat) * L, double *aos) {
 		int64_t x = c % L->nx, y = (c / L->nx) % L->ny, z = c / (L->nx * L->ny);
 		const REAL *f = cur + KO(gidx)(L, x, y, z) * L->d.Q;
 		for (int i = 0; i < L->d.Q; ++i) aos[c * L->d.Q + i] = (double)f[i];
+	}
+}
+
+/* FpLbmReset (fplbm.hpp:26-54) on every cell: porosity 1, force 0; cells
+ * whose flag is in plain_mask (the drivers' info 2) get the density and
+ * momentum (compute_rho_momentum, macroscopic.hpp:41-60) of their current
+ * populations in the density / velocity macros. */
+static void KO(fplbm_reset)(KO(ko_lat) * L, uint32_t plain_mask) {
+	const ko_desc *d = &L->d;
+	REAL *cur = KO(current)(L);
+	for (int64_t c = 0; c < L->n; ++c) {
+		L->por[c] = (REAL)1.0;
+		for (int k = 0; k < d->D; ++k) L->force[c * d->D + k] = (REAL)0.0;
+		const uint8_t info = L->info[c];
+		if (info >= 32u || !((plain_mask >> info) & 1u)) continue;
+		int64_t x = c % L->nx, y = (c / L->nx) % L->ny, z = c / (L->nx * L->ny);
+		const REAL *f = cur + KO(gidx)(L, x, y, z) * d->Q;
+		REAL r = 0, m[3] = {0, 0, 0};
+		for (int j = 0; j < d->Q; ++j) {
+			r = r + f[j];
+			for (int k = 0; k < d->D; ++k) m[k] = m[k] + (REAL)d->c[j][k] * f[j];
+		}
+		L->rho[c] = r;
+		for (int k = 0; k < d->D; ++k) L->vel[c * d->D + k] = m[k];
+	}
+}
+
+/* particle_porosity<T,D,1,ParticleSpheroid>::calculate (porosity.hpp:56-89)
+ * in the lattice's precision: the angle is formed in double and narrowed,
+ * its sine taken in REAL. */
+static REAL KO(fplbm_ramp)(REAL s, REAL rad, REAL eps) {
+	REAL eps_h = eps / 2;
+	REAL lo = rad - eps_h, hi = rad + eps_h;
+	if (s <= lo) return 0;
+	if (s >= hi) return 1;
+	REAL inner = (REAL)((3.14159265358979323846 / (double)(2 * eps)) * (double)(s - lo));
+	REAL c = sizeof(REAL) == 4 ? (REAL)sinf((float)inner) : (REAL)sin((double)inner);
+	return c * c;
+}
+
+/* FpLbmOneParticle (fplbm.hpp:150-247) for every body in index order: over
+ * the cells of an AABB (axis 0 outermost), the ramp porosity (eps 1.5) of
+ * the cell's offset from the body and the force (v_body - momentum) (1 -
+ * porosity) go to the porosity / force fields (a later body overwrites);
+ * the body's acceleration becomes minus their sum (FP64) over its mass plus
+ * the body acceleration, then its Verlet sub-steps (particle.hpp:171-211).
+ * The AABB and radius are body 0's (the reference's) unless `own`.  Cell
+ * quantities in REAL, body state in double. */
+static void KO(fplbm_particles)(KO(ko_lat) * L, kel_particle_state *P, int np, const kel_particle_params *prm, int own) {
+	const ko_desc *d = &L->d;
+	const int D = d->D;
+	const double sss = (double)prm->sub_steps;
+	const int64_t ext[3] = {L->nx, L->ny, L->nz};
+	for (int p = 0; p < np; ++p) {
+		kel_particle_state *q = &P[p];
+		const kel_particle_state *bx = own ? q : &P[0];
+		int64_t a[3] = {0, 0, 0}, b[3] = {1, 1, 1};
+		for (int k = 0; k < D; ++k) { /* aabb.hpp:41-84 */
+			const double X = bx->position[k], r = bx->radius;
+			a[k] = (X >= r) ? (int64_t)(X - r) : 0;
+			b[k] = (int64_t)(X + r + 1.0);
+			if (b[k] > ext[k]) b[k] = ext[k];
+		}
+		REAL vs[3] = {0, 0, 0};
+		for (int k = 0; k < D; ++k) vs[k] = (REAL)((q->position[k] - q->position_old[k]) * sss);
+		const REAL rad = (REAL)bx->radius;
+		double fs[3] = {0, 0, 0};
+		for (int64_t ix = a[0]; ix < b[0]; ++ix)
+			for (int64_t iy = a[1]; iy < b[1]; ++iy)
+				for (int64_t iz = a[2]; iz < b[2]; ++iz) {
+					const int64_t idx[3] = {ix, iy, iz};
+					const int64_t c = ix + L->nx * (iy + L->ny * iz);
+					REAL s2 = 0;
+					for (int k = 0; k < D; ++k) {
+						const REAL rel = (REAL)((double)idx[k] - q->position[k]);
+						s2 = s2 + rel * rel;
+					}
+					const REAL sd = sizeof(REAL) == 4 ? (REAL)sqrtf((float)s2) : (REAL)sqrt((double)s2);
+					const REAL por = KO(fplbm_ramp)(sd, rad, (REAL)1.5);
+					const REAL flip = (REAL)1.0 - por;
+					L->por[c] = por;
+					for (int k = 0; k < D; ++k) {
+						const REAL fk = (vs[k] - L->vel[c * D + k]) * (REAL)1.0 * flip;
+						L->force[c * D + k] = fk;
+						fs[k] = fs[k] - (double)fk;
+					}
+				}
+		for (int k = 0; k < D; ++k) q->acceleration[k] = fs[k] / q->mass + prm->body_acceleration[k];
+		if (prm->sub_steps > 0) {
+			const double ts = 1.0 / sss, t2 = ts * ts;
+			for (int s = 0; s < prm->sub_steps; ++s) {
+				for (int k = 0; k < D; ++k) {
+					const double nw = q->position[k] * 2.0 - q->position_old[k] + q->acceleration[k] * t2;
+					q->position_old[k] = q->position[k];
+					q->position[k] = nw;
+				}
+				const int nr = D == 2 ? 1 : 3;
+				for (int k = 0; k < nr; ++k) {
+					const double nw = q->rotation[k] * 2.0 - q->rotation_old[k] + q->angular_acceleration[k] * t2;
+					q->rotation_old[k] = q->rotation[k];
+					q->rotation[k] = nw;
+				}
+			}
+		}
 	}
 }
 

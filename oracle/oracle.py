@@ -72,6 +72,9 @@ def lib():
         L.ko_particles_hlbm_stamp.argtypes = [vp, vp, C.c_int, vp]
         L.ko_get_hlbm.argtypes = [vp, vp, vp]
         L.ko_set_hlbm.argtypes = [vp, vp, vp]
+        L.ko_fplbm_reset.argtypes = [vp, C.c_uint32]
+        L.ko_fplbm_particles.argtypes = [vp, vp, C.c_int, vp, C.c_int]
+        L.ko_get_force.argtypes = [vp, vp]
         _lib = L
     return _lib
 
@@ -163,6 +166,20 @@ class OracleLattice:
                                   _ptr(cf) if cf is not None else None)
         return cf
 
+
+    def fplbm_reset(self, plain_mask):
+        """FpLbmReset on every cell; cells whose flag is in plain_mask (bit
+        per flag value) get their density and momentum."""
+        lib().ko_fplbm_reset(self._h, int(plain_mask))
+
+    def fplbm_particles(self, states, params, own=False):
+        """FpLbmOneParticle for every body (body 0's AABB and radius unless own)."""
+        lib().ko_fplbm_particles(self._h, C.byref(states), len(states), C.byref(params), int(bool(own)))
+
+    def force(self):
+        out = np.empty(self.n * self.D, dtype=np.float64)
+        lib().ko_get_force(self._h, _ptr(out))
+        return out
 
     def hlbm_couple(self, states, params):
         lib().ko_particles_hlbm_couple(self._h, C.byref(states), len(states), C.byref(params))

@@ -669,6 +669,139 @@ struct HlbmCase {
 };
 
 /*
+ * FPLBM coupling, one time step phase by phase, driving the reference's own
+ * components (fplbm.hpp): FpLbmReset on every cell (porosity 1, force 0,
+ * density and momentum of the info-2 cells), FpLbmOneParticle for every
+ * particle (ramp porosity and coupling force over the AABB, the body's
+ * acceleration and its Verlet sub-steps), then the sweep of
+ * examples/moving_poiseulle_particles_2d_fplbm_gpu/sim.cpp:229-258
+ * (BounceBack on info 1, FpLbm on info 2) and the pull Stream.
+ * in_dir: pparams.txt (sub_steps gx gy tau), particles.f64 (8 per body as
+ *   ParticleCase), init.f64, flags.u8
+ * out_dir: reset_rho.f64, reset_mom.f64 (macros after FpLbmReset),
+ *   porosity.f64, force_field.f64, after_particle.f64 (bodies after
+ *   FpLbmOneParticle), dfs.f64 (t = 1), rho.f64, vel.f64
+ */
+template <typename T, typename Desc, uint64_t NX, uint64_t NY, uint64_t NP>
+struct FplbmCase {
+	using Base = Case<T, Desc, NX, NY>;
+	using PC = ParticleCase<T, Desc, NX, NY, NP>;
+	using NT = typename native_data_type<T>::type;
+	static constexpr uint64_t D = 2, Q = Desc::Q, N = NX * NY;
+	using GroupSch = sch::ParticleGroup<T, D, NP, coll::Spheroid<T>>;
+
+	static void dump_macros(const std::string &out, data<sch::Ptr<typename Base::MacroStruct>> &macros,
+							const char *rho_name, const char *vel_name) {
+		std::vector<double> rho(N), vel(N * D);
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			rho[c] = static_cast<double>(macros.template get<"density">().at(idx).at({}).get());
+			for (uint64_t d = 0; d < D; ++d)
+				vel[c * D + d] = static_cast<double>(macros.template get<"velocity">().at(idx).at({{d}}).get());
+		}
+		write_f64(out + "/" + rho_name, rho);
+		write_f64(out + "/" + vel_name, vel);
+	}
+
+	static int run(const std::string &in, const std::string &out) {
+		std::ifstream pf(in + "/pparams.txt");
+		uint64_t sub_steps;
+		double gx, gy, tau;
+		pf >> sub_steps >> gx >> gy >> tau;
+		auto pv = read_file(in + "/particles.f64", true);
+		auto init = read_file(in + "/init.f64", true);
+		auto flags = read_file(in + "/flags.u8", true);
+		if (pv.size() != NP * 8 * 8 || init.size() != N * Q * 8 || flags.size() != N) return 5;
+		const double *P = reinterpret_cast<const double *>(pv.data());
+		const double *I = reinterpret_cast<const double *>(init.data());
+
+		auto fields_own = heap<data<typename Base::ChunkStruct>>();
+		auto macros_own = heap<data<typename Base::MacroStruct>>();
+		data<sch::Ptr<typename Base::ChunkStruct>> fields{*fields_own};
+		data<sch::Ptr<typename Base::MacroStruct>> macros{*macros_own};
+		auto &dfs_old_f = fields.template get<"dfs_old">();
+		auto &info_f = fields.template get<"info">();
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			info_f.at(idx).set(static_cast<uint8_t>(flags[c]));
+			for (uint64_t i = 0; i < Q; ++i) dfs_old_f.at(idx).at({i}).set(static_cast<NT>(I[c * Q + i]));
+			macros.template get<"density">().at(idx).at({}).set(NT(1));
+		}
+		data<sch::LbmMeter<sch::Scalar<T>>> r0;
+		r0.at({}).set(static_cast<NT>(P[6]));
+		data<sch::Scalar<T>> d0;
+		d0.at({}).set(static_cast<NT>(P[7]));
+		auto g = create_spheroid_particle_group<T, D, NP>(r0, d0, {4u});
+		auto &parts = g.template get<"particles">();
+		for (uint64_t p = 0; p < NP; ++p) {
+			const double *q = P + p * 8;
+			auto &pi = parts.at({p});
+			auto &rb = pi.template get<"rigid_body">();
+			rb.template get<"position">().at({{0u}}).set(static_cast<NT>(q[0]));
+			rb.template get<"position">().at({{1u}}).set(static_cast<NT>(q[1]));
+			rb.template get<"position_old">().at({{0u}}).set(static_cast<NT>(q[2]));
+			rb.template get<"position_old">().at({{1u}}).set(static_cast<NT>(q[3]));
+			rb.template get<"rotation">().at({}).set(static_cast<NT>(q[4]));
+			rb.template get<"rotation_old">().at({}).set(static_cast<NT>(q[5]));
+			constexpr NT pi_c = 3.14159265358979323846;
+			NT r = static_cast<NT>(q[6]), rho = static_cast<NT>(q[7]);
+			NT m = pi_c * r * r * rho;
+			pi.template get<"collision">().template get<"radius">().at({}).set(r);
+			rb.template get<"mass">().at({}).set(m);
+			rb.template get<"inertia">().at({}).set(NT(0.5) * m * r * r);
+			rb.template get<"density">().at({}).set(rho);
+		}
+		data<sch::Ptr<GroupSch>, enc::Native> view{g};
+
+		component<T, Desc, cmpt::FpLbmReset> freset;
+		data<sch::LbmAcceleration<sch::Vector<T, D>>> grav;
+		grav.at({{0u}}).set(static_cast<NT>(gx));
+		grav.at({{1u}}).set(static_cast<NT>(gy));
+		component<T, Desc, cmpt::FpLbmOneParticle> one{grav};
+		data<sch::UInt64> t0{0u}, ss{sub_steps};
+
+		for (uint64_t c = 0; c < N; ++c) freset.apply(fields, macros, Base::unflat(c), t0);
+		dump_macros(out, macros, "reset_rho.f64", "reset_mom.f64");
+		for (uint64_t p = 0; p < NP; ++p) one.apply(fields, macros, view, {{p}}, t0, ss);
+		PC::dump(out + "/after_particle.f64", g);
+		{
+			std::vector<double> por(N), ff(N * D);
+			for (uint64_t c = 0; c < N; ++c) {
+				auto idx = Base::unflat(c);
+				por[c] = macros.template get<"porosity">().at(idx).at({}).get();
+				for (uint64_t k = 0; k < D; ++k) ff[c * D + k] = macros.template get<"force">().at(idx).at({{k}}).get();
+			}
+			write_f64(out + "/porosity.f64", por);
+			write_f64(out + "/force_field.f64", ff);
+		}
+		component<T, Desc, cmpt::FpLbm> collision{static_cast<NT>(tau)};
+		component<T, Desc, cmpt::BounceBack> bb;
+		component<T, Desc, cmpt::Stream> stream;
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			switch (info_f.at(idx).get()) {
+			case 1u: bb.apply(fields, idx, t0); break;
+			case 2u: collision.apply(fields, macros, idx, t0); break;
+			default: break;
+			}
+		}
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			if (info_f.at(idx).get() > 0u) stream.apply(fields, idx, t0);
+		}
+		auto &final_f = fields.template get<"dfs">();
+		std::vector<double> dfs(N * Q);
+		for (uint64_t c = 0; c < N; ++c) {
+			auto idx = Base::unflat(c);
+			for (uint64_t i = 0; i < Q; ++i) dfs[c * Q + i] = static_cast<double>(final_f.at(idx).at({i}).get());
+		}
+		write_f64(out + "/dfs.f64", dfs);
+		dump_macros(out, macros, "rho.f64", "vel.f64");
+		return 0;
+	}
+};
+
+/*
  * Field writers of the reference on given values: write_vtk_file /
  * write_csv_file (modules/core/c++/write_vtk.hpp, write_csv.hpp) of the
  * drivers' MacroStruct {velocity, density} and of the lattice struct {info,
@@ -748,6 +881,9 @@ int main(int argc, char **argv) {
 	if (c == "d3q27_f64_16x12x10") return Case<F64, sch::D3Q27, 16, 12, 10>::run(argv[2], argv[3]);
 	if (c == "hlbm_d2q9_f64_48x40x3") return HlbmCase<F64, sch::D2Q9, 48, 40, 3>::run(argv[2], argv[3]);
 	if (c == "hlbm_d2q9_f32_48x40x3") return HlbmCase<F32, sch::D2Q9, 48, 40, 3>::run(argv[2], argv[3]);
+	if (c == "fplbm_d2q9_f64_48x40x1") return FplbmCase<F64, sch::D2Q9, 48, 40, 1>::run(argv[2], argv[3]);
+	if (c == "fplbm_d2q9_f32_48x40x1") return FplbmCase<F32, sch::D2Q9, 48, 40, 1>::run(argv[2], argv[3]);
+	if (c == "fplbm_d2q9_f32_48x40x3") return FplbmCase<F32, sch::D2Q9, 48, 40, 3>::run(argv[2], argv[3]);
 	if (c == "writers_d2q9_f32_12x7") return WriterCase<F32, sch::D2Q9, 12, 7>::run(argv[2], argv[3]);
 	if (c == "writers_d3q19_f64_5x4x3") return WriterCase<F64, sch::D3Q19, 5, 4, 3>::run(argv[2], argv[3]);
 	std::fprintf(stderr, "unknown case %s\n", c.c_str());

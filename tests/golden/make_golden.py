@@ -230,6 +230,37 @@ def run_hlbm_harness(hcase, bodies, init, flags, workdir):
     return out
 
 
+FPLBM_PARAMS = dict(sub_steps=2, gravity=(0.0, -1e-4), tau=0.8)
+# name -> (harness case, bodies used)
+FPLBM_CASES = {"fplbm_d2q9_f64_48x40x1": ("fplbm_d2q9_f64_48x40x1", 1),
+               "fplbm_d2q9_f32_48x40x1": ("fplbm_d2q9_f32_48x40x1", 1),
+               "fplbm_d2q9_f32_48x40x3": ("fplbm_d2q9_f32_48x40x3", 3)}
+
+
+def fplbm_inputs(nbodies, seed=37):
+    """The HLBM box and populations; the first `nbodies` of its moving discs."""
+    bodies, init, flags = hlbm_inputs(seed)
+    return bodies[:nbodies].copy(), init, flags
+
+
+def run_fplbm_harness(hcase, bodies, init, flags, workdir):
+    ind, outd = os.path.join(workdir, "in"), os.path.join(workdir, "out")
+    os.makedirs(ind, exist_ok=True)
+    os.makedirs(outd, exist_ok=True)
+    P = FPLBM_PARAMS
+    open(os.path.join(ind, "pparams.txt"), "w").write(
+        f"{P['sub_steps']} {P['gravity'][0]!r} {P['gravity'][1]!r} {P['tau']!r}\n")
+    bodies.astype(np.float64).tofile(os.path.join(ind, "particles.f64"))
+    init.astype(np.float64).tofile(os.path.join(ind, "init.f64"))
+    flags.astype(np.uint8).tofile(os.path.join(ind, "flags.u8"))
+    subprocess.check_call([HARNESS, hcase, ind, outd])
+    out = {}
+    for k in ("reset_rho", "reset_mom", "porosity", "force_field", "after_particle", "dfs", "rho", "vel"):
+        a = np.fromfile(os.path.join(outd, k + ".f64"))
+        out[k] = a.reshape(-1, 28) if k.startswith("after") else a
+    return out
+
+
 def particle_registry():
     return {
         "particles_gather_f64": ("particles_d2q9_f64_64x48x5", "gather"),
@@ -245,7 +276,7 @@ def load_particles(name):
 
 def names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and not f.startswith(("particles_", "writers_", "cavity256_", "hlbm_")))
+                  if f.endswith(".npz") and not f.startswith(("particles_", "writers_", "cavity256_", "hlbm_", "fplbm_")))
 
 
 WRITER_CASES = {"writers_d2q9_f32_12x7": (9, (12, 7), np.float32),
@@ -309,6 +340,14 @@ def main():
         emit(name, bodies=bodies, init=init, flags=flags,
                             params=np.array(json.dumps(HLBM_PARAMS)), **out)
         print(f"{name:28s} hlbm: body force after gather {out['after_gather'][:, 18:20].ravel()[:4]}")
+    for name, (hcase, nb) in FPLBM_CASES.items():
+        if args.only and args.only not in name:
+            continue
+        bodies, init, flags = fplbm_inputs(nb)
+        with tempfile.TemporaryDirectory() as td:
+            out = run_fplbm_harness(hcase, bodies, init, flags, td)
+        emit(name, bodies=bodies, init=init, flags=flags, params=np.array(json.dumps(FPLBM_PARAMS)), **out)
+        print(f"{name:28s} fplbm: acceleration {out['after_particle'][:, 12:14].ravel()[:4]}")
     for name, (q, dims, dtype) in WRITER_CASES.items():
         if args.only and args.only not in name:
             continue
