@@ -132,6 +132,7 @@ struct BGKGuo {};
 struct Psm {};
 struct PsmGuo {};
 struct Hlbm {};
+struct FpLbm {};
 struct BounceBack {};
 template <uint64_t I>
 struct AntiBounceBack {};
@@ -196,6 +197,20 @@ public:
 	explicit component(double relaxation__) : relaxation{relaxation__} {}
 	void lower(kel_step_program &p) const {
 		p.collision = KEL_COLL_HLBM;
+		p.tau = relaxation;
+	}
+};
+
+// cmpt::FpLbm (fplbm.hpp:57-128), D2Q9: the collision of the FPLBM coupling;
+// the coupling force it applies comes from kel_particles_* with
+// KEL_COUPLING_FPLBM (FpLbmReset + FpLbmOneParticle).
+template <typename T, typename Desc>
+class component<T, Desc, cmpt::FpLbm> {
+public:
+	double relaxation;
+	explicit component(double relaxation__) : relaxation{relaxation__} {}
+	void lower(kel_step_program &p) const {
+		p.collision = KEL_COLL_FPLBM;
 		p.tau = relaxation;
 	}
 };

@@ -730,8 +730,15 @@ extern "C" int kel_upload_inlet_profile(kel_lattice *L, const double *host_ux, i
 
 static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops) {
 	const HostDesc &d = L->d;
-	if (P->collision < KEL_COLL_BGK || P->collision > KEL_COLL_HLBM)
+	if (P->collision < KEL_COLL_BGK || P->collision > KEL_COLL_FPLBM)
 		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_step: unknown collision %d", P->collision);
+	if (P->collision == KEL_COLL_FPLBM) {
+		if (d.Q != 9) return fail(KEL_ERR_UNSUPPORTED, "kel_step: the FPLBM collision is D2Q9 only");
+		if (P->global_force[0] != 0.0 || P->global_force[1] != 0.0 || P->global_force[2] != 0.0)
+			return fail(KEL_ERR_INVALID_ARGUMENT,
+						"kel_step: the FPLBM collision takes no global force (fplbm.hpp:57-128; gravity acts on "
+						"the bodies)");
+	}
 	if (P->collision == KEL_COLL_HLBM && d.Q != 9)
 		return fail(KEL_ERR_UNSUPPORTED, "kel_step: the HLBM collision is D2Q9 only");
 	if (P->arithmetic == KEL_ARITH_SHIFTED)
@@ -758,6 +765,11 @@ static int lower_program(kel_lattice *L, const kel_step_program *P, OpEntry *ops
 			return fail(KEL_ERR_UNSUPPORTED, "kel_step: AntiBounceBack is D2Q9 only (boundary.hpp:117)");
 		e.bc = used ? o.bc : KEL_BC_NONE;
 		e.collide = o.collide && o.bc != KEL_BC_HALFWAY_WALL ? 1 : 0; // a half-way wall is solid
+		if (P->collision == KEL_COLL_FPLBM && e.collide) { // the FPLBM drivers' cases
+			const bool plain_op = e.bc == KEL_BC_NONE || e.bc == KEL_BC_FLUID;
+			e.bgk_only = plain_op ? 0 : 1;
+			e.no_macros = plain_op ? 1 : 0;
+		}
 		e.east = o.east ? 1 : 0;
 		e.use_profile = o.use_profile ? 1 : 0;
 		e.rho = (float)o.rho;
@@ -822,6 +834,7 @@ static int update_halfway(kel_lattice *L, const kel_step_program *P) {
 }
 
 static cudaError_t launch_one(const kel_lattice *L, const SweepParams &p, int coll, bool exact, bool odd) {
+	if (coll == KEL_COLL_FPLBM) coll = COLL_BGK_GUO; // with the per-op FPLBM switches of lower_program
 	switch (L->d.Q) {
 	case 9: return launch_sweep<D2Q9>(p, L->desc.storage, odd, coll, exact, L->stream);
 	case 19: return launch_sweep<D3Q19>(p, L->desc.storage, odd, coll, exact, L->stream);
@@ -865,8 +878,8 @@ extern "C" int kel_lattice_get_launch(const kel_lattice *L, int32_t *cells_per_t
 // (1 = fluid), force (0), and for HLBM particle_N / particle_D (0).
 static int ensure_collision_fields(kel_lattice *L, int coll) {
 	int rc;
-	const bool por = coll == KEL_COLL_PSM || coll == KEL_COLL_PSM_GUO || coll == KEL_COLL_HLBM;
-	const bool guo = coll == KEL_COLL_BGK_GUO || coll == KEL_COLL_PSM_GUO;
+	const bool por = coll == KEL_COLL_PSM || coll == KEL_COLL_PSM_GUO || coll == KEL_COLL_HLBM || coll == KEL_COLL_FPLBM;
+	const bool guo = coll == KEL_COLL_BGK_GUO || coll == KEL_COLL_PSM_GUO || coll == KEL_COLL_FPLBM;
 	if (por && (rc = ensure_field(L, &L->por, L->plane, 1.0f))) return rc;
 	if (guo && (rc = ensure_field(L, &L->force, L->plane * L->d.D, 0.0f))) return rc;
 	if (coll == KEL_COLL_HLBM) {
@@ -1034,8 +1047,13 @@ extern "C" int kel_step(kel_lattice *L, const kel_step_program *P, uint64_t n_st
 		if ((rc = lower_program(L, P, ops))) return rc;
 		uint32_t plain = 0;
 		for (int fl = 1; fl < MAX_FLAGS; ++fl)
-			if ((ops[fl].bc == KEL_BC_NONE || ops[fl].bc == KEL_BC_FLUID) && ops[fl].collide) plain |= 1u << fl;
+			if ((ops[fl].bc == KEL_BC_NONE || ops[fl].bc == KEL_BC_FLUID) && ops[fl].collide && !ops[fl].no_macros)
+				plain |= 1u << fl;
 		L->plain_flags = plain;
+		uint32_t fp = 0;
+		for (int fl = 1; fl < MAX_FLAGS; ++fl)
+			if ((ops[fl].bc == KEL_BC_NONE || ops[fl].bc == KEL_BC_FLUID) && ops[fl].collide) fp |= 1u << fl;
+		L->plain_flags_fplbm = fp;
 		KEL_CUDA(cudaMemcpyAsync(L->ops, ops, sizeof(ops), cudaMemcpyHostToDevice, L->stream));
 		if ((rc = update_halfway(L, P))) return rc;
 		KEL_CUDA(cudaStreamSynchronize(L->stream));

@@ -63,6 +63,9 @@ struct kel_lattice {
 	float wshift[27];
 	bool have_ops = false;
 	uint32_t plain_flags = 0; // SweepParams::plain of the current program
+	// flags whose op has no boundary step and collides (the FPLBM drivers'
+	// info 2), from the last program passed to kel_step
+	uint32_t plain_flags_fplbm = 1u << 2;
 	uint8_t present[kel::gb::MAX_FLAGS] = {0}; // flag values present in the uploaded flag field
 	unsigned *d_seen = nullptr;                 // device scratch of the flag-presence scan (8 words)
 	kel_step_program last_prog;

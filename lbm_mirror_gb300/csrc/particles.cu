@@ -74,6 +74,7 @@ struct PView {
 	float *por;
 	float *cell_force;
 	float *hN, *hD; // HLBM particle_N (D planes) and particle_D
+	float *rho, *mom; // macros "density" and "velocity" (FPLBM: momentum), D planes
 	float wshift[27];
 };
 
@@ -683,6 +684,169 @@ __global__ void __launch_bounds__(TT) k_hlbm_stamp(PView v, const kel_particle_s
 	for (int d = 0; d < v.D; ++d) v.hN[(int64_t)d * v.plane + pc] = N[d];
 }
 
+// ---- FPLBM (fplbm.hpp) ----------------------------------------------------------------
+
+// FpLbmReset (fplbm.hpp:26-54), one thread per cell: porosity 1, force 0; a
+// cell whose flag is in `plain` (the drivers' info 2) gets the density and
+// momentum (compute_rho_momentum, macroscopic.hpp:41-60) of its current
+// (post-stream) populations in the density / velocity macros.
+template <int STORE>
+__global__ void k_fplbm_reset(PView v, const uint8_t *flags, uint32_t plain) {
+	const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+	if (x >= v.nx) return;
+	const int64_t pc = (int64_t)y * v.nxp + x;
+	v.por[pc] = 1.0f;
+	v.cell_force[pc] = 0.0f;
+	v.cell_force[v.plane + pc] = 0.0f;
+	const uint8_t fl = flags[pc];
+	if (fl >= 32 || !((plain >> fl) & 1u)) return;
+	float r = 0.f, m0 = 0.f, m1 = 0.f;
+#pragma unroll
+	for (int j = 0; j < 9; ++j) {
+		const float f = pop_post<D2Q9, STORE>(v, x, y, 0, j);
+		r = __fadd_rn(r, f);
+		if (D2Q9::cx(j) > 0) m0 = __fadd_rn(m0, f);
+		if (D2Q9::cx(j) < 0) m0 = __fsub_rn(m0, f);
+		if (D2Q9::cy(j) > 0) m1 = __fadd_rn(m1, f);
+		if (D2Q9::cy(j) < 0) m1 = __fsub_rn(m1, f);
+	}
+	v.rho[pc] = r;
+	v.mom[pc] = m0;
+	v.mom[v.plane + pc] = m1;
+}
+
+// The AABB of body p's coupling (aabb.hpp:41-84, from the per-body boxes of
+// k_pre): its own, or body 0's for every body as the reference's
+// FpLbmOneParticle takes it (fplbm.hpp:186).
+__device__ inline void fplbm_box(const BodyBox *box, int p, int own, int64_t *a, int64_t *b) {
+	const BodyBox &q = box[own ? p : 0];
+	for (int k = 0; k < 3; ++k) {
+		a[k] = q.a[k];
+		b[k] = q.b[k];
+	}
+}
+
+// particle_porosity<float,2,1,ParticleSpheroid>::calculate (porosity.hpp:56-89):
+// the angle formed in double and narrowed, its sine in float.
+__device__ inline float fplbm_ramp(float s, float rad, float eps) {
+	const float eps_h = __fdiv_rn(eps, 2.0f);
+	const float lo = __fsub_rn(rad, eps_h), hi = __fadd_rn(rad, eps_h);
+	if (s <= lo) return 0.f;
+	if (s >= hi) return 1.f;
+	const float inner = (float)((PI_D / (double)__fmul_rn(2.0f, eps)) * (double)__fsub_rn(s, lo));
+	const float c = sinf(inner);
+	return __fmul_rn(c, c);
+}
+
+// Body p's porosity and coupling force at cell (x, y): the body velocity
+// (X - X_old) sub_steps and the cell's offset formed in FP64 and narrowed,
+// the rest in float as the reference's T (fplbm.hpp:211-228).
+__device__ inline void fplbm_cell(const PView &v, const kel_particle_state &q, float rad, double sss, int x, int y,
+								  float &por, float &f0, float &f1) {
+	const float vs0 = (float)((q.position[0] - q.position_old[0]) * sss);
+	const float vs1 = (float)((q.position[1] - q.position_old[1]) * sss);
+	const float r0 = (float)((double)x - q.position[0]), r1 = (float)((double)y - q.position[1]);
+	float s2 = 0.f;
+	s2 = __fadd_rn(s2, __fmul_rn(r0, r0));
+	s2 = __fadd_rn(s2, __fmul_rn(r1, r1));
+	por = fplbm_ramp(__fsqrt_rn(s2), rad, 1.5f);
+	const float flip = __fsub_rn(1.0f, por);
+	const int64_t pc = (int64_t)y * v.nxp + x;
+	f0 = __fmul_rn(__fmul_rn(__fsub_rn(vs0, v.mom[pc]), 1.0f), flip);
+	f1 = __fmul_rn(__fmul_rn(__fsub_rn(vs1, v.mom[v.plane + pc]), 1.0f), flip);
+}
+
+// The porosity and force fields of FpLbmOneParticle (fplbm.hpp:207-228), one
+// thread per cell: of the bodies (index order) whose coupling AABB holds the
+// cell, the last one's values (the reference's later writes win).
+__global__ void __launch_bounds__(TT) k_fplbm_field(PView v, const kel_particle_state *P, const BodyBox *box, int np,
+													int own, double sss) {
+	const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y;
+	if (x >= v.nx || y >= v.ny) return;
+	int last = -1;
+	for (int p = 0; p < np; ++p) {
+		int64_t a[3], b[3];
+		fplbm_box(box, p, own, a, b);
+		if (x >= a[0] && x < b[0] && y >= a[1] && y < b[1]) last = p;
+	}
+	if (last < 0) return;
+	const float rad = (float)(own ? P[last].radius : P[0].radius);
+	float por, f0, f1;
+	fplbm_cell(v, P[last], rad, sss, x, y, por, f0, f1);
+	const int64_t pc = (int64_t)y * v.nxp + x;
+	v.por[pc] = por;
+	v.cell_force[pc] = f0;
+	v.cell_force[v.plane + pc] = f1;
+}
+
+// Minus the sum of body p's coupling forces over its AABB, FP64, G blocks per
+// body with fixed-order reductions into partial[(p * G + g) * 6 ..] (force
+// x, y; the other four entries zero), as k_gather lays them out.
+__global__ void __launch_bounds__(GT) k_fplbm_sums(PView v, const kel_particle_state *P, const BodyBox *box, int own,
+												   double sss, double *partial) {
+	__shared__ double part[GT / 32][2];
+	const int p = blockIdx.x;
+	const kel_particle_state &q = P[p];
+	int64_t a[3], b[3];
+	fplbm_box(box, p, own, a, b);
+	const int64_t ex = b[0] - a[0], ey = b[1] - a[1];
+	const int64_t ncell = (ex > 0 && ey > 0) ? ex * ey : 0;
+	const float rad = (float)(own ? q.radius : P[0].radius);
+	double acc0 = 0.0, acc1 = 0.0;
+	for (int64_t k = (int64_t)blockIdx.y * GT + threadIdx.x; k < ncell; k += (int64_t)gridDim.y * GT) {
+		const int x = (int)(a[0] + k % ex), y = (int)(a[1] + k / ex);
+		float por, f0, f1;
+		fplbm_cell(v, q, rad, sss, x, y, por, f0, f1);
+		acc0 -= (double)f0;
+		acc1 -= (double)f1;
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		acc0 += __shfl_down_sync(0xffffffffu, acc0, o);
+		acc1 += __shfl_down_sync(0xffffffffu, acc1, o);
+	}
+	if ((threadIdx.x & 31) == 0) {
+		part[threadIdx.x >> 5][0] = acc0;
+		part[threadIdx.x >> 5][1] = acc1;
+	}
+	__syncthreads();
+	if (threadIdx.x < 6) {
+		double tot = 0.0;
+		if (threadIdx.x < 2)
+			for (int w = 0; w < GT / 32; ++w) tot += part[w][threadIdx.x];
+		partial[((int64_t)p * gridDim.y + blockIdx.y) * 6 + threadIdx.x] = tot;
+	}
+}
+
+// FpLbmOneParticle's tail (fplbm.hpp:230-246), one thread per body:
+// acceleration = the summed coupling force / mass + the body acceleration
+// (with set_accel); then (with verlet and sub_steps > 0) the position Verlet
+// sub-steps of verlet_step_lambda (particle.hpp:171-211).
+__global__ void k_fplbm_integrate(kel_particle_state *P, int np, kel_particle_params prm, const double *partial, int G,
+								  int set_accel, int verlet) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= np) return;
+	kel_particle_state q = P[i];
+	if (set_accel) {
+		double tot[6];
+		gather_total(partial, i, G, tot);
+		for (int k = 0; k < 2; ++k) q.acceleration[k] = tot[k] / q.mass + prm.body_acceleration[k];
+	}
+	if (verlet && prm.sub_steps > 0) {
+		const double sss = (double)prm.sub_steps, ts = 1.0 / sss, t2 = ts * ts;
+		for (int s = 0; s < prm.sub_steps; ++s) {
+			for (int k = 0; k < 2; ++k) {
+				const double nw = q.position[k] * 2.0 - q.position_old[k] + q.acceleration[k] * t2;
+				q.position_old[k] = q.position[k];
+				q.position[k] = nw;
+			}
+			const double nw = q.rotation[0] * 2.0 - q.rotation_old[0] + q.angular_acceleration[0] * t2;
+			q.rotation_old[0] = q.rotation[0];
+			q.rotation[0] = nw;
+		}
+	}
+	P[i] = q;
+}
+
 // ---- DEM contact (contact.hpp) ----------------------------------------------------
 
 __device__ inline bool safe_normalize(int D, const double *in, double *out) {
@@ -939,35 +1103,34 @@ __global__ void k_integrate(kel_particle_state *P, int np, int D, kel_particle_p
 	integrate_one(P, pi, D, prm, nx, periodic);
 }
 
-constexpr int CI_MAX = 1024; // bodies the fused contact + integrate kernel takes (one CTA)
+// Contact of the coupled step: one warp per block and one block per body, so
+// that the FP64 pair work (issued at a small fraction of the FP32 rate on
+// this GPU) spreads over as many multiprocessors as there are bodies.  The
+// sums start from zero and take the gather partials first.
+__global__ void __launch_bounds__(32) k_contact_step(kel_particle_state *P, int np, int D, kel_particle_params prm,
+													 int nx, int ny, int nz, int periodic, const double *partial, int G) {
+	__shared__ double fs[32][4];
+	__shared__ int hs[32];
+	contact_one(P, blockIdx.x, np, D, prm, nx, ny, nz, periodic, partial, G, true, fs, hs);
+}
 
-// Contact and integrate of every body in one CTA, for the coupled step.  Warp
-// w takes bodies w, w + 32, ...: the gather sums and its contacts from a
-// zero force (contact_one), so no reset of the accumulators is needed; after
-// a barrier every thread integrates its bodies and, for the next step's
-// couple, moves each body's box to prev and writes the box of its new
-// position to cur (the shift k_pre would do).
-__global__ void __launch_bounds__(CI_MAX) k_contact_integrate(PView v, kel_particle_state *P, int np,
-															  kel_particle_params prm, const double *partial, int G,
-															  BodyBox *cur, BodyBox *prev, int sub) {
-	__shared__ double fs[CI_MAX / 32][32][4];
-	__shared__ int hs[CI_MAX / 32][32];
-	const int w = threadIdx.x >> 5;
-	for (int s = w; s < np; s += CI_MAX / 32) // warp-uniform
-		contact_one(P, s, np, v.D, prm, v.nx, v.ny, v.nz, v.periodic, partial, G, true, fs[w], hs[w]);
-	__syncthreads();
-	for (int i = threadIdx.x; i < np; i += CI_MAX) {
-		integrate_one(P, i, v.D, prm, v.nx, v.periodic);
-		int64_t a[3], b[3];
-		body_aabb(v.D, P[i], v.nx, v.ny, v.nz, v.periodic, sub, a, b);
-		BodyBox r;
-		for (int k = 0; k < 3; ++k) {
-			r.a[k] = (int)a[k];
-			r.b[k] = (int)b[k];
-		}
-		prev[i] = cur[i];
-		cur[i] = r;
+// Integrate of the coupled step, one thread per body; then, for the next
+// step's couple, the body's box moves to prev and the box of its new
+// position goes to cur (the shift k_pre would do).
+__global__ void k_integrate_boxes(PView v, kel_particle_state *P, int np, kel_particle_params prm, BodyBox *cur,
+								  BodyBox *prev, int sub) {
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= np) return;
+	integrate_one(P, i, v.D, prm, v.nx, v.periodic);
+	int64_t a[3], b[3];
+	body_aabb(v.D, P[i], v.nx, v.ny, v.nz, v.periodic, sub, a, b);
+	BodyBox r;
+	for (int k = 0; k < 3; ++k) {
+		r.a[k] = (int)a[k];
+		r.b[k] = (int)b[k];
 	}
+	prev[i] = cur[i];
+	cur[i] = r;
 }
 
 PView make_view(kel_lattice *L) {
@@ -987,6 +1150,8 @@ PView make_view(kel_lattice *L) {
 	v.por = L->por;
 	v.hN = L->hN;
 	v.hD = L->hD;
+	v.rho = L->rho;
+	v.mom = L->u;
 	for (int i = 0; i < 27; ++i) v.wshift[i] = L->wshift[i];
 	return v;
 }
@@ -998,8 +1163,15 @@ int check_params(const kel_particles *ps, const kel_particle_params *prm, const 
 	if (prm->sub_steps < 0) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: negative sub_steps", who);
 	if ((prm->porosity_mode == KEL_POROSITY_RAMP || prm->coupling == KEL_COUPLING_HLBM) && !(prm->eps > 0))
 		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: eps must be positive", who);
-	if (prm->coupling != KEL_COUPLING_PSM && prm->coupling != KEL_COUPLING_HLBM)
+	if (prm->coupling < KEL_COUPLING_PSM || prm->coupling > KEL_COUPLING_FPLBM_OWN)
 		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: unknown coupling %d", who, prm->coupling);
+	if (prm->coupling == KEL_COUPLING_FPLBM || prm->coupling == KEL_COUPLING_FPLBM_OWN) {
+		if (ps->lat->d.Q != 9) return fail(KEL_ERR_UNSUPPORTED, "%s: FPLBM coupling is D2Q9 only", who);
+		if (ps->lat->desc.flags & KEL_LATTICE_PERIODIC_X)
+			return fail(KEL_ERR_UNSUPPORTED, "%s: FPLBM coupling needs a non-periodic lattice", who);
+		int rc;
+		if ((rc = ensure_field(ps->lat, &ps->lat->force, ps->lat->plane * ps->lat->d.D, 0.0f))) return rc;
+	}
 	if (prm->coupling == KEL_COUPLING_HLBM) {
 		if (ps->lat->d.Q != 9) return fail(KEL_ERR_UNSUPPORTED, "%s: HLBM coupling is D2Q9 only", who);
 		int rc;
@@ -1229,6 +1401,47 @@ static int particles_gather(kel_particles *ps, const kel_particle_params *prm, b
 	return KEL_OK;
 }
 
+static bool is_fplbm(const kel_particle_params *prm) {
+	return prm->coupling == KEL_COUPLING_FPLBM || prm->coupling == KEL_COUPLING_FPLBM_OWN;
+}
+
+// FPLBM couple: the bodies' boxes, FpLbmReset on every cell, then the
+// porosity / force fields of the particle pass.
+static int particles_fplbm_couple(kel_particles *ps, const kel_particle_params *prm) {
+	kel_lattice *L = ps->lat;
+	PView v = make_view(L);
+	v.cell_force = L->force;
+	const int own = prm->coupling == KEL_COUPLING_FPLBM_OWN;
+	k_pre<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, 0, cur_boxes(ps), prev_boxes(ps), 1, 0, 0);
+	const dim3 rg((unsigned)((L->desc.nx + 127) / 128), (unsigned)L->desc.ny);
+	if (L->desc.storage == KEL_STORAGE_FP32) k_fplbm_reset<STORE_FP32><<<rg, 128, 0, L->stream>>>(v, L->flags, L->plain_flags_fplbm);
+	else k_fplbm_reset<STORE_FP16S><<<rg, 128, 0, L->stream>>>(v, L->flags, L->plain_flags_fplbm);
+	k_fplbm_field<<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, cur_boxes(ps), ps->n, own,
+																(double)prm->sub_steps);
+	KEL_CUDA(cudaGetLastError());
+	++L->por_epoch;
+	ps->epoch = 0;
+	ps->prev_is_last = ps->cur_fresh = false;
+	return KEL_OK;
+}
+
+// FPLBM gather: each body's coupling-force sum (boxes of the last couple),
+// then (set_accel) its acceleration and (verlet) the Verlet sub-steps.
+static int particles_fplbm_gather(kel_particles *ps, const kel_particle_params *prm, bool verlet) {
+	kel_lattice *L = ps->lat;
+	const int G = gather_blocks(ps);
+	int rc;
+	if ((rc = ensure_partials(ps, G))) return rc;
+	const int own = prm->coupling == KEL_COUPLING_FPLBM_OWN;
+	k_fplbm_sums<<<dim3((unsigned)ps->n, (unsigned)G), GT, 0, L->stream>>>(make_view(L), ps->d, cur_boxes(ps), own,
+																		   (double)prm->sub_steps, ps->partial);
+	k_fplbm_integrate<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(ps->d, ps->n, *prm, ps->partial, G, 1,
+																   verlet ? 1 : 0);
+	KEL_CUDA(cudaGetLastError());
+	if (verlet) ps->cur_fresh = false;
+	return KEL_OK;
+}
+
 // ParticleContact; with fold, the gather partials are added first.
 static int particles_contact(kel_particles *ps, const kel_particle_params *prm, bool fold) {
 	kel_lattice *L = ps->lat;
@@ -1248,13 +1461,16 @@ static int particles_integrate(kel_particles *ps, const kel_particle_params *prm
 	return KEL_OK;
 }
 
-// Contact (with the gather sums) and integrate of every body in one launch,
-// which also prepares the next couple's boxes.
+// Contact (from zero, with the gather sums) and integrate of the coupled
+// step; the integrate also prepares the next couple's boxes.
 static int particles_contact_integrate(kel_particles *ps, const kel_particle_params *prm) {
 	kel_lattice *L = ps->lat;
 	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
-	k_contact_integrate<<<1, CI_MAX, 0, L->stream>>>(make_view(L), ps->d, ps->n, *prm, ps->partial, gather_blocks(ps),
-													 cur_boxes(ps), prev_boxes(ps), sub);
+	const PView v = make_view(L);
+	k_contact_step<<<ps->n, 32, 0, L->stream>>>(ps->d, ps->n, v.D, *prm, v.nx, v.ny, v.nz, v.periodic, ps->partial,
+												 gather_blocks(ps));
+	k_integrate_boxes<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, *prm, cur_boxes(ps),
+																   prev_boxes(ps), sub);
 	KEL_CUDA(cudaGetLastError());
 	ps->prev_is_last = true;
 	ps->cur_fresh = true;
@@ -1272,7 +1488,10 @@ extern "C" int kel_particles_reset(kel_particles *ps) {
 
 extern "C" int kel_particles_couple(kel_particles *ps, const kel_particle_params *prm) {
 	int rc = check_params(ps, prm, "kel_particles_couple");
-	if (rc || (rc = particles_couple(ps, prm, false))) return rc;
+	if (rc) return rc;
+	if (is_fplbm(prm)) rc = particles_fplbm_couple(ps, prm);
+	else rc = particles_couple(ps, prm, false);
+	if (rc) return rc;
 	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
 	return KEL_OK;
 }
@@ -1280,6 +1499,12 @@ extern "C" int kel_particles_couple(kel_particles *ps, const kel_particle_params
 extern "C" int kel_particles_gather(kel_particles *ps, const kel_particle_params *prm, float *host_cell_force) {
 	int rc = check_params(ps, prm, "kel_particles_gather");
 	if (rc) return rc;
+	if (is_fplbm(prm)) { // the coupling forces are the "force" field the couple wrote
+		if ((rc = particles_fplbm_gather(ps, prm, false))) return rc;
+		if (host_cell_force && (rc = field_to_host(ps->lat, ps->lat->force, host_cell_force, 2))) return rc;
+		KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+		return KEL_OK;
+	}
 	// HLBM: the cell force is the momentum of the last gather writing each
 	// cell, computed on the populations before the bodies move
 	if (prm->coupling == KEL_COUPLING_HLBM && host_cell_force && (rc = particles_hlbm_couple(ps, prm, true)))
@@ -1302,7 +1527,14 @@ extern "C" int kel_particles_contact(kel_particles *ps, const kel_particle_param
 
 extern "C" int kel_particles_integrate(kel_particles *ps, const kel_particle_params *prm) {
 	int rc = check_params(ps, prm, "kel_particles_integrate");
-	if (rc || (rc = particles_integrate(ps, prm))) return rc;
+	if (rc) return rc;
+	if (is_fplbm(prm)) { // Verlet with the acceleration the gather set
+		k_fplbm_integrate<<<(ps->n + 127) / 128, 128, 0, ps->lat->stream>>>(ps->d, ps->n, *prm, ps->partial, 1, 0, 1);
+		KEL_CUDA(cudaGetLastError());
+		ps->cur_fresh = false;
+	} else if ((rc = particles_integrate(ps, prm))) {
+		return rc;
+	}
 	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
 	return KEL_OK;
 }
@@ -1318,14 +1550,21 @@ extern "C" int kel_particles_stamp(kel_particles *ps, const kel_particle_params 
 }
 
 // One coupled step: reset + couple (one launch), gather, contact (adding the
-// gather sums), integrate, (HLBM: stamp,) sweep.  With PSM coupling and up to
-// CI_MAX bodies, contact and integrate are one launch that also prepares the
-// next couple's boxes, so from the second step on a step is couple, gather,
-// contact + integrate and the sweep.
+// gather sums), integrate, (HLBM: stamp,) sweep.  With PSM coupling the
+// contact starts from zero and the integrate prepares the next couple's
+// boxes, so from the second step on a step is couple, gather, contact,
+// integrate and the sweep.
 static int coupled_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
 						uint32_t flags) {
 	int rc;
-	const bool fused = prm->coupling == KEL_COUPLING_PSM && ps->n <= CI_MAX;
+	if (is_fplbm(prm)) {
+		// examples/moving_poiseulle_particles_2d_fplbm_gpu/sim.cpp:186-258: reset
+		// + particle pass (with the integration), then the sweep; its BGK
+		// boundary cases store their macros every step
+		if ((rc = particles_fplbm_couple(ps, prm)) || (rc = particles_fplbm_gather(ps, prm, true))) return rc;
+		return kel_step(ps->lat, prog, 1, flags | KEL_STEP_ALL_MACROS);
+	}
+	const bool fused = prm->coupling == KEL_COUPLING_PSM;
 	if ((rc = particles_couple(ps, prm, !fused)) || (rc = particles_gather(ps, prm, false, false))) return rc;
 	if (fused) {
 		if ((rc = particles_contact_integrate(ps, prm))) return rc;
@@ -1405,6 +1644,8 @@ extern "C" int kel_particles_step(kel_particles *ps, const kel_particle_params *
 	const bool hlbm = prm->coupling == KEL_COUPLING_HLBM;
 	if (hlbm != (prog->collision == KEL_COLL_HLBM))
 		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_step: HLBM coupling goes with the KEL_COLL_HLBM collision");
+	if (is_fplbm(prm) != (prog->collision == KEL_COLL_FPLBM))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_step: FPLBM coupling goes with the KEL_COLL_FPLBM collision");
 	kel_lattice *L = ps->lat;
 	cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
 	if (L->stream != nullptr) KEL_CUDA(cudaStreamIsCapturing(L->stream, &cap));
@@ -1414,12 +1655,13 @@ extern "C" int kel_particles_step(kel_particles *ps, const kel_particle_params *
 	const uint64_t plain = (step_flags & KEL_STEP_ALL_MACROS)
 							   ? 0
 							   : ((step_flags & KEL_STEP_WRITE_MACROS) && n_steps > 0 ? n_steps - 1 : n_steps);
-	const bool graphable = !hlbm && L->stream != nullptr && cap == cudaStreamCaptureStatusNone && L->cpt != CPT_ROWS;
+	const bool graphable = prm->coupling == KEL_COUPLING_PSM && L->stream != nullptr &&
+						   cap == cudaStreamCaptureStatusNone && L->cpt != CPT_ROWS;
 	uint64_t s = 0;
 	for (; s < n_steps; ++s) {
 		// the captured steps must find what the replayed ones leave: an
 		// incremental couple and (fused path) boxes prepared by the previous step
-		const bool steady = ps->n > CI_MAX || (ps->prev_is_last && ps->cur_fresh);
+		const bool steady = ps->prev_is_last && ps->cur_fresh;
 		if (graphable && s < plain && plain - s >= 4 && (L->t & 1u) == 0 && ps->epoch != 0 &&
 			ps->epoch == L->por_epoch && steady && L->have_ops && memcmp(&L->last_prog, prog, sizeof(*prog)) == 0)
 			break;

@@ -51,6 +51,11 @@ constexpr int CPT_ROWS = -1; // launch shape of the row pipeline (KEL_LAUNCH_ROW
 // Per-flag operation, resident in device memory (read through the read-only path).
 struct OpEntry {
 	int32_t bc, collide, east, use_profile;
+	// FPLBM programs (swept with the Guo-forcing kernels): bgk_only -- this
+	// op's cells collide with plain BGK (a boundary step precedes); no_macros
+	// -- its cells leave the density / momentum macros as the FPLBM reset
+	// wrote them
+	int32_t bgk_only, no_macros;
 	float rho;
 	float u[3];
 	float lid[27]; // moving-wall additive term 2 w_i (c_i.u_w)/cs^2, rounded like the reference
@@ -522,6 +527,14 @@ __device__ __forceinline__ bool cell_update(float (&f)[L::Q], int flag, int y, c
 		break;
 	}
 	if (__ldg(&op->collide)) {
+		if (COLL == COLL_BGK_GUO) {
+			if (__ldg(&op->bgk_only)) {
+				collide<L, COLL_BGK, EXACT>(f, p, por, Fc, rho, u);
+				return true;
+			}
+			collide<L, COLL, EXACT>(f, p, por, Fc, rho, u);
+			return !__ldg(&op->no_macros);
+		}
 		collide<L, COLL, EXACT>(f, p, por, Fc, rho, u);
 		return true;
 	}
@@ -1087,8 +1100,12 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 	const int nxp = p.nxp;
 	const int64_t cell = (static_cast<int64_t>(z) * p.ny + y) * nxp + x;
 	const int64_t oy = nxp, oz = static_cast<int64_t>(nxp) * p.ny;
+	// the lanes still running (a row's last warp may be partial); the fast
+	// paths below are chosen per warp, so that no warp runs two variants
+	const unsigned lanes = __activemask();
 	// neighbour x offsets (periodic rows wrap; nxp == nx then)
 	const bool has_xm = x > 0, has_xp = x + 1 < nxp;
+	const bool x_inner = __all_sync(lanes, has_xm && has_xp); // no lane at the row's ends
 	const int xm = has_xm ? -1 : nxp - 1;     // offset of x - 1
 	const int xp = has_xp ? 1 : -(nxp - 1);   // offset of x + 1
 	const bool ok_xm = has_xm || p.periodic;  // x - 1 exists
@@ -1107,7 +1124,7 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 	} else if (!ODD) {
 #pragma unroll
 		for (int i = 0; i < Q; ++i) f[i] = S::ld1(p.f, i * p.plane + cell, p.wshift[i]);
-	} else if (row_interior && p.idx32 && has_xm && has_xp) {
+	} else if (row_interior && p.idx32 && x_inner) {
 		// every neighbour exists: unit x offsets, no predicates
 #pragma unroll
 		for (int i = 0; i < Q; ++i)
@@ -1155,7 +1172,7 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 	}
 	float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
 	bool col;
-	if (flag < MAX_FLAGS && ((p.plain >> flag) & 1u)) { // no boundary step: straight to the collision
+	if (__all_sync(lanes, flag < MAX_FLAGS && ((p.plain >> flag) & 1u))) { // no boundary step: straight to the collision
 		collide<L, COLL, EXACT>(f, cell_ctx(p), por, Fc, rho, u);
 		col = true;
 	} else {
@@ -1206,7 +1223,7 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 			if (p.idx32) S::st1(fc, L::opp(i) * pl32, f[i], p.wshift[i]);
 			else S::st1(p.f, static_cast<int64_t>(L::opp(i)) * p.plane + cell, f[i], p.wshift[i]);
 		}
-	} else if (row_interior && p.idx32 && has_xm && has_xp) {
+	} else if (row_interior && p.idx32 && x_inner) {
 		// every destination exists and no source lies outside: no predicates
 #pragma unroll
 		for (int i = 0; i < Q; ++i)

@@ -95,6 +95,8 @@ def unet_input(mask, u_max, tau):
                     run = 0
             h3[x] += run ** 3
         R = np.cumsum((1.0 / np.maximum(openf, 0.125) ** 3)[::-1])[::-1] / W
+        S = np.cumsum((1.0 / np.maximum(h3, 1.0))[::-1])[::-1]  # lubrication pressure, suffix sums
+        PL = S / S[0]
         out[b, :, :, 0] = m
         out[b, :, :, 1] = u_max[b] / 0.08
         out[b, :, :, 2] = (tau[b] - 0.55) / 0.45
@@ -119,5 +121,6 @@ def unet_input(mask, u_max, tau):
                     out[b, yy, x, 7] = h / hin
                     out[b, yy, x, 8] = shape
                     out[b, yy, x, 9] = 0.5 * min(hin * h * h / max(h3[x], 1.0) * shape, 8.0)
+                    out[b, yy, x, 10] = PL[x]
                 y += 1
     return out
