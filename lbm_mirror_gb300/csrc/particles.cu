@@ -189,7 +189,18 @@ struct Cand {
 	// squared-distance limits of the exact shortcuts (see body_factor),
 	// formed once per body with the same operations
 	double lim_in2, lim_out2;
+	// FP32 screen: the centre's nearest lattice point, the offset of that
+	// point from the centre, and the limits widened by SCREEN_MARGIN
+	int ic[3];
+	float fr[3];
+	float s_in, s_out;
 };
+
+// Squared-distance margin of the FP32 screen: far above its own error (the
+// offset of a cell from a body is formed from an exact integer part and a
+// fraction of at most 1/2, so |s2 - s2_float| stays below ~1e-4 for offsets
+// up to ~100 cells) and far below the band the shortcuts leave to FP64.
+constexpr float SCREEN_MARGIN = 1e-2f;
 
 // The shortcut limits of body_factor for a body of radius R.
 __device__ inline void cand_limits(Cand &c, int sub, double reach, double eps) {
@@ -203,6 +214,12 @@ __device__ inline void cand_limits(Cand &c, int sub, double reach, double eps) {
 		c.lim_in2 = lo > 0.0 ? lo * lo - 1e-6 : -1.0;
 		c.lim_out2 = hi * hi + 1e-6;
 	}
+	for (int d = 0; d < 3; ++d) {
+		c.ic[d] = (int)llround(c.X[d]);
+		c.fr[d] = (float)((double)c.ic[d] - c.X[d]);
+	}
+	c.s_out = (float)c.lim_out2 + SCREEN_MARGIN;
+	c.s_in = c.lim_in2 > 0.0 ? (float)c.lim_in2 - SCREEN_MARGIN : -1.0f;
 }
 
 // Body q's factor on the porosity of cell (x, y, z), multiplied into por
@@ -216,7 +233,12 @@ __device__ inline void cand_limits(Cand &c, int sub, double reach, double eps) {
 //   ramp mode: |r|^2 below (R - eps/2)^2 - 1e-6 gives 0, above
 //     (R + eps/2)^2 + 1e-6 gives 1.
 // The margins are far above the FP64 rounding of the coordinates, so the
-// factors equal those of the full computation bit for bit.
+// factors equal those of the full computation bit for bit.  An FP32 screen
+// decides first the cells whose squared distance lies SCREEN_MARGIN beyond
+// either limit (the same decision the FP64 test takes there; a cell that
+// deep inside has its nearest image in the body's box), so that only cells
+// near the limits pay for FP64, which issues at a small fraction of the FP32
+// rate on this GPU.
 __device__ inline void body_factor(const PView &v, int x, int y, int z, const Cand &c, int sub, double reach,
 								   double eps, double &por, bool &touched) {
 	const BodyBox &q = c.box;
@@ -228,6 +250,24 @@ __device__ inline void body_factor(const PView &v, int x, int y, int z, const Ca
 	const bool inp = v.periodic && x + v.nx >= q.a[0] && x + v.nx < q.b[0];
 	if (!(in0 || inm || inp)) return;
 	touched = true;
+	{
+		int dx = x - c.ic[0];
+		if (v.periodic) {
+			if (dx > v.nx / 2) dx -= v.nx;
+			else if (dx < -(v.nx / 2)) dx += v.nx;
+		}
+		const float r0 = __fadd_rn((float)dx, c.fr[0]), r1 = __fadd_rn((float)(y - c.ic[1]), c.fr[1]);
+		float s2f = __fadd_rn(__fmul_rn(r0, r0), __fmul_rn(r1, r1));
+		if (v.D == 3) {
+			const float r2 = __fadd_rn((float)(z - c.ic[2]), c.fr[2]);
+			s2f = __fadd_rn(s2f, __fmul_rn(r2, r2));
+		}
+		if (s2f > c.s_out) return; // factor 1
+		if (s2f < c.s_in) {        // factor 0
+			por = por * 0.0;
+			return;
+		}
+	}
 	const double X0 = c.X[0], X1 = c.X[1], X2 = c.X[2], R = c.R;
 	double rel[3] = {rel_coord((double)x, X0, v.periodic, v.nx), (double)y - X1, v.D == 3 ? (double)z - X2 : 0.0};
 	const double xi = X0 + rel[0];
@@ -257,8 +297,9 @@ __device__ inline void body_factor(const PView &v, int x, int y, int z, const Ca
 
 __device__ inline double subcell_reach(int D) { return D == 3 ? 0.6495190528383290 : 0.5303300858899106; } // 3 sqrt(D) / 8
 
-// Ordered compaction of the bodies [c0, c0 + TT) for which hit is true (one
-// thread per body, TT threads) into cand[0 .. *ncand).
+// Ordered compaction of the bodies [c0, c0 + NT) for which hit is true (one
+// thread per body, NT threads) into cand[0 .. *ncand).
+template <int NT>
 __device__ inline void compact_cands(bool hit, int pi, const BodyBox &bb, const kel_particle_state *P, Cand *cand,
 									 int *warp_count, int *ncand, int sub, double reach, double eps) {
 	const int tid = threadIdx.x + threadIdx.y * blockDim.x;
@@ -267,7 +308,7 @@ __device__ inline void compact_cands(bool hit, int pi, const BodyBox &bb, const 
 	__syncthreads();
 	if (tid == 0) {
 		int s = 0;
-		for (int w = 0; w < TT / 32; ++w) {
+		for (int w = 0; w < NT / 32; ++w) {
 			const int c = warp_count[w];
 			warp_count[w] = s;
 			s += c;
@@ -312,7 +353,7 @@ __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state
 				xs = xs || (bb.a[0] < x0 + TX - v.nx && bb.b[0] > x0 - v.nx) || (bb.a[0] < x0 + TX + v.nx && bb.b[0] > x0 + v.nx);
 			hit = yz && xs;
 		}
-		compact_cands(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
+		compact_cands<TT>(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
 		if (x < v.nx && y < v.ny)
 			for (int k = 0; k < ncand; ++k) body_factor(v, x, y, z, cand[k], sub, reach, eps, por, touched);
 		__syncthreads();
@@ -335,6 +376,7 @@ __device__ inline bool boxes_touch(const BodyBox &p, const BodyBox &q, const PVi
 }
 
 constexpr int RC_CPT = 1; // cells per thread and pass of the region couple (more blocks per body instead)
+constexpr int RT = 128;   // threads per block of the region couple
 
 // Incremental couple pass.  Only cells inside some body's box can have a
 // porosity other than 1, so after a couple whose boxes were prev[], the new
@@ -344,10 +386,10 @@ constexpr int RC_CPT = 1; // cells per thread and pass of the region couple (mor
 // bodies (index order) whose current box holds it, or 1 when none does --
 // the same value the full pass writes.  A cell in several bodies' regions is
 // written by several blocks with that same value.
-__global__ void __launch_bounds__(TT) k_couple_regions(PView v, const kel_particle_state *P, const BodyBox *cur,
+__global__ void __launch_bounds__(RT) k_couple_regions(PView v, const kel_particle_state *P, const BodyBox *cur,
 													   const BodyBox *prev, int np, int mode, double eps) {
-	__shared__ Cand cand[TT];
-	__shared__ int warp_count[TT / 32];
+	__shared__ Cand cand[RT];
+	__shared__ int warp_count[RT / 32];
 	__shared__ int ncand;
 	const int tid = threadIdx.x;
 	const int b = blockIdx.x;
@@ -357,13 +399,13 @@ __global__ void __launch_bounds__(TT) k_couple_regions(PView v, const kel_partic
 	const int64_t n0 = box_cells(A, v.D), n1 = same ? 0 : box_cells(B, v.D);
 	const int sub = mode == KEL_POROSITY_SUBCELL;
 	const double reach = sub ? subcell_reach(v.D) : 0.0;
-	for (int64_t base = (int64_t)blockIdx.y * TT * RC_CPT; base < n0 + n1; base += (int64_t)gridDim.y * TT * RC_CPT) {
+	for (int64_t base = (int64_t)blockIdx.y * RT * RC_CPT; base < n0 + n1; base += (int64_t)gridDim.y * RT * RC_CPT) {
 		int cx[RC_CPT], cy[RC_CPT], cz[RC_CPT];
 		bool ok[RC_CPT], touched[RC_CPT];
 		double por[RC_CPT];
 #pragma unroll
 		for (int j = 0; j < RC_CPT; ++j) {
-			const int64_t idx = base + (int64_t)j * TT + tid;
+			const int64_t idx = base + (int64_t)j * RT + tid;
 			ok[j] = idx < n0 + n1;
 			touched[j] = false;
 			por[j] = 1.0;
@@ -378,7 +420,7 @@ __global__ void __launch_bounds__(TT) k_couple_regions(PView v, const kel_partic
 			if (v.periodic) ix = ((ix % v.nx) + v.nx) % v.nx;
 			cx[j] = ix;
 		}
-		for (int c0 = 0; c0 < np; c0 += TT) {
+		for (int c0 = 0; c0 < np; c0 += RT) {
 			bool hit = false;
 			const int pi = c0 + tid;
 			BodyBox bb;
@@ -386,7 +428,7 @@ __global__ void __launch_bounds__(TT) k_couple_regions(PView v, const kel_partic
 				bb = cur[pi];
 				hit = boxes_touch(bb, A, v) || (!same && boxes_touch(bb, B, v));
 			}
-			compact_cands(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
+			compact_cands<RT>(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
 #pragma unroll
 			for (int j = 0; j < RC_CPT; ++j)
 				if (ok[j])
@@ -422,7 +464,7 @@ __device__ inline float pop_post(const PView &v, int x, int y, int z, int i) {
 	return __half2float(static_cast<const __half *>(v.f)[idx]) + v.wshift[i];
 }
 
-constexpr int GT = 128;
+constexpr int GT = 64; // threads per gather block: more blocks per body spread the FP64 sums over more SMs
 
 // PSM (HLBM false): psm.hpp:101-446, the porosity field the couple pass
 // wrote, cell force = momentum x (1 - porosity).  HLBM: hlbm.hpp:119-260,
@@ -1200,7 +1242,7 @@ static int gather_blocks(const kel_particles *ps) {
 
 // Blocks per body of the region couple (two boxes, RC_CPT cells per thread).
 static int couple_blocks(const kel_particles *ps) {
-	const int64_t g = (2 * box_cells_max(ps) + TT * RC_CPT - 1) / (TT * RC_CPT);
+	const int64_t g = (2 * box_cells_max(ps) + RT * RC_CPT - 1) / (RT * RC_CPT);
 	return (int)(g < 1 ? 1 : (g > 64 ? 64 : g));
 }
 
@@ -1328,7 +1370,7 @@ static int particles_couple(kel_particles *ps, const kel_particle_params *prm, b
 	ps->cur_fresh = true;
 	ps->cur_sub = sub;
 	if (incremental)
-		k_couple_regions<<<dim3((unsigned)ps->n, (unsigned)couple_blocks(ps)), TT, 0, L->stream>>>(
+		k_couple_regions<<<dim3((unsigned)ps->n, (unsigned)couple_blocks(ps)), RT, 0, L->stream>>>(
 			v, ps->d, cur_boxes(ps), prev_boxes(ps), ps->n, prm->porosity_mode, prm->eps);
 	else
 		k_couple<<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, cur_boxes(ps), ps->n, prm->porosity_mode,
