@@ -513,9 +513,9 @@ def run_particles(args, rank, world):
             "roofline": {"bound": "hbm", "achieved": bpu * cells / (sweep_ms / 1e3) / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": bpu * cells / (sweep_ms / 1e3) / 1e9 / peak, "traffic": None,
                          "peak_source": src, "bytes_per_update": bpu, "kernel": "PSM+Guo sweep"},
-            "gpu_launches": args.steps * 6,
-            "launches_per_step": "reset+boxes, couple (bodies' boxes only), gather (blocks per body), "
-                                 "contact (+ gather sums), integrate, sweep; graph-replayed in pairs of steps"}
+            "gpu_launches": args.steps * 3,
+            "launches_per_step": "couple + gather (the bodies' boxes only, blocks per body), contact + integrate "
+                                 "(one warp per body, beside the sweep), sweep; graph-replayed in pairs of steps"}
     if rank == 0:
         print(json.dumps(line))
 

@@ -43,10 +43,12 @@ struct kel_particles {
 	kel_lattice *lat = nullptr;
 	int n = 0;
 	kel_particle_state *d = nullptr; // device copy of the bodies
+	kel_particle_state *d_alt = nullptr; // the coupled step's second body buffer (swapped with d every step)
 	float *cell_force = nullptr;     // D planes, allocated on first request
 	void *boxes = nullptr;           // per-body integer boxes: current [0, n), previous couple [n, 2n)
 	double *partial = nullptr;       // gather partial sums, n x gather_g x 6
 	int partial_cap = 0;             // blocks per body the partial buffer holds
+	int gather_g = 1;                // blocks per body of the last gather (the partials' layout)
 	double max_radius = 0.0;         // largest radius of the uploaded bodies (sizes the launches)
 	// value of lat->por_epoch after this set's last PSM couple (0: none); the
 	// incremental couple needs the field to be untouched since then
@@ -58,6 +60,9 @@ struct kel_particles {
 	bool prev_is_last = false, cur_fresh = false;
 	int cur_sub = 0;
 	cudaGraphExec_t graph = nullptr; // two coupled steps from an even time step
+	// fork / join of the captured steps: contact + integrate beside the sweep
+	cudaStream_t side = nullptr;
+	cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 	ParticleGraphKey key;
 };
 
@@ -127,17 +132,24 @@ __device__ inline double ramp(double s, double rad, double eps) {
 	return c * c;
 }
 
-// Solid fraction by 4^D point sampling of the cell [x-1/2, x+1/2]^D.
-__device__ inline double subcell_porosity(int D, const double *x, const double *X, double rad) {
-	const double r2 = rad * rad;
+// Solid fraction by 4^D point sampling of the cell [x-1/2, x+1/2]^D, in
+// FP32: r is the cell centre's offset from the body centre formed as an
+// exact integer part plus the body's fraction (see Cand), the sample points
+// lie at r + (2 a - 3) / 8 per axis, and a sample is inside when its squared
+// distance (summed in axis order) is at most R^2, all rounded to nearest.
+__device__ inline double subcell_porosity(int D, const float *r, float rad) {
+	const float r2 = __fmul_rn(rad, rad);
 	int inside = 0;
 	for (int a = 0; a < 4; ++a)
 		for (int b = 0; b < 4; ++b)
 			for (int g = 0; g < (D == 3 ? 4 : 1); ++g) {
-				const double px = x[0] + (2 * a - 3) / 8.0 - X[0];
-				const double py = x[1] + (2 * b - 3) / 8.0 - X[1];
-				const double pz = D == 3 ? x[2] + (2 * g - 3) / 8.0 - X[2] : 0.0;
-				const double d2 = px * px + py * py + pz * pz;
+				const float px = __fadd_rn(r[0], (float)(2 * a - 3) * 0.125f);
+				const float py = __fadd_rn(r[1], (float)(2 * b - 3) * 0.125f);
+				float d2 = __fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py));
+				if (D == 3) {
+					const float pz = __fadd_rn(r[2], (float)(2 * g - 3) * 0.125f);
+					d2 = __fadd_rn(d2, __fmul_rn(pz, pz));
+				}
 				if (d2 <= r2) ++inside;
 			}
 	return 1.0 - (double)inside / (double)(D == 3 ? 64 : 16);
@@ -206,7 +218,8 @@ constexpr float SCREEN_MARGIN = 1e-2f;
 __device__ inline void cand_limits(Cand &c, int sub, double reach, double eps) {
 	const double R = c.R;
 	if (sub) {
-		const double out_r = R + reach + 1e-6, in_r = R - reach - 1e-6;
+		// margin 1e-3: far above the FP32 rounding of the sampled distances
+		const double out_r = R + reach + 1e-3, in_r = R - reach - 1e-3;
 		c.lim_out2 = out_r * out_r;
 		c.lim_in2 = in_r > 0.0 ? in_r * in_r : -1.0;
 	} else {
@@ -227,9 +240,9 @@ __device__ inline void cand_limits(Cand &c, int sub, double reach, double eps) {
 // it).  A cell none of whose images lies in the body's box is left alone.
 // Two exact shortcuts skip the FP64 sampling:
 //   sub-cell mode: the 16 (64) samples lie within 3 sqrt(D) / 8 of the cell
-//     centre, so a centre farther than R + that radius (+ 1e-6) from the body
+//     centre, so a centre farther than R + that radius (+ 1e-3) from the body
 //     centre has no sample inside (factor 1) and one nearer than R - radius
-//     (- 1e-6) has all inside (factor 0);
+//     (- 1e-3) has all inside (factor 0);
 //   ramp mode: |r|^2 below (R - eps/2)^2 - 1e-6 gives 0, above
 //     (R + eps/2)^2 + 1e-6 gives 1.
 // The margins are far above the FP64 rounding of the coordinates, so the
@@ -250,18 +263,20 @@ __device__ inline void body_factor(const PView &v, int x, int y, int z, const Ca
 	const bool inp = v.periodic && x + v.nx >= q.a[0] && x + v.nx < q.b[0];
 	if (!(in0 || inm || inp)) return;
 	touched = true;
+	// the cell's offset from the body in FP32: integer part (nearest image
+	// when periodic) plus the body's fraction
+	float rf[3];
 	{
 		int dx = x - c.ic[0];
 		if (v.periodic) {
 			if (dx > v.nx / 2) dx -= v.nx;
 			else if (dx < -(v.nx / 2)) dx += v.nx;
 		}
-		const float r0 = __fadd_rn((float)dx, c.fr[0]), r1 = __fadd_rn((float)(y - c.ic[1]), c.fr[1]);
-		float s2f = __fadd_rn(__fmul_rn(r0, r0), __fmul_rn(r1, r1));
-		if (v.D == 3) {
-			const float r2 = __fadd_rn((float)(z - c.ic[2]), c.fr[2]);
-			s2f = __fadd_rn(s2f, __fmul_rn(r2, r2));
-		}
+		rf[0] = __fadd_rn((float)dx, c.fr[0]);
+		rf[1] = __fadd_rn((float)(y - c.ic[1]), c.fr[1]);
+		rf[2] = v.D == 3 ? __fadd_rn((float)(z - c.ic[2]), c.fr[2]) : 0.f;
+		float s2f = __fadd_rn(__fmul_rn(rf[0], rf[0]), __fmul_rn(rf[1], rf[1]));
+		if (v.D == 3) s2f = __fadd_rn(s2f, __fmul_rn(rf[2], rf[2]));
 		if (s2f > c.s_out) return; // factor 1
 		if (s2f < c.s_in) {        // factor 0
 			por = por * 0.0;
@@ -282,9 +297,7 @@ __device__ inline void body_factor(const PView &v, int x, int y, int z, const Ca
 		} else if (s2 < c.lim_in2) {
 			pp = 0.0;
 		} else {
-			const double xs[3] = {xi, (double)y, (double)z};
-			const double Xs[3] = {X0, X1, X2};
-			pp = subcell_porosity(v.D, xs, Xs, R);
+			pp = subcell_porosity(v.D, rf, (float)R);
 		}
 	} else {
 		if (s2 < c.lim_in2) pp = 0.0;
@@ -567,6 +580,118 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, const kel_particle_state
 		double tot = 0.0;
 		for (int w = 0; w < GT / 32; ++w) tot += part[w][threadIdx.x];
 		partial[((int64_t)blockIdx.x * gridDim.y + blockIdx.y) * 6 + threadIdx.x] = tot;
+	}
+}
+
+// Incremental couple and PSM gather in one pass (the coupled step).  Block
+// (b, g) takes the cells g, g + G, ... (blocks of RT) of body b's current box
+// and, where it moved, its previous box, as k_couple_regions does: each cell
+// gets the product of the candidates' factors, written to the porosity field.
+// Cells of the current box -- body b's gather box -- then add their momentum
+// exchange to the block's FP64 sums, exactly as k_gather computes it from the
+// field (the porosity is the same value, computed here instead of read).
+// The sums go to partial[(b * G + g) * 6 ..] in k_gather's fixed order.
+template <class L, int STORE>
+__global__ void __launch_bounds__(RT) k_couple_gather(PView v, const kel_particle_state *P, const BodyBox *cur,
+													  const BodyBox *prev, int np, int mode, double eps, int steps,
+													  double *partial) {
+	constexpr int D = L::D;
+	__shared__ Cand cand[RT];
+	__shared__ int warp_count[RT / 32];
+	__shared__ int ncand;
+	__shared__ double part[RT / 32][6];
+	const int tid = threadIdx.x;
+	const int b = blockIdx.x;
+	const kel_particle_state &p = P[b];
+	const BodyBox A = cur[b], B = prev[b];
+	const bool same = A.a[0] == B.a[0] && A.b[0] == B.b[0] && A.a[1] == B.a[1] && A.b[1] == B.b[1] &&
+					  (D == 2 || (A.a[2] == B.a[2] && A.b[2] == B.b[2]));
+	const int64_t n0 = box_cells(A, D), n1 = same ? 0 : box_cells(B, D);
+	const int sub = mode == KEL_POROSITY_SUBCELL;
+	const double reach = sub ? subcell_reach(D) : 0.0;
+	// psm.hpp:178-184: u_p = (X - X_old) / (1 / sub_steps), raw sub_steps
+	const double ts = 1.0 / (double)steps;
+	double vp[3] = {0.0, 0.0, 0.0};
+	for (int k = 0; k < D; ++k) vp[k] = (p.position[k] - p.position_old[k]) / ts;
+	float upe[L::Q];
+#pragma unroll
+	for (int i = 1; i < L::Q; ++i) {
+		double upe_d = 0.0;
+		upe_d = upe_d + (double)L::cx(i) * vp[0];
+		upe_d = upe_d + (double)L::cy(i) * vp[1];
+		if (D == 3) upe_d = upe_d + (double)L::cz(i) * vp[2];
+		upe[i] = (float)upe_d;
+	}
+	double acc[6] = {0, 0, 0, 0, 0, 0};
+	for (int64_t base = (int64_t)blockIdx.y * RT; base < n0 + n1; base += (int64_t)gridDim.y * RT) {
+		const int64_t idx = base + tid;
+		const bool ok = idx < n0 + n1;
+		bool touched = false;
+		double por = 1.0;
+		int x = 0, iy = 0, iz = 0;
+		if (ok) {
+			const BodyBox &q = idx < n0 ? A : B;
+			const int64_t k = idx < n0 ? idx : idx - n0;
+			const int64_t ex = q.b[0] - q.a[0], ey = q.b[1] - q.a[1];
+			int ix = q.a[0] + (int)(k % ex);
+			iy = q.a[1] + (int)((k / ex) % ey);
+			iz = D == 3 ? q.a[2] + (int)(k / (ex * ey)) : 0;
+			if (v.periodic) ix = ((ix % v.nx) + v.nx) % v.nx;
+			x = ix;
+		}
+		for (int c0 = 0; c0 < np; c0 += RT) {
+			bool hit = false;
+			const int pi = c0 + tid;
+			BodyBox bb;
+			if (pi < np) {
+				bb = cur[pi];
+				hit = boxes_touch(bb, A, v) || (!same && boxes_touch(bb, B, v));
+			}
+			compact_cands<RT>(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
+			if (ok)
+				for (int k = 0; k < ncand; ++k) body_factor(v, x, iy, iz, cand[k], sub, reach, eps, por, touched);
+			__syncthreads();
+		}
+		if (!ok) continue;
+		const int64_t pc = ((int64_t)iz * v.ny + iy) * v.nxp + x;
+		const float porf = touched ? (float)por : 1.0f;
+		v.por[pc] = porf;
+		if (idx >= n0 || porf >= 1.0f) continue; // not in the gather box, or fluid
+		const double r[3] = {rel_coord((double)x, p.position[0], v.periodic, v.nx), (double)iy - p.position[1],
+							 D == 3 ? (double)iz - p.position[2] : 0.0};
+		float mom[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+		for (int i = 1; i < L::Q; ++i) {
+			const float fi = pop_post<L, STORE>(v, x, iy, iz, i);
+			const float fo = pop_post<L, STORE>(v, x + L::cx(i), iy + L::cy(i), iz + L::cz(i), L::opp(i));
+			const float da = __fadd_rn(__fmul_rn(fi, __fsub_rn(1.0f, upe[i])), __fmul_rn(fo, __fadd_rn(1.0f, upe[i])));
+			mom[0] = __fadd_rn(mom[0], __fmul_rn((float)L::cx(i), da));
+			mom[1] = __fadd_rn(mom[1], __fmul_rn((float)L::cy(i), da));
+			if (D == 3) mom[2] = __fadd_rn(mom[2], __fmul_rn((float)L::cz(i), da));
+		}
+		const float flip = __fsub_rn(1.0f, porf);
+		double F[3] = {0.0, 0.0, 0.0};
+		for (int d = 0; d < D; ++d) F[d] = (double)__fmul_rn(mom[d], flip);
+		for (int d = 0; d < D; ++d) acc[d] -= F[d];
+		if (D == 2) {
+			acc[3] -= r[0] * F[1] - r[1] * F[0];
+		} else {
+			acc[3] -= r[1] * F[2] - r[2] * F[1];
+			acc[4] -= r[2] * F[0] - r[0] * F[2];
+			acc[5] -= r[0] * F[1] - r[1] * F[0];
+		}
+	}
+#pragma unroll
+	for (int q = 0; q < 6; ++q) {
+		double sum = acc[q];
+		for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+		if ((tid & 31) == 0) part[tid >> 5][q] = sum;
+	}
+	__syncthreads();
+	if (tid < 6) {
+		double tot = 0.0;
+		for (int w = 0; w < RT / 32; ++w) tot += part[w][tid];
+		partial[((int64_t)b * gridDim.y + blockIdx.y) * 6 + tid] = tot;
 	}
 }
 
@@ -1018,7 +1143,7 @@ __device__ inline bool pair_response(const kel_particle_state &self, const kel_p
 // exactly as k_gather_finish would add them.  fs / hs: this warp's scratch.
 __device__ inline void contact_one(kel_particle_state *P, int s, int np, int D, const kel_particle_params &prm, int nx,
 								   int ny, int nz, int periodic, const double *partial, int G, bool zero_start,
-								   double (*fs)[4], int *hs) {
+								   double (*fs)[4], int *hs, kel_particle_state *out = nullptr) {
 	const int lane = threadIdx.x & 31;
 	const double steps = (double)(prm.sub_steps == 0 ? 1 : prm.sub_steps);
 	const double Lx = (double)nx;
@@ -1081,15 +1206,16 @@ __device__ inline void contact_one(kel_particle_state *P, int s, int np, int D, 
 			if (D == 2) torque0 = torque0 + t[0];
 		}
 	}
-	// only lane 0 of this warp writes body s; the other warps read its
-	// position fields only
-	P[s].force[0] = force[0];
-	P[s].force[1] = force[1];
-	P[s].force[2] = force[2];
-	if (D == 2 || partial || zero_start) P[s].torque[0] = torque0;
+	// only lane 0 of this warp writes body s (to P, or with out to *out, a
+	// copy of the body); the other warps read its position fields only
+	kel_particle_state &w = out ? *out : P[s];
+	w.force[0] = force[0];
+	w.force[1] = force[1];
+	w.force[2] = force[2];
+	if (D == 2 || partial || zero_start) w.torque[0] = torque0;
 	if (D == 3 && (partial || zero_start)) {
-		P[s].torque[1] = torque12[0];
-		P[s].torque[2] = torque12[1];
+		w.torque[1] = torque12[0];
+		w.torque[2] = torque12[1];
 	}
 }
 
@@ -1105,9 +1231,19 @@ __global__ void k_contact(kel_particle_state *P, int np, int D, kel_particle_par
 }
 
 // integrate_particle + verlet_step_lambda (integrate.hpp:45-83, particle.hpp:171-211)
+__device__ inline void integrate_state(kel_particle_state &q, int D, const kel_particle_params &prm, int nx,
+									   int periodic);
+
 __device__ inline void integrate_one(kel_particle_state *P, int pi, int D, const kel_particle_params &prm, int nx,
 									 int periodic) {
 	kel_particle_state q = P[pi];
+	integrate_state(q, D, prm, nx, periodic);
+	P[pi] = q;
+}
+
+// integrate_particle + verlet_step_lambda on a body held by the caller
+__device__ inline void integrate_state(kel_particle_state &q, int D, const kel_particle_params &prm, int nx,
+									   int periodic) {
 	const int steps = prm.sub_steps == 0 ? 1 : prm.sub_steps;
 	const double ts = 1.0 / (double)steps;
 	for (int k = 0; k < D; ++k) q.acceleration[k] = q.force[k] / q.mass + prm.body_acceleration[k];
@@ -1136,7 +1272,6 @@ __device__ inline void integrate_one(kel_particle_state *P, int pi, int D, const
 			q.position_old[0] += L;
 		}
 	}
-	P[pi] = q;
 }
 
 __global__ void k_integrate(kel_particle_state *P, int np, int D, kel_particle_params prm, int nx, int periodic) {
@@ -1145,34 +1280,45 @@ __global__ void k_integrate(kel_particle_state *P, int np, int D, kel_particle_p
 	integrate_one(P, pi, D, prm, nx, periodic);
 }
 
-// Contact of the coupled step: one warp per block and one block per body, so
-// that the FP64 pair work (issued at a small fraction of the FP32 rate on
-// this GPU) spreads over as many multiprocessors as there are bodies.  The
-// sums start from zero and take the gather partials first.
-__global__ void __launch_bounds__(32) k_contact_step(kel_particle_state *P, int np, int D, kel_particle_params prm,
-													 int nx, int ny, int nz, int periodic, const double *partial, int G) {
+// Contact and integrate of the coupled step in one launch, one warp (block)
+// per body: the contact of body s reads every body's state in P_in; lane 0
+// then integrates a copy of body s with that force and writes it to P_out
+// (the next step's state, so that no block reads a body another has already
+// moved), and prepares the next couple's boxes.
+__global__ void __launch_bounds__(32) k_contact_integrate(const kel_particle_state *P_in, kel_particle_state *P_out,
+														  PView v, kel_particle_params prm, const double *partial,
+														  int G, BodyBox *cur, BodyBox *prev, int sub) {
 	__shared__ double fs[32][4];
 	__shared__ int hs[32];
-	contact_one(P, blockIdx.x, np, D, prm, nx, ny, nz, periodic, partial, G, true, fs, hs);
-}
-
-// Integrate of the coupled step, one thread per body; then, for the next
-// step's couple, the body's box moves to prev and the box of its new
-// position goes to cur (the shift k_pre would do).
-__global__ void k_integrate_boxes(PView v, kel_particle_state *P, int np, kel_particle_params prm, BodyBox *cur,
-								  BodyBox *prev, int sub) {
-	const int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= np) return;
-	integrate_one(P, i, v.D, prm, v.nx, v.periodic);
+	const int s = blockIdx.x, np = (int)gridDim.x;
+	kel_particle_state q;
+	contact_one(const_cast<kel_particle_state *>(P_in), s, np, v.D, prm, v.nx, v.ny, v.nz, v.periodic, partial, G, true,
+				fs, hs, &q);
+	if ((threadIdx.x & 31) != 0) return;
+	// contact_one set q's force and torque; the rest of the body from P_in
+	const kel_particle_state &o = P_in[s];
+	const double f0 = q.force[0], f1 = q.force[1], f2 = q.force[2];
+	const double t0 = q.torque[0], t1 = q.torque[1], t2 = q.torque[2];
+	q = o;
+	q.force[0] = f0;
+	q.force[1] = f1;
+	q.force[2] = f2;
+	q.torque[0] = t0;
+	if (v.D == 3) {
+		q.torque[1] = t1;
+		q.torque[2] = t2;
+	}
+	integrate_state(q, v.D, prm, v.nx, v.periodic);
+	P_out[s] = q;
 	int64_t a[3], b[3];
-	body_aabb(v.D, P[i], v.nx, v.ny, v.nz, v.periodic, sub, a, b);
+	body_aabb(v.D, q, v.nx, v.ny, v.nz, v.periodic, sub, a, b);
 	BodyBox r;
 	for (int k = 0; k < 3; ++k) {
 		r.a[k] = (int)a[k];
 		r.b[k] = (int)b[k];
 	}
-	prev[i] = cur[i];
-	cur[i] = r;
+	prev[s] = cur[s];
+	cur[s] = r;
 }
 
 PView make_view(kel_lattice *L) {
@@ -1253,9 +1399,11 @@ extern "C" int kel_particles_create(kel_lattice *lat, int32_t count, kel_particl
 	ps->lat = lat;
 	ps->n = count;
 	cudaError_t e = cudaMalloc(&ps->d, sizeof(kel_particle_state) * count);
+	if (e == cudaSuccess) e = cudaMalloc(&ps->d_alt, sizeof(kel_particle_state) * count);
 	if (e == cudaSuccess) e = cudaMalloc(&ps->boxes, sizeof(BodyBox) * 2 * (size_t)count);
 	if (e != cudaSuccess) {
 		cudaFree(ps->d);
+		cudaFree(ps->d_alt);
 		delete ps;
 		return fail(e == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA, "kel_particles_create: %s",
 					cudaGetErrorString(e));
@@ -1264,6 +1412,7 @@ extern "C" int kel_particles_create(kel_lattice *lat, int32_t count, kel_particl
 	int rc = ensure_field(lat, &lat->por, lat->plane, 1.0f);
 	if (rc) {
 		cudaFree(ps->d);
+		cudaFree(ps->d_alt);
 		cudaFree(ps->boxes);
 		delete ps;
 		return rc;
@@ -1276,7 +1425,11 @@ extern "C" int kel_particles_destroy(kel_particles *ps) {
 	if (!ps) return KEL_OK;
 	cudaStreamSynchronize(ps->lat->stream);
 	if (ps->graph) cudaGraphExecDestroy(ps->graph);
+	if (ps->side) cudaStreamDestroy(ps->side);
+	if (ps->ev_fork) cudaEventDestroy(ps->ev_fork);
+	if (ps->ev_join) cudaEventDestroy(ps->ev_join);
 	cudaFree(ps->d);
+	cudaFree(ps->d_alt);
 	cudaFree(ps->cell_force);
 	cudaFree(ps->boxes);
 	cudaFree(ps->partial);
@@ -1414,6 +1567,7 @@ static int particles_gather(kel_particles *ps, const kel_particle_params *prm, b
 	const int G = gather_blocks(ps);
 	int rc;
 	if ((rc = ensure_partials(ps, G))) return rc;
+	ps->gather_g = G;
 	if (prm->coupling == KEL_COUPLING_HLBM) { // D2Q9 (checked); the couple pass wrote the cell forces
 		const dim3 grid((unsigned)ps->n, (unsigned)G);
 		if (L->desc.storage == KEL_STORAGE_FP32)
@@ -1474,6 +1628,7 @@ static int particles_fplbm_gather(kel_particles *ps, const kel_particle_params *
 	const int G = gather_blocks(ps);
 	int rc;
 	if ((rc = ensure_partials(ps, G))) return rc;
+	ps->gather_g = G;
 	const int own = prm->coupling == KEL_COUPLING_FPLBM_OWN;
 	k_fplbm_sums<<<dim3((unsigned)ps->n, (unsigned)G), GT, 0, L->stream>>>(make_view(L), ps->d, cur_boxes(ps), own,
 																		   (double)prm->sub_steps, ps->partial);
@@ -1489,7 +1644,7 @@ static int particles_contact(kel_particles *ps, const kel_particle_params *prm, 
 	kel_lattice *L = ps->lat;
 	k_contact<<<(ps->n + 3) / 4, 128, 0, L->stream>>>(ps->d, ps->n, L->d.D, *prm, (int)L->desc.nx, (int)L->desc.ny,
 													   (int)L->desc.nz, (L->desc.flags & KEL_LATTICE_PERIODIC_X) ? 1 : 0,
-													   fold ? ps->partial : nullptr, gather_blocks(ps));
+													   fold ? ps->partial : nullptr, ps->gather_g);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
@@ -1503,17 +1658,54 @@ static int particles_integrate(kel_particles *ps, const kel_particle_params *prm
 	return KEL_OK;
 }
 
+template <class Lc, int STORE>
+static void launch_couple_gather(const PView &v, kel_particles *ps, const kel_particle_params *prm, int G) {
+	k_couple_gather<Lc, STORE><<<dim3((unsigned)ps->n, (unsigned)G), RT, 0, ps->lat->stream>>>(
+		v, ps->d, cur_boxes(ps), prev_boxes(ps), ps->n, prm->porosity_mode, prm->eps, prm->sub_steps, ps->partial);
+}
+
+// Couple and gather of a coupled PSM step in one launch, when the couple is
+// incremental and the boxes are prepared (*done); otherwise nothing happens.
+static int particles_couple_gather(kel_particles *ps, const kel_particle_params *prm, bool *done) {
+	*done = false;
+	kel_lattice *L = ps->lat;
+	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
+	const bool incremental = ps->epoch != 0 && ps->epoch == L->por_epoch;
+	if (!(incremental && ps->prev_is_last && ps->cur_fresh && ps->cur_sub == sub)) return KEL_OK;
+	const int G = couple_blocks(ps);
+	int rc;
+	if ((rc = ensure_partials(ps, G))) return rc;
+	const PView v = make_view(L);
+	const bool f32 = L->desc.storage == KEL_STORAGE_FP32;
+	switch (L->d.Q) {
+	case 9: f32 ? launch_couple_gather<D2Q9, STORE_FP32>(v, ps, prm, G) : launch_couple_gather<D2Q9, STORE_FP16S>(v, ps, prm, G); break;
+	case 19: f32 ? launch_couple_gather<D3Q19, STORE_FP32>(v, ps, prm, G) : launch_couple_gather<D3Q19, STORE_FP16S>(v, ps, prm, G); break;
+	default: f32 ? launch_couple_gather<D3Q27, STORE_FP32>(v, ps, prm, G) : launch_couple_gather<D3Q27, STORE_FP16S>(v, ps, prm, G); break;
+	}
+	KEL_CUDA(cudaGetLastError());
+	ps->gather_g = G;
+	ps->prev_is_last = false;
+	ps->cur_fresh = true;
+	ps->cur_sub = sub;
+	ps->epoch = ++L->por_epoch;
+	*done = true;
+	return KEL_OK;
+}
+
 // Contact (from zero, with the gather sums) and integrate of the coupled
-// step; the integrate also prepares the next couple's boxes.
-static int particles_contact_integrate(kel_particles *ps, const kel_particle_params *prm) {
+// step in one launch, which also prepares the next couple's boxes; the
+// bodies' new state lands in the second buffer, which becomes the current
+// one.
+static int particles_contact_integrate(kel_particles *ps, const kel_particle_params *prm, cudaStream_t st) {
 	kel_lattice *L = ps->lat;
 	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
 	const PView v = make_view(L);
-	k_contact_step<<<ps->n, 32, 0, L->stream>>>(ps->d, ps->n, v.D, *prm, v.nx, v.ny, v.nz, v.periodic, ps->partial,
-												 gather_blocks(ps));
-	k_integrate_boxes<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, *prm, cur_boxes(ps),
-																   prev_boxes(ps), sub);
+	k_contact_integrate<<<ps->n, 32, 0, st>>>(ps->d, ps->d_alt, v, *prm, ps->partial, ps->gather_g, cur_boxes(ps),
+											  prev_boxes(ps), sub);
 	KEL_CUDA(cudaGetLastError());
+	kel_particle_state *t = ps->d; // the bodies' new state is in the other buffer
+	ps->d = ps->d_alt;
+	ps->d_alt = t;
 	ps->prev_is_last = true;
 	ps->cur_fresh = true;
 	ps->cur_sub = sub;
@@ -1596,8 +1788,13 @@ extern "C" int kel_particles_stamp(kel_particles *ps, const kel_particle_params 
 // contact starts from zero and the integrate prepares the next couple's
 // boxes, so from the second step on a step is couple, gather, contact,
 // integrate and the sweep.
+// With a side stream (graph capture only), contact and integrate run on it
+// while the sweep runs on the lattice's stream: the PSM sweep reads the
+// porosity the couple wrote and the populations the gather has read, the
+// bodies' pass reads and writes only the bodies and their boxes; the next
+// couple waits for both.
 static int coupled_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
-						uint32_t flags) {
+						uint32_t flags, cudaStream_t side = nullptr) {
 	int rc;
 	if (is_fplbm(prm)) {
 		// examples/moving_poiseulle_particles_2d_fplbm_gpu/sim.cpp:186-258: reset
@@ -1607,9 +1804,21 @@ static int coupled_step(kel_particles *ps, const kel_particle_params *prm, const
 		return kel_step(ps->lat, prog, 1, flags | KEL_STEP_ALL_MACROS);
 	}
 	const bool fused = prm->coupling == KEL_COUPLING_PSM;
-	if ((rc = particles_couple(ps, prm, !fused)) || (rc = particles_gather(ps, prm, false, false))) return rc;
+	bool cg = false;
+	if (fused && (rc = particles_couple_gather(ps, prm, &cg))) return rc;
+	if (!cg && ((rc = particles_couple(ps, prm, !fused)) || (rc = particles_gather(ps, prm, false, false)))) return rc;
+	if (fused && side) {
+		kel_lattice *L = ps->lat;
+		KEL_CUDA(cudaEventRecord(ps->ev_fork, L->stream));
+		KEL_CUDA(cudaStreamWaitEvent(side, ps->ev_fork, 0));
+		if ((rc = particles_contact_integrate(ps, prm, side))) return rc;
+		KEL_CUDA(cudaEventRecord(ps->ev_join, side));
+		if ((rc = kel_step(L, prog, 1, flags))) return rc;
+		KEL_CUDA(cudaStreamWaitEvent(L->stream, ps->ev_join, 0));
+		return KEL_OK;
+	}
 	if (fused) {
-		if ((rc = particles_contact_integrate(ps, prm))) return rc;
+		if ((rc = particles_contact_integrate(ps, prm, ps->lat->stream))) return rc;
 	} else if ((rc = particles_contact(ps, prm, true)) || (rc = particles_integrate(ps, prm))) {
 		return rc;
 	}
@@ -1645,7 +1854,13 @@ static ParticleGraphKey graph_key(kel_particles *ps, const kel_particle_params *
 static int ensure_particle_graph(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog) {
 	kel_lattice *L = ps->lat;
 	int rc;
-	if ((rc = ensure_partials(ps, gather_blocks(ps)))) return rc; // no allocation inside the capture
+	const int gmax = gather_blocks(ps) > couple_blocks(ps) ? gather_blocks(ps) : couple_blocks(ps);
+	if ((rc = ensure_partials(ps, gmax))) return rc; // no allocation inside the capture
+	if (!ps->side) {
+		KEL_CUDA(cudaStreamCreateWithFlags(&ps->side, cudaStreamNonBlocking));
+		KEL_CUDA(cudaEventCreateWithFlags(&ps->ev_fork, cudaEventDisableTiming));
+		KEL_CUDA(cudaEventCreateWithFlags(&ps->ev_join, cudaEventDisableTiming));
+	}
 	const ParticleGraphKey k = graph_key(ps, prm, prog);
 	if (ps->graph && memcmp(&k, &ps->key, sizeof(k)) == 0) return KEL_OK;
 	if (ps->graph) cudaGraphExecDestroy(ps->graph);
@@ -1657,8 +1872,8 @@ static int ensure_particle_graph(kel_particles *ps, const kel_particle_params *p
 		cudaGetLastError();
 		return KEL_ERR_CUDA;
 	}
-	rc = coupled_step(ps, prm, prog, 0);
-	if (rc == KEL_OK) rc = coupled_step(ps, prm, prog, 0);
+	rc = coupled_step(ps, prm, prog, 0, ps->side);
+	if (rc == KEL_OK) rc = coupled_step(ps, prm, prog, 0, ps->side);
 	cudaGraph_t g = nullptr;
 	cudaError_t e = cudaStreamEndCapture(L->stream, &g);
 	L->t = t0;

@@ -20,6 +20,7 @@
  *   lid               examples/cavity_2d_gpu/cavity_2d_gpu.cpp:204-235
  *   step order        examples/poiseulle_2d_gpu/poiseulle_2d_gpu.cpp:158-235, 384-399
  */
+#include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>

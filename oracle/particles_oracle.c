@@ -60,16 +60,36 @@ static double ramp(double s, double rad, double eps) {
 	return c * c;
 }
 
-static double subcell(int D, const double *x, const double *X, double rad) {
-	int n = D == 2 ? 4 : 4, total = D == 2 ? 16 : 64, inside = 0;
-	double r2 = rad * rad;
-	for (int a = 0; a < n; ++a)
-		for (int b = 0; b < n; ++b)
-			for (int g = 0; g < (D == 3 ? n : 1); ++g) {
-				double px = x[0] + (2 * a - 3) / 8.0 - X[0];
-				double py = x[1] + (2 * b - 3) / 8.0 - X[1];
-				double pz = D == 3 ? x[2] + (2 * g - 3) / 8.0 - X[2] : 0.0;
-				double d2 = px * px + py * py + pz * pz;
+/* 4^D sub-cell solid fraction (no reference counterpart), in float: the
+ * cell's offset from the body is its integer part (x - nearest lattice point
+ * of the centre, the nearest periodic image) plus the fraction (that point -
+ * the centre); samples at offset + (2 a - 3) / 8 per axis count as inside
+ * when their squared distance, summed in axis order, is at most R^2. */
+static double subcell(int D, int64_t x, int64_t y, int64_t z, const double *X, double rad, int per, int64_t nx) {
+	int total = D == 2 ? 16 : 64, inside = 0;
+	int64_t c[3] = {x, y, z};
+	float r[3] = {0.f, 0.f, 0.f};
+	for (int k = 0; k < D; ++k) {
+		const int ic = (int)llround(X[k]);
+		const float fr = (float)((double)ic - X[k]);
+		int d = (int)(c[k] - ic);
+		if (k == 0 && per) {
+			if (d > (int)nx / 2) d -= (int)nx;
+			else if (d < -((int)nx / 2)) d += (int)nx;
+		}
+		r[k] = (float)d + fr;
+	}
+	const float r2 = (float)rad * (float)rad;
+	for (int a = 0; a < 4; ++a)
+		for (int b = 0; b < 4; ++b)
+			for (int g = 0; g < (D == 3 ? 4 : 1); ++g) {
+				float px = r[0] + (float)(2 * a - 3) * 0.125f;
+				float py = r[1] + (float)(2 * b - 3) * 0.125f;
+				float d2 = px * px + py * py;
+				if (D == 3) {
+					float pz = r[2] + (float)(2 * g - 3) * 0.125f;
+					d2 = d2 + pz * pz;
+				}
 				if (d2 <= r2) ++inside;
 			}
 	return 1.0 - (double)inside / (double)total;
@@ -138,8 +158,7 @@ void ko_particles_couple(ko_lattice *h, const kel_particle_state *P, int np, con
 					if (xc != ix) continue; /* this image is not the nearest one (or lies outside the AABB) */
 					double pp;
 					if (sub) {
-						double xs[3] = {xi, (double)y, (double)z};
-						pp = subcell(D, xs, P[p].position, P[p].radius);
+						pp = subcell(D, x, y, z, P[p].position, P[p].radius, per, nx);
 					} else {
 						double s2 = 0.0;
 						for (int k = 0; k < D; ++k) s2 = s2 + rel[k] * rel[k];
