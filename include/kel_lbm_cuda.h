@@ -176,6 +176,12 @@ int kel_step(kel_lattice *lat, const kel_step_program *prog, uint64_t n_steps, u
 /* Solid fraction used by the couple pass. */
 #define KEL_POROSITY_RAMP 0    /* sin^2 ramp of width eps around R (particle/porosity.hpp:56-89) */
 #define KEL_POROSITY_SUBCELL 1 /* 4^D sub-cell point sampling over the cell [x-1/2, x+1/2]^D */
+/* 1 - the cos^2 solid fraction (width eps) of the signed distance read off
+ * the set's voxel shape (kel_particles_set_shape), in FP32, at each cell of
+ * the body's box: the sub-cell style box of radius R * reach + eps / 2
+ * (reach: kel_shape_info) (particle/porosity.hpp:24-54, mask.hpp:270-311).
+ * PSM coupling only. */
+#define KEL_POROSITY_VOXEL 2
 
 /* One rigid body, the fields of sch::ParticleRigidBody + collision radius
  * (particle/schema.hpp:51-115).  2D: rotation, torque and their derivatives
@@ -258,6 +264,58 @@ int kel_particles_stamp(kel_particles *ps, const kel_particle_params *prm);
  * HLBM coupling the program's collision must be KEL_COLL_HLBM. */
 int kel_particles_step(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog,
 					   uint64_t n_steps, uint32_t step_flags);
+
+/* ---- voxel shapes: signed distance masks (particle/mask.hpp) ----------- */
+
+/* A body shape as a signed distance on R^D voxels in normalised body-local
+ * units (bounding radius 1: local [-1, 1]^D, voxel k at -1 + (k + 1/2) 2/R,
+ * negative inside), scaled per body by its radius and placed by its position
+ * and rotation (2D: angle rotation[0]; 3D: rotation vector, Rodrigues):
+ * x = position + radius Rot(rotation) (u - center_of_mass)
+ * (particle/mask.hpp:11-180).  Masks are R^D doubles, the last axis fastest. */
+#define KEL_SHAPE_SPHERE 0 /* sdf::sphere (mask.hpp:317-322) */
+#define KEL_SHAPE_CUBE 1   /* sdf::cube, Chebyshev distance (mask.hpp:328-340) */
+typedef struct kel_shape kel_shape;
+
+/* fill_mask_from_sdf (mask.hpp:351-394) of a built-in shape, on the host:
+ * the mask and its centroid weighted by a one-voxel cos^2 solid fraction. */
+int kel_shape_create(int32_t dim, int32_t resolution, int32_t kind, kel_shape **out);
+/* A shape from a caller's mask (R^D doubles) and centre of mass (dim doubles). */
+int kel_shape_create_from_mask(int32_t dim, int32_t resolution, const double *mask, const double *center_of_mass,
+							   kel_shape **out);
+/* The shape's mask (R^D doubles, may be NULL), centre of mass (3 doubles, may
+ * be NULL) and normalised reach (may be NULL): the largest |u| over the
+ * voxels at distance <= 0 plus one voxel diagonal 2 sqrt(dim) / R. */
+int kel_shape_info(const kel_shape *shape, double *mask, double *center_of_mass, double *reach);
+int kel_shape_destroy(kel_shape *shape);
+/* The shape every body of the set takes (the reference's group mask,
+ * sch::ParticleGroup "mask" / "center_of_mass"); NULL detaches.  The shape
+ * must outlive its use and have the lattice's dimension. */
+int kel_particles_set_shape(kel_particles *ps, const kel_shape *shape);
+
+/* mask_signed_distance (mask.hpp:270-282) of body `body` of the set at
+ * `n` lattice points (host, dim doubles each), FP64 on the device, into
+ * out (host, n doubles). */
+int kel_particles_voxel_distance(kel_particles *ps, int32_t body, const double *points, int32_t n, double *out);
+
+/* voxel_contact (particle/voxel_narrow.hpp:78-259) of body pairs of the set,
+ * FP64 on the device, one block per pair: the overlap of the two bodies'
+ * solid fractions (width eps) over the lattice cells of their clamped
+ * bounding-box intersection gives the contact point (overlap centroid), the
+ * normal (overlap-weighted grad phi_hi - grad phi_lo, from hi toward lo) and
+ * the depth (extent of the cells both hold above 1/2 along the normal, + 1,
+ * capped at the smaller radius).  Sums are in a fixed order that does not
+ * depend on which body is lo: swapping a pair negates the normal exactly. */
+typedef struct kel_contact_manifold {
+	int32_t hit;
+	int32_t pad;
+	double normal[3];
+	double point[3];
+	double depth;
+} kel_contact_manifold;
+/* pairs: host, 2 body indices (lo, hi) per pair; out: host, npairs entries. */
+int kel_particles_voxel_contact(kel_particles *ps, const int32_t *pairs, int32_t npairs, double eps,
+								kel_contact_manifold *out);
 
 /* ---- batches: many independent D2Q9 channels in one launch ------------ */
 

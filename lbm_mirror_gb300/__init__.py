@@ -5,7 +5,7 @@ the C ABI of include/kel_lbm_cuda.h); this package is the Python host mirror.
 """
 from . import capi
 from .lattice import (BGK, Batch, UNet, AntiBounceBack, BGKGuo, BounceBack, Equilibrium, KelError, Lattice, MovingWall, Particles, Psm,
-                      PsmGuo, ZouHePressureX, ZouHeVelocityX, program_from_switch)
+                      PsmGuo, Shape, ZouHePressureX, ZouHeVelocityX, program_from_switch)
 
-__all__ = ["capi", "Lattice", "Particles", "Batch", "UNet", "KelError", "program_from_switch", "BGK", "BGKGuo", "Psm", "PsmGuo", "BounceBack",
+__all__ = ["capi", "Lattice", "Particles", "Shape", "Batch", "UNet", "KelError", "program_from_switch", "BGK", "BGKGuo", "Psm", "PsmGuo", "BounceBack",
            "AntiBounceBack", "Equilibrium", "ZouHePressureX", "ZouHeVelocityX", "MovingWall"]

@@ -135,7 +135,8 @@ def program_from_dict(d):
                         d["global_force"], d.get("arithmetic", KEL_ARITH_FAST))
 
 
-KEL_POROSITY_RAMP, KEL_POROSITY_SUBCELL = 0, 1
+KEL_POROSITY_RAMP, KEL_POROSITY_SUBCELL, KEL_POROSITY_VOXEL = 0, 1, 2
+KEL_SHAPE_SPHERE, KEL_SHAPE_CUBE = 0, 1
 KEL_COUPLING_PSM, KEL_COUPLING_HLBM, KEL_COUPLING_FPLBM, KEL_COUPLING_FPLBM_OWN = 0, 1, 2, 3
 
 
@@ -169,6 +170,17 @@ class ParticleParams(C.Structure):
         ("body_acceleration", C.c_double * 3),
         ("wall_axes", C.c_uint32),
         ("coupling", C.c_int32),
+    ]
+
+
+class ContactManifold(C.Structure):
+    """kel_contact_manifold (sch::ContactManifold, particle/contact.hpp:20-25, plus the hit flag)."""
+    _fields_ = [
+        ("hit", C.c_int32),
+        ("pad", C.c_int32),
+        ("normal", C.c_double * 3),
+        ("point", C.c_double * 3),
+        ("depth", C.c_double),
     ]
 
 
@@ -304,6 +316,13 @@ def load_library(path: str | None = None):
         "kel_particles_contact": ([vp, C.POINTER(ParticleParams)], C.c_int),
         "kel_particles_integrate": ([vp, C.POINTER(ParticleParams)], C.c_int),
         "kel_particles_step": ([vp, C.POINTER(ParticleParams), C.POINTER(StepProgram), u64, u32], C.c_int),
+        "kel_shape_create": ([i32, i32, i32, C.POINTER(vp)], C.c_int),
+        "kel_shape_create_from_mask": ([i32, i32, vp, vp, C.POINTER(vp)], C.c_int),
+        "kel_shape_info": ([vp, vp, vp, vp], C.c_int),
+        "kel_shape_destroy": ([vp], C.c_int),
+        "kel_particles_set_shape": ([vp, vp], C.c_int),
+        "kel_particles_voxel_distance": ([vp, i32, vp, i32, vp], C.c_int),
+        "kel_particles_voxel_contact": ([vp, vp, i32, C.c_double, vp], C.c_int),
         "kel_last_error_string": ([], C.c_char_p),
         "kel_version": ([], C.c_char_p),
     }

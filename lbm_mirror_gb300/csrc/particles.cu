@@ -25,18 +25,32 @@
 
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "lattice_internal.cuh"
 
 using namespace kel::gb;
+
+// A voxel shape (particle/mask.hpp): the mask on the host (double) and on
+// the device (float for the couple, double for the distance and contact
+// queries), its centre of mass and normalised reach.
+struct kel_shape {
+	int dim = 0, res = 0;
+	std::vector<double> mask;
+	double com[3] = {0, 0, 0};
+	double reach = 0.0;
+	float *d_mask_f = nullptr;
+	double *d_mask_d = nullptr;
+};
 
 // Key of the captured coupled step: everything its launches bake in.
 struct ParticleGraphKey {
 	kel_particle_params prm;
 	kel_step_program prog;
 	kel::gb::SweepParams sweep;
-	void *f, *por, *force, *bodies, *boxes, *partial;
-	int n, gather_g, couple_g, cpt, block;
+	void *f, *por, *force, *bodies, *boxes, *partial, *rec;
+	const void *shape;
+	int n, gather_g, couple_g, cpt, block, direct;
 };
 
 struct kel_particles {
@@ -56,9 +70,16 @@ struct kel_particles {
 	// box bookkeeping between couples: prev_is_last -- prev[] holds the boxes of
 	// the last couple (the fused contact + integrate moved them there);
 	// cur_fresh -- cur[] holds the boxes of the current positions, for
-	// porosity mode cur_sub
+	// porosity mode cur_mode and ramp width cur_eps
 	bool prev_is_last = false, cur_fresh = false;
-	int cur_sub = 0;
+	int cur_mode = 0;
+	double cur_eps = 0.0;
+	// the bodies' records for the fused couple + gather (CoupleRec), written by
+	// the fused contact + integrate with these parameters
+	void *rec = nullptr;
+	int rec_mode = -1, rec_steps = 0;
+	double rec_eps = 0.0;
+	const kel_shape *shape = nullptr; // voxel bodies' shape (KEL_POROSITY_VOXEL)
 	cudaGraphExec_t graph = nullptr; // two coupled steps from an even time step
 	// fork / join of the captured steps: contact + integrate beside the sweep
 	cudaStream_t side = nullptr;
@@ -81,21 +102,35 @@ struct PView {
 	float *hN, *hD; // HLBM particle_N (D planes) and particle_D
 	float *rho, *mom; // macros "density" and "velocity" (FPLBM: momentum), D planes
 	float wshift[27];
+	// body boxes: radius R * box_mul + box_add (1, 0 but for voxel bodies)
+	double box_mul, box_add;
+	// sub-cell and voxel factors may skip the FP64 nearest-image test (every
+	// box narrower than half the periodic length)
+	int direct;
+	// voxel shape (KEL_POROSITY_VOXEL): R^D mask as float and double, centre
+	// of mass, resolution
+	const float *vmask_f;
+	const double *vmask_d;
+	float vcom_f[3];
+	double vcom[3];
+	int vres;
 };
 
 // ---- geometry shared by couple and gather -----------------------------------
 
 // aabb.hpp:41-84: [a, b) per axis.  Sub-cell mode widens to every cell the
 // body can touch; periodic x leaves the x range unclamped (cells wrap).
+// Voxel bodies take the sub-cell rule with the radius R * rmul + radd (the
+// shape's reach and half the ramp width).
 __host__ __device__ inline void body_aabb(int D, const kel_particle_state &p, int nx, int ny, int nz, int periodic,
-										  int subcell, int64_t *a, int64_t *b) {
+										  int subcell, int64_t *a, int64_t *b, double rmul = 1.0, double radd = 0.0) {
 	const int64_t ext[3] = {nx, ny, nz};
 	for (int k = 0; k < 3; ++k) {
 		a[k] = 0;
 		b[k] = 1;
 	}
 	for (int k = 0; k < D; ++k) {
-		const double X = p.position[k], r = p.radius;
+		const double X = p.position[k], r = p.radius * rmul + radd;
 		if (subcell) {
 			a[k] = (int64_t)floor(X - r - 0.5);
 			b[k] = (int64_t)ceil(X + r + 0.5) + 1;
@@ -152,7 +187,8 @@ __device__ inline double subcell_porosity(int D, const float *r, float rad) {
 				}
 				if (d2 <= r2) ++inside;
 			}
-	return 1.0 - (double)inside / (double)(D == 3 ? 64 : 16);
+	// 1 - inside / 4^D, exact in FP32 (and so equal to the FP64 quotient)
+	return (double)(1.0f - (float)inside * (D == 3 ? 0.015625f : 0.0625f));
 }
 
 // ---- couple -------------------------------------------------------------------
@@ -184,7 +220,7 @@ __global__ void k_pre(PView v, kel_particle_state *P, int np, int sub, BodyBox *
 	if (!boxes) return;
 	if (shift) prev[i] = cur[i];
 	int64_t a[3], b[3];
-	body_aabb(v.D, P[i], v.nx, v.ny, v.nz, v.periodic, sub, a, b);
+	body_aabb(v.D, P[i], v.nx, v.ny, v.nz, v.periodic, sub, a, b, v.box_mul, v.box_add);
 	BodyBox r;
 	for (int k = 0; k < 3; ++k) {
 		r.a[k] = (int)a[k];
@@ -206,6 +242,8 @@ struct Cand {
 	int ic[3];
 	float fr[3];
 	float s_in, s_out;
+	float Rf; // the radius rounded to FP32 (the sub-cell and voxel sampling's)
+	float M[9]; // voxel bodies: the inverse rotation Rot(-theta), row-major, rounded to FP32
 };
 
 // Squared-distance margin of the FP32 screen: far above its own error (the
@@ -233,6 +271,143 @@ __device__ inline void cand_limits(Cand &c, int sub, double reach, double eps) {
 	}
 	c.s_out = (float)c.lim_out2 + SCREEN_MARGIN;
 	c.s_in = c.lim_in2 > 0.0 ? (float)c.lim_in2 - SCREEN_MARGIN : -1.0f;
+	c.Rf = (float)R;
+}
+
+// The voxel candidate's inverse rotation (mask.hpp:52-105 with the negated
+// angle) as a matrix: 2D [[c, -s], [s, c]], c = cos(-theta), s = sin(-theta);
+// 3D the Rodrigues matrix c I + s [n]x + (1 - c) n n^T of the rotation vector
+// with the angle negated.  Formed in FP64, rounded to FP32.
+__device__ inline void voxel_matrix(int D, const double *rot, float *M) {
+	double m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+	if (D == 2) {
+		const double a = -rot[0];
+		const double c = cos(a), s = sin(a);
+		m[0] = c;
+		m[1] = -s;
+		m[3] = s;
+		m[4] = c;
+	} else {
+		double th2 = 0.0;
+		for (int i = 0; i < 3; ++i) th2 = th2 + rot[i] * rot[i];
+		if (th2 > 0.0) {
+			const double th = -sqrt(th2);
+			double n[3];
+			for (int i = 0; i < 3; ++i) n[i] = rot[i] / sqrt(th2);
+			const double c = cos(th), s = sin(th);
+			const double K[9] = {0, -n[2], n[1], n[2], 0, -n[0], -n[1], n[0], 0};
+			for (int i = 0; i < 3; ++i)
+				for (int j = 0; j < 3; ++j) m[i * 3 + j] = (i == j ? c : 0.0) + K[i * 3 + j] * s + n[i] * n[j] * (1 - c);
+		}
+	}
+	for (int i = 0; i < 9; ++i) M[i] = (float)m[i];
+}
+
+// Couple mode of a pass: 0 ramp, 1 sub-cell with the FP64 shortcut test,
+// 2 sub-cell without it (direct), 3 voxel.
+__host__ __device__ inline int couple_mode(int porosity_mode, int direct) {
+	if (porosity_mode == KEL_POROSITY_SUBCELL) return direct ? 2 : 1;
+	return porosity_mode == KEL_POROSITY_VOXEL ? 3 : 0;
+}
+
+// A candidate's limits and (voxel mode) its transform.  Voxel bodies have no
+// distance shortcut: every cell of the box is sampled.
+__device__ inline void cand_prepare(Cand &c, int cm, double reach, double eps, const double *rot, int D) {
+	cand_limits(c, cm, reach, eps);
+	if (cm == 3) {
+		c.lim_in2 = -1.0;
+		c.lim_out2 = INFINITY;
+		c.s_in = -1.0f;
+		c.s_out = INFINITY;
+		voxel_matrix(D, rot, c.M);
+	}
+}
+
+// The voxel mask sampled at body-local u in FP32: mask_sample_local
+// (mask.hpp:194-264) with its order of operations, rounded to nearest.
+__device__ inline float mask_sample_f32(const float *__restrict__ mask, int D, int R, const float *u) {
+	const float step = __fdiv_rn(2.0f, (float)R);
+	float frac[3] = {0.f, 0.f, 0.f};
+	int base[3] = {0, 0, 0};
+	float outside = 0.0f;
+	for (int i = 0; i < D; ++i) {
+		float g = __fsub_rn(__fdiv_rn(__fadd_rn(u[i], 1.0f), step), 0.5f);
+		if (g < 0.0f) {
+			outside = __fadd_rn(outside, __fmul_rn(__fmul_rn(__fmul_rn(g, g), step), step));
+			g = 0.0f;
+		} else if (g > (float)(R - 1)) {
+			const float over = __fsub_rn(g, (float)(R - 1));
+			outside = __fadd_rn(outside, __fmul_rn(__fmul_rn(__fmul_rn(over, over), step), step));
+			g = (float)(R - 1);
+		}
+		base[i] = (int)floorf(g);
+		if (base[i] > R - 2) {
+			base[i] = R - 2;
+			if (base[i] < 0) base[i] = 0;
+		}
+		frac[i] = __fsub_rn(g, (float)base[i]);
+	}
+	float acc = 0.0f;
+	for (int c = 0; c < (1 << D); ++c) {
+		float w = 1.0f;
+		int flat = 0;
+		for (int i = 0; i < D; ++i) {
+			const int hi = (c >> i) & 1;
+			int idx = base[i] + hi;
+			if (idx < 0) idx = 0;
+			if (idx > R - 1) idx = R - 1;
+			flat = flat * R + idx;
+			w = __fmul_rn(w, hi ? frac[i] : __fsub_rn(1.0f, frac[i]));
+		}
+		acc = __fadd_rn(acc, __fmul_rn(w, __ldg(mask + flat)));
+	}
+	if (outside > 0.0f) acc = __fadd_rn(acc, __fsqrt_rn(outside));
+	return acc;
+}
+
+// Voxel body factor 1 - solid at a cell whose offset from the body centre is
+// r (FP32: exact integer part plus the body's fraction): u = M r / R + com,
+// the mask's signed distance times R, then solid_fraction_from_sdf
+// (mask.hpp:291-311) with cos^2 in FP32.
+__device__ inline float voxel_factor(const PView &v, const Cand &c, const float *r, float eps) {
+	const int D = v.D;
+	float q[3] = {0.f, 0.f, 0.f}, u[3] = {0.f, 0.f, 0.f};
+	for (int i = 0; i < D; ++i) q[i] = __fdiv_rn(r[i], c.Rf);
+	for (int i = 0; i < D; ++i) {
+		float a = __fadd_rn(__fmul_rn(c.M[i * 3 + 0], q[0]), __fmul_rn(c.M[i * 3 + 1], q[1]));
+		if (D == 3) a = __fadd_rn(a, __fmul_rn(c.M[i * 3 + 2], q[2]));
+		u[i] = __fadd_rn(a, v.vcom_f[i]);
+	}
+	const float sdf = __fmul_rn(mask_sample_f32(v.vmask_f, D, v.vres, u), c.Rf);
+	const float half = __fmul_rn(eps, 0.5f);
+	float solid;
+	if (sdf <= -half) {
+		solid = 1.0f;
+	} else if (sdf >= half) {
+		solid = 0.0f;
+	} else {
+		const float t = __fdiv_rn(__fadd_rn(sdf, half), eps);
+		const float cc = cosf(__fmul_rn(__fmul_rn(3.14159265358979323846f, t), 0.5f));
+		solid = __fmul_rn(cc, cc);
+	}
+	return __fsub_rn(1.0f, solid);
+}
+
+// Per-body record of the fused couple + gather, written by the pass that
+// moved the body (k_contact_integrate), so that the blocks of the next couple
+// + gather read what each of them would otherwise form in FP64: the body's
+// couple candidate and c_i . u_p per direction rounded to float.
+struct CoupleRec {
+	Cand cand;
+	float upe[27];
+};
+
+// psm.hpp:178-184: u_p = (X - X_old) / (1 / sub_steps) with the raw
+// sub_steps.  For a power-of-two sub_steps (and 0) the quotient is exactly
+// the product (X - X_old) * sub_steps, which needs no FP64 division.
+__host__ __device__ inline double wall_velocity(double dx, int steps) {
+	if ((steps & (steps - 1)) == 0) return dx * (double)steps;
+	return dx / (1.0 / (double)steps);
 }
 
 // Body q's factor on the porosity of cell (x, y, z), multiplied into por
@@ -246,7 +421,11 @@ __device__ inline void cand_limits(Cand &c, int sub, double reach, double eps) {
 //   ramp mode: |r|^2 below (R - eps/2)^2 - 1e-6 gives 0, above
 //     (R + eps/2)^2 + 1e-6 gives 1.
 // The margins are far above the FP64 rounding of the coordinates, so the
-// factors equal those of the full computation bit for bit.  An FP32 screen
+// factors equal those of the full computation bit for bit.  With sub == 2
+// (sub-cell mode where every box is narrower than half the periodic length,
+// so that the image of the cell in the box is the nearest one) the cells the
+// screen leaves go straight to the FP32 sampling: past either shortcut limit
+// it gives the shortcut's factor itself.  An FP32 screen
 // decides first the cells whose squared distance lies SCREEN_MARGIN beyond
 // either limit (the same decision the FP64 test takes there; a cell that
 // deep inside has its nearest image in the body's box), so that only cells
@@ -275,11 +454,23 @@ __device__ inline void body_factor(const PView &v, int x, int y, int z, const Ca
 		rf[0] = __fadd_rn((float)dx, c.fr[0]);
 		rf[1] = __fadd_rn((float)(y - c.ic[1]), c.fr[1]);
 		rf[2] = v.D == 3 ? __fadd_rn((float)(z - c.ic[2]), c.fr[2]) : 0.f;
+		if (sub == 3) {
+			if (v.periodic && !v.direct) { // the image of the cell nearest the body must be the one in the box
+				const int64_t xc = (int64_t)llround(c.X[0] + rel_coord((double)x, c.X[0], 1, v.nx));
+				if (xc < q.a[0] || xc >= q.b[0]) return;
+			}
+			por = por * (double)voxel_factor(v, c, rf, (float)eps);
+			return;
+		}
 		float s2f = __fadd_rn(__fmul_rn(rf[0], rf[0]), __fmul_rn(rf[1], rf[1]));
 		if (v.D == 3) s2f = __fadd_rn(s2f, __fmul_rn(rf[2], rf[2]));
 		if (s2f > c.s_out) return; // factor 1
 		if (s2f < c.s_in) {        // factor 0
 			por = por * 0.0;
+			return;
+		}
+		if (sub == 2) {
+			por = por * subcell_porosity(v.D, rf, c.Rf);
 			return;
 		}
 	}
@@ -297,7 +488,7 @@ __device__ inline void body_factor(const PView &v, int x, int y, int z, const Ca
 		} else if (s2 < c.lim_in2) {
 			pp = 0.0;
 		} else {
-			pp = subcell_porosity(v.D, rf, (float)R);
+			pp = subcell_porosity(v.D, rf, c.Rf);
 		}
 	} else {
 		if (s2 < c.lim_in2) pp = 0.0;
@@ -308,13 +499,15 @@ __device__ inline void body_factor(const PView &v, int x, int y, int z, const Ca
 	(void)reach;
 }
 
-__device__ inline double subcell_reach(int D) { return D == 3 ? 0.6495190528383290 : 0.5303300858899106; } // 3 sqrt(D) / 8
+__host__ __device__ inline double subcell_reach(int D) { return D == 3 ? 0.6495190528383290 : 0.5303300858899106; } // 3 sqrt(D) / 8
 
 // Ordered compaction of the bodies [c0, c0 + NT) for which hit is true (one
-// thread per body, NT threads) into cand[0 .. *ncand).
+// thread per body, NT threads) into cand[0 .. *ncand); with rec, the
+// candidates are the bodies' prepared records.
 template <int NT>
 __device__ inline void compact_cands(bool hit, int pi, const BodyBox &bb, const kel_particle_state *P, Cand *cand,
-									 int *warp_count, int *ncand, int sub, double reach, double eps) {
+									 int *warp_count, int *ncand, int sub, double reach, double eps, int D,
+									 const CoupleRec *rec = nullptr) {
 	const int tid = threadIdx.x + threadIdx.y * blockDim.x;
 	const unsigned m = __ballot_sync(0xffffffffu, hit);
 	if ((tid & 31) == 0) warp_count[tid >> 5] = __popc(m);
@@ -329,12 +522,14 @@ __device__ inline void compact_cands(bool hit, int pi, const BodyBox &bb, const 
 		*ncand = s;
 	}
 	__syncthreads();
-	if (hit) {
+	if (hit && rec) {
+		cand[warp_count[tid >> 5] + __popc(m & ((1u << (tid & 31)) - 1u))] = rec[pi].cand;
+	} else if (hit) {
 		Cand &c = cand[warp_count[tid >> 5] + __popc(m & ((1u << (tid & 31)) - 1u))];
 		c.box = bb;
 		for (int d = 0; d < 3; ++d) c.X[d] = P[pi].position[d];
 		c.R = P[pi].radius;
-		cand_limits(c, sub, reach, eps);
+		cand_prepare(c, sub, reach, eps, P[pi].rotation, D);
 	}
 	__syncthreads();
 }
@@ -350,8 +545,8 @@ __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state
 	const int tid = threadIdx.y * TX + threadIdx.x;
 	const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z = blockIdx.z;
 	const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
-	const int sub = mode == KEL_POROSITY_SUBCELL;
-	const double reach = sub ? subcell_reach(v.D) : 0.0;
+	const int sub = couple_mode(mode, v.direct);
+	const double reach = (sub == 1 || sub == 2) ? subcell_reach(v.D) : 0.0;
 	double por = 1.0;
 	bool touched = false; // some body's box holds the cell (otherwise por stays exactly 1)
 	for (int c0 = 0; c0 < np; c0 += TT) {
@@ -366,7 +561,7 @@ __global__ void __launch_bounds__(TT) k_couple(PView v, const kel_particle_state
 				xs = xs || (bb.a[0] < x0 + TX - v.nx && bb.b[0] > x0 - v.nx) || (bb.a[0] < x0 + TX + v.nx && bb.b[0] > x0 + v.nx);
 			hit = yz && xs;
 		}
-		compact_cands<TT>(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
+		compact_cands<TT>(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps, v.D);
 		if (x < v.nx && y < v.ny)
 			for (int k = 0; k < ncand; ++k) body_factor(v, x, y, z, cand[k], sub, reach, eps, por, touched);
 		__syncthreads();
@@ -410,8 +605,8 @@ __global__ void __launch_bounds__(RT) k_couple_regions(PView v, const kel_partic
 	const bool same = A.a[0] == B.a[0] && A.b[0] == B.b[0] && A.a[1] == B.a[1] && A.b[1] == B.b[1] &&
 					  (v.D == 2 || (A.a[2] == B.a[2] && A.b[2] == B.b[2]));
 	const int64_t n0 = box_cells(A, v.D), n1 = same ? 0 : box_cells(B, v.D);
-	const int sub = mode == KEL_POROSITY_SUBCELL;
-	const double reach = sub ? subcell_reach(v.D) : 0.0;
+	const int sub = couple_mode(mode, v.direct);
+	const double reach = (sub == 1 || sub == 2) ? subcell_reach(v.D) : 0.0;
 	for (int64_t base = (int64_t)blockIdx.y * RT * RC_CPT; base < n0 + n1; base += (int64_t)gridDim.y * RT * RC_CPT) {
 		int cx[RC_CPT], cy[RC_CPT], cz[RC_CPT];
 		bool ok[RC_CPT], touched[RC_CPT];
@@ -441,7 +636,7 @@ __global__ void __launch_bounds__(RT) k_couple_regions(PView v, const kel_partic
 				bb = cur[pi];
 				hit = boxes_touch(bb, A, v) || (!same && boxes_touch(bb, B, v));
 			}
-			compact_cands<RT>(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
+			compact_cands<RT>(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps, v.D);
 #pragma unroll
 			for (int j = 0; j < RC_CPT; ++j)
 				if (ok[j])
@@ -456,6 +651,41 @@ __global__ void __launch_bounds__(RT) k_couple_regions(PView v, const kel_partic
 }
 
 // ---- gather ---------------------------------------------------------------------
+
+// Fixed-order block sum of the per-thread force/torque sums acc[0..5]
+// (force[3], torque[3]) into out[0..5]: a warp-shuffle tree, then the warps in
+// index order.  In 2D only force x, y and torque z can be non-zero; the other
+// three are written as +0.0, the value their sums of +0.0 give.  A warp whose
+// sums are all +0.0 (no contributing cell: a difference that cancels rounds to
+// +0.0, so no sum is ever -0.0) writes +0.0 without the tree.  part: the
+// block's NT / 32 x 6 shared scratch.
+template <int D, int NT>
+__device__ inline void block_sums(const double *acc, double (*part)[6], double *out) {
+	constexpr int NQ = D == 2 ? 3 : 6;
+	const int tid = threadIdx.x;
+	bool nz = false;
+#pragma unroll
+	for (int j = 0; j < NQ; ++j) nz |= acc[D == 2 && j == 2 ? 3 : j] != 0.0;
+	if (__any_sync(0xffffffffu, nz)) {
+#pragma unroll
+		for (int j = 0; j < NQ; ++j) {
+			const int q = D == 2 && j == 2 ? 3 : j;
+			double sum = acc[q];
+			for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
+			if ((tid & 31) == 0) part[tid >> 5][q] = sum;
+		}
+	} else if ((tid & 31) == 0) {
+#pragma unroll
+		for (int j = 0; j < NQ; ++j) part[tid >> 5][D == 2 && j == 2 ? 3 : j] = 0.0;
+	}
+	__syncthreads();
+	if (tid < 6) {
+		double tot = 0.0;
+		if (D == 3 || tid == 0 || tid == 1 || tid == 3)
+			for (int w = 0; w < NT / 32; ++w) tot += part[w][tid];
+		out[tid] = tot;
+	}
+}
 
 // Post-stream population f_i at a lattice cell (the buffer the next collide
 // reads); outside the lattice the reference's zero ghost ring.
@@ -496,7 +726,7 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, const kel_particle_state
 	__shared__ double part[GT / 32][6];
 	const kel_particle_state &p = P[blockIdx.x];
 	int64_t a[3], b[3];
-	body_aabb(D, p, v.nx, v.ny, v.nz, v.periodic, mode == KEL_POROSITY_SUBCELL, a, b);
+	body_aabb(D, p, v.nx, v.ny, v.nz, v.periodic, mode != KEL_POROSITY_RAMP, a, b, v.box_mul, v.box_add);
 	const int64_t ex = b[0] - a[0], ey = b[1] - a[1], ez = D == 3 ? b[2] - a[2] : 1;
 	const int64_t ncell = (ex > 0 && ey > 0 && ez > 0) ? ex * ey * ez : 0;
 	// psm.hpp:178-184: u_p = (X - X_old) / (1 / sub_steps), raw sub_steps
@@ -568,19 +798,7 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, const kel_particle_state
 			acc[5] -= r[0] * F[1] - r[1] * F[0];
 		}
 	}
-	// fixed-order reduction: warp shuffle, then warps in index order
-#pragma unroll
-	for (int q = 0; q < 6; ++q) {
-		double s = acc[q];
-		for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-		if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5][q] = s;
-	}
-	__syncthreads();
-	if (threadIdx.x < 6) {
-		double tot = 0.0;
-		for (int w = 0; w < GT / 32; ++w) tot += part[w][threadIdx.x];
-		partial[((int64_t)blockIdx.x * gridDim.y + blockIdx.y) * 6 + threadIdx.x] = tot;
-	}
+	block_sums<D, GT>(acc, part, partial + ((int64_t)blockIdx.x * gridDim.y + blockIdx.y) * 6);
 }
 
 // Incremental couple and PSM gather in one pass (the coupled step).  Block
@@ -591,10 +809,11 @@ __global__ void __launch_bounds__(GT) k_gather(PView v, const kel_particle_state
 // exchange to the block's FP64 sums, exactly as k_gather computes it from the
 // field (the porosity is the same value, computed here instead of read).
 // The sums go to partial[(b * G + g) * 6 ..] in k_gather's fixed order.
+// The bodies' candidates and c_i . u_p come from their records (rec).
 template <class L, int STORE>
-__global__ void __launch_bounds__(RT) k_couple_gather(PView v, const kel_particle_state *P, const BodyBox *cur,
-													  const BodyBox *prev, int np, int mode, double eps, int steps,
-													  double *partial) {
+__global__ void __maxnreg__(128) k_couple_gather(PView v, const kel_particle_state *P, const BodyBox *cur,
+												 const BodyBox *prev, int np, int mode, double eps,
+												 const CoupleRec *rec, double *partial) {
 	constexpr int D = L::D;
 	__shared__ Cand cand[RT];
 	__shared__ int warp_count[RT / 32];
@@ -607,21 +826,11 @@ __global__ void __launch_bounds__(RT) k_couple_gather(PView v, const kel_particl
 	const bool same = A.a[0] == B.a[0] && A.b[0] == B.b[0] && A.a[1] == B.a[1] && A.b[1] == B.b[1] &&
 					  (D == 2 || (A.a[2] == B.a[2] && A.b[2] == B.b[2]));
 	const int64_t n0 = box_cells(A, D), n1 = same ? 0 : box_cells(B, D);
-	const int sub = mode == KEL_POROSITY_SUBCELL;
-	const double reach = sub ? subcell_reach(D) : 0.0;
-	// psm.hpp:178-184: u_p = (X - X_old) / (1 / sub_steps), raw sub_steps
-	const double ts = 1.0 / (double)steps;
-	double vp[3] = {0.0, 0.0, 0.0};
-	for (int k = 0; k < D; ++k) vp[k] = (p.position[k] - p.position_old[k]) / ts;
+	const int sub = couple_mode(mode, v.direct);
+	const double reach = (sub == 1 || sub == 2) ? subcell_reach(D) : 0.0;
 	float upe[L::Q];
 #pragma unroll
-	for (int i = 1; i < L::Q; ++i) {
-		double upe_d = 0.0;
-		upe_d = upe_d + (double)L::cx(i) * vp[0];
-		upe_d = upe_d + (double)L::cy(i) * vp[1];
-		if (D == 3) upe_d = upe_d + (double)L::cz(i) * vp[2];
-		upe[i] = (float)upe_d;
-	}
+	for (int i = 1; i < L::Q; ++i) upe[i] = rec[b].upe[i];
 	double acc[6] = {0, 0, 0, 0, 0, 0};
 	for (int64_t base = (int64_t)blockIdx.y * RT; base < n0 + n1; base += (int64_t)gridDim.y * RT) {
 		const int64_t idx = base + tid;
@@ -647,7 +856,7 @@ __global__ void __launch_bounds__(RT) k_couple_gather(PView v, const kel_particl
 				bb = cur[pi];
 				hit = boxes_touch(bb, A, v) || (!same && boxes_touch(bb, B, v));
 			}
-			compact_cands<RT>(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps);
+			compact_cands<RT>(hit, pi, bb, P, cand, warp_count, &ncand, sub, reach, eps, D, rec);
 			if (ok)
 				for (int k = 0; k < ncand; ++k) body_factor(v, x, iy, iz, cand[k], sub, reach, eps, por, touched);
 			__syncthreads();
@@ -681,18 +890,7 @@ __global__ void __launch_bounds__(RT) k_couple_gather(PView v, const kel_particl
 			acc[5] -= r[0] * F[1] - r[1] * F[0];
 		}
 	}
-#pragma unroll
-	for (int q = 0; q < 6; ++q) {
-		double sum = acc[q];
-		for (int o = 16; o > 0; o >>= 1) sum += __shfl_down_sync(0xffffffffu, sum, o);
-		if ((tid & 31) == 0) part[tid >> 5][q] = sum;
-	}
-	__syncthreads();
-	if (tid < 6) {
-		double tot = 0.0;
-		for (int w = 0; w < RT / 32; ++w) tot += part[w][tid];
-		partial[((int64_t)b * gridDim.y + blockIdx.y) * 6 + tid] = tot;
-	}
+	block_sums<D, RT>(acc, part, partial + ((int64_t)b * gridDim.y + blockIdx.y) * 6);
 }
 
 // Sum of body i's G gather partials, g = 0 .. G-1 in order.
@@ -1284,41 +1482,328 @@ __global__ void k_integrate(kel_particle_state *P, int np, int D, kel_particle_p
 // per body: the contact of body s reads every body's state in P_in; lane 0
 // then integrates a copy of body s with that force and writes it to P_out
 // (the next step's state, so that no block reads a body another has already
-// moved), and prepares the next couple's boxes.
+// moved), and prepares the next couple's boxes and the body's record for
+// the next couple + gather (its candidate for couple mode cm; lanes
+// 1 .. Q-1 form c_i . u_p).
+template <class L>
 __global__ void __launch_bounds__(32) k_contact_integrate(const kel_particle_state *P_in, kel_particle_state *P_out,
 														  PView v, kel_particle_params prm, const double *partial,
-														  int G, BodyBox *cur, BodyBox *prev, int sub) {
+														  int G, BodyBox *cur, BodyBox *prev, int cm, double reach,
+														  CoupleRec *rec) {
 	__shared__ double fs[32][4];
 	__shared__ int hs[32];
 	const int s = blockIdx.x, np = (int)gridDim.x;
+	const int lane = threadIdx.x & 31;
 	kel_particle_state q;
 	contact_one(const_cast<kel_particle_state *>(P_in), s, np, v.D, prm, v.nx, v.ny, v.nz, v.periodic, partial, G, true,
 				fs, hs, &q);
-	if ((threadIdx.x & 31) != 0) return;
-	// contact_one set q's force and torque; the rest of the body from P_in
-	const kel_particle_state &o = P_in[s];
-	const double f0 = q.force[0], f1 = q.force[1], f2 = q.force[2];
-	const double t0 = q.torque[0], t1 = q.torque[1], t2 = q.torque[2];
-	q = o;
-	q.force[0] = f0;
-	q.force[1] = f1;
-	q.force[2] = f2;
-	q.torque[0] = t0;
-	if (v.D == 3) {
-		q.torque[1] = t1;
-		q.torque[2] = t2;
+	if (lane == 0) {
+		// contact_one set q's force and torque; the rest of the body from P_in
+		const kel_particle_state &o = P_in[s];
+		const double f0 = q.force[0], f1 = q.force[1], f2 = q.force[2];
+		const double t0 = q.torque[0], t1 = q.torque[1], t2 = q.torque[2];
+		q = o;
+		q.force[0] = f0;
+		q.force[1] = f1;
+		q.force[2] = f2;
+		q.torque[0] = t0;
+		if (v.D == 3) {
+			q.torque[1] = t1;
+			q.torque[2] = t2;
+		}
+		integrate_state(q, v.D, prm, v.nx, v.periodic);
+		P_out[s] = q;
+		int64_t a[3], b[3];
+		body_aabb(v.D, q, v.nx, v.ny, v.nz, v.periodic, cm != 0, a, b, v.box_mul, v.box_add);
+		BodyBox r;
+		for (int k = 0; k < 3; ++k) {
+			r.a[k] = (int)a[k];
+			r.b[k] = (int)b[k];
+		}
+		prev[s] = cur[s];
+		cur[s] = r;
+		Cand c;
+		c.box = r;
+		for (int d = 0; d < 3; ++d) c.X[d] = q.position[d];
+		c.R = q.radius;
+		cand_prepare(c, cm, reach, prm.eps, q.rotation, v.D);
+		rec[s].cand = c;
 	}
-	integrate_state(q, v.D, prm, v.nx, v.periodic);
-	P_out[s] = q;
-	int64_t a[3], b[3];
-	body_aabb(v.D, q, v.nx, v.ny, v.nz, v.periodic, sub, a, b);
-	BodyBox r;
-	for (int k = 0; k < 3; ++k) {
-		r.a[k] = (int)a[k];
-		r.b[k] = (int)b[k];
+	__syncwarp();
+	if (lane >= 1 && lane < L::Q) {
+		// the gather's c_i . u_p, rounded to float as the reference rounds it
+		const kel_particle_state &n = P_out[s];
+		double vp[3] = {0.0, 0.0, 0.0};
+		for (int k = 0; k < L::D; ++k) vp[k] = wall_velocity(n.position[k] - n.position_old[k], prm.sub_steps);
+		double upe_d = 0.0;
+		upe_d = upe_d + (double)L::cx(lane) * vp[0];
+		upe_d = upe_d + (double)L::cy(lane) * vp[1];
+		if (L::D == 3) upe_d = upe_d + (double)L::cz(lane) * vp[2];
+		rec[s].upe[lane] = (float)upe_d;
 	}
-	prev[s] = cur[s];
-	cur[s] = r;
+}
+
+// ---- voxel queries (FP64): mask.hpp, voxel_narrow.hpp ------------------------
+
+// mask_sample_local (mask.hpp:194-264)
+__device__ inline double mask_sample_f64(const double *__restrict__ mask, int D, int R, const double *u) {
+	const double step = 2.0 / (double)R;
+	double frac[3] = {0, 0, 0};
+	int64_t base[3] = {0, 0, 0};
+	double outside = 0;
+	for (int i = 0; i < D; ++i) {
+		double g = (u[i] + 1) / step - 0.5;
+		if (g < 0) {
+			outside += g * g * step * step;
+			g = 0;
+		} else if (g > (double)(R - 1)) {
+			const double over = g - (double)(R - 1);
+			outside += over * over * step * step;
+			g = (double)(R - 1);
+		}
+		base[i] = (int64_t)floor(g);
+		if (base[i] > (int64_t)R - 2) {
+			base[i] = (int64_t)R - 2;
+			if (base[i] < 0) base[i] = 0;
+		}
+		frac[i] = g - (double)base[i];
+	}
+	double acc = 0;
+	for (int c = 0; c < (1 << D); ++c) {
+		double w = 1;
+		int64_t flat = 0;
+		for (int i = 0; i < D; ++i) {
+			const int hi = (c >> i) & 1;
+			int64_t idx = base[i] + hi;
+			if (idx < 0) idx = 0;
+			if (idx > (int64_t)R - 1) idx = (int64_t)R - 1;
+			flat = flat * R + idx;
+			w *= hi ? frac[i] : (1 - frac[i]);
+		}
+		acc += w * __ldg(mask + flat);
+	}
+	if (outside > 0) acc += sqrt(outside);
+	return acc;
+}
+
+// A body's pose for the FP64 queries: position, radius and the inverse
+// rotation's terms of impl::mask_rotate (mask.hpp:52-105): 2D c, s of the
+// negated angle; 3D the unit axis n, c and s of the negated angle (th2 = 0:
+// no rotation).
+struct VoxelPose {
+	double X[3], R;
+	double c, s, n[3];
+	bool rot3;
+};
+
+__device__ inline VoxelPose voxel_pose(int D, const kel_particle_state &p) {
+	VoxelPose q;
+	for (int i = 0; i < 3; ++i) q.X[i] = p.position[i];
+	q.R = p.radius;
+	q.rot3 = false;
+	q.n[0] = q.n[1] = q.n[2] = 0.0;
+	if (D == 2) {
+		const double a = -p.rotation[0];
+		q.c = cos(a);
+		q.s = sin(a);
+	} else {
+		double th2 = 0;
+		for (int i = 0; i < 3; ++i) th2 = th2 + p.rotation[i] * p.rotation[i];
+		q.c = 1.0;
+		q.s = 0.0;
+		if (th2 > 0) {
+			q.rot3 = true;
+			const double th = -sqrt(th2);
+			for (int i = 0; i < 3; ++i) q.n[i] = p.rotation[i] / sqrt(th2);
+			q.c = cos(th);
+			q.s = sin(th);
+		}
+	}
+	return q;
+}
+
+// mask_signed_distance (mask.hpp:270-282): lattice point x to body-local u
+// (mask_global_to_local, mask.hpp:158-180), sampled, times the radius.
+__device__ inline double voxel_sdf(const PView &v, const VoxelPose &q, const double *x) {
+	const int D = v.D;
+	double rel[3] = {0, 0, 0}, un[3] = {0, 0, 0};
+	for (int i = 0; i < D; ++i) rel[i] = (x[i] - q.X[i]) / q.R;
+	if (D == 2) {
+		un[0] = rel[0] * q.c - rel[1] * q.s;
+		un[1] = rel[0] * q.s + rel[1] * q.c;
+	} else if (!q.rot3) {
+		for (int i = 0; i < 3; ++i) un[i] = rel[i];
+	} else {
+		double ndv = 0;
+		for (int i = 0; i < 3; ++i) ndv = ndv + q.n[i] * rel[i];
+		const double cr[3] = {q.n[1] * rel[2] - q.n[2] * rel[1], q.n[2] * rel[0] - q.n[0] * rel[2],
+							  q.n[0] * rel[1] - q.n[1] * rel[0]};
+		for (int i = 0; i < 3; ++i) un[i] = rel[i] * q.c + cr[i] * q.s + q.n[i] * ndv * (1 - q.c);
+	}
+	double u[3] = {0, 0, 0};
+	for (int i = 0; i < D; ++i) u[i] = un[i] + v.vcom[i];
+	return mask_sample_f64(v.vmask_d, D, v.vres, u) * q.R;
+}
+
+// solid_fraction_from_sdf (mask.hpp:291-311)
+__device__ inline double solid_f64(double sdf, double eps) {
+	const double half = eps / 2;
+	if (sdf <= -half) return 1;
+	if (sdf >= half) return 0;
+	const double t = (sdf + half) / eps;
+	const double c = cos(PI_D * t / 2);
+	return c * c;
+}
+
+// One thread per point: body b's signed distance at points[k] (3 doubles).
+__global__ void k_voxel_distance(PView v, const kel_particle_state *P, int b, const double *points, int n, double *out) {
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= n) return;
+	const VoxelPose q = voxel_pose(v.D, P[b]);
+	out[k] = voxel_sdf(v, q, points + 3 * (int64_t)k);
+}
+
+constexpr int VT = 128; // threads per pair of the voxel contact
+
+// Fixed-order block sum of NQ doubles per thread (warp tree, then warps in
+// order) into out (every thread receives it).  red: VT / 32 x NQ scratch.
+template <int NQ>
+__device__ inline void voxel_block_sum(double *vals, double (*red)[NQ], double *out) {
+	const int tid = threadIdx.x;
+#pragma unroll
+	for (int j = 0; j < NQ; ++j) {
+		double s = vals[j];
+		for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+		if ((tid & 31) == 0) red[tid >> 5][j] = s;
+	}
+	__syncthreads();
+#pragma unroll
+	for (int j = 0; j < NQ; ++j) {
+		double t = 0.0;
+		for (int w = 0; w < VT / 32; ++w) t += red[w][j];
+		out[j] = t;
+	}
+	__syncthreads();
+}
+
+// voxel_contact (voxel_narrow.hpp:78-259) of pair blockIdx.x, one block per
+// pair.  The cells of the clamped intersection of the two bounding boxes are
+// spread over the block (axis 0 outermost in the flat index); the overlap
+// volume, centroid and weighted gradient difference are summed per thread
+// and then in a fixed order that does not depend on which body is lo (the
+// terms for (hi, lo) are the exact negations), so swapping a pair negates the
+// normal exactly.  The depth's extent is a min / max (exact).
+__global__ void __launch_bounds__(VT) k_voxel_contact(PView v, const kel_particle_state *P, const int *pairs,
+													  double eps, kel_contact_manifold *out) {
+	__shared__ double red[VT / 32][7];
+	__shared__ double nrm[3];
+	__shared__ int any_s;
+	const int D = v.D, tid = threadIdx.x;
+	const kel_particle_state &lo = P[pairs[2 * blockIdx.x]], &hi = P[pairs[2 * blockIdx.x + 1]];
+	kel_contact_manifold res;
+	memset(&res, 0, sizeof(res));
+	int64_t start[3] = {0, 0, 0}, stop[3] = {1, 1, 1};
+	const int64_t ext[3] = {v.nx, v.ny, v.nz};
+	for (int i = 0; i < D; ++i) {
+		const double a_lo = lo.position[i] - lo.radius, a_hi = hi.position[i] - hi.radius;
+		double a = a_lo > a_hi ? a_lo : a_hi;
+		const double b_lo = lo.position[i] + lo.radius, b_hi = hi.position[i] + hi.radius;
+		const double b = b_lo < b_hi ? b_lo : b_hi;
+		if (a < 0) a = 0;
+		int64_t ai = (int64_t)floor(a);
+		int64_t bi = (int64_t)ceil(b) + 1;
+		if (ai < 0) ai = 0;
+		if (bi > ext[i]) bi = ext[i];
+		if (bi <= ai) { // uniform over the block
+			if (tid == 0) out[blockIdx.x] = res;
+			return;
+		}
+		start[i] = ai;
+		stop[i] = bi;
+	}
+	const int64_t e1 = stop[1] - start[1], e2 = stop[2] - start[2];
+	const int64_t ncell = (stop[0] - start[0]) * e1 * e2;
+	const VoxelPose ql = voxel_pose(D, lo), qh = voxel_pose(D, hi);
+	const double h = 0.5;
+	double acc[7] = {0, 0, 0, 0, 0, 0, 0}; // volume, centroid[3], grad[3]
+	for (int64_t k = tid; k < ncell; k += VT) {
+		const double x[3] = {(double)(start[0] + k / (e1 * e2)), (double)(start[1] + (k / e2) % e1),
+							 D == 3 ? (double)(start[2] + k % e2) : 0.0};
+		const double s_lo = solid_f64(voxel_sdf(v, ql, x), eps);
+		if (!(s_lo > 0)) continue;
+		const double s_hi = solid_f64(voxel_sdf(v, qh, x), eps);
+		if (!(s_hi > 0)) continue;
+		const double w = s_lo * s_hi;
+		acc[0] += w;
+		for (int i = 0; i < D; ++i) acc[1 + i] = acc[1 + i] + w * x[i];
+		for (int i = 0; i < D; ++i) { // impl::sdf_gradient by central differences, both bodies
+			double xl[3] = {x[0], x[1], x[2]}, xh[3] = {x[0], x[1], x[2]};
+			xl[i] = x[i] - h;
+			xh[i] = x[i] + h;
+			const double g_lo = (voxel_sdf(v, ql, xh) - voxel_sdf(v, ql, xl)) / (2 * h);
+			const double g_hi = (voxel_sdf(v, qh, xh) - voxel_sdf(v, qh, xl)) / (2 * h);
+			acc[4 + i] = acc[4 + i] + w * (g_hi - g_lo);
+		}
+	}
+	double tot[7];
+	voxel_block_sum<7>(acc, red, tot);
+	if (!(tot[0] > 0)) {
+		if (tid == 0) out[blockIdx.x] = res;
+		return;
+	}
+	if (tid == 0) {
+		double n[3] = {0, 0, 0}, g[3] = {tot[4], tot[5], tot[6]};
+		if (!safe_normalize(D, g, n)) {
+			double fb[3] = {0, 0, 0};
+			for (int i = 0; i < D; ++i) fb[i] = lo.position[i] - hi.position[i];
+			if (!safe_normalize(D, fb, n)) {
+				n[0] = 1.0;
+				n[1] = n[2] = 0.0;
+			}
+		}
+		for (int i = 0; i < 3; ++i) nrm[i] = n[i];
+		any_s = 0;
+	}
+	__syncthreads();
+	double s_min = INFINITY, s_max = -INFINITY;
+	int any = 0;
+	for (int64_t k = tid; k < ncell; k += VT) {
+		const double x[3] = {(double)(start[0] + k / (e1 * e2)), (double)(start[1] + (k / e2) % e1),
+							 D == 3 ? (double)(start[2] + k % e2) : 0.0};
+		if (!(solid_f64(voxel_sdf(v, ql, x), eps) > 0.5)) continue;
+		if (!(solid_f64(voxel_sdf(v, qh, x), eps) > 0.5)) continue;
+		double s = 0;
+		for (int i = 0; i < D; ++i) s = s + x[i] * nrm[i];
+		any = 1;
+		s_min = fmin(s_min, s);
+		s_max = fmax(s_max, s);
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		s_min = fmin(s_min, __shfl_down_sync(0xffffffffu, s_min, o));
+		s_max = fmax(s_max, __shfl_down_sync(0xffffffffu, s_max, o));
+		any |= __shfl_down_sync(0xffffffffu, any, o);
+	}
+	if ((tid & 31) == 0) {
+		red[tid >> 5][0] = s_min;
+		red[tid >> 5][1] = s_max;
+		if (any) atomicOr(&any_s, 1);
+	}
+	__syncthreads();
+	if (tid != 0) return;
+	for (int w = 0; w < VT / 32; ++w) {
+		s_min = fmin(s_min, red[w][0]);
+		s_max = fmax(s_max, red[w][1]);
+	}
+	double depth = any_s ? (s_max - s_min + 1.0) : 1.0;
+	const double cap = lo.radius < hi.radius ? lo.radius : hi.radius;
+	if (depth > cap) depth = cap;
+	res.hit = 1;
+	res.depth = depth;
+	for (int i = 0; i < D; ++i) {
+		res.normal[i] = nrm[i];
+		res.point[i] = tot[1 + i] / tot[0];
+	}
+	out[blockIdx.x] = res;
 }
 
 PView make_view(kel_lattice *L) {
@@ -1341,13 +1826,64 @@ PView make_view(kel_lattice *L) {
 	v.rho = L->rho;
 	v.mom = L->u;
 	for (int i = 0; i < 27; ++i) v.wshift[i] = L->wshift[i];
+	v.box_mul = 1.0;
+	v.box_add = 0.0;
+	return v;
+}
+
+// Growth of the bodies' boxes for a porosity mode: voxel bodies reach
+// R * reach + eps / 2 (the shape's extent and half the ramp).
+void box_growth(const kel_particles *ps, const kel_particle_params *prm, double *mul, double *add) {
+	*mul = 1.0;
+	*add = 0.0;
+	if (prm->porosity_mode == KEL_POROSITY_VOXEL && ps->shape) {
+		*mul = ps->shape->reach;
+		*add = prm->eps / 2;
+	}
+}
+
+// Sub-cell and voxel factors without the FP64 nearest-image / shortcut test
+// (body_factor's direct mode): every body box narrower than half the
+// periodic length (boxes span at most 2 ceil(radius) + 4 cells), so that the
+// image of a cell in a box is its nearest.
+int direct_mode(const kel_particles *ps, const kel_particle_params *prm) {
+	if (prm->porosity_mode == KEL_POROSITY_RAMP) return 0;
+	const kel_lattice *L = ps->lat;
+	if (!(L->desc.flags & KEL_LATTICE_PERIODIC_X)) return 1;
+	double mul, add;
+	box_growth(ps, prm, &mul, &add);
+	return 2.0 * (ceil(ps->max_radius * mul + add) + 3.0) < 0.5 * (double)L->desc.nx ? 1 : 0;
+}
+
+// The particle passes' view: the lattice's plus the box growth, the direct
+// flag and (voxel mode) the shape.
+PView particle_view(kel_particles *ps, const kel_particle_params *prm) {
+	PView v = make_view(ps->lat);
+	box_growth(ps, prm, &v.box_mul, &v.box_add);
+	v.direct = direct_mode(ps, prm);
+	if (prm->porosity_mode == KEL_POROSITY_VOXEL && ps->shape) {
+		const kel_shape *sh = ps->shape;
+		v.vmask_f = sh->d_mask_f;
+		v.vmask_d = sh->d_mask_d;
+		v.vres = sh->res;
+		for (int i = 0; i < 3; ++i) {
+			v.vcom[i] = sh->com[i];
+			v.vcom_f[i] = (float)sh->com[i];
+		}
+	}
 	return v;
 }
 
 int check_params(const kel_particles *ps, const kel_particle_params *prm, const char *who) {
 	if (!ps || !prm) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: null argument", who);
-	if (prm->porosity_mode != KEL_POROSITY_RAMP && prm->porosity_mode != KEL_POROSITY_SUBCELL)
+	if (prm->porosity_mode < KEL_POROSITY_RAMP || prm->porosity_mode > KEL_POROSITY_VOXEL)
 		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: unknown porosity mode %d", who, prm->porosity_mode);
+	if (prm->porosity_mode == KEL_POROSITY_VOXEL) {
+		if (prm->coupling != KEL_COUPLING_PSM)
+			return fail(KEL_ERR_UNSUPPORTED, "%s: voxel porosity goes with PSM coupling", who);
+		if (!ps->shape) return fail(KEL_ERR_STATE, "%s: voxel porosity needs a shape (kel_particles_set_shape)", who);
+		if (!(prm->eps > 0)) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: eps must be positive", who);
+	}
 	if (prm->sub_steps < 0) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: negative sub_steps", who);
 	if ((prm->porosity_mode == KEL_POROSITY_RAMP || prm->coupling == KEL_COUPLING_HLBM) && !(prm->eps > 0))
 		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: eps must be positive", who);
@@ -1374,21 +1910,24 @@ int check_params(const kel_particles *ps, const kel_particle_params *prm, const 
 // ---------------------------------------------------------------------------
 // C ABI
 
-// Cells of a body's box per axis, at most: 2 r + 2 (ramp) or 2 r + 3 (sub-cell)
-static int64_t box_cells_max(const kel_particles *ps) {
-	const int64_t e = 2 * (int64_t)ceil(ps->max_radius) + 4;
+// Cells of a body's box per axis, at most: 2 r + 2 (ramp) or 2 r + 3
+// (sub-cell and voxel, r grown by box_growth)
+static int64_t box_cells_max(const kel_particles *ps, const kel_particle_params *prm) {
+	double mul, add;
+	box_growth(ps, prm, &mul, &add);
+	const int64_t e = 2 * (int64_t)ceil(ps->max_radius * mul + add) + 4;
 	return ps->lat->d.D == 3 ? e * e * e : e * e;
 }
 
 // Blocks per body of the gather: about one thread per box cell, 1 .. 64.
-static int gather_blocks(const kel_particles *ps) {
-	const int64_t g = (box_cells_max(ps) + GT - 1) / GT;
+static int gather_blocks(const kel_particles *ps, const kel_particle_params *prm) {
+	const int64_t g = (box_cells_max(ps, prm) + GT - 1) / GT;
 	return (int)(g < 1 ? 1 : (g > 64 ? 64 : g));
 }
 
 // Blocks per body of the region couple (two boxes, RC_CPT cells per thread).
-static int couple_blocks(const kel_particles *ps) {
-	const int64_t g = (2 * box_cells_max(ps) + RT * RC_CPT - 1) / (RT * RC_CPT);
+static int couple_blocks(const kel_particles *ps, const kel_particle_params *prm) {
+	const int64_t g = (2 * box_cells_max(ps, prm) + RT * RC_CPT - 1) / (RT * RC_CPT);
 	return (int)(g < 1 ? 1 : (g > 64 ? 64 : g));
 }
 
@@ -1401,9 +1940,11 @@ extern "C" int kel_particles_create(kel_lattice *lat, int32_t count, kel_particl
 	cudaError_t e = cudaMalloc(&ps->d, sizeof(kel_particle_state) * count);
 	if (e == cudaSuccess) e = cudaMalloc(&ps->d_alt, sizeof(kel_particle_state) * count);
 	if (e == cudaSuccess) e = cudaMalloc(&ps->boxes, sizeof(BodyBox) * 2 * (size_t)count);
+	if (e == cudaSuccess) e = cudaMalloc(&ps->rec, sizeof(CoupleRec) * (size_t)count);
 	if (e != cudaSuccess) {
 		cudaFree(ps->d);
 		cudaFree(ps->d_alt);
+		cudaFree(ps->boxes);
 		delete ps;
 		return fail(e == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA, "kel_particles_create: %s",
 					cudaGetErrorString(e));
@@ -1414,6 +1955,7 @@ extern "C" int kel_particles_create(kel_lattice *lat, int32_t count, kel_particl
 		cudaFree(ps->d);
 		cudaFree(ps->d_alt);
 		cudaFree(ps->boxes);
+		cudaFree(ps->rec);
 		delete ps;
 		return rc;
 	}
@@ -1432,6 +1974,7 @@ extern "C" int kel_particles_destroy(kel_particles *ps) {
 	cudaFree(ps->d_alt);
 	cudaFree(ps->cell_force);
 	cudaFree(ps->boxes);
+	cudaFree(ps->rec);
 	cudaFree(ps->partial);
 	delete ps;
 	return KEL_OK;
@@ -1510,20 +2053,23 @@ static int particles_couple(kel_particles *ps, const kel_particle_params *prm, b
 		ps->prev_is_last = ps->cur_fresh = false;
 		return particles_hlbm_couple(ps, prm, false);
 	}
-	PView v = make_view(L);
-	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
+	PView v = particle_view(ps, prm);
+	const int mode = prm->porosity_mode;
 	const bool incremental = ps->epoch != 0 && ps->epoch == L->por_epoch;
 	// after the fused contact + integrate, the boxes are ready and nothing
 	// needs resetting: no launch
-	const bool ready = incremental && ps->prev_is_last && ps->cur_fresh && ps->cur_sub == sub && !reset;
+	const bool ready = incremental && ps->prev_is_last && ps->cur_fresh && ps->cur_mode == mode &&
+					   ps->cur_eps == prm->eps && !reset;
 	if (!ready)
-		k_pre<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, sub, cur_boxes(ps), prev_boxes(ps), 1,
-														   incremental && !ps->prev_is_last ? 1 : 0, reset ? 1 : 0);
+		k_pre<<<(ps->n + 127) / 128, 128, 0, L->stream>>>(v, ps->d, ps->n, mode != KEL_POROSITY_RAMP, cur_boxes(ps),
+														   prev_boxes(ps), 1, incremental && !ps->prev_is_last ? 1 : 0,
+														   reset ? 1 : 0);
 	ps->prev_is_last = false;
 	ps->cur_fresh = true;
-	ps->cur_sub = sub;
+	ps->cur_mode = mode;
+	ps->cur_eps = prm->eps;
 	if (incremental)
-		k_couple_regions<<<dim3((unsigned)ps->n, (unsigned)couple_blocks(ps)), RT, 0, L->stream>>>(
+		k_couple_regions<<<dim3((unsigned)ps->n, (unsigned)couple_blocks(ps, prm)), RT, 0, L->stream>>>(
 			v, ps->d, cur_boxes(ps), prev_boxes(ps), ps->n, prm->porosity_mode, prm->eps);
 	else
 		k_couple<<<cell_grid(L), dim3(TX, TY), 0, L->stream>>>(v, ps->d, cur_boxes(ps), ps->n, prm->porosity_mode,
@@ -1563,8 +2109,8 @@ static void launch_gather(const PView &v, kel_particles *ps, int steps, int mode
 // contact pass adds them.
 static int particles_gather(kel_particles *ps, const kel_particle_params *prm, bool want_cell_force, bool finish) {
 	kel_lattice *L = ps->lat;
-	PView v = make_view(L);
-	const int G = gather_blocks(ps);
+	PView v = particle_view(ps, prm);
+	const int G = gather_blocks(ps, prm);
 	int rc;
 	if ((rc = ensure_partials(ps, G))) return rc;
 	ps->gather_g = G;
@@ -1625,7 +2171,7 @@ static int particles_fplbm_couple(kel_particles *ps, const kel_particle_params *
 // then (set_accel) its acceleration and (verlet) the Verlet sub-steps.
 static int particles_fplbm_gather(kel_particles *ps, const kel_particle_params *prm, bool verlet) {
 	kel_lattice *L = ps->lat;
-	const int G = gather_blocks(ps);
+	const int G = gather_blocks(ps, prm);
 	int rc;
 	if ((rc = ensure_partials(ps, G))) return rc;
 	ps->gather_g = G;
@@ -1661,7 +2207,8 @@ static int particles_integrate(kel_particles *ps, const kel_particle_params *prm
 template <class Lc, int STORE>
 static void launch_couple_gather(const PView &v, kel_particles *ps, const kel_particle_params *prm, int G) {
 	k_couple_gather<Lc, STORE><<<dim3((unsigned)ps->n, (unsigned)G), RT, 0, ps->lat->stream>>>(
-		v, ps->d, cur_boxes(ps), prev_boxes(ps), ps->n, prm->porosity_mode, prm->eps, prm->sub_steps, ps->partial);
+		v, ps->d, cur_boxes(ps), prev_boxes(ps), ps->n, prm->porosity_mode, prm->eps,
+		static_cast<const CoupleRec *>(ps->rec), ps->partial);
 }
 
 // Couple and gather of a coupled PSM step in one launch, when the couple is
@@ -1669,13 +2216,15 @@ static void launch_couple_gather(const PView &v, kel_particles *ps, const kel_pa
 static int particles_couple_gather(kel_particles *ps, const kel_particle_params *prm, bool *done) {
 	*done = false;
 	kel_lattice *L = ps->lat;
-	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
+	const int mode = prm->porosity_mode;
 	const bool incremental = ps->epoch != 0 && ps->epoch == L->por_epoch;
-	if (!(incremental && ps->prev_is_last && ps->cur_fresh && ps->cur_sub == sub)) return KEL_OK;
-	const int G = couple_blocks(ps);
+	if (!(incremental && ps->prev_is_last && ps->cur_fresh && ps->cur_mode == mode && ps->cur_eps == prm->eps))
+		return KEL_OK;
+	if (!(ps->rec_mode == mode && ps->rec_steps == prm->sub_steps && ps->rec_eps == prm->eps)) return KEL_OK;
+	const int G = couple_blocks(ps, prm);
 	int rc;
 	if ((rc = ensure_partials(ps, G))) return rc;
-	const PView v = make_view(L);
+	const PView v = particle_view(ps, prm);
 	const bool f32 = L->desc.storage == KEL_STORAGE_FP32;
 	switch (L->d.Q) {
 	case 9: f32 ? launch_couple_gather<D2Q9, STORE_FP32>(v, ps, prm, G) : launch_couple_gather<D2Q9, STORE_FP16S>(v, ps, prm, G); break;
@@ -1686,7 +2235,6 @@ static int particles_couple_gather(kel_particles *ps, const kel_particle_params 
 	ps->gather_g = G;
 	ps->prev_is_last = false;
 	ps->cur_fresh = true;
-	ps->cur_sub = sub;
 	ps->epoch = ++L->por_epoch;
 	*done = true;
 	return KEL_OK;
@@ -1698,17 +2246,30 @@ static int particles_couple_gather(kel_particles *ps, const kel_particle_params 
 // one.
 static int particles_contact_integrate(kel_particles *ps, const kel_particle_params *prm, cudaStream_t st) {
 	kel_lattice *L = ps->lat;
-	const int sub = prm->porosity_mode == KEL_POROSITY_SUBCELL;
-	const PView v = make_view(L);
-	k_contact_integrate<<<ps->n, 32, 0, st>>>(ps->d, ps->d_alt, v, *prm, ps->partial, ps->gather_g, cur_boxes(ps),
-											  prev_boxes(ps), sub);
+	const PView v = particle_view(ps, prm);
+	const int cm = couple_mode(prm->porosity_mode, v.direct);
+	const double reach = (cm == 1 || cm == 2) ? subcell_reach(L->d.D) : 0.0;
+	CoupleRec *rec = static_cast<CoupleRec *>(ps->rec);
+#define KEL_CI(Lc)                                                                                                     \
+	k_contact_integrate<Lc><<<ps->n, 32, 0, st>>>(ps->d, ps->d_alt, v, *prm, ps->partial, ps->gather_g, cur_boxes(ps),  \
+												  prev_boxes(ps), cm, reach, rec)
+	switch (L->d.Q) {
+	case 9: KEL_CI(D2Q9); break;
+	case 19: KEL_CI(D3Q19); break;
+	default: KEL_CI(D3Q27); break;
+	}
+#undef KEL_CI
 	KEL_CUDA(cudaGetLastError());
+	ps->rec_mode = prm->porosity_mode;
+	ps->rec_steps = prm->sub_steps;
+	ps->rec_eps = prm->eps;
 	kel_particle_state *t = ps->d; // the bodies' new state is in the other buffer
 	ps->d = ps->d_alt;
 	ps->d_alt = t;
 	ps->prev_is_last = true;
 	ps->cur_fresh = true;
-	ps->cur_sub = sub;
+	ps->cur_mode = prm->porosity_mode;
+	ps->cur_eps = prm->eps;
 	return KEL_OK;
 }
 
@@ -1839,9 +2400,12 @@ static ParticleGraphKey graph_key(kel_particles *ps, const kel_particle_params *
 	k.bodies = ps->d;
 	k.boxes = ps->boxes;
 	k.partial = ps->partial;
+	k.rec = ps->rec;
+	k.direct = direct_mode(ps, prm);
+	k.shape = ps->shape;
 	k.n = ps->n;
-	k.gather_g = gather_blocks(ps);
-	k.couple_g = couple_blocks(ps);
+	k.gather_g = gather_blocks(ps, prm);
+	k.couple_g = couple_blocks(ps, prm);
 	k.cpt = L->cpt;
 	k.block = L->block;
 	return k;
@@ -1854,7 +2418,7 @@ static ParticleGraphKey graph_key(kel_particles *ps, const kel_particle_params *
 static int ensure_particle_graph(kel_particles *ps, const kel_particle_params *prm, const kel_step_program *prog) {
 	kel_lattice *L = ps->lat;
 	int rc;
-	const int gmax = gather_blocks(ps) > couple_blocks(ps) ? gather_blocks(ps) : couple_blocks(ps);
+	const int gmax = gather_blocks(ps, prm) > couple_blocks(ps, prm) ? gather_blocks(ps, prm) : couple_blocks(ps, prm);
 	if ((rc = ensure_partials(ps, gmax))) return rc; // no allocation inside the capture
 	if (!ps->side) {
 		KEL_CUDA(cudaStreamCreateWithFlags(&ps->side, cudaStreamNonBlocking));
@@ -1867,7 +2431,8 @@ static int ensure_particle_graph(kel_particles *ps, const kel_particle_params *p
 	ps->graph = nullptr;
 	const uint64_t t0 = L->t, e0 = L->por_epoch, pe0 = ps->epoch;
 	const bool pl0 = ps->prev_is_last, cf0 = ps->cur_fresh;
-	const int cs0 = ps->cur_sub;
+	const int cm0 = ps->cur_mode;
+	const double ce0 = ps->cur_eps;
 	if (cudaStreamBeginCapture(L->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
 		cudaGetLastError();
 		return KEL_ERR_CUDA;
@@ -1881,7 +2446,8 @@ static int ensure_particle_graph(kel_particles *ps, const kel_particle_params *p
 	ps->epoch = pe0;
 	ps->prev_is_last = pl0;
 	ps->cur_fresh = cf0;
-	ps->cur_sub = cs0;
+	ps->cur_mode = cm0;
+	ps->cur_eps = ce0;
 	if (rc == KEL_OK && e == cudaSuccess && g) e = cudaGraphInstantiate(&ps->graph, g, 0);
 	if (g) cudaGraphDestroy(g);
 	if (rc != KEL_OK || e != cudaSuccess || !ps->graph) {
@@ -1942,5 +2508,238 @@ extern "C" int kel_particles_step(kel_particles *ps, const kel_particle_params *
 			if ((rc = coupled_step(ps, prm, prog, fl))) return rc;
 		}
 	}
+	return KEL_OK;
+}
+
+// ---- voxel shapes ------------------------------------------------------------
+
+namespace {
+
+// solid_fraction_from_sdf (mask.hpp:291-311) on the host
+double solid_host(double sdf, double eps) {
+	const double half = eps / 2;
+	if (sdf <= -half) return 1;
+	if (sdf >= half) return 0;
+	const double t = (sdf + half) / eps;
+	const double c = std::cos(PI_D * t / 2);
+	return c * c;
+}
+
+// Voxel k (flat, last axis fastest) -> normalised local position
+// (mask_voxel_to_local, mask.hpp:111-125).
+void voxel_local(int D, int R, int64_t k, double *u) {
+	const double step = 2.0 / (double)R;
+	int64_t idx[3] = {0, 0, 0};
+	for (int i = D - 1; i >= 0; --i) {
+		idx[i] = k % R;
+		k /= R;
+	}
+	for (int i = 0; i < D; ++i) u[i] = -1 + ((double)idx[i] + 0.5) * step;
+}
+
+int64_t voxel_count(int D, int R) { return D == 3 ? (int64_t)R * R * R : (int64_t)R * R; }
+
+// The largest |u| over the voxels at distance <= 0, plus one voxel diagonal.
+double mask_reach(const kel_shape *sh) {
+	double best = -1.0;
+	const int64_t n = voxel_count(sh->dim, sh->res);
+	for (int64_t k = 0; k < n; ++k) {
+		if (!(sh->mask[k] <= 0.0)) continue;
+		double u[3] = {0, 0, 0};
+		voxel_local(sh->dim, sh->res, k, u);
+		double s = 0;
+		for (int i = 0; i < sh->dim; ++i) s = s + u[i] * u[i];
+		s = std::sqrt(s);
+		if (s > best) best = s;
+	}
+	return best < 0 ? 0.0 : best + (2.0 / (double)sh->res) * std::sqrt((double)sh->dim);
+}
+
+int shape_upload(kel_shape *sh) {
+	const int64_t n = voxel_count(sh->dim, sh->res);
+	std::vector<float> mf((size_t)n);
+	for (int64_t k = 0; k < n; ++k) mf[k] = (float)sh->mask[k];
+	cudaError_t e = cudaMalloc(&sh->d_mask_f, sizeof(float) * n);
+	if (e == cudaSuccess) e = cudaMalloc(&sh->d_mask_d, sizeof(double) * n);
+	if (e == cudaSuccess) e = cudaMemcpy(sh->d_mask_f, mf.data(), sizeof(float) * n, cudaMemcpyHostToDevice);
+	if (e == cudaSuccess) e = cudaMemcpy(sh->d_mask_d, sh->mask.data(), sizeof(double) * n, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess)
+		return fail(e == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA, "kel_shape: %s",
+					cudaGetErrorString(e));
+	sh->reach = mask_reach(sh);
+	return KEL_OK;
+}
+
+int shape_args(int32_t dim, int32_t resolution, kel_shape **out, const char *who) {
+	if (!out) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: null argument", who);
+	*out = nullptr;
+	if (dim != 2 && dim != 3) return fail(KEL_ERR_INVALID_ARGUMENT, "%s: dimension %d", who, dim);
+	if (resolution < 2 || resolution > (dim == 2 ? 4096 : 512))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "%s: resolution %d", who, resolution);
+	return KEL_OK;
+}
+
+} // namespace
+
+extern "C" int kel_shape_create(int32_t dim, int32_t resolution, int32_t kind, kel_shape **out) {
+	int rc = shape_args(dim, resolution, out, "kel_shape_create");
+	if (rc) return rc;
+	if (kind != KEL_SHAPE_SPHERE && kind != KEL_SHAPE_CUBE)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_shape_create: unknown shape %d", kind);
+	kel_shape *sh = new kel_shape();
+	sh->dim = dim;
+	sh->res = resolution;
+	const int64_t n = voxel_count(dim, resolution);
+	sh->mask.resize((size_t)n);
+	// fill_mask_from_sdf (mask.hpp:351-394): voxels in iteration order, the
+	// centroid weighted by a one-voxel ramp
+	const double step = 2.0 / (double)resolution;
+	double wsum = 0, c[3] = {0, 0, 0};
+	for (int64_t k = 0; k < n; ++k) {
+		double u[3] = {0, 0, 0};
+		voxel_local(dim, resolution, k, u);
+		double d;
+		if (kind == KEL_SHAPE_CUBE) { // sdf::cube (mask.hpp:328-340)
+			double m = 0;
+			for (int i = 0; i < dim; ++i) {
+				const double a = std::fabs(u[i]);
+				if (a > m) m = a;
+			}
+			d = m - 1;
+		} else { // sdf::sphere (mask.hpp:317-322)
+			double q = 0;
+			for (int i = 0; i < dim; ++i) q = q + u[i] * u[i];
+			d = std::sqrt(q) - 1;
+		}
+		sh->mask[k] = d;
+		const double w = solid_host(d, step);
+		wsum += w;
+		for (int i = 0; i < dim; ++i) c[i] = c[i] + w * u[i];
+	}
+	if (wsum > 0)
+		for (int i = 0; i < dim; ++i) c[i] = c[i] / wsum;
+	for (int i = 0; i < 3; ++i) sh->com[i] = i < dim ? c[i] : 0.0;
+	if ((rc = shape_upload(sh))) {
+		kel_shape_destroy(sh);
+		return rc;
+	}
+	*out = sh;
+	return KEL_OK;
+}
+
+extern "C" int kel_shape_create_from_mask(int32_t dim, int32_t resolution, const double *mask,
+										  const double *center_of_mass, kel_shape **out) {
+	int rc = shape_args(dim, resolution, out, "kel_shape_create_from_mask");
+	if (rc) return rc;
+	if (!mask || !center_of_mass) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_shape_create_from_mask: null argument");
+	const int64_t n = voxel_count(dim, resolution);
+	for (int64_t k = 0; k < n; ++k)
+		if (!std::isfinite(mask[k]))
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_shape_create_from_mask: voxel %lld is not finite", (long long)k);
+	kel_shape *sh = new kel_shape();
+	sh->dim = dim;
+	sh->res = resolution;
+	sh->mask.assign(mask, mask + n);
+	for (int i = 0; i < 3; ++i) sh->com[i] = i < dim ? center_of_mass[i] : 0.0;
+	if ((rc = shape_upload(sh))) {
+		kel_shape_destroy(sh);
+		return rc;
+	}
+	*out = sh;
+	return KEL_OK;
+}
+
+extern "C" int kel_shape_info(const kel_shape *shape, double *mask, double *center_of_mass, double *reach) {
+	if (!shape) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_shape_info: null shape");
+	if (mask) std::memcpy(mask, shape->mask.data(), sizeof(double) * shape->mask.size());
+	if (center_of_mass)
+		for (int i = 0; i < 3; ++i) center_of_mass[i] = shape->com[i];
+	if (reach) *reach = shape->reach;
+	return KEL_OK;
+}
+
+extern "C" int kel_shape_destroy(kel_shape *shape) {
+	if (!shape) return KEL_OK;
+	cudaFree(shape->d_mask_f);
+	cudaFree(shape->d_mask_d);
+	delete shape;
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_set_shape(kel_particles *ps, const kel_shape *shape) {
+	if (!ps) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_set_shape: null particles");
+	if (shape && shape->dim != ps->lat->d.D)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_set_shape: %dD shape on a %dD lattice", shape->dim,
+					ps->lat->d.D);
+	KEL_CUDA(cudaStreamSynchronize(ps->lat->stream));
+	ps->shape = shape;
+	ps->cur_fresh = false; // voxel boxes depend on the shape's reach
+	ps->rec_mode = -1;
+	return KEL_OK;
+}
+
+static PView voxel_view(kel_particles *ps) {
+	kel_particle_params prm;
+	std::memset(&prm, 0, sizeof(prm));
+	prm.porosity_mode = KEL_POROSITY_VOXEL;
+	prm.eps = 1.0;
+	return particle_view(ps, &prm);
+}
+
+extern "C" int kel_particles_voxel_distance(kel_particles *ps, int32_t body, const double *points, int32_t n,
+											double *out) {
+	if (!ps || (!points && n > 0) || (!out && n > 0) || n < 0)
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_voxel_distance: bad arguments");
+	if (body < 0 || body >= ps->n) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_voxel_distance: body %d", body);
+	if (!ps->shape) return fail(KEL_ERR_STATE, "kel_particles_voxel_distance: no shape set");
+	if (n == 0) return KEL_OK;
+	kel_lattice *L = ps->lat;
+	const int D = L->d.D;
+	std::vector<double> p3((size_t)n * 3, 0.0);
+	for (int32_t k = 0; k < n; ++k)
+		for (int i = 0; i < D; ++i) p3[(size_t)k * 3 + i] = points[(size_t)k * D + i];
+	double *d_buf = nullptr;
+	KEL_CUDA(cudaMalloc(&d_buf, sizeof(double) * 4 * (size_t)n));
+	cudaError_t e = cudaMemcpyAsync(d_buf, p3.data(), sizeof(double) * 3 * (size_t)n, cudaMemcpyHostToDevice, L->stream);
+	if (e == cudaSuccess) {
+		k_voxel_distance<<<(n + 127) / 128, 128, 0, L->stream>>>(voxel_view(ps), ps->d, body, d_buf, n, d_buf + 3 * (size_t)n);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(out, d_buf + 3 * (size_t)n, sizeof(double) * n, cudaMemcpyDeviceToHost, L->stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+	cudaFree(d_buf);
+	if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_particles_voxel_distance: %s", cudaGetErrorString(e));
+	return KEL_OK;
+}
+
+extern "C" int kel_particles_voxel_contact(kel_particles *ps, const int32_t *pairs, int32_t npairs, double eps,
+										   kel_contact_manifold *out) {
+	if (!ps || npairs < 0 || (npairs > 0 && (!pairs || !out)))
+		return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_voxel_contact: bad arguments");
+	if (!(eps > 0)) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_voxel_contact: eps must be positive");
+	if (!ps->shape) return fail(KEL_ERR_STATE, "kel_particles_voxel_contact: no shape set");
+	for (int32_t k = 0; k < 2 * npairs; ++k)
+		if (pairs[k] < 0 || pairs[k] >= ps->n)
+			return fail(KEL_ERR_INVALID_ARGUMENT, "kel_particles_voxel_contact: body index %d", pairs[k]);
+	if (npairs == 0) return KEL_OK;
+	kel_lattice *L = ps->lat;
+	int *d_pairs = nullptr;
+	kel_contact_manifold *d_out = nullptr;
+	cudaError_t e = cudaMalloc(&d_pairs, sizeof(int) * 2 * (size_t)npairs);
+	if (e == cudaSuccess) e = cudaMalloc(&d_out, sizeof(kel_contact_manifold) * (size_t)npairs);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(d_pairs, pairs, sizeof(int) * 2 * (size_t)npairs, cudaMemcpyHostToDevice, L->stream);
+	if (e == cudaSuccess) {
+		k_voxel_contact<<<npairs, VT, 0, L->stream>>>(voxel_view(ps), ps->d, d_pairs, eps, d_out);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(out, d_out, sizeof(kel_contact_manifold) * (size_t)npairs, cudaMemcpyDeviceToHost,
+							L->stream);
+	if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+	cudaFree(d_pairs);
+	cudaFree(d_out);
+	if (e != cudaSuccess) return fail(KEL_ERR_CUDA, "kel_particles_voxel_contact: %s", cudaGetErrorString(e));
 	return KEL_OK;
 }

@@ -374,6 +374,74 @@ class Particles:
         fl = K.KEL_STEP_WRITE_MACROS if write_macros else 0
         _check(self.lib.kel_particles_step(self._h, C.byref(params), C.byref(program), n_steps, fl), self.lib)
 
+    def set_shape(self, shape):
+        """The voxel shape every body takes (KEL_POROSITY_VOXEL, voxel queries); None detaches."""
+        self._shape = shape
+        _check(self.lib.kel_particles_set_shape(self._h, shape.handle if shape is not None else None), self.lib)
+
+    def voxel_distance(self, body, points):
+        """mask_signed_distance (particle/mask.hpp:270-282) of one body at lattice points, FP64 on the device."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, self.lat.D)
+        out = np.empty(pts.shape[0])
+        _check(self.lib.kel_particles_voxel_distance(self._h, int(body), _ptr(pts), pts.shape[0], _ptr(out)), self.lib)
+        return out
+
+    def voxel_contact(self, pairs, eps):
+        """voxel_contact (particle/voxel_narrow.hpp:78-259) of body pairs (lo, hi), FP64 on the device.
+        Returns (n, 8): hit, depth, normal[3], point[3]."""
+        pr = np.ascontiguousarray(pairs, dtype=np.int32).reshape(-1, 2)
+        out = (K.ContactManifold * pr.shape[0])()
+        _check(self.lib.kel_particles_voxel_contact(self._h, _ptr(pr), pr.shape[0], float(eps), out), self.lib)
+        return np.array([[m.hit, m.depth, *m.normal, *m.point] for m in out], dtype=np.float64).reshape(-1, 8)
+
+
+class Shape:
+    """A voxel signed-distance body shape (C ABI kel_shape_*; particle/mask.hpp):
+    ``Shape(dim, resolution, kind)`` fills a built-in sphere or cube mask
+    (fill_mask_from_sdf); ``Shape.from_mask(dim, resolution, mask, com)`` takes
+    a caller's R^D mask (last axis fastest)."""
+
+    def __init__(self, dim, resolution, kind=K.KEL_SHAPE_SPHERE, _mask=None, _com=None):
+        self.lib = K.load_library()
+        self.dim, self.resolution = int(dim), int(resolution)
+        h = C.c_void_p()
+        if _mask is None:
+            _check(self.lib.kel_shape_create(self.dim, self.resolution, int(kind), C.byref(h)), self.lib)
+        else:
+            m = np.ascontiguousarray(_mask, dtype=np.float64).reshape(-1)
+            c = np.zeros(3)
+            c[:len(_com)] = _com
+            _check(self.lib.kel_shape_create_from_mask(self.dim, self.resolution, _ptr(m), _ptr(c), C.byref(h)),
+                   self.lib)
+        self._h = h
+
+    @classmethod
+    def from_mask(cls, dim, resolution, mask, com):
+        return cls(dim, resolution, _mask=mask, _com=np.asarray(com, dtype=np.float64)[:dim])
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self):
+        """(mask (R^D doubles), center of mass (3), reach)."""
+        mask = np.empty(self.resolution ** self.dim)
+        com = np.empty(3)
+        reach = C.c_double()
+        _check(self.lib.kel_shape_info(self._h, _ptr(mask), _ptr(com), C.byref(reach)), self.lib)
+        return mask, com, reach.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self.lib.kel_shape_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 
 class Batch:
     """Many independent D2Q9 channels of uneven size in one launch

@@ -24,7 +24,7 @@ _lib = None
 def build(force: bool = False) -> str:
     """Compile the restatement with gcc (no FMA contraction, OpenMP)."""
     src = [os.path.join(HERE, "lbm_oracle.c"), os.path.join(HERE, "lbm_oracle_impl.h"),
-           os.path.join(HERE, "particles_oracle.c")]
+           os.path.join(HERE, "particles_oracle.c"), os.path.join(HERE, "voxel_oracle.c")]
     src = [s for s in src if os.path.exists(s)]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in src):
         return LIB
@@ -75,6 +75,23 @@ def lib():
         L.ko_fplbm_reset.argtypes = [vp, C.c_uint32]
         L.ko_fplbm_particles.argtypes = [vp, vp, C.c_int, vp, C.c_int]
         L.ko_get_force.argtypes = [vp, vp]
+        d = C.c_double
+        L.ko_solid_fraction.argtypes = [d, d]
+        L.ko_solid_fraction.restype = d
+        L.ko_mask_fill.argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
+        L.ko_mask_reach.argtypes = [C.c_int, C.c_int, vp]
+        L.ko_mask_reach.restype = d
+        L.ko_mask_sample_local.argtypes = [C.c_int, C.c_int, vp, vp]
+        L.ko_mask_sample_local.restype = d
+        L.ko_mask_local_to_global.argtypes = [C.c_int, vp, vp, vp, vp]
+        L.ko_mask_signed_distance.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp]
+        L.ko_mask_signed_distance.restype = d
+        L.ko_voxel_porosity.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, d]
+        L.ko_voxel_porosity.restype = d
+        L.ko_voxel_contact.argtypes = [C.c_int, C.c_int, vp, vp, vp, vp, vp, d, vp]
+        L.ko_voxel_contact.restype = C.c_int
+        L.ko_voxel_couple.argtypes = [C.c_int, C.c_int, vp, vp, d, vp, C.c_int, vp, C.c_int, d, vp]
+        L.ko_particles_set_voxel_box.argtypes = [d, d]
         _lib = L
     return _lib
 
@@ -227,3 +244,94 @@ def equilibrium_f32(q, rho, u):
     out = np.zeros(q, dtype=np.float32)
     lib().ko_equilibrium_f32(q, C.c_float(rho), _ptr(u3), _ptr(out))
     return out
+
+
+# ---- voxel signed-distance bodies (voxel_oracle.c) ----------------------------
+
+def voxel_states(bodies):
+    """(n, 7) rows of position[3], rotation[3], radius -> kel_particle_state array."""
+    from lbm_mirror_gb300 import capi as K
+    b = np.asarray(bodies, dtype=np.float64).reshape(-1, 7)
+    a = np.zeros((b.shape[0], 28))
+    a[:, 0:3] = b[:, 0:3]
+    a[:, 6:9] = b[:, 3:6]
+    a[:, 26] = b[:, 6]
+    return K.states_from_array(a)
+
+
+def solid_fraction(sdf, eps):
+    return lib().ko_solid_fraction(float(sdf), float(eps))
+
+
+def mask_fill(D, R, kind):
+    mask = np.zeros(R ** D)
+    com = np.zeros(3)
+    lib().ko_mask_fill(D, R, kind, _ptr(mask), _ptr(com))
+    return mask, com
+
+
+def mask_reach(D, R, mask):
+    m = np.ascontiguousarray(mask, dtype=np.float64)
+    return lib().ko_mask_reach(D, R, _ptr(m))
+
+
+def mask_sample_local(D, R, mask, u):
+    m = np.ascontiguousarray(mask, dtype=np.float64)
+    u3 = np.zeros(3)
+    u3[:D] = np.asarray(u)[:D]
+    return lib().ko_mask_sample_local(D, R, _ptr(m), _ptr(u3))
+
+
+def mask_local_to_global(D, state, com, u):
+    c = np.ascontiguousarray(com, dtype=np.float64)
+    u3 = np.zeros(3)
+    u3[:D] = np.asarray(u)[:D]
+    x = np.zeros(3)
+    lib().ko_mask_local_to_global(D, C.byref(state), _ptr(c), _ptr(u3), _ptr(x))
+    return x
+
+
+def mask_signed_distance(D, R, mask, com, state, x):
+    m = np.ascontiguousarray(mask, dtype=np.float64)
+    c = np.ascontiguousarray(com, dtype=np.float64)
+    x3 = np.zeros(3)
+    x3[:D] = np.asarray(x)[:D]
+    return lib().ko_mask_signed_distance(D, R, _ptr(m), _ptr(c), C.byref(state), _ptr(x3))
+
+
+def voxel_porosity(D, R, mask, com, state, x, eps):
+    m = np.ascontiguousarray(mask, dtype=np.float64)
+    c = np.ascontiguousarray(com, dtype=np.float64)
+    x3 = np.zeros(3)
+    x3[:D] = np.asarray(x)[:D]
+    return lib().ko_voxel_porosity(D, R, _ptr(m), _ptr(c), C.byref(state), _ptr(x3), float(eps))
+
+
+def voxel_contact(D, R, mask, com, lo, hi, extent, eps):
+    """Manifold of voxel_contact(lo, hi) as (hit, depth, normal[3], point[3])."""
+    from lbm_mirror_gb300 import capi as K
+    m = np.ascontiguousarray(mask, dtype=np.float64)
+    c = np.ascontiguousarray(com, dtype=np.float64)
+    ext = np.ones(3, dtype=np.int64)
+    ext[:len(extent)] = extent
+    out = K.ContactManifold()
+    hit = lib().ko_voxel_contact(D, R, _ptr(m), _ptr(c), C.byref(lo), C.byref(hi), _ptr(ext), float(eps),
+                                 C.byref(out))
+    return np.array([float(hit), out.depth, *out.normal, *out.point])
+
+
+def voxel_couple(D, R, mask, com, reach, states, extent, eps, periodic_x=False):
+    """Porosity field (x fastest) of the FP32 voxel couple."""
+    m = np.ascontiguousarray(mask, dtype=np.float64)
+    c = np.ascontiguousarray(com, dtype=np.float64)
+    ext = np.ones(3, dtype=np.int64)
+    ext[:len(extent)] = extent
+    por = np.zeros(int(np.prod(ext[:D])))
+    lib().ko_voxel_couple(D, R, _ptr(m), _ptr(c), float(reach), C.byref(states), len(states), _ptr(ext),
+                          int(periodic_x), float(eps), _ptr(por))
+    return por
+
+
+def particles_set_voxel_box(mul, add):
+    """Box growth of the gather for KEL_POROSITY_VOXEL bodies (radius * mul + add)."""
+    lib().ko_particles_set_voxel_box(float(mul), float(add))

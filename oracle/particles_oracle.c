@@ -106,11 +106,22 @@ static double rel_coord(double cell, double X, int periodic, int64_t n) {
 	return r;
 }
 
-/* aabb.hpp:41-84: [a, b) per axis; x unclamped when periodic (cells wrap). */
+/* Growth of the voxel bodies' boxes (KEL_POROSITY_VOXEL): radius R * mul +
+ * add, the shape's reach and half the ramp width (set by the caller). */
+static double g_voxel_mul = 1.0, g_voxel_add = 0.0;
+
+void ko_particles_set_voxel_box(double mul, double add) {
+	g_voxel_mul = mul;
+	g_voxel_add = add;
+}
+
+/* aabb.hpp:41-84: [a, b) per axis; x unclamped when periodic (cells wrap).
+ * subcell_mode: 0 the reference's box, 1 the sub-cell box, 2 the sub-cell
+ * box of the grown voxel radius. */
 static void aabb(int D, const kel_particle_state *p, const int64_t *ext, int periodic, int subcell_mode,
 				 int64_t *a, int64_t *b) {
 	for (int k = 0; k < D; ++k) {
-		double X = p->position[k], r = p->radius;
+		double X = p->position[k], r = subcell_mode == 2 ? p->radius * g_voxel_mul + g_voxel_add : p->radius;
 		if (subcell_mode) {
 			a[k] = (int64_t)floor(X - r - 0.5);
 			b[k] = (int64_t)ceil(X + r + 0.5) + 1;
@@ -176,7 +187,8 @@ void ko_particles_couple(ko_lattice *h, const kel_particle_state *P, int np, con
 	for (int p = 0; p < np; ++p) {                                                                           \
 		kel_particle_state *pp = &P[p];                                                                      \
 		int64_t a[3] = {0, 0, 0}, b[3] = {1, 1, 1};                                                          \
-		aabb(D, pp, ext, per, prm->porosity_mode == KEL_POROSITY_SUBCELL, a, b);                             \
+		aabb(D, pp, ext, per, prm->porosity_mode == KEL_POROSITY_SUBCELL ? 1                                 \
+							  : (prm->porosity_mode == KEL_POROSITY_VOXEL ? 2 : 0), a, b);                       \
 		double ts = 1.0 / (double)steps;                                                                     \
 		double vp[3] = {0, 0, 0};                                                                            \
 		for (int k = 0; k < D; ++k) vp[k] = (pp->position[k] - pp->position_old[k]) / ts;                    \

@@ -32,6 +32,7 @@
  *   out_dir/rho.f64, out_dir/vel.f64   macros of the last collide
  */
 #include "lbm.hpp" /* modules/core/c++/lbm.hpp, via -I */
+#include "particle/voxel_narrow.hpp"
 #include "forst_chunk.hpp"
 #include "write_csv.hpp"
 #include "write_vtk.hpp"
@@ -862,6 +863,119 @@ struct WriterCase {
 	}
 };
 
+/*
+ * Voxel signed-distance bodies (particle/mask.hpp, particle/porosity.hpp:24-54,
+ * particle/voxel_narrow.hpp), T = Float64, a group of NB bodies made by
+ * create_spheroid_particle_group (sphere mask) or refilled with sdf::cube.
+ *   in_dir/vparams.txt  resolution kind(0 sphere, 1 cube) eps nx ny nz
+ *   in_dir/bodies.f64   NB x (position[3], rotation[3], radius)
+ *   in_dir/locals.f64   local points (3 doubles each) for mask_sample_local
+ *   in_dir/points.f64   lattice points (3 doubles each)
+ *   in_dir/pairs.f64    body pairs (lo, hi)
+ *   in_dir/sdfs.f64     signed distances for solid_fraction_from_sdf
+ * out: mask.f64 (iteration order), com.f64 (3), sample.f64, sdf.f64 and
+ * porosity.f64 (body-major, per point), global.f64 (mask_local_to_global of
+ * each local point per body, 3 each), solid.f64, contacts.f64 (per pair: hit,
+ * depth, normal[3], point[3]).
+ */
+template <uint64_t D, uint64_t NB>
+struct VoxelCase {
+	using T = sch::Float64;
+	using NT = double;
+
+	static std::vector<double> read_f64(const std::string &p) {
+		auto v = read_file(p, true);
+		std::vector<double> o(v.size() / 8);
+		std::memcpy(o.data(), v.data(), o.size() * 8);
+		return o;
+	}
+	template <typename V>
+	static data<sch::Vector<T, D>> vec(const V *x) {
+		data<sch::Vector<T, D>> u;
+		for (uint64_t i = 0; i < D; ++i) u.at({{i}}).set(static_cast<NT>(x[i]));
+		return u;
+	}
+
+	static int run(const std::string &in, const std::string &out) {
+		std::ifstream pf(in + "/vparams.txt");
+		uint64_t R, kind, ext[3];
+		double eps;
+		pf >> R >> kind >> eps >> ext[0] >> ext[1] >> ext[2];
+		auto B = read_f64(in + "/bodies.f64");
+		auto L = read_f64(in + "/locals.f64");
+		auto X = read_f64(in + "/points.f64");
+		auto PR = read_f64(in + "/pairs.f64");
+		auto S = read_f64(in + "/sdfs.f64");
+		if (B.size() != NB * 7) return 5;
+		data<sch::LbmMeter<sch::Scalar<T>>> r0;
+		r0.at({}).set(B[6]);
+		data<sch::Scalar<T>> d0;
+		d0.at({}).set(1.0);
+		auto g = create_spheroid_particle_group<T, D, NB>(r0, d0, {R});
+		auto &mask = g.template get<"mask">();
+		if (kind == 1)
+			g.template get<"center_of_mass">().at({0u}) = fill_mask_from_sdf<T, D>(
+				mask, R, [](const data<sch::Vector<T, D>> &u) { return sdf::cube<T, D>(u); });
+		auto &parts = g.template get<"particles">();
+		for (uint64_t p = 0; p < NB; ++p) {
+			const double *q = B.data() + p * 7;
+			auto &pi = parts.at({p});
+			auto &rb = pi.template get<"rigid_body">();
+			for (uint64_t i = 0; i < D; ++i) rb.template get<"position">().at({{i}}).set(q[i]);
+			if constexpr (D == 2) rb.template get<"rotation">().at({}).set(q[3]);
+			else
+				for (uint64_t i = 0; i < 3; ++i) rb.template get<"rotation">().at({{i}}).set(q[3 + i]);
+			pi.template get<"collision">().template get<"radius">().at({}).set(q[6]);
+		}
+		std::vector<double> m;
+		iterator<D>::apply([&](const auto &k) { m.push_back(static_cast<double>(mask.at(k).get())); }, {},
+						   mask.get_dims());
+		write_f64(out + "/mask.f64", m);
+		auto &com = g.template get<"center_of_mass">().at({0u});
+		std::vector<double> c(3, 0.0);
+		for (uint64_t i = 0; i < D; ++i) c[i] = com.at({{i}}).get();
+		write_f64(out + "/com.f64", c);
+		std::vector<double> samp, glob, sdf, por, sol, con;
+		for (size_t k = 0; k + 3 <= L.size(); k += 3) samp.push_back(mask_sample_local<T, D>(mask, vec(&L[k]), R));
+		for (uint64_t p = 0; p < NB; ++p) {
+			auto &pi = parts.at({p});
+			for (size_t k = 0; k + 3 <= L.size(); k += 3) {
+				auto x = mask_local_to_global<T, D>(vec(&L[k]), pi, com);
+				for (uint64_t i = 0; i < 3; ++i) glob.push_back(i < D ? x.at({{i}}).get() : 0.0);
+			}
+			for (size_t k = 0; k + 3 <= X.size(); k += 3) {
+				sdf.push_back(mask_signed_distance<T, D>(g, pi, vec(&X[k]), R));
+				data<sch::Scalar<T>> e;
+				e.at({}).set(eps);
+				por.push_back(particle_porosity<T, D, 1u, por::ParticleVoxel<T>>::calculate(g, p, vec(&X[k]), e)
+								  .at({})
+								  .get());
+			}
+		}
+		for (double v : S) sol.push_back(solid_fraction_from_sdf<T>(v, eps));
+		data<sch::FixedArray<sch::UInt64, D>> extent;
+		for (uint64_t i = 0; i < D; ++i) extent.at({i}).set(ext[i]);
+		data<sch::Scalar<T>> e;
+		e.at({}).set(eps);
+		for (size_t k = 0; k + 2 <= PR.size(); k += 2) {
+			data<sch::ContactManifold<T, D>> mf;
+			bool hit = voxel_contact<T, D>(g, parts.at({(uint64_t)PR[k]}), parts.at({(uint64_t)PR[k + 1]}), extent, e,
+										  mf);
+			con.push_back(hit ? 1.0 : 0.0);
+			con.push_back(hit ? mf.template get<"depth">().at({}).get() : 0.0);
+			for (uint64_t i = 0; i < 3; ++i) con.push_back(hit && i < D ? mf.template get<"normal">().at({{i}}).get() : 0.0);
+			for (uint64_t i = 0; i < 3; ++i) con.push_back(hit && i < D ? mf.template get<"point">().at({{i}}).get() : 0.0);
+		}
+		write_f64(out + "/sample.f64", samp);
+		write_f64(out + "/global.f64", glob);
+		write_f64(out + "/sdf.f64", sdf);
+		write_f64(out + "/porosity.f64", por);
+		write_f64(out + "/solid.f64", sol);
+		write_f64(out + "/contacts.f64", con);
+		return 0;
+	}
+};
+
 int main(int argc, char **argv) {
 	if (argc != 4) {
 		std::fprintf(stderr, "usage: %s <case> <in_dir> <out_dir>\n", argv[0]);
@@ -884,6 +998,8 @@ int main(int argc, char **argv) {
 	if (c == "fplbm_d2q9_f64_48x40x1") return FplbmCase<F64, sch::D2Q9, 48, 40, 1>::run(argv[2], argv[3]);
 	if (c == "fplbm_d2q9_f32_48x40x1") return FplbmCase<F32, sch::D2Q9, 48, 40, 1>::run(argv[2], argv[3]);
 	if (c == "fplbm_d2q9_f32_48x40x3") return FplbmCase<F32, sch::D2Q9, 48, 40, 3>::run(argv[2], argv[3]);
+	if (c == "voxel_2d_f64_4") return VoxelCase<2, 4>::run(argv[2], argv[3]);
+	if (c == "voxel_3d_f64_4") return VoxelCase<3, 4>::run(argv[2], argv[3]);
 	if (c == "writers_d2q9_f32_12x7") return WriterCase<F32, sch::D2Q9, 12, 7>::run(argv[2], argv[3]);
 	if (c == "writers_d3q19_f64_5x4x3") return WriterCase<F64, sch::D3Q19, 5, 4, 3>::run(argv[2], argv[3]);
 	std::fprintf(stderr, "unknown case %s\n", c.c_str());

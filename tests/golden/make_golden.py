@@ -261,6 +261,62 @@ def run_fplbm_harness(hcase, bodies, init, flags, workdir):
     return out
 
 
+# Voxel signed-distance bodies: harness case, dimension, mask resolution,
+# shape (0 sphere, 1 cube), eps, lattice extent.
+VOXEL_CASES = {"voxel_2d_sphere": ("voxel_2d_f64_4", 2, 32, 0, 1.0, (64, 64, 1)),
+               "voxel_2d_cube": ("voxel_2d_f64_4", 2, 32, 1, 1.5, (64, 64, 1)),
+               "voxel_3d_sphere": ("voxel_3d_f64_4", 3, 16, 0, 1.0, (40, 40, 40)),
+               "voxel_3d_cube": ("voxel_3d_f64_4", 3, 16, 1, 1.5, (40, 40, 40))}
+
+
+def voxel_inputs(dim, ext, seed=43):
+    """Four bodies (position, rotation, radius): 0 and 1 overlap off-axis, 2
+    touches 1, 3 stands apart; local points inside and outside the mask box;
+    lattice points around the bodies; pairs in both orders; distances across
+    the ramp."""
+    rng = np.random.default_rng(seed + dim)
+    if dim == 2:
+        pos = np.array([[29.0, 30.0, 0], [36.0, 33.5, 0], [42.3, 24.7, 0], [16.2, 47.9, 0]])
+        rot = np.array([[0.0, 0, 0], [0.7, 0, 0], [-1.3, 0, 0], [2.9, 0, 0]])
+        rad = np.array([5.0, 5.0, 6.0, 4.5])
+    else:
+        pos = np.array([[18.0, 19.0, 20.0], [23.0, 21.5, 20.5], [27.2, 14.6, 22.3], [9.1, 30.2, 28.4]])
+        rot = np.array([[0.0, 0.0, 0.0], [0.3, -0.5, 0.2], [1.1, 0.4, -0.7], [-0.2, 0.9, 1.6]])
+        rad = np.array([4.5, 4.5, 5.0, 3.5])
+    bodies = np.concatenate([pos, rot, rad[:, None]], axis=1)
+    locals_ = np.zeros((48, 3))
+    locals_[:40, :dim] = rng.uniform(-1.3, 1.3, (40, dim))
+    fixed = [[0, 0, 0], [1, 0, 0], [0.5, 0, 0], [-1, -1, 0], [0.99, 0.99, 0], [1.2, -1.25, 0], [-0.3, 0.4, 0],
+             [0.0, 1.0, 0]]
+    locals_[40:, :2] = np.array(fixed)[:, :2]
+    if dim == 3:
+        locals_[40:, 2] = rng.uniform(-1, 1, 8)
+    pts = np.zeros((160, 3))
+    for k in range(160):
+        b = k % 4
+        pts[k, :dim] = pos[b, :dim] + rng.uniform(-1.6, 1.6, dim) * rad[b]
+    pairs = np.array([[0, 1], [1, 0], [1, 2], [2, 1], [0, 2], [0, 3], [3, 2]], np.float64)
+    sdfs = np.concatenate([np.linspace(-1.0, 1.0, 41), [-5.0, 5.0]])
+    return dict(bodies=bodies, locals=locals_, points=pts, pairs=pairs, sdfs=sdfs)
+
+
+def run_voxel_harness(hcase, R, kind, eps, ext, inp, workdir):
+    ind, outd = os.path.join(workdir, "in"), os.path.join(workdir, "out")
+    os.makedirs(ind)
+    os.makedirs(outd)
+    open(os.path.join(ind, "vparams.txt"), "w").write(f"{R} {kind} {eps!r} {ext[0]} {ext[1]} {ext[2]}\n")
+    for k, f in (("bodies", "bodies"), ("locals", "locals"), ("points", "points"), ("pairs", "pairs"),
+                 ("sdfs", "sdfs")):
+        inp[k].astype(np.float64).tofile(os.path.join(ind, f + ".f64"))
+    subprocess.check_call([HARNESS, hcase, ind, outd])
+    out = {}
+    for k in ("mask", "com", "sample", "global", "sdf", "porosity", "solid", "contacts"):
+        out[k] = np.fromfile(os.path.join(outd, k + ".f64"))
+    out["contacts"] = out["contacts"].reshape(-1, 8)
+    out["global"] = out["global"].reshape(-1, 3)
+    return out
+
+
 def particle_registry():
     return {
         "particles_gather_f64": ("particles_d2q9_f64_64x48x5", "gather"),
@@ -276,7 +332,8 @@ def load_particles(name):
 
 def names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and not f.startswith(("particles_", "writers_", "cavity256_", "hlbm_", "fplbm_")))
+                  if f.endswith(".npz") and not f.startswith(("particles_", "writers_", "cavity256_", "hlbm_", "fplbm_",
+                                                               "voxel_")))
 
 
 WRITER_CASES = {"writers_d2q9_f32_12x7": (9, (12, 7), np.float32),
@@ -348,6 +405,15 @@ def main():
             out = run_fplbm_harness(hcase, bodies, init, flags, td)
         emit(name, bodies=bodies, init=init, flags=flags, params=np.array(json.dumps(FPLBM_PARAMS)), **out)
         print(f"{name:28s} fplbm: acceleration {out['after_particle'][:, 12:14].ravel()[:4]}")
+    for name, (hcase, dim, R, kind, eps, ext) in VOXEL_CASES.items():
+        if args.only and args.only not in name:
+            continue
+        inp = voxel_inputs(dim, ext)
+        with tempfile.TemporaryDirectory() as td:
+            out = run_voxel_harness(hcase, R, kind, eps, ext, inp, td)
+        emit(name, **inp, params=np.array(json.dumps(dict(dim=dim, resolution=R, kind=kind, eps=eps,
+                                                             extent=list(ext)))), **out)
+        print(f"{name:28s} voxel: hits {out['contacts'][:, 0].astype(int).tolist()} com {out['com']}")
     for name, (q, dims, dtype) in WRITER_CASES.items():
         if args.only and args.only not in name:
             continue
