@@ -346,7 +346,7 @@ def run_warm_start(args, rank, world):
     model = WS.train(WS.steady_subset(states), epochs=args.epochs, batch=32, lr=2e-3, widths=widths,
                      log_every=32, rho_target_rms=args.rho_rms, residual=args.residual,
                      weight_by_steps=args.weight_by_steps, rho_norm=args.rho_norm,
-                     rho_residual=args.rho_residual)
+                     rho_residual=args.rho_residual, flip=args.flip)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     n_steps = args.epochs * (args.train // 32)
@@ -378,7 +378,7 @@ def run_warm_start(args, rank, world):
                            "tol": args.tol, "check_every": 1000, "epochs": args.epochs,
                            "rho_target_rms": args.rho_rms, "residual_u": args.residual,
                            "weight_by_steps": args.weight_by_steps, "rho_norm": args.rho_norm,
-                           "rho_residual": args.rho_residual,
+                           "rho_residual": args.rho_residual, "flip_augment": args.flip,
                            "widths": list(widths),
                            "params": model.net.n_params, "rho_scale": model.rho_scale},
                 "plain_seconds": r["plain_seconds"], "speedup": r["speedup"],
@@ -569,6 +569,8 @@ def main():
     ap.add_argument("--rho-norm", default="lubrication", choices=["global", "lubrication"],
                     help="warm start: density target over u_max (global) or over the channel's lubrication "
                          "pressure drop")
+    ap.add_argument("--no-flip", dest="flip", action="store_false",
+                    help="warm start: no y-mirrored copies in the training minibatches")
     ap.add_argument("--rho-residual", action="store_true",
                     help="warm start: the density output corrects the lubrication pressure plane")
     args = ap.parse_args()

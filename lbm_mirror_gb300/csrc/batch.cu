@@ -70,6 +70,7 @@ struct BatchParams {
 	int write_macros;
 	int shifted; // populations hold g = f - w_i (MODE_SHIFTED)
 	int idx32;   // 9 * plane < 2^31: population offsets from a cell fit 32-bit arithmetic
+	int pf_ahead; // launched blocks ahead whose tiles a block prefetches into L2 (0: none)
 };
 
 // Arithmetic of a batch: the library's two (fast, reference rounding) on
@@ -228,6 +229,22 @@ __global__ void __launch_bounds__(512, MODE == MODE_EXACT ? 1 : 4) k_batch_sweep
 	ctx.g[0] = ctx.g[1] = ctx.g[2] = 0.f;
 	const float Fc[3] = {0.f, 0.f, 0.f};
 	float rho = 1.f, u[3] = {0.f, 0.f, 0.f};
+	// L2 prefetch of the tile p.pf_ahead launched blocks later (every
+	// direction plane, one 128-byte line per thread), issued after this
+	// block's own loads: requests in flight that hold no registers
+	if (p.pf_ahead > 0) {
+		const int64_t bt = (int64_t)blockIdx.x + p.pf_ahead;
+		const int lines = (int)blockDim.x / 32;
+		if (bt < (int64_t)gridDim.x && (int)threadIdx.x < 9 * lines) {
+			const int4 *tt = reinterpret_cast<const int4 *>(p.trec + bt);
+			const int4 q0 = __ldg(tt), q1 = __ldg(tt + 1);
+			if (q1.w) {
+				const int64_t c0 = (int64_t)(((uint64_t)(uint32_t)q0.y << 32) | (uint32_t)q0.x);
+				const int i = (int)threadIdx.x / lines, k = (int)threadIdx.x - i * lines;
+				asm volatile("prefetch.global.L2 [%0];" ::"l"(p.f + i * p.plane + c0 + k * 32));
+			}
+		}
+	}
 	const bool col = MODE == MODE_SHIFTED
 						 ? cell_update_shifted(f, p.flags[cell], y, ctx, rho, u)
 						 : cell_update<L, COLL_BGK, MODE == MODE_EXACT>(f, p.flags[cell], y, ctx, 1.f, Fc, rho, u);
@@ -505,6 +522,7 @@ __global__ void k_batch_shift(BatchParams p, float sign) {
 struct kel_batch {
 	int n = 0;
 	int tile = 256;
+	int sms = 1; // multiprocessors of the batch's device
 	std::vector<kel_channel_desc> desc;
 	std::vector<ChannelRec> rec;
 	std::vector<int> block_ch;
@@ -590,6 +608,9 @@ BatchParams params(const kel_batch *B, int write_macros) {
 	p.write_macros = write_macros;
 	p.shifted = B->shifted ? 1 : 0;
 	p.idx32 = 9 * B->plane < ((int64_t)1 << 31) ? 1 : 0;
+	// prefetch the tiles one resident wave later (2048 threads per SM):
+	// measured with 1024 channels 0.82 -> 0.85 of HBM; two waves gained less
+	p.pf_ahead = B->sms * (2048 / (B->tile > 0 ? B->tile : 256));
 	return p;
 }
 
@@ -745,6 +766,11 @@ extern "C" int kel_batch_create(int32_t n_channels, const kel_channel_desc *ch, 
 	}
 	kel_batch *B = new kel_batch();
 	B->n = n_channels;
+	{
+		int dev = 0;
+		if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&B->sms, cudaDevAttrMultiProcessorCount, dev);
+		if (B->sms < 1) B->sms = 1;
+	}
 	B->desc.assign(ch, ch + n_channels);
 	B->t.assign(n_channels, 0);
 	// parabolic inlet per channel, as the single-lattice inlet profile (float)

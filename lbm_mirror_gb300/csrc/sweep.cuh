@@ -94,6 +94,8 @@ struct SweepParams {
 	// bit f: flag value f (1 .. MAX_FLAGS-1) has no boundary step and collides,
 	// so its cells skip the operation-table dispatch (same result)
 	uint32_t plain;
+	// sweep1_kernel: blocks ahead whose rows a block prefetches into L2 (0: none)
+	int pf_ahead;
 };
 
 // What the per-cell physics needs from a launch: the flag -> operation table,
@@ -1116,6 +1118,28 @@ __global__ void __launch_bounds__(256, 4) sweep1_kernel(const __grid_constant__ 
 	using ST = typename S::T;
 	ST *const fc = static_cast<ST *>(p.f) + cell;
 	const int pl32 = (int)p.plane, oy32 = nxp, oz32 = nxp * p.ny;
+	// L2 prefetch of the rows the block p.pf_ahead places later in launch
+	// order will read (its x range in every direction plane; in odd steps its
+	// neighbours' rows are prefetched by their own predecessors): requests in
+	// flight that hold no registers, one 128-byte line per thread.
+	if (p.pf_ahead > 0) {
+		const unsigned gx = gridDim.x;
+		const int64_t nblk = (int64_t)gx * gridDim.y * gridDim.z;
+		const int64_t b = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gx + blockIdx.x + p.pf_ahead;
+		if (b < nblk) {
+			const int x0 = (int)(b % gx) * (int)blockDim.x;
+			const int64_t row = b / gx;
+			const int n = min((int)blockDim.x, nxp - x0);
+			constexpr int per = 128 / (int)sizeof(ST); // cells per line
+			const int lines = (n + per - 1) / per;
+			const int t = threadIdx.x;
+			if (t < Q * lines) {
+				const int i = t / lines, l = t - i * lines;
+				const ST *a = static_cast<const ST *>(p.f) + i * p.plane + row * nxp + x0 + l * per;
+				asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+			}
+		}
+	}
 
 	float f[Q];
 	if (!ODD && p.idx32) {

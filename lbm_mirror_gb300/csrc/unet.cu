@@ -16,6 +16,7 @@
 //               bias + ReLU fused into the epilogue;
 //   conv_wgrad  M = c_out, N = 9 c_in, K = pixels, split over pixel chunks
 //               into FP32 partial sums, reduced in fixed order (deterministic).
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -388,6 +389,197 @@ __global__ void __launch_bounds__(128) conv_tc(TcArgs a) {
 				dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
 				dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
 			}
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	if (warp == 0) {
+		asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tmem_cols));
+	}
+}
+
+// ---- the convolution from a TMA-loaded halo, for rows of 128 pixels --------------
+//
+// For a layer whose width is a multiple of 128: one CTA computes 128
+// consecutive pixels of one image row (the M = 128 rows of the accumulator)
+// by all Co outputs.  For each chunk of CK input channels the input reaches
+// shared memory as a halo, one TMA tile of 3 rows x 130 pixels x CK channels
+// at (x0 - 1 .. x0 + 128, y - 1 .. y + 1), zero-filled by the copy outside
+// the image, laid out channel-group major: element (row r, pixel p, channel
+// 8 g + e) at ((g * 3 + r) * 130 + p) * 16 + 2 e.  Pixels are 16 bytes apart
+// within a channel group, so the A operand of tap (dy, dx) -- the 128 pixels
+// shifted by (dy, dx) -- is the same halo read through a descriptor whose
+// start moves by (dy * 130 + dx) * 16 bytes (K-major, no swizzle: core
+// matrices of 8 pixels x 8 channels, 8-pixel stride SBO = 128 B, channel-group
+// stride LBO = 3 * 130 * 16 B).  The nine taps of a chunk read one halo, where
+// an im2col tile holds every input value nine times.  The chunk's weights
+// (Co x 9 x CK) arrive by TMA as [g][tap][co][8 channels]: B of tap t and
+// channel groups 2j, 2j + 1 at ((2 j) * 9 + t) * Co * 16, LBO = 9 * Co * 16,
+// SBO = 128.  One thread issues the copies (one mbarrier per stage counts
+// their bytes) and the MMAs (committed to the stage's second mbarrier, which
+// frees the stage for the chunk S later).  Every wait is bounded; on timeout
+// the CTA records the failure in *err, waits (bounded) for the copies it
+// issued, and frees its TMEM.
+
+constexpr int HX = 130; // halo pixels per row
+
+struct HaloArgs {
+	const float *bias;
+	bf16 *y; // (N,H,W,Co)
+	int N, H, W, Ci, Co, CK;
+	int relu, use_bias;
+	int stages;
+	uint32_t a_bytes, b_bytes; // bytes of the two TMA boxes of a chunk
+	uint32_t a_span, stage_bytes; // B's offset in a stage and the stage size (1024-byte multiples)
+	uint32_t tmem_cols;
+	int *err;
+};
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t addr, uint32_t bytes) {
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(addr), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap *map, uint32_t mbar, int c0, int c1, int c2,
+											int c3, int c4) {
+	asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, "
+				 "%6, %7}], [%2];\n" ::"r"(dst),
+				 "l"(map), "r"(mbar), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4)
+				 : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap *map, uint32_t mbar, int c0, int c1, int c2,
+											int c3) {
+	asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, "
+				 "%6}], [%2];\n" ::"r"(dst),
+				 "l"(map), "r"(mbar), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+				 : "memory");
+}
+
+__global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtensorMap tx,
+												 const __grid_constant__ CUtensorMap tw, HaloArgs a) {
+	extern __shared__ __align__(1024) uint8_t sm[];
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int S = a.stages;
+	uint64_t *full = reinterpret_cast<uint64_t *>(sm + (size_t)S * a.stage_bytes);
+	uint64_t *done = full + S;
+	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + S);
+
+	const int tpr = a.W / 128; // tiles per row
+	const int x0 = (int)(blockIdx.x % tpr) * 128;
+	const int row = (int)(blockIdx.x / tpr); // n * H + y
+	const int n = row / a.H, yy = row - n * a.H;
+	const int nch = a.Ci / a.CK;
+	const uint32_t tx_bytes = a.a_bytes + a.b_bytes;
+
+	if (tid == 0) {
+		for (int s = 0; s < S; ++s) {
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(full + s)));
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(done + s)));
+		}
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+					 "r"(a.tmem_cols));
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+	const uint32_t tmem = *tmem_slot;
+
+	// instruction descriptor: D f32, A bf16, B bf16, both K-major, N = Co, M = 128
+	const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+	const uint32_t lbo_a = 3u * HX * 16u, lbo_b = 9u * (uint32_t)a.Co * 16u;
+	int fail = 0, loaded = 0, issued = -1;
+	if (tid == 0) {
+		auto load = [&](int c) {
+			const int s = c % S;
+			const uint32_t base = smem_u32(sm + (size_t)s * a.stage_bytes);
+			mbar_expect_tx(smem_u32(full + s), tx_bytes);
+			tma_load_5d(base, &tx, smem_u32(full + s), 0, x0 - 1, yy - 1, c * (a.CK / 8), n);
+			tma_load_4d(base + a.a_span, &tw, smem_u32(full + s), 0, 0, 0, c * (a.CK / 8));
+		};
+		for (int c = 0; c < S && c < nch; ++c) load(c);
+		loaded = S < nch ? S : nch;
+		for (int c = 0; c < nch; ++c) {
+			const int s = c % S;
+			if (!mbar_wait(smem_u32(full + s), (uint32_t)((c / S) & 1))) {
+				fail = 1;
+				break;
+			}
+			asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+			const uint32_t abase = smem_u32(sm + (size_t)s * a.stage_bytes);
+			const uint32_t bbase = abase + a.a_span;
+			for (int j = 0; j < a.CK / 16; ++j)
+				for (int t = 0; t < 9; ++t) {
+					const int dy = t / 3, dx = t % 3;
+					const uint64_t ad = umma_desc(abase + (uint32_t)(2 * j) * lbo_a + (uint32_t)(dy * HX + dx) * 16u,
+												  lbo_a, 128u);
+					const uint64_t bd = umma_desc(bbase + ((uint32_t)(2 * j) * 9u + (uint32_t)t) * (uint32_t)a.Co * 16u,
+												  lbo_b, 128u);
+					const uint32_t acc = (c > 0 || j > 0 || t > 0) ? 1u : 0u;
+					asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+								 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+								 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+				}
+			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+				smem_u32(done + s)));
+			issued = c;
+			// refill the stage chunk c - 1 used with chunk c - 1 + S once its
+			// MMAs are done (chunk c's are queued behind them meanwhile)
+			if (c >= 1 && c - 1 + S < nch) {
+				const int cp = c - 1;
+				if (!mbar_wait(smem_u32(done + cp % S), (uint32_t)((cp / S) & 1))) {
+					fail = 1;
+					break;
+				}
+				load(cp + S);
+				++loaded;
+			}
+		}
+		// the last commit covers every MMA issued before it
+		if (issued >= 0 && !mbar_wait(smem_u32(done + issued % S), (uint32_t)((issued / S) & 1))) fail = 1;
+		// copies issued but not consumed (after a failure): wait for them
+		// (bounded) before the CTA's shared memory can be reused
+		for (int c = issued + 1; c < loaded; ++c) mbar_wait(smem_u32(full + c % S), (uint32_t)((c / S) & 1));
+		if (fail || issued != nch - 1) atomicExch(a.err, 1);
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	const int failed = __syncthreads_or(tid == 0 && (fail || issued != nch - 1));
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+	if (!failed) {
+		// epilogue: warp w owns TMEM lanes (= tile pixels) 32 w .. 32 w + 31
+		const int px = warp * 32 + lane;
+		const int64_t m = ((int64_t)row * a.W) + x0 + px;
+		for (int c0 = 0; c0 < a.Co; c0 += 16) {
+			uint32_t r[16];
+			const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+			asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+						 "[%16];\n"
+						 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+						   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+						   "=r"(r[14]), "=r"(r[15])
+						 : "r"(taddr));
+			asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+			__align__(16) __nv_bfloat162 o[8];
+#pragma unroll
+			for (int q = 0; q < 8; ++q) {
+				float v0 = __uint_as_float(r[2 * q]), v1 = __uint_as_float(r[2 * q + 1]);
+				if (a.use_bias) {
+					v0 += a.bias[c0 + 2 * q];
+					v1 += a.bias[c0 + 2 * q + 1];
+				}
+				if (a.relu) {
+					v0 = fmaxf(v0, 0.f);
+					v1 = fmaxf(v1, 0.f);
+				}
+				o[q] = __floats2bfloat162_rn(v0, v1);
+			}
+			uint4 *dst = reinterpret_cast<uint4 *>(a.y + m * a.Co + c0);
+			dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
+			dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
 		}
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -1112,6 +1304,104 @@ int64_t telems(const kel_unet *U, int t, int n) {
 	return (int64_t)n * (U->d.height >> s.level) * (U->d.width >> s.level) * s.ch;
 }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+								  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+								  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (null if
+// the driver does not provide it)
+EncodeTiledFn encode_tiled() {
+	static const EncodeTiledFn fn = []() -> EncodeTiledFn {
+		void *p = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+			q != cudaDriverEntryPointSuccess)
+			return nullptr;
+		return reinterpret_cast<EncodeTiledFn>(p);
+	}();
+	return fn;
+}
+
+uint32_t align1k(uint64_t v) { return (uint32_t)((v + 1023) / 1024 * 1024); }
+
+// Channel chunk and stage count of conv_halo: the largest chunk (64, 48, 32 or
+// 16 channels dividing Ci) whose stages (up to three, at least two when there
+// are two chunks or more) fit 110 KB (two CTAs per SM), else 200 KB; 0: none.
+int halo_plan(int Ci, int Co, HaloArgs &a) {
+	for (const uint32_t cap : {110u * 1024u, 200u * 1024u})
+		for (const int ck : {64, 48, 32, 16}) {
+			if (Ci % ck) continue;
+			const int nch = Ci / ck;
+			const uint32_t ab = 3u * HX * (uint32_t)ck * 2u, bb = 18u * (uint32_t)Co * (uint32_t)ck;
+			const uint32_t stage = align1k(ab) + align1k(bb);
+			int S = nch < 3 ? nch : 3;
+			while (S > 1 && (uint64_t)S * stage + 1024 > cap) --S;
+			if ((nch > 1 && S < 2) || (uint64_t)S * stage + 1024 > cap) continue;
+			a.CK = ck;
+			a.stages = S;
+			a.a_bytes = ab;
+			a.b_bytes = bb;
+			a.a_span = align1k(ab);
+			a.stage_bytes = stage;
+			return 1;
+		}
+	return 0;
+}
+
+// The halo convolution (conv_halo) for 128-pixel rows; returns 0 without
+// launching when the layer does not fit it.
+int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y, int n, int H, int W, int ci,
+					 int co, bool relu, bool bias, int *launched) {
+	*launched = 0;
+	const EncodeTiledFn enc = encode_tiled();
+	HaloArgs a;
+	memset(&a, 0, sizeof(a));
+	if (!enc || W % 128 || ci % 16 || co % 16 || co < 16 || co > 256 || !halo_plan(ci, co, a)) return KEL_OK;
+	CUtensorMap tx, tw;
+	{ // x (N,H,W,Ci) as (8 channels, x, y, channel group, n)
+		const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)(ci / 8), (cuuint64_t)n};
+		const cuuint64_t strides[4] = {(cuuint64_t)ci * 2, (cuuint64_t)W * ci * 2, 16, (cuuint64_t)H * W * ci * 2};
+		const cuuint32_t box[5] = {8, HX, 3, (cuuint32_t)(a.CK / 8), 1};
+		const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+		if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(x), dims, strides, box, es,
+				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+				CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+			return KEL_OK;
+	}
+	{ // w (Co, 9, Ci) as (8 channels, co, tap, channel group)
+		const cuuint64_t dims[4] = {8, (cuuint64_t)co, 9, (cuuint64_t)(ci / 8)};
+		const cuuint64_t strides[3] = {(cuuint64_t)9 * ci * 2, (cuuint64_t)ci * 2, 16};
+		const cuuint32_t box[4] = {8, (cuuint32_t)co, 9, (cuuint32_t)(a.CK / 8)};
+		const cuuint32_t es[4] = {1, 1, 1, 1};
+		if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(w), dims, strides, box, es,
+				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+				CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+			return KEL_OK;
+	}
+	a.bias = b;
+	a.y = y;
+	a.N = n;
+	a.H = H;
+	a.W = W;
+	a.Ci = ci;
+	a.Co = co;
+	a.relu = relu;
+	a.use_bias = bias;
+	a.tmem_cols = 32;
+	while (a.tmem_cols < (uint32_t)co) a.tmem_cols <<= 1;
+	a.err = U->d_err;
+	const size_t smem = (size_t)a.stages * a.stage_bytes + (size_t)a.stages * 16 + 16;
+	static bool attr_set = false;
+	if (!attr_set) {
+		KEL_CUDA(cudaFuncSetAttribute(conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+		attr_set = true;
+	}
+	conv_halo<<<(unsigned)((int64_t)n * H * (W / 128)), 128, smem, U->stream>>>(tx, tw, a);
+	KEL_CUDA(cudaGetLastError());
+	*launched = 1;
+	return KEL_OK;
+}
+
 int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y, int n, int level, int ci, int co,
 			 bool relu, bool bias) {
 	ConvArgs a;
@@ -1130,6 +1420,9 @@ int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
 	if (U->conv_kernel == KEL_UNET_CONV_TCGEN05) {
 		if (ci % 16 || co % 16 || co < 16 || co > 256)
 			return fail(KEL_ERR_UNSUPPORTED, "conv: tensor-core path needs c_in, c_out multiples of 16, c_out <= 256");
+		int launched = 0, rc;
+		if ((rc = conv_halo_launch(U, x, w, b, y, n, a.H, a.W, ci, co, relu, bias, &launched))) return rc;
+		if (launched) return KEL_OK;
 		TcArgs t;
 		t.x = x;
 		t.w = w;

@@ -187,7 +187,7 @@ def rho_denominator(model, d_mask, d_umax, d_tau):
 
 def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, warmup=100, seed=1,
           widths=(32, 64, 128, 128), log_every=0, rho_target_rms=0.25, residual=False, weight_by_steps=False,
-          rho_norm="global", rho_residual=False):
+          rho_norm="global", rho_residual=False, flip=False):
     """Train the U-Net on the steady states with Adam (cosine schedule).
     rho_target_rms sets the weight of the density in the loss (see targets).
     With weight_by_steps the minibatches draw channels with probability
@@ -199,6 +199,11 @@ def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, 
     selects the density target (see targets); with rho_residual (lubrication
     norm) the density output is the correction to the lubrication pressure
     plane 10 (scaled to the target): kel_unet_set_residual(2, 10, 1 / rho_scale).
+    With flip, a random half of every minibatch is the y-mirror image of its
+    channels (mask and targets mirrored, u_y negated; the input planes are
+    built from the mirrored mask): a channel and its mirror image (walls,
+    parabolic inlet and all) have mirrored steady flows, so this doubles the
+    distinct samples the network sees.
     Returns a WarmStartNet; its history holds (step, loss) pairs."""
     torch = _torch()
     ny, nx = states.rho.shape[1:]
@@ -238,6 +243,12 @@ def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, 
             mb_umax = d_umax.index_select(0, idx).contiguous()
             mb_tau = d_tau.index_select(0, idx).contiguous()
             mb_tgt = d_tgt.index_select(0, idx).contiguous()
+            if flip:
+                f = torch.rand(batch, device=dev, generator=gen) < 0.5
+                mt = mb_tgt.flip(1)
+                mt[..., 1] = -mt[..., 1]
+                mb_mask = torch.where(f[:, None, None], mb_mask.flip(1), mb_mask).contiguous()
+                mb_tgt = torch.where(f[:, None, None, None], mt, mb_tgt).contiguous()
             torch.cuda.synchronize()
             net.make_input(mb_mask.data_ptr(), mb_umax.data_ptr(), mb_tau.data_ptr(), batch)
             net.forward(batch)
