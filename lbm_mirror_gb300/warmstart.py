@@ -123,6 +123,34 @@ class WarmStartNet:
         return self.net.shape
 
 
+class WarmStartEnsemble:
+    """Networks trained on the same steady states with different seeds; the
+    prediction is the mean of theirs (the members share the normalisation:
+    rho_norm and rho_scale come from the training data).  Independent
+    trainings err differently, so the mean is nearer the steady state than a
+    typical member, and the slowest warm-started channel varies less."""
+
+    def __init__(self, members):
+        members = list(members)
+        if not members:
+            raise ValueError("empty ensemble")
+        m0 = members[0]
+        for m in members[1:]:
+            if m.rho_norm != m0.rho_norm or m.rho_scale != m0.rho_scale or m.shape != m0.shape:
+                raise ValueError("ensemble members differ in normalisation or shape")
+        self.members = members
+        self.rho_norm, self.rho_scale = m0.rho_norm, m0.rho_scale
+
+    @property
+    def shape(self):
+        return self.members[0].shape
+
+
+def train_ensemble(states: SteadyStates, seeds=(1, 2), **kw):
+    """train() once per seed; a WarmStartEnsemble of the results."""
+    return WarmStartEnsemble([train(states, seed=s, **kw) for s in seeds])
+
+
 def _gap_h3(fluid):
     """Per (channel, column): sum over the column's vertical runs of fluid
     cells of the run length cubed.  fluid: (n, ny, nx) bool numpy array or
@@ -269,6 +297,11 @@ def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, 
 
 
 def _predict_once(model, d_mask, d_umax, d_tau):
+    if isinstance(model, WarmStartEnsemble):
+        out = _predict_once(model.members[0], d_mask, d_umax, d_tau)
+        for m in model.members[1:]:
+            out += _predict_once(m, d_mask, d_umax, d_tau)
+        return out * (1.0 / len(model.members))
     torch = _torch()
     n = d_mask.shape[0]
     ny, nx, oc = model.shape
@@ -285,7 +318,8 @@ def _predict_once(model, d_mask, d_umax, d_tau):
 
 def predict(model: WarmStartNet, d_mask, d_umax, d_tau, mirror=False):
     """Normalised prediction (n, ny, nx, 3) float32 on the device for device
-    inputs (mask uint8 (n, ny, nx), u_max and tau float32 (n,)).  With mirror,
+    inputs (mask uint8 (n, ny, nx), u_max and tau float32 (n,)); for a
+    WarmStartEnsemble the mean of its members' predictions.  With mirror,
     the mean of the prediction and the mirror image of the prediction for the
     y-mirrored channel (u_y negated): a channel and its mirror image, walls,
     parabolic inlet and all, have mirrored flows, so the average keeps the
