@@ -866,12 +866,28 @@ __global__ void __launch_bounds__(128) conv_wgrad(WgradArgs a) {
 }
 
 // grad[j] += sum over chunks of partial[c][j], chunks in order
+// grad[j] += sum over the chunks of partial[c][j], in a fixed order: block
+// (32, 8) takes 32 consecutive j; thread row y sums the chunks of its eighth
+// [c0, c1) in order, then the eight sums are added in order of y.
 __global__ void reduce_partials(const float *partial, int64_t per, int chunks, float *grad) {
-	for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < per; j += (int64_t)gridDim.x * blockDim.x) {
-		float s = 0.f;
-		for (int c = 0; c < chunks; ++c) s += partial[(int64_t)c * per + j];
-		grad[j] += s;
+	__shared__ float sh[8][33];
+	const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
+	const int y = threadIdx.y;
+	const int c0 = (int)((int64_t)chunks * y / 8), c1 = (int)((int64_t)chunks * (y + 1) / 8);
+	float s = 0.f;
+	if (j < per)
+		for (int c = c0; c < c1; ++c) s += partial[(int64_t)c * per + j];
+	sh[y][threadIdx.x] = s;
+	__syncthreads();
+	if (y == 0 && j < per) {
+		float t = 0.f;
+		for (int k = 0; k < 8; ++k) t += sh[k][threadIdx.x];
+		grad[j] += t;
 	}
+}
+
+void launch_reduce_partials(const float *partial, int64_t per, int chunks, float *grad, cudaStream_t st) {
+	reduce_partials<<<(unsigned)((per + 31) / 32), dim3(32, 8), 0, st>>>(partial, per, chunks, grad);
 }
 
 // db[co] += sum over pixels of dY[m][co] (one block per channel, fixed order)
@@ -923,85 +939,140 @@ void bias_grads(const bf16 *dy, int64_t M, int Co, float *scratch, float *db, cu
 	const int64_t chunk = (M + blocks - 1) / blocks;
 	const int nb = (int)((M + chunk - 1) / chunk);
 	channel_sums_partial<<<nb, 256, 0, st>>>(dy, M, Co, chunk, scratch);
-	reduce_partials<<<(Co + 127) / 128, 128, 0, st>>>(scratch, Co, nb, db);
+	launch_reduce_partials(scratch, Co, nb, db, st);
 }
 
 // ---- element-wise pieces -----------------------------------------------------------
+//
+// One thread per pixel and group of 8 channels (channel counts are
+// multiples of 16): 16-byte loads and stores, index arithmetic once per 8
+// values; the per-value arithmetic and its rounding are those of one value
+// at a time.
 
+__device__ __forceinline__ void unpack8(const uint4 &q, float (&f)[8]) {
+	const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&q);
+#pragma unroll
+	for (int k = 0; k < 4; ++k) {
+		const float2 t = __bfloat1622float2(h[k]);
+		f[2 * k] = t.x;
+		f[2 * k + 1] = t.y;
+	}
+}
+
+__device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
+	uint4 q;
+	__nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&q);
+#pragma unroll
+	for (int k = 0; k < 4; ++k) h[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+	return q;
+}
+
+// dy = 0 where !(y > 0); n values (a multiple of 8)
 __global__ void relu_backward(bf16 *dy, const bf16 *y, int64_t n) {
-	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-		if (!(__bfloat162float(y[i]) > 0.f)) dy[i] = __float2bfloat16(0.f);
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n / 8; i += (int64_t)gridDim.x * blockDim.x) {
+		float yv[8];
+		unpack8(reinterpret_cast<const uint4 *>(y)[i], yv);
+		uint4 q = reinterpret_cast<const uint4 *>(dy)[i];
+		uint16_t *d = reinterpret_cast<uint16_t *>(&q);
+#pragma unroll
+		for (int k = 0; k < 8; ++k)
+			if (!(yv[k] > 0.f)) d[k] = 0; // bf16 +0
+		reinterpret_cast<uint4 *>(dy)[i] = q;
+	}
 }
 
 __global__ void pool_forward(const bf16 *x, bf16 *y, int N, int H, int W, int C) {
-	const int64_t n = (int64_t)N * (H / 2) * (W / 2) * C;
+	const int G = C / 8;
+	const int64_t n = (int64_t)N * (H / 2) * (W / 2) * G;
+	const uint4 *xv = reinterpret_cast<const uint4 *>(x);
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-		const int c = (int)(i % C);
-		int64_t r = i / C;
+		const int g = (int)(i % G);
+		int64_t r = i / G;
 		const int xo = (int)(r % (W / 2));
 		r /= (W / 2);
 		const int yo = (int)(r % (H / 2));
 		const int b = (int)(r / (H / 2));
-		const int64_t base = (((int64_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
-		const float s = __bfloat162float(x[base]) + __bfloat162float(x[base + C]) +
-						__bfloat162float(x[base + (int64_t)W * C]) + __bfloat162float(x[base + (int64_t)W * C + C]);
-		y[i] = __float2bfloat16(0.25f * s);
+		const int64_t base = (((int64_t)b * H + 2 * yo) * W + 2 * xo) * G + g;
+		float a[8], c[8], d[8], e[8], o[8];
+		unpack8(xv[base], a);
+		unpack8(xv[base + G], c);
+		unpack8(xv[base + (int64_t)W * G], d);
+		unpack8(xv[base + (int64_t)W * G + G], e);
+#pragma unroll
+		for (int k = 0; k < 8; ++k) o[k] = 0.25f * (a[k] + c[k] + d[k] + e[k]);
+		reinterpret_cast<uint4 *>(y)[i] = pack8(o);
 	}
 }
 
-// dx (N,H,W,C) = pool_backward(dy (N,H/2,W/2,C)) + skip_grad
+// dx (N,H,W,C) = pool_backward(dy (N,H/2,W/2,C)) + skip_grad (skip may be dx)
 __global__ void pool_backward_add(const bf16 *dy, const bf16 *skip, bf16 *dx, int N, int H, int W, int C) {
-	const int64_t n = (int64_t)N * H * W * C;
+	const int G = C / 8;
+	const int64_t n = (int64_t)N * H * W * G;
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-		const int c = (int)(i % C);
-		int64_t r = i / C;
+		const int g = (int)(i % G);
+		int64_t r = i / G;
 		const int x = (int)(r % W);
 		r /= W;
 		const int y = (int)(r % H);
 		const int b = (int)(r / H);
-		const float g = 0.25f * __bfloat162float(dy[(((int64_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * C + c]);
-		dx[i] = __float2bfloat16(g + __bfloat162float(skip[i]));
+		float p[8], s[8], o[8];
+		unpack8(reinterpret_cast<const uint4 *>(dy)[(((int64_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * G + g], p);
+		unpack8(reinterpret_cast<const uint4 *>(skip)[i], s);
+#pragma unroll
+		for (int k = 0; k < 8; ++k) o[k] = 0.25f * p[k] + s[k];
+		reinterpret_cast<uint4 *>(dx)[i] = pack8(o);
 	}
 }
 
 // cat (N,H,W,Cu+Cs) = [upsample2(u (N,H/2,W/2,Cu)), s (N,H,W,Cs)]
 __global__ void upcat_forward(const bf16 *u, const bf16 *s, bf16 *cat, int N, int H, int W, int Cu, int Cs) {
-	const int C = Cu + Cs;
-	const int64_t n = (int64_t)N * H * W * C;
+	const int Gu = Cu / 8, Gs = Cs / 8, G = Gu + Gs;
+	const int64_t n = (int64_t)N * H * W * G;
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-		const int c = (int)(i % C);
-		const int64_t p = i / C;
-		const int x = (int)(p % W);
-		const int64_t r = p / W;
-		const int y = (int)(r % H);
-		const int b = (int)(r / H);
-		cat[i] = c < Cu ? u[(((int64_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * Cu + c] : s[p * Cs + (c - Cu)];
+		const int g = (int)(i % G);
+		const int64_t p = i / G;
+		uint4 q;
+		if (g < Gu) {
+			const int x = (int)(p % W);
+			const int64_t r = p / W;
+			const int y = (int)(r % H);
+			const int b = (int)(r / H);
+			q = reinterpret_cast<const uint4 *>(u)[(((int64_t)b * (H / 2) + y / 2) * (W / 2) + x / 2) * Gu + g];
+		} else {
+			q = reinterpret_cast<const uint4 *>(s)[p * Gs + (g - Gu)];
+		}
+		reinterpret_cast<uint4 *>(cat)[i] = q;
 	}
 }
 
 // split d(cat): d_up (N,H/2,W/2,Cu) = upsample_backward(first Cu), d_skip = last Cs
 __global__ void upcat_backward(const bf16 *dcat, bf16 *du, bf16 *ds, int N, int H, int W, int Cu, int Cs) {
-	const int C = Cu + Cs;
-	const int64_t nu = (int64_t)N * (H / 2) * (W / 2) * Cu;
-	const int64_t ns = (int64_t)N * H * W * Cs;
+	const int Gu = Cu / 8, Gs = Cs / 8, G = Gu + Gs;
+	const int64_t nu = (int64_t)N * (H / 2) * (W / 2) * Gu;
+	const int64_t ns = (int64_t)N * H * W * Gs;
+	const uint4 *dv = reinterpret_cast<const uint4 *>(dcat);
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nu + ns; i += (int64_t)gridDim.x * blockDim.x) {
 		if (i < nu) {
-			const int c = (int)(i % Cu);
-			int64_t r = i / Cu;
+			const int g = (int)(i % Gu);
+			int64_t r = i / Gu;
 			const int xo = (int)(r % (W / 2));
 			r /= (W / 2);
 			const int yo = (int)(r % (H / 2));
 			const int b = (int)(r / (H / 2));
-			const int64_t base = (((int64_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
-			const float s = __bfloat162float(dcat[base]) + __bfloat162float(dcat[base + C]) +
-							__bfloat162float(dcat[base + (int64_t)W * C]) +
-							__bfloat162float(dcat[base + (int64_t)W * C + C]);
-			du[i] = __float2bfloat16(s);
+			const int64_t base = (((int64_t)b * H + 2 * yo) * W + 2 * xo) * G + g;
+			float a[8], c[8], d[8], e[8], o[8];
+			unpack8(dv[base], a);
+			unpack8(dv[base + G], c);
+			unpack8(dv[base + (int64_t)W * G], d);
+			unpack8(dv[base + (int64_t)W * G + G], e);
+#pragma unroll
+			for (int k = 0; k < 8; ++k) o[k] = a[k] + c[k] + d[k] + e[k];
+			reinterpret_cast<uint4 *>(du)[i] = pack8(o);
 		} else {
 			const int64_t j = i - nu;
-			const int c = (int)(j % Cs);
-			const int64_t p = j / Cs;
-			ds[j] = dcat[p * C + Cu + c];
+			const int g = (int)(j % Gs);
+			const int64_t p = j / Gs;
+			reinterpret_cast<uint4 *>(ds)[j] = dv[p * G + Gu + g];
 		}
 	}
 }
@@ -1017,13 +1088,33 @@ struct HeadRes {
 // channel co with r.in[co] >= 0, r.scale[co] times input plane r.in[co] of the
 // network input `in` (Cin planes): the network then learns the correction to
 // that plane (a residual target).
+// 1x1 head, one thread per pixel: the pixel's channels in 16-byte loads, the
+// weights (Co x Ci, Co <= 8) in shared memory; each output sums its inputs
+// in channel order from the bias
 __global__ void head_forward(const bf16 *x, const float *w, const float *b, float *y, int64_t M, int Ci, int Co,
 							 const bf16 *in, int Cin, HeadRes r) {
+	extern __shared__ float hw[];
+	for (int k = threadIdx.x; k < Co * Ci; k += blockDim.x) hw[k] = w[k];
+	__syncthreads();
 	for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
-		for (int co = 0; co < Co; ++co) {
-			float s = b[co];
-			for (int ci = 0; ci < Ci; ++ci) s += w[co * Ci + ci] * __bfloat162float(x[m * Ci + ci]);
-			if (co < MAX_RES && r.in[co] >= 0) s += r.scale[co] * __bfloat162float(in[m * Cin + r.in[co]]);
+		float acc[MAX_RES];
+#pragma unroll
+		for (int co = 0; co < MAX_RES; ++co) acc[co] = co < Co ? b[co] : 0.f;
+		const uint4 *xr = reinterpret_cast<const uint4 *>(x + m * Ci);
+		for (int v = 0; v < Ci / 8; ++v) {
+			float xv[8];
+			unpack8(xr[v], xv);
+#pragma unroll
+			for (int e = 0; e < 8; ++e)
+#pragma unroll
+				for (int co = 0; co < MAX_RES; ++co)
+					if (co < Co) acc[co] += hw[co * Ci + 8 * v + e] * xv[e];
+		}
+#pragma unroll
+		for (int co = 0; co < MAX_RES; ++co) {
+			if (co >= Co) break;
+			float s = acc[co];
+			if (r.in[co] >= 0) s += r.scale[co] * __bfloat162float(in[m * Cin + r.in[co]]);
 			y[m * Co + co] = s;
 		}
 	}
@@ -1048,13 +1139,30 @@ __global__ void mse_loss(const float *y, const float *tgt, float *dy, int64_t n,
 }
 
 // head backward: dx (bf16) = dy * Wh, dW/db accumulated per block then reduced
+// dx = W^T dy per pixel (Co <= 8): each input channel sums over the outputs
+// in order from 0; 8 channels per 16-byte store
 __global__ void head_backward_dx(const float *dy, const float *w, bf16 *dx, int64_t M, int Ci, int Co) {
-	for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x)
-		for (int ci = 0; ci < Ci; ++ci) {
-			float s = 0.f;
-			for (int co = 0; co < Co; ++co) s += dy[m * Co + co] * w[co * Ci + ci];
-			dx[m * Ci + ci] = __float2bfloat16(s);
+	extern __shared__ float hw[];
+	for (int k = threadIdx.x; k < Co * Ci; k += blockDim.x) hw[k] = w[k];
+	__syncthreads();
+	for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < M; m += (int64_t)gridDim.x * blockDim.x) {
+		float d[MAX_RES];
+#pragma unroll
+		for (int co = 0; co < MAX_RES; ++co) d[co] = co < Co ? dy[m * Co + co] : 0.f;
+		uint4 *xr = reinterpret_cast<uint4 *>(dx + m * Ci);
+		for (int v = 0; v < Ci / 8; ++v) {
+			float o[8];
+#pragma unroll
+			for (int e = 0; e < 8; ++e) {
+				float s = 0.f;
+#pragma unroll
+				for (int co = 0; co < MAX_RES; ++co)
+					if (co < Co) s += d[co] * hw[co * Ci + 8 * v + e];
+				o[e] = s;
+			}
+			xr[v] = pack8(o);
 		}
+	}
 }
 
 __global__ void head_backward_dw(const float *dy, const bf16 *x, int64_t M, int Ci, int Co, float *partial) {
@@ -1183,21 +1291,38 @@ __global__ void column_features(const uint8_t *mask, int N, int H, int W, float 
 	h3[idx] = s3;
 }
 
-// per sample: suffix sums of the column resistance 1 / max(open, 1/8)^3, and
-// of the lubrication resistance 1 / max(sum h^3, 1) normalised by its total
+// per sample (one block): suffix sums over the columns of the column
+// resistance 1 / max(open, 1/8)^3, and of the lubrication resistance
+// 1 / max(sum h^3, 1) normalised by its total; a Hillis-Steele scan in shared
+// memory (fixed order).  Dynamic shared memory: 4 W floats.
 __global__ void column_resistance(const float *open, const float *h3, int N, int W, float *R, float *PL) {
-	const int b = blockIdx.x * blockDim.x + threadIdx.x;
-	if (b >= N) return;
-	float acc = 0.f, acc2 = 0.f;
-	for (int x = W - 1; x >= 0; --x) {
+	extern __shared__ float cs[];
+	float *a0 = cs, *b0 = cs + W, *a1 = cs + 2 * W, *b1 = cs + 3 * W;
+	const int b = blockIdx.x;
+	for (int x = threadIdx.x; x < W; x += blockDim.x) {
 		const float o = fmaxf(open[(int64_t)b * W + x], 0.125f);
-		acc += 1.f / (o * o * o);
-		R[(int64_t)b * W + x] = acc / (float)W;
-		acc2 += 1.f / fmaxf(h3[(int64_t)b * W + x], 1.f);
-		PL[(int64_t)b * W + x] = acc2;
+		a0[x] = 1.f / (o * o * o);
+		b0[x] = 1.f / fmaxf(h3[(int64_t)b * W + x], 1.f);
 	}
-	const float inv = 1.f / acc2;
-	for (int x = 0; x < W; ++x) PL[(int64_t)b * W + x] *= inv;
+	__syncthreads();
+	for (int off = 1; off < W; off <<= 1) {
+		for (int x = threadIdx.x; x < W; x += blockDim.x) {
+			a1[x] = x + off < W ? a0[x] + a0[x + off] : a0[x];
+			b1[x] = x + off < W ? b0[x] + b0[x + off] : b0[x];
+		}
+		__syncthreads();
+		float *t = a0;
+		a0 = a1;
+		a1 = t;
+		t = b0;
+		b0 = b1;
+		b1 = t;
+	}
+	const float inv = 1.f / b0[0];
+	for (int x = threadIdx.x; x < W; x += blockDim.x) {
+		R[(int64_t)b * W + x] = a0[x] / (float)W;
+		PL[(int64_t)b * W + x] = b0[x] * inv;
+	}
 }
 
 __global__ void make_input(const uint8_t *mask, const float *umax, const float *tau, const float *open,
@@ -1489,7 +1614,7 @@ int conv_grads_tc(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy
 	}
 	conv_wgrad_tc<<<dim3((unsigned)tiles, (unsigned)chunks), 128, smem, U->stream>>>(a);
 	const int64_t per = (int64_t)l.co * K;
-	reduce_partials<<<grid_of(per), 256, 0, U->stream>>>(U->partial, per, (int)chunks, U->g + l.woff);
+	launch_reduce_partials(U->partial, per, (int)chunks, U->g + l.woff, U->stream);
 	bias_grads(dy, M, l.co, U->partial, U->g + l.woff + per, U->stream);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
@@ -1519,7 +1644,7 @@ int conv_grads(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy, i
 	dim3 grid((unsigned)((l.co + CB_M - 1) / CB_M), (unsigned)((K + CB_N - 1) / CB_N), (unsigned)chunks);
 	conv_wgrad<<<grid, 128, 0, U->stream>>>(a);
 	const int64_t per = (int64_t)l.co * K;
-	reduce_partials<<<grid_of(per), 256, 0, U->stream>>>(U->partial, per, (int)chunks, U->g + l.woff);
+	launch_reduce_partials(U->partial, per, (int)chunks, U->g + l.woff, U->stream);
 	bias_grads(dy, M, l.co, U->partial, U->g + l.woff + per, U->stream);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
@@ -1728,7 +1853,8 @@ extern "C" int kel_unet_make_input(kel_unet *U, const uint8_t *d_mask, const flo
 	const int64_t pix = (int64_t)n * U->d.height * U->d.width;
 	const int H = U->d.height, W = U->d.width;
 	column_features<<<(n * W + 127) / 128, 128, 0, U->stream>>>(d_mask, n, H, W, U->col_open, U->col_h3);
-	column_resistance<<<(n + 63) / 64, 64, 0, U->stream>>>(U->col_open, U->col_h3, n, W, U->col_res, U->col_pl);
+	column_resistance<<<n, 256, sizeof(float) * 4 * W, U->stream>>>(U->col_open, U->col_h3, n, W, U->col_res,
+																	 U->col_pl);
 	make_input<<<grid_of(pix), 256, 0, U->stream>>>(d_mask, d_umax, d_tau, U->col_open, U->col_h3, U->col_res,
 													 U->col_pl, U->input, n, H, W, 16);
 	KEL_CUDA(cudaGetLastError());
@@ -1747,23 +1873,23 @@ extern "C" int kel_unet_forward(kel_unet *U, int32_t n, float *d_out) {
 		return conv_fwd(U, x, l.w, U->p + l.woff + (int64_t)l.co * 9 * l.ci, y, n, l.level, l.ci, l.co, true, true);
 	};
 	if ((rc = cv(0, U->input, A[T_E0A])) || (rc = cv(1, A[T_E0A], A[T_E0B]))) return rc;
-	pool_forward<<<grid_of(telems(U, T_P0, n)), 256, 0, U->stream>>>(A[T_E0B], A[T_P0], n, H, W, w[0]);
+	pool_forward<<<grid_of(telems(U, T_P0, n) / 8), 256, 0, U->stream>>>(A[T_E0B], A[T_P0], n, H, W, w[0]);
 	if ((rc = cv(2, A[T_P0], A[T_E1A])) || (rc = cv(3, A[T_E1A], A[T_E1B]))) return rc;
-	pool_forward<<<grid_of(telems(U, T_P1, n)), 256, 0, U->stream>>>(A[T_E1B], A[T_P1], n, H / 2, W / 2, w[1]);
+	pool_forward<<<grid_of(telems(U, T_P1, n) / 8), 256, 0, U->stream>>>(A[T_E1B], A[T_P1], n, H / 2, W / 2, w[1]);
 	if ((rc = cv(4, A[T_P1], A[T_E2A])) || (rc = cv(5, A[T_E2A], A[T_E2B]))) return rc;
-	pool_forward<<<grid_of(telems(U, T_P2, n)), 256, 0, U->stream>>>(A[T_E2B], A[T_P2], n, H / 4, W / 4, w[2]);
+	pool_forward<<<grid_of(telems(U, T_P2, n) / 8), 256, 0, U->stream>>>(A[T_E2B], A[T_P2], n, H / 4, W / 4, w[2]);
 	if ((rc = cv(6, A[T_P2], A[T_BA])) || (rc = cv(7, A[T_BA], A[T_BB]))) return rc;
-	upcat_forward<<<grid_of(telems(U, T_C2, n)), 256, 0, U->stream>>>(A[T_BB], A[T_E2B], A[T_C2], n, H / 4, W / 4, w[3],
+	upcat_forward<<<grid_of(telems(U, T_C2, n) / 8), 256, 0, U->stream>>>(A[T_BB], A[T_E2B], A[T_C2], n, H / 4, W / 4, w[3],
 																	   w[2]);
 	if ((rc = cv(8, A[T_C2], A[T_D2A])) || (rc = cv(9, A[T_D2A], A[T_D2B]))) return rc;
-	upcat_forward<<<grid_of(telems(U, T_C1, n)), 256, 0, U->stream>>>(A[T_D2B], A[T_E1B], A[T_C1], n, H / 2, W / 2, w[2],
+	upcat_forward<<<grid_of(telems(U, T_C1, n) / 8), 256, 0, U->stream>>>(A[T_D2B], A[T_E1B], A[T_C1], n, H / 2, W / 2, w[2],
 																	   w[1]);
 	if ((rc = cv(10, A[T_C1], A[T_D1A])) || (rc = cv(11, A[T_D1A], A[T_D1B]))) return rc;
-	upcat_forward<<<grid_of(telems(U, T_C0, n)), 256, 0, U->stream>>>(A[T_D1B], A[T_E0B], A[T_C0], n, H, W, w[1], w[0]);
+	upcat_forward<<<grid_of(telems(U, T_C0, n) / 8), 256, 0, U->stream>>>(A[T_D1B], A[T_E0B], A[T_C0], n, H, W, w[1], w[0]);
 	if ((rc = cv(12, A[T_C0], A[T_D0A])) || (rc = cv(13, A[T_D0A], A[T_D0B]))) return rc;
 	const UnetLayer &hd = L[14];
 	const int64_t M = (int64_t)n * H * W;
-	head_forward<<<grid_of(M), 256, 0, U->stream>>>(A[T_D0B], U->p + hd.woff, U->p + hd.woff + (int64_t)hd.co * hd.ci,
+	head_forward<<<grid_of(M), 256, sizeof(float) * hd.co * hd.ci, U->stream>>>(A[T_D0B], U->p + hd.woff, U->p + hd.woff + (int64_t)hd.co * hd.ci,
 													U->out, M, hd.ci, hd.co, U->input, U->d.in_channels, U->res);
 	KEL_CUDA(cudaGetLastError());
 	if (d_out && d_out != U->out)
@@ -1790,13 +1916,16 @@ extern "C" int kel_unet_backward(kel_unet *U, const float *d_target, int32_t n, 
 	const int lb = 512;
 	mse_loss<<<lb, 256, 0, U->stream>>>(U->out, d_target, U->dout, nout, U->loss_partial);
 	// head
-	head_backward_dx<<<grid_of(M), 256, 0, U->stream>>>(U->dout, U->p + hd.woff, G[T_D0B], M, hd.ci, hd.co);
+	head_backward_dx<<<grid_of(M), 256, sizeof(float) * hd.co * hd.ci, U->stream>>>(U->dout, U->p + hd.woff, G[T_D0B],
+																						 M, hd.ci, hd.co);
 	if (hd.co <= 8 && 256 % hd.ci == 0) {
-		const int64_t chunk = (M + 303) / 304;
+		// enough blocks to keep every SM's loads in flight (each block's loop is
+		// a chain of dependent accumulations)
+		const int64_t chunk = (M + 1215) / 1216;
 		const int nb = (int)((M + chunk - 1) / chunk);
 		const int64_t per = (int64_t)hd.co * hd.ci + hd.co;
 		head_dw_partial<<<nb, 256, 0, U->stream>>>(U->dout, A[T_D0B], M, hd.ci, hd.co, chunk, U->partial);
-		reduce_partials<<<grid_of(per), 256, 0, U->stream>>>(U->partial, per, nb, U->g + hd.woff);
+		launch_reduce_partials(U->partial, per, nb, U->g + hd.woff, U->stream);
 	} else {
 		head_backward_dw<<<hd.co * hd.ci + hd.co, 256, 0, U->stream>>>(U->dout, A[T_D0B], M, hd.ci, hd.co,
 																	   U->g + hd.woff);
@@ -1804,7 +1933,7 @@ extern "C" int kel_unet_backward(kel_unet *U, const float *d_target, int32_t n, 
 	// one conv layer: relu backward on dy, weight/bias grads, data grad into dx
 	auto back = [&](int li, int t_in, const bf16 *x_in, int t_out, bf16 *dx) -> int {
 		const UnetLayer &l = L[li];
-		relu_backward<<<grid_of(telems(U, t_out, n)), 256, 0, U->stream>>>(G[t_out], A[t_out], telems(U, t_out, n));
+		relu_backward<<<grid_of(telems(U, t_out, n) / 8), 256, 0, U->stream>>>(G[t_out], A[t_out], telems(U, t_out, n));
 		int r = conv_grads(U, l, x_in, G[t_out], n);
 		if (r) return r;
 		if (dx) r = conv_fwd(U, G[t_out], l.wf, nullptr, dx, n, l.level, l.co, l.ci, false, false);
@@ -1812,22 +1941,22 @@ extern "C" int kel_unet_backward(kel_unet *U, const float *d_target, int32_t n, 
 		return r;
 	};
 	if ((rc = back(13, T_D0A, A[T_D0A], T_D0B, G[T_D0A])) || (rc = back(12, T_C0, A[T_C0], T_D0A, G[T_C0]))) return rc;
-	upcat_backward<<<grid_of(telems(U, T_C0, n)), 256, 0, U->stream>>>(G[T_C0], G[T_D1B], G[T_E0B], n, H, W, w[1], w[0]);
+	upcat_backward<<<grid_of(telems(U, T_C0, n) / 8), 256, 0, U->stream>>>(G[T_C0], G[T_D1B], G[T_E0B], n, H, W, w[1], w[0]);
 	if ((rc = back(11, T_D1A, A[T_D1A], T_D1B, G[T_D1A])) || (rc = back(10, T_C1, A[T_C1], T_D1A, G[T_C1]))) return rc;
-	upcat_backward<<<grid_of(telems(U, T_C1, n)), 256, 0, U->stream>>>(G[T_C1], G[T_D2B], G[T_E1B], n, H / 2, W / 2, w[2],
+	upcat_backward<<<grid_of(telems(U, T_C1, n) / 8), 256, 0, U->stream>>>(G[T_C1], G[T_D2B], G[T_E1B], n, H / 2, W / 2, w[2],
 																		w[1]);
 	if ((rc = back(9, T_D2A, A[T_D2A], T_D2B, G[T_D2A])) || (rc = back(8, T_C2, A[T_C2], T_D2A, G[T_C2]))) return rc;
-	upcat_backward<<<grid_of(telems(U, T_C2, n)), 256, 0, U->stream>>>(G[T_C2], G[T_BB], G[T_E2B], n, H / 4, W / 4, w[3],
+	upcat_backward<<<grid_of(telems(U, T_C2, n) / 8), 256, 0, U->stream>>>(G[T_C2], G[T_BB], G[T_E2B], n, H / 4, W / 4, w[3],
 																		w[2]);
 	if ((rc = back(7, T_BA, A[T_BA], T_BB, G[T_BA])) || (rc = back(6, T_P2, A[T_P2], T_BA, G[T_P2]))) return rc;
 	// encoder level 2: d(e2b) = pool_backward(d p2) + d skip2 (kept in G[T_E2B])
-	pool_backward_add<<<grid_of(telems(U, T_E2B, n)), 256, 0, U->stream>>>(G[T_P2], G[T_E2B], G[T_E2B], n, H / 4,
+	pool_backward_add<<<grid_of(telems(U, T_E2B, n) / 8), 256, 0, U->stream>>>(G[T_P2], G[T_E2B], G[T_E2B], n, H / 4,
 																			 W / 4, w[2]);
 	if ((rc = back(5, T_E2A, A[T_E2A], T_E2B, G[T_E2A])) || (rc = back(4, T_P1, A[T_P1], T_E2A, G[T_P1]))) return rc;
-	pool_backward_add<<<grid_of(telems(U, T_E1B, n)), 256, 0, U->stream>>>(G[T_P1], G[T_E1B], G[T_E1B], n, H / 2,
+	pool_backward_add<<<grid_of(telems(U, T_E1B, n) / 8), 256, 0, U->stream>>>(G[T_P1], G[T_E1B], G[T_E1B], n, H / 2,
 																			 W / 2, w[1]);
 	if ((rc = back(3, T_E1A, A[T_E1A], T_E1B, G[T_E1A])) || (rc = back(2, T_P0, A[T_P0], T_E1A, G[T_P0]))) return rc;
-	pool_backward_add<<<grid_of(telems(U, T_E0B, n)), 256, 0, U->stream>>>(G[T_P0], G[T_E0B], G[T_E0B], n, H, W, w[0]);
+	pool_backward_add<<<grid_of(telems(U, T_E0B, n) / 8), 256, 0, U->stream>>>(G[T_P0], G[T_E0B], G[T_E0B], n, H, W, w[0]);
 	if ((rc = back(1, T_E0A, A[T_E0A], T_E0B, G[T_E0A])) || (rc = back(0, -1, U->input, T_E0A, nullptr))) return rc;
 	KEL_CUDA(cudaGetLastError());
 	if (loss) {

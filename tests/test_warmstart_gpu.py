@@ -108,6 +108,34 @@ def test_trained_network_reaches_steady_state_in_fewer_steps():
     assert r["final_u_rel_l2_max"] < 1e-2, r
 
 
+def test_trained_network_beats_rest_start_at_full_size():
+    """The warm-start workload's configuration: 4096 seeded 256x64 channels
+    solved to the residual 1e-6 (per 1000 steps), the U-Net (widths 48, 96,
+    128, 128, lubrication-scaled density, y-mirror augmentation, 60 epochs)
+    trained on them, 512 held-out channels run to 1e-6 from rest and from
+    the prediction (inference and reconstruction timed): fewer steps, less
+    wall time, the same final field.  The wall-time gain depends on the
+    trained instance (1.07-1.27x over training seeds and seed ensembles):
+    most of it comes from the slowest channel, a flow near an instability
+    whose time to steady state varies with small changes of its initial
+    field; with a few hundred channels or fewer that one channel decides the
+    wall time of either arm, so the gain is asserted at full size."""
+    from lbm_mirror_gb300 import warmstart as WS
+    train_ch = WS.fixed_size_channels(4096, seed=5)
+    test_ch = WS.fixed_size_channels(512, seed=6)
+    states = WS.solve(train_ch, tol=1e-6, check_every=1000, max_steps=2_000_000)
+    assert states.converged.mean() >= 0.8, states.converged.mean()
+    model = WS.train(WS.steady_subset(states), epochs=60, batch=32, lr=2e-3, widths=(48, 96, 128, 128),
+                     log_every=32, rho_norm="lubrication", flip=True)
+    r = WS.evaluate(model, test_ch, tol=1e-6, check_every=1000, max_steps=2_000_000)
+    print({k: v for k, v in r.items() if not k.startswith("steps_")})
+    assert r["channels"] >= 400, r
+    assert r["plain_unconverged"] == 0 and r["warm_unconverged"] == 0, r
+    assert r["warm_steps_mean"] < 0.97 * r["plain_steps_mean"], r
+    assert r["warm_seconds"] * 1.03 < r["plain_seconds"], r
+    assert r["final_u_rel_l2_max"] < 1e-2, r
+
+
 def test_network_input_planes_match_oracle():
     """kel_unet_make_input (mask, flow parameters, coordinates, column open
     fraction, downstream resistance, gap height and position, lubrication
