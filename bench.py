@@ -419,7 +419,8 @@ def run_warm_start(args, rank, world):
 def run_unet_train(args, rank, world):
     """Training steps of the warm-start U-Net (widths 32, 64, 128, 128; 256x64
     grids; batch 32) on the input planes of seeded channels and a synthetic
-    target: make_input + forward + backward (loss read back) + Adam per step.
+    target: make_input + one captured training step (forward, backward, Adam)
+    per step; the loss is read back after the timed steps.
     value = model TFLOP/s of the whole step (3 x the forward FLOPs)."""
     import torch
     from lbm_mirror_gb300 import UNet
@@ -433,19 +434,18 @@ def run_unet_train(args, rank, world):
     net = UNet(height=ny, width=nx, widths=widths, max_batch=n, seed=1)
 
     def step():
+        # forward + backward + Adam as one captured graph (kel_unet_train_step)
         net.make_input(dm.data_ptr(), du.data_ptr(), dt.data_ptr(), n)
-        net.forward(n)
-        loss = net.backward(tgt.data_ptr(), n)
-        net.adam_step(lr=1e-3)
-        return loss
+        net.train_step(tgt.data_ptr(), n, lr=1e-3)
 
+    torch.cuda.synchronize()
     for _ in range(args.warmup):
         step()
     net.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        loss = step()
-    net.synchronize()
+        step()
+    loss = net.last_loss()  # synchronises
     dt_s = (time.perf_counter() - t0) / args.steps
     flops = 3 * unet_flops_per_sample(ny, nx, widths) * n
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")

@@ -434,6 +434,18 @@ int kel_unet_forward(kel_unet *net, int32_t n, float *d_out);
  * parameter gradient (FP32, overwritten).  *loss is written on the host. */
 int kel_unet_backward(kel_unet *net, const float *d_target, int32_t n, double *loss);
 int kel_unet_adam_step(kel_unet *net, float lr, float beta1, float beta2, float eps, int32_t step);
+/* One training step on the input set by kel_unet_make_input / set_input:
+ * forward, backward against d_target (device, copied into the net), Adam
+ * (step counts from 1, as in kel_unet_adam_step) and the bf16 weight copies,
+ * on the net's stream without a host synchronisation.  From the second call
+ * on, the step is a captured CUDA graph, replayed while n and the Adam
+ * constants beta1, beta2, eps stay the same (lr may change every step).  The
+ * mean loss goes to *d_loss (device, may be NULL) and is kept for
+ * kel_unet_last_loss.  The same arithmetic as forward + backward + adam_step. */
+int kel_unet_train_step(kel_unet *net, const float *d_target, int32_t n, float lr, float beta1, float beta2, float eps,
+						int32_t step, double *d_loss);
+/* The loss of the last kel_unet_train_step (synchronises the net's stream). */
+int kel_unet_last_loss(kel_unet *net, double *loss);
 /* Convolution kernels: KEL_UNET_CONV_TCGEN05 (default; tcgen05.mma with the
  * accumulator in tensor memory) or KEL_UNET_CONV_MMA_SYNC (warp-level
  * mma.sync).  Both compute bf16 x bf16 -> FP32; results agree to FP32

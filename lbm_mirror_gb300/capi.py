@@ -276,6 +276,8 @@ def load_library(path: str | None = None):
         "kel_unet_forward": ([vp, i32, vp], C.c_int),
         "kel_unet_backward": ([vp, vp, i32, C.POINTER(C.c_double)], C.c_int),
         "kel_unet_adam_step": ([vp, C.c_float, C.c_float, C.c_float, C.c_float, i32], C.c_int),
+        "kel_unet_train_step": ([vp, vp, i32, C.c_float, C.c_float, C.c_float, C.c_float, i32, vp], C.c_int),
+        "kel_unet_last_loss": ([vp, C.POINTER(C.c_double)], C.c_int),
         "kel_unet_set_conv_kernel": ([vp, i32], C.c_int),
         "kel_unet_set_residual": ([vp, i32, i32, C.c_float], C.c_int),
         "kel_batch_destroy": ([vp], C.c_int),

@@ -1237,6 +1237,34 @@ __global__ void adam_update(float *p, const float *g, float *m, float *v, int64_
 	}
 }
 
+// Adam with lr and the bias corrections read from the device (c = lr, c1, c2):
+// the same arithmetic as adam_update, for a step replayed from a graph
+__global__ void adam_update_dev(float *p, const float *g, float *m, float *v, int64_t n, const float *c, float b1,
+								float b2, float eps) {
+	const float lr = c[0], c1 = c[1], c2 = c[2];
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+		const float gi = g[i];
+		const float mi = b1 * m[i] + (1.f - b1) * gi;
+		const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+		m[i] = mi;
+		v[i] = vi;
+		p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+	}
+}
+
+__global__ void adam_consts(float *c, float lr, float c1, float c2) {
+	c[0] = lr;
+	c[1] = c1;
+	c[2] = c2;
+}
+
+// the mean loss from the blocks' partial sums, in block order (as the host adds them)
+__global__ void loss_finish(const double *partial, int nb, int64_t n, double *loss) {
+	double s = 0.0;
+	for (int k = 0; k < nb; ++k) s += partial[k];
+	*loss = s / (double)n;
+}
+
 __global__ void refresh_conv_weights(const float *w32, bf16 *w, bf16 *wf, int Co, int Ci, int k) {
 	const int64_t n = (int64_t)Co * k * k * Ci;
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -1393,6 +1421,16 @@ struct kel_unet {
 	int *d_err = nullptr; // set by a tensor-core kernel whose bounded wait ran out
 	float *col_open = nullptr, *col_h3 = nullptr, *col_res = nullptr, *col_pl = nullptr; // input-feature scratch (max_batch x W)
 	HeadRes res; // residual head per output channel (kel_unet_set_residual)
+	cudaStream_t own_stream = nullptr; // the stream the net created (stream may be a caller's)
+	// kel_unet_train_step: the target copy, Adam's lr and bias corrections on
+	// the device, the last loss, and the captured step (forward, backward,
+	// Adam, weight refresh) for batch train_n and these Adam constants
+	float *tgt = nullptr, *adam_c = nullptr;
+	double *dev_loss = nullptr;
+	cudaGraphExec_t train_graph = nullptr;
+	int train_n = 0;
+	float train_b1 = 0.f, train_b2 = 0.f, train_eps = 0.f;
+	bool train_warm = false;
 };
 
 namespace {
@@ -1729,6 +1767,7 @@ extern "C" int kel_unet_create(const kel_unet_desc *desc, uint64_t seed, kel_une
 	}
 	U->nparam = off;
 	cudaStreamCreateWithFlags(&U->stream, cudaStreamNonBlocking);
+	U->own_stream = U->stream;
 	auto fail_out = [&](cudaError_t e) {
 		kel_unet_destroy(U);
 		return fail(e == cudaErrorMemoryAllocation ? KEL_ERR_OUT_OF_MEMORY : KEL_ERR_CUDA, "kel_unet_create: %s",
@@ -1807,7 +1846,14 @@ extern "C" int kel_unet_destroy(kel_unet *U) {
 	cudaFree(U->col_h3);
 	cudaFree(U->col_res);
 	cudaFree(U->col_pl);
-	if (U->stream) cudaStreamDestroy(U->stream);
+	cudaFree(U->tgt);
+	cudaFree(U->adam_c);
+	cudaFree(U->dev_loss);
+	if (U->train_graph) cudaGraphExecDestroy(U->train_graph);
+	if (U->own_stream) {
+		cudaStreamSynchronize(U->own_stream);
+		cudaStreamDestroy(U->own_stream);
+	}
 	delete U;
 	return KEL_OK;
 }
@@ -1900,10 +1946,19 @@ extern "C" int kel_unet_forward(kel_unet *U, int32_t n, float *d_out) {
 // After kel_unet_forward with the same n: masked-free MSE against d_target
 // (N,H,W,out_channels), all gradients into the FP32 gradient vector
 // (overwritten).  *loss receives the loss (host).
+static int unet_backward(kel_unet *U, const float *d_target, int32_t n, double *loss, double *dev_loss);
+
 extern "C" int kel_unet_backward(kel_unet *U, const float *d_target, int32_t n, double *loss) {
 	int rc = check_batch(U, n, "kel_unet_backward");
 	if (rc) return rc;
 	if (!d_target) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_backward: null target");
+	return unet_backward(U, d_target, n, loss, nullptr);
+}
+
+// backward with the loss to the host (loss, synchronising) and/or to the
+// device (dev_loss, on the net's stream)
+static int unet_backward(kel_unet *U, const float *d_target, int32_t n, double *loss, double *dev_loss) {
+	int rc;
 	auto &A = U->act;
 	auto &G = U->grad;
 	const auto &L = U->L;
@@ -1959,6 +2014,10 @@ extern "C" int kel_unet_backward(kel_unet *U, const float *d_target, int32_t n, 
 	pool_backward_add<<<grid_of(telems(U, T_E0B, n) / 8), 256, 0, U->stream>>>(G[T_P0], G[T_E0B], G[T_E0B], n, H, W, w[0]);
 	if ((rc = back(1, T_E0A, A[T_E0A], T_E0B, G[T_E0A])) || (rc = back(0, -1, U->input, T_E0A, nullptr))) return rc;
 	KEL_CUDA(cudaGetLastError());
+	if (dev_loss) {
+		loss_finish<<<1, 1, 0, U->stream>>>(U->loss_partial, lb, nout, dev_loss);
+		KEL_CUDA(cudaGetLastError());
+	}
 	if (loss) {
 		std::vector<double> part(lb);
 		KEL_CUDA(cudaMemcpyAsync(part.data(), U->loss_partial, sizeof(double) * lb, cudaMemcpyDeviceToHost, U->stream));
@@ -1978,6 +2037,81 @@ extern "C" int kel_unet_adam_step(kel_unet *U, float lr, float beta1, float beta
 														   c2);
 	KEL_CUDA(cudaGetLastError());
 	return refresh(U);
+}
+
+// forward, backward (device loss), Adam from the device constants, refresh
+static int train_body(kel_unet *U, int32_t n, float b1, float b2, float eps) {
+	int rc;
+	if ((rc = kel_unet_forward(U, n, nullptr))) return rc;
+	if ((rc = unet_backward(U, U->tgt, n, nullptr, U->dev_loss))) return rc;
+	adam_update_dev<<<grid_of(U->nparam), 256, 0, U->stream>>>(U->p, U->g, U->m, U->v, U->nparam, U->adam_c, b1, b2, eps);
+	KEL_CUDA(cudaGetLastError());
+	return refresh(U);
+}
+
+extern "C" int kel_unet_train_step(kel_unet *U, const float *d_target, int32_t n, float lr, float beta1, float beta2,
+								   float eps, int32_t step, double *d_loss) {
+	int rc = check_batch(U, n, "kel_unet_train_step");
+	if (rc) return rc;
+	if (!d_target || step < 1) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_train_step: bad arguments");
+	const int64_t tcount = (int64_t)U->d.max_batch * U->d.height * U->d.width * U->d.out_channels;
+	if (!U->tgt) {
+		KEL_CUDA(cudaMalloc(&U->tgt, sizeof(float) * tcount));
+		KEL_CUDA(cudaMalloc(&U->adam_c, sizeof(float) * 4));
+		KEL_CUDA(cudaMalloc(&U->dev_loss, sizeof(double)));
+	}
+	const int64_t bytes = sizeof(float) * (int64_t)n * U->d.height * U->d.width * U->d.out_channels;
+	KEL_CUDA(cudaMemcpyAsync(U->tgt, d_target, bytes, cudaMemcpyDeviceToDevice, U->stream));
+	const float c1 = 1.f - powf(beta1, (float)step), c2 = 1.f - powf(beta2, (float)step);
+	adam_consts<<<1, 1, 0, U->stream>>>(U->adam_c, lr, c1, c2);
+	KEL_CUDA(cudaGetLastError());
+	const bool same = U->train_graph && U->train_n == n && U->train_b1 == beta1 && U->train_b2 == beta2 &&
+					  U->train_eps == eps;
+	if (!same) {
+		if (U->train_graph) cudaGraphExecDestroy(U->train_graph);
+		U->train_graph = nullptr;
+		if (!U->train_warm) {
+			// the first step runs its launches one by one (one-time set-up of
+			// the kernels happens outside any capture)
+			if ((rc = train_body(U, n, beta1, beta2, eps))) return rc;
+			U->train_warm = true;
+		} else {
+			cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+			KEL_CUDA(cudaStreamIsCapturing(U->stream, &cap));
+			cudaGraph_t g = nullptr;
+			bool ok = cap == cudaStreamCaptureStatusNone &&
+					  cudaStreamBeginCapture(U->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+			if (ok) {
+				rc = train_body(U, n, beta1, beta2, eps);
+				const cudaError_t e = cudaStreamEndCapture(U->stream, &g);
+				ok = rc == KEL_OK && e == cudaSuccess && g && cudaGraphInstantiate(&U->train_graph, g, 0) == cudaSuccess;
+				if (g) cudaGraphDestroy(g);
+				if (rc) return rc;
+			}
+			if (!ok) { // no graph: launches one by one
+				cudaGetLastError();
+				U->train_graph = nullptr;
+				if ((rc = train_body(U, n, beta1, beta2, eps))) return rc;
+			} else {
+				U->train_n = n;
+				U->train_b1 = beta1;
+				U->train_b2 = beta2;
+				U->train_eps = eps;
+			}
+		}
+	}
+	// replay (a graph captured just now has not run yet either)
+	if (U->train_graph) KEL_CUDA(cudaGraphLaunch(U->train_graph, U->stream));
+	if (d_loss) KEL_CUDA(cudaMemcpyAsync(d_loss, U->dev_loss, sizeof(double), cudaMemcpyDeviceToDevice, U->stream));
+	return KEL_OK;
+}
+
+extern "C" int kel_unet_last_loss(kel_unet *U, double *loss) {
+	if (!U || !loss) return fail(KEL_ERR_INVALID_ARGUMENT, "kel_unet_last_loss: null argument");
+	if (!U->dev_loss) return fail(KEL_ERR_STATE, "kel_unet_last_loss: no training step yet");
+	KEL_CUDA(cudaMemcpyAsync(loss, U->dev_loss, sizeof(double), cudaMemcpyDeviceToHost, U->stream));
+	KEL_CUDA(cudaStreamSynchronize(U->stream));
+	return check_device_error(U, "kel_unet_last_loss");
 }
 
 extern "C" int kel_unet_set_stream(kel_unet *U, void *stream) {

@@ -618,3 +618,16 @@ class UNet:
     def adam_step(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
         self.step_count += 1
         _check(self.lib.kel_unet_adam_step(self._h, lr, beta1, beta2, eps, self.step_count), self.lib)
+
+    def train_step(self, d_target, n, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
+        """forward + backward + Adam in one call without a host synchronisation,
+        replayed as a captured CUDA graph (kel_unet_train_step); the loss stays
+        on the device (last_loss reads it)."""
+        self.step_count += 1
+        _check(self.lib.kel_unet_train_step(self._h, C.c_void_p(d_target), n, lr, beta1, beta2, eps,
+                                            self.step_count, None), self.lib)
+
+    def last_loss(self):
+        loss = C.c_double()
+        _check(self.lib.kel_unet_last_loss(self._h, C.byref(loss)), self.lib)
+        return loss.value

@@ -279,19 +279,17 @@ def train(states: SteadyStates, epochs=30, batch=32, lr=2e-3, lr_min_frac=0.02, 
                 mb_tgt = torch.where(f[:, None, None, None], mt, mb_tgt).contiguous()
             torch.cuda.synchronize()
             net.make_input(mb_mask.data_ptr(), mb_umax.data_ptr(), mb_tau.data_ptr(), batch)
-            net.forward(batch)
-            loss = net.backward(mb_tgt.data_ptr(), batch)
             if step < warmup:
                 rate = lr * (step + 1) / warmup
             else:
                 q = (step - warmup) / max(1, total - warmup)
                 rate = lr * (lr_min_frac + (1 - lr_min_frac) * 0.5 * (1 + math.cos(math.pi * q)))
-            net.adam_step(lr=rate)
+            # forward + backward + Adam, a captured graph from the second step on;
+            # the loss is read back only when it is logged
+            net.train_step(mb_tgt.data_ptr(), batch, lr=rate)
             step += 1
-            if log_every and step % log_every == 0:
-                model.history.append((step, loss))
-            elif not log_every:
-                model.history.append((step, loss))
+            if not log_every or step % log_every == 0:
+                model.history.append((step, net.last_loss()))
     net.synchronize()
     return model
 

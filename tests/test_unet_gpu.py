@@ -157,3 +157,33 @@ def test_residual_head_adds_the_input_plane():
         net.set_residual(3, 9, 1.0)
     with pytest.raises(KelError):
         net.set_residual(0, 16, 1.0)
+
+
+def test_train_step_graph_equals_separate_calls():
+    """kel_unet_train_step (first step launched one by one, then a captured
+    graph replayed) against forward + backward + adam_step: the same
+    parameters and losses, bit for bit, over five steps with a changing
+    learning rate; on a 16x256 grid so that both convolution kernels run."""
+    from lbm_mirror_gb300 import UNet
+    rng = np.random.default_rng(12)
+    n, h, w = 2, 16, 256
+    x = np.zeros((n, h, w, 16), np.float32)
+    x[..., :3] = rng.standard_normal((n, h, w, 3))
+    xin = torch.tensor(x, dtype=torch.bfloat16, device="cuda").contiguous()
+    tg = torch.tensor(0.1 * rng.standard_normal((n, h, w, 3)).astype(np.float32), device="cuda").contiguous()
+    a = UNet(height=h, width=w, widths=(16, 32, 32, 48), out_channels=3, max_batch=n, seed=4)
+    b = UNet(height=h, width=w, widths=(16, 32, 32, 48), out_channels=3, max_batch=n, seed=4)
+    torch.cuda.synchronize()
+    la = []
+    for k in range(5):
+        lr = 1e-3 * (k + 1)
+        a.set_input(xin.data_ptr(), n)
+        a.forward(n)
+        la.append(a.backward(tg.data_ptr(), n))
+        a.adam_step(lr=lr)
+        b.set_input(xin.data_ptr(), n)
+        b.train_step(tg.data_ptr(), n, lr=lr)
+        assert b.last_loss() == la[-1], (k, b.last_loss(), la[-1])
+    a.synchronize()
+    b.synchronize()
+    assert np.array_equal(a.params(), b.params())
