@@ -910,45 +910,7 @@ __global__ void bias_grad(const bf16 *dy, int64_t M, int Co, float *db) {
 // channel t % Co and every (blockDim / Co)-th pixel of the chunk (coalesced
 // rows), then the threads of one channel are added in thread order.
 // partial[b][co] is reduced over blocks in order by reduce_partials.
-__global__ void __launch_bounds__(256) channel_sums_partial(const bf16 *dy, int64_t M, int Co, int64_t chunk,
-															 float *partial) {
-	__shared__ float sh[256];
-	const int per = blockDim.x / Co; // pixels in flight per block (Co divides 256)
-	const int c = threadIdx.x % Co, r = threadIdx.x / Co;
-	const int64_t m0 = (int64_t)blockIdx.x * chunk;
-	const int64_t m1 = m0 + chunk < M ? m0 + chunk : M;
-	float s = 0.f;
-	if (r < per)
-		for (int64_t m = m0 + r; m < m1; m += per) s += __bfloat162float(dy[m * Co + c]);
-	sh[threadIdx.x] = s;
-	__syncthreads();
-	if (threadIdx.x < Co) {
-		float t = 0.f;
-		for (int k = 0; k < per; ++k) t += sh[k * Co + threadIdx.x];
-		partial[(int64_t)blockIdx.x * Co + threadIdx.x] = t;
-	}
-}
-
-// db[co] += sum over pixels of dY[m][co], deterministic (fixed chunks and order)
-void bias_grads(const bf16 *dy, int64_t M, int Co, float *scratch, float *db, cudaStream_t st) {
-	if (Co > 256) {
-		bias_grad<<<Co, 256, 0, st>>>(dy, M, Co, db);
-		return;
-	}
-	const int blocks = 304;
-	const int64_t chunk = (M + blocks - 1) / blocks;
-	const int nb = (int)((M + chunk - 1) / chunk);
-	channel_sums_partial<<<nb, 256, 0, st>>>(dy, M, Co, chunk, scratch);
-	launch_reduce_partials(scratch, Co, nb, db, st);
-}
-
-// ---- element-wise pieces -----------------------------------------------------------
-//
-// One thread per pixel and group of 8 channels (channel counts are
-// multiples of 16): 16-byte loads and stores, index arithmetic once per 8
-// values; the per-value arithmetic and its rounding are those of one value
-// at a time.
-
+// 8 bf16 values (16 bytes) to and from floats
 __device__ __forceinline__ void unpack8(const uint4 &q, float (&f)[8]) {
 	const __nv_bfloat162 *h = reinterpret_cast<const __nv_bfloat162 *>(&q);
 #pragma unroll
@@ -966,6 +928,54 @@ __device__ __forceinline__ uint4 pack8(const float (&f)[8]) {
 	for (int k = 0; k < 4; ++k) h[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
 	return q;
 }
+
+// partial[block][c] = sum over the block's pixel chunk of dY[m][c]: thread
+// (g, r) takes channels 8g .. 8g + 7 (one 16-byte load) of the pixels r, r +
+// per, ... of the chunk; the per sums of a channel are then added in order of r
+__global__ void __launch_bounds__(256) channel_sums_partial(const bf16 *dy, int64_t M, int Co, int64_t chunk,
+															 float *partial) {
+	__shared__ float sh[256 * 8];
+	const int G = Co / 8, per = (int)blockDim.x / G; // pixels in flight per block (Co / 8 divides 256)
+	const int g = threadIdx.x % G, r = threadIdx.x / G;
+	const int64_t m0 = (int64_t)blockIdx.x * chunk;
+	const int64_t m1 = m0 + chunk < M ? m0 + chunk : M;
+	float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+	if (r < per)
+		for (int64_t m = m0 + r; m < m1; m += per) {
+			float v[8];
+			unpack8(reinterpret_cast<const uint4 *>(dy + m * Co)[g], v);
+#pragma unroll
+			for (int e = 0; e < 8; ++e) acc[e] += v[e];
+		}
+#pragma unroll
+	for (int e = 0; e < 8; ++e) sh[threadIdx.x * 8 + e] = acc[e];
+	__syncthreads();
+	for (int c = threadIdx.x; c < Co; c += blockDim.x) {
+		float t = 0.f;
+		for (int k = 0; k < per; ++k) t += sh[(k * G + c / 8) * 8 + c % 8];
+		partial[(int64_t)blockIdx.x * Co + c] = t;
+	}
+}
+
+// db[co] += sum over pixels of dY[m][co], deterministic (fixed chunks and order)
+void bias_grads(const bf16 *dy, int64_t M, int Co, float *scratch, float *db, cudaStream_t st) {
+	if (Co > 256) {
+		bias_grad<<<Co, 256, 0, st>>>(dy, M, Co, db);
+		return;
+	}
+	const int blocks = 1216;
+	const int64_t chunk = (M + blocks - 1) / blocks;
+	const int nb = (int)((M + chunk - 1) / chunk);
+	channel_sums_partial<<<nb, 256, 0, st>>>(dy, M, Co, chunk, scratch);
+	launch_reduce_partials(scratch, Co, nb, db, st);
+}
+
+// ---- element-wise pieces -----------------------------------------------------------
+//
+// One thread per pixel and group of 8 channels (channel counts are
+// multiples of 16): 16-byte loads and stores, index arithmetic once per 8
+// values; the per-value arithmetic and its rounding are those of one value
+// at a time.
 
 // dy = 0 where !(y > 0); n values (a multiple of 8)
 __global__ void relu_backward(bf16 *dy, const bf16 *y, int64_t n) {
@@ -1187,37 +1197,55 @@ __global__ void head_backward_dw(const float *dy, const bf16 *x, int64_t M, int 
 // block b covers pixels [b * chunk, ...); thread t owns input channel t % Ci
 // and every (256 / Ci)-th pixel; partial[b][co * Ci + ci] and, for the bias,
 // partial[b][Co * Ci + co]; reduced over blocks in order by reduce_partials.
+// Head weight and bias gradient partials over a chunk of pixels per block
+// (Co <= 8): thread (g, r) takes input channels 8g .. 8g + 7 (one 16-byte
+// load) of the pixels r, r + per, ...; per output channel the per sums are
+// then added in order of r (threads g = 0 also sum dy for the bias).
 __global__ void __launch_bounds__(256) head_dw_partial(const float *dy, const bf16 *x, int64_t M, int Ci, int Co,
 														int64_t chunk, float *partial) {
-	__shared__ float sh[2][256];
-	const int per = blockDim.x / Ci;
-	const int ci = threadIdx.x % Ci, r = threadIdx.x / Ci;
+	__shared__ float sh[256 * 8];
+	__shared__ float shb[256];
+	const int G = Ci / 8, per = (int)blockDim.x / G;
+	const int g = threadIdx.x % G, r = threadIdx.x / G;
 	const int64_t m0 = (int64_t)blockIdx.x * chunk;
 	const int64_t m1 = m0 + chunk < M ? m0 + chunk : M;
-	float acc[8], bacc[8];
-	for (int k = 0; k < 8; ++k) acc[k] = bacc[k] = 0.f;
+	float acc[MAX_RES][8], bacc[MAX_RES];
+#pragma unroll
+	for (int co = 0; co < MAX_RES; ++co) {
+		bacc[co] = 0.f;
+#pragma unroll
+		for (int e = 0; e < 8; ++e) acc[co][e] = 0.f;
+	}
 	if (r < per)
 		for (int64_t m = m0 + r; m < m1; m += per) {
-			const float xv = __bfloat162float(x[m * Ci + ci]);
-			for (int co = 0; co < Co; ++co) {
+			float xv[8];
+			unpack8(reinterpret_cast<const uint4 *>(x + m * Ci)[g], xv);
+#pragma unroll
+			for (int co = 0; co < MAX_RES; ++co) {
+				if (co >= Co) break;
 				const float d = dy[m * Co + co];
-				acc[co] += d * xv;
 				bacc[co] += d;
+#pragma unroll
+				for (int e = 0; e < 8; ++e) acc[co][e] += d * xv[e];
 			}
 		}
 	const int64_t base = (int64_t)blockIdx.x * (Co * Ci + Co);
-	for (int co = 0; co < Co; ++co) {
-		sh[0][threadIdx.x] = acc[co];
-		sh[1][threadIdx.x] = bacc[co];
+#pragma unroll
+	for (int co = 0; co < MAX_RES; ++co) {
+		if (co >= Co) break;
+#pragma unroll
+		for (int e = 0; e < 8; ++e) sh[threadIdx.x * 8 + e] = acc[co][e];
+		shb[threadIdx.x] = bacc[co];
 		__syncthreads();
-		if (threadIdx.x < Ci) {
-			float t = 0.f, tb = 0.f;
-			for (int k = 0; k < per; ++k) {
-				t += sh[0][k * Ci + threadIdx.x];
-				tb += sh[1][k * Ci + threadIdx.x];
-			}
-			partial[base + co * Ci + threadIdx.x] = t;
-			if (threadIdx.x == 0) partial[base + Co * Ci + co] = tb; // ci == 0 threads saw every pixel once
+		for (int c = threadIdx.x; c < Ci; c += blockDim.x) {
+			float t = 0.f;
+			for (int k = 0; k < per; ++k) t += sh[(k * G + c / 8) * 8 + c % 8];
+			partial[base + co * Ci + c] = t;
+		}
+		if (threadIdx.x == 0) { // the g = 0 threads saw every pixel once
+			float tb = 0.f;
+			for (int k = 0; k < per; ++k) tb += shb[k * G];
+			partial[base + Co * Ci + co] = tb;
 		}
 		__syncthreads();
 	}
@@ -1973,7 +2001,7 @@ static int unet_backward(kel_unet *U, const float *d_target, int32_t n, double *
 	// head
 	head_backward_dx<<<grid_of(M), 256, sizeof(float) * hd.co * hd.ci, U->stream>>>(U->dout, U->p + hd.woff, G[T_D0B],
 																						 M, hd.ci, hd.co);
-	if (hd.co <= 8 && 256 % hd.ci == 0) {
+	if (hd.co <= 8 && hd.ci % 8 == 0 && hd.ci <= 2048) {
 		// enough blocks to keep every SM's loads in flight (each block's loop is
 		// a chain of dependent accumulations)
 		const int64_t chunk = (M + 1215) / 1216;
