@@ -764,6 +764,187 @@ __global__ void __launch_bounds__(128) conv_wgrad_tc(TcWgradArgs a) {
 	}
 }
 
+// ---- weight gradient from TMA-loaded halo rows ----------------------------------
+//
+// For each column shift dx of the 3x3 stencil one accumulator
+// D[(r, ci)][co] = sum over the pixels p of the CTA's row tiles of
+// x[y - 1 + r][p - 1 + dx][ci] dY[y][p][co]: M = 128 rows of (halo row r,
+// input channel ci) pairs, N = Co, K = the WT pixels of a row tile (WT = W,
+// at most 128).  Per row tile the input arrives as one TMA box of rows_box
+// halo rows x (WT + 2) pixels x CT channels, zero-filled outside the image,
+// laid out halo row major: element (row r, channel group g, pixel p, channel
+// e) at ((r * CT / 8 + g) * (WT + 2) + p) * 16 + 2 e.  The 8-row groups of M
+// (channel groups, then halo rows) are then R = (WT + 2) * 16 bytes apart --
+// the descriptor's stride byte offset -- and pixels 16 bytes apart, so the
+// shift dx only moves the descriptor's start by 16 dx bytes (MN-major, no
+// swizzle: core matrices of 8 pixels x 8 channels, K-direction stride 128 B).
+// dY arrives as (channel group, pixel, 8 channels), N-direction stride WT * 16.
+// With CT <= 32 channels per tile one accumulator holds all three halo rows
+// (RPM = 3 rows per MMA, 3 CT of its 128 rows used); with CT = 128 each halo
+// row is a row group of its own (RPM = 1), and when 9 Co columns do not fit
+// TMEM the three row groups go to three CTAs (rows_box = 1).  M rows past the
+// loaded halo read other shared memory of the CTA; their accumulator lanes
+// are never stored.  A CTA sums the row tiles of its chunk (consecutive tiles
+// in (n, y, x tile) order) and writes partial[chunk][co][tap * Ci + ci],
+// reduced later in chunk order.  One thread issues the copies and the MMAs;
+// waits are bounded and handled as in conv_halo.
+
+struct WhaloArgs {
+	float *partial; // (chunks, Co, 9 Ci)
+	int N, H, W, Ci, Co;
+	int WT, CT, RPM, RG;    // row tile width, channels per tile, halo rows per MMA, row groups
+	int rg_cta, rows_box;   // row groups per CTA, halo rows per TMA box
+	int ci_tiles, cta_groups;
+	int64_t tiles, per_chunk; // row tiles in all and per chunk
+	int stages;
+	uint32_t x_bytes, dy_bytes;  // TMA box bytes
+	uint32_t x_span, dy_span;    // shared-memory bytes per stage of each
+	uint32_t dy_off, mbar_off;   // offsets of the dY stages and the mbarriers
+	uint32_t tmem_cols;
+	int *err;
+};
+
+__global__ void __launch_bounds__(128) conv_wgrad_halo(const __grid_constant__ CUtensorMap tx,
+													   const __grid_constant__ CUtensorMap tdy, WhaloArgs a) {
+	extern __shared__ __align__(1024) uint8_t sm[];
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int S = a.stages;
+	uint64_t *full = reinterpret_cast<uint64_t *>(sm + a.mbar_off);
+	uint64_t *done = full + S;
+	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + S);
+
+	const int grp = (int)(blockIdx.x % (unsigned)a.cta_groups);
+	const int rest = (int)(blockIdx.x / (unsigned)a.cta_groups);
+	const int ct = rest % a.ci_tiles;
+	const int64_t chunk = rest / a.ci_tiles;
+	const int64_t t0 = chunk * a.per_chunk;
+	const int64_t t1 = t0 + a.per_chunk < a.tiles ? t0 + a.per_chunk : a.tiles;
+	const int nsteps = (int)(t1 - t0);
+	const int tpr = a.W / a.WT;
+	const int row0 = grp * a.rg_cta * a.RPM; // first halo row of this CTA (0: y - 1)
+	const int cg = a.CT / 8;
+	const uint32_t R = (uint32_t)(a.WT + 2) * 16u;
+	const uint32_t grp_bytes = (uint32_t)(a.RPM * cg) * R;
+	const int nk = a.WT / 16;
+
+	if (tid == 0) {
+		for (int s = 0; s < S; ++s) {
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(full + s)));
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(done + s)));
+		}
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+	}
+	if (warp == 0) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+					 "r"(a.tmem_cols));
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+	const uint32_t tmem = *tmem_slot;
+
+	// D f32, A bf16, B bf16, A and B MN-major, N = Co, M = 128
+	const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 15) | (1u << 16) |
+						   ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+	int fail = 0, loaded = 0, issued = -1;
+	if (tid == 0) {
+		auto load = [&](int i) {
+			const int s = i % S;
+			const int64_t t = t0 + i;
+			const int xt = (int)(t % tpr);
+			const int64_t rw = t / tpr; // n * H + y
+			const int n = (int)(rw / a.H), y = (int)(rw - (int64_t)n * a.H);
+			const uint32_t xb = smem_u32(sm + (size_t)s * a.x_span);
+			const uint32_t db = smem_u32(sm + a.dy_off + (size_t)s * a.dy_span);
+			mbar_expect_tx(smem_u32(full + s), a.x_bytes + a.dy_bytes);
+			tma_load_5d(xb, &tx, smem_u32(full + s), 0, xt * a.WT - 1, ct * cg, y - 1 + row0, n);
+			tma_load_5d(db, &tdy, smem_u32(full + s), 0, xt * a.WT, 0, y, n);
+		};
+		for (int i = 0; i < S && i < nsteps; ++i) load(i);
+		loaded = S < nsteps ? S : nsteps;
+		for (int i = 0; i < nsteps; ++i) {
+			const int s = i % S;
+			if (!mbar_wait(smem_u32(full + s), (uint32_t)((i / S) & 1))) {
+				fail = 1;
+				break;
+			}
+			asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+			const uint32_t xb = smem_u32(sm + (size_t)s * a.x_span);
+			const uint32_t db = smem_u32(sm + a.dy_off + (size_t)s * a.dy_span);
+			for (int k = 0; k < nk; ++k) {
+				const uint64_t bd = umma_desc(db + (uint32_t)k * 256u, 128u, (uint32_t)a.WT * 16u);
+				for (int g = 0; g < a.rg_cta; ++g)
+					for (int dx = 0; dx < 3; ++dx) {
+						const uint64_t ad =
+							umma_desc(xb + (uint32_t)g * grp_bytes + (uint32_t)(16 * k + dx) * 16u, 128u, R);
+						const uint32_t acc = (i > 0 || k > 0) ? 1u : 0u;
+						asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+									 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+										 tmem + (uint32_t)((g * 3 + dx) * a.Co)),
+									 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+					}
+			}
+			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+				smem_u32(done + s)));
+			issued = i;
+			// refill the stage tile i - 1 used once its MMAs are done (tile
+			// i's are queued behind them meanwhile)
+			if (i >= 1 && i - 1 + S < nsteps) {
+				const int ip = i - 1;
+				if (!mbar_wait(smem_u32(done + ip % S), (uint32_t)((ip / S) & 1))) {
+					fail = 1;
+					break;
+				}
+				load(ip + S);
+				++loaded;
+			}
+		}
+		if (issued >= 0 && !mbar_wait(smem_u32(done + issued % S), (uint32_t)((issued / S) & 1))) fail = 1;
+		for (int i = issued + 1; i < loaded; ++i) mbar_wait(smem_u32(full + i % S), (uint32_t)((i / S) & 1));
+		if (fail || issued != nsteps - 1) atomicExch(a.err, 1);
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	const int failed = __syncthreads_or(tid == 0 && (fail || issued != nsteps - 1));
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+	if (!failed && warp * 32 < a.RPM * a.CT) {
+		// warp w owns TMEM lanes 32 w .. 32 w + 31: lane L = (halo row r, channel ci)
+		const int L = warp * 32 + lane;
+		const int r = L / a.CT, ci = L - (L / a.CT) * a.CT;
+		const int K = 9 * a.Ci;
+		float *out = a.partial + chunk * (int64_t)a.Co * K;
+		for (int g = 0; g < a.rg_cta; ++g) {
+			const int hrow = row0 + g * a.RPM + r;
+			const bool ok = r < a.RPM && hrow < 3;
+			for (int dx = 0; dx < 3; ++dx) {
+				const int col = (hrow * 3 + dx) * a.Ci + ct * a.CT + ci;
+				for (int c0 = 0; c0 < a.Co; c0 += 16) {
+					uint32_t v[16];
+					const uint32_t taddr =
+						tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((g * 3 + dx) * a.Co + c0);
+					asm volatile(
+						"tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+						"[%16];\n"
+						: "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+						  "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+						  "=r"(v[14]), "=r"(v[15])
+						: "r"(taddr));
+					asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+					if (ok)
+#pragma unroll
+						for (int q = 0; q < 16; ++q) out[(int64_t)(c0 + q) * K + col] = __uint_as_float(v[q]);
+				}
+			}
+		}
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	if (warp == 0) {
+		asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tmem_cols));
+	}
+}
+
 // ---- weight gradient: dW[co][k] = sum_m dY[m][co] * im2col(X)[m][k] -------------
 
 struct WgradArgs {
@@ -865,7 +1046,6 @@ __global__ void __launch_bounds__(128) conv_wgrad(WgradArgs a) {
 			}
 }
 
-// grad[j] += sum over chunks of partial[c][j], chunks in order
 // grad[j] += sum over the chunks of partial[c][j], in a fixed order: block
 // (32, 8) takes 32 consecutive j; thread row y sums the chunks of its eighth
 // [c0, c1) in order, then the eight sums are added in order of y.
@@ -1450,6 +1630,7 @@ struct kel_unet {
 	float *col_open = nullptr, *col_h3 = nullptr, *col_res = nullptr, *col_pl = nullptr; // input-feature scratch (max_batch x W)
 	HeadRes res; // residual head per output channel (kel_unet_set_residual)
 	cudaStream_t own_stream = nullptr; // the stream the net created (stream may be a caller's)
+	int sms = 0;                       // the device's SM count (grid sizing)
 	// kel_unet_train_step: the target copy, Adam's lr and bias corrections on
 	// the device, the last loss, and the captured step (forward, backward,
 	// Adam, weight refresh) for batch train_n and these Adam constants
@@ -1646,9 +1827,132 @@ int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
 	return KEL_OK;
 }
 
+// Plan of conv_wgrad_halo for a layer; 0 when the layer does not fit it.
+// Channels per tile: 128 when Ci allows (one halo row per MMA, all 128 M rows
+// used), else 32 or 16 (three halo rows per MMA).  Stages: up to four within
+// 110 KB when the CTA's TMEM columns leave room for a second CTA on the SM,
+// else up to six within 220 KB (one CTA per SM).
+int whalo_plan(int Ci, int Co, int W, WhaloArgs &a) {
+	if (Co % 16 || Co < 16 || Co > 256 || Ci % 16) return 0;
+	a.WT = W >= 128 ? 128 : W;
+	if (a.WT % 16 || W % a.WT) return 0;
+	if (Ci % 128 == 0) {
+		a.CT = 128;
+		a.RPM = 1;
+		a.RG = 3;
+	} else {
+		a.CT = Ci % 32 == 0 ? 32 : 16;
+		a.RPM = 3;
+		a.RG = 1;
+	}
+	a.rg_cta = a.RG * 3 * Co <= 512 ? a.RG : 1;
+	if (a.rg_cta * 3 * Co > 512) return 0;
+	a.cta_groups = a.RG / a.rg_cta;
+	a.ci_tiles = Ci / a.CT;
+	a.rows_box = a.rg_cta * a.RPM;
+	const uint32_t R = (uint32_t)(a.WT + 2) * 16u, cg = (uint32_t)a.CT / 8u;
+	a.x_bytes = (uint32_t)a.rows_box * cg * R;
+	a.dy_bytes = (uint32_t)a.WT * (uint32_t)Co * 2u;
+	a.x_span = align1k(a.x_bytes);
+	a.dy_span = align1k(a.dy_bytes);
+	// the last row group's MMAs read 16 channel groups of 8 rows from its start
+	const uint64_t need = ((uint64_t)(a.rg_cta - 1) * a.RPM * cg + 16u) * R;
+	a.tmem_cols = 32;
+	while (a.tmem_cols < (uint32_t)(a.rg_cta * 3 * Co)) a.tmem_cols <<= 1;
+	auto operand_bytes = [&](int S) -> uint64_t {
+		uint64_t t = (uint64_t)S * (a.x_span + a.dy_span), r = (uint64_t)(S - 1) * a.x_span + need;
+		return align1k(t > r ? t : r);
+	};
+	a.stages = 0;
+	if (a.tmem_cols <= 256)
+		for (int S = 4; S >= 2 && !a.stages; --S)
+			if (operand_bytes(S) + 1024 <= 110u * 1024u) a.stages = S;
+	if (!a.stages)
+		for (int S = 6; S >= 2 && !a.stages; --S)
+			if (operand_bytes(S) + 1024 <= 220u * 1024u) a.stages = S;
+	if (!a.stages) return 0;
+	a.dy_off = (uint32_t)a.stages * a.x_span;
+	a.mbar_off = (uint32_t)operand_bytes(a.stages);
+	return 1;
+}
+
+// conv_wgrad_halo for one layer (weight gradient into U->partial, reduced into
+// the layer's gradient); returns 0 without launching when the layer does not
+// fit it.
+int wgrad_halo_launch(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy, int n, int *launched) {
+	*launched = 0;
+	const EncodeTiledFn enc = encode_tiled();
+	WhaloArgs a;
+	memset(&a, 0, sizeof(a));
+	const int H = U->d.height >> l.level, W = U->d.width >> l.level;
+	if (!enc || !whalo_plan(l.ci, l.co, W, a)) return KEL_OK;
+	CUtensorMap tx, tdy;
+	{ // x (N,H,W,Ci) as (8 channels, x, channel group, y, n)
+		const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)(l.ci / 8), (cuuint64_t)H, (cuuint64_t)n};
+		const cuuint64_t strides[4] = {(cuuint64_t)l.ci * 2, 16, (cuuint64_t)W * l.ci * 2, (cuuint64_t)H * W * l.ci * 2};
+		const cuuint32_t box[5] = {8, (cuuint32_t)(a.WT + 2), (cuuint32_t)(a.CT / 8), (cuuint32_t)a.rows_box, 1};
+		const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+		if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(x), dims, strides, box, es,
+				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+				CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+			return KEL_OK;
+	}
+	{ // dY (N,H,W,Co) as (8 channels, x, channel group, y, n)
+		const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)(l.co / 8), (cuuint64_t)H, (cuuint64_t)n};
+		const cuuint64_t strides[4] = {(cuuint64_t)l.co * 2, 16, (cuuint64_t)W * l.co * 2, (cuuint64_t)H * W * l.co * 2};
+		const cuuint32_t box[5] = {8, (cuuint32_t)a.WT, (cuuint32_t)(l.co / 8), 1, 1};
+		const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+		if (enc(&tdy, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(dy), dims, strides, box, es,
+				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+				CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+			return KEL_OK;
+	}
+	a.partial = U->partial;
+	a.N = n;
+	a.H = H;
+	a.W = W;
+	a.Ci = l.ci;
+	a.Co = l.co;
+	a.err = U->d_err;
+	a.tiles = (int64_t)n * H * (W / a.WT);
+	// one wave: two CTAs per SM when TMEM and shared memory allow it
+	const size_t smem = (size_t)a.mbar_off + (size_t)a.stages * 16 + 16;
+	const int per_sm = (a.tmem_cols <= 256 && smem <= 110u * 1024u) ? 2 : 1;
+	const int per_chunk_ctas = a.ci_tiles * a.cta_groups;
+	const int64_t per = (int64_t)l.co * 9 * l.ci;
+	int64_t chunks = ((int64_t)per_sm * (U->sms > 0 ? U->sms : 148) + per_chunk_ctas / 2) / per_chunk_ctas;
+	if (chunks > U->partial_len / per) chunks = U->partial_len / per;
+	if (chunks > a.tiles) chunks = a.tiles;
+	if (chunks < 1) chunks = 1;
+	a.per_chunk = (a.tiles + chunks - 1) / chunks;
+	chunks = (a.tiles + a.per_chunk - 1) / a.per_chunk;
+	static bool attr_set = false;
+	if (!attr_set) {
+		KEL_CUDA(cudaFuncSetAttribute(conv_wgrad_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, 222 * 1024));
+		attr_set = true;
+	}
+	// one CTA per SM when its TMEM columns would not leave room for a second
+	const size_t smem_launch = per_sm == 1 && smem < 116u * 1024u ? 116u * 1024u : smem;
+	conv_wgrad_halo<<<(unsigned)(chunks * per_chunk_ctas), 128, smem_launch, U->stream>>>(tx, tdy, a);
+	KEL_CUDA(cudaGetLastError());
+	launch_reduce_partials(U->partial, per, (int)chunks, U->g + l.woff, U->stream);
+	*launched = 1;
+	return KEL_OK;
+}
+
 int conv_grads_tc(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy, int n) {
 	if (l.ci % 16 || l.co % 16 || l.co > 256)
 		return fail(KEL_ERR_UNSUPPORTED, "wgrad: tensor-core path needs c_in, c_out multiples of 16, c_out <= 256");
+	{
+		int launched = 0, rc;
+		if ((rc = wgrad_halo_launch(U, l, x, dy, n, &launched))) return rc;
+		if (launched) {
+			const int64_t M = (int64_t)n * (U->d.height >> l.level) * (U->d.width >> l.level);
+			bias_grads(dy, M, l.co, U->partial, U->g + l.woff + (int64_t)l.co * 9 * l.ci, U->stream);
+			KEL_CUDA(cudaGetLastError());
+			return KEL_OK;
+		}
+	}
 	TcWgradArgs a;
 	a.x = x;
 	a.dy = dy;
@@ -1794,6 +2098,11 @@ extern "C" int kel_unet_create(const kel_unet_desc *desc, uint64_t seed, kel_une
 		U->L.push_back(l);
 	}
 	U->nparam = off;
+	{
+		int dev = 0;
+		cudaGetDevice(&dev);
+		cudaDeviceGetAttribute(&U->sms, cudaDevAttrMultiProcessorCount, dev);
+	}
 	cudaStreamCreateWithFlags(&U->stream, cudaStreamNonBlocking);
 	U->own_stream = U->stream;
 	auto fail_out = [&](cudaError_t e) {
