@@ -590,6 +590,201 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 	}
 }
 
+// ---- row-run convolution: resident weights, rolling halo rows ---------------------
+//
+// For layers whose weights and four input rows fit shared memory: one CTA
+// computes RL consecutive output rows of one 128-pixel column tile (n, x0).
+// The weights (Co x 9 x Ci) arrive once, by TMA, as [g][tap][co][8 channels]
+// (B of tap t and channel groups 2j, 2j + 1 at ((2 j) * 9 + t) * Co * 16,
+// K-direction stride 9 * Co * 16 B).  Input rows y0 - 1 .. y0 + RL arrive one
+// by one into a ring of NR slots, each row a TMA box of 130 pixels x Ci
+// channels, zero-filled outside the image, laid out (channel group, pixel, 8
+// channels): the A operand of output row y and tap (dy, dx) is the slot of
+// input row y - 1 + dy read from pixel dx (K-major, no swizzle: 8-pixel stride
+// 128 B, channel-group stride 130 * 16 B).  So every input row is read once
+// per CTA instead of three times, and the weights once per RL rows.
+// Warp roles: warp 0 issues the copies, warp 1 the MMAs, warps 2-5 drain
+// the accumulators (bias, ReLU, bf16, NHWC stores).  The accumulator is
+// double-buffered in TMEM (2 x Co columns), so row i + 1's MMAs run while
+// row i is stored.  mbarriers: row_full/row_empty per ring slot (TMA bytes;
+// the MMAs of the last output row that reads the slot), w_full, acc_full and
+// acc_empty per accumulator (MMA commit; the four epilogue warps).  Every
+// wait is bounded; on timeout the thread records the failure in *err and
+// stops, the producer waits (bounded) for the copies it issued, and the MMA
+// thread for its MMAs before TMEM is freed.
+
+struct RowsArgs {
+	const float *bias;
+	bf16 *y; // (N,H,W,Co)
+	int N, H, W, Ci, Co;
+	int relu, use_bias;
+	int RL, NR, runs; // output rows per CTA, ring slots, CTAs per column tile
+	uint32_t row_bytes, row_span, w_bytes, w_off, mbar_off;
+	uint32_t tmem_cols;
+	int *err;
+};
+
+__global__ void __launch_bounds__(192) conv_rows(const __grid_constant__ CUtensorMap tx,
+												 const __grid_constant__ CUtensorMap tw, RowsArgs a) {
+	extern __shared__ __align__(1024) uint8_t sm[];
+	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+	const int NR = a.NR;
+	uint64_t *row_full = reinterpret_cast<uint64_t *>(sm + a.mbar_off);
+	uint64_t *row_empty = row_full + NR;
+	uint64_t *w_full = row_empty + NR;
+	uint64_t *acc_full = w_full + 1;
+	uint64_t *acc_empty = acc_full + 2;
+	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+
+	const int tpr = a.W / 128;
+	const int colt = (int)(blockIdx.x / (unsigned)a.runs), run = (int)(blockIdx.x % (unsigned)a.runs);
+	const int n = colt / tpr, x0 = (colt % tpr) * 128;
+	const int y0 = run * a.RL;
+	const int rows = a.H - y0 < a.RL ? a.H - y0 : a.RL;
+	const int nx = rows + 2;
+	constexpr uint32_t R = HX * 16u;
+
+	if (tid == 0) {
+		for (int s = 0; s < NR; ++s) {
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(row_full + s)));
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(row_empty + s)));
+		}
+		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(w_full)));
+		for (int b = 0; b < 2; ++b) {
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(acc_full + b)));
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(smem_u32(acc_empty + b)));
+		}
+		asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
+	}
+	if (warp == 1) {
+		asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(tmem_slot)),
+					 "r"(a.tmem_cols));
+		asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::);
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+	const uint32_t tmem = *tmem_slot;
+
+	if (warp == 0) {
+		if (lane == 0) { // producer
+			int fail = 0, issued = 0;
+			mbar_expect_tx(smem_u32(w_full), a.w_bytes);
+			tma_load_4d(smem_u32(sm + a.w_off), &tw, smem_u32(w_full), 0, 0, 0, 0);
+			for (int j = 0; j < nx; ++j) {
+				const int s = j % NR;
+				if (j >= NR && !mbar_wait(smem_u32(row_empty + s), (uint32_t)(((j / NR) - 1) & 1))) {
+					fail = 1;
+					break;
+				}
+				mbar_expect_tx(smem_u32(row_full + s), a.row_bytes);
+				tma_load_5d(smem_u32(sm + (size_t)s * a.row_span), &tx, smem_u32(row_full + s), 0, x0 - 1, 0,
+							y0 - 1 + j, n);
+				issued = j + 1;
+			}
+			// the last copy of each slot has landed before the CTA can end
+			for (int j = issued > NR ? issued - NR : 0; j < issued; ++j)
+				mbar_wait(smem_u32(row_full + j % NR), (uint32_t)((j / NR) & 1));
+			mbar_wait(smem_u32(w_full), 0u);
+			if (fail) atomicExch(a.err, 1);
+		}
+	} else if (warp == 1) {
+		if (lane == 0) { // MMA issuer
+			// D f32, A bf16, B bf16, both K-major, N = Co, M = 128
+			const uint32_t idesc =
+				(1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+			const uint32_t lbo_b = 9u * (uint32_t)a.Co * 16u;
+			const uint32_t wbase = smem_u32(sm + a.w_off);
+			const int nk = a.Ci / 16;
+			int fail = !mbar_wait(smem_u32(w_full), 0u), done = 0;
+			for (int i = 0; i < rows && !fail; ++i) {
+				for (int j = i == 0 ? 0 : i + 2; j <= i + 2 && !fail; ++j)
+					if (!mbar_wait(smem_u32(row_full + j % NR), (uint32_t)((j / NR) & 1))) fail = 1;
+				const int b = i & 1;
+				if (!fail && i >= 2 && !mbar_wait(smem_u32(acc_empty + b), (uint32_t)(((i >> 1) - 1) & 1))) fail = 1;
+				if (fail) break;
+				asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+				for (int t = 0; t < 9; ++t) {
+					const int dy = t / 3, dx = t % 3;
+					const uint32_t xbase = smem_u32(sm + (size_t)((i + dy) % NR) * a.row_span) + (uint32_t)dx * 16u;
+					for (int k = 0; k < nk; ++k) {
+						const uint64_t ad = umma_desc(xbase + (uint32_t)(2 * k) * R, R, 128u);
+						const uint64_t bd = umma_desc(wbase + ((uint32_t)(2 * k) * 9u + (uint32_t)t) * (uint32_t)a.Co * 16u,
+													  lbo_b, 128u);
+						const uint32_t acc = (t > 0 || k > 0) ? 1u : 0u;
+						asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+									 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+										 tmem + (uint32_t)(b * a.Co)),
+									 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+					}
+				}
+				// input row i is read by no later output row
+				if (i + 1 < rows)
+					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+						smem_u32(row_empty + i % NR)));
+				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+					smem_u32(acc_full + b)));
+				done = i + 1;
+			}
+			// the MMAs have finished before TMEM is freed
+			if (done > 0) mbar_wait(smem_u32(acc_full + ((done - 1) & 1)), (uint32_t)(((done - 1) >> 1) & 1));
+			if (fail) atomicExch(a.err, 1);
+		}
+	} else { // epilogue: warp w reads TMEM lanes (pixels) 32 (w % 4) .. + 31
+		const int q = warp & 3;
+		const int px = q * 32 + lane;
+		int fail = 0;
+		for (int i = 0; i < rows; ++i) {
+			const int b = i & 1;
+			if (!mbar_wait(smem_u32(acc_full + b), (uint32_t)((i >> 1) & 1))) {
+				fail = 1;
+				break;
+			}
+			asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+			const int64_t m = ((int64_t)n * a.H + y0 + i) * a.W + x0 + px;
+			for (int c0 = 0; c0 < a.Co; c0 += 16) {
+				uint32_t r[16];
+				const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * a.Co + c0);
+				asm volatile(
+					"tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+					"[%16];\n"
+					: "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+					  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+					  "=r"(r[15])
+					: "r"(taddr));
+				asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+				__align__(16) __nv_bfloat162 o[8];
+#pragma unroll
+				for (int k = 0; k < 8; ++k) {
+					float v0 = __uint_as_float(r[2 * k]), v1 = __uint_as_float(r[2 * k + 1]);
+					if (a.use_bias) {
+						v0 += a.bias[c0 + 2 * k];
+						v1 += a.bias[c0 + 2 * k + 1];
+					}
+					if (a.relu) {
+						v0 = fmaxf(v0, 0.f);
+						v1 = fmaxf(v1, 0.f);
+					}
+					o[k] = __floats2bfloat162_rn(v0, v1);
+				}
+				uint4 *dst = reinterpret_cast<uint4 *>(a.y + m * a.Co + c0);
+				dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
+				dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
+			}
+			asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+			__syncwarp();
+			if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(acc_empty + b)) : "memory");
+		}
+		if (fail && lane == 0) atomicExch(a.err, 1);
+	}
+	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+	__syncthreads();
+	if (warp == 1) {
+		asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+		asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(a.tmem_cols));
+	}
+}
+
 // ---- weight gradient on the tensor cores -----------------------------------------
 //
 // D[kcol][co] = sum over a chunk of pixels m of im2col(X)[m][kcol] dY[m][co]:
@@ -1774,6 +1969,91 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	return KEL_OK;
 }
 
+// Plan of conv_rows for a layer (W a multiple of 128; the weights and four
+// input rows within 200 KB of shared memory); 0 when the layer does not fit
+// it.  Rows per CTA: the run length that minimises (waves of CTAs) x (rows +
+// 3), the three being the two extra input rows and the weight load of a run.
+int rows_plan(const kel_unet *U, int n, int H, int W, int Ci, int Co, RowsArgs &a) {
+	if (W % 128 || Ci % 16 || Co % 16 || Co < 16 || Co > 256 || H < 1) return 0;
+	a.NR = 4;
+	a.row_bytes = (uint32_t)HX * (uint32_t)Ci * 2u;
+	a.row_span = (a.row_bytes + 127u) / 128u * 128u;
+	a.w_bytes = (uint32_t)Co * 9u * (uint32_t)Ci * 2u;
+	a.tmem_cols = 32;
+	while (a.tmem_cols < 2u * (uint32_t)Co) a.tmem_cols <<= 1;
+	a.w_off = (uint32_t)a.NR * a.row_span;
+	a.mbar_off = a.w_off + (a.w_bytes + 127u) / 128u * 128u;
+	const uint32_t smem = a.mbar_off + (2u * (uint32_t)a.NR + 5u) * 8u + 16u;
+	if (smem > 200u * 1024u) return 0;
+	int per_sm = (int)((227u * 1024u) / (smem + 1024u));
+	if (per_sm > (int)(512u / a.tmem_cols)) per_sm = (int)(512u / a.tmem_cols);
+	if (per_sm > 10) per_sm = 10;
+	if (per_sm < 1) per_sm = 1;
+	const int64_t cols = (int64_t)n * (W / 128), slots = (int64_t)per_sm * (U->sms > 0 ? U->sms : 148);
+	int64_t best = -1;
+	for (int k = 1; k <= H; ++k) {
+		const int RL = (H + k - 1) / k, runs = (H + RL - 1) / RL;
+		const int64_t waves = (cols * runs + slots - 1) / slots, cost = waves * (RL + 3);
+		if (best < 0 || cost < best) {
+			best = cost;
+			a.RL = RL;
+			a.runs = runs;
+		}
+	}
+	return 1;
+}
+
+// conv_rows for one layer; returns 0 without launching when it does not fit.
+int conv_rows_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y, int n, int H, int W, int ci,
+					 int co, bool relu, bool bias, int *launched) {
+	*launched = 0;
+	const EncodeTiledFn enc = encode_tiled();
+	RowsArgs a;
+	memset(&a, 0, sizeof(a));
+	if (!enc || !rows_plan(U, n, H, W, ci, co, a)) return KEL_OK;
+	CUtensorMap tx, tw;
+	{ // x (N,H,W,Ci) as (8 channels, x, channel group, y, n): one row per box
+		const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)(ci / 8), (cuuint64_t)H, (cuuint64_t)n};
+		const cuuint64_t strides[4] = {(cuuint64_t)ci * 2, 16, (cuuint64_t)W * ci * 2, (cuuint64_t)H * W * ci * 2};
+		const cuuint32_t box[5] = {8, HX, (cuuint32_t)(ci / 8), 1, 1};
+		const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+		if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(x), dims, strides, box, es,
+				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+				CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+			return KEL_OK;
+	}
+	{ // w (Co, 9, Ci) as (8 channels, co, tap, channel group): the whole tensor
+		const cuuint64_t dims[4] = {8, (cuuint64_t)co, 9, (cuuint64_t)(ci / 8)};
+		const cuuint64_t strides[3] = {(cuuint64_t)9 * ci * 2, (cuuint64_t)ci * 2, 16};
+		const cuuint32_t box[4] = {8, (cuuint32_t)co, 9, (cuuint32_t)(ci / 8)};
+		const cuuint32_t es[4] = {1, 1, 1, 1};
+		if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(w), dims, strides, box, es,
+				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+				CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+			return KEL_OK;
+	}
+	a.bias = b;
+	a.y = y;
+	a.N = n;
+	a.H = H;
+	a.W = W;
+	a.Ci = ci;
+	a.Co = co;
+	a.relu = relu;
+	a.use_bias = bias;
+	a.err = U->d_err;
+	const size_t smem = (size_t)a.mbar_off + (2u * (size_t)a.NR + 5u) * 8u + 16u;
+	static bool attr_set = false;
+	if (!attr_set) {
+		KEL_CUDA(cudaFuncSetAttribute(conv_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
+		attr_set = true;
+	}
+	conv_rows<<<(unsigned)((int64_t)n * (W / 128) * a.runs), 192, smem, U->stream>>>(tx, tw, a);
+	KEL_CUDA(cudaGetLastError());
+	*launched = 1;
+	return KEL_OK;
+}
+
 int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y, int n, int level, int ci, int co,
 			 bool relu, bool bias) {
 	ConvArgs a;
@@ -1793,6 +2073,8 @@ int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
 		if (ci % 16 || co % 16 || co < 16 || co > 256)
 			return fail(KEL_ERR_UNSUPPORTED, "conv: tensor-core path needs c_in, c_out multiples of 16, c_out <= 256");
 		int launched = 0, rc;
+		if ((rc = conv_rows_launch(U, x, w, b, y, n, a.H, a.W, ci, co, relu, bias, &launched))) return rc;
+		if (launched) return KEL_OK;
 		if ((rc = conv_halo_launch(U, x, w, b, y, n, a.H, a.W, ci, co, relu, bias, &launched))) return rc;
 		if (launched) return KEL_OK;
 		TcArgs t;

@@ -19,9 +19,9 @@ def bf16_round(a):
     return t.to(torch.float32).numpy().astype(np.float64)
 
 
-def _net(kind=None):
+def _net(kind=None, h=H, w=W, n=N):
     from lbm_mirror_gb300 import UNet
-    net = UNet(height=H, width=W, widths=WIDTHS, out_channels=3, max_batch=N, seed=7)
+    net = UNet(height=h, width=w, widths=WIDTHS, out_channels=3, max_batch=n, seed=7)
     if kind is not None:
         net.set_conv_kernel(kind)
     return net
@@ -30,26 +30,35 @@ def _net(kind=None):
 KINDS = [pytest.param(0, id="tcgen05"), pytest.param(1, id="mma_sync")]
 
 
-def _inputs(rng):
-    x = np.zeros((N, H, W, 16))
-    x[..., :3] = rng.standard_normal((N, H, W, 3))
+def _inputs(rng, h=H, w=W, n=N):
+    x = np.zeros((n, h, w, 16))
+    x[..., :3] = rng.standard_normal((n, h, w, 3))
     return bf16_round(x)
 
 
+# 16 x 32: every level below 128 pixels wide (per-tile kernels); 8 x 128: the
+# full-resolution level through the row-run convolution and the halo weight
+# gradient, the 64-pixel level through the halo weight gradient with 64-pixel
+# row tiles
+SHAPES = [pytest.param((H, W, N), id="16x32"), pytest.param((8, 128, 1), id="8x128")]
+
+
+@pytest.mark.parametrize("shape", SHAPES)
 @pytest.mark.parametrize("kind", KINDS)
-def test_forward_and_gradients_vs_fp64_oracle(kind):
+def test_forward_and_gradients_vs_fp64_oracle(kind, shape):
+    h, w, n = shape
     rng = np.random.default_rng(1)
-    net = _net(kind)
+    net = _net(kind, h, w, n)
     flat = net.params().astype(np.float64)
     assert flat.size == U.param_count(16, 3, WIDTHS)
-    x = _inputs(rng)
-    tgt = rng.standard_normal((N, H, W, 3)) * 0.1
+    x = _inputs(rng, h, w, n)
+    tgt = rng.standard_normal((n, h, w, 3)) * 0.1
     xin = torch.tensor(x, dtype=torch.bfloat16, device="cuda").contiguous()
     tg = torch.tensor(tgt, dtype=torch.float32, device="cuda").contiguous()
-    out = torch.empty((N, H, W, 3), dtype=torch.float32, device="cuda")
-    net.set_input(xin.data_ptr(), N)
-    net.forward(N, out.data_ptr())
-    loss_gpu = net.backward(tg.data_ptr(), N)
+    out = torch.empty((n, h, w, 3), dtype=torch.float32, device="cuda")
+    net.set_input(xin.data_ptr(), n)
+    net.forward(n, out.data_ptr())
+    loss_gpu = net.backward(tg.data_ptr(), n)
     net.synchronize()
     g_gpu = net.grads().astype(np.float64)
 
