@@ -402,17 +402,18 @@ __global__ void __launch_bounds__(128) conv_tc(TcArgs a) {
 // ---- the convolution from a TMA-loaded halo, for rows of 128 pixels --------------
 //
 // For a layer whose width is a multiple of 128: one CTA computes 128
-// consecutive pixels of one image row (the M = 128 rows of the accumulator)
-// by all Co outputs.  For each chunk of CK input channels the input reaches
-// shared memory as a halo, one TMA tile of 3 rows x 130 pixels x CK channels
-// at (x0 - 1 .. x0 + 128, y - 1 .. y + 1), zero-filled by the copy outside
-// the image, laid out channel-group major: element (row r, pixel p, channel
-// 8 g + e) at ((g * 3 + r) * 130 + p) * 16 + 2 e.  Pixels are 16 bytes apart
+// consecutive pixels of RT consecutive image rows (the M = 128 rows of each
+// of RT accumulators) by all Co outputs.  For each chunk of CK input channels
+// the input reaches shared memory as a halo, one TMA tile of RT + 2 rows x
+// 130 pixels x CK channels at (x0 - 1 .. x0 + 128, y0 - 1 .. y0 + RT),
+// zero-filled by the copy outside the image, laid out channel-group major:
+// element (row r, pixel p, channel 8 g + e) at ((g * (RT + 2) + r) * 130 + p)
+// * 16 + 2 e; the weights of a chunk serve all RT rows.  Pixels are 16 bytes apart
 // within a channel group, so the A operand of tap (dy, dx) -- the 128 pixels
 // shifted by (dy, dx) -- is the same halo read through a descriptor whose
-// start moves by (dy * 130 + dx) * 16 bytes (K-major, no swizzle: core
-// matrices of 8 pixels x 8 channels, 8-pixel stride SBO = 128 B, channel-group
-// stride LBO = 3 * 130 * 16 B).  The nine taps of a chunk read one halo, where
+// start moves by ((r + dy) * 130 + dx) * 16 bytes for output row r (K-major,
+// no swizzle: core matrices of 8 pixels x 8 channels, 8-pixel stride SBO =
+// 128 B, channel-group stride LBO = (RT + 2) * 130 * 16 B).  The nine taps of a chunk read one halo, where
 // an im2col tile holds every input value nine times.  The chunk's weights
 // (Co x 9 x CK) arrive by TMA as [g][tap][co][8 channels]: B of tap t and
 // channel groups 2j, 2j + 1 at ((2 j) * 9 + t) * Co * 16, LBO = 9 * Co * 16,
@@ -428,6 +429,7 @@ struct HaloArgs {
 	const float *bias;
 	bf16 *y; // (N,H,W,Co)
 	int N, H, W, Ci, Co, CK;
+	int RT; // output rows per CTA
 	int relu, use_bias;
 	int stages;
 	uint32_t a_bytes, b_bytes; // bytes of the two TMA boxes of a chunk
@@ -467,8 +469,9 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 
 	const int tpr = a.W / 128; // tiles per row
 	const int x0 = (int)(blockIdx.x % tpr) * 128;
-	const int row = (int)(blockIdx.x / tpr); // n * H + y
+	const int row = (int)(blockIdx.x / tpr) * a.RT; // n * H + y0
 	const int n = row / a.H, yy = row - n * a.H;
+	const int RT = a.RT;
 	const int nch = a.Ci / a.CK;
 	const uint32_t tx_bytes = a.a_bytes + a.b_bytes;
 
@@ -491,7 +494,7 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 
 	// instruction descriptor: D f32, A bf16, B bf16, both K-major, N = Co, M = 128
 	const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-	const uint32_t lbo_a = 3u * HX * 16u, lbo_b = 9u * (uint32_t)a.Co * 16u;
+	const uint32_t lbo_a = (uint32_t)(RT + 2) * HX * 16u, lbo_b = 9u * (uint32_t)a.Co * 16u;
 	int fail = 0, loaded = 0, issued = -1;
 	if (tid == 0) {
 		auto load = [&](int c) {
@@ -515,14 +518,17 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 			for (int j = 0; j < a.CK / 16; ++j)
 				for (int t = 0; t < 9; ++t) {
 					const int dy = t / 3, dx = t % 3;
-					const uint64_t ad = umma_desc(abase + (uint32_t)(2 * j) * lbo_a + (uint32_t)(dy * HX + dx) * 16u,
-												  lbo_a, 128u);
 					const uint64_t bd = umma_desc(bbase + ((uint32_t)(2 * j) * 9u + (uint32_t)t) * (uint32_t)a.Co * 16u,
 												  lbo_b, 128u);
 					const uint32_t acc = (c > 0 || j > 0 || t > 0) ? 1u : 0u;
-					asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-								 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-								 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+					for (int r = 0; r < RT; ++r) {
+						const uint64_t ad = umma_desc(
+							abase + (uint32_t)(2 * j) * lbo_a + (uint32_t)((r + dy) * HX + dx) * 16u, lbo_a, 128u);
+						asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+									 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+										 tmem + (uint32_t)(r * a.Co)),
+									 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+					}
 				}
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
 				smem_u32(done + s)));
@@ -552,34 +558,36 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 	if (!failed) {
 		// epilogue: warp w owns TMEM lanes (= tile pixels) 32 w .. 32 w + 31
 		const int px = warp * 32 + lane;
-		const int64_t m = ((int64_t)row * a.W) + x0 + px;
-		for (int c0 = 0; c0 < a.Co; c0 += 16) {
-			uint32_t r[16];
-			const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-			asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-						 "[%16];\n"
-						 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-						   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-						   "=r"(r[14]), "=r"(r[15])
-						 : "r"(taddr));
-			asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-			__align__(16) __nv_bfloat162 o[8];
+		for (int rr = 0; rr < RT; ++rr) {
+			for (int c0 = 0; c0 < a.Co; c0 += 16) {
+				const int64_t m = ((int64_t)(row + rr) * a.W) + x0 + px;
+				uint32_t r[16];
+				const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(rr * a.Co + c0);
+				asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+							 "[%16];\n"
+							 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+							   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+							   "=r"(r[14]), "=r"(r[15])
+							 : "r"(taddr));
+				asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+				__align__(16) __nv_bfloat162 o[8];
 #pragma unroll
-			for (int q = 0; q < 8; ++q) {
-				float v0 = __uint_as_float(r[2 * q]), v1 = __uint_as_float(r[2 * q + 1]);
-				if (a.use_bias) {
-					v0 += a.bias[c0 + 2 * q];
-					v1 += a.bias[c0 + 2 * q + 1];
+				for (int q = 0; q < 8; ++q) {
+					float v0 = __uint_as_float(r[2 * q]), v1 = __uint_as_float(r[2 * q + 1]);
+					if (a.use_bias) {
+						v0 += a.bias[c0 + 2 * q];
+						v1 += a.bias[c0 + 2 * q + 1];
+					}
+					if (a.relu) {
+						v0 = fmaxf(v0, 0.f);
+						v1 = fmaxf(v1, 0.f);
+					}
+					o[q] = __floats2bfloat162_rn(v0, v1);
 				}
-				if (a.relu) {
-					v0 = fmaxf(v0, 0.f);
-					v1 = fmaxf(v1, 0.f);
-				}
-				o[q] = __floats2bfloat162_rn(v0, v1);
+				uint4 *dst = reinterpret_cast<uint4 *>(a.y + m * a.Co + c0);
+				dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
+				dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
 			}
-			uint4 *dst = reinterpret_cast<uint4 *>(a.y + m * a.Co + c0);
-			dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
-			dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
 		}
 	}
 	asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -1242,27 +1250,29 @@ __global__ void __launch_bounds__(128) conv_wgrad(WgradArgs a) {
 }
 
 // grad[j] += sum over the chunks of partial[c][j], in a fixed order: block
-// (32, 8) takes 32 consecutive j; thread row y sums the chunks of its eighth
-// [c0, c1) in order, then the eight sums are added in order of y.
+// (32, SL) takes 32 consecutive j; thread row y sums the chunks of its slice
+// [c0, c1) in order, then the SL sums are added in order of y.  SL = 8, or 32
+// when there are few j (a long chain of loads per thread otherwise).
 __global__ void reduce_partials(const float *partial, int64_t per, int chunks, float *grad) {
-	__shared__ float sh[8][33];
+	__shared__ float sh[32][33];
 	const int64_t j = (int64_t)blockIdx.x * 32 + threadIdx.x;
-	const int y = threadIdx.y;
-	const int c0 = (int)((int64_t)chunks * y / 8), c1 = (int)((int64_t)chunks * (y + 1) / 8);
+	const int y = threadIdx.y, SL = blockDim.y;
+	const int c0 = (int)((int64_t)chunks * y / SL), c1 = (int)((int64_t)chunks * (y + 1) / SL);
 	float s = 0.f;
 	if (j < per)
+#pragma unroll 8
 		for (int c = c0; c < c1; ++c) s += partial[(int64_t)c * per + j];
 	sh[y][threadIdx.x] = s;
 	__syncthreads();
 	if (y == 0 && j < per) {
 		float t = 0.f;
-		for (int k = 0; k < 8; ++k) t += sh[k][threadIdx.x];
+		for (int k = 0; k < SL; ++k) t += sh[k][threadIdx.x];
 		grad[j] += t;
 	}
 }
 
 void launch_reduce_partials(const float *partial, int64_t per, int chunks, float *grad, cudaStream_t st) {
-	reduce_partials<<<(unsigned)((per + 31) / 32), dim3(32, 8), 0, st>>>(partial, per, chunks, grad);
+	reduce_partials<<<(unsigned)((per + 31) / 32), dim3(32, per < 4096 ? 32 : 8), 0, st>>>(partial, per, chunks, grad);
 }
 
 // db[co] += sum over pixels of dY[m][co] (one block per channel, fixed order)
@@ -1662,13 +1672,40 @@ __global__ void adam_consts(float *c, float lr, float c1, float c2) {
 }
 
 // the mean loss from the blocks' partial sums, in block order (as the host adds them)
+// loss = (sum of the nb block partials) / n in a fixed order that the host
+// path repeats: thread t of 64 sums partials t, t + 64, ... in order, then a
+// pairwise tree over the 64 sums (a single thread's chain of nb dependent
+// FP64 additions is slow on this GPU's FP64 pipe)
 __global__ void loss_finish(const double *partial, int nb, int64_t n, double *loss) {
+	__shared__ double sh[64];
+	const int t = threadIdx.x;
 	double s = 0.0;
-	for (int k = 0; k < nb; ++k) s += partial[k];
-	*loss = s / (double)n;
+	for (int k = t; k < nb; k += 64) s += partial[k];
+	sh[t] = s;
+	__syncthreads();
+	for (int o = 32; o > 0; o >>= 1) {
+		if (t < o) sh[t] += sh[t + o];
+		__syncthreads();
+	}
+	if (t == 0) *loss = sh[0] / (double)n;
 }
 
-__global__ void refresh_conv_weights(const float *w32, bf16 *w, bf16 *wf, int Co, int Ci, int k) {
+// bf16 copies of the 3x3 conv weights: w = [co][ky][kx][ci] and the flipped,
+// transposed wf = [ci][2-ky][2-kx][co] of the data gradient.  One launch for
+// every layer: blockIdx.y picks the layer from the table.
+constexpr int MAX_CONV = 16;
+struct ConvTable {
+	int nl;
+	int64_t off[MAX_CONV]; // FP32 weights in the parameter vector
+	int co[MAX_CONV], ci[MAX_CONV];
+	bf16 *w[MAX_CONV], *wf[MAX_CONV];
+};
+
+__global__ void refresh_conv_weights(const float *p, const __grid_constant__ ConvTable t) {
+	const int l = blockIdx.y;
+	const int Co = t.co[l], Ci = t.ci[l], k = 3;
+	const float *w32 = p + t.off[l];
+	bf16 *w = t.w[l], *wf = t.wf[l];
 	const int64_t n = (int64_t)Co * k * k * Ci;
 	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
 		const int ci = (int)(i % Ci);
@@ -1756,30 +1793,44 @@ __global__ void column_resistance(const float *open, const float *h3, int N, int
 	}
 }
 
+// One block per (sample, 32 columns): the block's mask columns are staged in
+// shared memory (H x 32 bytes), then thread (column c, row r) finds its
+// vertical gap's ends there and writes the pixel's 16 channels as two
+// 16-byte stores (a warp's stores cover 32 consecutive pixels of a row).
+// Dynamic shared memory: 32 H bytes.
 __global__ void make_input(const uint8_t *mask, const float *umax, const float *tau, const float *open,
-						   const float *h3, const float *R, const float *PL, bf16 *x, int N, int H, int W, int C) {
-	const int64_t n = (int64_t)N * H * W;
-	for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-		const int b = (int)(p / ((int64_t)H * W));
-		const int r = (int)(p - (int64_t)b * H * W);
-		const int yy = r / W, xx = r - yy * W;
-		const uint8_t *m = mask + (int64_t)b * H * W;
+						   const float *h3, const float *R, const float *PL, bf16 *x, int N, int H, int W) {
+	extern __shared__ uint8_t mt[]; // [H][32]
+	const int tpb = (W + 31) / 32;
+	const int b = blockIdx.x / tpb, x0 = (blockIdx.x % tpb) * 32;
+	const uint8_t *m = mask + (int64_t)b * H * W;
+	for (int i = threadIdx.x; i < H * 32; i += blockDim.x) {
+		const int yy = i >> 5, c = i & 31;
+		mt[i] = x0 + c < W ? m[(int64_t)yy * W + x0 + c] : (uint8_t)1;
+	}
+	__syncthreads();
+	const int c = threadIdx.x & 31, xx = x0 + c;
+	if (xx >= W) return;
+	const int64_t col = (int64_t)b * W + xx;
+	const float c1 = umax[b] / 0.08f, c2 = (tau[b] - 0.55f) / 0.45f, c4 = (float)xx / (float)(W - 1);
+	const float hin = (float)(H > 2 ? H - 2 : H);
+	for (int yy = threadIdx.x >> 5; yy < H; yy += blockDim.x >> 5) {
+		const uint8_t mv = mt[yy * 32 + c];
 		float v[16];
-		for (int c = 0; c < 16; ++c) v[c] = 0.f;
-		v[0] = (float)m[r];
-		v[1] = umax[b] / 0.08f;
-		v[2] = (tau[b] - 0.55f) / 0.45f;
+#pragma unroll
+		for (int k = 0; k < 16; ++k) v[k] = 0.f;
+		v[0] = (float)mv;
+		v[1] = c1;
+		v[2] = c2;
 		v[3] = (float)yy / (float)(H - 1);
-		v[4] = (float)xx / (float)(W - 1);
-		if (!m[r]) {
-			const int64_t col = (int64_t)b * W + xx;
+		v[4] = c4;
+		if (!mv) {
 			int lo = yy, hi = yy;
-			while (lo > 0 && !m[(int64_t)(lo - 1) * W + xx]) --lo;
-			while (hi + 1 < H && !m[(int64_t)(hi + 1) * W + xx]) ++hi;
+			while (lo > 0 && !mt[(lo - 1) * 32 + c]) --lo;
+			while (hi + 1 < H && !mt[(hi + 1) * 32 + c]) ++hi;
 			const float h = (float)(hi - lo + 1);
 			const float sp = ((float)(yy - lo) + 0.5f) / h;
 			const float shape = 4.f * sp * (1.f - sp);
-			const float hin = (float)(H > 2 ? H - 2 : H);
 			v[5] = open[col];
 			v[6] = R[col];
 			v[7] = h / hin;
@@ -1787,8 +1838,12 @@ __global__ void make_input(const uint8_t *mask, const float *umax, const float *
 			v[9] = 0.5f * fminf(hin * h * h / fmaxf(h3[col], 1.f) * shape, 8.f);
 			v[10] = PL[col];
 		}
-		bf16 *o = x + p * C;
-		for (int c = 0; c < C; ++c) o[c] = __float2bfloat16(c < 16 ? v[c] : 0.f);
+		__align__(16) __nv_bfloat162 q[8];
+#pragma unroll
+		for (int k = 0; k < 8; ++k) q[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+		uint4 *d = reinterpret_cast<uint4 *>(x + (((int64_t)b * H + yy) * W + xx) * 16);
+		d[0] = *reinterpret_cast<const uint4 *>(&q[0]);
+		d[1] = *reinterpret_cast<const uint4 *>(&q[4]);
 	}
 }
 
@@ -1894,12 +1949,12 @@ uint32_t align1k(uint64_t v) { return (uint32_t)((v + 1023) / 1024 * 1024); }
 // Channel chunk and stage count of conv_halo: the largest chunk (64, 48, 32 or
 // 16 channels dividing Ci) whose stages (up to three, at least two when there
 // are two chunks or more) fit 110 KB (two CTAs per SM), else 200 KB; 0: none.
-int halo_plan(int Ci, int Co, HaloArgs &a) {
+int halo_plan(int Ci, int Co, int RT, HaloArgs &a) {
 	for (const uint32_t cap : {110u * 1024u, 200u * 1024u})
 		for (const int ck : {64, 48, 32, 16}) {
 			if (Ci % ck) continue;
 			const int nch = Ci / ck;
-			const uint32_t ab = 3u * HX * (uint32_t)ck * 2u, bb = 18u * (uint32_t)Co * (uint32_t)ck;
+			const uint32_t ab = (uint32_t)(RT + 2) * HX * (uint32_t)ck * 2u, bb = 18u * (uint32_t)Co * (uint32_t)ck;
 			const uint32_t stage = align1k(ab) + align1k(bb);
 			int S = nch < 3 ? nch : 3;
 			while (S > 1 && (uint64_t)S * stage + 1024 > cap) --S;
@@ -1923,12 +1978,21 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	const EncodeTiledFn enc = encode_tiled();
 	HaloArgs a;
 	memset(&a, 0, sizeof(a));
-	if (!enc || W % 128 || ci % 16 || co % 16 || co < 16 || co > 256 || !halo_plan(ci, co, a)) return KEL_OK;
+	if (!enc || W % 128 || ci % 16 || co % 16 || co < 16 || co > 256) return KEL_OK;
+	// output rows per CTA: the most (4, 2, 1) whose accumulators fit TMEM and
+	// that still leave a CTA per SM
+	a.RT = 0;
+	for (const int rt : {4, 2, 1})
+		if (!a.RT && rt * co <= 512 && H % rt == 0 && (int64_t)n * (H / rt) * (W / 128) >= (U->sms > 0 ? U->sms : 148) &&
+			halo_plan(ci, co, rt, a))
+			a.RT = rt;
+	if (!a.RT && halo_plan(ci, co, 1, a)) a.RT = 1;
+	if (!a.RT) return KEL_OK;
 	CUtensorMap tx, tw;
 	{ // x (N,H,W,Ci) as (8 channels, x, y, channel group, n)
 		const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)(ci / 8), (cuuint64_t)n};
 		const cuuint64_t strides[4] = {(cuuint64_t)ci * 2, (cuuint64_t)W * ci * 2, 16, (cuuint64_t)H * W * ci * 2};
-		const cuuint32_t box[5] = {8, HX, 3, (cuuint32_t)(a.CK / 8), 1};
+		const cuuint32_t box[5] = {8, HX, (cuuint32_t)(a.RT + 2), (cuuint32_t)(a.CK / 8), 1};
 		const cuuint32_t es[5] = {1, 1, 1, 1, 1};
 		if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(x), dims, strides, box, es,
 				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -1955,7 +2019,7 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	a.relu = relu;
 	a.use_bias = bias;
 	a.tmem_cols = 32;
-	while (a.tmem_cols < (uint32_t)co) a.tmem_cols <<= 1;
+	while (a.tmem_cols < (uint32_t)(a.RT * co)) a.tmem_cols <<= 1;
 	a.err = U->d_err;
 	const size_t smem = (size_t)a.stages * a.stage_bytes + (size_t)a.stages * 16 + 16;
 	static bool attr_set = false;
@@ -1963,7 +2027,7 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 		KEL_CUDA(cudaFuncSetAttribute(conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
 		attr_set = true;
 	}
-	conv_halo<<<(unsigned)((int64_t)n * H * (W / 128)), 128, smem, U->stream>>>(tx, tw, a);
+	conv_halo<<<(unsigned)((int64_t)n * (H / a.RT) * (W / 128)), 128, smem, U->stream>>>(tx, tw, a);
 	KEL_CUDA(cudaGetLastError());
 	*launched = 1;
 	return KEL_OK;
@@ -2318,10 +2382,23 @@ void init_params(kel_unet *U, uint64_t seed, std::vector<float> &h) {
 }
 
 int refresh(kel_unet *U) {
+	ConvTable t;
+	memset(&t, 0, sizeof(t));
+	int64_t most = 0;
 	for (auto &l : U->L) {
 		if (l.k != 3) continue;
-		refresh_conv_weights<<<grid_of((int64_t)l.co * 9 * l.ci), 256, 0, U->stream>>>(U->p + l.woff, l.w, l.wf, l.co,
-																						   l.ci, 3);
+		if (t.nl == MAX_CONV) return fail(KEL_ERR_INVALID_ARGUMENT, "refresh: more than %d conv layers", MAX_CONV);
+		t.off[t.nl] = l.woff;
+		t.co[t.nl] = l.co;
+		t.ci[t.nl] = l.ci;
+		t.w[t.nl] = l.w;
+		t.wf[t.nl] = l.wf;
+		++t.nl;
+		if ((int64_t)l.co * 9 * l.ci > most) most = (int64_t)l.co * 9 * l.ci;
+	}
+	if (t.nl) {
+		const unsigned bx = (unsigned)((most + 255) / 256 < 296 ? (most + 255) / 256 : 296);
+		refresh_conv_weights<<<dim3(bx, (unsigned)t.nl), 256, 0, U->stream>>>(U->p, t);
 	}
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
@@ -2515,13 +2592,13 @@ extern "C" int kel_unet_make_input(kel_unet *U, const uint8_t *d_mask, const flo
 								   int32_t n) {
 	int rc = check_batch(U, n, "kel_unet_make_input");
 	if (rc) return rc;
-	const int64_t pix = (int64_t)n * U->d.height * U->d.width;
 	const int H = U->d.height, W = U->d.width;
 	column_features<<<(n * W + 127) / 128, 128, 0, U->stream>>>(d_mask, n, H, W, U->col_open, U->col_h3);
 	column_resistance<<<n, 256, sizeof(float) * 4 * W, U->stream>>>(U->col_open, U->col_h3, n, W, U->col_res,
 																	 U->col_pl);
-	make_input<<<grid_of(pix), 256, 0, U->stream>>>(d_mask, d_umax, d_tau, U->col_open, U->col_h3, U->col_res,
-													 U->col_pl, U->input, n, H, W, 16);
+	if ((size_t)H * 32 > 48 * 1024) return fail(KEL_ERR_UNSUPPORTED, "kel_unet_make_input: height above 1536");
+	make_input<<<n * ((W + 31) / 32), 256, (size_t)H * 32, U->stream>>>(d_mask, d_umax, d_tau, U->col_open, U->col_h3,
+																		  U->col_res, U->col_pl, U->input, n, H, W);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }
@@ -2634,7 +2711,7 @@ static int unet_backward(kel_unet *U, const float *d_target, int32_t n, double *
 	if ((rc = back(1, T_E0A, A[T_E0A], T_E0B, G[T_E0A])) || (rc = back(0, -1, U->input, T_E0A, nullptr))) return rc;
 	KEL_CUDA(cudaGetLastError());
 	if (dev_loss) {
-		loss_finish<<<1, 1, 0, U->stream>>>(U->loss_partial, lb, nout, dev_loss);
+		loss_finish<<<1, 64, 0, U->stream>>>(U->loss_partial, lb, nout, dev_loss);
 		KEL_CUDA(cudaGetLastError());
 	}
 	if (loss) {
@@ -2642,9 +2719,16 @@ static int unet_backward(kel_unet *U, const float *d_target, int32_t n, double *
 		KEL_CUDA(cudaMemcpyAsync(part.data(), U->loss_partial, sizeof(double) * lb, cudaMemcpyDeviceToHost, U->stream));
 		KEL_CUDA(cudaStreamSynchronize(U->stream));
 		if ((rc = check_device_error(U, "kel_unet_backward"))) return rc;
-		double s = 0.0;
-		for (double p : part) s += p;
-		*loss = s / (double)nout;
+		// loss_finish's order: 64 strided sums, then a pairwise tree
+		double s64[64];
+		for (int t = 0; t < 64; ++t) {
+			double s = 0.0;
+			for (int k = t; k < lb; k += 64) s += part[k];
+			s64[t] = s;
+		}
+		for (int o = 32; o > 0; o >>= 1)
+			for (int t = 0; t < o; ++t) s64[t] += s64[t + o];
+		*loss = s64[0] / (double)nout;
 	}
 	return KEL_OK;
 }
