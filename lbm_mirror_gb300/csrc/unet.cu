@@ -203,6 +203,15 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo = 128
 	return d;
 }
 
+// Descriptor of a shared-memory operand at 16-byte unit addr16 = address >> 4:
+// the address field is the low 14 bits, so adding n to the descriptor moves
+// the operand by 16 n bytes (shared addresses stay below 2^18).
+__device__ __forceinline__ void umma_f16(uint32_t d_tmem, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc) {
+	asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+				 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+				 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+
 __device__ __forceinline__ void cp_async16(uint32_t saddr, const void *g, bool valid) {
 	asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(saddr), "l"(g), "r"(valid ? 16 : 0));
 }
@@ -515,19 +524,17 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 			asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
 			const uint32_t abase = smem_u32(sm + (size_t)s * a.stage_bytes);
 			const uint32_t bbase = abase + a.a_span;
+			// descriptors stepped by constant adds (16-byte units)
+			const uint64_t ad0 = umma_desc(abase, lbo_a, 128u), bd0 = umma_desc(bbase, lbo_b, 128u);
 			for (int j = 0; j < a.CK / 16; ++j)
 				for (int t = 0; t < 9; ++t) {
 					const int dy = t / 3, dx = t % 3;
-					const uint64_t bd = umma_desc(bbase + ((uint32_t)(2 * j) * 9u + (uint32_t)t) * (uint32_t)a.Co * 16u,
-												  lbo_b, 128u);
+					const uint64_t bd = bd0 + (uint64_t)((2 * j * 9 + t) * a.Co);
 					const uint32_t acc = (c > 0 || j > 0 || t > 0) ? 1u : 0u;
+					uint64_t ad = ad0 + (uint64_t)(2 * j) * (lbo_a >> 4) + (uint64_t)(dy * HX + dx);
 					for (int r = 0; r < RT; ++r) {
-						const uint64_t ad = umma_desc(
-							abase + (uint32_t)(2 * j) * lbo_a + (uint32_t)((r + dy) * HX + dx) * 16u, lbo_a, 128u);
-						asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-									 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-										 tmem + (uint32_t)(r * a.Co)),
-									 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+						umma_f16(tmem + (uint32_t)(r * a.Co), ad, bd, idesc, acc);
+						ad += HX;
 					}
 				}
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
@@ -702,7 +709,8 @@ __global__ void __launch_bounds__(192) conv_rows(const __grid_constant__ CUtenso
 			const uint32_t idesc =
 				(1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
 			const uint32_t lbo_b = 9u * (uint32_t)a.Co * 16u;
-			const uint32_t wbase = smem_u32(sm + a.w_off);
+			const uint64_t bd0 = umma_desc(smem_u32(sm + a.w_off), lbo_b, 128u);
+			const uint64_t a_k = (2u * R) >> 4, b_k = 18u * (uint64_t)a.Co;
 			const int nk = a.Ci / 16;
 			int fail = !mbar_wait(smem_u32(w_full), 0u), done = 0;
 			for (int i = 0; i < rows && !fail; ++i) {
@@ -712,18 +720,21 @@ __global__ void __launch_bounds__(192) conv_rows(const __grid_constant__ CUtenso
 				if (!fail && i >= 2 && !mbar_wait(smem_u32(acc_empty + b), (uint32_t)(((i >> 1) - 1) & 1))) fail = 1;
 				if (fail) break;
 				asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+				// descriptors stepped by constant adds: a k-step moves A by two
+				// channel groups (2 R bytes) and B by 18 Co 16-byte units
+				const uint32_t d_tmem = tmem + (uint32_t)(b * a.Co);
+				uint64_t ad_row[3];
+				for (int dy = 0; dy < 3; ++dy) ad_row[dy] = umma_desc(smem_u32(sm + (size_t)((i + dy) % NR) * a.row_span), R, 128u);
+				uint32_t acc = 0u;
 				for (int t = 0; t < 9; ++t) {
-					const int dy = t / 3, dx = t % 3;
-					const uint32_t xbase = smem_u32(sm + (size_t)((i + dy) % NR) * a.row_span) + (uint32_t)dx * 16u;
+					uint64_t ad = ad_row[t / 3] + (uint64_t)(t % 3);
+					uint64_t bd = bd0 + (uint64_t)t * (uint64_t)a.Co;
+#pragma unroll 2
 					for (int k = 0; k < nk; ++k) {
-						const uint64_t ad = umma_desc(xbase + (uint32_t)(2 * k) * R, R, 128u);
-						const uint64_t bd = umma_desc(wbase + ((uint32_t)(2 * k) * 9u + (uint32_t)t) * (uint32_t)a.Co * 16u,
-													  lbo_b, 128u);
-						const uint32_t acc = (t > 0 || k > 0) ? 1u : 0u;
-						asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-									 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-										 tmem + (uint32_t)(b * a.Co)),
-									 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+						umma_f16(d_tmem, ad, bd, idesc, acc);
+						acc = 1u;
+						ad += a_k;
+						bd += b_k;
 					}
 				}
 				// input row i is read by no later output row
@@ -1075,18 +1086,17 @@ __global__ void __launch_bounds__(128) conv_wgrad_halo(const __grid_constant__ C
 			asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
 			const uint32_t xb = smem_u32(sm + (size_t)s * a.x_span);
 			const uint32_t db = smem_u32(sm + a.dy_off + (size_t)s * a.dy_span);
+			// descriptors stepped by constant adds (16-byte units): a k-step
+			// moves both operands by 16 pixels
+			const uint64_t ad0 = umma_desc(xb, 128u, R), bd0 = umma_desc(db, 128u, (uint32_t)a.WT * 16u);
 			for (int k = 0; k < nk; ++k) {
-				const uint64_t bd = umma_desc(db + (uint32_t)k * 256u, 128u, (uint32_t)a.WT * 16u);
-				for (int g = 0; g < a.rg_cta; ++g)
-					for (int dx = 0; dx < 3; ++dx) {
-						const uint64_t ad =
-							umma_desc(xb + (uint32_t)g * grp_bytes + (uint32_t)(16 * k + dx) * 16u, 128u, R);
-						const uint32_t acc = (i > 0 || k > 0) ? 1u : 0u;
-						asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-									 " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
-										 tmem + (uint32_t)((g * 3 + dx) * a.Co)),
-									 "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
-					}
+				const uint64_t bd = bd0 + (uint64_t)(16 * k);
+				const uint32_t acc = (i > 0 || k > 0) ? 1u : 0u;
+				for (int g = 0; g < a.rg_cta; ++g) {
+					const uint64_t ad = ad0 + (uint64_t)g * (grp_bytes >> 4) + (uint64_t)(16 * k);
+					for (int dx = 0; dx < 3; ++dx)
+						umma_f16(tmem + (uint32_t)((g * 3 + dx) * a.Co), ad + (uint64_t)dx, bd, idesc, acc);
+				}
 			}
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
 				smem_u32(done + s)));
