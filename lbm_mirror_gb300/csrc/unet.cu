@@ -408,25 +408,31 @@ __global__ void __launch_bounds__(128) conv_tc(TcArgs a) {
 	}
 }
 
-// ---- the convolution from a TMA-loaded halo, for rows of 128 pixels --------------
+// ---- the convolution from a TMA-loaded halo ----------------------------------------
 //
-// For a layer whose width is a multiple of 128: one CTA computes 128
-// consecutive pixels of RT consecutive image rows (the M = 128 rows of each
-// of RT accumulators) by all Co outputs.  For each chunk of CK input channels
-// the input reaches shared memory as a halo, one TMA tile of RT + 2 rows x
-// 130 pixels x CK channels at (x0 - 1 .. x0 + 128, y0 - 1 .. y0 + RT),
-// zero-filled by the copy outside the image, laid out channel-group major:
-// element (row r, pixel p, channel 8 g + e) at ((g * (RT + 2) + r) * 130 + p)
-// * 16 + 2 e; the weights of a chunk serve all RT rows.  Pixels are 16 bytes apart
-// within a channel group, so the A operand of tap (dy, dx) -- the 128 pixels
-// shifted by (dy, dx) -- is the same halo read through a descriptor whose
-// start moves by ((r + dy) * 130 + dx) * 16 bytes for output row r (K-major,
-// no swizzle: core matrices of 8 pixels x 8 channels, 8-pixel stride SBO =
-// 128 B, channel-group stride LBO = (RT + 2) * 130 * 16 B).  The nine taps of a chunk read one halo, where
-// an im2col tile holds every input value nine times.  The chunk's weights
-// (Co x 9 x CK) arrive by TMA as [g][tap][co][8 channels]: B of tap t and
-// channel groups 2j, 2j + 1 at ((2 j) * 9 + t) * Co * 16, LBO = 9 * Co * 16,
-// SBO = 128.  One thread issues the copies (one mbarrier per stage counts
+// One CTA computes RT M tiles of 128 pixels by all Co outputs, each tile in
+// its own TMEM accumulator; the weights of a chunk of CK input channels serve
+// all RT tiles.  For a layer whose width is a multiple of 128 a tile is 128
+// consecutive pixels of one image row (MR = 1) and the CTA takes RT
+// consecutive rows; the chunk's input reaches shared memory as one halo, a
+// TMA tile of RT + 2 rows x 130 pixels x CK channels at (x0 - 1 .. x0 + 128,
+// y0 - 1 .. y0 + RT), zero-filled by the copy outside the image, laid out
+// channel-group major: element (row r, pixel p, channel 8 g + e) at
+// ((g * rows + r) * P + p) * 16 + 2 e with P = 130.  Pixels are 16 bytes
+// apart within a channel group, so the A operand of tap (dy, dx) -- the 128
+// pixels shifted by (dy, dx) -- is the same halo read through a descriptor
+// whose start moves by ((r + dy) * P + dx) * 16 bytes for tile r (K-major, no
+// swizzle: core matrices of 8 pixels x 8 channels, 8-pixel stride SBO = 128
+// B, channel-group stride LBO = rows * P * 16 B).  For a narrower layer (W
+// dividing 128) a tile is MR = 128 / W whole image rows, which a single
+// descriptor covers only if consecutive rows are W pixels apart; so the halo
+// comes as NC = 3 copies of RT * MR + 2 rows x W pixels (P = W), taken at x =
+// -1, 0, +1 (zero-filled at the image edge), and the shift dx selects the
+// copy instead of moving by a pixel.  The nine taps of a chunk read one
+// halo, where an im2col tile holds every input value nine times.  The chunk's
+// weights (Co x 9 x CK) arrive by TMA as [g][tap][co][8 channels]: B of tap t
+// and channel groups 2j, 2j + 1 at ((2 j) * 9 + t) * Co * 16, LBO = 9 * Co *
+// 16, SBO = 128.  One thread issues the copies (one mbarrier per stage counts
 // their bytes) and the MMAs (committed to the stage's second mbarrier, which
 // frees the stage for the chunk S later).  Every wait is bounded; on timeout
 // the CTA records the failure in *err, waits (bounded) for the copies it
@@ -438,10 +444,12 @@ struct HaloArgs {
 	const float *bias;
 	bf16 *y; // (N,H,W,Co)
 	int N, H, W, Ci, Co, CK;
-	int RT; // output rows per CTA
+	int RT;        // accumulators (M tiles of 128 pixels) per CTA
+	int NC, P, MR; // halo copies (1, or 3 shifted by dx), pixels per copy row, image rows per M tile
 	int relu, use_bias;
 	int stages;
-	uint32_t a_bytes, b_bytes; // bytes of the two TMA boxes of a chunk
+	uint32_t copy_bytes;       // one halo copy of a chunk
+	uint32_t a_bytes, b_bytes; // bytes of the TMA boxes of a chunk (NC copies; the weights)
 	uint32_t a_span, stage_bytes; // B's offset in a stage and the stage size (1024-byte multiples)
 	uint32_t tmem_cols;
 	int *err;
@@ -476,9 +484,9 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 	uint64_t *done = full + S;
 	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + S);
 
-	const int tpr = a.W / 128; // tiles per row
+	const int tpr = a.W >= 128 ? a.W / 128 : 1; // tiles per row
 	const int x0 = (int)(blockIdx.x % tpr) * 128;
-	const int row = (int)(blockIdx.x / tpr) * a.RT; // n * H + y0
+	const int row = (int)(blockIdx.x / tpr) * a.RT * a.MR; // n * H + y0
 	const int n = row / a.H, yy = row - n * a.H;
 	const int RT = a.RT;
 	const int nch = a.Ci / a.CK;
@@ -503,14 +511,18 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 
 	// instruction descriptor: D f32, A bf16, B bf16, both K-major, N = Co, M = 128
 	const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-	const uint32_t lbo_a = (uint32_t)(RT + 2) * HX * 16u, lbo_b = 9u * (uint32_t)a.Co * 16u;
+	const uint32_t lbo_a = (uint32_t)(RT * a.MR + 2) * (uint32_t)a.P * 16u, lbo_b = 9u * (uint32_t)a.Co * 16u;
+	// the shift dx: a pixel (one copy) or a copy (three)
+	const uint64_t dx_step = a.NC == 3 ? (uint64_t)(a.copy_bytes >> 4) : 1u;
 	int fail = 0, loaded = 0, issued = -1;
 	if (tid == 0) {
 		auto load = [&](int c) {
 			const int s = c % S;
 			const uint32_t base = smem_u32(sm + (size_t)s * a.stage_bytes);
 			mbar_expect_tx(smem_u32(full + s), tx_bytes);
-			tma_load_5d(base, &tx, smem_u32(full + s), 0, x0 - 1, yy - 1, c * (a.CK / 8), n);
+			for (int cp = 0; cp < a.NC; ++cp)
+				tma_load_5d(base + (uint32_t)cp * a.copy_bytes, &tx, smem_u32(full + s), 0, x0 - 1 + (a.NC == 3 ? cp : 0),
+							yy - 1, c * (a.CK / 8), n);
 			tma_load_4d(base + a.a_span, &tw, smem_u32(full + s), 0, 0, 0, c * (a.CK / 8));
 		};
 		for (int c = 0; c < S && c < nch; ++c) load(c);
@@ -531,10 +543,10 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 					const int dy = t / 3, dx = t % 3;
 					const uint64_t bd = bd0 + (uint64_t)((2 * j * 9 + t) * a.Co);
 					const uint32_t acc = (c > 0 || j > 0 || t > 0) ? 1u : 0u;
-					uint64_t ad = ad0 + (uint64_t)(2 * j) * (lbo_a >> 4) + (uint64_t)(dy * HX + dx);
+					uint64_t ad = ad0 + (uint64_t)(2 * j) * (lbo_a >> 4) + (uint64_t)(dy * a.P) + (uint64_t)dx * dx_step;
 					for (int r = 0; r < RT; ++r) {
 						umma_f16(tmem + (uint32_t)(r * a.Co), ad, bd, idesc, acc);
-						ad += HX;
+						ad += (uint64_t)(a.MR * a.P);
 					}
 				}
 			asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
@@ -567,7 +579,7 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 		const int px = warp * 32 + lane;
 		for (int rr = 0; rr < RT; ++rr) {
 			for (int c0 = 0; c0 < a.Co; c0 += 16) {
-				const int64_t m = ((int64_t)(row + rr) * a.W) + x0 + px;
+				const int64_t m = ((int64_t)(row + rr * a.MR) * a.W) + x0 + px;
 				uint32_t r[16];
 				const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(rr * a.Co + c0);
 				asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
@@ -1964,13 +1976,15 @@ int halo_plan(int Ci, int Co, int RT, HaloArgs &a) {
 		for (const int ck : {64, 48, 32, 16}) {
 			if (Ci % ck) continue;
 			const int nch = Ci / ck;
-			const uint32_t ab = (uint32_t)(RT + 2) * HX * (uint32_t)ck * 2u, bb = 18u * (uint32_t)Co * (uint32_t)ck;
+			const uint32_t cb = (uint32_t)(RT * a.MR + 2) * (uint32_t)a.P * (uint32_t)ck * 2u;
+			const uint32_t ab = (uint32_t)a.NC * cb, bb = 18u * (uint32_t)Co * (uint32_t)ck;
 			const uint32_t stage = align1k(ab) + align1k(bb);
 			int S = nch < 3 ? nch : 3;
 			while (S > 1 && (uint64_t)S * stage + 1024 > cap) --S;
 			if ((nch > 1 && S < 2) || (uint64_t)S * stage + 1024 > cap) continue;
 			a.CK = ck;
 			a.stages = S;
+			a.copy_bytes = cb;
 			a.a_bytes = ab;
 			a.b_bytes = bb;
 			a.a_span = align1k(ab);
@@ -1980,7 +1994,7 @@ int halo_plan(int Ci, int Co, int RT, HaloArgs &a) {
 	return 0;
 }
 
-// The halo convolution (conv_halo) for 128-pixel rows; returns 0 without
+// The halo convolution (conv_halo); returns 0 without
 // launching when the layer does not fit it.
 int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y, int n, int H, int W, int ci,
 					 int co, bool relu, bool bias, int *launched) {
@@ -1988,13 +2002,25 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	const EncodeTiledFn enc = encode_tiled();
 	HaloArgs a;
 	memset(&a, 0, sizeof(a));
-	if (!enc || W % 128 || ci % 16 || co % 16 || co < 16 || co > 256) return KEL_OK;
-	// output rows per CTA: the most (4, 2, 1) whose accumulators fit TMEM and
+	if (!enc || ci % 16 || co % 16 || co < 16 || co > 256) return KEL_OK;
+	if (W % 128 == 0) {
+		a.NC = 1;
+		a.P = HX;
+		a.MR = 1;
+	} else if (W >= 8 && W % 8 == 0 && 128 % W == 0 && H % (128 / W) == 0) {
+		a.NC = 3;
+		a.P = W;
+		a.MR = 128 / W;
+	} else {
+		return KEL_OK;
+	}
+	const int tpr = W >= 128 ? W / 128 : 1;
+	// M tiles per CTA: the most (4, 2, 1) whose accumulators fit TMEM and
 	// that still leave a CTA per SM
 	a.RT = 0;
 	for (const int rt : {4, 2, 1})
-		if (!a.RT && rt * co <= 512 && H % rt == 0 && (int64_t)n * (H / rt) * (W / 128) >= (U->sms > 0 ? U->sms : 148) &&
-			halo_plan(ci, co, rt, a))
+		if (!a.RT && rt * co <= 512 && H % (rt * a.MR) == 0 &&
+			(int64_t)n * (H / (rt * a.MR)) * tpr >= (U->sms > 0 ? U->sms : 148) && halo_plan(ci, co, rt, a))
 			a.RT = rt;
 	if (!a.RT && halo_plan(ci, co, 1, a)) a.RT = 1;
 	if (!a.RT) return KEL_OK;
@@ -2002,7 +2028,7 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	{ // x (N,H,W,Ci) as (8 channels, x, y, channel group, n)
 		const cuuint64_t dims[5] = {8, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)(ci / 8), (cuuint64_t)n};
 		const cuuint64_t strides[4] = {(cuuint64_t)ci * 2, (cuuint64_t)W * ci * 2, 16, (cuuint64_t)H * W * ci * 2};
-		const cuuint32_t box[5] = {8, HX, (cuuint32_t)(a.RT + 2), (cuuint32_t)(a.CK / 8), 1};
+		const cuuint32_t box[5] = {8, (cuuint32_t)a.P, (cuuint32_t)(a.RT * a.MR + 2), (cuuint32_t)(a.CK / 8), 1};
 		const cuuint32_t es[5] = {1, 1, 1, 1, 1};
 		if (enc(&tx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(x), dims, strides, box, es,
 				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -2037,7 +2063,7 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 		KEL_CUDA(cudaFuncSetAttribute(conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
 		attr_set = true;
 	}
-	conv_halo<<<(unsigned)((int64_t)n * (H / a.RT) * (W / 128)), 128, smem, U->stream>>>(tx, tw, a);
+	conv_halo<<<(unsigned)((int64_t)n * (H / (a.RT * a.MR)) * tpr), 128, smem, U->stream>>>(tx, tw, a);
 	KEL_CUDA(cudaGetLastError());
 	*launched = 1;
 	return KEL_OK;
