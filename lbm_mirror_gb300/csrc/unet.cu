@@ -446,6 +446,7 @@ struct HaloArgs {
 	int N, H, W, Ci, Co, CK;
 	int RT;        // accumulators (M tiles of 128 pixels) per CTA
 	int NC, P, MR; // halo copies (1, or 3 shifted by dx), pixels per copy row, image rows per M tile
+	int CoT;       // output channels per CTA (Co / CoT CTAs share a pixel tile)
 	int relu, use_bias;
 	int stages;
 	uint32_t copy_bytes;       // one halo copy of a chunk
@@ -485,8 +486,11 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(done + S);
 
 	const int tpr = a.W >= 128 ? a.W / 128 : 1; // tiles per row
-	const int x0 = (int)(blockIdx.x % tpr) * 128;
-	const int row = (int)(blockIdx.x / tpr) * a.RT * a.MR; // n * H + y0
+	const int cot = a.Co / a.CoT;
+	const int co0 = (int)(blockIdx.x % cot) * a.CoT;
+	const int tile = (int)(blockIdx.x / cot);
+	const int x0 = (tile % tpr) * 128;
+	const int row = (tile / tpr) * a.RT * a.MR; // n * H + y0
 	const int n = row / a.H, yy = row - n * a.H;
 	const int RT = a.RT;
 	const int nch = a.Ci / a.CK;
@@ -510,8 +514,8 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 	const uint32_t tmem = *tmem_slot;
 
 	// instruction descriptor: D f32, A bf16, B bf16, both K-major, N = Co, M = 128
-	const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
-	const uint32_t lbo_a = (uint32_t)(RT * a.MR + 2) * (uint32_t)a.P * 16u, lbo_b = 9u * (uint32_t)a.Co * 16u;
+	const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.CoT >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+	const uint32_t lbo_a = (uint32_t)(RT * a.MR + 2) * (uint32_t)a.P * 16u, lbo_b = 9u * (uint32_t)a.CoT * 16u;
 	// the shift dx: a pixel (one copy) or a copy (three)
 	const uint64_t dx_step = a.NC == 3 ? (uint64_t)(a.copy_bytes >> 4) : 1u;
 	int fail = 0, loaded = 0, issued = -1;
@@ -523,7 +527,7 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 			for (int cp = 0; cp < a.NC; ++cp)
 				tma_load_5d(base + (uint32_t)cp * a.copy_bytes, &tx, smem_u32(full + s), 0, x0 - 1 + (a.NC == 3 ? cp : 0),
 							yy - 1, c * (a.CK / 8), n);
-			tma_load_4d(base + a.a_span, &tw, smem_u32(full + s), 0, 0, 0, c * (a.CK / 8));
+			tma_load_4d(base + a.a_span, &tw, smem_u32(full + s), 0, co0, 0, c * (a.CK / 8));
 		};
 		for (int c = 0; c < S && c < nch; ++c) load(c);
 		loaded = S < nch ? S : nch;
@@ -541,11 +545,11 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 			for (int j = 0; j < a.CK / 16; ++j)
 				for (int t = 0; t < 9; ++t) {
 					const int dy = t / 3, dx = t % 3;
-					const uint64_t bd = bd0 + (uint64_t)((2 * j * 9 + t) * a.Co);
+					const uint64_t bd = bd0 + (uint64_t)((2 * j * 9 + t) * a.CoT);
 					const uint32_t acc = (c > 0 || j > 0 || t > 0) ? 1u : 0u;
 					uint64_t ad = ad0 + (uint64_t)(2 * j) * (lbo_a >> 4) + (uint64_t)(dy * a.P) + (uint64_t)dx * dx_step;
 					for (int r = 0; r < RT; ++r) {
-						umma_f16(tmem + (uint32_t)(r * a.Co), ad, bd, idesc, acc);
+						umma_f16(tmem + (uint32_t)(r * a.CoT), ad, bd, idesc, acc);
 						ad += (uint64_t)(a.MR * a.P);
 					}
 				}
@@ -578,10 +582,10 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 		// epilogue: warp w owns TMEM lanes (= tile pixels) 32 w .. 32 w + 31
 		const int px = warp * 32 + lane;
 		for (int rr = 0; rr < RT; ++rr) {
-			for (int c0 = 0; c0 < a.Co; c0 += 16) {
+			for (int c0 = 0; c0 < a.CoT; c0 += 16) {
 				const int64_t m = ((int64_t)(row + rr * a.MR) * a.W) + x0 + px;
 				uint32_t r[16];
-				const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(rr * a.Co + c0);
+				const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(rr * a.CoT + c0);
 				asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
 							 "[%16];\n"
 							 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
@@ -594,8 +598,8 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 				for (int q = 0; q < 8; ++q) {
 					float v0 = __uint_as_float(r[2 * q]), v1 = __uint_as_float(r[2 * q + 1]);
 					if (a.use_bias) {
-						v0 += a.bias[c0 + 2 * q];
-						v1 += a.bias[c0 + 2 * q + 1];
+						v0 += a.bias[co0 + c0 + 2 * q];
+						v1 += a.bias[co0 + c0 + 2 * q + 1];
 					}
 					if (a.relu) {
 						v0 = fmaxf(v0, 0.f);
@@ -603,7 +607,7 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 					}
 					o[q] = __floats2bfloat162_rn(v0, v1);
 				}
-				uint4 *dst = reinterpret_cast<uint4 *>(a.y + m * a.Co + c0);
+				uint4 *dst = reinterpret_cast<uint4 *>(a.y + m * a.Co + co0 + c0);
 				dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
 				dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
 			}
@@ -1977,7 +1981,7 @@ int halo_plan(int Ci, int Co, int RT, HaloArgs &a) {
 			if (Ci % ck) continue;
 			const int nch = Ci / ck;
 			const uint32_t cb = (uint32_t)(RT * a.MR + 2) * (uint32_t)a.P * (uint32_t)ck * 2u;
-			const uint32_t ab = (uint32_t)a.NC * cb, bb = 18u * (uint32_t)Co * (uint32_t)ck;
+			const uint32_t ab = (uint32_t)a.NC * cb, bb = 18u * (uint32_t)a.CoT * (uint32_t)ck;
 			const uint32_t stage = align1k(ab) + align1k(bb);
 			int S = nch < 3 ? nch : 3;
 			while (S > 1 && (uint64_t)S * stage + 1024 > cap) --S;
@@ -2015,14 +2019,21 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 		return KEL_OK;
 	}
 	const int tpr = W >= 128 ? W / 128 : 1;
+	const int sms = U->sms > 0 ? U->sms : 148;
 	// M tiles per CTA: the most (4, 2, 1) whose accumulators fit TMEM and
-	// that still leave a CTA per SM
+	// that still leave a CTA per SM; with fewer tiles than SMs, the output
+	// channels split over two CTAs (at least 32 channels each)
 	a.RT = 0;
+	a.CoT = co;
 	for (const int rt : {4, 2, 1})
-		if (!a.RT && rt * co <= 512 && H % (rt * a.MR) == 0 &&
-			(int64_t)n * (H / (rt * a.MR)) * tpr >= (U->sms > 0 ? U->sms : 148) && halo_plan(ci, co, rt, a))
+		if (!a.RT && rt * co <= 512 && H % (rt * a.MR) == 0 && (int64_t)n * (H / (rt * a.MR)) * tpr >= sms &&
+			halo_plan(ci, co, rt, a))
 			a.RT = rt;
-	if (!a.RT && halo_plan(ci, co, 1, a)) a.RT = 1;
+	if (!a.RT && H % a.MR == 0) {
+		const int64_t tiles = (int64_t)n * (H / a.MR) * tpr;
+		if (tiles < sms && co % 32 == 0 && co / 2 >= 32) a.CoT = co / 2;
+		if (halo_plan(ci, co, 1, a)) a.RT = 1;
+	}
 	if (!a.RT) return KEL_OK;
 	CUtensorMap tx, tw;
 	{ // x (N,H,W,Ci) as (8 channels, x, y, channel group, n)
@@ -2038,7 +2049,7 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	{ // w (Co, 9, Ci) as (8 channels, co, tap, channel group)
 		const cuuint64_t dims[4] = {8, (cuuint64_t)co, 9, (cuuint64_t)(ci / 8)};
 		const cuuint64_t strides[3] = {(cuuint64_t)9 * ci * 2, (cuuint64_t)ci * 2, 16};
-		const cuuint32_t box[4] = {8, (cuuint32_t)co, 9, (cuuint32_t)(a.CK / 8)};
+		const cuuint32_t box[4] = {8, (cuuint32_t)a.CoT, 9, (cuuint32_t)(a.CK / 8)};
 		const cuuint32_t es[4] = {1, 1, 1, 1};
 		if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(w), dims, strides, box, es,
 				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -2055,7 +2066,7 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	a.relu = relu;
 	a.use_bias = bias;
 	a.tmem_cols = 32;
-	while (a.tmem_cols < (uint32_t)(a.RT * co)) a.tmem_cols <<= 1;
+	while (a.tmem_cols < (uint32_t)(a.RT * a.CoT)) a.tmem_cols <<= 1;
 	a.err = U->d_err;
 	const size_t smem = (size_t)a.stages * a.stage_bytes + (size_t)a.stages * 16 + 16;
 	static bool attr_set = false;
@@ -2063,7 +2074,7 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 		KEL_CUDA(cudaFuncSetAttribute(conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
 		attr_set = true;
 	}
-	conv_halo<<<(unsigned)((int64_t)n * (H / (a.RT * a.MR)) * tpr), 128, smem, U->stream>>>(tx, tw, a);
+	conv_halo<<<(unsigned)((int64_t)n * (H / (a.RT * a.MR)) * tpr * (co / a.CoT)), 128, smem, U->stream>>>(tx, tw, a);
 	KEL_CUDA(cudaGetLastError());
 	*launched = 1;
 	return KEL_OK;
