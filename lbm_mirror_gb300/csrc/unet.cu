@@ -621,28 +621,35 @@ __global__ void __launch_bounds__(128) conv_halo(const __grid_constant__ CUtenso
 	}
 }
 
-// ---- row-run convolution: resident weights, rolling halo rows ---------------------
+// ---- row-run convolution: resident weights, input-row stationary ----------------
 //
 // For layers whose weights and four input rows fit shared memory: one CTA
 // computes RL consecutive output rows of one 128-pixel column tile (n, x0).
-// The weights (Co x 9 x Ci) arrive once, by TMA, as [g][tap][co][8 channels]
-// (B of tap t and channel groups 2j, 2j + 1 at ((2 j) * 9 + t) * Co * 16,
-// K-direction stride 9 * Co * 16 B).  Input rows y0 - 1 .. y0 + RL arrive one
-// by one into a ring of NR slots, each row a TMA box of 130 pixels x Ci
-// channels, zero-filled outside the image, laid out (channel group, pixel, 8
-// channels): the A operand of output row y and tap (dy, dx) is the slot of
-// input row y - 1 + dy read from pixel dx (K-major, no swizzle: 8-pixel stride
-// 128 B, channel-group stride 130 * 16 B).  So every input row is read once
-// per CTA instead of three times, and the weights once per RL rows.
-// Warp roles: warp 0 issues the copies, warp 1 the MMAs, warps 2-5 drain
-// the accumulators (bias, ReLU, bf16, NHWC stores).  The accumulator is
-// double-buffered in TMEM (2 x Co columns), so row i + 1's MMAs run while
-// row i is stored.  mbarriers: row_full/row_empty per ring slot (TMA bytes;
-// the MMAs of the last output row that reads the slot), w_full, acc_full and
-// acc_empty per accumulator (MMA commit; the four epilogue warps).  Every
-// wait is bounded; on timeout the thread records the failure in *err and
-// stops, the producer waits (bounded) for the copies it issued, and the MMA
-// thread for its MMAs before TMEM is freed.
+// The weights (Co x 9 x Ci) arrive once, by TMA, as [g][kx][ky][co][8
+// channels]: for a column shift dx the three kernel rows' Co x 8 blocks are
+// consecutive, so B rows (ky, co) form one operand of up to 3 Co rows (8-row
+// stride 128 B, channel-group stride 9 * Co * 16 B).  Input rows y0 - 1 ..
+// y0 + RL stream once each through a ring of NR slots, each row a TMA box of
+// 130 pixels x Ci channels, zero-filled outside the image, laid out (channel
+// group, pixel, 8 channels): the A operand of input row X and shift dx is
+// the slot read from pixel dx (K-major, no swizzle: 8-pixel stride 128 B,
+// channel-group stride 130 * 16 B).  Input row X feeds output rows X + 1, X,
+// X - 1 through kernel rows ky = 0, 1, 2; the accumulators of consecutive
+// output rows sit in TMEM in decreasing row order (Co columns each), so one
+// MMA with N = (number of kernel rows) x Co adds X's contribution to up to
+// three output rows at once: the A operand is read once per input row
+// instead of three times.  Accumulators come in blocks of RB output rows,
+// double-buffered (2 RB Co columns); an MMA whose output rows fall in two
+// blocks is split in two.  The epilogue warps zero a block's columns after
+// draining it (and both blocks at the start), so every MMA accumulates.
+// Warp roles: warp 0 issues the copies, warp 1 the MMAs, warps 2-5 drain the
+// accumulators (bias, ReLU, bf16, NHWC stores) row by row as each output
+// row completes.  mbarriers: row_full / row_empty per ring slot (TMA bytes;
+// the MMAs that read the row), w_full, row_done per accumulator row slot
+// (MMA commit) and acc_empty per block buffer (the four epilogue warps, once
+// the block's rows are drained and zeroed).  Every wait is bounded; on timeout the thread records the failure
+// in *err and stops, the producer waits (bounded) for the copies it issued,
+// and the MMA thread for its MMAs before TMEM is freed.
 
 struct RowsArgs {
 	const float *bias;
@@ -650,6 +657,7 @@ struct RowsArgs {
 	int N, H, W, Ci, Co;
 	int relu, use_bias;
 	int RL, NR, runs; // output rows per CTA, ring slots, CTAs per column tile
+	int RB, KY;       // output rows per accumulator block, kernel rows per MMA (N = KY Co <= 256)
 	uint32_t row_bytes, row_span, w_bytes, w_off, mbar_off;
 	uint32_t tmem_cols;
 	int *err;
@@ -659,13 +667,13 @@ __global__ void __launch_bounds__(192) conv_rows(const __grid_constant__ CUtenso
 												 const __grid_constant__ CUtensorMap tw, RowsArgs a) {
 	extern __shared__ __align__(1024) uint8_t sm[];
 	const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-	const int NR = a.NR;
+	const int NR = a.NR, RB = a.RB;
 	uint64_t *row_full = reinterpret_cast<uint64_t *>(sm + a.mbar_off);
 	uint64_t *row_empty = row_full + NR;
 	uint64_t *w_full = row_empty + NR;
-	uint64_t *acc_full = w_full + 1;
-	uint64_t *acc_empty = acc_full + 2;
-	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(acc_empty + 2);
+	uint64_t *acc_empty = w_full + 1;  // [2]: a block buffer drained and zeroed
+	uint64_t *row_done = acc_empty + 2; // [2 RB]: an output row's accumulator complete
+	uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(row_done + 2 * RB);
 
 	const int tpr = a.W / 128;
 	const int colt = (int)(blockIdx.x / (unsigned)a.runs), run = (int)(blockIdx.x % (unsigned)a.runs);
@@ -674,6 +682,11 @@ __global__ void __launch_bounds__(192) conv_rows(const __grid_constant__ CUtenso
 	const int rows = a.H - y0 < a.RL ? a.H - y0 : a.RL;
 	const int nx = rows + 2;
 	constexpr uint32_t R = HX * 16u;
+	// TMEM column of output row r (0 .. rows - 1): block r / RB in buffer
+	// (r / RB) & 1, rows of a block in decreasing order; slot_of(r) numbers
+	// the 2 RB row slots, used by rows r, r + 2 RB, ...
+	auto slot_of = [&](int r) -> int { return ((r / RB) & 1) * RB + (RB - 1 - r % RB); };
+	auto col_of = [&](int r) -> uint32_t { return (uint32_t)(slot_of(r) * a.Co); };
 
 	if (tid == 0) {
 		for (int s = 0; s < NR; ++s) {
@@ -681,10 +694,10 @@ __global__ void __launch_bounds__(192) conv_rows(const __grid_constant__ CUtenso
 			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(row_empty + s)));
 		}
 		asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(w_full)));
-		for (int b = 0; b < 2; ++b) {
-			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(acc_full + b)));
+		for (int b = 0; b < 2; ++b)
 			asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(smem_u32(acc_empty + b)));
-		}
+		for (int k = 0; k < 2 * RB; ++k)
+			asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(row_done + k)));
 		asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
 	}
 	if (warp == 1) {
@@ -701,7 +714,7 @@ __global__ void __launch_bounds__(192) conv_rows(const __grid_constant__ CUtenso
 		if (lane == 0) { // producer
 			int fail = 0, issued = 0;
 			mbar_expect_tx(smem_u32(w_full), a.w_bytes);
-			tma_load_4d(smem_u32(sm + a.w_off), &tw, smem_u32(w_full), 0, 0, 0, 0);
+			tma_load_5d(smem_u32(sm + a.w_off), &tw, smem_u32(w_full), 0, 0, 0, 0, 0);
 			for (int j = 0; j < nx; ++j) {
 				const int s = j % NR;
 				if (j >= NR && !mbar_wait(smem_u32(row_empty + s), (uint32_t)(((j / NR) - 1) & 1))) {
@@ -720,95 +733,137 @@ __global__ void __launch_bounds__(192) conv_rows(const __grid_constant__ CUtenso
 			if (fail) atomicExch(a.err, 1);
 		}
 	} else if (warp == 1) {
-		if (lane == 0) { // MMA issuer
-			// D f32, A bf16, B bf16, both K-major, N = Co, M = 128
-			const uint32_t idesc =
-				(1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(a.Co >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+		if (lane == 0) { // MMA issuer: input row j feeds output rows j - ky, ky = 0, 1, 2
+			// D f32, A bf16, B bf16, both K-major, M = 128, N = nky * Co
+			const uint32_t idesc0 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(128 >> 4) << 24);
 			const uint32_t lbo_b = 9u * (uint32_t)a.Co * 16u;
 			const uint64_t bd0 = umma_desc(smem_u32(sm + a.w_off), lbo_b, 128u);
 			const uint64_t a_k = (2u * R) >> 4, b_k = 18u * (uint64_t)a.Co;
 			const int nk = a.Ci / 16;
-			int fail = !mbar_wait(smem_u32(w_full), 0u), done = 0;
-			for (int i = 0; i < rows && !fail; ++i) {
-				for (int j = i == 0 ? 0 : i + 2; j <= i + 2 && !fail; ++j)
-					if (!mbar_wait(smem_u32(row_full + j % NR), (uint32_t)((j / NR) & 1))) fail = 1;
-				const int b = i & 1;
-				if (!fail && i >= 2 && !mbar_wait(smem_u32(acc_empty + b), (uint32_t)(((i >> 1) - 1) & 1))) fail = 1;
-				if (fail) break;
-				asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-				// descriptors stepped by constant adds: a k-step moves A by two
-				// channel groups (2 R bytes) and B by 18 Co 16-byte units
-				const uint32_t d_tmem = tmem + (uint32_t)(b * a.Co);
-				uint64_t ad_row[3];
-				for (int dy = 0; dy < 3; ++dy) ad_row[dy] = umma_desc(smem_u32(sm + (size_t)((i + dy) % NR) * a.row_span), R, 128u);
-				uint32_t acc = 0u;
-				for (int t = 0; t < 9; ++t) {
-					uint64_t ad = ad_row[t / 3] + (uint64_t)(t % 3);
-					uint64_t bd = bd0 + (uint64_t)t * (uint64_t)a.Co;
-#pragma unroll 2
-					for (int k = 0; k < nk; ++k) {
-						umma_f16(d_tmem, ad, bd, idesc, acc);
-						acc = 1u;
-						ad += a_k;
-						bd += b_k;
+			int fail = !mbar_wait(smem_u32(w_full), 0u), done = 0; // output rows committed
+			for (int j = 0; j < nx && !fail; ++j) {
+				if (!mbar_wait(smem_u32(row_full + j % NR), (uint32_t)((j / NR) & 1))) {
+					fail = 1;
+					break;
+				}
+				// the first output row of a block: its buffer must be drained
+				// (and zeroed) by the epilogue
+				if (j < rows && j % RB == 0) {
+					const int blk = j / RB;
+					if (!mbar_wait(smem_u32(acc_empty + (blk & 1)), (uint32_t)((blk >> 1) & 1))) {
+						fail = 1;
+						break;
 					}
 				}
-				// input row i is read by no later output row
-				if (i + 1 < rows)
-					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-						smem_u32(row_empty + i % NR)));
+				asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
+				const int kmin = j - rows + 1 > 0 ? j - rows + 1 : 0, kmax = j < 2 ? j : 2;
+				const uint64_t ad_row = umma_desc(smem_u32(sm + (size_t)(j % NR) * a.row_span), R, 128u);
+				// groups of kernel rows [k0, k1] whose output rows share a block
+				for (int k0 = kmin; k0 <= kmax;) {
+					int k1 = k0;
+					while (k1 + 1 <= kmax && k1 + 1 - k0 < a.KY && (j - k1 - 1) / RB == (j - k0) / RB) ++k1;
+					const int nky = k1 - k0 + 1;
+					const uint32_t idesc = idesc0 | ((uint32_t)((nky * a.Co) >> 3) << 17);
+					const uint32_t d_tmem = tmem + col_of(j - k0);
+					for (int dx = 0; dx < 3; ++dx) {
+						uint64_t ad = ad_row + (uint64_t)dx;
+						uint64_t bd = bd0 + (uint64_t)((dx * 3 + k0) * a.Co);
+#pragma unroll 2
+						for (int k = 0; k < nk; ++k) {
+							umma_f16(d_tmem, ad, bd, idesc, 1u);
+							ad += a_k;
+							bd += b_k;
+						}
+					}
+					k0 = k1 + 1;
+				}
+				// input row j is read by no later MMA
 				asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-					smem_u32(acc_full + b)));
-				done = i + 1;
+					smem_u32(row_empty + j % NR)));
+				// output row j - 2 is complete
+				const int rl = j - 2;
+				if (rl >= 0 && rl < rows) {
+					asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+						smem_u32(row_done + slot_of(rl))));
+					done = rl + 1;
+				}
 			}
-			// the MMAs have finished before TMEM is freed
-			if (done > 0) mbar_wait(smem_u32(acc_full + ((done - 1) & 1)), (uint32_t)(((done - 1) >> 1) & 1));
+			// the MMAs and their arrivals have finished before TMEM is freed
+			if (done > 0)
+				mbar_wait(smem_u32(row_done + slot_of(done - 1)), (uint32_t)(((done - 1) / (2 * RB)) & 1));
 			if (fail) atomicExch(a.err, 1);
 		}
 	} else { // epilogue: warp w reads TMEM lanes (pixels) 32 (w % 4) .. + 31
 		const int q = warp & 3;
 		const int px = q * 32 + lane;
+		const uint32_t lane_base = tmem + ((uint32_t)(q * 32) << 16);
+		uint32_t zero[16];
+#pragma unroll
+		for (int k = 0; k < 16; ++k) zero[k] = 0u;
+		auto zero_cols = [&](uint32_t c_begin, uint32_t c_end) {
+			for (uint32_t c = c_begin; c < c_end; c += 16)
+				asm volatile("tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};\n" ::"r"(
+								 lane_base + c),
+							 "r"(zero[0]), "r"(zero[1]), "r"(zero[2]), "r"(zero[3]), "r"(zero[4]), "r"(zero[5]),
+							 "r"(zero[6]), "r"(zero[7]), "r"(zero[8]), "r"(zero[9]), "r"(zero[10]), "r"(zero[11]),
+							 "r"(zero[12]), "r"(zero[13]), "r"(zero[14]), "r"(zero[15]));
+			asm volatile("tcgen05.wait::st.sync.aligned;\n" ::: "memory");
+		};
+		// both buffers start zeroed and free
+		zero_cols(0u, 2u * (uint32_t)(RB * a.Co));
+		asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+		__syncwarp();
+		if (lane == 0)
+			for (int b = 0; b < 2; ++b)
+				asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(acc_empty + b)) : "memory");
 		int fail = 0;
-		for (int i = 0; i < rows; ++i) {
-			const int b = i & 1;
-			if (!mbar_wait(smem_u32(acc_full + b), (uint32_t)((i >> 1) & 1))) {
+		for (int r = 0; r < rows; ++r) {
+			if (!mbar_wait(smem_u32(row_done + slot_of(r)), (uint32_t)((r / (2 * RB)) & 1))) {
 				fail = 1;
 				break;
 			}
 			asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-			const int64_t m = ((int64_t)n * a.H + y0 + i) * a.W + x0 + px;
-			for (int c0 = 0; c0 < a.Co; c0 += 16) {
-				uint32_t r[16];
-				const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * a.Co + c0);
-				asm volatile(
-					"tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-					"[%16];\n"
-					: "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-					  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-					  "=r"(r[15])
-					: "r"(taddr));
-				asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-				__align__(16) __nv_bfloat162 o[8];
+			{
+				const int64_t m = ((int64_t)n * a.H + y0 + r) * a.W + x0 + px;
+				for (int c0 = 0; c0 < a.Co; c0 += 16) {
+					uint32_t v[16];
+					asm volatile(
+						"tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+						"[%16];\n"
+						: "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+						  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+						  "=r"(v[15])
+						: "r"(lane_base + col_of(r) + (uint32_t)c0));
+					asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+					__align__(16) __nv_bfloat162 o[8];
 #pragma unroll
-				for (int k = 0; k < 8; ++k) {
-					float v0 = __uint_as_float(r[2 * k]), v1 = __uint_as_float(r[2 * k + 1]);
-					if (a.use_bias) {
-						v0 += a.bias[c0 + 2 * k];
-						v1 += a.bias[c0 + 2 * k + 1];
+					for (int k = 0; k < 8; ++k) {
+						float v0 = __uint_as_float(v[2 * k]), v1 = __uint_as_float(v[2 * k + 1]);
+						if (a.use_bias) {
+							v0 += a.bias[c0 + 2 * k];
+							v1 += a.bias[c0 + 2 * k + 1];
+						}
+						if (a.relu) {
+							v0 = fmaxf(v0, 0.f);
+							v1 = fmaxf(v1, 0.f);
+						}
+						o[k] = __floats2bfloat162_rn(v0, v1);
 					}
-					if (a.relu) {
-						v0 = fmaxf(v0, 0.f);
-						v1 = fmaxf(v1, 0.f);
-					}
-					o[k] = __floats2bfloat162_rn(v0, v1);
+					uint4 *dst = reinterpret_cast<uint4 *>(a.y + m * a.Co + c0);
+					dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
+					dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
 				}
-				uint4 *dst = reinterpret_cast<uint4 *>(a.y + m * a.Co + c0);
-				dst[0] = *reinterpret_cast<const uint4 *>(&o[0]);
-				dst[1] = *reinterpret_cast<const uint4 *>(&o[4]);
 			}
-			asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
-			__syncwarp();
-			if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(acc_empty + b)) : "memory");
+			// zero the row's columns for the slot's next use; after the
+			// block's last row, free the block buffer
+			zero_cols(col_of(r), col_of(r) + (uint32_t)a.Co);
+			if (r % RB == RB - 1 || r == rows - 1) {
+				asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
+				__syncwarp();
+				if (lane == 0)
+					asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(acc_empty + ((r / RB) & 1)))
+								 : "memory");
+			}
 		}
 		if (fail && lane == 0) atomicExch(a.err, 1);
 	}
@@ -2090,11 +2145,19 @@ int rows_plan(const kel_unet *U, int n, int H, int W, int Ci, int Co, RowsArgs &
 	a.row_bytes = (uint32_t)HX * (uint32_t)Ci * 2u;
 	a.row_span = (a.row_bytes + 127u) / 128u * 128u;
 	a.w_bytes = (uint32_t)Co * 9u * (uint32_t)Ci * 2u;
+	// accumulator blocks of RB output rows (two of them within 256 TMEM
+	// columns when Co allows, so that two CTAs share an SM), up to three
+	// kernel rows per MMA.  RB >= 2: the three output rows an input row feeds
+	// must lie in the two buffered blocks, or the MMAs would wait for a
+	// block that they have yet to complete.
+	a.RB = 128 / Co < 2 ? 2 : (128 / Co > 8 ? 8 : 128 / Co);
+	if (2 * a.RB * Co > 512) return 0;
+	a.KY = 256 / Co < 3 ? 256 / Co : 3;
 	a.tmem_cols = 32;
-	while (a.tmem_cols < 2u * (uint32_t)Co) a.tmem_cols <<= 1;
+	while (a.tmem_cols < 2u * (uint32_t)(a.RB * Co)) a.tmem_cols <<= 1;
 	a.w_off = (uint32_t)a.NR * a.row_span;
 	a.mbar_off = a.w_off + (a.w_bytes + 127u) / 128u * 128u;
-	const uint32_t smem = a.mbar_off + (2u * (uint32_t)a.NR + 5u) * 8u + 16u;
+	const uint32_t smem = a.mbar_off + (2u * (uint32_t)a.NR + 3u + 2u * (uint32_t)a.RB) * 8u + 16u;
 	if (smem > 200u * 1024u) return 0;
 	int per_sm = (int)((227u * 1024u) / (smem + 1024u));
 	if (per_sm > (int)(512u / a.tmem_cols)) per_sm = (int)(512u / a.tmem_cols);
@@ -2133,12 +2196,13 @@ int conv_rows_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 				CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
 			return KEL_OK;
 	}
-	{ // w (Co, 9, Ci) as (8 channels, co, tap, channel group): the whole tensor
-		const cuuint64_t dims[4] = {8, (cuuint64_t)co, 9, (cuuint64_t)(ci / 8)};
-		const cuuint64_t strides[3] = {(cuuint64_t)9 * ci * 2, (cuuint64_t)ci * 2, 16};
-		const cuuint32_t box[4] = {8, (cuuint32_t)co, 9, (cuuint32_t)(ci / 8)};
-		const cuuint32_t es[4] = {1, 1, 1, 1};
-		if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<bf16 *>(w), dims, strides, box, es,
+	{ // w (Co, 3, 3, Ci) as (8 channels, co, ky, kx, channel group): the whole
+	  // tensor, in shared memory as [g][kx][ky][co][8]
+		const cuuint64_t dims[5] = {8, (cuuint64_t)co, 3, 3, (cuuint64_t)(ci / 8)};
+		const cuuint64_t strides[4] = {(cuuint64_t)9 * ci * 2, (cuuint64_t)3 * ci * 2, (cuuint64_t)ci * 2, 16};
+		const cuuint32_t box[5] = {8, (cuuint32_t)co, 3, 3, (cuuint32_t)(ci / 8)};
+		const cuuint32_t es[5] = {1, 1, 1, 1, 1};
+		if (enc(&tw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 5, const_cast<bf16 *>(w), dims, strides, box, es,
 				CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
 				CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
 			return KEL_OK;
@@ -2153,7 +2217,7 @@ int conv_rows_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	a.relu = relu;
 	a.use_bias = bias;
 	a.err = U->d_err;
-	const size_t smem = (size_t)a.mbar_off + (2u * (size_t)a.NR + 5u) * 8u + 16u;
+	const size_t smem = (size_t)a.mbar_off + (2u * (size_t)a.NR + 3u + 2u * (size_t)a.RB) * 8u + 16u;
 	static bool attr_set = false;
 	if (!attr_set) {
 		KEL_CUDA(cudaFuncSetAttribute(conv_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
