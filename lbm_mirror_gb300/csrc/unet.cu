@@ -2145,21 +2145,24 @@ int rows_plan(const kel_unet *U, int n, int H, int W, int Ci, int Co, RowsArgs &
 	a.row_bytes = (uint32_t)HX * (uint32_t)Ci * 2u;
 	a.row_span = (a.row_bytes + 127u) / 128u * 128u;
 	a.w_bytes = (uint32_t)Co * 9u * (uint32_t)Ci * 2u;
-	// accumulator blocks of RB output rows (two of them within 256 TMEM
-	// columns when Co allows, so that two CTAs share an SM), up to three
-	// kernel rows per MMA.  RB >= 2: the three output rows an input row feeds
-	// must lie in the two buffered blocks, or the MMAs would wait for a
-	// block that they have yet to complete.
-	a.RB = 128 / Co < 2 ? 2 : (128 / Co > 8 ? 8 : 128 / Co);
+	a.w_off = (uint32_t)a.NR * a.row_span;
+	a.mbar_off = a.w_off + (a.w_bytes + 127u) / 128u * 128u;
+	const uint32_t smem = a.mbar_off + (2u * (uint32_t)a.NR + 3u + 16u) * 8u + 16u;
+	if (smem > 200u * 1024u) return 0;
+	const int smem_per_sm = (int)((227u * 1024u) / (smem + 1024u));
+	// accumulator blocks of RB output rows, up to three kernel rows per MMA:
+	// RB as large as the TMEM share of the CTAs that shared memory lets onto
+	// an SM allows (up to four CTAs, at most 8 rows).  RB >= 2: the three
+	// output rows an input row feeds must lie in the two buffered blocks, or
+	// the MMAs would wait for a block that they have yet to complete.
+	const int share = 512 / (smem_per_sm < 1 ? 1 : (smem_per_sm > 4 ? 4 : smem_per_sm));
+	a.RB = share / (2 * Co) > 8 ? 8 : share / (2 * Co);
+	if (a.RB < 2) a.RB = 2;
 	if (2 * a.RB * Co > 512) return 0;
 	a.KY = 256 / Co < 3 ? 256 / Co : 3;
 	a.tmem_cols = 32;
 	while (a.tmem_cols < 2u * (uint32_t)(a.RB * Co)) a.tmem_cols <<= 1;
-	a.w_off = (uint32_t)a.NR * a.row_span;
-	a.mbar_off = a.w_off + (a.w_bytes + 127u) / 128u * 128u;
-	const uint32_t smem = a.mbar_off + (2u * (uint32_t)a.NR + 3u + 2u * (uint32_t)a.RB) * 8u + 16u;
-	if (smem > 200u * 1024u) return 0;
-	int per_sm = (int)((227u * 1024u) / (smem + 1024u));
+	int per_sm = smem_per_sm;
 	if (per_sm > (int)(512u / a.tmem_cols)) per_sm = (int)(512u / a.tmem_cols);
 	if (per_sm > 10) per_sm = 10;
 	if (per_sm < 1) per_sm = 1;
@@ -2217,7 +2220,7 @@ int conv_rows_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	a.relu = relu;
 	a.use_bias = bias;
 	a.err = U->d_err;
-	const size_t smem = (size_t)a.mbar_off + (2u * (size_t)a.NR + 3u + 2u * (size_t)a.RB) * 8u + 16u;
+	const size_t smem = (size_t)a.mbar_off + (2u * (size_t)a.NR + 3u + 16u) * 8u + 16u;
 	static bool attr_set = false;
 	if (!attr_set) {
 		KEL_CUDA(cudaFuncSetAttribute(conv_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
