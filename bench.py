@@ -343,13 +343,17 @@ def run_warm_start(args, rank, world):
     gen_updates = float(np.sum(states.steps.astype(np.float64)) * nx * ny)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    model = WS.train(WS.steady_subset(states), epochs=args.epochs, batch=32, lr=2e-3, widths=widths,
-                     log_every=32, rho_target_rms=args.rho_rms, residual=args.residual,
-                     weight_by_steps=args.weight_by_steps, rho_norm=args.rho_norm,
-                     rho_residual=args.rho_residual, flip=args.flip)
+    kw = dict(epochs=args.epochs, batch=32, lr=2e-3, widths=widths, log_every=32, rho_target_rms=args.rho_rms,
+              residual=args.residual, weight_by_steps=args.weight_by_steps, rho_norm=args.rho_norm,
+              rho_residual=args.rho_residual, flip=args.flip)
+    if args.ensemble > 1:
+        # the mean prediction of networks trained with seeds 1 .. K
+        model = WS.train_ensemble(WS.steady_subset(states), seeds=tuple(range(1, args.ensemble + 1)), **kw)
+    else:
+        model = WS.train(WS.steady_subset(states), **kw)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
-    n_steps = args.epochs * (args.train // 32)
+    n_steps = args.epochs * (args.train // 32) * max(args.ensemble, 1)
     train_flops = 3 * unet_flops_per_sample(ny, nx, widths) * 32 * n_steps
     r = WS.evaluate(model, test_ch, tol=args.tol, check_every=1000, max_steps=args.max_steps, variants=True)
     r2 = WS.evaluate(model, test_ch, tol=args.tol, check_every=1000, max_steps=args.max_steps)  # a second pair
@@ -363,14 +367,18 @@ def run_warm_start(args, rank, world):
     t1 = time.perf_counter()
     WS.predict(model, d_mask, d_umax, d_tau)
     t_inf = time.perf_counter() - t1
-    inf_flops = unet_flops_per_sample(ny, nx, widths) * args.test
+    inf_flops = unet_flops_per_sample(ny, nx, widths) * args.test * max(args.ensemble, 1)
     bf16 = None
     pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk):
         bf16 = json.load(open(pk)).get("bf16_tflops")
+    # the first member's training history stands for the ensemble's
+    hist = model.members[0].history if args.ensemble > 1 else model.history
     if rank == 0:
         if args.save_dir:
-            np.save(os.path.join(args.save_dir, "warm_start_unet_params.npy"), model.net.params())
+            nets = [m.net for m in model.members] if args.ensemble > 1 else [model.net]
+            for k, net in enumerate(nets):
+                np.save(os.path.join(args.save_dir, "warm_start_unet_params_%d.npy" % k), net.params())
         line = {"metric": "time_to_steady_state_s", "value": r["warm_seconds"], "unit": "s", "n_gpus": world,
                 "steps": r["warm_steps_max"], "warmup": 0, "ms_per_step": None, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 lattice, bf16 network", "data": "synthetic",
@@ -379,8 +387,10 @@ def run_warm_start(args, rank, world):
                            "rho_target_rms": args.rho_rms, "residual_u": args.residual,
                            "weight_by_steps": args.weight_by_steps, "rho_norm": args.rho_norm,
                            "rho_residual": args.rho_residual, "flip_augment": args.flip,
+                           "ensemble": args.ensemble,
                            "widths": list(widths),
-                           "params": model.net.n_params, "rho_scale": model.rho_scale},
+                           "params": sum(m.net.n_params for m in model.members) if args.ensemble > 1
+                           else model.net.n_params, "rho_scale": model.rho_scale},
                 "plain_seconds": r["plain_seconds"], "speedup": r["speedup"],
                 "repeat": {"plain_seconds": r2["plain_seconds"], "warm_seconds": r2["warm_seconds"],
                            "speedup": r2["speedup"]},
@@ -398,8 +408,8 @@ def run_warm_start(args, rank, world):
                                              "exact_u_net_rho": r["exact_u_net_rho_steps_mean"],
                                              "net_u_exact_rho": r["net_u_exact_rho_steps_mean"]},
                 "training": {"seconds": t_train, "adam_steps": n_steps, "batch": 32,
-                             "loss_first": model.history[0][1] if model.history else None,
-                             "loss_last": model.history[-1][1] if model.history else None,
+                             "loss_first": hist[0][1] if hist else None,
+                             "loss_last": hist[-1][1] if hist else None,
                              "tflops": train_flops / t_train / 1e12},
                 "inference": {"seconds": t_inf, "samples": args.test, "tflops": inf_flops / t_inf / 1e12},
                 "data_generation": {"seconds": states.seconds, "channels": args.train,
@@ -573,6 +583,8 @@ def main():
                     help="warm start: no y-mirrored copies in the training minibatches")
     ap.add_argument("--rho-residual", action="store_true",
                     help="warm start: the density output corrects the lubrication pressure plane")
+    ap.add_argument("--ensemble", type=int, default=1,
+                    help="warm start: networks trained with seeds 1 .. K, predictions averaged")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
