@@ -10,7 +10,18 @@
 // [c_in][2-ky][2-kx][c_out] for the data gradient.  Architecture as in
 // oracle/unet_oracle.py (4 levels, concat skips, 1x1 head).
 //
-// Tensor-core GEMMs (bf16 in, FP32 accumulate, mma.sync m16n8k16):
+// Convolutions on the fifth-generation tensor cores (tcgen05.mma, bf16 in,
+// FP32 accumulators in TMEM, operands staged by TMA; the default):
+//   conv_rows        forward and data gradient of layers 128+ pixels wide
+//                    whose weights stay in shared memory: input rows stream
+//                    once each, one MMA feeds three output-row accumulators;
+//   conv_halo        the other layers: per chunk of input channels a TMA halo
+//                    tile, the nine taps as shifted descriptors;
+//   conv_wgrad_halo  weight gradients from TMA-loaded halo rows, FP32
+//                    partials per pixel chunk reduced in fixed order;
+//   conv_tc, conv_wgrad_tc  im2col forms for levels narrower than the halo
+//                    kernels take.
+// The same GEMMs on warp-level mma.sync m16n8k16 (kel_unet_set_conv_kernel):
 //   conv_igemm  implicit GEMM, M = pixels, N = c_out, K = 9 c_in; also the
 //               data gradient (same kernel on dY with the flipped weights);
 //               bias + ReLU fused into the epilogue;
