@@ -1885,6 +1885,46 @@ __global__ void column_resistance(const float *open, const float *h3, int N, int
 	}
 }
 
+// The 16 input channels of pixel (yy, xx) of a sample, mv its mask value;
+// solid(y) reads the mask of the pixel's column at row y (to find the
+// vertical gap holding the pixel).
+template <typename Solid>
+__device__ __forceinline__ void input_pixel(float (&v)[16], uint8_t mv, const Solid &solid, int yy, int H, int64_t col,
+											float c1, float c2, float c4, const float *open, const float *h3,
+											const float *R, const float *PL) {
+#pragma unroll
+	for (int k = 0; k < 16; ++k) v[k] = 0.f;
+	v[0] = (float)mv;
+	v[1] = c1;
+	v[2] = c2;
+	v[3] = (float)yy / (float)(H - 1);
+	v[4] = c4;
+	if (!mv) {
+		const float hin = (float)(H > 2 ? H - 2 : H);
+		int lo = yy, hi = yy;
+		while (lo > 0 && !solid(lo - 1)) --lo;
+		while (hi + 1 < H && !solid(hi + 1)) ++hi;
+		const float h = (float)(hi - lo + 1);
+		const float sp = ((float)(yy - lo) + 0.5f) / h;
+		const float shape = 4.f * sp * (1.f - sp);
+		v[5] = open[col];
+		v[6] = R[col];
+		v[7] = h / hin;
+		v[8] = shape;
+		v[9] = 0.5f * fminf(hin * h * h / fmaxf(h3[col], 1.f) * shape, 8.f);
+		v[10] = PL[col];
+	}
+}
+
+__device__ __forceinline__ void store_input16(bf16 *o, const float (&v)[16]) {
+	__align__(16) __nv_bfloat162 q[8];
+#pragma unroll
+	for (int k = 0; k < 8; ++k) q[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
+	uint4 *d = reinterpret_cast<uint4 *>(o);
+	d[0] = *reinterpret_cast<const uint4 *>(&q[0]);
+	d[1] = *reinterpret_cast<const uint4 *>(&q[4]);
+}
+
 // One block per (sample, 32 columns): the block's mask columns are staged in
 // shared memory (H x 32 bytes), then thread (column c, row r) finds its
 // vertical gap's ends there and writes the pixel's 16 channels as two
@@ -1905,37 +1945,29 @@ __global__ void make_input(const uint8_t *mask, const float *umax, const float *
 	if (xx >= W) return;
 	const int64_t col = (int64_t)b * W + xx;
 	const float c1 = umax[b] / 0.08f, c2 = (tau[b] - 0.55f) / 0.45f, c4 = (float)xx / (float)(W - 1);
-	const float hin = (float)(H > 2 ? H - 2 : H);
+	const auto solid = [&](int y) { return mt[y * 32 + c] != 0; };
 	for (int yy = threadIdx.x >> 5; yy < H; yy += blockDim.x >> 5) {
-		const uint8_t mv = mt[yy * 32 + c];
 		float v[16];
-#pragma unroll
-		for (int k = 0; k < 16; ++k) v[k] = 0.f;
-		v[0] = (float)mv;
-		v[1] = c1;
-		v[2] = c2;
-		v[3] = (float)yy / (float)(H - 1);
-		v[4] = c4;
-		if (!mv) {
-			int lo = yy, hi = yy;
-			while (lo > 0 && !mt[(lo - 1) * 32 + c]) --lo;
-			while (hi + 1 < H && !mt[(hi + 1) * 32 + c]) ++hi;
-			const float h = (float)(hi - lo + 1);
-			const float sp = ((float)(yy - lo) + 0.5f) / h;
-			const float shape = 4.f * sp * (1.f - sp);
-			v[5] = open[col];
-			v[6] = R[col];
-			v[7] = h / hin;
-			v[8] = shape;
-			v[9] = 0.5f * fminf(hin * h * h / fmaxf(h3[col], 1.f) * shape, 8.f);
-			v[10] = PL[col];
-		}
-		__align__(16) __nv_bfloat162 q[8];
-#pragma unroll
-		for (int k = 0; k < 8; ++k) q[k] = __floats2bfloat162_rn(v[2 * k], v[2 * k + 1]);
-		uint4 *d = reinterpret_cast<uint4 *>(x + (((int64_t)b * H + yy) * W + xx) * 16);
-		d[0] = *reinterpret_cast<const uint4 *>(&q[0]);
-		d[1] = *reinterpret_cast<const uint4 *>(&q[4]);
+		input_pixel(v, mt[yy * 32 + c], solid, yy, H, col, c1, c2, c4, open, h3, R, PL);
+		store_input16(x + (((int64_t)b * H + yy) * W + xx) * 16, v);
+	}
+}
+
+// The same for grids too tall for the shared-memory tile: one thread per
+// pixel, the gap found in global memory.
+__global__ void make_input_tall(const uint8_t *mask, const float *umax, const float *tau, const float *open,
+								const float *h3, const float *R, const float *PL, bf16 *x, int N, int H, int W) {
+	const int64_t n = (int64_t)N * H * W;
+	for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+		const int b = (int)(p / ((int64_t)H * W));
+		const int r = (int)(p - (int64_t)b * H * W);
+		const int yy = r / W, xx = r - yy * W;
+		const uint8_t *m = mask + (int64_t)b * H * W;
+		const auto solid = [&](int y) { return m[(int64_t)y * W + xx] != 0; };
+		float v[16];
+		input_pixel(v, m[r], solid, yy, H, (int64_t)b * W + xx, umax[b] / 0.08f, (tau[b] - 0.55f) / 0.45f,
+					(float)xx / (float)(W - 1), open, h3, R, PL);
+		store_input16(x + p * 16, v);
 	}
 }
 
@@ -2038,6 +2070,21 @@ EncodeTiledFn encode_tiled() {
 
 uint32_t align1k(uint64_t v) { return (uint32_t)((v + 1023) / 1024 * 1024); }
 
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per kernel and
+// device: the attribute belongs to the device's context, so a flag per
+// process would leave a second device's launches without it.
+template <typename K>
+cudaError_t allow_dynamic_smem(K *kernel, int bytes) {
+	static bool done[64] = {};
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return e;
+	if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
+	e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
+	return e;
+}
+
 // Channel chunk and stage count of conv_halo: the largest chunk (64, 48, 32 or
 // 16 channels dividing Ci) whose stages (up to three, at least two when there
 // are two chunks or more) fit 110 KB (two CTAs per SM), else 200 KB; 0: none.
@@ -2135,11 +2182,7 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	while (a.tmem_cols < (uint32_t)(a.RT * a.CoT)) a.tmem_cols <<= 1;
 	a.err = U->d_err;
 	const size_t smem = (size_t)a.stages * a.stage_bytes + (size_t)a.stages * 16 + 16;
-	static bool attr_set = false;
-	if (!attr_set) {
-		KEL_CUDA(cudaFuncSetAttribute(conv_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
-		attr_set = true;
-	}
+	KEL_CUDA(allow_dynamic_smem(conv_halo, 210 * 1024));
 	conv_halo<<<(unsigned)((int64_t)n * (H / (a.RT * a.MR)) * tpr * (co / a.CoT)), 128, smem, U->stream>>>(tx, tw, a);
 	KEL_CUDA(cudaGetLastError());
 	*launched = 1;
@@ -2232,11 +2275,7 @@ int conv_rows_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	a.use_bias = bias;
 	a.err = U->d_err;
 	const size_t smem = (size_t)a.mbar_off + (2u * (size_t)a.NR + 3u + 16u) * 8u + 16u;
-	static bool attr_set = false;
-	if (!attr_set) {
-		KEL_CUDA(cudaFuncSetAttribute(conv_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024));
-		attr_set = true;
-	}
+	KEL_CUDA(allow_dynamic_smem(conv_rows, 210 * 1024));
 	conv_rows<<<(unsigned)((int64_t)n * (W / 128) * a.runs), 192, smem, U->stream>>>(tx, tw, a);
 	KEL_CUDA(cudaGetLastError());
 	*launched = 1;
@@ -2283,11 +2322,7 @@ int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
 		while (t.tmem_cols < (uint32_t)co) t.tmem_cols <<= 1;
 		t.err = U->d_err;
 		const size_t smem = (size_t)t.stages * ((size_t)co * 128 + (size_t)TC_M * 128) + (size_t)t.stages * 8 + 16;
-		static bool attr_set = false;
-		if (!attr_set) {
-			KEL_CUDA(cudaFuncSetAttribute(conv_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-			attr_set = true;
-		}
+		KEL_CUDA(allow_dynamic_smem(conv_tc, 200 * 1024));
 		conv_tc<<<(unsigned)((M + TC_M - 1) / TC_M), 128, smem, U->stream>>>(t);
 		KEL_CUDA(cudaGetLastError());
 		return KEL_OK;
@@ -2397,11 +2432,7 @@ int wgrad_halo_launch(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16
 	if (chunks < 1) chunks = 1;
 	a.per_chunk = (a.tiles + chunks - 1) / chunks;
 	chunks = (a.tiles + a.per_chunk - 1) / a.per_chunk;
-	static bool attr_set = false;
-	if (!attr_set) {
-		KEL_CUDA(cudaFuncSetAttribute(conv_wgrad_halo, cudaFuncAttributeMaxDynamicSharedMemorySize, 222 * 1024));
-		attr_set = true;
-	}
+	KEL_CUDA(allow_dynamic_smem(conv_wgrad_halo, 222 * 1024));
 	// one CTA per SM when its TMEM columns would not leave room for a second
 	const size_t smem_launch = per_sm == 1 && smem < 116u * 1024u ? 116u * 1024u : smem;
 	conv_wgrad_halo<<<(unsigned)(chunks * per_chunk_ctas), 128, smem_launch, U->stream>>>(tx, tdy, a);
@@ -2448,11 +2479,7 @@ int conv_grads_tc(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy
 	while (a.tmem_cols < (uint32_t)l.co) a.tmem_cols <<= 1;
 	a.err = U->d_err;
 	const size_t smem = (size_t)a.stages * ((size_t)l.co * 128 + (size_t)TC_M * 128) + (size_t)a.stages * 8 + 16;
-	static bool attr_set = false;
-	if (!attr_set) {
-		KEL_CUDA(cudaFuncSetAttribute(conv_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-		attr_set = true;
-	}
+	KEL_CUDA(allow_dynamic_smem(conv_wgrad_tc, 200 * 1024));
 	conv_wgrad_tc<<<dim3((unsigned)tiles, (unsigned)chunks), 128, smem, U->stream>>>(a);
 	const int64_t per = (int64_t)l.co * K;
 	launch_reduce_partials(U->partial, per, (int)chunks, U->g + l.woff, U->stream);
@@ -2721,9 +2748,12 @@ extern "C" int kel_unet_make_input(kel_unet *U, const uint8_t *d_mask, const flo
 	column_features<<<(n * W + 127) / 128, 128, 0, U->stream>>>(d_mask, n, H, W, U->col_open, U->col_h3);
 	column_resistance<<<n, 256, sizeof(float) * 4 * W, U->stream>>>(U->col_open, U->col_h3, n, W, U->col_res,
 																	 U->col_pl);
-	if ((size_t)H * 32 > 48 * 1024) return fail(KEL_ERR_UNSUPPORTED, "kel_unet_make_input: height above 1536");
-	make_input<<<n * ((W + 31) / 32), 256, (size_t)H * 32, U->stream>>>(d_mask, d_umax, d_tau, U->col_open, U->col_h3,
-																		  U->col_res, U->col_pl, U->input, n, H, W);
+	if ((size_t)H * 32 <= 48 * 1024)
+		make_input<<<n * ((W + 31) / 32), 256, (size_t)H * 32, U->stream>>>(d_mask, d_umax, d_tau, U->col_open, U->col_h3,
+																			  U->col_res, U->col_pl, U->input, n, H, W);
+	else
+		make_input_tall<<<grid_of((int64_t)n * H * W), 256, 0, U->stream>>>(d_mask, d_umax, d_tau, U->col_open, U->col_h3,
+																			 U->col_res, U->col_pl, U->input, n, H, W);
 	KEL_CUDA(cudaGetLastError());
 	return KEL_OK;
 }

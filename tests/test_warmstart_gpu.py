@@ -154,3 +154,22 @@ def test_network_input_planes_match_oracle():
     want_bf = torch.tensor(want, dtype=torch.float32).to(torch.bfloat16).float().numpy()
     g = got.float().cpu().numpy()
     assert np.max(np.abs(g - want_bf) / np.maximum(np.abs(want_bf), 1e-3)) <= 1e-2
+
+
+def test_network_input_planes_tall_grid_match_oracle():
+    """The same for a grid taller than the shared-memory column tile of
+    kel_unet_make_input (1,600 rows: the per-pixel form of the kernel)."""
+    from lbm_mirror_gb300 import UNet
+    from lbm_mirror_gb300 import warmstart as WS
+    chans = WS.fixed_size_channels(1, seed=62, nx=16, ny=1600)
+    mask, u_max, tau = WS.channel_inputs(chans)
+    net = UNet(height=1600, width=16, widths=(16, 16, 16, 16), max_batch=1, seed=1)
+    dm, du, dt = (torch.from_numpy(a).cuda() for a in (mask, u_max, tau))
+    torch.cuda.synchronize()
+    net.make_input(dm.data_ptr(), du.data_ptr(), dt.data_ptr(), 1)
+    got = torch.empty((1, 1600, 16, 16), dtype=torch.bfloat16, device="cuda")
+    net.get_input(got.data_ptr(), 1)
+    want = O.unet_input(mask, u_max.astype(np.float64), tau.astype(np.float64))
+    want_bf = torch.tensor(want, dtype=torch.float32).to(torch.bfloat16).float().numpy()
+    g = got.float().cpu().numpy()
+    assert np.max(np.abs(g - want_bf) / np.maximum(np.abs(want_bf), 1e-3)) <= 1e-2
