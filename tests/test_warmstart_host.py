@@ -1,6 +1,8 @@
 """Host side of the learned warm start: the FP64 reconstruction oracle's
-moments (no GPU) and the target normalisation."""
+moments (no GPU), the target normalisation, and the warm-start bench line's
+bookkeeping."""
 import numpy as np
+import pytest
 
 from lbm_mirror_gb300 import warmstart as WS
 from oracle import warmstart_oracle as O
@@ -115,3 +117,63 @@ def test_lubrication_input_splits_flux_as_gap_cubes():
     s1 = sum(4 * ((k + 0.5) / 3) * (1 - (k + 0.5) / 3) for k in range(3))
     s2 = sum(4 * ((k + 0.5) / 5) * (1 - (k + 0.5) / 5) for k in range(5))
     np.testing.assert_allclose(q1 / q2, (3 ** 2 * s1) / (5 ** 2 * s2), rtol=1e-12)
+
+
+def test_bench_warm_start_line_for_single_networks_and_ensembles(monkeypatch, capsys):
+    """bench.py's warm-start workload assembles its JSON line for one network
+    and for an ensemble (`--ensemble K`): the GPU steps (steady states,
+    training, the two runs, inference) replaced by fakes, the bookkeeping
+    around them run as is."""
+    import json
+    import types
+    torch = pytest.importorskip("torch")
+    import bench
+
+    class Net:
+        n_params = 1000
+
+        def params(self):
+            return np.zeros(3)
+
+    class Model:
+        def __init__(self):
+            self.net, self.history, self.rho_scale, self.rho_norm = Net(), [(0, 0.5), (1, 0.1)], 2.0, "lubrication"
+
+    class States:
+        steps = np.ones(4, np.int64)
+        seconds = 1.0
+        converged = np.ones(4, bool)
+        residual = np.zeros(4)
+
+    keys = ["warm_seconds", "plain_seconds", "speedup", "warm_steps_max", "warm_init_seconds", "plain_steps_mean",
+            "warm_steps_mean", "plain_steps_max", "plain_unconverged", "warm_unconverged", "final_u_rel_l2_mean",
+            "final_u_rel_l2_max", "prediction_u_rel_l2_mean", "prediction_u_rel_l2_max",
+            "prediction_drho_rel_l2_mean", "nonfinite_channels", "warm_fallbacks_to_rest", "steady_init_steps_mean",
+            "rho_one_steps_mean", "no_neq_steps_mean", "exact_u_net_rho_steps_mean", "net_u_exact_rho_steps_mean"]
+    monkeypatch.setattr(WS, "fixed_size_channels", lambda n, seed, nx, ny: list(range(n)))
+    monkeypatch.setattr(WS, "solve", lambda *a, **k: States())
+    monkeypatch.setattr(WS, "steady_subset", lambda s: s)
+    monkeypatch.setattr(WS, "train", lambda s, **k: Model())
+    monkeypatch.setattr(WS, "evaluate", lambda *a, **k: {key: 1.0 for key in keys})
+    monkeypatch.setattr(WS, "channel_inputs", lambda ch: (np.zeros(2), np.zeros(2), np.zeros(2)))
+    monkeypatch.setattr(WS, "predict", lambda *a, **k: None)
+    monkeypatch.setattr(torch.cuda, "synchronize", lambda *a, **k: None)
+    monkeypatch.setattr(torch.Tensor, "cuda", lambda self, *a, **k: self)
+
+    def ensemble(s, seeds, **k):
+        e = WS.WarmStartEnsemble.__new__(WS.WarmStartEnsemble)
+        e.members = [Model() for _ in seeds]
+        e.rho_norm, e.rho_scale = "lubrication", 2.0
+        return e
+
+    monkeypatch.setattr(WS, "train_ensemble", ensemble)
+    for k in (1, 3):
+        args = types.SimpleNamespace(workload="d2q9_warm_start_256x64", train=64, test=8, tol=1e-6, max_steps=10,
+                                     epochs=1, rho_rms=0.25, residual=False, weight_by_steps=False,
+                                     rho_norm="lubrication", rho_residual=False, flip=True, ensemble=k, save_dir="")
+        bench.run_warm_start(args, 0, 1)
+        line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+        assert line["config"]["ensemble"] == k
+        assert line["config"]["params"] == 1000 * k
+        assert line["training"]["adam_steps"] == 1 * (64 // 32) * k
+        assert line["training"]["loss_last"] == 0.1
