@@ -2072,15 +2072,16 @@ uint32_t align1k(uint64_t v) { return (uint32_t)((v + 1023) / 1024 * 1024); }
 
 // cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per kernel and
 // device: the attribute belongs to the device's context, so a flag per
-// process would leave a second device's launches without it.
-template <typename K>
-cudaError_t allow_dynamic_smem(K *kernel, int bytes) {
+// process would leave a second device's launches without it.  One
+// instantiation (and flag array) per kernel.
+template <auto Kernel>
+cudaError_t allow_dynamic_smem(int bytes) {
 	static bool done[64] = {};
 	int dev = 0;
 	cudaError_t e = cudaGetDevice(&dev);
 	if (e != cudaSuccess) return e;
 	if (dev >= 0 && dev < 64 && done[dev]) return cudaSuccess;
-	e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+	e = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 	if (e == cudaSuccess && dev >= 0 && dev < 64) done[dev] = true;
 	return e;
 }
@@ -2182,7 +2183,7 @@ int conv_halo_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	while (a.tmem_cols < (uint32_t)(a.RT * a.CoT)) a.tmem_cols <<= 1;
 	a.err = U->d_err;
 	const size_t smem = (size_t)a.stages * a.stage_bytes + (size_t)a.stages * 16 + 16;
-	KEL_CUDA(allow_dynamic_smem(conv_halo, 210 * 1024));
+	KEL_CUDA(allow_dynamic_smem<conv_halo>(210 * 1024));
 	conv_halo<<<(unsigned)((int64_t)n * (H / (a.RT * a.MR)) * tpr * (co / a.CoT)), 128, smem, U->stream>>>(tx, tw, a);
 	KEL_CUDA(cudaGetLastError());
 	*launched = 1;
@@ -2275,7 +2276,7 @@ int conv_rows_launch(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, 
 	a.use_bias = bias;
 	a.err = U->d_err;
 	const size_t smem = (size_t)a.mbar_off + (2u * (size_t)a.NR + 3u + 16u) * 8u + 16u;
-	KEL_CUDA(allow_dynamic_smem(conv_rows, 210 * 1024));
+	KEL_CUDA(allow_dynamic_smem<conv_rows>(210 * 1024));
 	conv_rows<<<(unsigned)((int64_t)n * (W / 128) * a.runs), 192, smem, U->stream>>>(tx, tw, a);
 	KEL_CUDA(cudaGetLastError());
 	*launched = 1;
@@ -2322,7 +2323,7 @@ int conv_fwd(kel_unet *U, const bf16 *x, const bf16 *w, const float *b, bf16 *y,
 		while (t.tmem_cols < (uint32_t)co) t.tmem_cols <<= 1;
 		t.err = U->d_err;
 		const size_t smem = (size_t)t.stages * ((size_t)co * 128 + (size_t)TC_M * 128) + (size_t)t.stages * 8 + 16;
-		KEL_CUDA(allow_dynamic_smem(conv_tc, 200 * 1024));
+		KEL_CUDA(allow_dynamic_smem<conv_tc>(200 * 1024));
 		conv_tc<<<(unsigned)((M + TC_M - 1) / TC_M), 128, smem, U->stream>>>(t);
 		KEL_CUDA(cudaGetLastError());
 		return KEL_OK;
@@ -2432,7 +2433,7 @@ int wgrad_halo_launch(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16
 	if (chunks < 1) chunks = 1;
 	a.per_chunk = (a.tiles + chunks - 1) / chunks;
 	chunks = (a.tiles + a.per_chunk - 1) / a.per_chunk;
-	KEL_CUDA(allow_dynamic_smem(conv_wgrad_halo, 222 * 1024));
+	KEL_CUDA(allow_dynamic_smem<conv_wgrad_halo>(222 * 1024));
 	// one CTA per SM when its TMEM columns would not leave room for a second
 	const size_t smem_launch = per_sm == 1 && smem < 116u * 1024u ? 116u * 1024u : smem;
 	conv_wgrad_halo<<<(unsigned)(chunks * per_chunk_ctas), 128, smem_launch, U->stream>>>(tx, tdy, a);
@@ -2479,7 +2480,7 @@ int conv_grads_tc(kel_unet *U, const UnetLayer &l, const bf16 *x, const bf16 *dy
 	while (a.tmem_cols < (uint32_t)l.co) a.tmem_cols <<= 1;
 	a.err = U->d_err;
 	const size_t smem = (size_t)a.stages * ((size_t)l.co * 128 + (size_t)TC_M * 128) + (size_t)a.stages * 8 + 16;
-	KEL_CUDA(allow_dynamic_smem(conv_wgrad_tc, 200 * 1024));
+	KEL_CUDA(allow_dynamic_smem<conv_wgrad_tc>(200 * 1024));
 	conv_wgrad_tc<<<dim3((unsigned)tiles, (unsigned)chunks), 128, smem, U->stream>>>(a);
 	const int64_t per = (int64_t)l.co * K;
 	launch_reduce_partials(U->partial, per, (int)chunks, U->g + l.woff, U->stream);
